@@ -1,0 +1,854 @@
+// api.cu -- the C ABI of libbeastgpu (include/beastgpu.h): handles, uploads, the chunked
+// assembly driver, dense solves, GMRES and the one-call solve job.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <complex>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "internal.h"
+
+int beast_fail(beast_ctx* ctx, int code, const std::string& msg) {
+  if (ctx) ctx->err = msg;
+  return code;
+}
+
+#define ARG_CHECK(ctx, cond, msg) \
+  do {                            \
+    if (!(cond)) return beast_fail((ctx), BEAST_ERR_ARG, (msg)); \
+  } while (0)
+
+namespace {
+
+// device workspace: grows on demand, kept by the context
+int ws_reserve(beast_ctx* ctx, size_t bytes) {
+  if (bytes <= ctx->ws_size) return BEAST_OK;
+  if (ctx->ws) {
+    cudaStreamSynchronize(ctx->stream);
+    cudaFree(ctx->ws);
+    ctx->ws = nullptr;
+    ctx->ws_size = 0;
+  }
+  cudaError_t e = cudaMalloc(&ctx->ws, bytes);
+  if (e != cudaSuccess) {
+    ctx->ws = nullptr;
+    return beast_fail(ctx, BEAST_ERR_OOM, "workspace allocation of " + std::to_string(bytes) +
+                                              " bytes failed: " + cudaGetErrorString(e));
+  }
+  ctx->ws_size = bytes;
+  return BEAST_OK;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+OpParams to_params(const beast_op_desc* op) {
+  OpParams p;
+  p.kind = op->kind;
+  p.gr = op->gamma_re;
+  p.gi = op->gamma_im;
+  p.ar = op->alpha_re;
+  p.ai = op->alpha_im;
+  p.br = op->beta_re;
+  p.bi = op->beta_im;
+  return p;
+}
+
+int set_device(beast_ctx* ctx) {
+  BEAST_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  return BEAST_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* beast_version(void) { return "beastgpu 0.1 (sm_103a)"; }
+
+int beast_ctx_create(int device, beast_ctx** out) {
+  if (!out) return BEAST_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BEAST_ERR_CUDA;
+  if (device < 0 || device >= ndev) return BEAST_ERR_ARG;
+  beast_ctx* c = new beast_ctx();
+  c->device = device;
+  if (cudaSetDevice(device) != cudaSuccess) {
+    delete c;
+    return BEAST_ERR_CUDA;
+  }
+  cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return BEAST_ERR_CUDA;
+  }
+  c->own_stream = true;
+  size_t fr = 0, tot = 0;
+  cudaMemGetInfo(&fr, &tot);
+  c->ws_limit = fr / 4;
+  if (cudaMalloc(&c->d_flag, 64) != cudaSuccess) {
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return BEAST_ERR_OOM;
+  }
+  *out = c;
+  return BEAST_OK;
+}
+
+int beast_ctx_destroy(beast_ctx* ctx) {
+  if (!ctx) return BEAST_OK;
+  cudaSetDevice(ctx->device);
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->ws) cudaFree(ctx->ws);
+  if (ctx->d_flag) cudaFree(ctx->d_flag);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return BEAST_OK;
+}
+
+int beast_last_error(beast_ctx* ctx, char* buf, size_t len) {
+  if (!buf || len == 0) return BEAST_ERR_ARG;
+  const char* m = ctx ? ctx->err.c_str() : "no context";
+  snprintf(buf, len, "%s", m);
+  return BEAST_OK;
+}
+
+int beast_ctx_set_stream(beast_ctx* ctx, void* stream) {
+  ARG_CHECK(ctx, ctx, "null context");
+  if (!stream) return BEAST_OK;
+  cudaStreamSynchronize(ctx->stream);
+  if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  ctx->stream = (cudaStream_t)stream;
+  ctx->own_stream = false;
+  return BEAST_OK;
+}
+
+int beast_ctx_set_workspace_limit(beast_ctx* ctx, size_t bytes) {
+  ARG_CHECK(ctx, ctx && bytes >= (1u << 20), "workspace limit below 1 MiB");
+  ctx->ws_limit = bytes;
+  return BEAST_OK;
+}
+
+int beast_ctx_synchronize(beast_ctx* ctx) {
+  ARG_CHECK(ctx, ctx, "null context");
+  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return BEAST_OK;
+}
+
+int beast_mesh_upload(beast_ctx* ctx, const double* verts, int64_t nv, const int32_t* cells,
+                      int64_t nc, int index_base, beast_mesh** out) {
+  ARG_CHECK(ctx, ctx && out && verts && cells && nv > 0 && nc > 0, "invalid mesh arguments");
+  ARG_CHECK(ctx, index_base == 0 || index_base == 1, "index_base must be 0 or 1");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  std::vector<int> c(3 * nc);
+  for (int64_t i = 0; i < 3 * nc; ++i) {
+    int v = cells[i] - index_base;
+    ARG_CHECK(ctx, v >= 0 && v < nv, "cell vertex index out of range");
+    c[i] = v;
+  }
+  beast_mesh* m = new beast_mesh();
+  m->ctx = ctx;
+  m->nv = nv;
+  m->nc = nc;
+  cudaError_t e = cudaMalloc(&m->verts, sizeof(double) * 3 * nv);
+  if (e == cudaSuccess) e = cudaMalloc(&m->cells, sizeof(int) * 3 * nc);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->verts, verts, sizeof(double) * 3 * nv, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(m->cells, c.data(), sizeof(int) * 3 * nc, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    cudaFree(m->verts);
+    cudaFree(m->cells);
+    delete m;
+    return beast_fail(ctx, BEAST_ERR_CUDA, std::string("mesh upload: ") + cudaGetErrorString(e));
+  }
+  *out = m;
+  return BEAST_OK;
+}
+
+int beast_mesh_free(beast_mesh* m) {
+  if (!m) return BEAST_OK;
+  cudaSetDevice(m->ctx->device);
+  cudaStreamSynchronize(m->ctx->stream);
+  cudaFree(m->verts);
+  cudaFree(m->cells);
+  delete m;
+  return BEAST_OK;
+}
+
+int beast_space_upload(beast_ctx* ctx, const beast_mesh* mesh, int kind, int64_t ncells,
+                       const int64_t* cells, int maxfn, int nshapes, const int64_t* ad_dof,
+                       const double* ad_coeff, int64_t nfuncs, int index_base, beast_space** out) {
+  ARG_CHECK(ctx, ctx && mesh && out && cells && ad_dof && ad_coeff, "null argument");
+  ARG_CHECK(ctx, kind == BEAST_P0 || kind == BEAST_P1 || kind == BEAST_RT, "unknown space kind");
+  ARG_CHECK(ctx, nshapes == (kind == BEAST_P0 ? 1 : 3), "nshapes does not match the space kind");
+  ARG_CHECK(ctx, ncells > 0 && maxfn >= 1 && nfuncs > 0 && nfuncs < (1LL << 31), "invalid sizes");
+  ARG_CHECK(ctx, index_base == 0 || index_base == 1, "index_base must be 0 or 1");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  beast_space* s = new beast_space();
+  s->ctx = ctx;
+  s->mesh = mesh;
+  s->kind = kind;
+  s->nshapes = nshapes;
+  s->maxfn = maxfn;
+  s->ncells = ncells;
+  s->nfuncs = nfuncs;
+  std::vector<int> hc(ncells), c2a(mesh->nc, -1);
+  for (int64_t c = 0; c < ncells; ++c) {
+    int64_t mc = cells[c] - index_base;
+    if (mc < 0 || mc >= mesh->nc) {
+      delete s;
+      return beast_fail(ctx, BEAST_ERR_ARG, "active cell index out of range");
+    }
+    hc[c] = (int)mc;
+    c2a[mc] = (int)c;
+  }
+  const int64_t nad = ncells * nshapes * maxfn;
+  s->h_ad_dof.resize(nad);
+  s->h_ad_coeff.assign(ad_coeff, ad_coeff + nad);
+  std::vector<int64_t> cnt(nfuncs + 1, 0);
+  for (int64_t i = 0; i < nad; ++i) {
+    int64_t d = ad_dof[i] - index_base;
+    if (ad_dof[i] < index_base) d = -1;
+    if (d >= nfuncs) {
+      delete s;
+      return beast_fail(ctx, BEAST_ERR_ARG, "assembly data dof index out of range");
+    }
+    s->h_ad_dof[i] = (int)d;
+    if (d >= 0) cnt[d + 1]++;
+  }
+  for (int64_t f = 0; f < nfuncs; ++f) cnt[f + 1] += cnt[f];
+  s->h_fn_ptr = cnt;
+  s->h_fn_cell.resize(cnt[nfuncs]);
+  s->h_fn_shape.resize(cnt[nfuncs]);
+  s->h_fn_coeff.resize(cnt[nfuncs]);
+  std::vector<int64_t> fill(cnt.begin(), cnt.end() - 1);
+  for (int64_t c = 0; c < ncells; ++c)
+    for (int r = 0; r < nshapes; ++r)
+      for (int k = 0; k < maxfn; ++k) {
+        int64_t i = (c * nshapes + r) * maxfn + k;
+        int d = s->h_ad_dof[i];
+        if (d < 0) continue;
+        int64_t o = fill[d]++;
+        s->h_fn_cell[o] = (int)c;
+        s->h_fn_shape[o] = r;
+        s->h_fn_coeff[o] = s->h_ad_coeff[i];
+      }
+  cudaStream_t st = ctx->stream;
+  cudaError_t e = cudaSuccess;
+  auto up = [&](void** dst, const void* src, size_t bytes) {
+    if (e != cudaSuccess) return;
+    e = cudaMalloc(dst, std::max<size_t>(bytes, 16));
+    if (e == cudaSuccess && bytes) e = cudaMemcpyAsync(*dst, src, bytes, cudaMemcpyHostToDevice, st);
+  };
+  up((void**)&s->cells, hc.data(), sizeof(int) * ncells);
+  up((void**)&s->cell2act, c2a.data(), sizeof(int) * mesh->nc);
+  up((void**)&s->ad_dof, s->h_ad_dof.data(), sizeof(int) * nad);
+  up((void**)&s->ad_coeff, s->h_ad_coeff.data(), sizeof(double) * nad);
+  up((void**)&s->fn_ptr, s->h_fn_ptr.data(), sizeof(int64_t) * (nfuncs + 1));
+  up((void**)&s->fn_cell, s->h_fn_cell.data(), sizeof(int) * s->h_fn_cell.size());
+  up((void**)&s->fn_shape, s->h_fn_shape.data(), sizeof(int) * s->h_fn_shape.size());
+  up((void**)&s->fn_coeff, s->h_fn_coeff.data(), sizeof(double) * s->h_fn_coeff.size());
+  if (e == cudaSuccess) e = cudaMalloc(&s->geo, sizeof(double) * GEO_STRIDE * ncells);
+  if (e == cudaSuccess) e = cudaMalloc(&s->geof, sizeof(float) * 4 * ncells);
+  if (e == cudaSuccess) e = launch_geometry(s, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    beast_space_free(s);
+    return beast_fail(ctx, BEAST_ERR_CUDA, std::string("space upload: ") + cudaGetErrorString(e));
+  }
+  *out = s;
+  return BEAST_OK;
+}
+
+int beast_space_free(beast_space* s) {
+  if (!s) return BEAST_OK;
+  cudaSetDevice(s->ctx->device);
+  cudaStreamSynchronize(s->ctx->stream);
+  void* ptrs[] = {s->cells, s->cell2act, s->ad_dof, s->ad_coeff, s->geo, s->geof,
+                  s->fn_ptr, s->fn_cell, s->fn_shape, s->fn_coeff};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete s;
+  return BEAST_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// assembly driver
+// ---------------------------------------------------------------------------------------
+static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs,
+                           const beast_space* ts, const beast_space* bs, int precision, void* Z,
+                           int64_t ldz, int z_c64, int64_t row_off, int64_t col_off, double cr,
+                           double ci, int accumulate) {
+  cudaStream_t st = ctx->stream;
+  const int nst = ts->kind == BEAST_P0 ? 1 : 3, nsb = bs->kind == BEAST_P0 ? 1 : 3;
+  const int64_t ldc = (int64_t)nst * ts->ncells;
+  const int zc64 = precision == BEAST_MIXED ? 1 : 0;
+  const size_t elem = zc64 ? 8 : 16;
+  // rules
+  TriRuleDev ro, ri, ron, rin;
+  ARG_CHECK(ctx, make_trirule(qs->outer_far, &ro) && make_trirule(qs->inner_far, &ri),
+            "far rule degree not available (1..10)");
+  bool has_near = qs->kind == BEAST_QS_WILTON_SAUTER || qs->kind == BEAST_QS_SAUTER;
+  if (qs->kind == BEAST_QS_WILTON_SAUTER) {
+    ARG_CHECK(ctx, make_trirule(qs->outer_near, &ron) && make_trirule(qs->inner_near, &rin),
+              "near rule degree not available (1..10)");
+  } else {
+    ron = ro;
+    rin = ri;
+  }
+  if (has_near)
+    ARG_CHECK(ctx, qs->ss_face >= 1 && qs->ss_face <= 20 && qs->ss_edge >= 1 && qs->ss_edge <= 20 &&
+                       qs->ss_vert >= 1 && qs->ss_vert <= 20,
+              "Sauter-Schwab orders must be in 1..20");
+  // chunking over trial dofs: cells needed per chunk fit the workspace
+  const int64_t near_cap = std::max<int64_t>(1 << 16, 48 * ts->ncells);
+  size_t fixed = align256(near_cap * sizeof(NearPair)) + align256(sizeof(int) * bs->ncells) * 2 + 4096;
+  size_t budget = ctx->ws_limit > fixed ? ctx->ws_limit - fixed : 0;
+  int64_t max_cells = (int64_t)(budget / ((size_t)ldc * nsb * elem));
+  ARG_CHECK(ctx, max_cells >= 4, "workspace limit too small for one trial chunk");
+  max_cells = std::min<int64_t>(max_cells, bs->ncells);
+  std::vector<int> qlocal_h(bs->ncells, -1), qcells_h;
+  qcells_h.reserve(max_cells);
+  struct Chunk {
+    int64_t n0, n1;
+    std::vector<int> cells;
+  };
+  std::vector<Chunk> chunks;
+  {
+    int64_t n0 = 0;
+    std::vector<int> cur;
+    std::vector<char> in(bs->ncells, 0);
+    for (int64_t n = 0; n < bs->nfuncs; ++n) {
+      int add = 0;
+      for (int64_t f = bs->h_fn_ptr[n]; f < bs->h_fn_ptr[n + 1]; ++f) add += !in[bs->h_fn_cell[f]];
+      if ((int64_t)cur.size() + add > max_cells && n > n0) {
+        chunks.push_back({n0, n, cur});
+        for (int c : cur) in[c] = 0;
+        cur.clear();
+        n0 = n;
+      }
+      for (int64_t f = bs->h_fn_ptr[n]; f < bs->h_fn_ptr[n + 1]; ++f) {
+        int c = bs->h_fn_cell[f];
+        if (!in[c]) {
+          in[c] = 1;
+          cur.push_back(c);
+        }
+      }
+    }
+    chunks.push_back({n0, bs->nfuncs, cur});
+  }
+  int64_t maxq = 1;
+  for (auto& c : chunks) maxq = std::max<int64_t>(maxq, (int64_t)c.cells.size());
+  size_t zbytes = align256((size_t)ldc * nsb * maxq * elem);
+  size_t need = zbytes + align256(near_cap * sizeof(NearPair)) + align256(sizeof(int) * maxq) +
+                align256(sizeof(int) * bs->ncells) + 256;
+  int rc = ws_reserve(ctx, need);
+  if (rc) return rc;
+  char* w = (char*)ctx->ws;
+  void* zcell = w;
+  NearPair* nearl = (NearPair*)(w + zbytes);
+  int* qcells_d = (int*)((char*)nearl + align256(near_cap * sizeof(NearPair)));
+  int* qlocal_d = (int*)((char*)qcells_d + align256(sizeof(int) * maxq));
+  int* counter = (int*)((char*)qlocal_d + align256(sizeof(int) * bs->ncells));
+  BEAST_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_flag, 0, 64, st));
+  std::vector<int> ql(bs->ncells, -1);
+  for (auto& ch : chunks) {
+    for (size_t i = 0; i < ch.cells.size(); ++i) ql[ch.cells[i]] = (int)i;
+    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(qcells_d, ch.cells.data(), sizeof(int) * ch.cells.size(), cudaMemcpyHostToDevice, st));
+    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(qlocal_d, ql.data(), sizeof(int) * bs->ncells, cudaMemcpyHostToDevice, st));
+    BEAST_CUDA_TRY(ctx, cudaMemsetAsync(counter, 0, sizeof(int), st));
+    AsmArgs a;
+    a.op = to_params(op);
+    a.qs = *qs;
+    a.ts = ts;
+    a.bs = bs;
+    a.precision = precision;
+    a.qcells = qcells_d;
+    a.nq = (int)ch.cells.size();
+    a.zcell = zcell;
+    a.zcell_c64 = zc64;
+    a.ldc = ldc;
+    a.near = nearl;
+    a.near_cap = (int)near_cap;
+    a.near_count = counter;
+    a.flag = ctx->d_flag;
+    cudaError_t e = launch_far(a, ro, ri, st);
+    if (e == cudaErrorInvalidValue)
+      return beast_fail(ctx, BEAST_ERR_UNSUPPORTED, "operator / space combination not supported");
+    BEAST_CUDA_TRY(ctx, e);
+    int nnear = 0;
+    if (has_near) {
+      BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(&nnear, counter, sizeof(int), cudaMemcpyDeviceToHost, st));
+      BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+      if (nnear > near_cap) return beast_fail(ctx, BEAST_ERR_ARG, "near-pair list overflow");
+      BEAST_CUDA_TRY(ctx, launch_near(a, nnear, ron, rin, st));
+    }
+    GatherArgs g;
+    g.ts = ts;
+    g.bs = bs;
+    g.zcell = zcell;
+    g.zcell_c64 = zc64;
+    g.ldc = ldc;
+    g.qlocal = qlocal_d;
+    g.n0 = ch.n0;
+    g.n1 = ch.n1;
+    g.Z = Z;
+    g.ldz = ldz;
+    g.z_c64 = z_c64;
+    g.row_off = row_off;
+    g.col_off = col_off;
+    g.cr = cr;
+    g.ci = ci;
+    g.accumulate = accumulate;
+    BEAST_CUDA_TRY(ctx, launch_gather(g, st));
+    for (int c : ch.cells) ql[c] = -1;
+  }
+  int flag = 0;
+  BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  if (flag & 1) return beast_fail(ctx, BEAST_ERR_ARG, "near-pair list overflow");
+  if (flag & 2)
+    return beast_fail(ctx, BEAST_ERR_UNSUPPORTED,
+                      "singularity extraction not available for this operator/space pairing");
+  return BEAST_OK;
+}
+
+int beast_assemble(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs,
+                   const beast_space* ts, const beast_space* bs, int precision, void* Z,
+                   int64_t ldz, int z_dtype, int z_loc, int64_t row_off, int64_t col_off,
+                   double cr, double ci, int accumulate) {
+  ARG_CHECK(ctx, ctx && op && qs && ts && bs && Z, "null argument");
+  ARG_CHECK(ctx, ts->mesh == bs->mesh, "test and trial spaces must share the mesh");
+  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED, "unknown precision");
+  ARG_CHECK(ctx, z_dtype == BEAST_C128 || z_dtype == BEAST_C64, "unknown matrix dtype");
+  ARG_CHECK(ctx, row_off >= 0 && col_off >= 0 && ldz >= row_off + ts->nfuncs, "bad Z addressing");
+  ARG_CHECK(ctx, op->kind >= BEAST_MW_SL && op->kind <= BEAST_HH_DLT, "unknown operator kind");
+  ARG_CHECK(ctx, qs->kind >= 1 && qs->kind <= 3, "unknown quadrature strategy");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  const int zc = z_dtype == BEAST_C64;
+  if (z_loc == BEAST_DEVICE)
+    return assemble_device(ctx, op, qs, ts, bs, precision, Z, ldz, zc, row_off, col_off, cr, ci,
+                           accumulate);
+  // host Z: assemble the addressed block on the device and copy it out
+  const size_t elem = zc ? 8 : 16;
+  void* dz = nullptr;
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&dz, (size_t)ts->nfuncs * bs->nfuncs * elem, ctx->stream));
+  char* hz = (char*)Z + (row_off + col_off * ldz) * elem;
+  if (accumulate)
+    BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(dz, ts->nfuncs * elem, hz, ldz * elem, ts->nfuncs * elem,
+                                          bs->nfuncs, cudaMemcpyHostToDevice, ctx->stream));
+  int rc = assemble_device(ctx, op, qs, ts, bs, precision, dz, ts->nfuncs, zc, 0, 0, cr, ci, accumulate);
+  if (rc == BEAST_OK) {
+    cudaError_t e = cudaMemcpy2DAsync(hz, ldz * elem, dz, ts->nfuncs * elem, ts->nfuncs * elem,
+                                      bs->nfuncs, cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) rc = beast_fail(ctx, BEAST_ERR_CUDA, cudaGetErrorString(e));
+  }
+  cudaFreeAsync(dz, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  return rc;
+}
+
+int beast_assemble_local(beast_ctx* ctx, int which, const beast_space* ts, const beast_space* bs,
+                         int degree, void* Z, int64_t ldz, int z_dtype, int z_loc, int64_t row_off,
+                         int64_t col_off, double cr, double ci) {
+  ARG_CHECK(ctx, ctx && ts && bs && Z, "null argument");
+  ARG_CHECK(ctx, which == 0 || which == 1, "which must be 0 (Identity) or 1 (NCross)");
+  ARG_CHECK(ctx, ts->kind == BEAST_RT && bs->kind == BEAST_RT, "local operators: RT x RT only");
+  ARG_CHECK(ctx, ts->mesh == bs->mesh, "test and trial spaces must share the mesh");
+  TriRuleDev r;
+  ARG_CHECK(ctx, make_trirule(degree, &r), "rule degree not available (1..10)");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  const int zc = z_dtype == BEAST_C64;
+  const size_t elem = zc ? 8 : 16;
+  if (z_loc == BEAST_DEVICE) {
+    BEAST_CUDA_TRY(ctx, launch_local_impl(which, ts, bs, bs->cell2act, r, Z, ldz, zc, row_off, col_off,
+                                          cr, ci, ctx->stream));
+    BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+    return BEAST_OK;
+  }
+  void* dz = nullptr;
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&dz, (size_t)ts->nfuncs * bs->nfuncs * elem, ctx->stream));
+  char* hz = (char*)Z + (row_off + col_off * ldz) * elem;
+  BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(dz, ts->nfuncs * elem, hz, ldz * elem, ts->nfuncs * elem,
+                                        bs->nfuncs, cudaMemcpyHostToDevice, ctx->stream));
+  BEAST_CUDA_TRY(ctx, launch_local_impl(which, ts, bs, bs->cell2act, r, dz, ts->nfuncs, zc, 0, 0, cr,
+                                        ci, ctx->stream));
+  BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(hz, ldz * elem, dz, ts->nfuncs * elem, ts->nfuncs * elem,
+                                        bs->nfuncs, cudaMemcpyDeviceToHost, ctx->stream));
+  BEAST_CUDA_TRY(ctx, cudaFreeAsync(dz, ctx->stream));
+  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return BEAST_OK;
+}
+
+int beast_rhs_planewave(beast_ctx* ctx, int kind, const beast_space* ts, const double* dir,
+                        const double* pol, double gr, double gi, double ar, double ai, int degree,
+                        double* b, int b_loc) {
+  ARG_CHECK(ctx, ctx && ts && dir && b, "null argument");
+  ARG_CHECK(ctx, kind >= 0 && kind <= 2, "unknown excitation kind");
+  ARG_CHECK(ctx, (kind == BEAST_EXC_HH_DIRICHLET) == (ts->kind != BEAST_RT),
+            "excitation kind does not match the test space");
+  TriRuleDev r;
+  ARG_CHECK(ctx, make_trirule(degree, &r), "rule degree not available (1..10)");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  double p3[3] = {0, 0, 0};
+  if (pol) memcpy(p3, pol, sizeof(p3));
+  double* db = b;
+  if (b_loc != BEAST_DEVICE) BEAST_CUDA_TRY(ctx, cudaMallocAsync(&db, ts->nfuncs * 16, ctx->stream));
+  BEAST_CUDA_TRY(ctx, launch_rhs(kind, ts, dir, p3, gr, gi, ar, ai, r, db, ctx->stream));
+  if (b_loc != BEAST_DEVICE) {
+    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(b, db, ts->nfuncs * 16, cudaMemcpyDeviceToHost, ctx->stream));
+    BEAST_CUDA_TRY(ctx, cudaFreeAsync(db, ctx->stream));
+  }
+  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return BEAST_OK;
+}
+
+int beast_farfield(beast_ctx* ctx, const beast_space* s, const double* u, const double* pts,
+                   int64_t npts, double gr, double gi, int degree, double* ff, int loc) {
+  ARG_CHECK(ctx, ctx && s && u && pts && ff && npts >= 0, "null argument");
+  ARG_CHECK(ctx, s->kind == BEAST_RT, "far field: RT space only");
+  TriRuleDev r;
+  ARG_CHECK(ctx, make_trirule(degree, &r), "rule degree not available (1..10)");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  cudaStream_t st = ctx->stream;
+  const double *du = u, *dp = pts;
+  double* dff = ff;
+  void *t1 = nullptr, *t2 = nullptr, *t3 = nullptr;
+  if (loc != BEAST_DEVICE) {
+    BEAST_CUDA_TRY(ctx, cudaMallocAsync(&t1, s->nfuncs * 16, st));
+    BEAST_CUDA_TRY(ctx, cudaMallocAsync(&t2, npts * 24 + 8, st));
+    BEAST_CUDA_TRY(ctx, cudaMallocAsync(&t3, npts * 48 + 8, st));
+    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(t1, u, s->nfuncs * 16, cudaMemcpyHostToDevice, st));
+    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(t2, pts, npts * 24, cudaMemcpyHostToDevice, st));
+    du = (double*)t1;
+    dp = (double*)t2;
+    dff = (double*)t3;
+  }
+  BEAST_CUDA_TRY(ctx, launch_farfield(s, du, dp, npts, gr, gi, r, dff, st));
+  if (loc != BEAST_DEVICE) {
+    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(ff, dff, npts * 48, cudaMemcpyDeviceToHost, st));
+    cudaFreeAsync(t1, st);
+    cudaFreeAsync(t2, st);
+    cudaFreeAsync(t3, st);
+  }
+  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  return BEAST_OK;
+}
+
+// ---------------------------------------------------------------------------------------
+// dense solve
+// ---------------------------------------------------------------------------------------
+int beast_lu_factor(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, beast_lu** out) {
+  ARG_CHECK(ctx, ctx && A && out && n > 0 && lda >= n, "invalid LU arguments");
+  ARG_CHECK(ctx, dtype == BEAST_C128 || dtype == BEAST_C64, "unknown dtype");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  beast_lu* lu = new beast_lu();
+  lu->ctx = ctx;
+  lu->n = n;
+  lu->lda = lda;
+  lu->dtype = dtype;
+  lu->A = A;
+  cudaError_t e = cudaMalloc(&lu->ipiv, sizeof(int) * 2 * n);
+  if (e != cudaSuccess) {
+    delete lu;
+    return beast_fail(ctx, BEAST_ERR_OOM, "pivot allocation failed");
+  }
+  int rc = lu_factor_dev(ctx, n, A, lda, dtype, lu->ipiv, &lu->info);
+  if (rc) {
+    beast_lu_free(lu);
+    return rc;
+  }
+  *out = lu;
+  if (lu->info > 0)
+    return beast_fail(ctx, BEAST_ERR_SINGULAR, "exactly singular pivot in column " + std::to_string(lu->info));
+  return BEAST_OK;
+}
+
+int beast_lu_solve(beast_ctx* ctx, const beast_lu* lu, int64_t nrhs, void* B, int64_t ldb) {
+  ARG_CHECK(ctx, ctx && lu && B && nrhs >= 0 && ldb >= lu->n, "invalid solve arguments");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  int rc = lu_solve_dev(ctx, lu->n, lu->A, lu->lda, lu->dtype, lu->ipiv, B, ldb, nrhs);
+  if (rc) return rc;
+  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  return BEAST_OK;
+}
+
+int beast_lu_free(beast_lu* lu) {
+  if (!lu) return BEAST_OK;
+  cudaSetDevice(lu->ctx->device);
+  cudaStreamSynchronize(lu->ctx->stream);
+  if (lu->ipiv) cudaFree(lu->ipiv);
+  delete lu;
+  return BEAST_OK;
+}
+
+static double dev_norm(beast_ctx* ctx, int64_t n, const double* x, double* scratch) {
+  vec_norm2(n, x, scratch, ctx->stream);
+  double h = 0;
+  cudaMemcpyAsync(&h, scratch, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  return std::sqrt(h);
+}
+
+// core of the dense solve on device vectors (b, x: c128 [n x nrhs], ld n)
+static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dtype,
+                              int precision, const double* b, double* x, int64_t nrhs, double tol,
+                              int maxiter, int* iters, double* resid) {
+  cudaStream_t st = ctx->stream;
+  const bool mixed = precision == BEAST_MIXED;
+  const int fdt = mixed ? BEAST_C64 : BEAST_C128;
+  const size_t fel = mixed ? 8 : 16;
+  void* F = nullptr;
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&F, (size_t)n * n * fel, st));
+  // factor a copy (c64 for the mixed path)
+  if (mixed) {
+    if (a_dtype == BEAST_C64)
+      BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(F, n * 8, A, lda * 8, n * 8, n, cudaMemcpyDeviceToDevice, st));
+    else
+      BEAST_CUDA_TRY(ctx, convert_c128_to_c64(n, n, (const double*)A, lda, (float*)F, n, st));
+  } else {
+    ARG_CHECK(ctx, a_dtype == BEAST_C128, "plain FP64 solve needs a c128 matrix");
+    BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(F, n * 16, A, lda * 16, n * 16, n, cudaMemcpyDeviceToDevice, st));
+  }
+  beast_lu* lu = nullptr;
+  int rc = beast_lu_factor(ctx, n, F, n, fdt, &lu);
+  if (rc) {
+    beast_lu_free(lu);
+    cudaFreeAsync(F, st);
+    return rc;
+  }
+  double *r = nullptr, *d = nullptr, *nrm = nullptr;
+  float* d32 = nullptr;
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&r, n * 16, st));
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&d, n * 16, st));
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&nrm, 64, st));
+  if (mixed) BEAST_CUDA_TRY(ctx, cudaMallocAsync(&d32, n * 8, st));
+  int it_max = 0;
+  double res_max = 0;
+  for (int64_t k = 0; k < nrhs && rc == BEAST_OK; ++k) {
+    const double* bk = b + 2 * k * n;
+    double* xk = x + 2 * k * n;
+    double bn = dev_norm(ctx, n, bk, nrm);
+    if (!mixed) {
+      BEAST_CUDA_TRY(ctx, vec_copy(n, bk, xk, st));
+      rc = lu_solve_dev(ctx, n, F, n, BEAST_C128, lu->ipiv, xk, n, 1);
+      if (rc) break;
+      BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
+      BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, 0, xk, r, -1.0, 1.0, st));
+      double rn = dev_norm(ctx, n, r, nrm);
+      res_max = std::max(res_max, bn > 0 ? rn / bn : rn);
+      continue;
+    }
+    // mixed: FP32 LU + FP64 iterative refinement
+    BEAST_CUDA_TRY(ctx, cudaMemsetAsync(xk, 0, n * 16, st));
+    BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
+    int it = 0;
+    double rel = 1.0;
+    while (true) {
+      BEAST_CUDA_TRY(ctx, convert_c128_to_c64(n, 1, r, n, d32, n, st));
+      rc = lu_solve_dev(ctx, n, F, n, BEAST_C64, lu->ipiv, d32, n, 1);
+      if (rc) break;
+      BEAST_CUDA_TRY(ctx, convert_c64_to_c128(n, 1, d32, n, d, n, st));
+      BEAST_CUDA_TRY(ctx, vec_axpy(n, 1.0, 0.0, d, xk, st));
+      BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
+      BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, a_dtype == BEAST_C64, xk, r, -1.0, 1.0, st));
+      ++it;
+      double rn = dev_norm(ctx, n, r, nrm);
+      rel = bn > 0 ? rn / bn : rn;
+      if (rel <= tol || it >= maxiter) break;
+    }
+    it_max = std::max(it_max, it);
+    res_max = std::max(res_max, rel);
+    if (rc == BEAST_OK && rel > tol)
+      rc = beast_fail(ctx, BEAST_ERR_NOCONV, "iterative refinement did not reach the tolerance");
+  }
+  cudaFreeAsync(r, st);
+  cudaFreeAsync(d, st);
+  cudaFreeAsync(nrm, st);
+  if (d32) cudaFreeAsync(d32, st);
+  beast_lu_free(lu);
+  cudaFreeAsync(F, st);
+  cudaStreamSynchronize(st);
+  if (iters) *iters = it_max;
+  if (resid) *resid = res_max;
+  return rc;
+}
+
+int beast_solve_dense(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dtype,
+                      int precision, const double* b, double* x, int64_t nrhs, int bx_loc,
+                      double tol, int maxiter, int* iters, double* resid) {
+  ARG_CHECK(ctx, ctx && A && b && x && n > 0 && lda >= n && nrhs >= 1, "invalid solve arguments");
+  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED, "unknown precision");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  if (maxiter <= 0) maxiter = 30;
+  if (tol <= 0) tol = 1e-12;
+  if (bx_loc == BEAST_DEVICE)
+    return solve_dense_device(ctx, n, A, lda, a_dtype, precision, b, x, nrhs, tol, maxiter, iters, resid);
+  double *db = nullptr, *dx = nullptr;
+  cudaStream_t st = ctx->stream;
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&db, n * nrhs * 16, st));
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&dx, n * nrhs * 16, st));
+  BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(db, b, n * nrhs * 16, cudaMemcpyHostToDevice, st));
+  int rc = solve_dense_device(ctx, n, A, lda, a_dtype, precision, db, dx, nrhs, tol, maxiter, iters, resid);
+  if (rc == BEAST_OK || rc == BEAST_ERR_NOCONV)
+    cudaMemcpyAsync(x, dx, n * nrhs * 16, cudaMemcpyDeviceToHost, st);
+  cudaFreeAsync(db, st);
+  cudaFreeAsync(dx, st);
+  cudaStreamSynchronize(st);
+  return rc;
+}
+
+// restarted GMRES with modified Gram-Schmidt (one dot kernel per basis vector) and Givens
+// rotations on the host (the Hessenberg matrix is tiny)
+int beast_gmres(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dtype, const double* b,
+                double* x, int bx_loc, double reltol, int restart, int maxiter, int* iters,
+                double* resid) {
+  ARG_CHECK(ctx, ctx && A && b && x && n > 0 && lda >= n, "invalid GMRES arguments");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  cudaStream_t st = ctx->stream;
+  if (restart <= 0) restart = (int)std::min<int64_t>(n, 200);
+  if (maxiter <= 0) maxiter = (int)n;
+  const int m = restart;
+  double *V = nullptr, *w = nullptr, *db = nullptr, *dx = nullptr, *h = nullptr, *nrm = nullptr;
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&V, (size_t)n * (m + 1) * 16, st));
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&w, n * 16, st));
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&h, (m + 2) * 16, st));
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&nrm, 64, st));
+  if (bx_loc != BEAST_DEVICE) {
+    BEAST_CUDA_TRY(ctx, cudaMallocAsync(&db, n * 16, st));
+    BEAST_CUDA_TRY(ctx, cudaMallocAsync(&dx, n * 16, st));
+    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(db, b, n * 16, cudaMemcpyHostToDevice, st));
+  } else {
+    db = (double*)b;
+    dx = x;
+  }
+  BEAST_CUDA_TRY(ctx, cudaMemsetAsync(dx, 0, n * 16, st));
+  typedef std::complex<double> cd;
+  double bn = dev_norm(ctx, n, db, nrm);
+  int it = 0;
+  double rel = 1.0;
+  std::vector<cd> H((size_t)(m + 1) * m), cs(m), sn(m), g(m + 1), y(m), hh(m + 1);
+  while (true) {
+    // r = b - A x  into V[:,0]
+    BEAST_CUDA_TRY(ctx, vec_copy(n, db, V, st));
+    BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, a_dtype == BEAST_C64, dx, V, -1.0, 1.0, st));
+    double rn = dev_norm(ctx, n, V, nrm);
+    rel = bn > 0 ? rn / bn : rn;
+    if (rel <= reltol || it >= maxiter || rn == 0.0) break;
+    BEAST_CUDA_TRY(ctx, vec_axpy(n, 1.0 / rn - 1.0, 0.0, V, V, st));  // V0 *= 1/rn
+    std::fill(g.begin(), g.end(), cd(0));
+    g[0] = rn;
+    int k = 0;
+    for (; k < m && it < maxiter; ++k) {
+      double* vk = V + 2 * (int64_t)k * n;
+      double* vk1 = V + 2 * (int64_t)(k + 1) * n;
+      BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, a_dtype == BEAST_C64, vk, w, 1.0, 0.0, st));
+      // modified Gram-Schmidt as two classical passes (reorthogonalisation), FP64
+      for (int pass = 0; pass < 2; ++pass) {
+        BEAST_CUDA_TRY(ctx, vec_dots(n, k + 1, V, n, w, h, st));
+        BEAST_CUDA_TRY(ctx, vec_gemv_sub(n, k + 1, V, n, h, w, st));
+        BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(hh.data(), h, (k + 1) * 16, cudaMemcpyDeviceToHost, st));
+        BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+        for (int j = 0; j <= k; ++j) {
+          if (pass == 0)
+            H[j + (size_t)k * (m + 1)] = hh[j];
+          else
+            H[j + (size_t)k * (m + 1)] += hh[j];
+        }
+      }
+      double hn = dev_norm(ctx, n, w, nrm);
+      H[k + 1 + (size_t)k * (m + 1)] = hn;
+      BEAST_CUDA_TRY(ctx, cudaMemsetAsync(vk1, 0, n * 16, st));
+      if (hn > 0) BEAST_CUDA_TRY(ctx, vec_axpy(n, 1.0 / hn, 0.0, w, vk1, st));
+      for (int j = 0; j < k; ++j) {
+        cd h0 = H[j + (size_t)k * (m + 1)], h1 = H[j + 1 + (size_t)k * (m + 1)];
+        H[j + (size_t)k * (m + 1)] = std::conj(cs[j]) * h0 + std::conj(sn[j]) * h1;
+        H[j + 1 + (size_t)k * (m + 1)] = -sn[j] * h0 + cs[j] * h1;
+      }
+      cd h0 = H[k + (size_t)k * (m + 1)], h1 = H[k + 1 + (size_t)k * (m + 1)];
+      double den = std::sqrt(std::norm(h0) + std::norm(h1));
+      cs[k] = den > 0 ? h0 / den : cd(1);
+      sn[k] = den > 0 ? h1 / den : cd(0);
+      H[k + (size_t)k * (m + 1)] = den;
+      g[k + 1] = -sn[k] * g[k];
+      g[k] = std::conj(cs[k]) * g[k];
+      ++it;
+      if (std::abs(g[k + 1]) <= reltol * bn) {
+        ++k;
+        break;
+      }
+    }
+    for (int j = k - 1; j >= 0; --j) {
+      cd s = g[j];
+      for (int l = j + 1; l < k; ++l) s -= H[j + (size_t)l * (m + 1)] * y[l];
+      y[j] = s / H[j + (size_t)j * (m + 1)];
+    }
+    std::vector<double> yh(2 * k);
+    for (int j = 0; j < k; ++j) {
+      yh[2 * j] = -y[j].real();  // vec_gemv_sub subtracts
+      yh[2 * j + 1] = -y[j].imag();
+    }
+    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(h, yh.data(), k * 16, cudaMemcpyHostToDevice, st));
+    BEAST_CUDA_TRY(ctx, vec_gemv_sub(n, k, V, n, h, dx, st));
+  }
+  if (bx_loc != BEAST_DEVICE) BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(x, dx, n * 16, cudaMemcpyDeviceToHost, st));
+  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  cudaFreeAsync(V, st);
+  cudaFreeAsync(w, st);
+  cudaFreeAsync(h, st);
+  cudaFreeAsync(nrm, st);
+  if (bx_loc != BEAST_DEVICE) {
+    cudaFreeAsync(db, st);
+    cudaFreeAsync(dx, st);
+  }
+  cudaStreamSynchronize(st);
+  if (iters) *iters = it;
+  if (resid) *resid = rel;
+  if (rel > reltol) return beast_fail(ctx, BEAST_ERR_NOCONV, "GMRES did not converge");
+  return BEAST_OK;
+}
+
+int beast_solve_job(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs,
+                    const beast_space* space, int exc_kind, const double* dir, const double* pol,
+                    double egr, double egi, int precision, double tol, double* x, int x_loc,
+                    int* iters, double* resid) {
+  ARG_CHECK(ctx, ctx && op && qs && space && dir && x, "null argument");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  cudaStream_t st = ctx->stream;
+  const int64_t n = space->nfuncs;
+  const int dt = precision == BEAST_MIXED ? BEAST_C64 : BEAST_C128;
+  const size_t el = dt == BEAST_C64 ? 8 : 16;
+  void* Z = nullptr;
+  double *b = nullptr, *dx = nullptr;
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&Z, (size_t)n * n * el, st));
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&b, n * 16, st));
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&dx, n * 16, st));
+  int rc = beast_assemble(ctx, op, qs, space, space, precision, Z, n, dt, BEAST_DEVICE, 0, 0, 1.0, 0.0, 0);
+  if (rc == BEAST_OK) {
+    double p3[3] = {0, 0, 0};
+    if (pol) memcpy(p3, pol, sizeof(p3));
+    TriRuleDev r;
+    make_trirule(8, &r);
+    cudaError_t e = launch_rhs(exc_kind, space, dir, p3, egr, egi, 1.0, 0.0, r, b, st);
+    if (e != cudaSuccess) rc = beast_fail(ctx, BEAST_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (rc == BEAST_OK)
+    rc = solve_dense_device(ctx, n, Z, n, dt, precision, b, dx, 1, tol > 0 ? tol : 1e-12, 30, iters, resid);
+  if (rc == BEAST_OK || rc == BEAST_ERR_NOCONV) {
+    if (x_loc == BEAST_DEVICE)
+      cudaMemcpyAsync(x, dx, n * 16, cudaMemcpyDeviceToDevice, st);
+    else
+      cudaMemcpyAsync(x, dx, n * 16, cudaMemcpyDeviceToHost, st);
+  }
+  cudaFreeAsync(Z, st);
+  cudaFreeAsync(b, st);
+  cudaFreeAsync(dx, st);
+  cudaStreamSynchronize(st);
+  return rc;
+}
+
+}  // extern "C"

@@ -1,0 +1,1390 @@
+// assemble.cu -- GB300 kernels of the Galerkin assembly path.
+//
+// Pipeline of one beast_assemble call (per trial-dof chunk):
+//   k_far     every (test cell p, trial cell q) pair of the chunk: pair classification
+//             (quadrule, src/quadrature/doublenumwiltonsauterqstrat.jl:32-69) and, for far
+//             pairs, the DoubleQuadRule block (src/quadrature/doublenumints.jl:12-43) in FP64
+//             or FP32.  The per-point-pair work is reduced algebraically: for RT shapes
+//             f_i = (x - v_i)/2A the 3x3 block is a fixed combination of 8 (single layer) or
+//             10/16 (double layer, n x K) complex moments of the kernel, accumulated with
+//             coordinates relative to the cell centroids.  Near pairs go to a list.
+//   k_near    one warp per listed pair: Sauter-Schwab (touching) or Wilton singularity
+//             extraction (near), FP64 (src/quadrature/sauterschwabints.jl:156-182,
+//             src/quadrature/singularityextractionints.jl:4-22).
+//   k_gather  Z[m,n] = sum over the shapes of dof m and dof n of a*b*Zcell: the RT/P0/P1
+//             local-to-global scatter (src/integralop.jl:173-184) as an owner-computes
+//             gather: every output entry written once, no atomics, deterministic.
+#include <cuda_runtime.h>
+
+#include <cmath>
+
+#include "internal.h"
+
+namespace {
+
+#define DEV __device__ __forceinline__
+
+template <typename R>
+struct V3 {
+  R x, y, z;
+};
+template <typename R>
+DEV V3<R> mk(R a, R b, R c) {
+  return V3<R>{a, b, c};
+}
+template <typename R>
+DEV V3<R> operator+(V3<R> a, V3<R> b) {
+  return {a.x + b.x, a.y + b.y, a.z + b.z};
+}
+template <typename R>
+DEV V3<R> operator-(V3<R> a, V3<R> b) {
+  return {a.x - b.x, a.y - b.y, a.z - b.z};
+}
+template <typename R>
+DEV V3<R> operator*(R s, V3<R> a) {
+  return {s * a.x, s * a.y, s * a.z};
+}
+template <typename R>
+DEV R dot(V3<R> a, V3<R> b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+template <typename R>
+DEV V3<R> cross(V3<R> a, V3<R> b) {
+  return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x};
+}
+
+// complex numbers as (re, im) pairs
+template <typename R>
+struct C2 {
+  R re, im;
+};
+template <typename R>
+DEV C2<R> cmul(C2<R> a, C2<R> b) {
+  return {a.re * b.re - a.im * b.im, a.re * b.im + a.im * b.re};
+}
+template <typename R>
+DEV C2<R> cadd(C2<R> a, C2<R> b) {
+  return {a.re + b.re, a.im + b.im};
+}
+template <typename R>
+DEV C2<R> csub(C2<R> a, C2<R> b) {
+  return {a.re - b.re, a.im - b.im};
+}
+template <typename R>
+DEV C2<R> cscale(R s, C2<R> a) {
+  return {s * a.re, s * a.im};
+}
+// complex vector (3 complex components)
+template <typename R>
+struct CV {
+  C2<R> x, y, z;
+};
+template <typename R>
+DEV void cv_zero(CV<R>& a) {
+  a.x = a.y = a.z = C2<R>{0, 0};
+}
+template <typename R>
+DEV void cv_axpy(C2<R> s, V3<R> v, CV<R>& acc) {  // acc += s * v
+  acc.x.re += s.re * v.x; acc.x.im += s.im * v.x;
+  acc.y.re += s.re * v.y; acc.y.im += s.im * v.y;
+  acc.z.re += s.re * v.z; acc.z.im += s.im * v.z;
+}
+template <typename R>
+DEV C2<R> rdot(V3<R> v, const CV<R>& c) {  // v . c
+  return {v.x * c.x.re + v.y * c.y.re + v.z * c.z.re, v.x * c.x.im + v.y * c.y.im + v.z * c.z.im};
+}
+template <typename R>
+DEV CV<R> rcross_cv(V3<R> a, const CV<R>& c) {  // a x c
+  CV<R> r;
+  r.x = {a.y * c.z.re - a.z * c.y.re, a.y * c.z.im - a.z * c.y.im};
+  r.y = {a.z * c.x.re - a.x * c.z.re, a.z * c.x.im - a.x * c.z.im};
+  r.z = {a.x * c.y.re - a.y * c.x.re, a.x * c.y.im - a.y * c.x.im};
+  return r;
+}
+
+const double PI = 3.14159265358979323846;
+const double I4PI = 0.07957747154594767;  // 1/(4 pi)
+
+// exp(-gamma R) / (4 pi R) for gamma = gr + i gi
+DEV C2<double> green_d(double gr, double gi, double R, double iR) {
+  double s, c;
+  sincos(gi * R, &s, &c);
+  double a = (gr == 0.0 ? 1.0 : exp(-gr * R)) * I4PI * iR;
+  return {a * c, -a * s};
+}
+DEV C2<float> green_f(float gr, float gi, float R, float iR) {
+  float s, c;
+  sincosf(gi * R, &s, &c);
+  float a = (gr == 0.0f ? 1.0f : expf(-gr * R)) * (float)I4PI * iR;
+  return {a * c, -a * s};
+}
+template <typename R>
+DEV C2<R> green(R gr, R gi, R Rr, R iR);
+template <>
+DEV C2<double> green<double>(double gr, double gi, double Rr, double iR) {
+  return green_d(gr, gi, Rr, iR);
+}
+template <>
+DEV C2<float> green<float>(float gr, float gi, float Rr, float iR) {
+  return green_f(gr, gi, Rr, iR);
+}
+template <typename R>
+DEV R rsq(R x);
+template <>
+DEV double rsq<double>(double x) {
+  return rsqrt(x);
+}
+template <>
+DEV float rsq<float>(float x) {
+  return rsqrtf(x);
+}
+
+// expm1 of a complex argument (accurate for small |z|)
+DEV C2<double> cexpm1_d(C2<double> z) {
+  double s, c, sh;
+  sincos(z.im, &s, &c);
+  sh = sin(0.5 * z.im);
+  double ea = exp(z.re), em = expm1(z.re);
+  return {em * c - 2.0 * sh * sh, ea * s};
+}
+DEV C2<double> cexp_d(C2<double> z) {
+  double s, c;
+  sincos(z.im, &s, &c);
+  double e = exp(z.re);
+  return {e * c, e * s};
+}
+
+struct Geo {
+  V3<double> v[3];
+  V3<double> c, n;
+  double area;
+};
+DEV Geo load_geo(const double* g) {
+  Geo r;
+  for (int i = 0; i < 3; ++i) r.v[i] = mk(g[3 * i], g[3 * i + 1], g[3 * i + 2]);
+  r.c = mk(g[9], g[10], g[11]);
+  r.n = mk(g[12], g[13], g[14]);
+  r.area = g[15];
+  return r;
+}
+
+// ------------------------------------------------------------------------------------
+// per-cell geometry (chart: x = u v1 + v v2 + (1-u-v) v3, normal (v1-v3)x(v2-v3)/|.|)
+// ------------------------------------------------------------------------------------
+__global__ void k_geometry(const double* verts, const int* mcells, const int* act, int64_t n,
+                           double* geo, float* geof) {
+  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (c >= n) return;
+  int mc = act[c];
+  V3<double> v[3];
+  for (int i = 0; i < 3; ++i) {
+    const double* p = verts + 3 * (int64_t)mcells[3 * (int64_t)mc + i];
+    v[i] = mk(p[0], p[1], p[2]);
+  }
+  V3<double> cr = cross(v[0] - v[2], v[1] - v[2]);
+  double j = sqrt(dot(cr, cr));
+  V3<double> cen = (1.0 / 3.0) * (v[0] + v[1] + v[2]);
+  double* g = geo + c * GEO_STRIDE;
+  for (int i = 0; i < 3; ++i) {
+    g[3 * i] = v[i].x;
+    g[3 * i + 1] = v[i].y;
+    g[3 * i + 2] = v[i].z;
+  }
+  g[9] = cen.x; g[10] = cen.y; g[11] = cen.z;
+  g[12] = cr.x / j; g[13] = cr.y / j; g[14] = cr.z / j;
+  g[15] = 0.5 * j;
+  double rad = 0;
+  for (int i = 0; i < 3; ++i) {
+    V3<double> d = v[i] - cen;
+    rad = fmax(rad, sqrt(dot(d, d)));
+  }
+  geof[4 * c] = (float)cen.x;
+  geof[4 * c + 1] = (float)cen.y;
+  geof[4 * c + 2] = (float)cen.z;
+  geof[4 * c + 3] = (float)(rad * (1.0 + 1e-6));
+}
+
+// ------------------------------------------------------------------------------------
+// pair classification: quadrule(..., ::DoubleNumWiltonSauterQStrat)
+// returns 3/2/1 (common face/edge/vertex), -1 (Wilton SE) or 0 (far DQ)
+// ------------------------------------------------------------------------------------
+DEV int classify_exact(const Geo& t, const Geo& s, int qs_kind, double k2) {
+  const double dtol = 1.0e3 * 2.220446049250313e-16;
+  int hits = 0;
+  double dmin2 = 1e308;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      V3<double> d = t.v[i] - s.v[j];
+      double d2 = dot(d, d);
+      dmin2 = fmin(dmin2, d2);
+      if (sqrt(d2) < dtol) ++hits;
+    }
+  if (qs_kind == BEAST_QS_DOUBLENUM) return 0;
+  if (hits > 0) return hits;
+  if (qs_kind == BEAST_QS_SAUTER) return 0;
+  double h2 = s.area;
+  if (fmax(dmin2 * k2, dmin2 / (16.0 * h2)) < 0.2 * 0.2) return -1;
+  return 0;
+}
+
+// squared distance below which a pair can be near (strategy threshold of the trial cell)
+DEV double near_threshold2(int qs_kind, double k2, double area) {
+  if (qs_kind == BEAST_QS_DOUBLENUM) return -1.0;
+  if (qs_kind == BEAST_QS_SAUTER) return 0.0;
+  // max(d^2 k2, d^2/(16 A)) < 0.04  <=>  d^2 < 0.04 min(1/k2, 16 A)
+  double t = 0.04 * 16.0 * area;
+  if (k2 > 0) t = fmin(t, 0.04 / k2);
+  return t;
+}
+
+// ------------------------------------------------------------------------------------
+// far-pair kernel
+// ------------------------------------------------------------------------------------
+struct FarParams {
+  OpParams op;
+  int qs_kind;
+  double k2;
+  const double* tgeo;
+  const float* tgeof;
+  int64_t np;
+  const double* bgeo;
+  const float* bgeof;
+  const int* qcells;
+  int nq;
+  void* zcell;
+  int64_t ldc;
+  NearPair* near;
+  int near_cap;
+  int* near_count;
+  int* flag;
+  TriRuleDev ro, ri;
+};
+
+constexpr int FAR_THREADS = 128;
+constexpr int FAR_QT = 16;  // trial cells staged per CTA
+
+template <typename R>
+DEV void store_c(void* z, int64_t idx, C2<R> v, int c64);
+
+template <typename R>
+DEV void store_c(void* z, int64_t idx, C2<R> v, int c64) {
+  if (c64)
+    reinterpret_cast<float2*>(z)[idx] = make_float2((float)v.re, (float)v.im);
+  else
+    reinterpret_cast<double2*>(z)[idx] = make_double2((double)v.re, (double)v.im);
+}
+
+// shared trial-cell record: sigma_j (9), centroid (3), normal (3), area, then the inner rule
+// points eta_b (3) + weight per point, all relative to the trial centroid
+constexpr int QREC_HDR = 16;
+
+template <int OPK, int TK, int BK, typename R, int C64>
+__global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
+  extern __shared__ double sm[];
+  const int ni = P.ri.n;
+  const int rec = QREC_HDR + 4 * ni;
+  const int q0 = blockIdx.y * FAR_QT;
+  const int nqt = min(FAR_QT, P.nq - q0);
+  // ---- stage trial cells
+  for (int k = threadIdx.x; k < nqt * (1 + ni); k += blockDim.x) {
+    int qi = k / (1 + ni), b = k % (1 + ni);
+    const double* g = P.bgeo + (int64_t)P.qcells[q0 + qi] * GEO_STRIDE;
+    double* r = sm + qi * rec;
+    V3<double> c = mk(g[9], g[10], g[11]);
+    if (b == 0) {
+      for (int j = 0; j < 3; ++j) {
+        r[3 * j] = g[3 * j] - c.x;
+        r[3 * j + 1] = g[3 * j + 1] - c.y;
+        r[3 * j + 2] = g[3 * j + 2] - c.z;
+      }
+      r[9] = c.x; r[10] = c.y; r[11] = c.z;
+      r[12] = g[12]; r[13] = g[13]; r[14] = g[14];
+      r[15] = g[15];
+    } else {
+      int bb = b - 1;
+      double u = P.ri.u[bb], v = P.ri.v[bb], w = 1.0 - u - v;
+      // eta = u sigma0 + v sigma1 + w sigma2  (sigma relative to the centroid)
+      double ex = u * (g[0] - c.x) + v * (g[3] - c.x) + w * (g[6] - c.x);
+      double ey = u * (g[1] - c.y) + v * (g[4] - c.y) + w * (g[7] - c.y);
+      double ez = u * (g[2] - c.z) + v * (g[5] - c.z) + w * (g[8] - c.z);
+      double* pt = r + QREC_HDR + 4 * bb;
+      pt[0] = ex; pt[1] = ey; pt[2] = ez; pt[3] = P.ri.w[bb];
+    }
+  }
+  __syncthreads();
+  const int64_t p = blockIdx.x * (int64_t)FAR_THREADS + threadIdx.x;
+  if (p >= P.np) return;
+  const double* tg = P.tgeo + p * GEO_STRIDE;
+  const V3<double> cp = mk(tg[9], tg[10], tg[11]);
+  V3<double> tau[3];
+  for (int i = 0; i < 3; ++i) tau[i] = mk(tg[3 * i] - cp.x, tg[3 * i + 1] - cp.y, tg[3 * i + 2] - cp.z);
+  const V3<double> np_ = mk(tg[12], tg[13], tg[14]);
+  const double Ap = tg[15];
+  const float4 tf = reinterpret_cast<const float4*>(P.tgeof)[p];
+  const R gr = (R)P.op.gr, gi = (R)P.op.gi;
+  const int nst = (TK == BEAST_P0) ? 1 : 3, nsb = (BK == BEAST_P0) ? 1 : 3;
+  const int no = P.ro.n;
+
+  for (int qi = 0; qi < nqt; ++qi) {
+    const double* rq = sm + qi * rec;
+    const int ql = q0 + qi;
+    const V3<double> cq = mk(rq[9], rq[10], rq[11]);
+    const double Aq = rq[15];
+    // ---- near test (FP32 candidate filter, exact FP64 classification of candidates)
+    if (P.qs_kind != BEAST_QS_DOUBLENUM) {
+      const float4 bf = reinterpret_cast<const float4*>(P.bgeof)[P.qcells[ql]];
+      float dx = tf.x - bf.x, dy = tf.y - bf.y, dz = tf.z - bf.z;
+      float d2f = dx * dx + dy * dy + dz * dz;
+      double thr2 = near_threshold2(P.qs_kind, P.k2, Aq);
+      float lim = tf.w + bf.w + (float)sqrt(fmax(thr2, 0.0));
+      if (d2f <= lim * lim * 1.0001f + 1e-30f) {
+        Geo t = load_geo(tg);
+        Geo s = load_geo(P.bgeo + (int64_t)P.qcells[ql] * GEO_STRIDE);
+        int cls = classify_exact(t, s, P.qs_kind, P.k2);
+        if (cls != 0) {
+          int idx = atomicAdd(P.near_count, 1);
+          if (idx < P.near_cap)
+            P.near[idx] = NearPair{(int)p, ql, cls, 0};
+          else
+            atomicOr(P.flag, 1);
+          for (int i = 0; i < nst; ++i)
+            for (int j = 0; j < nsb; ++j)
+              store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * p + i, C2<R>{0, 0}, C64);
+          continue;
+        }
+      }
+    }
+    const V3<R> d = mk((R)(cp.x - cq.x), (R)(cp.y - cq.y), (R)(cp.z - cq.z));
+    const double* pts = rq + QREC_HDR;
+
+    if (OPK == BEAST_MW_SL || OPK == BEAST_MW_DL || OPK == BEAST_MW_NXDL) {
+      // ---- RT x RT with moment reduction
+      C2<R> M0{0, 0}, M1{0, 0}, M2{0, 0}, M3{0, 0};  // scalar moments
+      CV<R> V1, V2, V3_, V4, V5, V6;                   // vector moments
+      cv_zero(V1); cv_zero(V2); cv_zero(V3_); cv_zero(V4); cv_zero(V5); cv_zero(V6);
+      const V3<R> nn = mk((R)np_.x, (R)np_.y, (R)np_.z);
+      for (int a = 0; a < no; ++a) {
+        const double ua = P.ro.u[a], va = P.ro.v[a], wa3 = 1.0 - ua - va;
+        const V3<R> xi = mk((R)(ua * tau[0].x + va * tau[1].x + wa3 * tau[2].x),
+                            (R)(ua * tau[0].y + va * tau[1].y + wa3 * tau[2].y),
+                            (R)(ua * tau[0].z + va * tau[1].z + wa3 * tau[2].z));
+        const R wa = (R)P.ro.w[a];
+        const V3<R> dx = d + xi;
+        // inner sums over trial points: U0 = sum w K, U1 = sum w K eta,
+        // U2 = sum w K eta (n.eta), U3 = sum w K (n.eta)   (K = G or grad coefficient)
+        C2<R> U0{0, 0}, U3{0, 0};
+        CV<R> U1, U2;
+        cv_zero(U1); cv_zero(U2);
+        for (int b = 0; b < ni; ++b) {
+          const double* pb = pts + 4 * b;
+          const V3<R> eta = mk((R)pb[0], (R)pb[1], (R)pb[2]);
+          const R wb = (R)pb[3];
+          const V3<R> r = dx - eta;
+          const R R2 = dot(r, r);
+          const R iR = rsq<R>(R2);
+          const R Rr = R2 * iR;
+          C2<R> G = green<R>(gr, gi, Rr, iR);
+          C2<R> K;
+          if (OPK == BEAST_MW_SL) {
+            K = cscale(wb, G);
+          } else {  // grad G = c r, c = -(gamma + 1/R) G / R
+            C2<R> c = cmul(C2<R>{-(gr + iR), -gi}, G);
+            K = cscale(wb * iR, c);
+          }
+          U0 = cadd(U0, K);
+          cv_axpy(K, eta, U1);
+          if (OPK == BEAST_MW_NXDL) {
+            R ne = dot(nn, eta);
+            C2<R> Kn = cscale(ne, K);
+            U3 = cadd(U3, Kn);
+            cv_axpy(Kn, eta, U2);
+          }
+        }
+        // fold the inner sums into the pair moments
+        if (OPK == BEAST_MW_SL) {
+          // M0 = sum G, V1 = sum G xi, V2 = sum G eta, M1 = sum G xi.eta
+          C2<R> s0 = cscale(wa, U0);
+          M0 = cadd(M0, s0);
+          cv_axpy(s0, xi, V1);
+          V2.x = cadd(V2.x, cscale(wa, U1.x));
+          V2.y = cadd(V2.y, cscale(wa, U1.y));
+          V2.z = cadd(V2.z, cscale(wa, U1.z));
+          M1 = cadd(M1, cscale(wa, rdot(xi, U1)));
+        } else if (OPK == BEAST_MW_DL) {
+          // D0 = sum c xi.(d x eta) = xi.(d x U1) ; Dxr = sum c (xi x r) = (xi x d) U0 - xi x U1
+          // Drh = sum c (r x eta) = (d + xi) x U1 ; Dr = sum c r = (d + xi) U0 - U1
+          M0 = cadd(M0, cscale(wa, rdot(xi, rcross_cv(d, U1))));
+          CV<R> xu = rcross_cv(xi, U1);
+          V3<R> xd = cross(xi, d);
+          V1.x = cadd(V1.x, cscale(wa, csub(cscale(xd.x, U0), xu.x)));
+          V1.y = cadd(V1.y, cscale(wa, csub(cscale(xd.y, U0), xu.y)));
+          V1.z = cadd(V1.z, cscale(wa, csub(cscale(xd.z, U0), xu.z)));
+          CV<R> du = rcross_cv(dx, U1);
+          V2.x = cadd(V2.x, cscale(wa, du.x));
+          V2.y = cadd(V2.y, cscale(wa, du.y));
+          V2.z = cadd(V2.z, cscale(wa, du.z));
+          V3_.x = cadd(V3_.x, cscale(wa, csub(cscale(dx.x, U0), U1.x)));
+          V3_.y = cadd(V3_.y, cscale(wa, csub(cscale(dx.y, U0), U1.y)));
+          V3_.z = cadd(V3_.z, cscale(wa, csub(cscale(dx.z, U0), U1.z)));
+        } else {  // n x K, n = test normal
+          const R xr = dot(xi, dx);     // xi.(d + xi)
+          const R nd = dot(nn, dx);     // n.(d + xi)
+          C2<R> xU1 = rdot(xi, U1), xU2 = rdot(xi, U2);
+          // N1 = (xi.(d+xi)) U3 - xi.U2
+          M0 = cadd(M0, cscale(wa, csub(cscale(xr, U3), xU2)));
+          // N2 = (xi.(d+xi)) U0 - xi.U1
+          M1 = cadd(M1, cscale(wa, csub(cscale(xr, U0), xU1)));
+          // N3 = (d + xi) U3 - U2
+          V1.x = cadd(V1.x, cscale(wa, csub(cscale(dx.x, U3), U2.x)));
+          V1.y = cadd(V1.y, cscale(wa, csub(cscale(dx.y, U3), U2.y)));
+          V1.z = cadd(V1.z, cscale(wa, csub(cscale(dx.z, U3), U2.z)));
+          // N4 = (d + xi) U0 - U1
+          V2.x = cadd(V2.x, cscale(wa, csub(cscale(dx.x, U0), U1.x)));
+          V2.y = cadd(V2.y, cscale(wa, csub(cscale(dx.y, U0), U1.y)));
+          V2.z = cadd(V2.z, cscale(wa, csub(cscale(dx.z, U0), U1.z)));
+          // N5 = n.(d+xi) xi.U1 - xi.U2
+          M2 = cadd(M2, cscale(wa, csub(cscale(nd, xU1), xU2)));
+          // N6 = xi (n.(d+xi) U0 - U3)
+          C2<R> t6 = cscale(wa, csub(cscale(nd, U0), U3));
+          cv_axpy(t6, xi, V3_);
+          // N7 = n.(d+xi) U1 - U2
+          V4.x = cadd(V4.x, cscale(wa, csub(cscale(nd, U1.x), U2.x)));
+          V4.y = cadd(V4.y, cscale(wa, csub(cscale(nd, U1.y), U2.y)));
+          V4.z = cadd(V4.z, cscale(wa, csub(cscale(nd, U1.z), U2.z)));
+          // N8 = n.(d+xi) U0 - U3
+          M3 = cadd(M3, t6);
+        }
+      }
+      // ---- finalize the 3x3 block (x Ap Aq from the rule weights, / (4 Ap Aq) from the shapes)
+      for (int i = 0; i < 3; ++i) {
+        const V3<R> ti = mk((R)tau[i].x, (R)tau[i].y, (R)tau[i].z);
+        for (int j = 0; j < 3; ++j) {
+          const V3<R> sj = mk((R)rq[3 * j], (R)rq[3 * j + 1], (R)rq[3 * j + 2]);
+          C2<R> z;
+          if (OPK == BEAST_MW_SL) {
+            // alpha/4 (Mxe - Mx.s - t.Me + (t.s) M0) + beta M0
+            C2<R> f = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
+            f = cadd(f, cscale(dot(ti, sj), M0));
+            C2<R> al{(R)P.op.ar, (R)P.op.ai}, be{(R)P.op.br, (R)P.op.bi};
+            z = cadd(cscale((R)0.25, cmul(al, f)), cmul(be, M0));
+          } else if (OPK == BEAST_MW_DL) {
+            // 1/4 [D0 - Dxr.s - t.Drh + (s x t).Dr]
+            C2<R> f = csub(csub(M0, rdot(sj, V1)), rdot(ti, V2));
+            f = cadd(f, rdot(cross(sj, ti), V3_));
+            z = cscale((R)0.25, f);
+          } else {
+            const R ns = dot(nn, sj);
+            // 1/4 [N1 - N2 n.s - t.N3 + (t.N4) n.s - N5 + N6.s + t.N7 - (t.s) N8]
+            C2<R> f = csub(M0, cscale(ns, M1));
+            f = csub(f, rdot(ti, V1));
+            f = cadd(f, cscale(ns, rdot(ti, V2)));
+            f = csub(f, M2);
+            f = cadd(f, rdot(sj, V3_));
+            f = cadd(f, rdot(ti, V4));
+            f = csub(f, cscale(dot(ti, sj), M3));
+            z = cscale((R)0.25, f);
+          }
+          store_c<R>(P.zcell, (int64_t)(3 * ql + j) * P.ldc + 3 * p + i, z, C64);
+        }
+      }
+    } else {
+      // ---- Helmholtz kernels on P0/P1: per point pair with shape products
+      C2<R> acc[9];
+      for (int k = 0; k < 9; ++k) acc[k] = C2<R>{0, 0};
+      const V3<R> nq = mk((R)rq[12], (R)rq[13], (R)rq[14]);
+      const V3<R> nn = mk((R)np_.x, (R)np_.y, (R)np_.z);
+      for (int a = 0; a < no; ++a) {
+        const double ua = P.ro.u[a], va = P.ro.v[a], wa3 = 1.0 - ua - va;
+        const V3<R> xi = mk((R)(ua * tau[0].x + va * tau[1].x + wa3 * tau[2].x),
+                            (R)(ua * tau[0].y + va * tau[1].y + wa3 * tau[2].y),
+                            (R)(ua * tau[0].z + va * tau[1].z + wa3 * tau[2].z));
+        const R lt[3] = {(R)ua, (R)va, (R)wa3};
+        const R wa = (R)P.ro.w[a];
+        const V3<R> dx = d + xi;
+        for (int b = 0; b < ni; ++b) {
+          const double* pb = pts + 4 * b;
+          const V3<R> eta = mk((R)pb[0], (R)pb[1], (R)pb[2]);
+          const R wb = (R)pb[3] * wa;
+          const V3<R> r = dx - eta;
+          const R R2 = dot(r, r);
+          const R iR = rsq<R>(R2);
+          const R Rr = R2 * iR;
+          C2<R> G = green<R>(gr, gi, Rr, iR);
+          C2<R> K;
+          C2<R> al{(R)P.op.ar, (R)P.op.ai};
+          if (OPK == BEAST_HH_SL) {
+            K = cmul(al, G);
+          } else {
+            C2<R> c = cscale(iR, cmul(C2<R>{-(gr + iR), -gi}, G));  // grad G = c r
+            c = cmul(al, c);
+            if (OPK == BEAST_HH_DL)
+              K = cscale(-dot(nq, r), c);
+            else
+              K = cscale(dot(nn, r), c);
+          }
+          K = cscale(wb, K);
+          const double ub = P.ri.u[b], vb = P.ri.v[b];
+          const R lb[3] = {(R)ub, (R)vb, (R)(1.0 - ub - vb)};
+          for (int i = 0; i < nst; ++i)
+            for (int j = 0; j < nsb; ++j) {
+              R s = (TK == BEAST_P0 ? (R)1 : lt[i]) * (BK == BEAST_P0 ? (R)1 : lb[j]);
+              acc[i * nsb + j] = cadd(acc[i * nsb + j], cscale(s, K));
+            }
+        }
+      }
+      const R ApAq = (R)(Ap * Aq);
+      for (int i = 0; i < nst; ++i)
+        for (int j = 0; j < nsb; ++j)
+          store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * p + i,
+                     cscale(ApAq, acc[i * nsb + j]), C64);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// near pairs (FP64): generic per-point integrand
+// ------------------------------------------------------------------------------------
+struct Shp {
+  double s[3];
+  V3<double> v[3];
+  double div[3];
+};
+
+DEV void shapes(int kind, const Geo& g, V3<double> x, const double* bary, Shp& S) {
+  if (kind == BEAST_RT) {
+    double ij = 0.5 / g.area;
+    for (int i = 0; i < 3; ++i) {
+      S.v[i] = ij * (x - g.v[i]);
+      S.div[i] = 2.0 * ij;
+    }
+  } else if (kind == BEAST_P0) {
+    S.s[0] = 1.0;
+  } else {
+    for (int i = 0; i < 3; ++i) S.s[i] = bary[i];
+  }
+}
+
+// operator kinds for the regular parts of singularity extraction
+enum { REG = 100 };
+
+// adds w * k_ij(x, y) to acc[i*nb + j]
+DEV void integrand(int kind, const OpParams& op, V3<double> x, V3<double> y, V3<double> nx,
+                   V3<double> ny, int tk, const Shp& f, int bk, const Shp& g, double w,
+                   C2<double>* acc) {
+  const int nt = tk == BEAST_P0 ? 1 : 3, nb = bk == BEAST_P0 ? 1 : 3;
+  V3<double> r = x - y;
+  double R = sqrt(dot(r, r));
+  double iR = 1.0 / R;
+  C2<double> gam{op.gr, op.gi};
+  C2<double> gR{op.gr * R, op.gi * R};
+  C2<double> al{op.ar, op.ai}, be{op.br, op.bi};
+  switch (kind) {
+    case BEAST_MW_SL:
+    case REG + BEAST_MW_SL: {
+      C2<double> G;
+      if (kind == BEAST_MW_SL) {
+        G = cexp_d(C2<double>{-gR.re, -gR.im});
+        G = cscale(I4PI * iR, G);
+      } else {  // (expm1(-gR) + gR - gR^2/2) / (4 pi R)
+        C2<double> e = cexpm1_d(C2<double>{-gR.re, -gR.im});
+        C2<double> g2 = cmul(gR, gR);
+        G = cadd(e, csub(gR, cscale(0.5, g2)));
+        G = cscale(1.0 / (4.0 * PI * R), G);
+      }
+      C2<double> aG = cmul(al, G), bG = cmul(be, G);
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          C2<double> t = cadd(cscale(dot(f.v[i], g.v[j]), aG), cscale(f.div[i] * g.div[j], bG));
+          acc[i * 3 + j] = cadd(acc[i * 3 + j], cscale(w, t));
+        }
+      break;
+    }
+    case BEAST_MW_DL:
+    case REG + BEAST_MW_DL:
+    case BEAST_MW_NXDL: {
+      C2<double> c;
+      if (kind == REG + BEAST_MW_DL) {
+        C2<double> ex = cexp_d(C2<double>{-gR.re, -gR.im});
+        C2<double> g2 = cmul(gR, gR);
+        C2<double> t = cmul(C2<double>{-(gR.re + 1.0), -gR.im}, ex);
+        t = cadd(t, C2<double>{1.0 - 0.5 * g2.re, -0.5 * g2.im});
+        c = cscale(I4PI * iR * iR * iR, t);
+      } else {
+        C2<double> G = cscale(I4PI * iR, cexp_d(C2<double>{-gR.re, -gR.im}));
+        c = cscale(iR, cmul(C2<double>{-(op.gr + iR), -op.gi}, G));
+      }
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          double t;
+          if (kind == BEAST_MW_NXDL)
+            t = dot(f.v[i], cross(nx, cross(r, g.v[j])));
+          else
+            t = dot(f.v[i], cross(r, g.v[j]));
+          acc[i * 3 + j] = cadd(acc[i * 3 + j], cscale(w * t, c));
+        }
+      break;
+    }
+    case BEAST_HH_SL:
+    case REG + BEAST_HH_SL: {
+      C2<double> G;
+      if (kind == BEAST_HH_SL) {
+        G = cscale(I4PI * iR, cexp_d(C2<double>{-gR.re, -gR.im}));
+      } else {  // (expm1(-gR) - gR^2/2) / (4 pi R)
+        C2<double> e = cexpm1_d(C2<double>{-gR.re, -gR.im});
+        C2<double> g2 = cmul(gR, gR);
+        G = cscale(1.0 / (4.0 * PI * R), csub(e, cscale(0.5, g2)));
+      }
+      C2<double> aG = cmul(al, G);
+      for (int i = 0; i < nt; ++i)
+        for (int j = 0; j < nb; ++j)
+          acc[i * nb + j] = cadd(acc[i * nb + j], cscale(w * f.s[i] * g.s[j], aG));
+      break;
+    }
+    default: {  // HH DL / DLT and their regular parts
+      bool reg = kind >= REG;
+      int base = reg ? kind - REG : kind;
+      C2<double> c;
+      if (reg) {
+        C2<double> ex = cexp_d(C2<double>{-gR.re, -gR.im});
+        C2<double> g2 = cmul(gR, gR);
+        C2<double> t = cmul(C2<double>{-(gR.re + 1.0), -gR.im}, ex);
+        t = cadd(t, C2<double>{1.0 - 0.5 * g2.re, -0.5 * g2.im});
+        c = cscale(I4PI * iR * iR * iR, t);  // the reference's regular part omits alpha
+      } else {
+        C2<double> G = cscale(I4PI * iR, cexp_d(C2<double>{-gR.re, -gR.im}));
+        c = cmul(al, cscale(iR, cmul(C2<double>{-(op.gr + iR), -op.gi}, G)));
+      }
+      C2<double> k = base == BEAST_HH_DL ? cscale(-dot(ny, r), c) : cscale(dot(nx, r), c);
+      for (int i = 0; i < nt; ++i)
+        for (int j = 0; j < nb; ++j)
+          acc[i * nb + j] = cadd(acc[i * nb + j], cscale(w * f.s[i] * g.s[j], k));
+      break;
+    }
+  }
+}
+
+// Wilton et al. (1984) potential integrals over triangle s seen from x:
+// S[0] = int d/R^3, S[1] = int 1/R, S[2] = int 1, S[3] = int R;
+// Vm1 = int (rho'-rho)/R^3, V1 = int (rho'-rho)/R, V2 = int (rho'-rho), V3 = int (rho'-rho) R
+struct Wilton {
+  double S[4];
+  V3<double> V[4];
+  V3<double> n;
+  double d;
+};
+
+DEV void wilton(const Geo& s, V3<double> x, Wilton& W) {
+  const double tol = 2.220446049250313e-16 * 1e3;
+  V3<double> n = cross(s.v[1] - s.v[0], s.v[2] - s.v[0]);
+  n = (1.0 / sqrt(dot(n, n))) * n;
+  double d = dot(x - s.v[0], n);
+  double D = fabs(d);
+  V3<double> c = x - d * n;
+  for (int k = 0; k < 4; ++k) {
+    W.S[k] = 0;
+    W.V[k] = mk(0.0, 0.0, 0.0);
+  }
+  bool inside = true;
+  int nthru = 0;
+  int thru[3] = {0, 0, 0};
+  for (int i = 0; i < 3; ++i) {
+    V3<double> a = s.v[i], b = s.v[(i + 1) % 3];
+    V3<double> ab = b - a;
+    double l = sqrt(dot(ab, ab));
+    V3<double> t = (1.0 / l) * ab;
+    V3<double> m = cross(t, n);
+    double xa = dot(a - c, t), xb = dot(b - c, t);
+    double p = dot(a - c, m);
+    if (p < 0) inside = false;
+    double w2 = p * p + d * d;
+    double ra = sqrt(xa * xa + w2), rb = sqrt(xb * xb + w2);
+    double lg;
+    if (fabs(p) > tol) {
+      lg = log((xb + rb) / (xa + ra));
+      double at = atan(d * xb / (p * rb)) - atan(d * xa / (p * ra));
+      W.S[0] += -at;
+      W.S[1] += p * lg + d * at;
+      W.S[2] += 0.5 * p * (xb - xa);
+      W.S[3] += p * (xb * rb - xa * ra) / 6.0 + (0.5 * d * d + p * p / 6.0) * p * lg + d * d * d * at / 3.0;
+      W.V[1] = W.V[1] + (0.5 * ((xb * rb - xa * ra) + w2 * lg)) * m;
+      W.V[2] = W.V[2] + (0.5 * xb * (xb * xb / 3.0 + p * p) - 0.5 * xa * (xa * xa / 3.0 + p * p)) * m;
+    } else {
+      if (xa * xb < tol * tol) thru[nthru++] = i;
+      if (D > tol) {
+        lg = log((xb + rb) / (xa + ra));
+        W.V[1] = W.V[1] + (0.5 * (xb * rb - xa * ra) + 0.5 * w2 * lg) * m;
+      } else {
+        lg = (xb > 0) ? log(xb / xa) : log(xa / xb);
+        W.V[1] = W.V[1] + (0.5 * (xb * rb - xa * ra)) * m;
+      }
+      W.V[2] = W.V[2] + (xb * xb * xb / 6.0 - xa * xa * xa / 6.0) * m;
+    }
+    W.V[0] = W.V[0] + (-lg) * m;
+    W.V[3] = W.V[3] + ((xb * rb * rb * rb - xa * ra * ra * ra) / 12.0 + w2 * (xb * rb - xa * ra) / 8.0 +
+                       w2 * w2 * lg / 8.0) * m;
+  }
+  double sgn = D < tol ? 0.0 : (d > 0 ? 1.0 : (d < 0 ? -1.0 : 0.0));
+  double alpha = 0;
+  if (nthru == 0 && inside)
+    alpha = 2 * PI;
+  else if (nthru == 1)
+    alpha = PI;
+  else if (nthru == 2) {
+    V3<double> e1 = s.v[(thru[0] + 1) % 3] - s.v[thru[0]];
+    V3<double> e2 = s.v[(thru[1] + 1) % 3] - s.v[thru[1]];
+    double ca = -dot(e1, e2) / sqrt(dot(e1, e1) * dot(e2, e2));
+    alpha = acos(fmax(-1.0, fmin(1.0, ca)));
+  }
+  W.S[0] += alpha * sgn;
+  W.S[1] += -alpha * D;
+  W.S[3] += -alpha * D * D * D / 3.0;
+  W.n = n;
+  W.d = d;
+}
+
+// singular part at one test point x (weight dx); returns false if not available
+DEV bool se_singular(const OpParams& op, int tk, int bk, const Geo& t, const Geo& s,
+                     V3<double> x, double dx, C2<double>* acc) {
+  Wilton W;
+  wilton(s, x, W);
+  V3<double> rho = x - W.d * W.n;
+  C2<double> g{op.gr, op.gi};
+  C2<double> g2 = cmul(g, g);
+  C2<double> h = cscale(0.5, g2);
+  // grad'(1/R) and grad' R integrated over the trial triangle
+  V3<double> gm1 = (-1.0) * (W.V[0] - W.S[0] * W.n);
+  V3<double> gR = W.V[1] - (W.d * W.S[1]) * W.n;
+  C2<double> al{op.ar, op.ai}, be{op.br, op.bi};
+  switch (op.kind) {
+    case BEAST_MW_SL: {
+      if (tk != BEAST_RT || bk != BEAST_RT) return false;
+      // int G = (S1 - g S2 + g^2/2 S3) / 4pi ; int G y = (V1 + S1 rho - g (V2 + S2 rho) + g^2/2 (V3 + S3 rho)) / 4pi
+      C2<double> iG = cscale(1.0 / (4 * PI), cadd(csub(C2<double>{W.S[1], 0}, cscale(W.S[2], g)),
+                                                  cscale(W.S[3], h)));
+      V3<double> a1 = W.V[1] + W.S[1] * rho, a2 = W.V[2] + W.S[2] * rho, a3 = W.V[3] + W.S[3] * rho;
+      CV<double> iGy;
+      iGy.x = cscale(1.0 / (4 * PI), cadd(csub(C2<double>{a1.x, 0}, cscale(a2.x, g)), cscale(a3.x, h)));
+      iGy.y = cscale(1.0 / (4 * PI), cadd(csub(C2<double>{a1.y, 0}, cscale(a2.y, g)), cscale(a3.y, h)));
+      iGy.z = cscale(1.0 / (4 * PI), cadd(csub(C2<double>{a1.z, 0}, cscale(a2.z, g)), cscale(a3.z, h)));
+      double a = 1.0 / (4.0 * t.area * s.area);
+      for (int i = 0; i < 3; ++i) {
+        V3<double> gi = x - t.v[i];
+        for (int j = 0; j < 3; ++j) {
+          V3<double> b = s.v[j];
+          CV<double> f;
+          f.x = csub(iGy.x, cscale(b.x, iG));
+          f.y = csub(iGy.y, cscale(b.y, iG));
+          f.z = csub(iGy.z, cscale(b.z, iG));
+          C2<double> dg = rdot(gi, f);
+          C2<double> v = cadd(cscale(a, cmul(al, dg)), cscale(a * 4.0, cmul(be, iG)));
+          acc[i * 3 + j] = cadd(acc[i * 3 + j], cscale(dx, v));
+        }
+      }
+      return true;
+    }
+    case BEAST_MW_DL: {
+      if (tk != BEAST_RT || bk != BEAST_RT) return false;
+      // int grad_x G_s = -(grad'(1/R) + g^2/2 grad'R) / 4pi
+      CV<double> iDG;
+      iDG.x = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.x, 0}, cscale(gR.x, h)));
+      iDG.y = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.y, 0}, cscale(gR.y, h)));
+      iDG.z = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.z, 0}, cscale(gR.z, h)));
+      double a = 1.0 / (4.0 * t.area * s.area);
+      for (int i = 0; i < 3; ++i) {
+        V3<double> gi = x - t.v[i];
+        for (int j = 0; j < 3; ++j) {
+          V3<double> cr = cross(x - s.v[j], gi);
+          acc[i * 3 + j] = cadd(acc[i * 3 + j], cscale(a * dx, rdot(cr, iDG)));
+        }
+      }
+      return true;
+    }
+    case BEAST_HH_SL: {
+      if (tk != BEAST_P0 || bk != BEAST_P0) return false;
+      C2<double> iG = cscale(1.0 / (4 * PI), cadd(C2<double>{W.S[1], 0}, cscale(W.S[3], h)));
+      acc[0] = cadd(acc[0], cscale(dx, cmul(al, iG)));
+      return true;
+    }
+    case BEAST_HH_DL:
+    case BEAST_HH_DLT: {
+      if (tk != BEAST_P0 || bk != BEAST_P0) return false;
+      CV<double> iDG;
+      iDG.x = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.x, 0}, cscale(gR.x, h)));
+      iDG.y = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.y, 0}, cscale(gR.y, h)));
+      iDG.z = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.z, 0}, cscale(gR.z, h)));
+      C2<double> v;
+      if (op.kind == BEAST_HH_DL)
+        v = cscale(-1.0, rdot(s.n, iDG));
+      else
+        v = rdot(t.n, iDG);
+      acc[0] = cadd(acc[0], cscale(dx, cmul(al, v)));
+      return true;
+    }
+  }
+  return false;
+}
+
+__constant__ double c_gl_x[210];
+__constant__ double c_gl_w[210];
+__constant__ int c_gl_off[21];
+
+// one Sauter-Schwab node: map index -> reference points X, Y on {0<=x2<=x1<=1} and weight
+DEV void ss_node(int cls, int n, int64_t item, double* X, double* Y, double* w) {
+  int nreg = cls == 1 ? 2 : 6;
+  int reg = (int)(item % nreg);
+  int64_t k = item / nreg;
+  int i4 = (int)(k % n); k /= n;
+  int i3 = (int)(k % n); k /= n;
+  int i2 = (int)(k % n); k /= n;
+  int i1 = (int)k;
+  int o = c_gl_off[n - 1];
+  double xi = c_gl_x[o + i1], e1 = c_gl_x[o + i2], e2 = c_gl_x[o + i3], e3 = c_gl_x[o + i4];
+  double ww = c_gl_w[o + i1] * c_gl_w[o + i2] * c_gl_w[o + i3] * c_gl_w[o + i4];
+  double A[2], B[2], wt;
+  int sub = reg >> 1;
+  bool swap = reg & 1;
+  if (cls == 1) {  // common vertex: 2 regions
+    wt = ww * xi * xi * xi * e2;
+    A[0] = xi; A[1] = xi * e1;
+    B[0] = xi * e2; B[1] = xi * e2 * e3;
+  } else if (cls == 2) {  // common edge: x1 = xi, x2 = xi b, y1 = xi(1-a'), y2 = xi(1-a')c
+    double ap, bb, cc;
+    if (sub == 0) { ap = e1; bb = e1 * e2; cc = e1 * e3; }
+    else if (sub == 1) { bb = e1; ap = e1 * e2; cc = e1 * e3; }
+    else { cc = e1; ap = e1 * e2; bb = e1 * e3; }
+    wt = ww * xi * xi * xi * (1.0 - ap) * e1 * e1;
+    A[0] = xi; A[1] = xi * bb;
+    B[0] = xi * (1.0 - ap); B[1] = xi * (1.0 - ap) * cc;
+  } else {  // common face
+    double s = e1, t = e2, u = e3;
+    wt = ww * xi * xi * xi * s * (1.0 - s);
+    if (sub == 0) {
+      double ap = s * t, e = s * (1.0 - t), b = (1.0 - s) * u;
+      A[0] = xi; A[1] = xi * b;
+      B[0] = xi * (1.0 - ap); B[1] = xi * (b + e);
+    } else if (sub == 1) {
+      double ap = s, ep = s * t, cp = (1.0 - s) * u;
+      A[0] = xi; A[1] = xi * (cp + ep);
+      B[0] = xi * (1.0 - ap); B[1] = xi * cp;
+    } else {
+      double ep = s, ap = s * t, cp = (1.0 - s) * u;
+      A[0] = xi; A[1] = xi * (cp + ep);
+      B[0] = xi * (1.0 - ap); B[1] = xi * cp;
+    }
+  }
+  if (swap) {
+    X[0] = B[0]; X[1] = B[1]; Y[0] = A[0]; Y[1] = A[1];
+  } else {
+    X[0] = A[0]; X[1] = A[1]; Y[0] = B[0]; Y[1] = B[1];
+  }
+  *w = wt;
+}
+
+struct NearParams {
+  OpParams op;
+  beast_qs_desc qs;
+  int tk, bk;
+  const double* tgeo;
+  const double* bgeo;
+  const int* qcells;
+  const NearPair* near;
+  int nnear;
+  void* zcell;
+  int c64;
+  int64_t ldc;
+  int* flag;
+  TriRuleDev ro, ri;
+};
+
+constexpr int NEAR_WARPS = 4;
+
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
+  if (e >= P.nnear) return;
+  const NearPair np_ = P.near[e];
+  const Geo t = load_geo(P.tgeo + (int64_t)np_.p * GEO_STRIDE);
+  const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
+  const int nt = P.tk == BEAST_P0 ? 1 : 3, nb = P.bk == BEAST_P0 ? 1 : 3;
+  C2<double> acc[9];
+  for (int k = 0; k < 9; ++k) acc[k] = C2<double>{0, 0};
+  Shp f, g;
+  bool dl_face = np_.cls == 3 && (P.op.kind == BEAST_MW_DL || P.op.kind == BEAST_HH_DL ||
+                                  P.op.kind == BEAST_HH_DLT);
+  if (np_.cls >= 1 && !dl_face) {
+    // ---- Sauter-Schwab: shared vertices first, same order (SauterSchwabQuadrature.reorder)
+    const double dtol = 1.0e3 * 2.220446049250313e-16;
+    int pt[3], ps[3], hits = 0, ti[3], si[3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        V3<double> dd = t.v[i] - s.v[j];
+        if (sqrt(dot(dd, dd)) < dtol && hits < 3) {
+          ti[hits] = i;
+          si[hits] = j;
+          ++hits;
+        }
+      }
+    int k = 0;
+    for (int h = 0; h < hits; ++h) pt[k++] = ti[h];
+    for (int i = 0; i < 3; ++i) {
+      bool used = false;
+      for (int h = 0; h < hits; ++h) used |= ti[h] == i;
+      if (!used) pt[k++] = i;
+    }
+    k = 0;
+    for (int h = 0; h < hits; ++h) ps[k++] = si[h];
+    for (int j = 0; j < 3; ++j) {
+      bool used = false;
+      for (int h = 0; h < hits; ++h) used |= si[h] == j;
+      if (!used) ps[k++] = j;
+    }
+    const int n = np_.cls == 3 ? P.qs.ss_face : (np_.cls == 2 ? P.qs.ss_edge : P.qs.ss_vert);
+    const int nreg = np_.cls == 1 ? 2 : 6;
+    const int64_t items = (int64_t)nreg * n * n * n * n;
+    const double jac = 4.0 * t.area * s.area;
+    for (int64_t it = lane; it < items; it += 32) {
+      double X[2], Y[2], w;
+      ss_node(np_.cls, n, it, X, Y, &w);
+      double lt[3] = {1.0 - X[0], X[0] - X[1], X[1]}, ls[3] = {1.0 - Y[0], Y[0] - Y[1], Y[1]};
+      double bx[3], by[3];
+      for (int q = 0; q < 3; ++q) {
+        bx[pt[q]] = lt[q];
+        by[ps[q]] = ls[q];
+      }
+      V3<double> x = lt[0] * t.v[pt[0]] + lt[1] * t.v[pt[1]] + lt[2] * t.v[pt[2]];
+      V3<double> y = ls[0] * s.v[ps[0]] + ls[1] * s.v[ps[1]] + ls[2] * s.v[ps[2]];
+      shapes(P.tk, t, x, bx, f);
+      shapes(P.bk, s, y, by, g);
+      integrand(P.op.kind, P.op, x, y, t.n, s.n, P.tk, f, P.bk, g, w * jac, acc);
+    }
+  } else if (np_.cls == -1) {
+    // ---- singularity extraction: regular part by DQ (near rules) + analytic inner part
+    const int no = P.ro.n, ni = P.ri.n;
+    for (int it = lane; it < no * ni; it += 32) {
+      int a = it / ni, b = it % ni;
+      double bx[3] = {P.ro.u[a], P.ro.v[a], 1.0 - P.ro.u[a] - P.ro.v[a]};
+      double by[3] = {P.ri.u[b], P.ri.v[b], 1.0 - P.ri.u[b] - P.ri.v[b]};
+      V3<double> x = bx[0] * t.v[0] + bx[1] * t.v[1] + bx[2] * t.v[2];
+      V3<double> y = by[0] * s.v[0] + by[1] * s.v[1] + by[2] * s.v[2];
+      shapes(P.tk, t, x, bx, f);
+      shapes(P.bk, s, y, by, g);
+      integrand(REG + P.op.kind, P.op, x, y, t.n, s.n, P.tk, f, P.bk, g,
+                P.ro.w[a] * t.area * P.ri.w[b] * s.area, acc);
+    }
+    for (int a = lane; a < no; a += 32) {
+      double bx[3] = {P.ro.u[a], P.ro.v[a], 1.0 - P.ro.u[a] - P.ro.v[a]};
+      V3<double> x = bx[0] * t.v[0] + bx[1] * t.v[1] + bx[2] * t.v[2];
+      if (!se_singular(P.op, P.tk, P.bk, t, s, x, P.ro.w[a] * t.area, acc)) atomicOr(P.flag, 2);
+    }
+  }
+  // ---- warp reduction and store
+  for (int k = 0; k < nt * nb; ++k) {
+    double re = acc[k].re, im = acc[k].im;
+    for (int o = 16; o > 0; o >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, o);
+      im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    acc[k] = C2<double>{re, im};
+  }
+  if (lane == 0) {
+    for (int i = 0; i < nt; ++i)
+      for (int j = 0; j < nb; ++j)
+        store_c<double>(P.zcell, (int64_t)(nb * np_.q + j) * P.ldc + nt * (int64_t)np_.p + i,
+                        acc[i * nb + j], P.c64);
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// gather: Z[m, n] = sum_{(p,r,a) of m} sum_{(q,s,b) of n} a b Zcell[nst p + r, nsb q' + s]
+// ------------------------------------------------------------------------------------
+template <int ZC64, int OC64>
+__global__ void k_gather(GatherArgs G, const int64_t* tptr, const int* tcell, const int* tshape,
+                         const double* tcoef, const int64_t* bptr, const int* bcell,
+                         const int* bshape, const double* bcoef, int nst, int nsb,
+                         int64_t nrows) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  for (int64_t n = G.n0 + blockIdx.y; n < G.n1; n += gridDim.y) {
+    if (m >= nrows) continue;
+    double re = 0, im = 0;
+    for (int64_t f = bptr[n]; f < bptr[n + 1]; ++f) {
+      int ql = G.qlocal[bcell[f]];
+      int64_t col = (int64_t)nsb * ql + bshape[f];
+      double b = bcoef[f];
+      for (int64_t e = tptr[m]; e < tptr[m + 1]; ++e) {
+        int64_t row = (int64_t)nst * tcell[e] + tshape[e];
+        double ab = tcoef[e] * b;
+        int64_t idx = col * G.ldc + row;
+        if (ZC64) {
+          float2 z = reinterpret_cast<const float2*>(G.zcell)[idx];
+          re += ab * z.x;
+          im += ab * z.y;
+        } else {
+          double2 z = reinterpret_cast<const double2*>(G.zcell)[idx];
+          re += ab * z.x;
+          im += ab * z.y;
+        }
+      }
+    }
+    double vr = G.cr * re - G.ci * im, vi = G.cr * im + G.ci * re;
+    int64_t o = (G.row_off + m) + (G.col_off + n) * G.ldz;
+    if (OC64) {
+      float2* Z = reinterpret_cast<float2*>(G.Z);
+      if (G.accumulate) {
+        float2 old = Z[o];
+        vr += old.x;
+        vi += old.y;
+      }
+      Z[o] = make_float2((float)vr, (float)vi);
+    } else {
+      double2* Z = reinterpret_cast<double2*>(G.Z);
+      if (G.accumulate) {
+        double2 old = Z[o];
+        vr += old.x;
+        vi += old.y;
+      }
+      Z[o] = make_double2(vr, vi);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// local operators (Identity / NCross on RT x RT), deterministic per test dof
+// ------------------------------------------------------------------------------------
+__global__ void k_local(int which, const int64_t* tptr, const int* tcell, const int* tshape,
+                        const double* tcoef, const int* tcells_mesh, const double* tgeo,
+                        const int* b_cell2act, const int* bad_dof, const double* bad_coef,
+                        int bmaxfn, TriRuleDev r, int64_t nrows, void* Z, int64_t ldz, int zc64,
+                        int64_t row_off, int64_t col_off, double cr, double ci) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= nrows) return;
+  int64_t cols[16];
+  double vals[16];
+  int nc = 0;
+  for (int64_t e = tptr[m]; e < tptr[m + 1]; ++e) {
+    int pa = tcell[e], ra = tshape[e];
+    double a = tcoef[e];
+    int qb = b_cell2act[tcells_mesh[pa]];
+    if (qb < 0) continue;
+    Geo g = load_geo(tgeo + (int64_t)pa * GEO_STRIDE);
+    double gram[3] = {0, 0, 0};
+    for (int k = 0; k < r.n; ++k) {
+      double bx[3] = {r.u[k], r.v[k], 1.0 - r.u[k] - r.v[k]};
+      V3<double> x = bx[0] * g.v[0] + bx[1] * g.v[1] + bx[2] * g.v[2];
+      double w = r.w[k] * g.area;
+      Shp f;
+      shapes(BEAST_RT, g, x, bx, f);
+      for (int j = 0; j < 3; ++j)
+        gram[j] += w * (which == 0 ? dot(f.v[ra], f.v[j]) : dot(f.v[ra], cross(g.n, f.v[j])));
+    }
+    for (int j = 0; j < 3; ++j)
+      for (int kb = 0; kb < bmaxfn; ++kb) {
+        int n = bad_dof[((int64_t)qb * 3 + j) * bmaxfn + kb];
+        if (n < 0) continue;
+        double v = a * gram[j] * bad_coef[((int64_t)qb * 3 + j) * bmaxfn + kb];
+        int slot = -1;
+        for (int s = 0; s < nc; ++s)
+          if (cols[s] == n) slot = s;
+        if (slot < 0 && nc < 16) {
+          slot = nc++;
+          cols[slot] = n;
+          vals[slot] = 0;
+        }
+        if (slot >= 0) vals[slot] += v;
+      }
+  }
+  for (int s = 0; s < nc; ++s) {
+    int64_t o = (row_off + m) + (col_off + cols[s]) * ldz;
+    if (zc64) {
+      float2* z = reinterpret_cast<float2*>(Z);
+      float2 old = z[o];
+      z[o] = make_float2((float)(old.x + cr * vals[s]), (float)(old.y + ci * vals[s]));
+    } else {
+      double2* z = reinterpret_cast<double2*>(Z);
+      double2 old = z[o];
+      z[o] = make_double2(old.x + cr * vals[s], old.y + ci * vals[s]);
+    }
+  }
+}
+
+// ------------------------------------------------------------------------------------
+// excitation: b[m] = sum_{(p,r,a) of m} a * int f_r . F  (deterministic per dof)
+// ------------------------------------------------------------------------------------
+__global__ void k_rhs(int kind, int tk, const int64_t* tptr, const int* tcell, const int* tshape,
+                      const double* tcoef, const double* tgeo, double dx, double dy, double dz,
+                      double px, double py, double pz, double gr, double gi, double ar, double ai,
+                      TriRuleDev r, int64_t nrows, double* b) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (m >= nrows) return;
+  V3<double> d = mk(dx, dy, dz), u = mk(px, py, pz);
+  C2<double> gam{gr, gi}, amp{ar, ai};
+  C2<double> pref{1.0, 0.0};
+  V3<double> fu = u;
+  if (kind == BEAST_EXC_CROSSTRACE_H) {
+    // H = -1/(i k) curl E, curl E = -gamma (d x u) E0 ; with k = -i gamma: H = (d x u) E0 gamma/(i k)
+    C2<double> k{gi, -gr};                 // k = -i gamma
+    C2<double> ik{-k.im, k.re};            // i k
+    double den = ik.re * ik.re + ik.im * ik.im;
+    pref = C2<double>{(gam.re * ik.re + gam.im * ik.im) / den, (gam.im * ik.re - gam.re * ik.im) / den};
+    fu = cross(d, u);
+  }
+  double re = 0, im = 0;
+  for (int64_t e = tptr[m]; e < tptr[m + 1]; ++e) {
+    int pa = tcell[e], ra = tshape[e];
+    double a = tcoef[e];
+    Geo g = load_geo(tgeo + (int64_t)pa * GEO_STRIDE);
+    for (int k = 0; k < r.n; ++k) {
+      double bx[3] = {r.u[k], r.v[k], 1.0 - r.u[k] - r.v[k]};
+      V3<double> x = bx[0] * g.v[0] + bx[1] * g.v[1] + bx[2] * g.v[2];
+      double w = r.w[k] * g.area;
+      C2<double> ph = cmul(amp, cexp_d(C2<double>{-(gr * dot(d, x)), -(gi * dot(d, x))}));
+      double val;
+      if (kind == BEAST_EXC_HH_DIRICHLET) {
+        val = tk == BEAST_P0 ? 1.0 : bx[ra];
+      } else {
+        Shp f;
+        shapes(BEAST_RT, g, x, bx, f);
+        if (kind == BEAST_EXC_TANGTRACE_E)
+          val = dot(f.v[ra], cross(cross(g.n, fu), g.n));
+        else
+          val = dot(f.v[ra], cross(g.n, fu));
+      }
+      C2<double> t = cscale(w * val * a, cmul(pref, ph));
+      re += t.re;
+      im += t.im;
+    }
+  }
+  b[2 * m] = re;
+  b[2 * m + 1] = im;
+}
+
+// ------------------------------------------------------------------------------------
+// far field (src/postproc.jl:174-211, 273-288; src/maxwell/farfield.jl:60-63)
+// ------------------------------------------------------------------------------------
+__global__ void k_farfield(const double* geo, const int* ad_dof, const double* ad_coef, int maxfn,
+                           int64_t ncells, const double* u, const double* pts, double gr,
+                           double gi, TriRuleDev r, double* ff) {
+  const int p = blockIdx.x;
+  V3<double> yh = mk(pts[3 * p], pts[3 * p + 1], pts[3 * p + 2]);
+  double acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t c = threadIdx.x; c < ncells; c += blockDim.x) {
+    Geo g = load_geo(geo + c * GEO_STRIDE);
+    for (int k = 0; k < r.n; ++k) {
+      double bx[3] = {r.u[k], r.v[k], 1.0 - r.u[k] - r.v[k]};
+      V3<double> x = bx[0] * g.v[0] + bx[1] * g.v[1] + bx[2] * g.v[2];
+      double w = r.w[k] * g.area;
+      double ph = dot(yh, x);
+      C2<double> krn = cexp_d(C2<double>{gr * ph, gi * ph});  // exp(gamma yhat.x)
+      Shp f;
+      shapes(BEAST_RT, g, x, bx, f);
+      for (int i = 0; i < 3; ++i) {
+        C2<double> cu{0, 0};
+        for (int kk = 0; kk < maxfn; ++kk) {
+          int mdof = ad_dof[(c * 3 + i) * maxfn + kk];
+          if (mdof < 0) continue;
+          double a = ad_coef[(c * 3 + i) * maxfn + kk];
+          cu = cadd(cu, cscale(a, C2<double>{u[2 * mdof], u[2 * mdof + 1]}));
+        }
+        C2<double> s = cscale(w, cmul(krn, cu));
+        V3<double> tr = cross(cross(yh, f.v[i]), yh);
+        acc[0] += s.re * tr.x; acc[1] += s.im * tr.x;
+        acc[2] += s.re * tr.y; acc[3] += s.im * tr.y;
+        acc[4] += s.re * tr.z; acc[5] += s.im * tr.z;
+      }
+    }
+  }
+  __shared__ double red[6][256];
+  for (int k = 0; k < 6; ++k) red[k][threadIdx.x] = acc[k];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if (threadIdx.x < o)
+      for (int k = 0; k < 6; ++k) red[k][threadIdx.x] += red[k][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int k = 0; k < 6; ++k) ff[6 * p + k] = red[k][0];
+}
+
+}  // namespace
+
+#include "rules_gen.h"
+
+bool make_trirule(int degree, TriRuleDev* r) {
+  if (degree < 1 || degree > BEAST_TRI_MAXDEG) return false;
+  int off = beast_tri_off[degree], cnt = beast_tri_cnt[degree];
+  r->n = cnt;
+  for (int i = 0; i < cnt; ++i) {
+    r->u[i] = beast_tri_pts[off + i][0];
+    r->v[i] = beast_tri_pts[off + i][1];
+    r->w[i] = beast_tri_pts[off + i][2];
+  }
+  return true;
+}
+
+cudaError_t launch_geometry(const beast_space* s, cudaStream_t st) {
+  if (s->ncells == 0) return cudaSuccess;
+  int th = 256;
+  int64_t bl = (s->ncells + th - 1) / th;
+  k_geometry<<<(unsigned)bl, th, 0, st>>>(s->mesh->verts, s->mesh->cells, s->cells, s->ncells,
+                                           s->geo, s->geof);
+  return cudaGetLastError();
+}
+
+template <int OPK, int TK, int BK, typename R, int C64>
+static cudaError_t far_t(const FarParams& P, cudaStream_t st) {
+  dim3 grid((unsigned)((P.np + FAR_THREADS - 1) / FAR_THREADS), (unsigned)((P.nq + FAR_QT - 1) / FAR_QT));
+  size_t sm = (size_t)FAR_QT * (QREC_HDR + 4 * P.ri.n) * sizeof(double);
+  k_far<OPK, TK, BK, R, C64><<<grid, FAR_THREADS, sm, st>>>(P);
+  return cudaGetLastError();
+}
+
+template <int OPK, int TK, int BK>
+static cudaError_t far_prec(const FarParams& P, int precision, int c64, cudaStream_t st) {
+  if (precision == BEAST_MIXED) return far_t<OPK, TK, BK, float, 1>(P, st);
+  if (c64) return far_t<OPK, TK, BK, double, 1>(P, st);
+  return far_t<OPK, TK, BK, double, 0>(P, st);
+}
+
+template <int OPK>
+static cudaError_t far_hh(const FarParams& P, int tk, int bk, int precision, int c64, cudaStream_t st) {
+  if (tk == BEAST_P0 && bk == BEAST_P0) return far_prec<OPK, BEAST_P0, BEAST_P0>(P, precision, c64, st);
+  if (tk == BEAST_P0 && bk == BEAST_P1) return far_prec<OPK, BEAST_P0, BEAST_P1>(P, precision, c64, st);
+  if (tk == BEAST_P1 && bk == BEAST_P0) return far_prec<OPK, BEAST_P1, BEAST_P0>(P, precision, c64, st);
+  if (tk == BEAST_P1 && bk == BEAST_P1) return far_prec<OPK, BEAST_P1, BEAST_P1>(P, precision, c64, st);
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev& ri, cudaStream_t st) {
+  FarParams P;
+  P.op = a.op;
+  P.qs_kind = a.qs.kind;
+  P.k2 = a.op.gr * a.op.gr + a.op.gi * a.op.gi;
+  P.tgeo = a.ts->geo;
+  P.tgeof = a.ts->geof;
+  P.np = a.ts->ncells;
+  P.bgeo = a.bs->geo;
+  P.bgeof = a.bs->geof;
+  P.qcells = a.qcells;
+  P.nq = a.nq;
+  P.zcell = a.zcell;
+  P.ldc = a.ldc;
+  P.near = a.near;
+  P.near_cap = a.near_cap;
+  P.near_count = a.near_count;
+  P.flag = a.flag;
+  P.ro = ro;
+  P.ri = ri;
+  if (P.np == 0 || P.nq == 0) return cudaSuccess;
+  const int tk = a.ts->kind, bk = a.bs->kind;
+  const int kind = a.op.kind;
+  if (kind == BEAST_MW_SL || kind == BEAST_MW_DL || kind == BEAST_MW_NXDL) {
+    if (tk != BEAST_RT || bk != BEAST_RT) return cudaErrorInvalidValue;
+    if (kind == BEAST_MW_SL) return far_prec<BEAST_MW_SL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_c64, st);
+    if (kind == BEAST_MW_DL) return far_prec<BEAST_MW_DL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_c64, st);
+    return far_prec<BEAST_MW_NXDL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_c64, st);
+  }
+  if (kind == BEAST_HH_SL) return far_hh<BEAST_HH_SL>(P, tk, bk, a.precision, a.zcell_c64, st);
+  if (kind == BEAST_HH_DL) return far_hh<BEAST_HH_DL>(P, tk, bk, a.precision, a.zcell_c64, st);
+  if (kind == BEAST_HH_DLT) return far_hh<BEAST_HH_DLT>(P, tk, bk, a.precision, a.zcell_c64, st);
+  return cudaErrorInvalidValue;
+}
+
+static cudaError_t upload_gl(cudaStream_t st) {
+  static bool done[64] = {false};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (done[dev]) return cudaSuccess;
+  double x[210], w[210];
+  for (int i = 0; i < 210; ++i) {
+    x[i] = beast_gl_pts[i][0];
+    w[i] = beast_gl_pts[i][1];
+  }
+  cudaError_t e = cudaMemcpyToSymbol(c_gl_x, x, sizeof(x));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gl_w, w, sizeof(w));
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(c_gl_off, beast_gl_off, sizeof(int) * 21);
+  if (e == cudaSuccess) done[dev] = true;
+  (void)st;
+  return e;
+}
+
+cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const TriRuleDev& ri,
+                        cudaStream_t st) {
+  if (nnear <= 0) return cudaSuccess;
+  cudaError_t e = upload_gl(st);
+  if (e != cudaSuccess) return e;
+  NearParams P;
+  P.op = a.op;
+  P.qs = a.qs;
+  P.tk = a.ts->kind;
+  P.bk = a.bs->kind;
+  P.tgeo = a.ts->geo;
+  P.bgeo = a.bs->geo;
+  P.qcells = a.qcells;
+  P.near = a.near;
+  P.nnear = nnear;
+  P.zcell = a.zcell;
+  P.c64 = a.zcell_c64;
+  P.ldc = a.ldc;
+  P.flag = a.flag;
+  P.ro = ro;
+  P.ri = ri;
+  unsigned blocks = (unsigned)((nnear + NEAR_WARPS - 1) / NEAR_WARPS);
+  k_near<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_gather(const GatherArgs& g, cudaStream_t st) {
+  const beast_space* ts = g.ts;
+  const beast_space* bs = g.bs;
+  int64_t nrows = ts->nfuncs;
+  if (nrows == 0 || g.n1 <= g.n0) return cudaSuccess;
+  int th = 256;
+  dim3 grid((unsigned)((nrows + th - 1) / th), (unsigned)std::min<int64_t>(g.n1 - g.n0, 65535));
+  int nst = ts->kind == BEAST_P0 ? 1 : 3, nsb = bs->kind == BEAST_P0 ? 1 : 3;
+#define GATHER(ZC, OC)                                                                       \
+  k_gather<ZC, OC><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_cell, ts->fn_shape, ts->fn_coeff, \
+                                        bs->fn_ptr, bs->fn_cell, bs->fn_shape, bs->fn_coeff, nst, \
+                                        nsb, nrows)
+  if (g.zcell_c64) {
+    if (g.z_c64) GATHER(1, 1); else GATHER(1, 0);
+  } else {
+    if (g.z_c64) GATHER(0, 1); else GATHER(0, 0);
+  }
+#undef GATHER
+  return cudaGetLastError();
+}
+
+cudaError_t launch_rhs(int kind, const beast_space* ts, const double* dir, const double* pol,
+                       double gr, double gi, double ar, double ai, const TriRuleDev& r, double* b,
+                       cudaStream_t st) {
+  int64_t n = ts->nfuncs;
+  if (n == 0) return cudaSuccess;
+  int th = 128;
+  k_rhs<<<(unsigned)((n + th - 1) / th), th, 0, st>>>(kind, ts->kind, ts->fn_ptr, ts->fn_cell,
+                                                    ts->fn_shape, ts->fn_coeff, ts->geo, dir[0],
+                                                    dir[1], dir[2], pol[0], pol[1], pol[2], gr, gi,
+                                                    ar, ai, r, n, b);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_farfield(const beast_space* s, const double* u, const double* pts, int64_t npts,
+                            double gr, double gi, const TriRuleDev& r, double* ff, cudaStream_t st) {
+  if (npts == 0) return cudaSuccess;
+  k_farfield<<<(unsigned)npts, 256, 0, st>>>(s->geo, s->ad_dof, s->ad_coeff, s->maxfn, s->ncells, u,
+                                             pts, gr, gi, r, ff);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_local_impl(int which, const beast_space* ts, const beast_space* bs,
+                              const int* b_cell2act, const TriRuleDev& r, void* Z, int64_t ldz,
+                              int z_c64, int64_t row_off, int64_t col_off, double cr, double ci,
+                              cudaStream_t st) {
+  int64_t n = ts->nfuncs;
+  if (n == 0) return cudaSuccess;
+  int th = 128;
+  k_local<<<(unsigned)((n + th - 1) / th), th, 0, st>>>(which, ts->fn_ptr, ts->fn_cell, ts->fn_shape,
+                                                      ts->fn_coeff, ts->cells, ts->geo, b_cell2act,
+                                                      bs->ad_dof, bs->ad_coeff, bs->maxfn, r, n, Z,
+                                                      ldz, z_c64, row_off, col_off, cr, ci);
+  return cudaGetLastError();
+}

@@ -1,0 +1,171 @@
+// internal.h -- shared host/device declarations of libbeastgpu (not part of the ABI).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/beastgpu.h"
+
+#define BEAST_CUDA_TRY(ctx, expr)                                                  \
+  do {                                                                             \
+    cudaError_t e_ = (expr);                                                       \
+    if (e_ != cudaSuccess)                                                         \
+      return beast_fail((ctx), e_ == cudaErrorMemoryAllocation ? BEAST_ERR_OOM      \
+                                                               : BEAST_ERR_CUDA,  \
+                        std::string(#expr) + ": " + cudaGetErrorString(e_));       \
+  } while (0)
+
+struct beast_ctx {
+  int device = 0;
+  int num_sms = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  size_t ws_limit = 0;   // assembly workspace byte limit
+  std::string err;
+  // reusable device workspace
+  void* ws = nullptr;
+  size_t ws_size = 0;
+  int* d_flag = nullptr;  // device error / status word
+};
+
+struct beast_mesh {
+  beast_ctx* ctx = nullptr;
+  int64_t nv = 0, nc = 0;
+  double* verts = nullptr;   // [nv][3]
+  int* cells = nullptr;      // [nc][3] 0-based
+};
+
+// per active cell geometry, 16 doubles: v0 v1 v2 (9) | centroid (3) | unit normal (3) | area
+enum { GEO_STRIDE = 16 };
+
+struct beast_space {
+  beast_ctx* ctx = nullptr;
+  const beast_mesh* mesh = nullptr;
+  int kind = 0, nshapes = 0, maxfn = 0;
+  int64_t ncells = 0, nfuncs = 0;
+  int* cells = nullptr;        // active -> mesh cell
+  int* cell2act = nullptr;     // mesh cell -> active index (-1 if inactive)
+  int* ad_dof = nullptr;       // [ncells][nshapes][maxfn], -1 empty
+  double* ad_coeff = nullptr;
+  double* geo = nullptr;       // [ncells][GEO_STRIDE]
+  float* geof = nullptr;       // [ncells][4]: centroid (3), circumradius about centroid
+  // dof -> (active cell, local shape, coefficient), CSR
+  int64_t* fn_ptr = nullptr;
+  int* fn_cell = nullptr;
+  int* fn_shape = nullptr;
+  double* fn_coeff = nullptr;
+  std::vector<int64_t> h_fn_ptr;
+  std::vector<int> h_fn_cell, h_fn_shape;
+  std::vector<double> h_fn_coeff;
+  std::vector<int> h_ad_dof;   // host copy of the assembly data
+  std::vector<double> h_ad_coeff;
+};
+
+struct beast_lu {
+  beast_ctx* ctx = nullptr;
+  int64_t n = 0, lda = 0;
+  int dtype = 0;
+  void* A = nullptr;     // factors (not owned)
+  int* ipiv = nullptr;   // device, 0-based
+  int info = 0;
+};
+
+int beast_fail(beast_ctx* ctx, int code, const std::string& msg);
+
+// quadrature rule set passed by value to kernels
+enum { RULE_MAXPTS = 25 };
+struct TriRuleDev {
+  int n;
+  double u[RULE_MAXPTS], v[RULE_MAXPTS], w[RULE_MAXPTS];
+};
+bool make_trirule(int degree, TriRuleDev* r);
+
+struct OpParams {
+  int kind;
+  double gr, gi;   // gamma
+  double ar, ai;   // alpha
+  double br, bi;   // beta
+};
+
+// near-pair list entry
+struct NearPair {
+  int p, q;       // test active cell, trial cell (chunk-local index)
+  int cls;        // 3/2/1 Sauter-Schwab face/edge/vertex, -1 Wilton SE
+  int pad;
+};
+
+// ---- assembly launchers (assemble.cu)
+struct AsmArgs {
+  OpParams op;
+  beast_qs_desc qs;
+  const beast_space* ts;
+  const beast_space* bs;
+  int precision;
+  // chunk description
+  const int* qcells;   // device: trial active cell ids of this chunk [nq]
+  int nq;
+  void* zcell;         // device Zcell [ns_t*ncells_t x ns_b*nq], c128 or c64
+  int zcell_c64;
+  int64_t ldc;
+  NearPair* near;      // device near list
+  int near_cap;
+  int* near_count;     // device counter
+  int* flag;           // device error flag
+};
+cudaError_t launch_geometry(const beast_space* s, cudaStream_t st);
+cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev& ri,
+                       cudaStream_t st);
+cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro_near,
+                        const TriRuleDev& ri_near, cudaStream_t st);
+struct GatherArgs {
+  const beast_space* ts;
+  const beast_space* bs;
+  const void* zcell;
+  int zcell_c64;
+  int64_t ldc;
+  const int* qlocal;      // device: trial active cell -> chunk-local index (-1 absent)
+  int64_t n0, n1;         // trial dof range of this chunk
+  void* Z;
+  int64_t ldz;
+  int z_c64;
+  int64_t row_off, col_off;
+  double cr, ci;
+  int accumulate;
+};
+cudaError_t launch_gather(const GatherArgs& g, cudaStream_t st);
+cudaError_t launch_local_impl(int which, const beast_space* ts, const beast_space* bs,
+                              const int* b_cell2act, const TriRuleDev& r, void* Z, int64_t ldz,
+                              int z_c64, int64_t row_off, int64_t col_off, double cr, double ci,
+                              cudaStream_t st);
+cudaError_t launch_rhs(int kind, const beast_space* ts, const double* dir, const double* pol,
+                       double gr, double gi, double ar, double ai, const TriRuleDev& r,
+                       double* b, cudaStream_t st);
+cudaError_t launch_farfield(const beast_space* s, const double* u, const double* pts,
+                            int64_t npts, double gr, double gi, const TriRuleDev& r, double* ff,
+                            cudaStream_t st);
+
+// ---- dense linear algebra (linalg.cu)
+int lu_factor_dev(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, int* ipiv,
+                  int* info);
+int lu_solve_dev(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int dtype,
+                 const int* ipiv, void* B, int64_t ldb, int64_t nrhs);
+// y = alpha * A x + beta * y (FP64 arithmetic, A c128 or c64, x/y c128)
+cudaError_t gemv_dev(int64_t n, const void* A, int64_t lda, int a_c64, const double* x,
+                     double* y, double alpha, double beta, cudaStream_t st);
+cudaError_t convert_c128_to_c64(int64_t rows, int64_t cols, const double* src, int64_t lds,
+                                float* dst, int64_t ldd, cudaStream_t st);
+cudaError_t convert_c64_to_c128(int64_t rows, int64_t cols, const float* src, int64_t lds,
+                                double* dst, int64_t ldd, cudaStream_t st);
+// complex FP64 vector helpers
+cudaError_t vec_axpy(int64_t n, double ar, double ai, const double* x, double* y, cudaStream_t st);
+cudaError_t vec_copy(int64_t n, const double* x, double* y, cudaStream_t st);
+// reduction: sum of |x|^2 into out (device double), deterministic
+cudaError_t vec_norm2(int64_t n, const double* x, double* out, cudaStream_t st);
+// h[k] = <v_k, w> for k < m (columns of V with ld), FP64
+cudaError_t vec_dots(int64_t n, int m, const double* V, int64_t ldv, const double* w, double* h,
+                     cudaStream_t st);
+// w -= V h (m columns)
+cudaError_t vec_gemv_sub(int64_t n, int m, const double* V, int64_t ldv, const double* h,
+                         double* w, cudaStream_t st);

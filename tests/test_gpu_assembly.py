@@ -1,0 +1,134 @@
+"""GPU parity: libbeastgpu (through the C ABI) against the CPU oracle.
+
+Tolerances: FP64 path 1e-10 relative to the largest matrix entry, per entry; mixed path
+(FP32 far pairs, c64 storage) 2e-5 relative to the largest entry.
+"""
+import numpy as np
+import pytest
+
+import beastgpu as bg
+import oracle as O
+from conftest import mesh_path
+
+pytestmark = pytest.mark.gpu
+
+WS = (2, 3, 6, 7, 5, 5, 4, 3)
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    return bg.get_context(0)
+
+
+def rel(a, b):
+    return float(np.abs(a - b).max() / np.abs(b).max())
+
+
+def _orc_op(op):
+    return O.make_op(op.kind, op.gamma, op.alpha, op.beta)
+
+
+def _orc_qs(qs):
+    o = qs.orders()
+    return O.OrcQs(*o)
+
+
+def _check(op, X, Y, ctx, tol=1e-10, precision=bg.FP64, qs=None):
+    qs = qs or bg.defaultquadstrat(op, X, Y)
+    Z = bg.assemble(op, X, Y, quadstrat=qs, precision=precision, ctx=ctx)
+    Zo = O.assemble(_orc_op(op), _orc_qs(qs), X, Y)
+    e = rel(Z, Zo)
+    assert e < tol, e
+    return Z, Zo
+
+
+def test_efie_icosphere(ctx):
+    X = bg.raviartthomas(bg.icosphere(2))
+    _check(bg.Maxwell3D.singlelayer(wavenumber=2.0), X, X, ctx)
+
+
+def test_efie_reference_mesh_with_near_pairs(ctx):
+    # sphere45 is irregular enough to produce Wilton singularity-extraction pairs
+    X = bg.raviartthomas(bg.readmesh(mesh_path("sphere45.in")))
+    op = bg.Maxwell3D.singlelayer(wavenumber=3.0)
+    _check(op, X, X, ctx)
+
+
+def test_efie_static_alpha_beta(ctx):
+    X = bg.raviartthomas(bg.icosphere(1))
+    op = bg.operators.IntegralOperator(bg.operators.MW_SL, 1.0, 250.0, 1.0)
+    _check(op, X, X, ctx)
+
+
+def test_mfie_double_layer(ctx):
+    X = bg.raviartthomas(bg.icosphere(2))
+    _check(bg.Maxwell3D.doublelayer(wavenumber=2.0), X, X, ctx)
+
+
+def test_nxk(ctx):
+    X = bg.raviartthomas(bg.icosphere(1))
+    _check(bg.nxdoublelayer(wavenumber=2.0), X, X, ctx, tol=1e-9)
+
+
+@pytest.mark.parametrize("which", ["sl", "dl", "dlt"])
+def test_helmholtz_p0(ctx, which):
+    m = bg.ellipsoid(2, (1.0, 0.7, 1.3), perturb=0.01, rng=3)
+    X = bg.lagrangecxd0(m)
+    op = getattr(bg.Helmholtz3D, {"sl": "singlelayer", "dl": "doublelayer",
+                                  "dlt": "doublelayer_transposed"}[which])(gamma=1.0 + 1.0j)
+    _check(op, X, X, ctx)
+
+
+def test_helmholtz_p1_sauter(ctx):
+    m = bg.icosphere(1)
+    X = bg.lagrangec0d1(m)
+    op = bg.Helmholtz3D.singlelayer(wavenumber=1.5)
+    _check(op, X, X, ctx, qs=bg.DoubleNumSauterQstrat(2, 3, 4, 4, 4, 4))
+
+
+def test_mixed_precision_assembly(ctx):
+    X = bg.raviartthomas(bg.icosphere(2))
+    op = bg.Maxwell3D.singlelayer(wavenumber=2.0)
+    Z = bg.assemble(op, X, X, precision=bg.MIXED, ctx=ctx)
+    assert Z.dtype == np.complex64
+    Zo = O.assemble(_orc_op(op), _orc_qs(bg.defaultquadstrat(op, X, X)), X, X)
+    assert rel(Z.astype(np.complex128), Zo) < 2e-5
+
+
+def test_chunked_assembly_identical(ctx):
+    X = bg.raviartthomas(bg.icosphere(2))
+    op = bg.Maxwell3D.singlelayer(wavenumber=2.0)
+    Z1 = bg.assemble(op, X, X, ctx=ctx)
+    c2 = bg.Context(0)
+    c2.set_workspace_limit(4 << 20)  # forces many trial chunks
+    Z2 = bg.assemble(op, X, X, ctx=c2)
+    c2.close()
+    assert np.array_equal(Z1, Z2)
+
+
+def test_linear_combination_mfie(ctx):
+    # (n x K - 1/2 Id), examples/nxmfie.jl
+    X = bg.raviartthomas(bg.icosphere(1))
+    nxk = bg.nxdoublelayer(wavenumber=1.0)
+    Z = bg.assemble(nxk - 0.5 * bg.Identity(), X, X, ctx=ctx)
+    Zo = O.assemble(_orc_op(nxk), _orc_qs(bg.defaultquadstrat(nxk, X, X)), X, X)
+    Zo = Zo - 0.5 * O.assemble_local(0, X, X, degree=6)
+    assert rel(Z, Zo) < 1e-9
+
+
+def test_rhs_and_farfield(ctx):
+    X = bg.raviartthomas(bg.icosphere(2))
+    k = 2.0
+    E = bg.Maxwell3D.planewave(direction=(1, 0, 0), polarization=(0, 0, 1), wavenumber=k)
+    b = bg.assemble_rhs(bg.tangential_trace(E), X)
+    bo = O.rhs_planewave(0, X, (1, 0, 0), (0, 0, 1), 1j * k)
+    assert np.abs(b - bo).max() <= 1e-12 * np.abs(bo).max()
+    bh = bg.assemble_rhs(bg.cross_trace_H(E), X)
+    bho = O.rhs_planewave(1, X, (1, 0, 0), (0, 0, 1), 1j * k)
+    assert np.abs(bh - bho).max() <= 1e-12 * np.abs(bho).max()
+    u = np.random.default_rng(0).normal(size=X.numfunctions()) * (1 + 0.5j)
+    th = np.linspace(0, np.pi, 7)
+    dirs = np.stack([np.sin(th), np.zeros_like(th), np.cos(th)], axis=1)
+    ff = bg.farfield(X, u, dirs, 1j * k)
+    ffo = O.farfield(X, u, dirs, 1j * k)
+    assert np.abs(ff - ffo).max() <= 1e-12 * np.abs(ffo).max()

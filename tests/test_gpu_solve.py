@@ -1,0 +1,65 @@
+"""GPU parity of the dense solves: FP64 LU, mixed FP32 LU + FP64 refinement, GMRES."""
+import numpy as np
+import pytest
+
+import beastgpu as bg
+import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def efie():
+    m = bg.icosphere(3)  # 1280 triangles, 1920 RT edges
+    X = bg.raviartthomas(m)
+    k = 2.0
+    op = bg.Maxwell3D.singlelayer(wavenumber=k)
+    E = bg.Maxwell3D.planewave(direction=(1, 0, 0), polarization=(0, 0, 1), wavenumber=k)
+    Z = bg.assemble(op, X, X)
+    b = bg.assemble_rhs(bg.tangential_trace(E), X)
+    return X, op, E, Z, b
+
+
+def test_lu_fp64_matches_oracle(efie):
+    X, op, E, Z, b = efie
+    x, _, res = bg.solve(Z, b, precision=bg.FP64)
+    xo = O.lu_solve(Z, b)
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-10
+    assert res < 1e-12
+
+
+def test_lu_random_matrix_pivoting():
+    rng = np.random.default_rng(1)
+    n = 300
+    A = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    A[:, 5] *= 1e-3  # forces row interchanges
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    x, _, _ = bg.solve(A, b, precision=bg.FP64)
+    assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-12
+
+
+def test_mixed_refinement(efie):
+    X, op, E, Z, b = efie
+    xo = O.lu_solve(Z, b)
+    x, it, res = bg.solve(Z, b, precision=bg.MIXED, tol=1e-12)
+    assert res < 1e-12 and it >= 1
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-10
+
+
+def test_solve_job_matches_oracle(efie):
+    X, op, E, Z, b = efie
+    xo = O.lu_solve(Z, b)
+    x, it, res = bg.solve_job(op, X, bg.tangential_trace(E), precision=bg.FP64)
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-10
+    xm, itm, resm = bg.solve_job(op, X, bg.tangential_trace(E), precision=bg.MIXED, tol=1e-10)
+    assert np.linalg.norm(xm - xo) / np.linalg.norm(xo) < 1e-5
+
+
+def test_gmres_contract(efie):
+    # test/test_itsolver.jl:24-37
+    X, op, E, Z, b = efie
+    u = O.lu_solve(Z, b)
+    for rtol in (1e-6, 1e-8):
+        x, it, res = bg.gmres(Z, b, reltol=rtol, restart=200, maxiter=2000)
+        assert np.linalg.norm(Z @ x - b) / np.linalg.norm(b) < rtol
+        assert np.linalg.norm(x - u) / np.linalg.norm(x) < 100 * rtol
