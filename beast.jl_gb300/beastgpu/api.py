@@ -51,6 +51,25 @@ class Context:
         except Exception:
             pass
 
+    def prof_enable(self, on=True):
+        self.check(self.lib.beast_prof_enable(self.handle, 1 if on else 0))
+
+    def prof_read(self):
+        """{kind: (ms, launches, work)} for the records since prof_enable"""
+        out = {}
+        for k, name in enumerate(L.PROF_KINDS):
+            ms, nl, w = C.c_double(), C.c_int64(), C.c_double()
+            self.check(self.lib.beast_prof_read(self.handle, k, C.byref(ms), C.byref(nl),
+                                                C.byref(w)))
+            if nl.value:
+                out[name] = (ms.value, nl.value, w.value)
+        return out
+
+    def launches(self):
+        n = C.c_int64()
+        self.check(self.lib.beast_prof_launches(self.handle, C.byref(n)))
+        return n.value
+
     def set_workspace_limit(self, nbytes):
         self.check(self.lib.beast_ctx_set_workspace_limit(self.handle, int(nbytes)))
 

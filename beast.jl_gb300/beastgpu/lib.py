@@ -15,6 +15,8 @@ OK, ERR_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_NOCONV, ERR_SINGULAR, ERR_UNSUP
 FP64, MIXED = 0, 1
 C128, C64 = 0, 1
 HOST, DEVICE = 0, 1
+PROF_KINDS = ["geometry", "far", "near", "gather", "local", "rhs", "farfield", "lu_panel",
+              "lu_laswp", "lu_trsm", "lu_gemm", "trsv", "gemv", "vec", "convert"]
 
 
 class BeastError(RuntimeError):
@@ -41,7 +43,7 @@ EXPORTS = [
     "beast_mesh_free", "beast_space_upload", "beast_space_free", "beast_assemble",
     "beast_assemble_local", "beast_rhs_planewave", "beast_lu_factor", "beast_lu_solve",
     "beast_lu_free", "beast_solve_dense", "beast_gmres", "beast_farfield", "beast_solve_job",
-    "beast_version",
+    "beast_prof_enable", "beast_prof_read", "beast_prof_launches", "beast_version",
 ]
 
 
@@ -84,6 +86,10 @@ def load(build_if_needed=True):
     L.beast_farfield.argtypes = [vp, vp, vp, vp, i64, d, d, i, vp, i]
     L.beast_solve_job.argtypes = [vp, C.POINTER(OpDesc), C.POINTER(QsDesc), vp, i, vp, vp, d, d, i,
                                   d, vp, i, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    L.beast_prof_enable.argtypes = [vp, i]
+    L.beast_prof_read.argtypes = [vp, i, C.POINTER(C.c_double), C.POINTER(C.c_int64),
+                                  C.POINTER(C.c_double)]
+    L.beast_prof_launches.argtypes = [vp, C.POINTER(C.c_int64)]
     L.beast_version.restype = C.c_char_p
     for name in EXPORTS:
         if name != "beast_version":

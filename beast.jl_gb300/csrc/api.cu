@@ -12,6 +12,31 @@
 
 #include "internal.h"
 
+static cudaEvent_t ev_get(beast_ctx* c) {
+  if (!c->evpool.empty()) {
+    cudaEvent_t e = c->evpool.back();
+    c->evpool.pop_back();
+    return e;
+  }
+  cudaEvent_t e = nullptr;
+  cudaEventCreate(&e);
+  return e;
+}
+
+ProfScope::ProfScope(beast_ctx* c, int k, double w, int nlaunch) : ctx(c), kind(k), work(w) {
+  ctx->launches += nlaunch;
+  if (ctx->prof_on) {
+    a = ev_get(ctx);
+    cudaEventRecord(a, ctx->stream);
+  }
+}
+ProfScope::~ProfScope() {
+  if (!a) return;
+  cudaEvent_t b = ev_get(ctx);
+  cudaEventRecord(b, ctx->stream);
+  ctx->prof.push_back(ProfRec{kind, a, b, work});
+}
+
 int beast_fail(beast_ctx* ctx, int code, const std::string& msg) {
   if (ctx) ctx->err = msg;
   return code;
@@ -129,6 +154,44 @@ int beast_ctx_set_stream(beast_ctx* ctx, void* stream) {
 int beast_ctx_set_workspace_limit(beast_ctx* ctx, size_t bytes) {
   ARG_CHECK(ctx, ctx && bytes >= (1u << 20), "workspace limit below 1 MiB");
   ctx->ws_limit = bytes;
+  return BEAST_OK;
+}
+
+int beast_prof_enable(beast_ctx* ctx, int on) {
+  ARG_CHECK(ctx, ctx, "null context");
+  cudaStreamSynchronize(ctx->stream);
+  for (auto& r : ctx->prof) {
+    ctx->evpool.push_back(r.a);
+    ctx->evpool.push_back(r.b);
+  }
+  ctx->prof.clear();
+  ctx->prof_on = on != 0;
+  ctx->launches = 0;
+  return BEAST_OK;
+}
+
+int beast_prof_read(beast_ctx* ctx, int kind, double* ms, int64_t* launches, double* work) {
+  ARG_CHECK(ctx, ctx && kind >= 0 && kind < PK_COUNT, "bad profiler query");
+  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  double t = 0, w = 0;
+  int64_t nl = 0;
+  for (auto& r : ctx->prof) {
+    if (r.kind != kind) continue;
+    float e = 0;
+    cudaEventElapsedTime(&e, r.a, r.b);
+    t += e;
+    w += r.work;
+    ++nl;
+  }
+  if (ms) *ms = t;
+  if (launches) *launches = nl;
+  if (work) *work = w;
+  return BEAST_OK;
+}
+
+int beast_prof_launches(beast_ctx* ctx, int64_t* n) {
+  ARG_CHECK(ctx, ctx && n, "null argument");
+  *n = ctx->launches;
   return BEAST_OK;
 }
 
@@ -375,7 +438,15 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
     a.near_cap = (int)near_cap;
     a.near_count = counter;
     a.flag = ctx->d_flag;
-    cudaError_t e = launch_far(a, ro, ri, st);
+    cudaError_t e;
+    {
+      // algorithmic work: far pairs x flops per pair (EFIE 1200, MFIE 2040, n x K 29600,
+      // Helmholtz P0 228 -- per-unit figures from the reference integrands)
+      double fpp = op->kind == BEAST_MW_SL ? 1200.0 : op->kind == BEAST_MW_DL ? 2040.0
+                 : op->kind == BEAST_MW_NXDL ? 29600.0 : 228.0;
+      ProfScope ps(ctx, PK_FAR, fpp * (double)ts->ncells * (double)ch.cells.size());
+      e = launch_far(a, ro, ri, st);
+    }
     if (e == cudaErrorInvalidValue)
       return beast_fail(ctx, BEAST_ERR_UNSUPPORTED, "operator / space combination not supported");
     BEAST_CUDA_TRY(ctx, e);
@@ -384,6 +455,7 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
       BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(&nnear, counter, sizeof(int), cudaMemcpyDeviceToHost, st));
       BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(st));
       if (nnear > near_cap) return beast_fail(ctx, BEAST_ERR_ARG, "near-pair list overflow");
+      ProfScope ps(ctx, PK_NEAR, (double)nnear, nnear > 0);
       BEAST_CUDA_TRY(ctx, launch_near(a, nnear, ron, rin, st));
     }
     GatherArgs g;
@@ -403,7 +475,13 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
     g.cr = cr;
     g.ci = ci;
     g.accumulate = accumulate;
-    BEAST_CUDA_TRY(ctx, launch_gather(g, st));
+    {
+      // bytes: Zcell chunk read once + output block written (read too when accumulating)
+      double by = (double)ldc * nsb * ch.cells.size() * elem +
+                  (double)ts->nfuncs * (ch.n1 - ch.n0) * (z_c64 ? 8 : 16) * (accumulate ? 2 : 1);
+      ProfScope ps(ctx, PK_GATHER, by);
+      BEAST_CUDA_TRY(ctx, launch_gather(g, st));
+    }
     for (int c : ch.cells) ql[c] = -1;
   }
   int flag = 0;
@@ -498,7 +576,10 @@ int beast_rhs_planewave(beast_ctx* ctx, int kind, const beast_space* ts, const d
   if (pol) memcpy(p3, pol, sizeof(p3));
   double* db = b;
   if (b_loc != BEAST_DEVICE) BEAST_CUDA_TRY(ctx, cudaMallocAsync(&db, ts->nfuncs * 16, ctx->stream));
-  BEAST_CUDA_TRY(ctx, launch_rhs(kind, ts, dir, p3, gr, gi, ar, ai, r, db, ctx->stream));
+  {
+    ProfScope ps(ctx, PK_RHS, (double)ts->nfuncs);
+    BEAST_CUDA_TRY(ctx, launch_rhs(kind, ts, dir, p3, gr, gi, ar, ai, r, db, ctx->stream));
+  }
   if (b_loc != BEAST_DEVICE) {
     BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(b, db, ts->nfuncs * 16, cudaMemcpyDeviceToHost, ctx->stream));
     BEAST_CUDA_TRY(ctx, cudaFreeAsync(db, ctx->stream));
@@ -608,8 +689,10 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
   if (mixed) {
     if (a_dtype == BEAST_C64)
       BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(F, n * 8, A, lda * 8, n * 8, n, cudaMemcpyDeviceToDevice, st));
-    else
+    else {
+      ProfScope ps(ctx, PK_CONVERT, (double)n * n * 24);
       BEAST_CUDA_TRY(ctx, convert_c128_to_c64(n, n, (const double*)A, lda, (float*)F, n, st));
+    }
   } else {
     ARG_CHECK(ctx, a_dtype == BEAST_C128, "plain FP64 solve needs a c128 matrix");
     BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(F, n * 16, A, lda * 16, n * 16, n, cudaMemcpyDeviceToDevice, st));
@@ -638,7 +721,10 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
       rc = lu_solve_dev(ctx, n, F, n, BEAST_C128, lu->ipiv, xk, n, 1);
       if (rc) break;
       BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
-      BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, 0, xk, r, -1.0, 1.0, st));
+      {
+        ProfScope ps(ctx, PK_GEMV, (double)n * n * 16, 2);
+        BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, 0, xk, r, -1.0, 1.0, st));
+      }
       double rn = dev_norm(ctx, n, r, nrm);
       res_max = std::max(res_max, bn > 0 ? rn / bn : rn);
       continue;
@@ -655,7 +741,10 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
       BEAST_CUDA_TRY(ctx, convert_c64_to_c128(n, 1, d32, n, d, n, st));
       BEAST_CUDA_TRY(ctx, vec_axpy(n, 1.0, 0.0, d, xk, st));
       BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
-      BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, a_dtype == BEAST_C64, xk, r, -1.0, 1.0, st));
+      {
+        ProfScope ps(ctx, PK_GEMV, (double)n * n * (a_dtype == BEAST_C64 ? 8 : 16), 2);
+        BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, a_dtype == BEAST_C64, xk, r, -1.0, 1.0, st));
+      }
       ++it;
       double rn = dev_norm(ctx, n, r, nrm);
       rel = bn > 0 ? rn / bn : rn;
@@ -833,6 +922,7 @@ int beast_solve_job(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc
     if (pol) memcpy(p3, pol, sizeof(p3));
     TriRuleDev r;
     make_trirule(8, &r);
+    ProfScope ps(ctx, PK_RHS, (double)n);
     cudaError_t e = launch_rhs(exc_kind, space, dir, p3, egr, egi, 1.0, 0.0, r, b, st);
     if (e != cudaSuccess) rc = beast_fail(ctx, BEAST_ERR_CUDA, cudaGetErrorString(e));
   }

@@ -17,6 +17,17 @@
                         std::string(#expr) + ": " + cudaGetErrorString(e_));       \
   } while (0)
 
+// kernel classes timed by the optional profiler (beast_prof_*)
+enum {
+  PK_GEOM = 0, PK_FAR, PK_NEAR, PK_GATHER, PK_LOCAL, PK_RHS, PK_FARFIELD, PK_PANEL, PK_LASWP,
+  PK_TRSM, PK_GEMM, PK_TRSV, PK_GEMV, PK_VEC, PK_CONVERT, PK_COUNT
+};
+struct ProfRec {
+  int kind;
+  cudaEvent_t a, b;
+  double work;
+};
+
 struct beast_ctx {
   int device = 0;
   int num_sms = 0;
@@ -28,6 +39,21 @@ struct beast_ctx {
   void* ws = nullptr;
   size_t ws_size = 0;
   int* d_flag = nullptr;  // device error / status word
+  // profiler: CUDA events around instrumented launches on `stream`
+  bool prof_on = false;
+  std::vector<ProfRec> prof;
+  std::vector<cudaEvent_t> evpool;
+  int64_t launches = 0;   // kernels launched by this context (counted always)
+};
+
+// brackets one or more launches of class `kind`; `work` = algorithmic flops or bytes
+struct ProfScope {
+  beast_ctx* ctx;
+  int kind;
+  double work;
+  cudaEvent_t a = nullptr;
+  ProfScope(beast_ctx* c, int k, double w, int nlaunch = 1);
+  ~ProfScope();
 };
 
 struct beast_mesh {

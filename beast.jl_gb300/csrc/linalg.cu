@@ -494,16 +494,24 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
     int nblk = (int)std::min<int64_t>({(int64_t)ctx->num_sms * std::max(occ, 1), (M + 255) / 256, (int64_t)maxblk});
     nblk = std::max(nblk, 1);
     void* args[] = {&A, &lda, &n, &j0, &kb, &ipiv, &dinfo, &cval, &cidx, &gs};
-    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_panel<T>, nblk, 256, args, 0, st));
+    {
+      ProfScope ps(ctx, PK_PANEL, 8.0 * (double)M * kb * kb / 2);
+      BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_panel<T>, nblk, 256, args, 0, st));
+    }
     int64_t other = n - kb;
     if (other > 0) {
+      ProfScope ps(ctx, PK_LASWP, (double)other * kb * 2 * sizeof(T));
       k_laswp<T><<<(unsigned)((other + 255) / 256), 256, 0, st>>>(A, lda, n, j0, kb, ipiv);
     }
     int64_t rest = n - j0 - kb;
     if (rest > 0) {
       size_t smb = (size_t)kb * kb * sizeof(T);
-      k_trsm<T><<<(unsigned)((rest + 127) / 128), 128, smb, st>>>(A, lda, n, j0, kb);
+      {
+        ProfScope ps(ctx, PK_TRSM, 4.0 * (double)rest * kb * kb);
+        k_trsm<T><<<(unsigned)((rest + 127) / 128), 128, smb, st>>>(A, lda, n, j0, kb);
+      }
       dim3 g((unsigned)((rest + GT - 1) / GT), (unsigned)((rest + GT - 1) / GT));
+      ProfScope ps(ctx, PK_GEMM, 8.0 * (double)rest * rest * kb);
       k_gemm_sub<T, R><<<g, 256, 0, st>>>(A + (j0 + kb) + (j0 + kb) * lda, lda, A + (j0 + kb) + j0 * lda,
                                           lda, A + j0 + (j0 + kb) * lda, lda, rest, rest, kb);
     }
@@ -535,6 +543,8 @@ int lu_solve_t(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* pe
   for (int64_t r = 0; r < nrhs; ++r) {
     T* b = B + r * ldb;
     BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(tmp, b, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    // the two triangular solves read the factors once: n^2 elements
+    ProfScope ps(ctx, PK_TRSV, (double)n * n * sizeof(T), 1 + 4 * (int)((n + nb - 1) / nb));
     k_permute<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tmp, b, perm, n);
     for (int64_t k0 = 0; k0 < n; k0 += nb) {
       int kb = (int)std::min<int64_t>(nb, n - k0);

@@ -1,0 +1,318 @@
+"""Benchmark: EFIE solves/s on one GB300 (Galerkin assembly + excitation + dense solve).
+
+Workload (default): icosphere subdivided 5x (20480 triangles, 30720 RT unknowns), EFIE
+(Maxwell3D.singlelayer, k = 10), plane wave x-hat / z-hat polarisation, default quadrature
+strategy DoubleNumWiltonSauterQStrat(2,3,6,7,5,5,4,3), mixed precision (FP32 far pairs +
+FP64 near/singular pairs, c64 matrix, FP32 LU, FP64 iterative refinement to 1e-10).
+A step = one assemble + excitation + solve of that system.
+
+  value   steps/s with mesh and spaces resident on the device (timed with CUDA events)
+  e2e     the same through the C ABI from host buffers: mesh + assembly data uploaded and
+          the solution read back inside every step
+  roofline, gpu_launches from the library's event instrumentation over the timed steps
+  cpu_baseline  the CPU oracle (a restatement of BEAST's algorithm) on a bounded sample
+
+`--impl reference` times the reference's CPU algorithm (the oracle port; Julia is not
+available) on the host cores and prints the same line with "impl": "reference".
+Multi-GPU: replicas only (each rank solves its own copy; no collective on the data path).
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for p in (os.path.join(ROOT, "beast.jl_gb300"), os.path.join(ROOT, "oracle")):
+    if p not in sys.path:
+        sys.path.insert(0, p)
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--level", type=int, default=5)
+    ap.add_argument("--k", type=float, default=10.0)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64"])
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    return ap.parse_args()
+
+
+def workload(args):
+    import beastgpu as bg
+    m = bg.icosphere(args.level)
+    X = bg.raviartthomas(m)
+    op = bg.Maxwell3D.singlelayer(wavenumber=args.k)
+    E = bg.Maxwell3D.planewave(direction=(1, 0, 0), polarization=(0, 0, 1), wavenumber=args.k)
+    return m, X, op, E
+
+
+def config_dict(args, X, m):
+    return {"workload": f"EFIE k={args.k:g} on icosphere level {args.level} "
+                        f"({m.numcells()} triangles, {X.numfunctions()} RT unknowns), "
+                        f"{args.precision} precision, 1 plane-wave RHS",
+            "triangles": int(m.numcells()), "unknowns": int(X.numfunctions()),
+            "quadstrat": "DoubleNumWiltonSauterQStrat(2,3,6,7,5,5,4,3)",
+            "precision": args.precision, "refinement_tol": args.tol,
+            "l2": "inputs larger than L2 (matrix 7.5 GB c64 / 15 GB c128)",
+            "parallelism": f"replicas x{args.gpus}"}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            return json.load(fh), "measured"
+    except OSError:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region"""
+
+    def __init__(self, dev):
+        self.f = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        os.makedirs(os.path.dirname(self.f), exist_ok=True)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(dev), f"--query-gpu={q}",
+                                       "--format=csv,noheader,nounits", "-lms", "200"],
+                                      stdout=open(self.f, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.f):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": float(max(smax)) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(args, X, m, budget_s=20.0):
+    """oracle (BEAST's algorithm restated in C++) timed on a bounded sample on all host cores"""
+    import oracle as O
+    nthreads = os.cpu_count() or 1
+    g = 1j * args.k
+    op = O.make_op(O.MW_SL, g, -g, -1 / g)
+    qs = O.make_qs(O.QS_WILTON_SAUTER, 2, 3, 6, 7, 5, 5, 4, 3)
+    n = X.numfunctions()
+    rows = 8
+    t = 0.0
+    while True:  # grow the row sample until it takes a few seconds
+        t0 = time.perf_counter()
+        O.assemble(op, qs, X, X, row_lo=0, row_hi=rows, nthreads=nthreads)
+        t = time.perf_counter() - t0
+        if t > budget_s / 4 or rows >= n:
+            break
+        rows = min(n, rows * 4)
+    t_asm = t * n / rows
+    ns = 1536
+    rng = np.random.default_rng(0)
+    A = rng.normal(size=(ns, ns)) + 1j * rng.normal(size=(ns, ns))
+    b = rng.normal(size=ns) + 0j
+    t0 = time.perf_counter()
+    O.lu_solve(A, b, nthreads=nthreads)
+    t_lu = (time.perf_counter() - t0) * (n / ns) ** 3
+    total = t_asm + t_lu
+    return {"value": 1.0 / total, "unit": "solves/s", "cores": nthreads, "kind": "port",
+            "sample": f"oracle FP64: assembly of {rows}/{n} test rows ({t:.1f}s, scaled by "
+                      f"rows) + dense LU at n={ns} scaled by (n/{ns})^3; est. assembly "
+                      f"{t_asm:.0f}s + LU {t_lu:.0f}s per solve"}
+
+
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    import beastgpu as bg  # mesh/space construction only (host code)
+    m, X, op, E = workload(args)
+    vals = []
+    for _ in range(args.warmup):
+        pass
+    for _ in range(max(1, args.steps)):
+        cb = cpu_baseline(args, X, m, budget_s=8.0)
+        vals.append(cb["value"])
+    v = float(np.median(vals))
+    cb["value"] = v
+    out = {"metric": "solves/s", "value": v, "unit": "solves/s", "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 / v,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "c128", "data": "synthetic icosphere mesh", "impl": "reference",
+           "config": config_dict(args, X, m), "cpu_baseline": cb,
+           "e2e": {"value": v, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                   "d2h_bytes_per_step": 0}}
+    print(json.dumps(out))
+
+
+def main():
+    args = parse()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        return run_reference(args, rank, world)
+    import torch
+    import beastgpu as bg
+    from beastgpu import lib as L
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    dev = local
+    torch.cuda.set_device(dev)
+    m, X, op, E = workload(args)
+    n = X.numfunctions()
+    prec = L.MIXED if args.precision == "mixed" else L.FP64
+    ctx = bg.Context(dev)
+    stream = torch.cuda.current_stream()
+    ctx.check(ctx.lib.beast_ctx_set_stream(ctx.handle, C.c_void_p(stream.cuda_stream)))
+    lib = ctx.lib
+    sh = ctx.space_handle(X)
+    qs = bg.defaultquadstrat(op, X, X)
+    od, qd = bg.api._op_desc(op), bg.api._qs_desc(qs)
+    dt = L.C64 if prec == L.MIXED else L.C128
+    Z = torch.empty((n, n), dtype=torch.complex64 if dt == L.C64 else torch.complex128,
+                    device=f"cuda:{dev}")
+    b = torch.empty(n, dtype=torch.complex128, device=f"cuda:{dev}")
+    x = torch.empty(n, dtype=torch.complex128, device=f"cuda:{dev}")
+    d = np.array([1.0, 0, 0])
+    pol = np.array([0, 0, 1.0])
+    g = complex(E.gamma)
+    it, res = C.c_int(0), C.c_double(0)
+
+    def step():
+        ctx.check(lib.beast_assemble(ctx.handle, C.byref(od), C.byref(qd), sh, sh, prec,
+                                     Z.data_ptr(), n, dt, L.DEVICE, 0, 0, 1.0, 0.0, 0))
+        ctx.check(lib.beast_rhs_planewave(ctx.handle, 0, sh, d.ctypes.data, pol.ctypes.data,
+                                          g.real, g.imag, 1.0, 0.0, 8, b.data_ptr(), L.DEVICE))
+        ctx.check(lib.beast_solve_dense(ctx.handle, n, Z.data_ptr(), n, dt, prec, b.data_ptr(),
+                                        x.data_ptr(), 1, L.DEVICE, args.tol, 30, C.byref(it),
+                                        C.byref(res)))
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = Clocks(dev)
+    ctx.prof_enable(True)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clocks = clk.stop()
+    prof = ctx.prof_read()
+    launches = ctx.launches()
+    ctx.prof_enable(False)
+    if dist:
+        t = torch.tensor([ms], device=f"cuda:{dev}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        dist.barrier()
+    ms_step = ms / args.steps
+    value = world * 1000.0 / ms_step
+
+    # ---- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        ad = X.assemblydata()
+        verts = np.ascontiguousarray(m.vertices)
+        cells = np.ascontiguousarray(m.cells, dtype=np.int32)
+        xh = np.zeros(n, dtype=np.complex128)
+        h2d = verts.nbytes + cells.nbytes + ad.cells.nbytes + ad.dof.nbytes + ad.coeff.nbytes
+        d2h = xh.nbytes
+        c2 = bg.Context(dev)
+
+        def e2e_step():
+            mh, shh = C.c_void_p(), C.c_void_p()
+            c2.check(lib.beast_mesh_upload(c2.handle, verts.ctypes.data, verts.shape[0],
+                                           cells.ctypes.data, cells.shape[0], 0, C.byref(mh)))
+            c2.check(lib.beast_space_upload(c2.handle, mh, ad.kind, ad.cells.shape[0],
+                                            ad.cells.ctypes.data, ad.maxfn, ad.nshapes,
+                                            ad.dof.ctypes.data, ad.coeff.ctypes.data, n, 0,
+                                            C.byref(shh)))
+            c2.check(lib.beast_solve_job(c2.handle, C.byref(od), C.byref(qd), shh, 0,
+                                         d.ctypes.data, pol.ctypes.data, g.real, g.imag, prec,
+                                         args.tol, xh.ctypes.data, L.HOST, C.byref(it),
+                                         C.byref(res)))
+            lib.beast_space_free(shh)
+            lib.beast_mesh_free(mh)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / args.steps
+        if dist:
+            t = torch.tensor([te], device=f"cuda:{dev}")
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            te = float(t.item())
+        e2e = {"value": world / te, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+        c2.close()
+    if rank != 0:
+        return
+    # ---- roofline of the dominant kernel class
+    pk, src = peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1][0])
+    name, (kms, nl, work) = dom
+    memory_bound = name in ("gather", "gemv", "trsv", "convert", "lu_laswp")
+    if memory_bound:
+        achieved = work / (kms * 1e-3) / 1e9
+        peak, unit, bound = pk["hbm_gbs"], "GB/s", "hbm"
+    else:
+        achieved = work / (kms * 1e-3) / 1e12
+        peak, unit, bound = pk.get("bf16_tflops_sustained", pk["bf16_tflops"]), "TFLOP/s", "tensor"
+    roof = {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak, "unit": unit,
+            "frac": achieved / peak, "peak_source": src, "traffic": None,
+            "launches": nl, "avg_launch_ms": kms / nl}
+    breakdown = {k: {"ms": v[0], "launches": v[1], "share": v[0] / sum(w[0] for w in prof.values())}
+                 for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    out = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": world,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": "c64+f64" if prec == L.MIXED else "c128", "data": "synthetic icosphere mesh",
+           "config": config_dict(args, X, m), "refinement": {"iters": it.value,
+                                                            "rel_residual": res.value},
+           "roofline": roof, "kernel_breakdown": breakdown, "gpu_launches": int(launches),
+           "clocks": clocks, "e2e": e2e}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, X, m)
+    print(json.dumps(out))
+
+
+if __name__ == "__main__":
+    main()

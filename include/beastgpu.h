@@ -201,6 +201,18 @@ int beast_solve_job(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc
                     double exc_gamma_re, double exc_gamma_im, int precision, double tol,
                     double* x, int x_loc, int* iters, double* resid);
 
+/* ---- instrumentation (no reference counterpart: the reference has no device) ---------
+ * When enabled, every instrumented kernel launch on the context stream is bracketed by
+ * CUDA events.  Kinds: 0 geometry, 1 far pairs, 2 near pairs, 3 gather/scatter, 4 local
+ * operators, 5 excitation, 6 far field, 7 LU panel, 8 row swaps, 9 TRSM, 10 trailing GEMM,
+ * 11 triangular solves, 12 FP64 matvec, 13 vector ops, 14 precision conversion.
+ * beast_prof_read sums event time (ms), bracketed launches and algorithmic work (flops for
+ * compute kinds, bytes for memory kinds) over the records since the last enable. */
+int beast_prof_enable(beast_ctx* ctx, int on);
+int beast_prof_read(beast_ctx* ctx, int kind, double* ms, int64_t* launches, double* work);
+/* kernels launched by this context since the last beast_prof_enable (counted always) */
+int beast_prof_launches(beast_ctx* ctx, int64_t* n);
+
 /* library version string */
 const char* beast_version(void);
 
