@@ -274,13 +274,15 @@ DEV void store_c(void* z, int64_t idx, C2<R> v, int c64) {
     reinterpret_cast<double2*>(z)[idx] = make_double2((double)v.re, (double)v.im);
 }
 
-// shared trial-cell record: sigma_j (9), centroid (3), normal (3), area, then the inner rule
-// points eta_b (3) + weight per point, all relative to the trial centroid
-constexpr int QREC_HDR = 16;
+// shared trial-cell record (in the arithmetic type R): sigma_j = s_j - c (9), centroid hi
+// (3) and lo (3) parts, unit normal (3), area, near-test radius (radius + threshold
+// distance); then per inner rule point eta_b = y_b - c (3) and weight
+constexpr int QREC_HDR = 20;
 
 template <int OPK, int TK, int BK, typename R, int C64>
 __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
-  extern __shared__ double sm[];
+  extern __shared__ unsigned char smraw[];
+  R* sm = reinterpret_cast<R*>(smraw);
   const int ni = P.ri.n;
   const int rec = QREC_HDR + 4 * ni;
   const int q0 = blockIdx.y * FAR_QT;
@@ -288,56 +290,59 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
   // ---- stage trial cells
   for (int k = threadIdx.x; k < nqt * (1 + ni); k += blockDim.x) {
     int qi = k / (1 + ni), b = k % (1 + ni);
-    const double* g = P.bgeo + (int64_t)P.qcells[q0 + qi] * GEO_STRIDE;
-    double* r = sm + qi * rec;
-    V3<double> c = mk(g[9], g[10], g[11]);
+    const int qc = P.qcells[q0 + qi];
+    const double* g = P.bgeo + (int64_t)qc * GEO_STRIDE;
+    R* r = sm + qi * rec;
+    const double cx = g[9], cy = g[10], cz = g[11];
     if (b == 0) {
       for (int j = 0; j < 3; ++j) {
-        r[3 * j] = g[3 * j] - c.x;
-        r[3 * j + 1] = g[3 * j + 1] - c.y;
-        r[3 * j + 2] = g[3 * j + 2] - c.z;
+        r[3 * j] = (R)(g[3 * j] - cx);
+        r[3 * j + 1] = (R)(g[3 * j + 1] - cy);
+        r[3 * j + 2] = (R)(g[3 * j + 2] - cz);
       }
-      r[9] = c.x; r[10] = c.y; r[11] = c.z;
-      r[12] = g[12]; r[13] = g[13]; r[14] = g[14];
-      r[15] = g[15];
+      r[9] = (R)cx; r[10] = (R)cy; r[11] = (R)cz;
+      r[12] = (R)(cx - (double)(R)cx); r[13] = (R)(cy - (double)(R)cy); r[14] = (R)(cz - (double)(R)cz);
+      r[15] = (R)g[12]; r[16] = (R)g[13]; r[17] = (R)g[14];
+      r[18] = (R)g[15];
+      double thr2 = near_threshold2(P.qs_kind, P.k2, g[15]);
+      r[19] = (R)((double)P.bgeof[4 * qc + 3] + sqrt(fmax(thr2, 0.0)));
     } else {
       int bb = b - 1;
       double u = P.ri.u[bb], v = P.ri.v[bb], w = 1.0 - u - v;
-      // eta = u sigma0 + v sigma1 + w sigma2  (sigma relative to the centroid)
-      double ex = u * (g[0] - c.x) + v * (g[3] - c.x) + w * (g[6] - c.x);
-      double ey = u * (g[1] - c.y) + v * (g[4] - c.y) + w * (g[7] - c.y);
-      double ez = u * (g[2] - c.z) + v * (g[5] - c.z) + w * (g[8] - c.z);
-      double* pt = r + QREC_HDR + 4 * bb;
-      pt[0] = ex; pt[1] = ey; pt[2] = ez; pt[3] = P.ri.w[bb];
+      R* pt = r + QREC_HDR + 4 * bb;
+      pt[0] = (R)(u * (g[0] - cx) + v * (g[3] - cx) + w * (g[6] - cx));
+      pt[1] = (R)(u * (g[1] - cy) + v * (g[4] - cy) + w * (g[7] - cy));
+      pt[2] = (R)(u * (g[2] - cz) + v * (g[5] - cz) + w * (g[8] - cz));
+      pt[3] = (R)P.ri.w[bb];
     }
   }
   __syncthreads();
   const int64_t p = blockIdx.x * (int64_t)FAR_THREADS + threadIdx.x;
   if (p >= P.np) return;
   const double* tg = P.tgeo + p * GEO_STRIDE;
-  const V3<double> cp = mk(tg[9], tg[10], tg[11]);
-  V3<double> tau[3];
-  for (int i = 0; i < 3; ++i) tau[i] = mk(tg[3 * i] - cp.x, tg[3 * i + 1] - cp.y, tg[3 * i + 2] - cp.z);
-  const V3<double> np_ = mk(tg[12], tg[13], tg[14]);
+  const double cpx = tg[9], cpy = tg[10], cpz = tg[11];
+  const V3<R> chp = mk((R)cpx, (R)cpy, (R)cpz);
+  const V3<R> clp = mk((R)(cpx - (double)(R)cpx), (R)(cpy - (double)(R)cpy), (R)(cpz - (double)(R)cpz));
+  V3<R> tau[3];
+  for (int i = 0; i < 3; ++i)
+    tau[i] = mk((R)(tg[3 * i] - cpx), (R)(tg[3 * i + 1] - cpy), (R)(tg[3 * i + 2] - cpz));
+  const V3<R> nn = mk((R)tg[12], (R)tg[13], (R)tg[14]);
   const double Ap = tg[15];
-  const float4 tf = reinterpret_cast<const float4*>(P.tgeof)[p];
+  const R radp = (R)P.tgeof[4 * p + 3];
   const R gr = (R)P.op.gr, gi = (R)P.op.gi;
   const int nst = (TK == BEAST_P0) ? 1 : 3, nsb = (BK == BEAST_P0) ? 1 : 3;
   const int no = P.ro.n;
 
   for (int qi = 0; qi < nqt; ++qi) {
-    const double* rq = sm + qi * rec;
+    const R* rq = sm + qi * rec;
     const int ql = q0 + qi;
-    const V3<double> cq = mk(rq[9], rq[10], rq[11]);
-    const double Aq = rq[15];
-    // ---- near test (FP32 candidate filter, exact FP64 classification of candidates)
+    // d = c_p - c_q from hi/lo parts
+    const V3<R> d = mk((chp.x - rq[9]) + (clp.x - rq[12]), (chp.y - rq[10]) + (clp.y - rq[13]),
+                       (chp.z - rq[11]) + (clp.z - rq[14]));
+    // ---- near test (candidate filter on centroid distance, exact FP64 classification)
     if (P.qs_kind != BEAST_QS_DOUBLENUM) {
-      const float4 bf = reinterpret_cast<const float4*>(P.bgeof)[P.qcells[ql]];
-      float dx = tf.x - bf.x, dy = tf.y - bf.y, dz = tf.z - bf.z;
-      float d2f = dx * dx + dy * dy + dz * dz;
-      double thr2 = near_threshold2(P.qs_kind, P.k2, Aq);
-      float lim = tf.w + bf.w + (float)sqrt(fmax(thr2, 0.0));
-      if (d2f <= lim * lim * 1.0001f + 1e-30f) {
+      const R lim = radp + rq[19];
+      if (dot(d, d) <= lim * lim * (R)1.0001 + (R)1e-30) {
         Geo t = load_geo(tg);
         Geo s = load_geo(P.bgeo + (int64_t)P.qcells[ql] * GEO_STRIDE);
         int cls = classify_exact(t, s, P.qs_kind, P.k2);
@@ -354,20 +359,19 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
         }
       }
     }
-    const V3<R> d = mk((R)(cp.x - cq.x), (R)(cp.y - cq.y), (R)(cp.z - cq.z));
-    const double* pts = rq + QREC_HDR;
+    const R Aq = rq[18];
+    const R* pts = rq + QREC_HDR;
 
     if (OPK == BEAST_MW_SL || OPK == BEAST_MW_DL || OPK == BEAST_MW_NXDL) {
       // ---- RT x RT with moment reduction
       C2<R> M0{0, 0}, M1{0, 0}, M2{0, 0}, M3{0, 0};  // scalar moments
       CV<R> V1, V2, V3_, V4, V5, V6;                   // vector moments
       cv_zero(V1); cv_zero(V2); cv_zero(V3_); cv_zero(V4); cv_zero(V5); cv_zero(V6);
-      const V3<R> nn = mk((R)np_.x, (R)np_.y, (R)np_.z);
       for (int a = 0; a < no; ++a) {
-        const double ua = P.ro.u[a], va = P.ro.v[a], wa3 = 1.0 - ua - va;
-        const V3<R> xi = mk((R)(ua * tau[0].x + va * tau[1].x + wa3 * tau[2].x),
-                            (R)(ua * tau[0].y + va * tau[1].y + wa3 * tau[2].y),
-                            (R)(ua * tau[0].z + va * tau[1].z + wa3 * tau[2].z));
+        const R ua = (R)P.ro.u[a], va = (R)P.ro.v[a], wa3 = (R)1 - ua - va;
+        const V3<R> xi = mk(ua * tau[0].x + va * tau[1].x + wa3 * tau[2].x,
+                            ua * tau[0].y + va * tau[1].y + wa3 * tau[2].y,
+                            ua * tau[0].z + va * tau[1].z + wa3 * tau[2].z);
         const R wa = (R)P.ro.w[a];
         const V3<R> dx = d + xi;
         // inner sums over trial points: U0 = sum w K, U1 = sum w K eta,
@@ -376,9 +380,9 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
         CV<R> U1, U2;
         cv_zero(U1); cv_zero(U2);
         for (int b = 0; b < ni; ++b) {
-          const double* pb = pts + 4 * b;
-          const V3<R> eta = mk((R)pb[0], (R)pb[1], (R)pb[2]);
-          const R wb = (R)pb[3];
+          const R* pb = pts + 4 * b;
+          const V3<R> eta = mk(pb[0], pb[1], pb[2]);
+          const R wb = pb[3];
           const V3<R> r = dx - eta;
           const R R2 = dot(r, r);
           const R iR = rsq<R>(R2);
@@ -457,9 +461,9 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
       }
       // ---- finalize the 3x3 block (x Ap Aq from the rule weights, / (4 Ap Aq) from the shapes)
       for (int i = 0; i < 3; ++i) {
-        const V3<R> ti = mk((R)tau[i].x, (R)tau[i].y, (R)tau[i].z);
+        const V3<R> ti = tau[i];
         for (int j = 0; j < 3; ++j) {
-          const V3<R> sj = mk((R)rq[3 * j], (R)rq[3 * j + 1], (R)rq[3 * j + 2]);
+          const V3<R> sj = mk(rq[3 * j], rq[3 * j + 1], rq[3 * j + 2]);
           C2<R> z;
           if (OPK == BEAST_MW_SL) {
             // alpha/4 (Mxe - Mx.s - t.Me + (t.s) M0) + beta M0
@@ -491,20 +495,19 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
       // ---- Helmholtz kernels on P0/P1: per point pair with shape products
       C2<R> acc[9];
       for (int k = 0; k < 9; ++k) acc[k] = C2<R>{0, 0};
-      const V3<R> nq = mk((R)rq[12], (R)rq[13], (R)rq[14]);
-      const V3<R> nn = mk((R)np_.x, (R)np_.y, (R)np_.z);
+      const V3<R> nq = mk(rq[15], rq[16], rq[17]);
       for (int a = 0; a < no; ++a) {
-        const double ua = P.ro.u[a], va = P.ro.v[a], wa3 = 1.0 - ua - va;
-        const V3<R> xi = mk((R)(ua * tau[0].x + va * tau[1].x + wa3 * tau[2].x),
-                            (R)(ua * tau[0].y + va * tau[1].y + wa3 * tau[2].y),
-                            (R)(ua * tau[0].z + va * tau[1].z + wa3 * tau[2].z));
-        const R lt[3] = {(R)ua, (R)va, (R)wa3};
+        const R ua = (R)P.ro.u[a], va = (R)P.ro.v[a], wa3 = (R)1 - ua - va;
+        const V3<R> xi = mk(ua * tau[0].x + va * tau[1].x + wa3 * tau[2].x,
+                            ua * tau[0].y + va * tau[1].y + wa3 * tau[2].y,
+                            ua * tau[0].z + va * tau[1].z + wa3 * tau[2].z);
+        const R lt[3] = {ua, va, wa3};
         const R wa = (R)P.ro.w[a];
         const V3<R> dx = d + xi;
         for (int b = 0; b < ni; ++b) {
-          const double* pb = pts + 4 * b;
-          const V3<R> eta = mk((R)pb[0], (R)pb[1], (R)pb[2]);
-          const R wb = (R)pb[3] * wa;
+          const R* pb = pts + 4 * b;
+          const V3<R> eta = mk(pb[0], pb[1], pb[2]);
+          const R wb = pb[3] * wa;
           const V3<R> r = dx - eta;
           const R R2 = dot(r, r);
           const R iR = rsq<R>(R2);
@@ -532,7 +535,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
             }
         }
       }
-      const R ApAq = (R)(Ap * Aq);
+      const R ApAq = (R)Ap * Aq;
       for (int i = 0; i < nst; ++i)
         for (int j = 0; j < nsb; ++j)
           store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * p + i,
@@ -1232,7 +1235,7 @@ cudaError_t launch_geometry(const beast_space* s, cudaStream_t st) {
 template <int OPK, int TK, int BK, typename R, int C64>
 static cudaError_t far_t(const FarParams& P, cudaStream_t st) {
   dim3 grid((unsigned)((P.np + FAR_THREADS - 1) / FAR_THREADS), (unsigned)((P.nq + FAR_QT - 1) / FAR_QT));
-  size_t sm = (size_t)FAR_QT * (QREC_HDR + 4 * P.ri.n) * sizeof(double);
+  size_t sm = (size_t)FAR_QT * (QREC_HDR + 4 * P.ri.n) * sizeof(R);
   k_far<OPK, TK, BK, R, C64><<<grid, FAR_THREADS, sm, st>>>(P);
   return cudaGetLastError();
 }

@@ -18,6 +18,10 @@
 
 #include "internal.h"
 
+bool tc_gemm_supported(const void* A, int64_t lda, int K);
+int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t n_total, int64_t rowA, int64_t colA,
+                int64_t colB, int64_t M, int64_t N, int K, float* work);
+
 namespace {
 
 template <typename R>
@@ -85,26 +89,45 @@ __device__ __forceinline__ double cabs1(T z) {
 }
 
 // ---- panel factorisation ---------------------------------------------------------------
+// One CTA per SM keeps its slice of the panel rows in shared memory for the whole panel.
+// Per column: local pivot candidate -> publish (value, index, candidate row, and row j if
+// owned) into a double-buffered exchange area -> one grid barrier -> every CTA picks the
+// same pivot (max |re|+|im|, first index on ties), the owners of rows j and p swap them
+// in shared memory, and every CTA scales / rank-1 updates its own rows.
 template <typename T>
-__global__ void k_panel(T* A, int64_t lda, int64_t n, int64_t j0, int nb, int* ipiv, int* info,
-                        double* cand_val, int* cand_idx, GridSync gs) {
-  const unsigned nblk = gridDim.x;
-  const int64_t M = n - j0;
-  const int64_t per = (M + nblk - 1) / nblk;
-  const int64_t r0 = j0 + blockIdx.x * per, r1 = min(n, r0 + per);
+__global__ void __launch_bounds__(256) k_panel(T* A, int64_t lda, int64_t n, int64_t j0, int nb,
+                                               int rows_per, int* ipiv, int* info, double* cand_val,
+                                               int* cand_idx, T* cand_row, T* rowj, GridSync gs) {
+  extern __shared__ unsigned char smraw[];
+  const int ld = nb + 1;  // padded row stride (bank spread)
+  T* S = reinterpret_cast<T*>(smraw);              // rows_per x ld
+  T* U = S + (size_t)rows_per * ld;                // pivot row (nb)
   __shared__ double sval[256];
   __shared__ int sidx[256];
-  __shared__ int piv_s;
+  __shared__ int s_p;
+  __shared__ int s_w[256];
+  const unsigned G = gridDim.x;
+  const int64_t r0 = j0 + (int64_t)blockIdx.x * rows_per;
+  const int nloc = (int)(n - r0 < (int64_t)rows_per ? (n - r0 > 0 ? n - r0 : 0) : (int64_t)rows_per);
+  // load own rows of the panel
+  for (int e = threadIdx.x; e < nloc * nb; e += blockDim.x) {
+    int i = e % nloc, k = e / nloc;
+    S[i * ld + k] = A[(r0 + i) + (j0 + k) * lda];
+  }
+  __syncthreads();
   for (int jj = 0; jj < nb; ++jj) {
     const int64_t j = j0 + jj;
-    // 1. local pivot candidate over own rows >= j
+    const int buf = jj & 1;
+    // 1. local candidate over own rows with global index >= j
     double bv = -1.0;
     int bi = 0x7fffffff;
-    for (int64_t i = max(r0, j) + threadIdx.x; i < r1; i += blockDim.x) {
-      double v = cabs1(__ldcg(A + i + j * lda));
-      if (v > bv || (v == bv && i < bi)) {
+    for (int i = threadIdx.x; i < nloc; i += blockDim.x) {
+      if (r0 + i < j) continue;
+      T a = S[i * ld + jj];
+      double v = fabs((double)a.x) + fabs((double)a.y);
+      if (v > bv) {
         bv = v;
-        bi = (int)i;
+        bi = i;
       }
     }
     sval[threadIdx.x] = bv;
@@ -121,67 +144,124 @@ __global__ void k_panel(T* A, int64_t lda, int64_t n, int64_t j0, int nb, int* i
       }
       __syncthreads();
     }
+    const int li = sidx[0];
     if (threadIdx.x == 0) {
-      cand_val[blockIdx.x] = sval[0];
-      cand_idx[blockIdx.x] = sidx[0];
+      cand_val[buf * G + blockIdx.x] = sval[0];
+      cand_idx[buf * G + blockIdx.x] = sval[0] >= 0.0 ? (int)(r0 + li) : 0x7fffffff;
     }
-    if (!grid_barrier(gs, nblk)) return;
-    // 2. global pivot (every CTA computes the same answer); CTA 0 swaps the panel rows
-    if (threadIdx.x == 0) {
+    if (sval[0] >= 0.0)
+      for (int k = threadIdx.x; k < nb; k += blockDim.x)
+        cand_row[((size_t)buf * G + blockIdx.x) * nb + k] = S[li * ld + k];
+    const bool own_j = (j >= r0 && j < r0 + nloc);
+    if (own_j)
+      for (int k = threadIdx.x; k < nb; k += blockDim.x) rowj[(size_t)buf * nb + k] = S[(j - r0) * ld + k];
+    if (!grid_barrier(gs, G)) return;
+    // 2. global pivot: the G candidates are read in parallel and reduced in shared memory
+    {
       double v = -1.0;
-      int p = 0x7fffffff;
-      for (unsigned b = 0; b < nblk; ++b) {
-        double cv = ((volatile double*)cand_val)[b];
-        int ci = ((volatile int*)cand_idx)[b];
+      int p = 0x7fffffff, w = 0;
+      for (unsigned b = threadIdx.x; b < G; b += blockDim.x) {
+        double cv = __ldcg(cand_val + buf * G + b);
+        int ci = __ldcg(cand_idx + buf * G + b);
         if (cv > v || (cv == v && ci < p)) {
           v = cv;
           p = ci;
+          w = (int)b;
         }
       }
-      if (v <= 0.0) p = (int)j;
-      piv_s = p;
-      if (blockIdx.x == 0) {
-        ipiv[j] = p;
-        if (v <= 0.0 && *info == 0) *info = (int)j + 1;
+      __syncthreads();  // everyone has read li / sidx of step 1
+      sval[threadIdx.x] = v;
+      sidx[threadIdx.x] = p;
+      s_w[threadIdx.x] = w;
+      __syncthreads();
+      for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if (threadIdx.x < o) {
+          double v2 = sval[threadIdx.x + o];
+          int i2 = sidx[threadIdx.x + o];
+          if (v2 > sval[threadIdx.x] || (v2 == sval[threadIdx.x] && i2 < sidx[threadIdx.x])) {
+            sval[threadIdx.x] = v2;
+            sidx[threadIdx.x] = i2;
+            s_w[threadIdx.x] = s_w[threadIdx.x + o];
+          }
+        }
+        __syncthreads();
+      }
+    }
+    if (threadIdx.x == 0) {
+      double v = sval[0];
+      int p = sidx[0], w = s_w[0];
+      if (v <= 0.0) {  // exactly singular column: record, no interchange
+        p = (int)j;
+        w = -1;
+        if (blockIdx.x == 0 && *info == 0) *info = (int)j + 1;
+      }
+      if (blockIdx.x == 0) ipiv[j] = p;
+      s_p = p;
+      sidx[0] = w;
+    }
+    __syncthreads();
+    const int64_t p = s_p;
+    const int wblk = sidx[0];
+    if (wblk < 0) {
+      for (int k = threadIdx.x; k < nb; k += blockDim.x) U[k] = own_j ? S[(j - r0) * ld + k] : __ldcg(rowj + (size_t)buf * nb + k);
+    } else {
+      for (int k = threadIdx.x; k < nb; k += blockDim.x)
+        U[k] = __ldcg(cand_row + ((size_t)buf * G + wblk) * nb + k);
+    }
+    __syncthreads();
+    // the owners exchange rows j and p (row p receives row j's content)
+    if (p != j) {
+      if (p >= r0 && p < r0 + nloc)
+        for (int k = threadIdx.x; k < nb; k += blockDim.x) S[(p - r0) * ld + k] = __ldcg(rowj + (size_t)buf * nb + k);
+      __syncthreads();
+      if (own_j)
+        for (int k = threadIdx.x; k < nb; k += blockDim.x) S[(j - r0) * ld + k] = U[k];
+    }
+    __syncthreads();
+    // 3. scale and rank-1 update of own rows below j
+    T piv = U[jj];
+    double den = (double)piv.x * piv.x + (double)piv.y * piv.y;
+    if (den != 0.0) {
+      typedef decltype(piv.x) RT;
+      const RT ir = (RT)(piv.x / den), ii = (RT)(-piv.y / den);
+      const int ncol = nb - jj - 1;
+      const int64_t ibeg = (j + 1 - r0) > 0 ? (j + 1 - r0) : 0;
+      for (int64_t i = ibeg + threadIdx.x; i < nloc; i += blockDim.x) {  // multipliers
+        T a = S[i * ld + jj];
+        T l;
+        l.x = a.x * ir - a.y * ii;
+        l.y = a.x * ii + a.y * ir;
+        S[i * ld + jj] = l;
+      }
+      __syncthreads();
+      for (int64_t e = threadIdx.x; e < (nloc - ibeg) * (int64_t)ncol; e += blockDim.x) {
+        int i = (int)(ibeg + e / ncol);
+        int k = jj + 1 + (int)(e % ncol);
+        T l = S[i * ld + jj];
+        T u = U[k];
+        T c = S[i * ld + k];
+        c.x -= l.x * u.x - l.y * u.y;
+        c.y -= l.x * u.y + l.y * u.x;
+        S[i * ld + k] = c;
       }
     }
     __syncthreads();
-    const int64_t p = piv_s;
-    if (blockIdx.x == 0 && p != j) {
-      for (int k = threadIdx.x; k < nb; k += blockDim.x) {
-        T a = __ldcg(A + j + (j0 + k) * lda);
-        A[j + (j0 + k) * lda] = __ldcg(A + p + (j0 + k) * lda);
-        A[p + (j0 + k) * lda] = a;
-      }
-    }
-    if (!grid_barrier(gs, nblk)) return;
-    // 3. scale column j below the diagonal and rank-1 update of the panel (own rows)
-    T piv = __ldcg(A + j + j * lda);
-    double den = (double)piv.x * piv.x + (double)piv.y * piv.y;
-    if (den == 0.0) continue;
-    double ir = piv.x / den, ii = -piv.y / den;
-    for (int64_t i = max(r0, j + 1) + threadIdx.x; i < r1; i += blockDim.x) {
-      T a = __ldcg(A + i + j * lda);
-      double lr = a.x * ir - a.y * ii, li = a.x * ii + a.y * ir;
-      A[i + j * lda] = cmk<T>(lr, li);
-      for (int k = jj + 1; k < nb; ++k) {
-        T u = __ldcg(A + j + (j0 + k) * lda);
-        T c = __ldcg(A + i + (j0 + k) * lda);
-        A[i + (j0 + k) * lda] = cmk<T>(c.x - (lr * u.x - li * u.y), c.y - (lr * u.y + li * u.x));
-      }
-    }
+  }
+  // write back
+  for (int e = threadIdx.x; e < nloc * nb; e += blockDim.x) {
+    int i = e % nloc, k = e / nloc;
+    A[(r0 + i) + (j0 + k) * lda] = S[i * ld + k];
   }
 }
 
-// ---- row interchanges on columns outside the panel --------------------------------------
+// ---- row interchanges ipiv[p0, p1) applied (in order) to columns [c0, c1) ----------------
 template <typename T>
-__global__ void k_laswp(T* A, int64_t lda, int64_t ncols_total, int64_t j0, int nb, const int* ipiv) {
-  int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  // columns [0, j0) and [j0+nb, n)
-  int64_t col = c < j0 ? c : c + nb;
-  if (col >= ncols_total) return;
-  for (int k = 0; k < nb; ++k) {
-    int64_t r = j0 + k, p = ipiv[j0 + k];
+__global__ void k_laswp(T* A, int64_t lda, int64_t c0, int64_t c1, int64_t p0, int64_t p1,
+                        const int* ipiv) {
+  int64_t col = c0 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (col >= c1) return;
+  for (int64_t r = p0; r < p1; ++r) {
+    int64_t p = ipiv[r];
     if (p != r) {
       T a = A[r + col * lda];
       A[r + col * lda] = A[p + col * lda];
@@ -190,26 +270,41 @@ __global__ void k_laswp(T* A, int64_t lda, int64_t ncols_total, int64_t j0, int 
   }
 }
 
-// ---- U12 = L11^{-1} A12 (unit lower), one thread per column -----------------------------
+// ---- U12 = L11^{-1} A12 (unit lower): a CTA solves 64 columns held in shared memory ---
+// L11 = A[j0:j0+nb, j0:j0+nb], right-hand sides = columns [c0, c1) of rows j0:j0+nb
 template <typename T>
-__global__ void k_trsm(T* A, int64_t lda, int64_t n, int64_t j0, int nb) {
+__global__ void k_trsm(T* A, int64_t lda, int64_t j0, int nb, int64_t c0g, int64_t c1) {
   extern __shared__ unsigned char smraw[];
-  T* L = reinterpret_cast<T*>(smraw);  // nb x nb
+  T* L = reinterpret_cast<T*>(smraw);       // nb x nb (column-major)
+  T* B = L + nb * nb;                        // nb rows x 64 columns, column stride nb + 1
+  const int ldb = nb + 1;
+  const int64_t c0 = c0g + (int64_t)blockIdx.x * 64;
+  const int ncol = (int)(c1 - c0 < 64 ? c1 - c0 : 64);
   for (int k = threadIdx.x; k < nb * nb; k += blockDim.x) {
     int r = k % nb, c = k / nb;
     L[k] = A[(j0 + r) + (j0 + c) * lda];
   }
+  for (int e = threadIdx.x; e < nb * ncol; e += blockDim.x) {
+    int r = e % nb, c = e / nb;
+    B[c * ldb + r] = A[(j0 + r) + (c0 + c) * lda];
+  }
   __syncthreads();
-  int64_t col = j0 + nb + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (col >= n) return;
-  T* b = A + j0 + col * lda;
-  for (int k = 0; k < nb; ++k) {
-    T bk = b[k];
-    for (int i = k + 1; i < nb; ++i) {
-      T l = L[i + k * nb];
-      T bi = b[i];
-      b[i] = cmk<T>(bi.x - (l.x * bk.x - l.y * bk.y), bi.y - (l.x * bk.y + l.y * bk.x));
+  const int c = threadIdx.x;
+  if (c < ncol) {
+    T* b = B + c * ldb;
+    for (int k = 0; k < nb; ++k) {
+      T bk = b[k];
+      for (int i = k + 1; i < nb; ++i) {
+        T l = L[i + k * nb];
+        T bi = b[i];
+        b[i] = cmk<T>(bi.x - (l.x * bk.x - l.y * bk.y), bi.y - (l.x * bk.y + l.y * bk.x));
+      }
     }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nb * ncol; e += blockDim.x) {
+    int r = e % nb, cc = e / nb;
+    A[(j0 + r) + (c0 + cc) * lda] = B[cc * ldb + r];
   }
 }
 
@@ -278,7 +373,13 @@ __global__ void __launch_bounds__(256) k_gemm_sub(T* C, int64_t ldc, const T* Am
 // lower=0: upper, backward
 template <typename T>
 __global__ void k_trsv_block(const T* A, int64_t lda, T* b, int64_t k0, int kb, int lower) {
+  extern __shared__ unsigned char smraw[];
+  T* D = reinterpret_cast<T*>(smraw);  // kb x kb diagonal block, column-major
   __shared__ double xr[128], xi[128];
+  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+    int r = e % kb, c = e / kb;
+    D[e] = A[(k0 + r) + (k0 + c) * lda];
+  }
   for (int i = threadIdx.x; i < kb; i += blockDim.x) {
     xr[i] = b[k0 + i].x;
     xi[i] = b[k0 + i].y;
@@ -288,7 +389,7 @@ __global__ void k_trsv_block(const T* A, int64_t lda, T* b, int64_t k0, int kb, 
     for (int k = 0; k < kb; ++k) {
       double vr = xr[k], vi = xi[k];
       for (int i = k + 1 + threadIdx.x; i < kb; i += blockDim.x) {
-        T l = A[(k0 + i) + (k0 + k) * lda];
+        T l = D[i + k * kb];
         xr[i] -= l.x * vr - l.y * vi;
         xi[i] -= l.x * vi + l.y * vr;
       }
@@ -297,7 +398,7 @@ __global__ void k_trsv_block(const T* A, int64_t lda, T* b, int64_t k0, int kb, 
   } else {
     for (int k = kb - 1; k >= 0; --k) {
       if (threadIdx.x == 0) {
-        T d = A[(k0 + k) + (k0 + k) * lda];
+        T d = D[k + k * kb];
         double den = (double)d.x * d.x + (double)d.y * d.y;
         double r = (xr[k] * d.x + xi[k] * d.y) / den, im = (xi[k] * d.x - xr[k] * d.y) / den;
         xr[k] = r;
@@ -306,7 +407,7 @@ __global__ void k_trsv_block(const T* A, int64_t lda, T* b, int64_t k0, int kb, 
       __syncthreads();
       double vr = xr[k], vi = xi[k];
       for (int i = threadIdx.x; i < k; i += blockDim.x) {
-        T u = A[(k0 + i) + (k0 + k) * lda];
+        T u = D[i + k * kb];
         xr[i] -= u.x * vr - u.y * vi;
         xi[i] -= u.x * vi + u.y * vr;
       }
@@ -331,6 +432,112 @@ __global__ void k_trsv_update(const T* A, int64_t lda, T* b, int64_t k0, int kb,
   }
   T v = b[i];
   b[i] = cmk<T>(v.x - sr, v.y - si);
+}
+
+// ---- triangular solve on one right-hand side as a wavefront ------------------------------
+// Block rows of 64 are owned round-robin by co-resident CTAs (cooperative launch).  A CTA
+// accumulates the off-diagonal products of its block row as the solved blocks it depends on
+// are published (flag per block), solves its diagonal block in shared memory and publishes
+// it.  lower = 1: unit lower, forward; lower = 0: upper, backward.  Arithmetic in RT (the
+// factors' precision).  Flag waits are bounded; on expiry a status bit is set and the CTA
+// returns.
+template <typename T, typename RT>
+__global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int64_t n, T* x, int lower,
+                                                   int* flags, int* status) {
+  extern __shared__ unsigned char smraw[];
+  T* D = reinterpret_cast<T*>(smraw);  // 64 x 65 (row-major, padded)
+  __shared__ RT sr[64], si[64];
+  __shared__ RT pr[4][64], pim[4][64];
+  __shared__ int s_abort;
+  const int nblk = (int)((n + 63) / 64);
+  const int tid = threadIdx.x, r = tid & 63, q = tid >> 6;
+  for (int t = blockIdx.x; t < nblk; t += gridDim.x) {
+    const int b = lower ? t : nblk - 1 - t;
+    const int64_t r0 = (int64_t)b * 64;
+    const int rb = (int)(n - r0 < 64 ? n - r0 : 64);
+    RT ar = 0, ai = 0;
+    const int ndep = lower ? b : nblk - 1 - b;
+    for (int s = 0; s < ndep; ++s) {
+      const int k = lower ? s : nblk - 1 - s;
+      if (tid == 0) {
+        s_abort = 0;
+        long long it = 0;
+        while (atomicAdd(flags + k, 0) == 0) {
+          if (++it > (1LL << 24)) {
+            atomicOr(status, 8);
+            s_abort = 1;
+            break;
+          }
+          __nanosleep(32);
+        }
+        __threadfence();
+      }
+      __syncthreads();
+      if (s_abort) return;
+      const int64_t c0 = (int64_t)k * 64;
+      const int cb = (int)(n - c0 < 64 ? n - c0 : 64);
+      if (r < rb) {
+        const T* Ar = A + (r0 + r) + c0 * lda;
+        for (int c = q * 16; c < q * 16 + 16 && c < cb; ++c) {
+          T a = Ar[c * lda];
+          T xv = __ldcg(x + c0 + c);
+          ar += (RT)a.x * (RT)xv.x - (RT)a.y * (RT)xv.y;
+          ai += (RT)a.x * (RT)xv.y + (RT)a.y * (RT)xv.x;
+        }
+      }
+    }
+    pr[q][r] = ar;
+    pim[q][r] = ai;
+    for (int e = tid; e < rb * rb; e += blockDim.x) {
+      int i = e % rb, c = e / rb;
+      D[i * 65 + c] = A[(r0 + i) + (r0 + c) * lda];
+    }
+    __syncthreads();
+    if (tid < rb) {
+      T bv = __ldcg(x + r0 + tid);
+      sr[tid] = (RT)bv.x - (pr[0][tid] + pr[1][tid] + pr[2][tid] + pr[3][tid]);
+      si[tid] = (RT)bv.y - (pim[0][tid] + pim[1][tid] + pim[2][tid] + pim[3][tid]);
+    }
+    __syncthreads();
+    if (lower) {
+      for (int k = 0; k < rb; ++k) {
+        RT vr = sr[k], vi = si[k];
+        if (tid > k && tid < rb) {
+          T l = D[tid * 65 + k];
+          sr[tid] -= (RT)l.x * vr - (RT)l.y * vi;
+          si[tid] -= (RT)l.x * vi + (RT)l.y * vr;
+        }
+        __syncthreads();
+      }
+    } else {
+      for (int k = rb - 1; k >= 0; --k) {
+        if (tid == 0) {
+          T d = D[k * 65 + k];
+          RT den = (RT)d.x * (RT)d.x + (RT)d.y * (RT)d.y;
+          RT xr = (sr[k] * (RT)d.x + si[k] * (RT)d.y) / den, xi = (si[k] * (RT)d.x - sr[k] * (RT)d.y) / den;
+          sr[k] = xr;
+          si[k] = xi;
+        }
+        __syncthreads();
+        RT vr = sr[k], vi = si[k];
+        if (tid < k) {
+          T u = D[tid * 65 + k];
+          sr[tid] -= (RT)u.x * vr - (RT)u.y * vi;
+          si[tid] -= (RT)u.x * vi + (RT)u.y * vr;
+        }
+        __syncthreads();
+      }
+    }
+    if (tid < rb) {
+      T o;
+      o.x = sr[tid];
+      o.y = si[tid];
+      x[r0 + tid] = o;
+    }
+    __threadfence();
+    __syncthreads();
+    if (tid == 0) atomicExch(flags + b, 1);
+  }
 }
 
 // out[i] = in[perm[i]]: the row interchanges of the factorisation applied as one gather
@@ -469,60 +676,128 @@ __global__ void k_gemv_sub(int64_t n, int m, const double* V, int64_t ldv, const
 }
 
 template <typename T, typename R>
+struct LUSteps {
+  beast_ctx* ctx;
+  T* A;
+  int64_t lda, n;
+  int* ipiv;
+  cudaStream_t st;
+  int laswp(int64_t c0, int64_t c1, int64_t p0, int64_t p1) {
+    if (c1 <= c0 || p1 <= p0) return BEAST_OK;
+    ProfScope ps(ctx, PK_LASWP, (double)(c1 - c0) * (p1 - p0) * 2 * sizeof(T));
+    k_laswp<T><<<(unsigned)((c1 - c0 + 255) / 256), 256, 0, st>>>(A, lda, c0, c1, p0, p1, ipiv);
+    BEAST_CUDA_TRY(ctx, cudaGetLastError());
+    return BEAST_OK;
+  }
+  int trsm(int64_t j0, int kb, int64_t c0, int64_t c1) {
+    if (c1 <= c0) return BEAST_OK;
+    ProfScope ps(ctx, PK_TRSM, 4.0 * (double)(c1 - c0) * kb * kb);
+    size_t smb = (size_t)(kb * kb + 64 * (kb + 1)) * sizeof(T);
+    k_trsm<T><<<(unsigned)((c1 - c0 + 63) / 64), 64, smb, st>>>(A, lda, j0, kb, c0, c1);
+    BEAST_CUDA_TRY(ctx, cudaGetLastError());
+    return BEAST_OK;
+  }
+  // A[r0:r0+m, c0:c0+nc] -= A[r0:r0+m, k0:k0+k] A[k0:k0+k, c0:c0+nc]
+  int gemm(int64_t r0, int64_t m, int64_t c0, int64_t nc, int64_t k0, int k, float* tcwork) {
+    if (m <= 0 || nc <= 0 || k <= 0) return BEAST_OK;
+    ProfScope ps(ctx, PK_GEMM, 8.0 * (double)m * nc * k);
+    if (sizeof(T) == 8 && tcwork && m >= 128 && nc >= 256) {
+      return tc_gemm_sub(ctx, reinterpret_cast<float2*>(A), lda, n, r0, k0, c0, m, nc, k, tcwork);
+    }
+    dim3 g((unsigned)((m + GT - 1) / GT), (unsigned)((nc + GT - 1) / GT));
+    k_gemm_sub<T, R><<<g, 256, 0, st>>>(A + r0 + c0 * lda, lda, A + r0 + k0 * lda, lda, A + k0 + c0 * lda,
+                                        lda, m, nc, k);
+    BEAST_CUDA_TRY(ctx, cudaGetLastError());
+    return BEAST_OK;
+  }
+};
+
+// Two-level right-looking LU: column blocks of NB are factored with nb-wide panels (panel,
+// interchanges, TRSM and GEMM restricted to the block); then the block's interchanges are
+// applied to the other columns and the trailing matrix gets one rank-NB update
+// (TRSM for U12, GEMM with K = NB -- on the tensor cores for complex FP32).
+template <typename T, typename R>
 int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* info) {
   cudaStream_t st = ctx->stream;
-  const int nb = 64;
-  // scratch for the panel kernel: candidates + barrier words + info
-  const int maxblk = 1024;
-  size_t need = maxblk * sizeof(double) + maxblk * sizeof(int) + 4 * sizeof(unsigned int) + sizeof(int);
+  const int G0 = std::max(1, ctx->num_sms);
+  const size_t smem_cap = 220 * 1024;
+  int nb = 64;
+  int64_t rows0 = (n + G0 - 1) / G0;
+  while (nb > 8 && (size_t)(rows0 * (nb + 1) + nb) * sizeof(T) > smem_cap) nb /= 2;
+  if ((size_t)(rows0 * (nb + 1) + nb) * sizeof(T) > smem_cap)
+    return beast_fail(ctx, BEAST_ERR_ARG, "matrix too large for the shared-memory panel");
+  const int NB = 4 * nb;
+  const size_t panel_smem = (size_t)(rows0 * (nb + 1) + nb) * sizeof(T);
+  const size_t trsm_smem = (size_t)(nb * nb + 64 * (nb + 1)) * sizeof(T);
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem));
+  int occ = 0;
+  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_panel<T>, 256, panel_smem));
+  if (occ < 1) return beast_fail(ctx, BEAST_ERR_CUDA, "panel kernel does not fit on an SM");
+  size_t need = 2 * G0 * sizeof(double) + 2 * G0 * sizeof(int) + (2 * (size_t)G0 * nb + 2 * nb) * sizeof(T) +
+                8 * sizeof(unsigned int) + 256;
   char* scr = nullptr;
   BEAST_CUDA_TRY(ctx, cudaMallocAsync(&scr, need, st));
   double* cval = reinterpret_cast<double*>(scr);
-  int* cidx = reinterpret_cast<int*>(scr + maxblk * sizeof(double));
-  unsigned int* bar = reinterpret_cast<unsigned int*>(scr + maxblk * (sizeof(double) + sizeof(int)));
+  int* cidx = reinterpret_cast<int*>(cval + 2 * G0);
+  T* crow = reinterpret_cast<T*>(((uintptr_t)(cidx + 2 * G0) + 15) & ~(uintptr_t)15);
+  T* rowj = crow + 2 * (size_t)G0 * nb;
+  unsigned int* bar = reinterpret_cast<unsigned int*>(rowj + 2 * nb);
   int* dinfo = reinterpret_cast<int*>(bar + 4);
   BEAST_CUDA_TRY(ctx, cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned int) + sizeof(int), st));
+  BEAST_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), st));
   GridSync gs{bar, bar + 1, reinterpret_cast<int*>(bar + 2)};
-  int occ = 0;
-  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_panel<T>, 256, 0));
-  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)(nb * nb * sizeof(T))));
+  // tensor-core workspace: the expanded L21 block (2M x 2NB floats)
+  float* tcwork = nullptr;
+  if (sizeof(T) == 8 && tc_gemm_supported(A, lda, NB) && n > NB)
+    BEAST_CUDA_TRY(ctx, cudaMallocAsync(&tcwork, (size_t)2 * n * 2 * NB * sizeof(float), st));
+  LUSteps<T, R> S{ctx, A, lda, n, ipiv, st};
   int rc = BEAST_OK;
-  for (int64_t j0 = 0; j0 < n; j0 += nb) {
-    int kb = (int)std::min<int64_t>(nb, n - j0);
-    int64_t M = n - j0;
-    int nblk = (int)std::min<int64_t>({(int64_t)ctx->num_sms * std::max(occ, 1), (M + 255) / 256, (int64_t)maxblk});
-    nblk = std::max(nblk, 1);
-    void* args[] = {&A, &lda, &n, &j0, &kb, &ipiv, &dinfo, &cval, &cidx, &gs};
-    {
-      ProfScope ps(ctx, PK_PANEL, 8.0 * (double)M * kb * kb / 2);
-      BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_panel<T>, nblk, 256, args, 0, st));
-    }
-    int64_t other = n - kb;
-    if (other > 0) {
-      ProfScope ps(ctx, PK_LASWP, (double)other * kb * 2 * sizeof(T));
-      k_laswp<T><<<(unsigned)((other + 255) / 256), 256, 0, st>>>(A, lda, n, j0, kb, ipiv);
-    }
-    int64_t rest = n - j0 - kb;
-    if (rest > 0) {
-      size_t smb = (size_t)kb * kb * sizeof(T);
+  for (int64_t J0 = 0; J0 < n && rc == BEAST_OK; J0 += NB) {
+    const int64_t J1 = std::min<int64_t>(n, J0 + NB);
+    for (int64_t j0 = J0; j0 < J1 && rc == BEAST_OK; j0 += nb) {
+      int kb = (int)std::min<int64_t>(nb, J1 - j0);
+      int64_t M = n - j0;
+      int rows_per = (int)((M + G0 - 1) / G0);
+      int G = (int)((M + rows_per - 1) / rows_per);
+      size_t sm = (size_t)(rows_per * (kb + 1) + kb) * sizeof(T);
+      void* args[] = {&A, &lda, &n, &j0, &kb, &rows_per, &ipiv, &dinfo, &cval, &cidx, &crow, &rowj, &gs};
       {
-        ProfScope ps(ctx, PK_TRSM, 4.0 * (double)rest * kb * kb);
-        k_trsm<T><<<(unsigned)((rest + 127) / 128), 128, smb, st>>>(A, lda, n, j0, kb);
+        ProfScope ps(ctx, PK_PANEL, 8.0 * (double)M * kb * kb / 2);
+        BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_panel<T>, G, 256, args, sm, st));
       }
-      dim3 g((unsigned)((rest + GT - 1) / GT), (unsigned)((rest + GT - 1) / GT));
-      ProfScope ps(ctx, PK_GEMM, 8.0 * (double)rest * rest * kb);
-      k_gemm_sub<T, R><<<g, 256, 0, st>>>(A + (j0 + kb) + (j0 + kb) * lda, lda, A + (j0 + kb) + j0 * lda,
-                                          lda, A + j0 + (j0 + kb) * lda, lda, rest, rest, kb);
+      // interchanges inside the column block, TRSM + GEMM for the rest of the block
+      if ((rc = S.laswp(J0, j0, j0, j0 + kb))) break;
+      if ((rc = S.laswp(j0 + kb, J1, j0, j0 + kb))) break;
+      if ((rc = S.trsm(j0, kb, j0 + kb, J1))) break;
+      if ((rc = S.gemm(j0 + kb, n - j0 - kb, j0 + kb, J1 - j0 - kb, j0, kb, nullptr))) break;
     }
-    BEAST_CUDA_TRY(ctx, cudaGetLastError());
+    if (rc) break;
+    // the block's interchanges on the columns left and right of it
+    if ((rc = S.laswp(0, J0, J0, J1))) break;
+    if ((rc = S.laswp(J1, n, J0, J1))) break;
+    if (J1 < n) {
+      // U12 = L11^{-1} A12 (blocked: nb-row TRSM, then GEMM on the rows below inside the block)
+      for (int64_t j0 = J0; j0 < J1 && rc == BEAST_OK; j0 += nb) {
+        int kb = (int)std::min<int64_t>(nb, J1 - j0);
+        if ((rc = S.trsm(j0, kb, J1, n))) break;
+        if ((rc = S.gemm(j0 + kb, J1 - j0 - kb, J1, n - J1, j0, kb, nullptr))) break;
+      }
+      if (rc) break;
+      // trailing update with K = NB
+      rc = S.gemm(J1, n - J1, J1, n - J1, J0, (int)(J1 - J0), tcwork);
+    }
   }
-  int hinfo[2] = {0, 0};
+  if (tcwork) cudaFreeAsync(tcwork, st);
+  int hinfo[3] = {0, 0, 0};
   BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo[0], dinfo, sizeof(int), cudaMemcpyDeviceToHost, st));
   BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo[1], bar + 2, sizeof(int), cudaMemcpyDeviceToHost, st));
+  BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(&hinfo[2], ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost, st));
   BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(st));
   BEAST_CUDA_TRY(ctx, cudaFreeAsync(scr, st));
+  if (rc) return rc;
   if (hinfo[1]) return beast_fail(ctx, BEAST_ERR_TIMEOUT, "LU panel: grid barrier timed out");
+  if (hinfo[2] & 4) return beast_fail(ctx, BEAST_ERR_TIMEOUT, "LU tensor-core update: wait timed out");
   *info = hinfo[0];
   // the sequential interchanges ipiv[0..n) as one permutation: perm[i] = source row of row i
   std::vector<int> hp(n), perm(n);
@@ -530,36 +805,42 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   for (int64_t i = 0; i < n; ++i) perm[i] = (int)i;
   for (int64_t k = 0; k < n; ++k) std::swap(perm[k], perm[hp[k]]);
   BEAST_CUDA_TRY(ctx, cudaMemcpy(ipiv + n, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-  return rc;
+  return BEAST_OK;
 }
 
-template <typename T>
+template <typename T, typename RT>
 int lu_solve_t(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* perm, T* B,
                int64_t ldb, int64_t nrhs) {
   cudaStream_t st = ctx->stream;
-  const int nb = 64;
+  const int nblk = (int)((n + 63) / 64);
   T* tmp = nullptr;
+  int* flags = nullptr;
   BEAST_CUDA_TRY(ctx, cudaMallocAsync(&tmp, (size_t)n * sizeof(T), st));
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&flags, (size_t)2 * nblk * sizeof(int) + 16, st));
+  const size_t dsm = (size_t)64 * 65 * sizeof(T);
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsv_wave<T, RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+  int occ = 0;
+  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, dsm));
+  int G = std::max(1, std::min(nblk, ctx->num_sms * std::max(occ, 1)));
+  int* status = ctx->d_flag;
   for (int64_t r = 0; r < nrhs; ++r) {
     T* b = B + r * ldb;
     BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(tmp, b, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    BEAST_CUDA_TRY(ctx, cudaMemsetAsync(flags, 0, (size_t)2 * nblk * sizeof(int), st));
     // the two triangular solves read the factors once: n^2 elements
-    ProfScope ps(ctx, PK_TRSV, (double)n * n * sizeof(T), 1 + 4 * (int)((n + nb - 1) / nb));
+    ProfScope ps(ctx, PK_TRSV, (double)n * n * sizeof(T), 3);
     k_permute<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tmp, b, perm, n);
-    for (int64_t k0 = 0; k0 < n; k0 += nb) {
-      int kb = (int)std::min<int64_t>(nb, n - k0);
-      k_trsv_block<T><<<1, 128, 0, st>>>(A, lda, b, k0, kb, 1);
-      int64_t r0 = k0 + kb;
-      if (r0 < n) k_trsv_update<T><<<(unsigned)((n - r0 + 255) / 256), 256, 0, st>>>(A, lda, b, k0, kb, r0, n);
-    }
-    for (int64_t k0 = ((n - 1) / nb) * nb; k0 >= 0; k0 -= nb) {
-      int kb = (int)std::min<int64_t>(nb, n - k0);
-      k_trsv_block<T><<<1, 128, 0, st>>>(A, lda, b, k0, kb, 0);
-      if (k0 > 0) k_trsv_update<T><<<(unsigned)((k0 + 255) / 256), 256, 0, st>>>(A, lda, b, k0, kb, 0, k0);
-    }
+    int lower = 1;
+    int* fl = flags;
+    void* args[] = {&A, &lda, &n, &b, &lower, &fl, &status};
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, dsm, st));
+    lower = 0;
+    fl = flags + nblk;
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, dsm, st));
   }
   BEAST_CUDA_TRY(ctx, cudaGetLastError());
   BEAST_CUDA_TRY(ctx, cudaFreeAsync(tmp, st));
+  BEAST_CUDA_TRY(ctx, cudaFreeAsync(flags, st));
   return BEAST_OK;
 }
 
@@ -574,8 +855,8 @@ int lu_factor_dev(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, in
 int lu_solve_dev(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int dtype, const int* ipiv,
                  void* B, int64_t ldb, int64_t nrhs) {
   if (dtype == BEAST_C64)
-    return lu_solve_t<float2>(ctx, n, (const float2*)A, lda, ipiv + n, (float2*)B, ldb, nrhs);
-  return lu_solve_t<double2>(ctx, n, (const double2*)A, lda, ipiv + n, (double2*)B, ldb, nrhs);
+    return lu_solve_t<float2, float>(ctx, n, (const float2*)A, lda, ipiv + n, (float2*)B, ldb, nrhs);
+  return lu_solve_t<double2, double>(ctx, n, (const double2*)A, lda, ipiv + n, (double2*)B, ldb, nrhs);
 }
 
 static double* g_part = nullptr;

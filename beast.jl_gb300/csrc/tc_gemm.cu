@@ -1,0 +1,328 @@
+// tc_gemm.cu -- tensor-core (tcgen05, TF32) trailing update of the complex FP32 LU.
+//
+//   C -= A B   with C (M x N), A (M x K), B (K x N) complex64, column-major
+//
+// is evaluated as one real GEMM on the interleaved (re, im) storage:
+//   C' (2M x N) -= A' (2M x 2K) B' (2K x N)
+//   C', B' = the real views of C and B (no copy: element (r, c) of the complex matrix
+//            occupies rows 2r, 2r+1 of column c of the real view)
+//   A'     = A expanded into 2x2 real blocks [[ar, -ai], [ai, ar]], written K-major and
+//            rounded to TF32 by k_expand.
+// Kernel k_tc_gemm: one CTA per 128 x 256 tile of C'; a single thread issues the TMA loads
+// (128-byte swizzle, 4-stage ring over K) and the tcgen05.mma instructions (M=128, N=256,
+// K=8 per instruction) into a 256-column TMEM accumulator; after tcgen05.commit all four
+// warps read their 32 TMEM lanes with tcgen05.ld and apply C' -= D with coalesced stores.
+// Every mbarrier wait is bounded by a clock budget: on expiry the CTA raises a status bit,
+// still frees its TMEM and returns (the host turns the bit into BEAST_ERR_TIMEOUT).
+#include <cuda.h>
+#include <cuda_runtime.h>
+
+#include <cstring>
+
+#include "internal.h"
+
+namespace {
+
+constexpr int TM = 128, TN = 256, TK = 32;  // tile M (real rows), N, K per stage (floats)
+constexpr int STAGES = 4;
+constexpr int A_BYTES = TM * TK * 4, B_BYTES = TN * TK * 4, STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(bar), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(bar), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// bounded wait on an mbarrier phase; false (and status bit 4) on timeout
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* status) {
+  long long t0 = clock64();
+  while (!mbar_test(bar, parity)) {
+    if (clock64() - t0 > WAIT_CYCLES) {
+      atomicOr(status, 4);
+      return false;
+    }
+  }
+  return true;
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y,
+                                            uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes "
+      "[%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+// shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row atoms of 1024 B
+__device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((addr & 0x3FFFF) >> 4);   // start address
+  d |= (uint64_t)1 << 16;                    // leading byte offset (unused for this layout)
+  d |= (uint64_t)(1024 >> 4) << 32;          // stride byte offset: next 8-row atom
+  d |= (uint64_t)1 << 46;                    // descriptor version
+  d |= (uint64_t)2 << 61;                    // swizzle: 128 B
+  return d;
+}
+
+// instruction descriptor: D f32, A/B tf32, both K-major, M = 128, N = 256
+__host__ __device__ constexpr uint32_t idesc_tf32() {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.u32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accum)
+      : "memory");
+}
+
+__device__ __forceinline__ void mma_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
+               : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]),
+        "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// C' (real view, ldc floats) -= A' B' for a tile grid over (m_rows x n_cols);
+// c_row0 / c_col0: position of the update block inside C'
+__global__ void __launch_bounds__(128, 1)
+    k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+              float* C, int64_t ldc, int64_t c_row0, int64_t c_col0, int m_rows, int n_cols,
+              int b_x0, int b_y0, int nk, int* status) {
+  extern __shared__ unsigned char smraw[];
+  const uint32_t base = (smem_u32(smraw) + 1023u) & ~1023u;
+  unsigned char* gbase = smraw + (base - smem_u32(smraw));
+  uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + STAGES * STAGE_BYTES);
+  // bars[0..STAGES): full, bars[STAGES..2*STAGES): empty, bars[2*STAGES]: done
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
+  __shared__ int s_abort;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
+
+  if (threadIdx.x == 0) {
+    s_abort = 0;
+    for (int s = 0; s < 2 * STAGES + 1; ++s) mbar_init(smem_u32(bars + s), 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 0) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
+                 "r"(TN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (threadIdx.x == 0) {
+    const uint32_t idesc = idesc_tf32();
+    bool ok = true;
+    // prologue: fill the ring
+    for (int kb = 0; kb < nk && kb < STAGES; ++kb) {
+      uint32_t sa = base + kb * STAGE_BYTES, sb = sa + A_BYTES;
+      uint32_t full = smem_u32(bars + kb);
+      mbar_expect_tx(full, STAGE_BYTES);
+      tma_load_2d(sa, &tmA, kb * TK, m0, full);
+      tma_load_2d(sb, &tmB, b_x0 + kb * TK, b_y0 + n0, full);
+    }
+    for (int kb = 0; kb < nk && ok; ++kb) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (kb / STAGES) & 1;
+      if (!mbar_wait(smem_u32(bars + s), ph, status)) {
+        ok = false;
+        break;
+      }
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t sa = base + s * STAGE_BYTES, sb = sa + A_BYTES;
+#pragma unroll
+      for (int kk = 0; kk < TK / 8; ++kk)
+        mma_tf32(tmem, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), idesc, (kb | kk) ? 1u : 0u);
+      mma_commit(smem_u32(bars + STAGES + s));
+      const int nxt = kb + STAGES;
+      if (nxt < nk) {
+        // the stage is reloaded once the MMAs that read it have completed
+        if (!mbar_wait(smem_u32(bars + STAGES + s), ph, status)) {
+          ok = false;
+          break;
+        }
+        uint32_t full = smem_u32(bars + s);
+        mbar_expect_tx(full, STAGE_BYTES);
+        tma_load_2d(sa, &tmA, nxt * TK, m0, full);
+        tma_load_2d(sb, &tmB, b_x0 + nxt * TK, b_y0 + n0, full);
+      }
+    }
+    // the done barrier tracks every MMA issued above (also after an abort, so that no
+    // MMA is in flight when the accumulator is released)
+    mma_commit(smem_u32(bars + 2 * STAGES));
+    if (!ok) s_abort = 1;
+  }
+  __syncthreads();
+  bool have = mbar_wait(smem_u32(bars + 2 * STAGES), 0, status) && !s_abort;
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  if (have) {
+    // epilogue: warp w owns TMEM lanes (= tile rows) 32w .. 32w+31; 64 columns per round
+    // with all 64 loads of C issued before the stores
+    const int row = m0 + warp * 32 + lane;
+    const bool row_ok = row < m_rows;
+    float* __restrict__ crow = C + (c_row0 + row);
+    for (int c0 = 0; c0 < TN; c0 += 64) {
+      float v[64], c[64];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c0 + 16 * q), v + 16 * q);
+      if (row_ok) {
+#pragma unroll
+        for (int i = 0; i < 64; ++i) {
+          int col = n0 + c0 + i;
+          c[i] = col < n_cols ? __ldcs(crow + (c_col0 + col) * ldc) : 0.f;
+        }
+#pragma unroll
+        for (int i = 0; i < 64; ++i) {
+          int col = n0 + c0 + i;
+          if (col < n_cols) __stcs(crow + (c_col0 + col) * ldc, c[i] - v[i]);
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 0) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TN) : "memory");
+  }
+}
+
+// A' (K-major, row m' = 2m + t holds 2K floats): [[ar, -ai], [ai, ar]] blocks, TF32-rounded
+__global__ void k_expand(const float2* A, int64_t lda, int M, int K, float* Ap) {
+  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)M * K) return;
+  int m = (int)(e % M), k = (int)(e / M);
+  float2 a = A[m + (int64_t)k * lda];
+  auto tf = [](float x) {
+    uint32_t r;
+    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
+    return __uint_as_float(r);
+  };
+  float ar = tf(a.x), ai = tf(a.y);
+  float* r0 = Ap + (int64_t)(2 * m) * (2 * K);
+  float* r1 = r0 + 2 * K;
+  r0[2 * k] = ar;
+  r0[2 * k + 1] = -ai;
+  r1[2 * k] = ai;
+  r1[2 * k + 1] = ar;
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+bool make_map(CUtensorMap* m, const float* base, uint64_t dim0, uint64_t dim1, uint64_t stride1_bytes,
+              uint32_t box0, uint32_t box1) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return false;
+  cuuint64_t dims[2] = {dim0, dim1};
+  cuuint64_t strides[1] = {stride1_bytes};
+  cuuint32_t box[2] = {box0, box1};
+  cuuint32_t es[2] = {1, 1};
+  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+// is the tensor-core path usable for this update (alignment rules of TMA)?
+bool tc_gemm_supported(const void* A, int64_t lda, int K) {
+  if (!encode_fn()) return false;
+  if ((reinterpret_cast<uintptr_t>(A) & 15) != 0) return false;
+  if (lda % 2 != 0) return false;         // column stride of the real view: multiple of 16 B
+  if (K % 16 != 0) return false;          // 2K real = whole 32-float K blocks
+  return true;
+}
+
+// C -= A B (complex64) for the LU trailing update:
+//   A at (rowA, colA) of the matrix, M x K;  B at (rowB = colA, colB), K x N;  C at (rowA, colB)
+// Mat: base of the full matrix (n_total x n_total, ld lda); work: >= 2M x 2K floats
+int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t n_total, int64_t rowA,
+                int64_t colA, int64_t colB, int64_t M, int64_t N, int K, float* work) {
+  cudaStream_t st = ctx->stream;
+  static bool attr_done[64] = {false};
+  int dev = ctx->device;
+  if (!attr_done[dev]) {
+    BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    attr_done[dev] = true;
+  }
+  {
+    int64_t tot = M * (int64_t)K;
+    k_expand<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(Mat + rowA + colA * lda, lda, (int)M, K, work);
+  }
+  CUtensorMap tmA, tmB;
+  // A': 2K floats per row (x), 2M rows (y)
+  if (!make_map(&tmA, work, (uint64_t)2 * K, (uint64_t)2 * M, (uint64_t)2 * K * 4, TK, TM))
+    return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (A') failed");
+  // B': real view of the whole matrix: 2 n_total floats per column (x), n_total columns (y)
+  const float* real = reinterpret_cast<const float*>(Mat);
+  if (!make_map(&tmB, real, (uint64_t)2 * n_total, (uint64_t)n_total, (uint64_t)2 * lda * 4, TK, TN))
+    return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (B') failed");
+  const int m_rows = (int)(2 * M), n_cols = (int)N;
+  dim3 grid((unsigned)((n_cols + TN - 1) / TN), (unsigned)((m_rows + TM - 1) / TM));
+  const int nk = (2 * K) / TK;
+  k_tc_gemm<<<grid, 128, SMEM_BYTES, st>>>(tmA, tmB, reinterpret_cast<float*>(Mat), 2 * lda, 2 * rowA,
+                                           colB, m_rows, n_cols, (int)(2 * colA), (int)colB, nk,
+                                           ctx->d_flag);
+  BEAST_CUDA_TRY(ctx, cudaGetLastError());
+  return BEAST_OK;
+}

@@ -63,3 +63,31 @@ def test_gmres_contract(efie):
         x, it, res = bg.gmres(Z, b, reltol=rtol, restart=200, maxiter=2000)
         assert np.linalg.norm(Z @ x - b) / np.linalg.norm(b) < rtol
         assert np.linalg.norm(x - u) / np.linalg.norm(x) < 100 * rtol
+
+
+@pytest.mark.parametrize("n,dtype", [(1100, "c64"), (700, "c128"), (1537, "c64")])
+def test_lu_factors_exact(n, dtype):
+    """P A = L U reproduced exactly: L has dyadic entries (k/64, |re|+|im| < 1, at most 7
+    significant bits), U small integers with a dominant power-of-two diagonal, so every
+    product and partial sum of the factorisation is exact in TF32 x TF32 -> FP32 (the
+    tensor-core trailing update for c64) and in FP64, and partial pivoting keeps the
+    diagonal.  Any indexing or layout error of the GEMM shows up as a nonzero error."""
+    import ctypes as C
+    import torch
+    ctx = bg.get_context(0)
+    rng = np.random.default_rng(11)
+    L = np.tril((rng.integers(-15, 16, size=(n, n)) + 1j * rng.integers(-15, 16, size=(n, n))) / 64.0, -1)
+    L += np.eye(n)
+    U = np.triu(rng.integers(-8, 9, size=(n, n)) + 1j * rng.integers(-8, 9, size=(n, n)), 1)
+    U += 256.0 * np.eye(n)
+    A = L @ U
+    dt = np.complex64 if dtype == "c64" else np.complex128
+    assert np.array_equal(A.astype(dt).astype(np.complex128), A)
+    At = torch.from_numpy(np.ascontiguousarray(A.astype(dt).T)).cuda()
+    h = C.c_void_p()
+    ctx.check(ctx.lib.beast_lu_factor(ctx.handle, n, At.data_ptr(), n,
+                                      bg.C64 if dtype == "c64" else bg.C128, C.byref(h)))
+    F = At.cpu().numpy().T.astype(np.complex128)
+    ctx.lib.beast_lu_free(h)
+    assert np.abs(np.tril(F, -1) - np.tril(L, -1)).max() == 0.0
+    assert np.abs(np.triu(F) - U).max() == 0.0
