@@ -42,7 +42,7 @@ EXPORTS = [
     "beast_ctx_set_workspace_limit", "beast_ctx_synchronize", "beast_mesh_upload",
     "beast_mesh_free", "beast_space_upload", "beast_space_free", "beast_assemble",
     "beast_assemble_local", "beast_rhs_planewave", "beast_lu_factor", "beast_lu_solve",
-    "beast_lu_free", "beast_solve_dense", "beast_gmres", "beast_farfield", "beast_solve_job",
+    "beast_lu_free", "beast_lu_solve_noalloc", "beast_solve_dense", "beast_gmres", "beast_farfield", "beast_solve_job",
     "beast_prof_enable", "beast_prof_read", "beast_prof_launches", "beast_version",
 ]
 
@@ -79,6 +79,7 @@ def load(build_if_needed=True):
     L.beast_lu_factor.argtypes = [vp, i64, vp, i64, i, pp]
     L.beast_lu_solve.argtypes = [vp, vp, i64, vp, i64]
     L.beast_lu_free.argtypes = [vp]
+    L.beast_lu_solve_noalloc.argtypes = [vp, vp, i64, vp, i64]
     L.beast_solve_dense.argtypes = [vp, i64, vp, i64, i, i, vp, vp, i64, i, d, i,
                                     C.POINTER(C.c_int), C.POINTER(C.c_double)]
     L.beast_gmres.argtypes = [vp, i64, vp, i64, i, vp, vp, i, d, i, i, C.POINTER(C.c_int),

@@ -14,6 +14,8 @@
 
 #include <algorithm>
 #include <cmath>
+#include <mutex>
+#include <string>
 #include <vector>
 
 #include "internal.h"
@@ -844,6 +846,45 @@ int lu_solve_t(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* pe
   return BEAST_OK;
 }
 
+// ---- allocation-free triangular solve ----------------------------------------------------
+// Scratch of beast_lu_solve_noalloc: one permuted right-hand side of up to
+// NOALLOC_MAX_N complex128 values, then the per-block flags of the two wavefront sweeps.
+// Held by every GPU that loads the library, for the life of the process.
+constexpr int64_t NOALLOC_MAX_N = 65536;
+constexpr int64_t NOALLOC_FLAGS = 2 * ((NOALLOC_MAX_N + 63) / 64);
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_MAX_N * 16 + NOALLOC_FLAGS * 4];
+
+template <typename T, typename RT>
+int lu_solve_fixed_scratch(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* perm, T* B,
+                           int64_t ldb, int64_t nrhs, unsigned char* scratch) {
+  cudaStream_t st = ctx->stream;
+  const int nblk = (int)((n + 63) / 64);
+  T* tmp = reinterpret_cast<T*>(scratch);
+  int* flags = reinterpret_cast<int*>(scratch + NOALLOC_MAX_N * 16);
+  const size_t dsm = (size_t)64 * 65 * sizeof(T);
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsv_wave<T, RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
+  int occ = 0;
+  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, dsm));
+  int G = std::max(1, std::min(nblk, ctx->num_sms * std::max(occ, 1)));
+  int* status = ctx->d_flag;
+  for (int64_t r = 0; r < nrhs; ++r) {
+    T* b = B + r * ldb;
+    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(tmp, b, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+    // the array keeps the previous call's flags: clear them for this solve
+    BEAST_CUDA_TRY(ctx, cudaMemsetAsync(flags, 0, (size_t)2 * nblk * sizeof(int), st));
+    k_permute<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tmp, b, perm, n);
+    int lower = 1;
+    int* fl = flags;
+    void* args[] = {&A, &lda, &n, &b, &lower, &fl, &status};
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, dsm, st));
+    lower = 0;
+    fl = flags + nblk;
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, dsm, st));
+  }
+  BEAST_CUDA_TRY(ctx, cudaGetLastError());
+  return BEAST_OK;
+}
+
 }  // namespace
 
 int lu_factor_dev(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, int* ipiv, int* info) {
@@ -924,4 +965,47 @@ cudaError_t vec_gemv_sub(int64_t n, int m, const double* V, int64_t ldv, const d
   if (m <= 0) return cudaSuccess;
   k_gemv_sub<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, m, V, ldv, h, w);
   return cudaGetLastError();
+}
+
+// Device address of the fixed scratch, looked up once per device with that device current.
+// (In host code the array's name is only a host-side stand-in, never a device address.)
+static unsigned char* noalloc_scratch(beast_ctx* ctx) {
+  static std::mutex mtx;
+  static unsigned char* addr[64] = {nullptr};
+  std::lock_guard<std::mutex> lk(mtx);
+  if (ctx->device < 0 || ctx->device >= 64) return nullptr;
+  if (!addr[ctx->device]) {
+    void* p = nullptr;
+    if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess) return nullptr;
+    addr[ctx->device] = static_cast<unsigned char*>(p);
+  }
+  return addr[ctx->device];
+}
+
+extern "C" int beast_lu_solve_noalloc(beast_ctx* ctx, const beast_lu* lu, int64_t nrhs, void* B,
+                                      int64_t ldb) {
+  if (!ctx) return BEAST_ERR_ARG;
+  if (!lu || !B || nrhs < 0 || ldb < lu->n)
+    return beast_fail(ctx, BEAST_ERR_ARG, "invalid solve arguments");
+  if (lu->n > NOALLOC_MAX_N)
+    return beast_fail(ctx, BEAST_ERR_ARG,
+                      "beast_lu_solve_noalloc: n = " + std::to_string(lu->n) +
+                          " exceeds the fixed scratch limit of " + std::to_string(NOALLOC_MAX_N) +
+                          " unknowns; use beast_lu_solve");
+  BEAST_CUDA_TRY(ctx, cudaSetDevice(ctx->device));
+  unsigned char* scratch = noalloc_scratch(ctx);
+  if (!scratch) return beast_fail(ctx, BEAST_ERR_CUDA, "cudaGetSymbolAddress of the fixed scratch failed");
+  int rc;
+  if (lu->dtype == BEAST_C64)
+    rc = lu_solve_fixed_scratch<float2, float>(ctx, lu->n, (const float2*)lu->A, lu->lda, lu->ipiv + lu->n,
+                                               (float2*)B, ldb, nrhs, scratch);
+  else
+    rc = lu_solve_fixed_scratch<double2, double>(ctx, lu->n, (const double2*)lu->A, lu->lda,
+                                                 lu->ipiv + lu->n, (double2*)B, ldb, nrhs, scratch);
+  if (rc) return rc;
+  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  int status = 0;
+  BEAST_CUDA_TRY(ctx, cudaMemcpy(&status, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (status & 8) return beast_fail(ctx, BEAST_ERR_TIMEOUT, "triangular solve: flag wait timed out");
+  return BEAST_OK;
 }

@@ -169,6 +169,18 @@ int beast_lu_factor(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, 
 int beast_lu_solve(beast_ctx* ctx, const beast_lu* lu, int64_t nrhs, void* B, int64_t ldb);
 int beast_lu_free(beast_lu* lu);
 
+/* Same result as beast_lu_solve, but the call allocates no device memory: its scratch (one
+ * permuted right-hand side and the wavefront flags) is a fixed array inside the library,
+ * sized for n <= 65536 (about 1 MiB, held by every GPU that loads the library until the
+ * process exits).  For callers that cannot allocate at solve time: a host runtime that owns
+ * the device memory pool (such as Julia's CUDA.jl allocator) or a serving loop that reserves
+ * all memory up front.  Larger n is rejected with BEAST_ERR_ARG.  The first call on a device
+ * looks up the array's device address; make that first call before any stream capture.
+ * All calls share the one array and it keeps the previous call's contents: calls that
+ * overlap on the GPU (other streams, other host threads) race -- serialise them.
+ * No counterpart in the reference (it has no device memory). */
+int beast_lu_solve_noalloc(beast_ctx* ctx, const beast_lu* lu, int64_t nrhs, void* B, int64_t ldb);
+
 /* x = A \ b for a device matrix A (c128 or c64).  precision BEAST_FP64: FP64 LU;
  * BEAST_MIXED: FP32 LU of a c64 copy + FP64 iterative refinement to `tol` relative
  * residual (residual matvec and update in FP64, against A as stored).
