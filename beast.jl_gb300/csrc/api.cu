@@ -633,7 +633,7 @@ int beast_lu_factor(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, 
   lu->lda = lda;
   lu->dtype = dtype;
   lu->A = A;
-  cudaError_t e = cudaMalloc(&lu->ipiv, sizeof(int) * 2 * n);
+  cudaError_t e = cudaMalloc(&lu->ipiv, lu_aux_bytes(n, dtype));
   if (e != cudaSuccess) {
     delete lu;
     return beast_fail(ctx, BEAST_ERR_OOM, "pivot allocation failed");
@@ -675,18 +675,11 @@ static double dev_norm(beast_ctx* ctx, int64_t n, const double* x, double* scrat
   return std::sqrt(h);
 }
 
-// core of the dense solve on device vectors (b, x: c128 [n x nrhs], ld n)
-static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dtype,
-                              int precision, const double* b, double* x, int64_t nrhs, double tol,
-                              int maxiter, int* iters, double* resid) {
+// copy A into F (c64 for the mixed path, c128 otherwise) and factor F in place
+static int factor_copy(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dtype, void* F,
+                       int fdt, bool pivot, beast_lu** out) {
   cudaStream_t st = ctx->stream;
-  const bool mixed = precision == BEAST_MIXED;
-  const int fdt = mixed ? BEAST_C64 : BEAST_C128;
-  const size_t fel = mixed ? 8 : 16;
-  void* F = nullptr;
-  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&F, (size_t)n * n * fel, st));
-  // factor a copy (c64 for the mixed path)
-  if (mixed) {
+  if (fdt == BEAST_C64) {
     if (a_dtype == BEAST_C64)
       BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(F, n * 8, A, lda * 8, n * 8, n, cudaMemcpyDeviceToDevice, st));
     else {
@@ -697,13 +690,42 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
     ARG_CHECK(ctx, a_dtype == BEAST_C128, "plain FP64 solve needs a c128 matrix");
     BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(F, n * 16, A, lda * 16, n * 16, n, cudaMemcpyDeviceToDevice, st));
   }
-  beast_lu* lu = nullptr;
-  int rc = beast_lu_factor(ctx, n, F, n, fdt, &lu);
+  beast_lu* lu = new beast_lu();
+  lu->ctx = ctx;
+  lu->n = n;
+  lu->lda = n;
+  lu->dtype = fdt;
+  lu->A = F;
+  cudaError_t e = cudaMalloc(&lu->ipiv, lu_aux_bytes(n, fdt));
+  if (e != cudaSuccess) {
+    delete lu;
+    return beast_fail(ctx, BEAST_ERR_OOM, "pivot allocation failed");
+  }
+  int rc = lu_factor_dev(ctx, n, F, n, fdt, lu->ipiv, &lu->info, pivot);
+  if (rc == BEAST_OK && lu->info > 0)
+    rc = beast_fail(ctx, BEAST_ERR_SINGULAR, "zero pivot in column " + std::to_string(lu->info));
   if (rc) {
     beast_lu_free(lu);
-    cudaFreeAsync(F, st);
     return rc;
   }
+  *out = lu;
+  return BEAST_OK;
+}
+
+// core of the dense solve on device vectors (b, x: c128 [n x nrhs], ld n)
+// FP64: partial-pivoting LU in complex FP64 (zgetrf semantics) + one solve.
+// MIXED: complex FP32 LU (tensor-core trailing updates) of a c64 copy, first without row
+// interchanges; FP64 iterative refinement against A as stored.  A zero pivot, a diverging
+// or stagnating refinement triggers one refactorisation with partial pivoting.
+static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dtype,
+                              int precision, const double* b, double* x, int64_t nrhs, double tol,
+                              int maxiter, int* iters, double* resid) {
+  cudaStream_t st = ctx->stream;
+  const bool mixed = precision == BEAST_MIXED;
+  const int fdt = mixed ? BEAST_C64 : BEAST_C128;
+  const size_t fel = mixed ? 8 : 16;
+  void* F = nullptr;
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&F, (size_t)n * n * fel, st));
   double *r = nullptr, *d = nullptr, *nrm = nullptr;
   float* d32 = nullptr;
   BEAST_CUDA_TRY(ctx, cudaMallocAsync(&r, n * 16, st));
@@ -712,54 +734,84 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
   if (mixed) BEAST_CUDA_TRY(ctx, cudaMallocAsync(&d32, n * 8, st));
   int it_max = 0;
   double res_max = 0;
-  for (int64_t k = 0; k < nrhs && rc == BEAST_OK; ++k) {
-    const double* bk = b + 2 * k * n;
-    double* xk = x + 2 * k * n;
-    double bn = dev_norm(ctx, n, bk, nrm);
-    if (!mixed) {
-      BEAST_CUDA_TRY(ctx, vec_copy(n, bk, xk, st));
-      rc = lu_solve_dev(ctx, n, F, n, BEAST_C128, lu->ipiv, xk, n, 1);
-      if (rc) break;
-      BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
-      {
-        ProfScope ps(ctx, PK_GEMV, (double)n * n * 16, 2);
-        BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, 0, xk, r, -1.0, 1.0, st));
-      }
-      double rn = dev_norm(ctx, n, r, nrm);
-      res_max = std::max(res_max, bn > 0 ? rn / bn : rn);
+  int rc = BEAST_OK;
+  beast_lu* lu = nullptr;
+  bool pivot = !mixed;
+  for (int attempt = 0; attempt < 2; ++attempt) {
+    if (lu) {
+      beast_lu_free(lu);
+      lu = nullptr;
+    }
+    rc = factor_copy(ctx, n, A, lda, a_dtype, F, fdt, pivot, &lu);
+    if (rc == BEAST_ERR_SINGULAR && !pivot) {
+      pivot = true;
       continue;
     }
-    // mixed: FP32 LU + FP64 iterative refinement
-    BEAST_CUDA_TRY(ctx, cudaMemsetAsync(xk, 0, n * 16, st));
-    BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
-    int it = 0;
-    double rel = 1.0;
-    while (true) {
-      BEAST_CUDA_TRY(ctx, convert_c128_to_c64(n, 1, r, n, d32, n, st));
-      rc = lu_solve_dev(ctx, n, F, n, BEAST_C64, lu->ipiv, d32, n, 1);
-      if (rc) break;
-      BEAST_CUDA_TRY(ctx, convert_c64_to_c128(n, 1, d32, n, d, n, st));
-      BEAST_CUDA_TRY(ctx, vec_axpy(n, 1.0, 0.0, d, xk, st));
-      BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
-      {
-        ProfScope ps(ctx, PK_GEMV, (double)n * n * (a_dtype == BEAST_C64 ? 8 : 16), 2);
-        BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, a_dtype == BEAST_C64, xk, r, -1.0, 1.0, st));
+    if (rc) break;
+    it_max = 0;
+    res_max = 0;
+    bool retry = false;
+    for (int64_t k = 0; k < nrhs && rc == BEAST_OK; ++k) {
+      const double* bk = b + 2 * k * n;
+      double* xk = x + 2 * k * n;
+      double bn = dev_norm(ctx, n, bk, nrm);
+      if (!mixed) {
+        BEAST_CUDA_TRY(ctx, vec_copy(n, bk, xk, st));
+        rc = lu_solve_dev(ctx, n, F, n, BEAST_C128, lu->ipiv, xk, n, 1);
+        if (rc) break;
+        BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
+        {
+          ProfScope ps(ctx, PK_GEMV, (double)n * n * 16, 2);
+          BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, 0, xk, r, -1.0, 1.0, st));
+        }
+        double rn = dev_norm(ctx, n, r, nrm);
+        res_max = std::max(res_max, bn > 0 ? rn / bn : rn);
+        continue;
       }
-      ++it;
-      double rn = dev_norm(ctx, n, r, nrm);
-      rel = bn > 0 ? rn / bn : rn;
-      if (rel <= tol || it >= maxiter) break;
+      BEAST_CUDA_TRY(ctx, cudaMemsetAsync(xk, 0, n * 16, st));
+      BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
+      int it = 0;
+      double rel = 1.0, prev = 1e300;
+      int slow = 0;
+      while (true) {
+        BEAST_CUDA_TRY(ctx, convert_c128_to_c64(n, 1, r, n, d32, n, st));
+        rc = lu_solve_dev(ctx, n, F, n, BEAST_C64, lu->ipiv, d32, n, 1);
+        if (rc) break;
+        BEAST_CUDA_TRY(ctx, convert_c64_to_c128(n, 1, d32, n, d, n, st));
+        BEAST_CUDA_TRY(ctx, vec_axpy(n, 1.0, 0.0, d, xk, st));
+        BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
+        {
+          ProfScope ps(ctx, PK_GEMV, (double)n * n * (a_dtype == BEAST_C64 ? 8 : 16), 2);
+          BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, a_dtype == BEAST_C64, xk, r, -1.0, 1.0, st));
+        }
+        ++it;
+        double rn = dev_norm(ctx, n, r, nrm);
+        rel = bn > 0 ? rn / bn : rn;
+        if (rel <= tol || it >= maxiter) break;
+        // contraction slower than 1/2 per step twice in a row: the factors are not good enough
+        if (!(rel < 0.5 * prev)) ++slow; else slow = 0;
+        if (!std::isfinite(rel) || slow >= 2) break;
+        prev = rel;
+      }
+      if (rc) break;
+      it_max = std::max(it_max, it);
+      res_max = std::max(res_max, rel);
+      if (rel > tol) {
+        if (!pivot) retry = true;
+        else rc = beast_fail(ctx, BEAST_ERR_NOCONV, "iterative refinement did not reach the tolerance");
+      }
     }
-    it_max = std::max(it_max, it);
-    res_max = std::max(res_max, rel);
-    if (rc == BEAST_OK && rel > tol)
-      rc = beast_fail(ctx, BEAST_ERR_NOCONV, "iterative refinement did not reach the tolerance");
+    if (retry && rc == BEAST_OK) {
+      pivot = true;
+      continue;
+    }
+    break;
   }
   cudaFreeAsync(r, st);
   cudaFreeAsync(d, st);
   cudaFreeAsync(nrm, st);
   if (d32) cudaFreeAsync(d32, st);
-  beast_lu_free(lu);
+  if (lu) beast_lu_free(lu);
   cudaFreeAsync(F, st);
   cudaStreamSynchronize(st);
   if (iters) *iters = it_max;

@@ -173,8 +173,14 @@ cudaError_t launch_farfield(const beast_space* s, const double* u, const double*
                             cudaStream_t st);
 
 // ---- dense linear algebra (linalg.cu)
+// bytes of the auxiliary allocation of a factorisation (pivots, permutation, inverses of the
+// diagonal blocks); lu_dinv locates the inverses inside it
+size_t lu_aux_bytes(int64_t n, int dtype);
+void* lu_dinv(const int* ipiv, int64_t n);
+// pivot = false: no row interchanges (the mixed path; guarded by refinement and a
+// fall-back to partial pivoting in the caller)
 int lu_factor_dev(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, int* ipiv,
-                  int* info);
+                  int* info, bool pivot = true);
 int lu_solve_dev(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int dtype,
                  const int* ipiv, void* B, int64_t ldb, int64_t nrhs);
 // y = alpha * A x + beta * y (FP64 arithmetic, A c128 or c64, x/y c128)

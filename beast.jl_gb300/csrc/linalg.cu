@@ -20,6 +20,18 @@
 
 #include "internal.h"
 
+// the pivot allocation of a factorisation: ipiv[n], perm[n], then (256-byte aligned) the
+// inverses of the 64 x 64 diagonal blocks of L and U
+size_t lu_aux_bytes(int64_t n, int dtype) {
+  size_t head = ((size_t)2 * n * sizeof(int) + 255) & ~(size_t)255;
+  size_t el = dtype == BEAST_C64 ? 8 : 16;
+  return head + (size_t)((n + 63) / 64) * 2 * 4096 * el;
+}
+void* lu_dinv(const int* ipiv, int64_t n) {
+  size_t head = ((size_t)2 * n * sizeof(int) + 255) & ~(size_t)255;
+  return (void*)(reinterpret_cast<const char*>(ipiv) + head);
+}
+
 bool tc_gemm_supported(const void* A, int64_t lda, int K);
 int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t n_total, int64_t rowA, int64_t colA,
                 int64_t colB, int64_t M, int64_t N, int K, float* work);
@@ -310,6 +322,95 @@ __global__ void k_trsm(T* A, int64_t lda, int64_t j0, int nb, int64_t c0g, int64
   }
 }
 
+// ---- LU without pivoting (mixed path) ----------------------------------------------------
+// Diagonal block A[j0:j0+kb, j0:j0+kb] = L11 U11 in place, one CTA; a zero pivot sets *info.
+template <typename T>
+__global__ void __launch_bounds__(256) k_getrf_nopiv_diag(T* A, int64_t lda, int64_t j0, int kb, int* info) {
+  extern __shared__ unsigned char smraw[];
+  T* D = reinterpret_cast<T*>(smraw);  // kb x (kb+1), row-major
+  typedef decltype(D[0].x) RT;
+  const int ld = kb + 1;
+  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+    int i = e % kb, c = e / kb;
+    D[i * ld + c] = A[(j0 + i) + (j0 + c) * lda];
+  }
+  __syncthreads();
+  for (int k = 0; k < kb; ++k) {
+    T piv = D[k * ld + k];
+    RT den = piv.x * piv.x + piv.y * piv.y;
+    if (den == (RT)0) {
+      if (threadIdx.x == 0) atomicCAS(info, 0, (int)(j0 + k + 1));
+      return;
+    }
+    RT ir = piv.x / den, ii = -piv.y / den;
+    for (int i = k + 1 + threadIdx.x; i < kb; i += blockDim.x) {
+      T a = D[i * ld + k];
+      T l;
+      l.x = a.x * ir - a.y * ii;
+      l.y = a.x * ii + a.y * ir;
+      D[i * ld + k] = l;
+    }
+    __syncthreads();
+    const int w = kb - k - 1;
+    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
+      int i = k + 1 + e / w, c = k + 1 + e % w;
+      T l = D[i * ld + k], u = D[k * ld + c], v = D[i * ld + c];
+      v.x -= l.x * u.x - l.y * u.y;
+      v.y -= l.x * u.y + l.y * u.x;
+      D[i * ld + c] = v;
+    }
+    __syncthreads();
+  }
+  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+    int i = e % kb, c = e / kb;
+    A[(j0 + i) + (j0 + c) * lda] = D[i * ld + c];
+  }
+}
+
+// L21 = A21 U11^{-1} for rows [r0, r1): x U11 = a per row, 64 rows per CTA (thread per row)
+template <typename T>
+__global__ void k_trsm_right_upper(T* A, int64_t lda, int64_t j0, int kb, int64_t r0g, int64_t r1) {
+  extern __shared__ unsigned char smraw[];
+  T* U = reinterpret_cast<T*>(smraw);   // kb x kb column-major
+  T* X = U + kb * kb;                   // 64 rows x (kb + 1)
+  typedef decltype(U[0].x) RT;
+  const int ldx = kb + 1;
+  const int64_t r0 = r0g + (int64_t)blockIdx.x * 64;
+  const int nr = (int)(r1 - r0 < 64 ? r1 - r0 : 64);
+  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+    int r = e % kb, c = e / kb;
+    U[e] = A[(j0 + r) + (j0 + c) * lda];
+  }
+  for (int e = threadIdx.x; e < nr * kb; e += blockDim.x) {
+    int r = e % nr, c = e / nr;
+    X[r * ldx + c] = A[(r0 + r) + (j0 + c) * lda];
+  }
+  __syncthreads();
+  const int t = threadIdx.x;
+  if (t < nr) {
+    T* x = X + t * ldx;
+    for (int k = 0; k < kb; ++k) {
+      T s = x[k];
+      for (int i = 0; i < k; ++i) {
+        T xi = x[i], u = U[i + k * kb];
+        s.x -= xi.x * u.x - xi.y * u.y;
+        s.y -= xi.x * u.y + xi.y * u.x;
+      }
+      T d = U[k + k * kb];
+      RT den = d.x * d.x + d.y * d.y;
+      T q;
+      q.x = (s.x * d.x + s.y * d.y) / den;
+      q.y = (s.y * d.x - s.x * d.y) / den;
+      x[k] = q;
+    }
+  }
+  __syncthreads();
+  for (int e = threadIdx.x; e < nr * kb; e += blockDim.x) {
+    int r = e % nr, c = e / nr;
+    A[(r0 + r) + (j0 + c) * lda] = X[r * ldx + c];
+  }
+}
+
 // ---- C -= A B  (complex; C m x n, A m x k, B k x n; all column-major with ld) -------------
 constexpr int GT = 64, GK = 8;
 template <typename T, typename R>
@@ -436,6 +537,70 @@ __global__ void k_trsv_update(const T* A, int64_t lda, T* b, int64_t k0, int kb,
   b[i] = cmk<T>(v.x - sr, v.y - si);
 }
 
+// ---- inverses of the 64 x 64 diagonal blocks of L (unit lower) and U (upper) ----------
+// dinv + b * 2 * 4096: Linv_b then Uinv_b, column-major 64 x 64 (identity beyond rb)
+template <typename T, typename RT>
+__global__ void k_invert_diag(const T* A, int64_t lda, int64_t n, T* dinv) {
+  extern __shared__ unsigned char smraw[];
+  T* D = reinterpret_cast<T*>(smraw);   // 64 x 65 row-major
+  T* X = D + 64 * 65;                   // 64 columns x 65 (column j of the inverse)
+  const int b = blockIdx.x;
+  const int64_t r0 = (int64_t)b * 64;
+  const int rb = (int)(n - r0 < 64 ? n - r0 : 64);
+  for (int e = threadIdx.x; e < 64 * 64; e += blockDim.x) {
+    int i = e % 64, c = e / 64;
+    T v;
+    v.x = (RT)(i == c ? 1 : 0);
+    v.y = 0;
+    if (i < rb && c < rb) v = A[(r0 + i) + (r0 + c) * lda];
+    D[i * 65 + c] = v;
+  }
+  __syncthreads();
+  const int j = threadIdx.x;  // one column of each inverse per thread
+  T* x = X + j * 65;
+  T* Lout = dinv + (int64_t)b * 2 * 4096;
+  T* Uout = Lout + 4096;
+  // L x = e_j (unit lower)
+  for (int i = 0; i < 64; ++i) {
+    T v;
+    v.x = (RT)(i == j ? 1 : 0);
+    v.y = 0;
+    if (i > j)
+      for (int m = j; m < i; ++m) {
+        T l = D[i * 65 + m], xm = x[m];
+        v.x -= l.x * xm.x - l.y * xm.y;
+        v.y -= l.x * xm.y + l.y * xm.x;
+      }
+    x[i] = v;
+  }
+  for (int i = 0; i < 64; ++i) Lout[j * 64 + i] = x[i];
+  // U x = e_j (upper)
+  for (int i = 63; i >= 0; --i) {
+    T v;
+    v.x = (RT)(i == j ? 1 : 0);
+    v.y = 0;
+    if (i < j)
+      for (int m = i + 1; m <= j; ++m) {
+        T u = D[i * 65 + m], xm = x[m];
+        v.x -= u.x * xm.x - u.y * xm.y;
+        v.y -= u.x * xm.y + u.y * xm.x;
+      }
+    if (i > j) {
+      v.x = 0;
+      v.y = 0;
+    } else {
+      T d = D[i * 65 + i];
+      RT den = d.x * d.x + d.y * d.y;
+      T q;
+      q.x = (v.x * d.x + v.y * d.y) / den;
+      q.y = (v.y * d.x - v.x * d.y) / den;
+      v = q;
+    }
+    x[i] = v;
+  }
+  for (int i = 0; i < 64; ++i) Uout[j * 64 + i] = x[i];
+}
+
 // ---- triangular solve on one right-hand side as a wavefront ------------------------------
 // Block rows of 64 are owned round-robin by co-resident CTAs (cooperative launch).  A CTA
 // accumulates the off-diagonal products of its block row as the solved blocks it depends on
@@ -445,9 +610,7 @@ __global__ void k_trsv_update(const T* A, int64_t lda, T* b, int64_t k0, int kb,
 // returns.
 template <typename T, typename RT>
 __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int64_t n, T* x, int lower,
-                                                   int* flags, int* status) {
-  extern __shared__ unsigned char smraw[];
-  T* D = reinterpret_cast<T*>(smraw);  // 64 x 65 (row-major, padded)
+                                                   int* flags, int* status, const T* dinv) {
   __shared__ RT sr[64], si[64];
   __shared__ RT pr[4][64], pim[4][64];
   __shared__ int s_abort;
@@ -490,50 +653,35 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
     }
     pr[q][r] = ar;
     pim[q][r] = ai;
-    for (int e = tid; e < rb * rb; e += blockDim.x) {
-      int i = e % rb, c = e / rb;
-      D[i * 65 + c] = A[(r0 + i) + (r0 + c) * lda];
+    __syncthreads();
+    if (tid < 64) {
+      RT vr = 0, vi = 0;
+      if (tid < rb) {
+        T bv = __ldcg(x + r0 + tid);
+        vr = (RT)bv.x - (pr[0][tid] + pr[1][tid] + pr[2][tid] + pr[3][tid]);
+        vi = (RT)bv.y - (pim[0][tid] + pim[1][tid] + pim[2][tid] + pim[3][tid]);
+      }
+      sr[tid] = vr;
+      si[tid] = vi;
     }
     __syncthreads();
-    if (tid < rb) {
-      T bv = __ldcg(x + r0 + tid);
-      sr[tid] = (RT)bv.x - (pr[0][tid] + pr[1][tid] + pr[2][tid] + pr[3][tid]);
-      si[tid] = (RT)bv.y - (pim[0][tid] + pim[1][tid] + pim[2][tid] + pim[3][tid]);
+    // x_b = inv(D_b) * rhs_b  (64 x 64 matvec, 4 quarter sums per row)
+    {
+      const T* Di = dinv + (int64_t)b * 2 * 4096 + (lower ? 0 : 4096);
+      RT accr = 0, acci = 0;
+      for (int c = q * 16; c < q * 16 + 16; ++c) {
+        T m = Di[c * 64 + r];
+        accr += (RT)m.x * sr[c] - (RT)m.y * si[c];
+        acci += (RT)m.x * si[c] + (RT)m.y * sr[c];
+      }
+      pr[q][r] = accr;
+      pim[q][r] = acci;
     }
     __syncthreads();
-    if (lower) {
-      for (int k = 0; k < rb; ++k) {
-        RT vr = sr[k], vi = si[k];
-        if (tid > k && tid < rb) {
-          T l = D[tid * 65 + k];
-          sr[tid] -= (RT)l.x * vr - (RT)l.y * vi;
-          si[tid] -= (RT)l.x * vi + (RT)l.y * vr;
-        }
-        __syncthreads();
-      }
-    } else {
-      for (int k = rb - 1; k >= 0; --k) {
-        if (tid == 0) {
-          T d = D[k * 65 + k];
-          RT den = (RT)d.x * (RT)d.x + (RT)d.y * (RT)d.y;
-          RT xr = (sr[k] * (RT)d.x + si[k] * (RT)d.y) / den, xi = (si[k] * (RT)d.x - sr[k] * (RT)d.y) / den;
-          sr[k] = xr;
-          si[k] = xi;
-        }
-        __syncthreads();
-        RT vr = sr[k], vi = si[k];
-        if (tid < k) {
-          T u = D[tid * 65 + k];
-          sr[tid] -= (RT)u.x * vr - (RT)u.y * vi;
-          si[tid] -= (RT)u.x * vi + (RT)u.y * vr;
-        }
-        __syncthreads();
-      }
-    }
     if (tid < rb) {
       T o;
-      o.x = sr[tid];
-      o.y = si[tid];
+      o.x = pr[0][tid] + pr[1][tid] + pr[2][tid] + pr[3][tid];
+      o.y = pim[0][tid] + pim[1][tid] + pim[2][tid] + pim[3][tid];
       x[r0 + tid] = o;
     }
     __threadfence();
@@ -567,6 +715,62 @@ __global__ void k_gemv_partial(int64_t n, const T* A, int64_t lda, const double*
   part[2 * (s * n + i)] = sr;
   part[2 * (s * n + i) + 1] = si;
 }
+// x (complex FP64) split into float hi + lo parts: (re_hi, im_hi, re_lo, im_lo)
+__global__ void k_split_x(int64_t n, const double* x, float4* xs) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double xr = x[2 * i], xi = x[2 * i + 1];
+  float rh = (float)xr, ih = (float)xi;
+  xs[i] = make_float4(rh, ih, (float)(xr - (double)rh), (float)(xi - (double)ih));
+}
+
+// s_hi + s_lo += p with the rounding error of the addition kept (TwoSum)
+__device__ __forceinline__ void two_sum_acc(float& sh, float& sl, float p) {
+  float s = __fadd_rn(sh, p);
+  float bb = __fsub_rn(s, sh);
+  float t = __fadd_rn(__fsub_rn(sh, __fsub_rn(s, bb)), __fsub_rn(p, bb));
+  sh = s;
+  sl = __fadd_rn(sl, t);
+}
+
+// partial sums of A x for a c64 matrix with FP64-level accuracy from FP32 arithmetic:
+// each product a * x_hi is split exactly into p + e (e = fma(a, x_hi, -p)), p is added with
+// TwoSum, e and a * x_lo go to the low part (compensated dot product of Ogita, Rump and
+// Oishi, SIAM J. Sci. Comput. 26 (2005)).
+__global__ void k_gemv_partial_c64_df(int64_t n, const float2* A, int64_t lda, const float4* xs,
+                                      double* part) {
+  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  int s = blockIdx.y;
+  int64_t c0 = n * s / MV_SLABS, c1 = n * (s + 1) / MV_SLABS;
+  if (i >= n) return;
+  float shr = 0.f, slr = 0.f, shi = 0.f, sli = 0.f;
+  for (int64_t j = c0; j < c1; ++j) {
+    float2 a = A[i + j * lda];
+    float4 xv = xs[j];
+    float p, e;
+    p = __fmul_rn(a.x, xv.x);
+    e = fmaf(a.x, xv.x, -p);
+    two_sum_acc(shr, slr, p);
+    slr = __fadd_rn(slr, e);
+    p = __fmul_rn(-a.y, xv.y);
+    e = fmaf(-a.y, xv.y, -p);
+    two_sum_acc(shr, slr, p);
+    slr = __fadd_rn(slr, e);
+    slr = __fadd_rn(slr, __fsub_rn(__fmul_rn(a.x, xv.z), __fmul_rn(a.y, xv.w)));
+    p = __fmul_rn(a.x, xv.y);
+    e = fmaf(a.x, xv.y, -p);
+    two_sum_acc(shi, sli, p);
+    sli = __fadd_rn(sli, e);
+    p = __fmul_rn(a.y, xv.x);
+    e = fmaf(a.y, xv.x, -p);
+    two_sum_acc(shi, sli, p);
+    sli = __fadd_rn(sli, e);
+    sli = __fadd_rn(sli, __fadd_rn(__fmul_rn(a.x, xv.w), __fmul_rn(a.y, xv.z)));
+  }
+  part[2 * (s * n + i)] = (double)shr + (double)slr;
+  part[2 * (s * n + i) + 1] = (double)shi + (double)sli;
+}
+
 __global__ void k_gemv_reduce(int64_t n, const double* part, double* y, double alpha, double beta) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -719,7 +923,7 @@ struct LUSteps {
 // applied to the other columns and the trailing matrix gets one rank-NB update
 // (TRSM for U12, GEMM with K = NB -- on the tensor cores for complex FP32).
 template <typename T, typename R>
-int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* info) {
+int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* info, bool pivot) {
   cudaStream_t st = ctx->stream;
   const int G0 = std::max(1, ctx->num_sms);
   const size_t smem_cap = 220 * 1024;
@@ -733,6 +937,10 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   const size_t trsm_smem = (size_t)(nb * nb + 64 * (nb + 1)) * sizeof(T);
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem));
+  const size_t diag_smem = (size_t)nb * (nb + 1) * sizeof(T);
+  const size_t rtrsm_smem = (size_t)(nb * nb + 64 * (nb + 1)) * sizeof(T);
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_getrf_nopiv_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_smem));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_right_upper<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rtrsm_smem));
   int occ = 0;
   BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_panel<T>, 256, panel_smem));
   if (occ < 1) return beast_fail(ctx, BEAST_ERR_CUDA, "panel kernel does not fit on an SM");
@@ -763,21 +971,34 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       int rows_per = (int)((M + G0 - 1) / G0);
       int G = (int)((M + rows_per - 1) / rows_per);
       size_t sm = (size_t)(rows_per * (kb + 1) + kb) * sizeof(T);
-      void* args[] = {&A, &lda, &n, &j0, &kb, &rows_per, &ipiv, &dinfo, &cval, &cidx, &crow, &rowj, &gs};
-      {
-        ProfScope ps(ctx, PK_PANEL, 8.0 * (double)M * kb * kb / 2);
-        BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_panel<T>, G, 256, args, sm, st));
+      if (pivot) {
+        void* args[] = {&A, &lda, &n, &j0, &kb, &rows_per, &ipiv, &dinfo, &cval, &cidx, &crow, &rowj, &gs};
+        {
+          ProfScope ps(ctx, PK_PANEL, 8.0 * (double)M * kb * kb / 2);
+          BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_panel<T>, G, 256, args, sm, st));
+        }
+        // interchanges inside the column block
+        if ((rc = S.laswp(J0, j0, j0, j0 + kb))) break;
+        if ((rc = S.laswp(j0 + kb, J1, j0, j0 + kb))) break;
+      } else {
+        // no pivoting: diagonal block LU, then L21 = A21 U11^{-1} for every row below
+        ProfScope ps(ctx, PK_PANEL, 8.0 * (double)M * kb * kb / 2, 2);
+        k_getrf_nopiv_diag<T><<<1, 256, diag_smem, st>>>(A, lda, j0, kb, dinfo);
+        int64_t rb = n - j0 - kb;
+        if (rb > 0)
+          k_trsm_right_upper<T><<<(unsigned)((rb + 63) / 64), 64, rtrsm_smem, st>>>(A, lda, j0, kb, j0 + kb, n);
+        BEAST_CUDA_TRY(ctx, cudaGetLastError());
       }
-      // interchanges inside the column block, TRSM + GEMM for the rest of the block
-      if ((rc = S.laswp(J0, j0, j0, j0 + kb))) break;
-      if ((rc = S.laswp(j0 + kb, J1, j0, j0 + kb))) break;
+      // TRSM + GEMM for the rest of the block
       if ((rc = S.trsm(j0, kb, j0 + kb, J1))) break;
       if ((rc = S.gemm(j0 + kb, n - j0 - kb, j0 + kb, J1 - j0 - kb, j0, kb, nullptr))) break;
     }
     if (rc) break;
     // the block's interchanges on the columns left and right of it
-    if ((rc = S.laswp(0, J0, J0, J1))) break;
-    if ((rc = S.laswp(J1, n, J0, J1))) break;
+    if (pivot) {
+      if ((rc = S.laswp(0, J0, J0, J1))) break;
+      if ((rc = S.laswp(J1, n, J0, J1))) break;
+    }
     if (J1 < n) {
       // U12 = L11^{-1} A12 (blocked: nb-row TRSM, then GEMM on the rows below inside the block)
       for (int64_t j0 = J0; j0 < J1 && rc == BEAST_OK; j0 += nb) {
@@ -803,26 +1024,33 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   *info = hinfo[0];
   // the sequential interchanges ipiv[0..n) as one permutation: perm[i] = source row of row i
   std::vector<int> hp(n), perm(n);
-  BEAST_CUDA_TRY(ctx, cudaMemcpy(hp.data(), ipiv, n * sizeof(int), cudaMemcpyDeviceToHost));
   for (int64_t i = 0; i < n; ++i) perm[i] = (int)i;
-  for (int64_t k = 0; k < n; ++k) std::swap(perm[k], perm[hp[k]]);
+  if (pivot) {
+    BEAST_CUDA_TRY(ctx, cudaMemcpy(hp.data(), ipiv, n * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int64_t k = 0; k < n; ++k) std::swap(perm[k], perm[hp[k]]);
+  } else {
+    BEAST_CUDA_TRY(ctx, cudaMemcpy(ipiv, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  }
   BEAST_CUDA_TRY(ctx, cudaMemcpy(ipiv + n, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  // inverses of the diagonal blocks for the triangular solves
+  const size_t ism = (size_t)2 * 64 * 65 * sizeof(T);
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_invert_diag<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism));
+  k_invert_diag<T, R><<<(unsigned)((n + 63) / 64), 64, ism, st>>>(A, lda, n, reinterpret_cast<T*>(lu_dinv(ipiv, n)));
+  BEAST_CUDA_TRY(ctx, cudaGetLastError());
   return BEAST_OK;
 }
 
 template <typename T, typename RT>
 int lu_solve_t(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* perm, T* B,
-               int64_t ldb, int64_t nrhs) {
+               int64_t ldb, int64_t nrhs, const T* dinv) {
   cudaStream_t st = ctx->stream;
   const int nblk = (int)((n + 63) / 64);
   T* tmp = nullptr;
   int* flags = nullptr;
   BEAST_CUDA_TRY(ctx, cudaMallocAsync(&tmp, (size_t)n * sizeof(T), st));
   BEAST_CUDA_TRY(ctx, cudaMallocAsync(&flags, (size_t)2 * nblk * sizeof(int) + 16, st));
-  const size_t dsm = (size_t)64 * 65 * sizeof(T);
-  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsv_wave<T, RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
   int occ = 0;
-  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, dsm));
+  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, 0));
   int G = std::max(1, std::min(nblk, ctx->num_sms * std::max(occ, 1)));
   int* status = ctx->d_flag;
   for (int64_t r = 0; r < nrhs; ++r) {
@@ -834,11 +1062,11 @@ int lu_solve_t(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* pe
     k_permute<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tmp, b, perm, n);
     int lower = 1;
     int* fl = flags;
-    void* args[] = {&A, &lda, &n, &b, &lower, &fl, &status};
-    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, dsm, st));
+    void* args[] = {&A, &lda, &n, &b, &lower, &fl, &status, &dinv};
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
     lower = 0;
     fl = flags + nblk;
-    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, dsm, st));
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
   }
   BEAST_CUDA_TRY(ctx, cudaGetLastError());
   BEAST_CUDA_TRY(ctx, cudaFreeAsync(tmp, st));
@@ -856,15 +1084,13 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_MAX_N *
 
 template <typename T, typename RT>
 int lu_solve_fixed_scratch(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* perm, T* B,
-                           int64_t ldb, int64_t nrhs, unsigned char* scratch) {
+                           int64_t ldb, int64_t nrhs, unsigned char* scratch, const T* dinv) {
   cudaStream_t st = ctx->stream;
   const int nblk = (int)((n + 63) / 64);
   T* tmp = reinterpret_cast<T*>(scratch);
   int* flags = reinterpret_cast<int*>(scratch + NOALLOC_MAX_N * 16);
-  const size_t dsm = (size_t)64 * 65 * sizeof(T);
-  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsv_wave<T, RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm));
   int occ = 0;
-  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, dsm));
+  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, 0));
   int G = std::max(1, std::min(nblk, ctx->num_sms * std::max(occ, 1)));
   int* status = ctx->d_flag;
   for (int64_t r = 0; r < nrhs; ++r) {
@@ -875,11 +1101,11 @@ int lu_solve_fixed_scratch(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, c
     k_permute<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tmp, b, perm, n);
     int lower = 1;
     int* fl = flags;
-    void* args[] = {&A, &lda, &n, &b, &lower, &fl, &status};
-    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, dsm, st));
+    void* args[] = {&A, &lda, &n, &b, &lower, &fl, &status, &dinv};
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
     lower = 0;
     fl = flags + nblk;
-    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, dsm, st));
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
   }
   BEAST_CUDA_TRY(ctx, cudaGetLastError());
   return BEAST_OK;
@@ -887,17 +1113,20 @@ int lu_solve_fixed_scratch(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, c
 
 }  // namespace
 
-int lu_factor_dev(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, int* ipiv, int* info) {
-  if (dtype == BEAST_C64) return lu_factor_t<float2, float>(ctx, n, (float2*)A, lda, ipiv, info);
-  return lu_factor_t<double2, double>(ctx, n, (double2*)A, lda, ipiv, info);
+int lu_factor_dev(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, int* ipiv, int* info,
+                  bool pivot) {
+  if (dtype == BEAST_C64) return lu_factor_t<float2, float>(ctx, n, (float2*)A, lda, ipiv, info, pivot);
+  return lu_factor_t<double2, double>(ctx, n, (double2*)A, lda, ipiv, info, pivot);
 }
 
 // ipiv holds 2n ints: the pivots, then the permutation built by lu_factor_dev
 int lu_solve_dev(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int dtype, const int* ipiv,
                  void* B, int64_t ldb, int64_t nrhs) {
   if (dtype == BEAST_C64)
-    return lu_solve_t<float2, float>(ctx, n, (const float2*)A, lda, ipiv + n, (float2*)B, ldb, nrhs);
-  return lu_solve_t<double2, double>(ctx, n, (const double2*)A, lda, ipiv + n, (double2*)B, ldb, nrhs);
+    return lu_solve_t<float2, float>(ctx, n, (const float2*)A, lda, ipiv + n, (float2*)B, ldb, nrhs,
+                                     (const float2*)lu_dinv(ipiv, n));
+  return lu_solve_t<double2, double>(ctx, n, (const double2*)A, lda, ipiv + n, (double2*)B, ldb, nrhs,
+                                     (const double2*)lu_dinv(ipiv, n));
 }
 
 static double* g_part = nullptr;
@@ -905,7 +1134,7 @@ static size_t g_part_size = 0;
 
 cudaError_t gemv_dev(int64_t n, const void* A, int64_t lda, int a_c64, const double* x, double* y,
                      double alpha, double beta, cudaStream_t st) {
-  size_t need = (size_t)MV_SLABS * n * 2 * sizeof(double);
+  size_t need = (size_t)MV_SLABS * n * 2 * sizeof(double) + (size_t)n * sizeof(float4) + 256;
   if (need > g_part_size) {
     if (g_part) cudaFree(g_part);
     cudaError_t e = cudaMalloc(&g_part, need);
@@ -917,9 +1146,11 @@ cudaError_t gemv_dev(int64_t n, const void* A, int64_t lda, int a_c64, const dou
     g_part_size = need;
   }
   dim3 g((unsigned)((n + 127) / 128), MV_SLABS);
-  if (a_c64)
-    k_gemv_partial<float2><<<g, 128, 0, st>>>(n, (const float2*)A, lda, x, g_part);
-  else
+  if (a_c64) {
+    float4* xs = reinterpret_cast<float4*>(g_part + (size_t)MV_SLABS * n * 2);
+    k_split_x<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x, xs);
+    k_gemv_partial_c64_df<<<g, 128, 0, st>>>(n, (const float2*)A, lda, xs, g_part);
+  } else
     k_gemv_partial<double2><<<g, 128, 0, st>>>(n, (const double2*)A, lda, x, g_part);
   k_gemv_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, g_part, y, alpha, beta);
   return cudaGetLastError();
@@ -998,10 +1229,12 @@ extern "C" int beast_lu_solve_noalloc(beast_ctx* ctx, const beast_lu* lu, int64_
   int rc;
   if (lu->dtype == BEAST_C64)
     rc = lu_solve_fixed_scratch<float2, float>(ctx, lu->n, (const float2*)lu->A, lu->lda, lu->ipiv + lu->n,
-                                               (float2*)B, ldb, nrhs, scratch);
+                                               (float2*)B, ldb, nrhs, scratch,
+                                               (const float2*)lu_dinv(lu->ipiv, lu->n));
   else
     rc = lu_solve_fixed_scratch<double2, double>(ctx, lu->n, (const double2*)lu->A, lu->lda,
-                                                 lu->ipiv + lu->n, (double2*)B, ldb, nrhs, scratch);
+                                                 lu->ipiv + lu->n, (double2*)B, ldb, nrhs, scratch,
+                                                 (const double2*)lu_dinv(lu->ipiv, lu->n));
   if (rc) return rc;
   BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
   int status = 0;

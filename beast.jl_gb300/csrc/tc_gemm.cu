@@ -17,6 +17,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 
+#include <algorithm>
 #include <cstring>
 
 #include "internal.h"
@@ -27,6 +28,7 @@ constexpr int TM = 128, TN = 256, TK = 32;  // tile M (real rows), N, K per stag
 constexpr int STAGES = 4;
 constexpr int A_BYTES = TM * TK * 4, B_BYTES = TN * TK * 4, STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int MAX_CTAS = 1024;
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -54,12 +56,16 @@ __device__ __forceinline__ bool mbar_test(uint32_t bar, uint32_t parity) {
   return ok != 0;
 }
 
-// bounded wait on an mbarrier phase; false (and status bit 4) on timeout
-__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* status) {
+// bounded wait on an mbarrier phase; false (status bit 4, CTA abort flag raised) on timeout,
+// and false at once when another role of the CTA has already given up
+__device__ __forceinline__ bool mbar_wait(uint32_t bar, uint32_t parity, int* status,
+                                          volatile int* abort) {
   long long t0 = clock64();
   while (!mbar_test(bar, parity)) {
+    if (*abort) return false;
     if (clock64() - t0 > WAIT_CYCLES) {
       atomicOr(status, 4);
+      *abort = 1;
       return false;
     }
   }
@@ -120,9 +126,13 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
-// C' (real view, ldc floats) -= A' B' for a tile grid over (m_rows x n_cols);
-// c_row0 / c_col0: position of the update block inside C'
-__global__ void __launch_bounds__(128, 1)
+// C' (real view, ldc floats) -= A' B' over a grid of 128 x 256 tiles, persistent CTAs.
+// Warp roles: warp 0 lane 0 issues TMA loads into a STAGES-deep ring, warp 1 lane 0 issues
+// tcgen05.mma into one of two 256-column TMEM accumulators, warps 2..5 drain the other
+// accumulator (tcgen05.ld -> C' -= D) so that the epilogue of tile t overlaps the loads and
+// MMAs of tile t+1.  Barriers: full/empty per stage (TMA <-> MMA), tfull/tempty per
+// accumulator (MMA <-> epilogue).  Tiles are visited N-fastest (B' stays in L2).
+__global__ void __launch_bounds__(192, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               float* C, int64_t ldc, int64_t c_row0, int64_t c_col0, int m_rows, int n_cols,
               int b_x0, int b_y0, int nk, int* status) {
@@ -130,20 +140,32 @@ __global__ void __launch_bounds__(128, 1)
   const uint32_t base = (smem_u32(smraw) + 1023u) & ~1023u;
   unsigned char* gbase = smraw + (base - smem_u32(smraw));
   uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + STAGES * STAGE_BYTES);
-  // bars[0..STAGES): full, bars[STAGES..2*STAGES): empty, bars[2*STAGES]: done
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 1);
-  __shared__ int s_abort;
+  // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2], done
+  const int B_FULL = 0, B_EMPTY = STAGES, B_TFULL = 2 * STAGES, B_TEMPTY = 2 * STAGES + 2,
+            B_DONE = 2 * STAGES + 4;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
+  __shared__ int s_abort_mem;
+  volatile int* s_abort = &s_abort_mem;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int m0 = blockIdx.y * TM, n0 = blockIdx.x * TN;
+  const int ntn = (n_cols + TN - 1) / TN, ntm = (m_rows + TM - 1) / TM;
+  const int ntiles = ntn * ntm;
 
   if (threadIdx.x == 0) {
-    s_abort = 0;
-    for (int s = 0; s < 2 * STAGES + 1; ++s) mbar_init(smem_u32(bars + s), 1);
+    *s_abort = 0;
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(smem_u32(bars + B_FULL + s), 1);
+      mbar_init(smem_u32(bars + B_EMPTY + s), 1);
+    }
+    for (int a = 0; a < 2; ++a) {
+      mbar_init(smem_u32(bars + B_TFULL + a), 1);
+      mbar_init(smem_u32(bars + B_TEMPTY + a), 4);  // one arrival per epilogue warp
+    }
+    mbar_init(smem_u32(bars + B_DONE), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(tmem_slot)),
-                 "r"(TN)
+                 "r"(2 * TN)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -152,80 +174,98 @@ __global__ void __launch_bounds__(128, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  if (threadIdx.x == 0) {
-    const uint32_t idesc = idesc_tf32();
-    bool ok = true;
-    // prologue: fill the ring
-    for (int kb = 0; kb < nk && kb < STAGES; ++kb) {
-      uint32_t sa = base + kb * STAGE_BYTES, sb = sa + A_BYTES;
-      uint32_t full = smem_u32(bars + kb);
-      mbar_expect_tx(full, STAGE_BYTES);
-      tma_load_2d(sa, &tmA, kb * TK, m0, full);
-      tma_load_2d(sb, &tmB, b_x0 + kb * TK, b_y0 + n0, full);
-    }
-    for (int kb = 0; kb < nk && ok; ++kb) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (kb / STAGES) & 1;
-      if (!mbar_wait(smem_u32(bars + s), ph, status)) {
-        ok = false;
-        break;
-      }
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const uint32_t sa = base + s * STAGE_BYTES, sb = sa + A_BYTES;
-#pragma unroll
-      for (int kk = 0; kk < TK / 8; ++kk)
-        mma_tf32(tmem, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), idesc, (kb | kk) ? 1u : 0u);
-      mma_commit(smem_u32(bars + STAGES + s));
-      const int nxt = kb + STAGES;
-      if (nxt < nk) {
-        // the stage is reloaded once the MMAs that read it have completed
-        if (!mbar_wait(smem_u32(bars + STAGES + s), ph, status)) {
-          ok = false;
-          break;
-        }
-        uint32_t full = smem_u32(bars + s);
+  if (warp == 0 && lane == 0) {
+    // ---- TMA producer
+    uint32_t it = 0;
+    for (int tile = blockIdx.x; tile < ntiles && !*s_abort; tile += gridDim.x) {
+      const int m0 = (tile / ntn) * TM, n0 = (tile % ntn) * TN;
+      for (int kb = 0; kb < nk; ++kb, ++it) {
+        const int s = it % STAGES;
+        const uint32_t ph = (it / STAGES) & 1;
+        if (!mbar_wait(smem_u32(bars + B_EMPTY + s), ph ^ 1, status, s_abort)) break;
+        const uint32_t sa = base + s * STAGE_BYTES, sb = sa + A_BYTES;
+        const uint32_t full = smem_u32(bars + B_FULL + s);
         mbar_expect_tx(full, STAGE_BYTES);
-        tma_load_2d(sa, &tmA, nxt * TK, m0, full);
-        tma_load_2d(sb, &tmB, b_x0 + nxt * TK, b_y0 + n0, full);
+        tma_load_2d(sa, &tmA, kb * TK, m0, full);
+        tma_load_2d(sb, &tmB, b_x0 + kb * TK, b_y0 + n0, full);
       }
     }
-    // the done barrier tracks every MMA issued above (also after an abort, so that no
-    // MMA is in flight when the accumulator is released)
-    mma_commit(smem_u32(bars + 2 * STAGES));
-    if (!ok) s_abort = 1;
-  }
-  __syncthreads();
-  bool have = mbar_wait(smem_u32(bars + 2 * STAGES), 0, status) && !s_abort;
-  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-  if (have) {
-    // epilogue: warp w owns TMEM lanes (= tile rows) 32w .. 32w+31; 64 columns per round
-    // with all 64 loads of C issued before the stores
-    const int row = m0 + warp * 32 + lane;
-    const bool row_ok = row < m_rows;
-    float* __restrict__ crow = C + (c_row0 + row);
-    for (int c0 = 0; c0 < TN; c0 += 64) {
-      float v[64], c[64];
+    // no copy may still be landing in shared memory when the CTA exits: wait (bounded,
+    // whatever the abort state) for the last load issued into each stage
+    int no_abort = 0;
+    for (uint32_t j = it > (uint32_t)STAGES ? it - STAGES : 0; j < it; ++j)
+      mbar_wait(smem_u32(bars + B_FULL + j % STAGES), (j / STAGES) & 1, status, &no_abort);
+  } else if (warp == 1 && lane == 0) {
+    // ---- MMA issuer
+    const uint32_t idesc = idesc_tf32();
+    uint32_t it = 0;
+    int t = 0;
+    for (int tile = blockIdx.x; tile < ntiles && !*s_abort; tile += gridDim.x, ++t) {
+      const int a = t & 1;
+      const uint32_t aph = (t >> 1) & 1;
+      if (!mbar_wait(smem_u32(bars + B_TEMPTY + a), aph ^ 1, status, s_abort)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const uint32_t acc = tmem + (uint32_t)(a * TN);
+      for (int kb = 0; kb < nk; ++kb, ++it) {
+        const int s = it % STAGES;
+        const uint32_t ph = (it / STAGES) & 1;
+        if (!mbar_wait(smem_u32(bars + B_FULL + s), ph, status, s_abort)) break;
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t sa = base + s * STAGE_BYTES, sb = sa + A_BYTES;
 #pragma unroll
-      for (int q = 0; q < 4; ++q) tmem_ld16(tmem + ((uint32_t)(warp * 32) << 16) + (uint32_t)(c0 + 16 * q), v + 16 * q);
-      if (row_ok) {
+        for (int kk = 0; kk < TK / 8; ++kk)
+          mma_tf32(acc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), idesc, (kb | kk) ? 1u : 0u);
+        mma_commit(smem_u32(bars + B_EMPTY + s));
+      }
+      if (*s_abort) break;
+      mma_commit(smem_u32(bars + B_TFULL + a));
+    }
+    // every MMA issued above has completed once this barrier phase does (waited for even
+    // after an abort, with its own budget, so that no MMA runs when TMEM is released)
+    mma_commit(smem_u32(bars + B_DONE));
+    int no_abort = 0;
+    mbar_wait(smem_u32(bars + B_DONE), 0, status, &no_abort);
+  } else if (warp >= 2) {
+    // ---- epilogue: warp w drains TMEM lanes 32*(w%4) .. +31 (= tile rows)
+    const int q = warp & 3;
+    int t = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
+      const int a = t & 1;
+      const uint32_t aph = (t >> 1) & 1;
+      if (!mbar_wait(smem_u32(bars + B_TFULL + a), aph, status, s_abort)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int m0 = (tile / ntn) * TM, n0 = (tile % ntn) * TN;
+      const int row = m0 + q * 32 + lane;
+      const bool row_ok = row < m_rows;
+      float* __restrict__ crow = C + (c_row0 + row);
+      const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * TN);
+      for (int c0 = 0; c0 < TN; c0 += 64) {
+        float v[64], c[64];
 #pragma unroll
-        for (int i = 0; i < 64; ++i) {
-          int col = n0 + c0 + i;
-          c[i] = col < n_cols ? __ldcs(crow + (c_col0 + col) * ldc) : 0.f;
-        }
+        for (int k = 0; k < 4; ++k) tmem_ld16(tbase + (uint32_t)(c0 + 16 * k), v + 16 * k);
+        if (row_ok) {
 #pragma unroll
-        for (int i = 0; i < 64; ++i) {
-          int col = n0 + c0 + i;
-          if (col < n_cols) __stcs(crow + (c_col0 + col) * ldc, c[i] - v[i]);
+          for (int i = 0; i < 64; ++i) {
+            int col = n0 + c0 + i;
+            c[i] = col < n_cols ? __ldcs(crow + (c_col0 + col) * ldc) : 0.f;
+          }
+#pragma unroll
+          for (int i = 0; i < 64; ++i) {
+            int col = n0 + c0 + i;
+            if (col < n_cols) __stcs(crow + (c_col0 + col) * ldc, c[i] - v[i]);
+          }
         }
       }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bars + B_TEMPTY + a)) : "memory");
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (warp == 0) {
+  if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TN) : "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TN) : "memory");
   }
 }
 
@@ -318,9 +358,10 @@ int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t n_total, int64
   if (!make_map(&tmB, real, (uint64_t)2 * n_total, (uint64_t)n_total, (uint64_t)2 * lda * 4, TK, TN))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (B') failed");
   const int m_rows = (int)(2 * M), n_cols = (int)N;
-  dim3 grid((unsigned)((n_cols + TN - 1) / TN), (unsigned)((m_rows + TM - 1) / TM));
+  const int ntiles = ((n_cols + TN - 1) / TN) * ((m_rows + TM - 1) / TM);
+  const int grid = std::min(ntiles, std::max(1, ctx->num_sms));
   const int nk = (2 * K) / TK;
-  k_tc_gemm<<<grid, 128, SMEM_BYTES, st>>>(tmA, tmB, reinterpret_cast<float*>(Mat), 2 * lda, 2 * rowA,
+  k_tc_gemm<<<grid, 192, SMEM_BYTES, st>>>(tmA, tmB, reinterpret_cast<float*>(Mat), 2 * lda, 2 * rowA,
                                            colB, m_rows, n_cols, (int)(2 * colA), (int)colB, nk,
                                            ctx->d_flag);
   BEAST_CUDA_TRY(ctx, cudaGetLastError());

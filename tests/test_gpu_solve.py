@@ -91,3 +91,29 @@ def test_lu_factors_exact(n, dtype):
     ctx.lib.beast_lu_free(h)
     assert np.abs(np.tril(F, -1) - np.tril(L, -1)).max() == 0.0
     assert np.abs(np.triu(F) - U).max() == 0.0
+
+
+def test_mixed_c64_matrix_refines_to_fp64_residual():
+    """with a c64 matrix the residual matvec is a compensated (double-float) dot product:
+    refinement must reach an FP64-level residual of the stored matrix"""
+    import torch
+    rng = np.random.default_rng(3)
+    n = 1500
+    A = (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)) + 3 * n ** 0.5 * np.eye(n)).astype(np.complex64)
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda().T
+    x, it, res = bg.solve(At, b, precision=bg.MIXED, tol=1e-13)
+    r = A.astype(np.complex128) @ x - b
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-12
+    assert res < 1e-12
+
+
+def test_mixed_falls_back_to_pivoting():
+    """a zero leading pivot: the unpivoted mixed factorisation must hand over to partial pivoting"""
+    rng = np.random.default_rng(4)
+    n = 900
+    A = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    A[0, 0] = 0.0
+    b = rng.normal(size=n) + 0j
+    x, it, res = bg.solve(A.astype(np.complex64), b, precision=bg.MIXED, tol=1e-10)
+    assert np.linalg.norm(A.astype(np.complex64).astype(np.complex128) @ x - b) / np.linalg.norm(b) < 1e-9
