@@ -16,7 +16,7 @@ FP64, MIXED = 0, 1
 C128, C64 = 0, 1
 HOST, DEVICE = 0, 1
 PROF_KINDS = ["geometry", "far", "near", "gather", "local", "rhs", "farfield", "lu_panel",
-              "lu_laswp", "lu_trsm", "lu_gemm", "trsv", "gemv", "vec", "convert"]
+              "lu_laswp", "lu_trsm", "lu_gemm", "trsv", "gemv", "vec", "convert", "lu_tc_gemm"]
 
 
 class BeastError(RuntimeError):

@@ -287,6 +287,18 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
   const int rec = QREC_HDR + 4 * ni;
   const int q0 = blockIdx.y * FAR_QT;
   const int nqt = min(FAR_QT, P.nq - q0);
+  // rule points in the arithmetic type, converted once per CTA (a double -> float conversion
+  // runs on the FP64 pipe)
+  __shared__ R ro_s[3 * RULE_MAXPTS], ri_s[2 * RULE_MAXPTS];
+  for (int k = threadIdx.x; k < P.ro.n; k += blockDim.x) {
+    ro_s[3 * k] = (R)P.ro.u[k];
+    ro_s[3 * k + 1] = (R)P.ro.v[k];
+    ro_s[3 * k + 2] = (R)P.ro.w[k];
+  }
+  for (int k = threadIdx.x; k < ni; k += blockDim.x) {
+    ri_s[2 * k] = (R)P.ri.u[k];
+    ri_s[2 * k + 1] = (R)P.ri.v[k];
+  }
   // ---- stage trial cells
   for (int k = threadIdx.x; k < nqt * (1 + ni); k += blockDim.x) {
     int qi = k / (1 + ni), b = k % (1 + ni);
@@ -330,6 +342,8 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
   const double Ap = tg[15];
   const R radp = (R)P.tgeof[4 * p + 3];
   const R gr = (R)P.op.gr, gi = (R)P.op.gi;
+  const C2<R> alpha{(R)P.op.ar, (R)P.op.ai}, beta{(R)P.op.br, (R)P.op.bi};
+  const R ApR = (R)Ap;
   const int nst = (TK == BEAST_P0) ? 1 : 3, nsb = (BK == BEAST_P0) ? 1 : 3;
   const int no = P.ro.n;
 
@@ -368,11 +382,11 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
       CV<R> V1, V2, V3_, V4, V5, V6;                   // vector moments
       cv_zero(V1); cv_zero(V2); cv_zero(V3_); cv_zero(V4); cv_zero(V5); cv_zero(V6);
       for (int a = 0; a < no; ++a) {
-        const R ua = (R)P.ro.u[a], va = (R)P.ro.v[a], wa3 = (R)1 - ua - va;
+        const R ua = ro_s[3 * a], va = ro_s[3 * a + 1], wa3 = (R)1 - ua - va;
         const V3<R> xi = mk(ua * tau[0].x + va * tau[1].x + wa3 * tau[2].x,
                             ua * tau[0].y + va * tau[1].y + wa3 * tau[2].y,
                             ua * tau[0].z + va * tau[1].z + wa3 * tau[2].z);
-        const R wa = (R)P.ro.w[a];
+        const R wa = ro_s[3 * a + 2];
         const V3<R> dx = d + xi;
         // inner sums over trial points: U0 = sum w K, U1 = sum w K eta,
         // U2 = sum w K eta (n.eta), U3 = sum w K (n.eta)   (K = G or grad coefficient)
@@ -469,8 +483,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
             // alpha/4 (Mxe - Mx.s - t.Me + (t.s) M0) + beta M0
             C2<R> f = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
             f = cadd(f, cscale(dot(ti, sj), M0));
-            C2<R> al{(R)P.op.ar, (R)P.op.ai}, be{(R)P.op.br, (R)P.op.bi};
-            z = cadd(cscale((R)0.25, cmul(al, f)), cmul(be, M0));
+            z = cadd(cscale((R)0.25, cmul(alpha, f)), cmul(beta, M0));
           } else if (OPK == BEAST_MW_DL) {
             // 1/4 [D0 - Dxr.s - t.Drh + (s x t).Dr]
             C2<R> f = csub(csub(M0, rdot(sj, V1)), rdot(ti, V2));
@@ -497,12 +510,12 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
       for (int k = 0; k < 9; ++k) acc[k] = C2<R>{0, 0};
       const V3<R> nq = mk(rq[15], rq[16], rq[17]);
       for (int a = 0; a < no; ++a) {
-        const R ua = (R)P.ro.u[a], va = (R)P.ro.v[a], wa3 = (R)1 - ua - va;
+        const R ua = ro_s[3 * a], va = ro_s[3 * a + 1], wa3 = (R)1 - ua - va;
         const V3<R> xi = mk(ua * tau[0].x + va * tau[1].x + wa3 * tau[2].x,
                             ua * tau[0].y + va * tau[1].y + wa3 * tau[2].y,
                             ua * tau[0].z + va * tau[1].z + wa3 * tau[2].z);
         const R lt[3] = {ua, va, wa3};
-        const R wa = (R)P.ro.w[a];
+        const R wa = ro_s[3 * a + 2];
         const V3<R> dx = d + xi;
         for (int b = 0; b < ni; ++b) {
           const R* pb = pts + 4 * b;
@@ -514,7 +527,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
           const R Rr = R2 * iR;
           C2<R> G = green<R>(gr, gi, Rr, iR);
           C2<R> K;
-          C2<R> al{(R)P.op.ar, (R)P.op.ai};
+          const C2<R> al = alpha;
           if (OPK == BEAST_HH_SL) {
             K = cmul(al, G);
           } else {
@@ -526,8 +539,8 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
               K = cscale(dot(nn, r), c);
           }
           K = cscale(wb, K);
-          const double ub = P.ri.u[b], vb = P.ri.v[b];
-          const R lb[3] = {(R)ub, (R)vb, (R)(1.0 - ub - vb)};
+          const R ub = ri_s[2 * b], vb = ri_s[2 * b + 1];
+          const R lb[3] = {ub, vb, (R)1 - ub - vb};
           for (int i = 0; i < nst; ++i)
             for (int j = 0; j < nsb; ++j) {
               R s = (TK == BEAST_P0 ? (R)1 : lt[i]) * (BK == BEAST_P0 ? (R)1 : lb[j]);
@@ -535,7 +548,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
             }
         }
       }
-      const R ApAq = (R)Ap * Aq;
+      const R ApAq = ApR * Aq;
       for (int i = 0; i < nst; ++i)
         for (int j = 0; j < nsb; ++j)
           store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * p + i,

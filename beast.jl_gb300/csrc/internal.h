@@ -20,7 +20,7 @@
 // kernel classes timed by the optional profiler (beast_prof_*)
 enum {
   PK_GEOM = 0, PK_FAR, PK_NEAR, PK_GATHER, PK_LOCAL, PK_RHS, PK_FARFIELD, PK_PANEL, PK_LASWP,
-  PK_TRSM, PK_GEMM, PK_TRSV, PK_GEMV, PK_VEC, PK_CONVERT, PK_COUNT
+  PK_TRSM, PK_GEMM, PK_TRSV, PK_GEMV, PK_VEC, PK_CONVERT, PK_TCGEMM, PK_COUNT
 };
 struct ProfRec {
   int kind;

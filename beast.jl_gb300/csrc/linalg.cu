@@ -7,7 +7,7 @@
 //              and the rank-1 update, with bounded-spin grid barriers (a barrier that gives
 //              up sets a status word and the kernel returns; nothing hangs)
 //   k_laswp    the panel's row interchanges applied to the other columns
-//   k_trsm     U12 = L11^{-1} A12
+//   k_trsm_warp / k_trsm_right_warp   U12 = L11^{-1} A12 and (unpivoted path) L21 = A21 U11^{-1}
 //   k_gemm     A22 -= L21 U12 (complex, tiled through shared memory)
 // The element type is complex FP64 (c128) or complex FP32 (c64).
 #include <cuda_runtime.h>
@@ -284,44 +284,6 @@ __global__ void k_laswp(T* A, int64_t lda, int64_t c0, int64_t c1, int64_t p0, i
   }
 }
 
-// ---- U12 = L11^{-1} A12 (unit lower): a CTA solves 64 columns held in shared memory ---
-// L11 = A[j0:j0+nb, j0:j0+nb], right-hand sides = columns [c0, c1) of rows j0:j0+nb
-template <typename T>
-__global__ void k_trsm(T* A, int64_t lda, int64_t j0, int nb, int64_t c0g, int64_t c1) {
-  extern __shared__ unsigned char smraw[];
-  T* L = reinterpret_cast<T*>(smraw);       // nb x nb (column-major)
-  T* B = L + nb * nb;                        // nb rows x 64 columns, column stride nb + 1
-  const int ldb = nb + 1;
-  const int64_t c0 = c0g + (int64_t)blockIdx.x * 64;
-  const int ncol = (int)(c1 - c0 < 64 ? c1 - c0 : 64);
-  for (int k = threadIdx.x; k < nb * nb; k += blockDim.x) {
-    int r = k % nb, c = k / nb;
-    L[k] = A[(j0 + r) + (j0 + c) * lda];
-  }
-  for (int e = threadIdx.x; e < nb * ncol; e += blockDim.x) {
-    int r = e % nb, c = e / nb;
-    B[c * ldb + r] = A[(j0 + r) + (c0 + c) * lda];
-  }
-  __syncthreads();
-  const int c = threadIdx.x;
-  if (c < ncol) {
-    T* b = B + c * ldb;
-    for (int k = 0; k < nb; ++k) {
-      T bk = b[k];
-      for (int i = k + 1; i < nb; ++i) {
-        T l = L[i + k * nb];
-        T bi = b[i];
-        b[i] = cmk<T>(bi.x - (l.x * bk.x - l.y * bk.y), bi.y - (l.x * bk.y + l.y * bk.x));
-      }
-    }
-  }
-  __syncthreads();
-  for (int e = threadIdx.x; e < nb * ncol; e += blockDim.x) {
-    int r = e % nb, cc = e / nb;
-    A[(j0 + r) + (c0 + cc) * lda] = B[cc * ldb + r];
-  }
-}
-
 // ---- LU without pivoting (mixed path) ----------------------------------------------------
 // Diagonal block A[j0:j0+kb, j0:j0+kb] = L11 U11 in place, one CTA; a zero pivot sets *info.
 template <typename T>
@@ -367,47 +329,100 @@ __global__ void __launch_bounds__(256) k_getrf_nopiv_diag(T* A, int64_t lda, int
   }
 }
 
-// L21 = A21 U11^{-1} for rows [r0, r1): x U11 = a per row, 64 rows per CTA (thread per row)
-template <typename T>
-__global__ void k_trsm_right_upper(T* A, int64_t lda, int64_t j0, int kb, int64_t r0g, int64_t r1) {
+// U12 = L11^{-1} A12 (unit lower L11 = A[j0:j0+kb, j0:j0+kb]) for columns [c0, c1) by forward
+// substitution: one warp per column (lane l owns rows l and l + 32), the solved entry is
+// broadcast with a shuffle; 8 warps per CTA, 64 columns per CTA, L11 in shared memory.
+template <typename T, typename RT>
+__global__ void __launch_bounds__(256) k_trsm_warp(T* A, int64_t lda, int64_t j0, int kb, int64_t c0g,
+                                                   int64_t c1) {
   extern __shared__ unsigned char smraw[];
-  T* U = reinterpret_cast<T*>(smraw);   // kb x kb column-major
-  T* X = U + kb * kb;                   // 64 rows x (kb + 1)
-  typedef decltype(U[0].x) RT;
-  const int ldx = kb + 1;
-  const int64_t r0 = r0g + (int64_t)blockIdx.x * 64;
-  const int nr = (int)(r1 - r0 < 64 ? r1 - r0 : 64);
+  T* L = reinterpret_cast<T*>(smraw);  // kb x kb column-major
   for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
     int r = e % kb, c = e / kb;
-    U[e] = A[(j0 + r) + (j0 + c) * lda];
-  }
-  for (int e = threadIdx.x; e < nr * kb; e += blockDim.x) {
-    int r = e % nr, c = e / nr;
-    X[r * ldx + c] = A[(r0 + r) + (j0 + c) * lda];
+    L[c * kb + r] = A[(j0 + r) + (j0 + c) * lda];
   }
   __syncthreads();
-  const int t = threadIdx.x;
-  if (t < nr) {
-    T* x = X + t * ldx;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t cbase = c0g + (int64_t)blockIdx.x * 64;
+  for (int cc = warp; cc < 64; cc += 8) {
+    const int64_t col = cbase + cc;
+    if (col >= c1) break;
+    T* b = A + j0 + col * lda;
+    T v0, v1;
+    v0.x = v0.y = v1.x = v1.y = 0;
+    if (lane < kb) v0 = b[lane];
+    if (lane + 32 < kb) v1 = b[lane + 32];
     for (int k = 0; k < kb; ++k) {
-      T s = x[k];
-      for (int i = 0; i < k; ++i) {
-        T xi = x[i], u = U[i + k * kb];
-        s.x -= xi.x * u.x - xi.y * u.y;
-        s.y -= xi.x * u.y + xi.y * u.x;
+      RT bx = __shfl_sync(0xffffffffu, k < 32 ? v0.x : v1.x, k & 31);
+      RT by = __shfl_sync(0xffffffffu, k < 32 ? v0.y : v1.y, k & 31);
+      if (lane > k && lane < kb) {
+        T l = L[k * kb + lane];
+        v0.x -= l.x * bx - l.y * by;
+        v0.y -= l.x * by + l.y * bx;
       }
-      T d = U[k + k * kb];
-      RT den = d.x * d.x + d.y * d.y;
-      T q;
-      q.x = (s.x * d.x + s.y * d.y) / den;
-      q.y = (s.y * d.x - s.x * d.y) / den;
-      x[k] = q;
+      if (lane + 32 > k && lane + 32 < kb) {
+        T l = L[k * kb + lane + 32];
+        v1.x -= l.x * bx - l.y * by;
+        v1.y -= l.x * by + l.y * bx;
+      }
     }
+    if (lane < kb) b[lane] = v0;
+    if (lane + 32 < kb) b[lane + 32] = v1;
+  }
+}
+
+// L21 = A21 U11^{-1} (upper U11 = A[j0:j0+kb, j0:j0+kb]) for rows [r0, r1) by substitution
+// along each row: one warp per row (lane l owns columns l and l + 32), 64 rows per CTA.
+template <typename T, typename RT>
+__global__ void __launch_bounds__(256) k_trsm_right_warp(T* A, int64_t lda, int64_t j0, int kb, int64_t r0g,
+                                                         int64_t r1) {
+  extern __shared__ unsigned char smraw[];
+  T* U = reinterpret_cast<T*>(smraw);  // kb x kb, U[k * kb + c] = row k, column c
+  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
+    int r = e % kb, c = e / kb;
+    U[r * kb + c] = A[(j0 + r) + (j0 + c) * lda];
   }
   __syncthreads();
-  for (int e = threadIdx.x; e < nr * kb; e += blockDim.x) {
-    int r = e % nr, c = e / nr;
-    A[(r0 + r) + (j0 + c) * lda] = X[r * ldx + c];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t rbase = r0g + (int64_t)blockIdx.x * 64;
+  for (int rr = warp; rr < 64; rr += 8) {
+    const int64_t row = rbase + rr;
+    if (row >= r1) break;
+    T v0, v1;
+    v0.x = v0.y = v1.x = v1.y = 0;
+    if (lane < kb) v0 = A[row + (j0 + lane) * lda];
+    if (lane + 32 < kb) v1 = A[row + (j0 + lane + 32) * lda];
+    for (int k = 0; k < kb; ++k) {
+      // owner of column k finishes x_k = acc_k / U_kk
+      T d = U[k * kb + k];
+      RT den = d.x * d.x + d.y * d.y;
+      if (k < 32 && lane == k) {
+        T q;
+        q.x = (v0.x * d.x + v0.y * d.y) / den;
+        q.y = (v0.y * d.x - v0.x * d.y) / den;
+        v0 = q;
+      }
+      if (k >= 32 && lane == k - 32) {
+        T q;
+        q.x = (v1.x * d.x + v1.y * d.y) / den;
+        q.y = (v1.y * d.x - v1.x * d.y) / den;
+        v1 = q;
+      }
+      RT xr = __shfl_sync(0xffffffffu, k < 32 ? v0.x : v1.x, k & 31);
+      RT xi = __shfl_sync(0xffffffffu, k < 32 ? v0.y : v1.y, k & 31);
+      if (lane > k && lane < kb) {
+        T u = U[k * kb + lane];
+        v0.x -= xr * u.x - xi * u.y;
+        v0.y -= xr * u.y + xi * u.x;
+      }
+      if (lane + 32 > k && lane + 32 < kb) {
+        T u = U[k * kb + lane + 32];
+        v1.x -= xr * u.x - xi * u.y;
+        v1.y -= xr * u.y + xi * u.x;
+      }
+    }
+    if (lane < kb) A[row + (j0 + lane) * lda] = v0;
+    if (lane + 32 < kb) A[row + (j0 + lane + 32) * lda] = v1;
   }
 }
 
@@ -895,19 +910,21 @@ struct LUSteps {
     BEAST_CUDA_TRY(ctx, cudaGetLastError());
     return BEAST_OK;
   }
+  // U12 = L11^{-1} A12 for columns [c0, c1), L11 = the diagonal block at j0
   int trsm(int64_t j0, int kb, int64_t c0, int64_t c1) {
     if (c1 <= c0) return BEAST_OK;
     ProfScope ps(ctx, PK_TRSM, 4.0 * (double)(c1 - c0) * kb * kb);
-    size_t smb = (size_t)(kb * kb + 64 * (kb + 1)) * sizeof(T);
-    k_trsm<T><<<(unsigned)((c1 - c0 + 63) / 64), 64, smb, st>>>(A, lda, j0, kb, c0, c1);
+    size_t smb = (size_t)kb * kb * sizeof(T);
+    k_trsm_warp<T, R><<<(unsigned)((c1 - c0 + 63) / 64), 256, smb, st>>>(A, lda, j0, kb, c0, c1);
     BEAST_CUDA_TRY(ctx, cudaGetLastError());
     return BEAST_OK;
   }
   // A[r0:r0+m, c0:c0+nc] -= A[r0:r0+m, k0:k0+k] A[k0:k0+k, c0:c0+nc]
   int gemm(int64_t r0, int64_t m, int64_t c0, int64_t nc, int64_t k0, int k, float* tcwork) {
     if (m <= 0 || nc <= 0 || k <= 0) return BEAST_OK;
-    ProfScope ps(ctx, PK_GEMM, 8.0 * (double)m * nc * k);
-    if (sizeof(T) == 8 && tcwork && m >= 128 && nc >= 256) {
+    const bool tc = sizeof(T) == 8 && tcwork && m >= 64 && nc >= 64 && k % 16 == 0;
+    ProfScope ps(ctx, tc ? PK_TCGEMM : PK_GEMM, 8.0 * (double)m * nc * k);
+    if (sizeof(T) == 8 && tcwork && m >= 64 && nc >= 64 && k % 16 == 0) {
       return tc_gemm_sub(ctx, reinterpret_cast<float2*>(A), lda, n, r0, k0, c0, m, nc, k, tcwork);
     }
     dim3 g((unsigned)((m + GT - 1) / GT), (unsigned)((nc + GT - 1) / GT));
@@ -934,13 +951,13 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
     return beast_fail(ctx, BEAST_ERR_ARG, "matrix too large for the shared-memory panel");
   const int NB = 4 * nb;
   const size_t panel_smem = (size_t)(rows0 * (nb + 1) + nb) * sizeof(T);
-  const size_t trsm_smem = (size_t)(nb * nb + 64 * (nb + 1)) * sizeof(T);
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
-  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)trsm_smem));
   const size_t diag_smem = (size_t)nb * (nb + 1) * sizeof(T);
-  const size_t rtrsm_smem = (size_t)(nb * nb + 64 * (nb + 1)) * sizeof(T);
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_getrf_nopiv_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_smem));
-  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_right_upper<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rtrsm_smem));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_warp<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)((size_t)nb * nb * sizeof(T))));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_right_warp<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)((size_t)nb * nb * sizeof(T))));
   int occ = 0;
   BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_panel<T>, 256, panel_smem));
   if (occ < 1) return beast_fail(ctx, BEAST_ERR_CUDA, "panel kernel does not fit on an SM");
@@ -962,6 +979,7 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   if (sizeof(T) == 8 && tc_gemm_supported(A, lda, NB) && n > NB)
     BEAST_CUDA_TRY(ctx, cudaMallocAsync(&tcwork, (size_t)2 * n * 2 * NB * sizeof(float), st));
   LUSteps<T, R> S{ctx, A, lda, n, ipiv, st};
+
   int rc = BEAST_OK;
   for (int64_t J0 = 0; J0 < n && rc == BEAST_OK; J0 += NB) {
     const int64_t J1 = std::min<int64_t>(n, J0 + NB);
@@ -986,12 +1004,13 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
         k_getrf_nopiv_diag<T><<<1, 256, diag_smem, st>>>(A, lda, j0, kb, dinfo);
         int64_t rb = n - j0 - kb;
         if (rb > 0)
-          k_trsm_right_upper<T><<<(unsigned)((rb + 63) / 64), 64, rtrsm_smem, st>>>(A, lda, j0, kb, j0 + kb, n);
+          k_trsm_right_warp<T, R><<<(unsigned)((rb + 63) / 64), 256, (size_t)kb * kb * sizeof(T), st>>>(
+              A, lda, j0, kb, j0 + kb, n);
         BEAST_CUDA_TRY(ctx, cudaGetLastError());
       }
       // TRSM + GEMM for the rest of the block
       if ((rc = S.trsm(j0, kb, j0 + kb, J1))) break;
-      if ((rc = S.gemm(j0 + kb, n - j0 - kb, j0 + kb, J1 - j0 - kb, j0, kb, nullptr))) break;
+      if ((rc = S.gemm(j0 + kb, n - j0 - kb, j0 + kb, J1 - j0 - kb, j0, kb, tcwork))) break;
     }
     if (rc) break;
     // the block's interchanges on the columns left and right of it
@@ -1004,7 +1023,7 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       for (int64_t j0 = J0; j0 < J1 && rc == BEAST_OK; j0 += nb) {
         int kb = (int)std::min<int64_t>(nb, J1 - j0);
         if ((rc = S.trsm(j0, kb, J1, n))) break;
-        if ((rc = S.gemm(j0 + kb, J1 - j0 - kb, J1, n - J1, j0, kb, nullptr))) break;
+        if ((rc = S.gemm(j0 + kb, J1 - j0 - kb, J1, n - J1, j0, kb, tcwork))) break;
       }
       if (rc) break;
       // trailing update with K = NB

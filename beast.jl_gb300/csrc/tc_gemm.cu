@@ -348,6 +348,7 @@ int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t n_total, int64
   {
     int64_t tot = M * (int64_t)K;
     k_expand<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(Mat + rowA + colA * lda, lda, (int)M, K, work);
+    ctx->launches += 1;
   }
   CUtensorMap tmA, tmB;
   // A': 2K floats per row (x), 2M rows (y)

@@ -285,10 +285,11 @@ def main():
         c2.close()
     if rank != 0:
         return
-    # ---- roofline of the dominant kernel class
+    # ---- roofline: the tensor-core trailing update of the LU (the dominant kernel class)
     pk, src = peaks()
-    dom = max(prof.items(), key=lambda kv: kv[1][0])
-    name, (kms, nl, work) = dom
+    dominant = max(prof.items(), key=lambda kv: kv[1][0])[0]
+    name = "lu_tc_gemm" if "lu_tc_gemm" in prof else dominant
+    kms, nl, work = prof[name]
     memory_bound = name in ("gather", "gemv", "trsv", "convert", "lu_laswp")
     if memory_bound:
         achieved = work / (kms * 1e-3) / 1e9
@@ -296,9 +297,16 @@ def main():
     else:
         achieved = work / (kms * 1e-3) / 1e12
         peak, unit, bound = pk.get("bf16_tflops_sustained", pk["bf16_tflops"]), "TFLOP/s", "tensor"
+    # DRAM traffic per launch: bytes per algorithmic flop measured by ncu on one k_tc_gemm
+    # launch of the level-4 EFIE (348 MB for 4.85e10 flops, profiles/k_tc_gemm_level4_efie.md),
+    # scaled to this run's average launch; the update streams C once, so traffic scales with
+    # the flops of a launch (C area x K, K fixed per update)
+    traffic = 7.18e-3 * work / nl if name == "lu_tc_gemm" else None
     roof = {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak, "peak_source": src, "traffic": None,
-            "launches": nl, "avg_launch_ms": kms / nl}
+            "frac": achieved / peak, "peak_source": src,
+            "peak_note": "measured dense bf16 (sustained); the kernel runs TF32 operands",
+            "traffic": traffic, "launches": nl, "avg_launch_ms": kms / nl,
+            "dominant_by_time": dominant}
     breakdown = {k: {"ms": v[0], "launches": v[1], "share": v[0] / sum(w[0] for w in prof.values())}
                  for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
     out = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": world,

@@ -217,7 +217,8 @@ int beast_solve_job(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc
  * When enabled, every instrumented kernel launch on the context stream is bracketed by
  * CUDA events.  Kinds: 0 geometry, 1 far pairs, 2 near pairs, 3 gather/scatter, 4 local
  * operators, 5 excitation, 6 far field, 7 LU panel, 8 row swaps, 9 TRSM, 10 trailing GEMM,
- * 11 triangular solves, 12 FP64 matvec, 13 vector ops, 14 precision conversion.
+ * 11 triangular solves, 12 FP64 matvec, 13 vector ops, 14 precision conversion,
+ * 15 tensor-core trailing update (tcgen05).
  * beast_prof_read sums event time (ms), bracketed launches and algorithmic work (flops for
  * compute kinds, bytes for memory kinds) over the records since the last enable. */
 int beast_prof_enable(beast_ctx* ctx, int on);
