@@ -27,7 +27,9 @@ namespace {
 constexpr int TM = 128, TN = 256, TK = 32;  // tile M (real rows), N, K per stage (floats)
 constexpr int STAGES = 4;
 constexpr int A_BYTES = TM * TK * 4, B_BYTES = TN * TK * 4, STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 + 256;
+constexpr int CCH = 32;                           // epilogue chunk: 128 rows x 32 columns of C'
+constexpr int C_BYTES = TM * CCH * 4;              // 16 KB per chunk buffer
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 2 * C_BYTES + 1024 + 256;
 constexpr int MAX_CTAS = 1024;
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
@@ -80,6 +82,15 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar)
       : "memory");
 }
+
+__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
+  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"((uint64_t)map),
+               "r"(x), "r"(y), "r"(src)
+               : "memory");
+}
+__device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row atoms of 1024 B
 __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
@@ -134,16 +145,20 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 // accumulator (MMA <-> epilogue).  Tiles are visited N-fastest (B' stays in L2).
 __global__ void __launch_bounds__(192, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-              float* C, int64_t ldc, int64_t c_row0, int64_t c_col0, int m_rows, int n_cols,
+              const __grid_constant__ CUtensorMap tmC, int c_row0, int c_col0, int m_rows, int n_cols,
               int b_x0, int b_y0, int nk, int* status) {
   extern __shared__ unsigned char smraw[];
   const uint32_t base = (smem_u32(smraw) + 1023u) & ~1023u;
   unsigned char* gbase = smraw + (base - smem_u32(smraw));
   uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + STAGES * STAGE_BYTES);
-  // bars: full[STAGES], empty[STAGES], tfull[2], tempty[2], done
+  // C' chunk buffers follow the operand ring; then the barriers:
+  // full[STAGES], empty[STAGES], tfull[2], tempty[2], done, cload[2]
+  const uint32_t cbuf0 = base + STAGES * STAGE_BYTES;
+  float* cbuf_g = reinterpret_cast<float*>(gbase + STAGES * STAGE_BYTES);
+  bars = reinterpret_cast<uint64_t*>(gbase + STAGES * STAGE_BYTES + 2 * C_BYTES);
   const int B_FULL = 0, B_EMPTY = STAGES, B_TFULL = 2 * STAGES, B_TEMPTY = 2 * STAGES + 2,
-            B_DONE = 2 * STAGES + 4;
-  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 5);
+            B_DONE = 2 * STAGES + 4, B_CLOAD = 2 * STAGES + 5;
+  uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 7);
   __shared__ int s_abort_mem;
   volatile int* s_abort = &s_abort_mem;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -161,6 +176,8 @@ __global__ void __launch_bounds__(192, 1)
       mbar_init(smem_u32(bars + B_TEMPTY + a), 4);  // one arrival per epilogue warp
     }
     mbar_init(smem_u32(bars + B_DONE), 1);
+    mbar_init(smem_u32(bars + B_CLOAD), 1);
+    mbar_init(smem_u32(bars + B_CLOAD + 1), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -226,40 +243,69 @@ __global__ void __launch_bounds__(192, 1)
     int no_abort = 0;
     mbar_wait(smem_u32(bars + B_DONE), 0, status, &no_abort);
   } else if (warp >= 2) {
-    // ---- epilogue: warp w drains TMEM lanes 32*(w%4) .. +31 (= tile rows)
+    // ---- epilogue: warp w owns TMEM lanes 32*(w%4) .. +31 (= tile rows).  C' streams
+    // through two shared-memory chunk buffers (128 rows x 32 columns, column-major like C'):
+    // TMA load -> subtract the accumulator -> TMA store; the load of chunk c+2 is issued
+    // once the store of chunk c has read its buffer.
     const int q = warp & 3;
+    const bool leader = (warp == 2 && lane == 0);
+    const int nch = TN / CCH;
+    uint32_t cuse[2] = {0, 0};  // completed phases of the chunk-load barriers
     int t = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
       const int a = t & 1;
       const uint32_t aph = (t >> 1) & 1;
+      const int m0 = (tile / ntn) * TM, n0 = (tile % ntn) * TN;
+      if (leader) {
+        for (int c = 0; c < 2; ++c) {
+          const uint32_t cl = smem_u32(bars + B_CLOAD + c);
+          mbar_expect_tx(cl, C_BYTES);
+          tma_load_2d(cbuf0 + c * C_BYTES, &tmC, c_row0 + m0, c_col0 + n0 + c * CCH, cl);
+        }
+      }
       if (!mbar_wait(smem_u32(bars + B_TFULL + a), aph, status, s_abort)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int m0 = (tile / ntn) * TM, n0 = (tile % ntn) * TN;
-      const int row = m0 + q * 32 + lane;
-      const bool row_ok = row < m_rows;
-      float* __restrict__ crow = C + (c_row0 + row);
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * TN);
-      for (int c0 = 0; c0 < TN; c0 += 64) {
-        float v[64], c[64];
+      const int row = q * 32 + lane;
+      bool ok = true;
+      for (int c = 0; c < nch; ++c) {
+        const int b = c & 1;
+        float v[CCH];
+        tmem_ld16(tbase + (uint32_t)(c * CCH), v);
+        tmem_ld16(tbase + (uint32_t)(c * CCH + 16), v + 16);
+        if (c == nch - 1) {
+          // accumulator fully read: hand it back to the MMA warp
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+          __syncwarp();
+          if (lane == 0)
+            asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bars + B_TEMPTY + a)) : "memory");
+        }
+        if (!mbar_wait(smem_u32(bars + B_CLOAD + b), cuse[b] & 1, status, s_abort)) {
+          ok = false;
+          break;
+        }
+        cuse[b]++;
+        float* cb = cbuf_g + b * (TM * CCH);
 #pragma unroll
-        for (int k = 0; k < 4; ++k) tmem_ld16(tbase + (uint32_t)(c0 + 16 * k), v + 16 * k);
-        if (row_ok) {
-#pragma unroll
-          for (int i = 0; i < 64; ++i) {
-            int col = n0 + c0 + i;
-            c[i] = col < n_cols ? __ldcs(crow + (c_col0 + col) * ldc) : 0.f;
-          }
-#pragma unroll
-          for (int i = 0; i < 64; ++i) {
-            int col = n0 + c0 + i;
-            if (col < n_cols) __stcs(crow + (c_col0 + col) * ldc, c[i] - v[i]);
+        for (int i = 0; i < CCH; ++i) cb[i * TM + row] -= v[i];
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        if (leader) {
+          tma_store_2d(&tmC, c_row0 + m0, c_col0 + n0 + c * CCH, cbuf0 + b * C_BYTES);
+          bulk_commit();
+          if (c + 2 < nch) {
+            bulk_wait_read0();
+            const uint32_t cl = smem_u32(bars + B_CLOAD + b);
+            mbar_expect_tx(cl, C_BYTES);
+            tma_load_2d(cbuf0 + b * C_BYTES, &tmC, c_row0 + m0, c_col0 + n0 + (c + 2) * CCH, cl);
           }
         }
       }
-      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      __syncwarp();
-      if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bars + B_TEMPTY + a)) : "memory");
+      if (!ok) break;
+      if (leader) bulk_wait_read0();  // both buffers are reloaded for the next tile
+      asm volatile("bar.sync 1, 128;" ::: "memory");
     }
+    if (leader) bulk_wait0();
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -309,7 +355,7 @@ EncodeTiledFn encode_fn() {
 }
 
 bool make_map(CUtensorMap* m, const float* base, uint64_t dim0, uint64_t dim1, uint64_t stride1_bytes,
-              uint32_t box0, uint32_t box1) {
+              uint32_t box0, uint32_t box1, bool swizzle = true) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {dim0, dim1};
@@ -317,7 +363,8 @@ bool make_map(CUtensorMap* m, const float* base, uint64_t dim0, uint64_t dim1, u
   cuuint32_t box[2] = {box0, box1};
   cuuint32_t es[2] = {1, 1};
   CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS;
 }
@@ -339,6 +386,9 @@ bool tc_gemm_supported(const void* A, int64_t lda, int K) {
 int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t n_total, int64_t rowA,
                 int64_t colA, int64_t colB, int64_t M, int64_t N, int K, float* work) {
   cudaStream_t st = ctx->stream;
+  // TMA: the first C' row (2 rowA floats) and the B' rows (2 colA) must start on 16 bytes
+  if ((2 * rowA) % 4 != 0 || (2 * colA) % 4 != 0 || 2 * (rowA + M) > INT32_MAX)
+    return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: unaligned block");
   static bool attr_done[64] = {false};
   int dev = ctx->device;
   if (!attr_done[dev]) {
@@ -354,17 +404,22 @@ int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t n_total, int64
   // A': 2K floats per row (x), 2M rows (y)
   if (!make_map(&tmA, work, (uint64_t)2 * K, (uint64_t)2 * M, (uint64_t)2 * K * 4, TK, TM))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (A') failed");
-  // B': real view of the whole matrix: 2 n_total floats per column (x), n_total columns (y)
+  // B': real view of the matrix, columns clipped at the end of the update block so that the
+  // tile columns beyond it load zeros (and contribute nothing)
   const float* real = reinterpret_cast<const float*>(Mat);
-  if (!make_map(&tmB, real, (uint64_t)2 * n_total, (uint64_t)n_total, (uint64_t)2 * lda * 4, TK, TN))
+  if (!make_map(&tmB, real, (uint64_t)2 * n_total, (uint64_t)(colB + N), (uint64_t)2 * lda * 4, TK, TN))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (B') failed");
+  // C': real view clipped to the update block (rows up to 2(rowA+M), columns up to colB+N):
+  // the bulk stores never touch anything outside it
+  CUtensorMap tmC;
+  if (!make_map(&tmC, real, (uint64_t)2 * (rowA + M), (uint64_t)(colB + N), (uint64_t)2 * lda * 4, TM, CCH, false))
+    return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (C') failed");
   const int m_rows = (int)(2 * M), n_cols = (int)N;
   const int ntiles = ((n_cols + TN - 1) / TN) * ((m_rows + TM - 1) / TM);
   const int grid = std::min(ntiles, std::max(1, ctx->num_sms));
   const int nk = (2 * K) / TK;
-  k_tc_gemm<<<grid, 192, SMEM_BYTES, st>>>(tmA, tmB, reinterpret_cast<float*>(Mat), 2 * lda, 2 * rowA,
-                                           colB, m_rows, n_cols, (int)(2 * colA), (int)colB, nk,
-                                           ctx->d_flag);
+  k_tc_gemm<<<grid, 192, SMEM_BYTES, st>>>(tmA, tmB, tmC, (int)(2 * rowA), (int)colB, m_rows, n_cols,
+                                           (int)(2 * colA), (int)colB, nk, ctx->d_flag);
   BEAST_CUDA_TRY(ctx, cudaGetLastError());
   return BEAST_OK;
 }
