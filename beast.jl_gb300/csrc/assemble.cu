@@ -150,7 +150,7 @@ DEV C2<double> cexpm1_d(C2<double> z) {
 DEV C2<double> cexp_d(C2<double> z) {
   double s, c;
   sincos(z.im, &s, &c);
-  double e = exp(z.re);
+  double e = z.re == 0.0 ? 1.0 : exp(z.re);
   return {e * c, e * s};
 }
 
@@ -845,7 +845,8 @@ __constant__ double c_gl_w[210];
 __constant__ int c_gl_off[21];
 
 // one Sauter-Schwab node: map index -> reference points X, Y on {0<=x2<=x1<=1} and weight
-DEV void ss_node(int cls, int n, int64_t item, double* X, double* Y, double* w) {
+DEV void ss_node(int cls, int n, int64_t item, const double* glx, const double* glw, double* X,
+                 double* Y, double* w) {
   int nreg = cls == 1 ? 2 : 6;
   int reg = (int)(item % nreg);
   int64_t k = item / nreg;
@@ -853,9 +854,8 @@ DEV void ss_node(int cls, int n, int64_t item, double* X, double* Y, double* w) 
   int i3 = (int)(k % n); k /= n;
   int i2 = (int)(k % n); k /= n;
   int i1 = (int)k;
-  int o = c_gl_off[n - 1];
-  double xi = c_gl_x[o + i1], e1 = c_gl_x[o + i2], e2 = c_gl_x[o + i3], e3 = c_gl_x[o + i4];
-  double ww = c_gl_w[o + i1] * c_gl_w[o + i2] * c_gl_w[o + i3] * c_gl_w[o + i4];
+  double xi = glx[i1], e1 = glx[i2], e2 = glx[i3], e3 = glx[i4];
+  double ww = glw[i1] * glw[i2] * glw[i3] * glw[i4];
   double A[2], B[2], wt;
   int sub = reg >> 1;
   bool swap = reg & 1;
@@ -915,6 +915,14 @@ struct NearParams {
 constexpr int NEAR_WARPS = 4;
 
 __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
+  // Gauss-Legendre nodes in shared memory (lanes read different nodes: a constant-memory
+  // read would serialise)
+  __shared__ double s_glx[210], s_glw[210];
+  for (int k = threadIdx.x; k < 210; k += blockDim.x) {
+    s_glx[k] = c_gl_x[k];
+    s_glw[k] = c_gl_w[k];
+  }
+  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
   if (e >= P.nnear) return;
@@ -958,9 +966,96 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
     const int nreg = np_.cls == 1 ? 2 : 6;
     const int64_t items = (int64_t)nreg * n * n * n * n;
     const double jac = 4.0 * t.area * s.area;
+    const double* glx = s_glx + c_gl_off[n - 1];
+    const double* glw = s_glw + c_gl_off[n - 1];
+    const bool mw_rt = P.tk == BEAST_RT && P.bk == BEAST_RT &&
+                       (P.op.kind == BEAST_MW_SL || P.op.kind == BEAST_MW_DL);
+    if (mw_rt) {
+      // moment form: with xi = x - c_p, eta = y - c_q and W = node weight x kernel,
+      //  single layer: z_ij = alpha (Mxe - s_j.Mx - t_i.Me + (t_i.s_j) M0) + 4 beta M0
+      //  double layer: z_ij = D0 - s_j.Dxr - t_i.Dre + (s_j x t_i).Dr
+      // (t_i = v_i - c_p, s_j = w_j - c_q; the shape normalisations cancel the Jacobian)
+      const bool sl = P.op.kind == BEAST_MW_SL;
+      const V3<double> cp = t.c, cq = s.c;
+      const double gi = P.op.gi, gr = P.op.gr;
+      // m[0..1] M0, m[2..3] M1 (SL) ; m[4..9] V1, m[10..15] V2, m[16..21] V3 as (re, im) per axis
+      double m[22];
+#pragma unroll
+      for (int k = 0; k < 22; ++k) m[k] = 0.0;
+      const V3<double> d = cp - cq;
+      for (int64_t it = lane; it < items; it += 32) {
+        double X[2], Y[2], w;
+        ss_node(np_.cls, n, it, glx, glw, X, Y, &w);
+        const double lt[3] = {1.0 - X[0], X[0] - X[1], X[1]}, ls[3] = {1.0 - Y[0], Y[0] - Y[1], Y[1]};
+        const V3<double> xi = lt[0] * (t.v[pt[0]] - cp) + lt[1] * (t.v[pt[1]] - cp) + lt[2] * (t.v[pt[2]] - cp);
+        const V3<double> eta = ls[0] * (s.v[ps[0]] - cq) + ls[1] * (s.v[ps[1]] - cq) + ls[2] * (s.v[ps[2]] - cq);
+        const V3<double> r = (d + xi) - eta;
+        const double R = sqrt(dot(r, r));
+        const double iR = 1.0 / R;
+        double sn, cs;
+        sincos(gi * R, &sn, &cs);
+        const double amp = (gr == 0.0 ? 1.0 : exp(-gr * R)) * I4PI * iR * w;
+        double cr = amp * cs, ci = -amp * sn;  // w e^{-gamma R} / (4 pi R)
+        V3<double> a, b, c3;
+        double s0;
+        if (sl) {
+          s0 = dot(xi, eta);
+          a = xi;
+          b = eta;
+          c3 = V3<double>{0, 0, 0};
+          m[0] += cr;
+          m[1] += ci;
+        } else {
+          // grad G = c r with c = -(gamma + 1/R) G / R
+          const double pr = -(gr + iR) * iR, pi = -gi * iR;
+          const double nr = pr * cr - pi * ci, ni = pr * ci + pi * cr;
+          cr = nr;
+          ci = ni;
+          s0 = dot(xi, cross(d, eta));  // xi.(r x eta) = xi.(d x eta)
+          a = cross(xi, r);
+          b = cross(r, eta);
+          c3 = r;
+        }
+        m[2] += s0 * cr; m[3] += s0 * ci;
+        m[4] += a.x * cr; m[5] += a.x * ci; m[6] += a.y * cr; m[7] += a.y * ci; m[8] += a.z * cr; m[9] += a.z * ci;
+        m[10] += b.x * cr; m[11] += b.x * ci; m[12] += b.y * cr; m[13] += b.y * ci; m[14] += b.z * cr; m[15] += b.z * ci;
+        m[16] += c3.x * cr; m[17] += c3.x * ci; m[18] += c3.y * cr; m[19] += c3.y * ci; m[20] += c3.z * cr; m[21] += c3.z * ci;
+      }
+#pragma unroll
+      for (int k = 0; k < 22; ++k) {
+        double v = m[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        m[k] = v;
+      }
+      const C2<double> M0{m[0], m[1]}, M1{m[2], m[3]};
+      CV<double> V1, V2, V3_;
+      V1.x = {m[4], m[5]}; V1.y = {m[6], m[7]}; V1.z = {m[8], m[9]};
+      V2.x = {m[10], m[11]}; V2.y = {m[12], m[13]}; V2.z = {m[14], m[15]};
+      V3_.x = {m[16], m[17]}; V3_.y = {m[18], m[19]}; V3_.z = {m[20], m[21]};
+      if (lane == 0) {
+        const C2<double> al{P.op.ar, P.op.ai}, be{P.op.br, P.op.bi};
+        for (int i = 0; i < 3; ++i) {
+          const V3<double> ti = t.v[i] - cp;
+          for (int j = 0; j < 3; ++j) {
+            const V3<double> sj = s.v[j] - cq;
+            C2<double> z;
+            if (sl) {
+              C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
+              fm = cadd(fm, cscale(dot(ti, sj), M0));
+              z = cadd(cmul(al, fm), cscale(4.0, cmul(be, M0)));
+            } else {
+              C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
+              z = cadd(fm, rdot(cross(sj, ti), V3_));
+            }
+            store_c<double>(P.zcell, (int64_t)(3 * np_.q + j) * P.ldc + 3 * (int64_t)np_.p + i, z, P.c64);
+          }
+        }
+      }
+      return;
+    }
     for (int64_t it = lane; it < items; it += 32) {
       double X[2], Y[2], w;
-      ss_node(np_.cls, n, it, X, Y, &w);
+      ss_node(np_.cls, n, it, glx, glw, X, Y, &w);
       double lt[3] = {1.0 - X[0], X[0] - X[1], X[1]}, ls[3] = {1.0 - Y[0], Y[0] - Y[1], Y[1]};
       double bx[3], by[3];
       for (int q = 0; q < 3; ++q) {
