@@ -7,7 +7,8 @@
 //              and the rank-1 update, with bounded-spin grid barriers (a barrier that gives
 //              up sets a status word and the kernel returns; nothing hangs)
 //   k_laswp    the panel's row interchanges applied to the other columns
-//   k_trsm_warp / k_trsm_right_warp   U12 = L11^{-1} A12 and (unpivoted path) L21 = A21 U11^{-1}
+//   k_trsm_tile   U12 = L11^{-1} A12 and (unpivoted path, after k_getrf64 on the diagonal
+//                 block) L21 = A21 U11^{-1}
 //   k_gemm     A22 -= L21 U12 (complex, tiled through shared memory)
 // The element type is complex FP64 (c128) or complex FP32 (c64).
 #include <cuda_runtime.h>
@@ -284,145 +285,218 @@ __global__ void k_laswp(T* A, int64_t lda, int64_t c0, int64_t c1, int64_t p0, i
   }
 }
 
-// ---- LU without pivoting (mixed path) ----------------------------------------------------
-// Diagonal block A[j0:j0+kb, j0:j0+kb] = L11 U11 in place, one CTA; a zero pivot sets *info.
+// ---- LU of a diagonal block without pivoting (mixed path) --------------------------------
+// A[j0:j0+kb, j0:j0+kb] = L11 U11 in place, kb <= 64, one CTA of 256 threads in shared
+// memory; thread t updates column t % 64 of the rows congruent to t / 64 modulo 4.  A zero
+// pivot sets *info (1-based column) and the kernel stops.
+constexpr int TRI = 64;
+
 template <typename T>
-__global__ void __launch_bounds__(256) k_getrf_nopiv_diag(T* A, int64_t lda, int64_t j0, int kb, int* info) {
+__device__ __forceinline__ void cfms(T& acc, T a, T b) {  // acc -= a b
+  acc.x -= a.x * b.x - a.y * b.y;
+  acc.y -= a.x * b.y + a.y * b.x;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_getrf64(T* A, int64_t lda, int64_t j0, int kb, int* info) {
+  typedef decltype(T().x) RT;
+  constexpr int LD = TRI + 1;
   extern __shared__ unsigned char smraw[];
-  T* D = reinterpret_cast<T*>(smraw);  // kb x (kb+1), row-major
-  typedef decltype(D[0].x) RT;
-  const int ld = kb + 1;
-  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-    int i = e % kb, c = e / kb;
-    D[i * ld + c] = A[(j0 + i) + (j0 + c) * lda];
+  T* D = reinterpret_cast<T*>(smraw);  // row-major, ld LD
+  const int tid = threadIdx.x, c = tid % TRI, rg = tid / TRI;
+  for (int e = tid; e < kb * kb; e += 256) {
+    const int r = e % kb, k = e / kb;
+    D[r * LD + k] = A[(j0 + r) + (j0 + k) * lda];
   }
   __syncthreads();
   for (int k = 0; k < kb; ++k) {
-    T piv = D[k * ld + k];
-    RT den = piv.x * piv.x + piv.y * piv.y;
-    if (den == (RT)0) {
-      if (threadIdx.x == 0) atomicCAS(info, 0, (int)(j0 + k + 1));
+    const T p = D[k * LD + k];
+    const RT den = p.x * p.x + p.y * p.y;
+    if (den == (RT)0) {  // uniform
+      if (tid == 0) atomicCAS(info, 0, (int)(j0 + k + 1));
       return;
     }
-    RT ir = piv.x / den, ii = -piv.y / den;
-    for (int i = k + 1 + threadIdx.x; i < kb; i += blockDim.x) {
-      T a = D[i * ld + k];
+    const int i = k + 1 + tid;
+    if (i < kb) {
+      const RT ir = p.x / den, ii = -p.y / den;
+      const T a = D[i * LD + k];
       T l;
       l.x = a.x * ir - a.y * ii;
       l.y = a.x * ii + a.y * ir;
-      D[i * ld + k] = l;
+      D[i * LD + k] = l;
     }
     __syncthreads();
-    const int w = kb - k - 1;
-    for (int e = threadIdx.x; e < w * w; e += blockDim.x) {
-      int i = k + 1 + e / w, c = k + 1 + e % w;
-      T l = D[i * ld + k], u = D[k * ld + c], v = D[i * ld + c];
-      v.x -= l.x * u.x - l.y * u.y;
-      v.y -= l.x * u.y + l.y * u.x;
-      D[i * ld + c] = v;
+    if (c > k && c < kb) {
+      const T u = D[k * LD + c];
+      // rows i = rg + 4 j > k
+      const int jb = (k + 1 - rg + 3) >> 2;
+      for (int j0r = jb; j0r < 16; j0r += 4) {
+        T l[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i2 = rg + 4 * (j0r + q);
+          l[q] = (j0r + q < 16 && i2 < kb) ? D[i2 * LD + k] : T{0, 0};
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          const int i2 = rg + 4 * (j0r + q);
+          if (j0r + q < 16 && i2 < kb) cfms(D[i2 * LD + c], l[q], u);
+        }
+      }
     }
     __syncthreads();
   }
-  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-    int i = e % kb, c = e / kb;
-    A[(j0 + i) + (j0 + c) * lda] = D[i * ld + c];
+  for (int e = tid; e < kb * kb; e += 256) {
+    const int r = e % kb, k = e / kb;
+    A[(j0 + r) + (j0 + k) * lda] = D[r * LD + k];
   }
 }
 
-// U12 = L11^{-1} A12 (unit lower L11 = A[j0:j0+kb, j0:j0+kb]) for columns [c0, c1) by forward
-// substitution: one warp per column (lane l owns rows l and l + 32), the solved entry is
-// broadcast with a shuffle; 8 warps per CTA, 64 columns per CTA, L11 in shared memory.
-template <typename T, typename RT>
-__global__ void __launch_bounds__(256) k_trsm_warp(T* A, int64_t lda, int64_t j0, int kb, int64_t c0g,
-                                                   int64_t c1) {
-  extern __shared__ unsigned char smraw[];
-  T* L = reinterpret_cast<T*>(smraw);  // kb x kb column-major
-  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-    int r = e % kb, c = e / kb;
-    L[c * kb + r] = A[(j0 + r) + (j0 + c) * lda];
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t cbase = c0g + (int64_t)blockIdx.x * 64;
-  for (int cc = warp; cc < 64; cc += 8) {
-    const int64_t col = cbase + cc;
-    if (col >= c1) break;
-    T* b = A + j0 + col * lda;
-    T v0, v1;
-    v0.x = v0.y = v1.x = v1.y = 0;
-    if (lane < kb) v0 = b[lane];
-    if (lane + 32 < kb) v1 = b[lane + 32];
-    for (int k = 0; k < kb; ++k) {
-      RT bx = __shfl_sync(0xffffffffu, k < 32 ? v0.x : v1.x, k & 31);
-      RT by = __shfl_sync(0xffffffffu, k < 32 ? v0.y : v1.y, k & 31);
-      if (lane > k && lane < kb) {
-        T l = L[k * kb + lane];
-        v0.x -= l.x * bx - l.y * by;
-        v0.y -= l.x * by + l.y * bx;
-      }
-      if (lane + 32 > k && lane + 32 < kb) {
-        T l = L[k * kb + lane + 32];
-        v1.x -= l.x * bx - l.y * by;
-        v1.y -= l.x * by + l.y * bx;
-      }
-    }
-    if (lane < kb) b[lane] = v0;
-    if (lane + 32 < kb) b[lane + 32] = v1;
-  }
+// ---- blocked triangular solves on 64-wide triangles ---------------------------------------
+// Both TRSMs of the LU are batches of independent triangular systems of order kb <= 64 that
+// share one triangle of the factored diagonal block at (j0, j0):
+//   left  (U12 = L11^{-1} A12): one system per column of A12, unit lower L11;
+//   right (unpivoted path, L21 = A21 U11^{-1}): one system per row of A21, upper U11.
+// A CTA stages NS systems (coalesced global loads) as X[k][s] in shared memory, one system
+// per thread, and the triangle as M[k][c] = coefficient of x_k in equation c (k < c).  Each
+// thread then substitutes in blocks of 16 unknowns held in registers,
+//   x_c = (a_c - sum_{k<c} M[k][c] x_k) * d_c     (d_c = 1 or 1/U_cc),
+// reading its solved unknowns back from its own shared-memory column; the triangle rows are
+// warp-wide broadcasts, prefetched one row ahead.
+template <typename T>
+struct TrsmTile {
+  static constexpr int NS = 64;                          // systems (threads) per CTA
+  static constexpr int MLD = sizeof(T) == 8 ? 66 : 65;   // row stride of M: 16-byte rows
+};
+
+template <typename T>
+size_t trsm_tile_smem() {
+  return ((size_t)TRI * TrsmTile<T>::MLD + TRI + (size_t)TRI * (TrsmTile<T>::NS + 1)) * sizeof(T);
 }
 
-// L21 = A21 U11^{-1} (upper U11 = A[j0:j0+kb, j0:j0+kb]) for rows [r0, r1) by substitution
-// along each row: one warp per row (lane l owns columns l and l + 32), 64 rows per CTA.
-template <typename T, typename RT>
-__global__ void __launch_bounds__(256) k_trsm_right_warp(T* A, int64_t lda, int64_t j0, int kb, int64_t r0g,
-                                                         int64_t r1) {
-  extern __shared__ unsigned char smraw[];
-  T* U = reinterpret_cast<T*>(smraw);  // kb x kb, U[k * kb + c] = row k, column c
-  for (int e = threadIdx.x; e < kb * kb; e += blockDim.x) {
-    int r = e % kb, c = e / kb;
-    U[r * kb + c] = A[(j0 + r) + (j0 + c) * lda];
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t rbase = r0g + (int64_t)blockIdx.x * 64;
-  for (int rr = warp; rr < 64; rr += 8) {
-    const int64_t row = rbase + rr;
-    if (row >= r1) break;
-    T v0, v1;
-    v0.x = v0.y = v1.x = v1.y = 0;
-    if (lane < kb) v0 = A[row + (j0 + lane) * lda];
-    if (lane + 32 < kb) v1 = A[row + (j0 + lane + 32) * lda];
-    for (int k = 0; k < kb; ++k) {
-      // owner of column k finishes x_k = acc_k / U_kk
-      T d = U[k * kb + k];
-      RT den = d.x * d.x + d.y * d.y;
-      if (k < 32 && lane == k) {
-        T q;
-        q.x = (v0.x * d.x + v0.y * d.y) / den;
-        q.y = (v0.y * d.x - v0.x * d.y) / den;
-        v0 = q;
-      }
-      if (k >= 32 && lane == k - 32) {
-        T q;
-        q.x = (v1.x * d.x + v1.y * d.y) / den;
-        q.y = (v1.y * d.x - v1.x * d.y) / den;
-        v1 = q;
-      }
-      RT xr = __shfl_sync(0xffffffffu, k < 32 ? v0.x : v1.x, k & 31);
-      RT xi = __shfl_sync(0xffffffffu, k < 32 ? v0.y : v1.y, k & 31);
-      if (lane > k && lane < kb) {
-        T u = U[k * kb + lane];
-        v0.x -= xr * u.x - xi * u.y;
-        v0.y -= xr * u.y + xi * u.x;
-      }
-      if (lane + 32 > k && lane + 32 < kb) {
-        T u = U[k * kb + lane + 32];
-        v1.x -= xr * u.x - xi * u.y;
-        v1.y -= xr * u.y + xi * u.x;
+template <typename T, typename RT, bool RIGHT>
+__global__ void __launch_bounds__(TrsmTile<T>::NS) k_trsm_tile(T* A, int64_t lda, int64_t j0, int kb,
+                                                               int64_t s0, int64_t s1) {
+  constexpr int NS = TrsmTile<T>::NS, MLD = TrsmTile<T>::MLD, LDX = NS + 1;
+  extern __shared__ __align__(16) unsigned char smraw[];
+  T* M = reinterpret_cast<T*>(smraw);  // TRI x MLD
+  T* dinv = M + TRI * MLD;             // TRI
+  T* X = dinv + TRI;                   // TRI x LDX
+  const int tid = threadIdx.x;
+  const int64_t sb = s0 + (int64_t)blockIdx.x * NS;  // first system of this CTA
+  const T zero = {0, 0};
+
+  // the triangle (zero outside kb x kb and on/below the diagonal of M) and the systems
+  // X[k][s]; the loads of a thread are issued in batches of LB before their stores
+  constexpr int LB = 16;
+  static_assert((TRI * TRI / NS) % LB == 0 && TRI % LB == 0, "load batches");
+  for (int m0 = 0; m0 < TRI * TRI / NS; m0 += LB) {
+    T v[LB];
+#pragma unroll
+    for (int j = 0; j < LB; ++j) {
+      const int e = tid + NS * (m0 + j);
+      const int r = e % TRI, k = e / TRI;  // global element (j0 + r, j0 + k), coalesced along r
+      v[j] = (r < kb && k < kb) ? A[(j0 + r) + (j0 + k) * lda] : zero;
+    }
+#pragma unroll
+    for (int j = 0; j < LB; ++j) {
+      const int e = tid + NS * (m0 + j);
+      const int r = e % TRI, k = e / TRI;
+      if (RIGHT) {
+        M[r * MLD + k] = r < k ? v[j] : zero;  // U[r][k]: coefficient of x_r in equation k
+        if (r == k) {
+          T d = zero;
+          if (r < kb) {
+            const RT den = v[j].x * v[j].x + v[j].y * v[j].y;
+            d.x = v[j].x / den;
+            d.y = -v[j].y / den;
+          }
+          dinv[r] = d;
+        }
+      } else {
+        M[k * MLD + r] = r > k ? v[j] : zero;  // L[r][k]: coefficient of x_k in equation r
       }
     }
-    if (lane < kb) A[row + (j0 + lane) * lda] = v0;
-    if (lane + 32 < kb) A[row + (j0 + lane + 32) * lda] = v1;
+  }
+  for (int m0 = 0; m0 < TRI; m0 += LB) {
+    T v[LB];
+#pragma unroll
+    for (int j = 0; j < LB; ++j) {
+      const int e = tid + NS * (m0 + j);
+      if (RIGHT) {
+        const int s = e % NS, k = e / NS;  // row sb + s, column j0 + k: coalesced along s
+        v[j] = (k < kb && sb + s < s1) ? A[(sb + s) + (j0 + k) * lda] : zero;
+      } else {
+        const int k = e % TRI, s = e / TRI;  // row j0 + k, column sb + s: coalesced along k
+        v[j] = (k < kb && sb + s < s1) ? A[(j0 + k) + (sb + s) * lda] : zero;
+      }
+    }
+#pragma unroll
+    for (int j = 0; j < LB; ++j) {
+      const int e = tid + NS * (m0 + j);
+      if (RIGHT)
+        X[(e / NS) * LDX + e % NS] = v[j];
+      else
+        X[(e % TRI) * LDX + e / TRI] = v[j];
+    }
+  }
+  __syncthreads();
+
+  // substitution, 16 unknowns at a time
+  const int nblk = (kb + 15) / 16;
+  T* x = X + tid;
+  for (int B = 0; B < nblk; ++B) {
+    const int c0 = 16 * B;
+    T acc[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) acc[c] = x[(c0 + c) * LDX];
+    if (c0 > 0) {
+      // acc_c -= sum_{k < c0} M[k][c0 + c] x_k, the next row of M prefetched
+      T mc[16], xc = x[0];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) mc[c] = M[c0 + c];
+      for (int k = 0; k < c0; ++k) {
+        const int kn = k + 1 < c0 ? k + 1 : k;
+        T mn[16];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) mn[c] = M[kn * MLD + c0 + c];
+        const T xn = x[kn * LDX];
+#pragma unroll
+        for (int c = 0; c < 16; ++c) cfms(acc[c], mc[c], xc);
+#pragma unroll
+        for (int c = 0; c < 16; ++c) mc[c] = mn[c];
+        xc = xn;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 16; ++c) {
+#pragma unroll
+      for (int k = 0; k < c; ++k) cfms(acc[c], M[(c0 + k) * MLD + c0 + c], acc[k]);
+      if (RIGHT) {
+        const T d = dinv[c0 + c];
+        T q;
+        q.x = acc[c].x * d.x - acc[c].y * d.y;
+        q.y = acc[c].x * d.y + acc[c].y * d.x;
+        acc[c] = q;
+      }
+      x[(c0 + c) * LDX] = acc[c];
+    }
+  }
+  __syncthreads();
+
+  // write the solved systems back
+  for (int m0 = 0; m0 < TRI; m0 += LB) {
+#pragma unroll
+    for (int j = 0; j < LB; ++j) {
+      const int e = tid + NS * (m0 + j);
+      if (RIGHT) {
+        const int s = e % NS, k = e / NS;
+        if (k < kb && sb + s < s1) A[(sb + s) + (j0 + k) * lda] = X[k * LDX + s];
+      } else {
+        const int k = e % TRI, s = e / TRI;
+        if (k < kb && sb + s < s1) A[(j0 + k) + (sb + s) * lda] = X[k * LDX + s];
+      }
+    }
   }
 }
 
@@ -617,52 +691,88 @@ __global__ void k_invert_diag(const T* A, int64_t lda, int64_t n, T* dinv) {
 }
 
 // ---- triangular solve on one right-hand side as a wavefront ------------------------------
-// Block rows of 64 are owned round-robin by co-resident CTAs (cooperative launch).  A CTA
-// accumulates the off-diagonal products of its block row as the solved blocks it depends on
-// are published (flag per block), solves its diagonal block in shared memory and publishes
-// it.  lower = 1: unit lower, forward; lower = 0: upper, backward.  Arithmetic in RT (the
-// factors' precision).  Flag waits are bounded; on expiry a status bit is set and the CTA
-// returns.
+// Block rows of 64 are owned round-robin by co-resident CTAs (cooperative launch).  A block
+// row depends on every block solved before it, so blocks are published strictly in solve
+// order and one counter (flags[0] = blocks published) tells a CTA which solved blocks it may
+// read.  A CTA walks its dependencies in order: the 64 x 64 factor block of the next
+// dependency and its slice of the diagonal block's inverse are loaded before it waits, the
+// counter is polled only when the next dependency is beyond the last value seen, then it
+// solves its diagonal block (inverse matvec) and publishes.  lower = 1: unit lower,
+// forward; lower = 0: upper, backward.  Arithmetic in RT (the factors' precision).  Waits
+// are bounded; on expiry a status bit is set and the CTA returns.
 template <typename T, typename RT>
 __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int64_t n, T* x, int lower,
                                                    int* flags, int* status, const T* dinv) {
   __shared__ RT sr[64], si[64];
   __shared__ RT pr[4][64], pim[4][64];
-  __shared__ int s_abort;
+  __shared__ int s_avail[2];
   const int nblk = (int)((n + 63) / 64);
   const int tid = threadIdx.x, r = tid & 63, q = tid >> 6;
+  int* done = flags;
+  const T zero = {0, 0};
+  int avail = 0, polls = 0;
   for (int t = blockIdx.x; t < nblk; t += gridDim.x) {
     const int b = lower ? t : nblk - 1 - t;
     const int64_t r0 = (int64_t)b * 64;
     const int rb = (int)(n - r0 < 64 ? n - r0 : 64);
-    RT ar = 0, ai = 0;
-    const int ndep = lower ? b : nblk - 1 - b;
-    for (int s = 0; s < ndep; ++s) {
+    // this thread's 16 entries of the diagonal block's inverse (row r, columns q*16..)
+    const T* Di = dinv + (int64_t)b * 2 * 4096 + (lower ? 0 : 4096);
+    T dv[16];
+#pragma unroll
+    for (int c = 0; c < 16; ++c) dv[c] = Di[(q * 16 + c) * 64 + r];
+    // this thread's 16 entries of the factor block of dependency s (row r0 + r)
+    auto load_blk = [&](int s, T* dst) {
       const int k = lower ? s : nblk - 1 - s;
-      if (tid == 0) {
-        s_abort = 0;
-        long long it = 0;
-        while (atomicAdd(flags + k, 0) == 0) {
-          if (++it > (1LL << 24)) {
-            atomicOr(status, 8);
-            s_abort = 1;
-            break;
-          }
-          __nanosleep(32);
-        }
-        __threadfence();
-      }
-      __syncthreads();
-      if (s_abort) return;
       const int64_t c0 = (int64_t)k * 64;
       const int cb = (int)(n - c0 < 64 ? n - c0 : 64);
-      if (r < rb) {
-        const T* Ar = A + (r0 + r) + c0 * lda;
-        for (int c = q * 16; c < q * 16 + 16 && c < cb; ++c) {
-          T a = Ar[c * lda];
-          T xv = __ldcg(x + c0 + c);
-          ar += (RT)a.x * (RT)xv.x - (RT)a.y * (RT)xv.y;
-          ai += (RT)a.x * (RT)xv.y + (RT)a.y * (RT)xv.x;
+      const T* Ar = A + (r0 + r) + c0 * lda;
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int col = q * 16 + c;
+        dst[c] = (r < rb && col < cb) ? Ar[col * lda] : zero;
+      }
+    };
+    RT ar = 0, ai = 0;
+    T nxt[16];
+    if (t > 0) load_blk(0, nxt);
+    for (int s = 0; s < t; ++s) {
+      T cur[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) cur[c] = nxt[c];
+      if (s + 1 < t) load_blk(s + 1, nxt);
+      if (s >= avail) {
+        // wait until block s (in solve order) is published; two alternating slots so that
+        // a slot is rewritten only after every thread has passed the next barrier
+        const int slot = polls & 1;
+        if (tid == 0) {
+          long long it = 0;
+          int v;
+          while ((v = atomicAdd(done, 0)) <= s) {
+            if (++it > (1LL << 24)) {
+              atomicOr(status, 8);
+              v = -1;
+              break;
+            }
+            __nanosleep(32);
+          }
+          __threadfence();
+          s_avail[slot] = v;
+        }
+        __syncthreads();
+        avail = s_avail[slot];
+        ++polls;
+        if (avail < 0) return;
+      }
+      const int k = lower ? s : nblk - 1 - s;
+      const int64_t c0 = (int64_t)k * 64;
+      const int cb = (int)(n - c0 < 64 ? n - c0 : 64);
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const int col = q * 16 + c;
+        if (col < cb) {
+          const T xv = __ldcg(x + c0 + col);
+          ar += (RT)cur[c].x * (RT)xv.x - (RT)cur[c].y * (RT)xv.y;
+          ai += (RT)cur[c].x * (RT)xv.y + (RT)cur[c].y * (RT)xv.x;
         }
       }
     }
@@ -682,12 +792,12 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
     __syncthreads();
     // x_b = inv(D_b) * rhs_b  (64 x 64 matvec, 4 quarter sums per row)
     {
-      const T* Di = dinv + (int64_t)b * 2 * 4096 + (lower ? 0 : 4096);
       RT accr = 0, acci = 0;
-      for (int c = q * 16; c < q * 16 + 16; ++c) {
-        T m = Di[c * 64 + r];
-        accr += (RT)m.x * sr[c] - (RT)m.y * si[c];
-        acci += (RT)m.x * si[c] + (RT)m.y * sr[c];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        const T m = dv[c];
+        accr += (RT)m.x * sr[q * 16 + c] - (RT)m.y * si[q * 16 + c];
+        acci += (RT)m.x * si[q * 16 + c] + (RT)m.y * sr[q * 16 + c];
       }
       pr[q][r] = accr;
       pim[q][r] = acci;
@@ -701,7 +811,7 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
     }
     __threadfence();
     __syncthreads();
-    if (tid == 0) atomicExch(flags + b, 1);
+    if (tid == 0) atomicAdd(done, 1);
   }
 }
 
@@ -914,8 +1024,9 @@ struct LUSteps {
   int trsm(int64_t j0, int kb, int64_t c0, int64_t c1) {
     if (c1 <= c0) return BEAST_OK;
     ProfScope ps(ctx, PK_TRSM, 4.0 * (double)(c1 - c0) * kb * kb);
-    size_t smb = (size_t)kb * kb * sizeof(T);
-    k_trsm_warp<T, R><<<(unsigned)((c1 - c0 + 63) / 64), 256, smb, st>>>(A, lda, j0, kb, c0, c1);
+    constexpr int NS = TrsmTile<T>::NS;
+    k_trsm_tile<T, R, false><<<(unsigned)((c1 - c0 + NS - 1) / NS), NS, trsm_tile_smem<T>(), st>>>(
+        A, lda, j0, kb, c0, c1);
     BEAST_CUDA_TRY(ctx, cudaGetLastError());
     return BEAST_OK;
   }
@@ -952,12 +1063,12 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   const int NB = 8 * nb;
   const size_t panel_smem = (size_t)(rows0 * (nb + 1) + nb) * sizeof(T);
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
-  const size_t diag_smem = (size_t)nb * (nb + 1) * sizeof(T);
-  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_getrf_nopiv_diag<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)diag_smem));
-  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_warp<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)((size_t)nb * nb * sizeof(T))));
-  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_right_warp<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)((size_t)nb * nb * sizeof(T))));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_getrf64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)((size_t)TRI * (TRI + 1) * sizeof(T))));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_tile<T, R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)trsm_tile_smem<T>()));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_tile<T, R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                           (int)trsm_tile_smem<T>()));
   int occ = 0;
   BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_panel<T>, 256, panel_smem));
   if (occ < 1) return beast_fail(ctx, BEAST_ERR_CUDA, "panel kernel does not fit on an SM");
@@ -1001,10 +1112,11 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       } else {
         // no pivoting: diagonal block LU, then L21 = A21 U11^{-1} for every row below
         ProfScope ps(ctx, PK_PANEL, 8.0 * (double)M * kb * kb / 2, 2);
-        k_getrf_nopiv_diag<T><<<1, 256, diag_smem, st>>>(A, lda, j0, kb, dinfo);
-        int64_t rb = n - j0 - kb;
+        constexpr int NS = TrsmTile<T>::NS;
+        k_getrf64<T><<<1, 256, (size_t)TRI * (TRI + 1) * sizeof(T), st>>>(A, lda, j0, kb, dinfo);
+        const int64_t rb = n - j0 - kb;
         if (rb > 0)
-          k_trsm_right_warp<T, R><<<(unsigned)((rb + 63) / 64), 256, (size_t)kb * kb * sizeof(T), st>>>(
+          k_trsm_tile<T, R, true><<<(unsigned)((rb + NS - 1) / NS), NS, trsm_tile_smem<T>(), st>>>(
               A, lda, j0, kb, j0 + kb, n);
         BEAST_CUDA_TRY(ctx, cudaGetLastError());
       }
