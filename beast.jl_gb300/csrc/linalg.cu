@@ -34,8 +34,9 @@ void* lu_dinv(const int* ipiv, int64_t n) {
 }
 
 bool tc_gemm_supported(const void* A, int64_t lda, int K);
-int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t n_total, int64_t rowA, int64_t colA,
-                int64_t colB, int64_t M, int64_t N, int K, float* work);
+size_t tc_gemm_work_bytes(int64_t M, int64_t N, int K);
+int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t colB, int64_t M,
+                int64_t N, int K, void* work, size_t work_bytes);
 
 namespace {
 
@@ -292,9 +293,11 @@ __global__ void k_laswp(T* A, int64_t lda, int64_t c0, int64_t c1, int64_t p0, i
 constexpr int TRI = 64;
 
 template <typename T>
-__device__ __forceinline__ void cfms(T& acc, T a, T b) {  // acc -= a b
-  acc.x -= a.x * b.x - a.y * b.y;
-  acc.y -= a.x * b.y + a.y * b.x;
+__device__ __forceinline__ void cfms(T& acc, T a, T b) {  // acc -= a b, four fused multiply-adds
+  acc.x = fma(-a.x, b.x, acc.x);
+  acc.x = fma(a.y, b.y, acc.x);
+  acc.y = fma(-a.x, b.y, acc.y);
+  acc.y = fma(-a.y, b.x, acc.y);
 }
 
 template <typename T>
@@ -327,21 +330,18 @@ __global__ void __launch_bounds__(256) k_getrf64(T* A, int64_t lda, int64_t j0, 
     }
     __syncthreads();
     if (c > k && c < kb) {
+      // rows i = rg + 4 j > k: all 16 candidates at once (predicated) so the loads overlap
       const T u = D[k * LD + c];
-      // rows i = rg + 4 j > k
-      const int jb = (k + 1 - rg + 3) >> 2;
-      for (int j0r = jb; j0r < 16; j0r += 4) {
-        T l[4];
+      T l[16];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int i2 = rg + 4 * (j0r + q);
-          l[q] = (j0r + q < 16 && i2 < kb) ? D[i2 * LD + k] : T{0, 0};
-        }
+      for (int j = 0; j < 16; ++j) {
+        const int i2 = rg + 4 * j;
+        l[j] = (i2 > k && i2 < kb) ? D[i2 * LD + k] : T{0, 0};
+      }
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int i2 = rg + 4 * (j0r + q);
-          if (j0r + q < 16 && i2 < kb) cfms(D[i2 * LD + c], l[q], u);
-        }
+      for (int j = 0; j < 16; ++j) {
+        const int i2 = rg + 4 * j;
+        if (i2 > k && i2 < kb) cfms(D[i2 * LD + c], l[j], u);
       }
     }
     __syncthreads();
@@ -1013,6 +1013,7 @@ struct LUSteps {
   int64_t lda, n;
   int* ipiv;
   cudaStream_t st;
+  size_t tcwork_bytes;
   int laswp(int64_t c0, int64_t c1, int64_t p0, int64_t p1) {
     if (c1 <= c0 || p1 <= p0) return BEAST_OK;
     ProfScope ps(ctx, PK_LASWP, (double)(c1 - c0) * (p1 - p0) * 2 * sizeof(T));
@@ -1031,12 +1032,12 @@ struct LUSteps {
     return BEAST_OK;
   }
   // A[r0:r0+m, c0:c0+nc] -= A[r0:r0+m, k0:k0+k] A[k0:k0+k, c0:c0+nc]
-  int gemm(int64_t r0, int64_t m, int64_t c0, int64_t nc, int64_t k0, int k, float* tcwork) {
+  int gemm(int64_t r0, int64_t m, int64_t c0, int64_t nc, int64_t k0, int k, void* tcwork) {
     if (m <= 0 || nc <= 0 || k <= 0) return BEAST_OK;
-    const bool tc = sizeof(T) == 8 && tcwork && m >= 64 && nc >= 64 && k % 16 == 0;
+    const bool tc = sizeof(T) == 8 && tcwork && m >= 64 && nc >= 64 && k % 32 == 0;
     ProfScope ps(ctx, tc ? PK_TCGEMM : PK_GEMM, 8.0 * (double)m * nc * k);
-    if (sizeof(T) == 8 && tcwork && m >= 64 && nc >= 64 && k % 16 == 0) {
-      return tc_gemm_sub(ctx, reinterpret_cast<float2*>(A), lda, n, r0, k0, c0, m, nc, k, tcwork);
+    if (tc) {
+      return tc_gemm_sub(ctx, reinterpret_cast<float2*>(A), lda, r0, k0, c0, m, nc, k, tcwork, tcwork_bytes);
     }
     dim3 g((unsigned)((m + GT - 1) / GT), (unsigned)((nc + GT - 1) / GT));
     k_gemm_sub<T, R><<<g, 256, 0, st>>>(A + r0 + c0 * lda, lda, A + r0 + k0 * lda, lda, A + k0 + c0 * lda,
@@ -1085,11 +1086,14 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   BEAST_CUDA_TRY(ctx, cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned int) + sizeof(int), st));
   BEAST_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), st));
   GridSync gs{bar, bar + 1, reinterpret_cast<int*>(bar + 2)};
-  // tensor-core workspace: the expanded L21 block (2M x 2NB floats)
-  float* tcwork = nullptr;
-  if (sizeof(T) == 8 && tc_gemm_supported(A, lda, NB) && n > NB)
-    BEAST_CUDA_TRY(ctx, cudaMallocAsync(&tcwork, (size_t)2 * n * 2 * NB * sizeof(float), st));
-  LUSteps<T, R> S{ctx, A, lda, n, ipiv, st};
+  // tensor-core workspace: the FP16 operands of the largest update (M, N <= n, K <= NB)
+  void* tcwork = nullptr;
+  size_t tcwork_bytes = 0;
+  if (sizeof(T) == 8 && tc_gemm_supported(A, lda, NB) && n > NB) {
+    tcwork_bytes = tc_gemm_work_bytes(n, n, NB);
+    BEAST_CUDA_TRY(ctx, cudaMallocAsync(&tcwork, tcwork_bytes, st));
+  }
+  LUSteps<T, R> S{ctx, A, lda, n, ipiv, st, tcwork_bytes};
 
   int rc = BEAST_OK;
   for (int64_t J0 = 0; J0 < n && rc == BEAST_OK; J0 += NB) {

@@ -1,20 +1,28 @@
-// tc_gemm.cu -- tensor-core (tcgen05, TF32) trailing update of the complex FP32 LU.
+// tc_gemm.cu -- tensor-core (tcgen05, FP16 operands, FP32 accumulation) trailing update of
+// the complex FP32 LU.
 //
 //   C -= A B   with C (M x N), A (M x K), B (K x N) complex64, column-major
 //
 // is evaluated as one real GEMM on the interleaved (re, im) storage:
 //   C' (2M x N) -= A' (2M x 2K) B' (2K x N)
-//   C', B' = the real views of C and B (no copy: element (r, c) of the complex matrix
-//            occupies rows 2r, 2r+1 of column c of the real view)
-//   A'     = A expanded into 2x2 real blocks [[ar, -ai], [ai, ar]], written K-major and
-//            rounded to TF32 by k_expand.
-// Kernel k_tc_gemm: one CTA per 128 x 256 tile of C'; a single thread issues the TMA loads
-// (128-byte swizzle, 4-stage ring over K) and the tcgen05.mma instructions (M=128, N=256,
-// K=8 per instruction) into a 256-column TMEM accumulator; after tcgen05.commit all four
-// warps read their 32 TMEM lanes with tcgen05.ld and apply C' -= D with coalesced stores.
+//   C'  = the real view of C (no copy: element (r, c) of the complex matrix occupies rows
+//         2r, 2r+1 of column c of the real view)
+//   A'  = A expanded into 2x2 real blocks [[ar, -ai], [ai, ar]], K-major, row pair of complex
+//         row m scaled by a power of two s_m (k_expand_h)
+//   B'  = the real view of B, column j scaled by a power of two t_j (k_convert_bh)
+// Both operands are rounded to FP16 (11 significant bits, the precision of TF32) after the
+// scaling puts each row's / column's largest magnitude in [2^13, 2^14), so the FP16 range
+// never clips; the products accumulate in FP32 in TMEM and the epilogue multiplies by the
+// exact factor 1 / (s_m t_j).  FP16 runs the tensor cores at twice the TF32 rate with half
+// the operand bytes.
+// Kernel k_tc_gemm: persistent CTAs over 128 x 256 tiles of C'; a single thread issues the
+// TMA loads (128-byte swizzle, 4-stage ring over K) and the tcgen05.mma instructions (M=128,
+// N=256, K=16 per instruction) into a 256-column TMEM accumulator; four epilogue warps read
+// their 32 TMEM lanes with tcgen05.ld and apply C' -= D / (s t) through TMA bulk copies.
 // Every mbarrier wait is bounded by a clock budget: on expiry the CTA raises a status bit,
 // still frees its TMEM and returns (the host turns the bit into BEAST_ERR_TIMEOUT).
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -24,9 +32,9 @@
 
 namespace {
 
-constexpr int TM = 128, TN = 256, TK = 32;  // tile M (real rows), N, K per stage (floats)
+constexpr int TM = 128, TN = 256, TK = 64;  // tile M (real rows), N, K per stage (halves)
 constexpr int STAGES = 4;
-constexpr int A_BYTES = TM * TK * 4, B_BYTES = TN * TK * 4, STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int A_BYTES = TM * TK * 2, B_BYTES = TN * TK * 2, STAGE_BYTES = A_BYTES + B_BYTES;
 constexpr int CCH = 32;                           // epilogue chunk: 128 rows x 32 columns of C'
 constexpr int C_BYTES = TM * CCH * 4;              // 16 KB per chunk buffer
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 2 * C_BYTES + 1024 + 256;
@@ -103,17 +111,17 @@ __device__ __forceinline__ uint64_t smem_desc(uint32_t addr) {
   return d;
 }
 
-// instruction descriptor: D f32, A/B tf32, both K-major, M = 128, N = 256
-__host__ __device__ constexpr uint32_t idesc_tf32() {
-  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
+// instruction descriptor: D f32, A/B f16, both K-major, M = 128, N = 256
+__host__ __device__ constexpr uint32_t idesc_f16() {
+  return (1u << 4) | (0u << 7) | (0u << 10) | ((uint32_t)(TN >> 3) << 17) | ((uint32_t)(TM >> 4) << 24);
 }
 
-__device__ __forceinline__ void mma_tf32(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
-                                         uint32_t accum) {
+__device__ __forceinline__ void mma_f16(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                        uint32_t accum) {
   asm volatile(
       "{\n\t.reg .pred p;\n\t"
       "setp.ne.u32 p, %4, 0;\n\t"
-      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d_tmem),
       "l"(a), "l"(b), "r"(idesc), "r"(accum)
       : "memory");
 }
@@ -146,7 +154,7 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 __global__ void __launch_bounds__(192, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const __grid_constant__ CUtensorMap tmC, int c_row0, int c_col0, int m_rows, int n_cols,
-              int b_x0, int b_y0, int nk, int* status) {
+              const float* __restrict__ inv_sa, const float* __restrict__ inv_sb, int nk, int* status) {
   extern __shared__ unsigned char smraw[];
   const uint32_t base = (smem_u32(smraw) + 1023u) & ~1023u;
   unsigned char* gbase = smraw + (base - smem_u32(smraw));
@@ -204,7 +212,7 @@ __global__ void __launch_bounds__(192, 1)
         const uint32_t full = smem_u32(bars + B_FULL + s);
         mbar_expect_tx(full, STAGE_BYTES);
         tma_load_2d(sa, &tmA, kb * TK, m0, full);
-        tma_load_2d(sb, &tmB, b_x0 + kb * TK, b_y0 + n0, full);
+        tma_load_2d(sb, &tmB, kb * TK, n0, full);
       }
     }
     // no copy may still be landing in shared memory when the CTA exits: wait (bounded,
@@ -214,7 +222,7 @@ __global__ void __launch_bounds__(192, 1)
       mbar_wait(smem_u32(bars + B_FULL + j % STAGES), (j / STAGES) & 1, status, &no_abort);
   } else if (warp == 1 && lane == 0) {
     // ---- MMA issuer
-    const uint32_t idesc = idesc_tf32();
+    const uint32_t idesc = idesc_f16();
     uint32_t it = 0;
     int t = 0;
     for (int tile = blockIdx.x; tile < ntiles && !*s_abort; tile += gridDim.x, ++t) {
@@ -230,8 +238,8 @@ __global__ void __launch_bounds__(192, 1)
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t sa = base + s * STAGE_BYTES, sb = sa + A_BYTES;
 #pragma unroll
-        for (int kk = 0; kk < TK / 8; ++kk)
-          mma_tf32(acc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), idesc, (kb | kk) ? 1u : 0u);
+        for (int kk = 0; kk < TK / 16; ++kk)
+          mma_f16(acc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), idesc, (kb | kk) ? 1u : 0u);
         mma_commit(smem_u32(bars + B_EMPTY + s));
       }
       if (*s_abort) break;
@@ -267,6 +275,8 @@ __global__ void __launch_bounds__(192, 1)
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * TN);
       const int row = q * 32 + lane;
+      // 1 / s of this thread's row (rows beyond the block are clipped by the TMA store)
+      const float rs = m0 + row < m_rows ? inv_sa[(m0 + row) >> 1] : 0.f;
       bool ok = true;
       for (int c = 0; c < nch; ++c) {
         const int b = c & 1;
@@ -286,8 +296,14 @@ __global__ void __launch_bounds__(192, 1)
         }
         cuse[b]++;
         float* cb = cbuf_g + b * (TM * CCH);
+        // 1 / t of the chunk's columns, one per lane, broadcast by shuffles
+        const int gcol = n0 + c * CCH + lane;
+        const float cs = gcol < n_cols ? inv_sb[gcol] : 0.f;
 #pragma unroll
-        for (int i = 0; i < CCH; ++i) cb[i * TM + row] -= v[i];
+        for (int i = 0; i < CCH; ++i) {
+          const float ci = __shfl_sync(0xffffffffu, cs, i);
+          cb[i * TM + row] = fmaf(-(v[i] * ci), rs, cb[i * TM + row]);
+        }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("bar.sync 1, 128;" ::: "memory");
         if (leader) {
@@ -315,24 +331,90 @@ __global__ void __launch_bounds__(192, 1)
   }
 }
 
-// A' (K-major, row m' = 2m + t holds 2K floats): [[ar, -ai], [ai, ar]] blocks, TF32-rounded
-__global__ void k_expand(const float2* A, int64_t lda, int M, int K, float* Ap) {
-  int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  if (e >= (int64_t)M * K) return;
-  int m = (int)(e % M), k = (int)(e / M);
-  float2 a = A[m + (int64_t)k * lda];
-  auto tf = [](float x) {
-    uint32_t r;
-    asm("cvt.rna.tf32.f32 %0, %1;" : "=r"(r) : "f"(x));
-    return __uint_as_float(r);
-  };
-  float ar = tf(a.x), ai = tf(a.y);
-  float* r0 = Ap + (int64_t)(2 * m) * (2 * K);
-  float* r1 = r0 + 2 * K;
-  r0[2 * k] = ar;
-  r0[2 * k + 1] = -ai;
-  r1[2 * k] = ai;
-  r1[2 * k + 1] = ar;
+// scale 2^sh that brings a largest magnitude mx into [2^13, 2^14) (1 for mx = 0)
+__device__ __forceinline__ int scale_shift(float mx) {
+  if (!(mx > 0.f)) return 0;
+  int e;
+  frexpf(mx, &e);  // mx = f 2^e, f in [0.5, 1)
+  return max(-120, min(120, 14 - e));
+}
+
+// A' (K-major; rows 2m, 2m+1 hold 2K halves): [[ar, -ai], [ai, ar]] blocks times s_m;
+// inv_sa[m] = 1 / s_m.  A CTA takes 32 rows: the row maxima first, then 64-column slices
+// transposed through shared memory so that every warp writes whole row segments.
+__global__ void __launch_bounds__(256) k_expand_h(const float2* A, int64_t lda, int M, int K, __half2* Ap,
+                                                  float* inv_sa) {
+  __shared__ float red[8][33];
+  __shared__ float2 tile[32][65];
+  __shared__ float s_scale[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int m0 = blockIdx.x * 32, m = m0 + lane;
+  float mx = 0.f;
+  if (m < M)
+    for (int k = w; k < K; k += 8) {
+      const float2 a = A[m + (int64_t)k * lda];
+      mx = fmaxf(mx, fmaxf(fabsf(a.x), fabsf(a.y)));
+    }
+  red[w][lane] = mx;
+  __syncthreads();
+  if (w == 0) {
+    for (int j = 1; j < 8; ++j) mx = fmaxf(mx, red[j][lane]);
+    const int sh = scale_shift(mx);
+    s_scale[lane] = ldexpf(1.f, sh);
+    if (m < M) inv_sa[m] = ldexpf(1.f, -sh);
+  }
+  __syncthreads();
+  for (int k0 = 0; k0 < K; k0 += 64) {
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      const int k = k0 + w + 8 * j;
+      tile[lane][w + 8 * j] = (m < M && k < K) ? A[m + (int64_t)k * lda] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int r = w + 8 * i, mr = m0 + r;
+      if (mr < M) {
+        const float sc = s_scale[r];
+        __half2* row0 = Ap + (int64_t)(2 * mr) * K;  // 2K halves = K half2 per row
+        __half2* row1 = row0 + K;
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int kk = lane + 32 * h, k = k0 + kk;
+          if (k < K) {
+            const float2 a = tile[r][kk];
+            row0[k] = __floats2half2_rn(a.x * sc, -a.y * sc);
+            row1[k] = __floats2half2_rn(a.y * sc, a.x * sc);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+// B' (column j: 2K halves, (re, im) per k) times t_j; inv_sb[j] = 1 / t_j.  One warp per column.
+__global__ void __launch_bounds__(256) k_convert_bh(const float2* B, int64_t lda, int K, int N, __half2* Bp,
+                                                    float* inv_sb) {
+  const int lane = threadIdx.x & 31;
+  const int j = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (j >= N) return;
+  const float2* col = B + (int64_t)j * lda;
+  float mx = 0.f;
+  for (int k = lane; k < K; k += 32) {
+    const float2 a = col[k];
+    mx = fmaxf(mx, fmaxf(fabsf(a.x), fabsf(a.y)));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  const int sh = scale_shift(mx);
+  const float sc = ldexpf(1.f, sh);
+  if (lane == 0) inv_sb[j] = ldexpf(1.f, -sh);
+  __half2* out = Bp + (int64_t)j * K;
+  for (int k = lane; k < K; k += 32) {
+    const float2 a = col[k];
+    out[k] = __floats2half2_rn(a.x * sc, a.y * sc);
+  }
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
@@ -354,15 +436,15 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-bool make_map(CUtensorMap* m, const float* base, uint64_t dim0, uint64_t dim1, uint64_t stride1_bytes,
-              uint32_t box0, uint32_t box1, bool swizzle = true) {
+bool make_map(CUtensorMap* m, const void* base, uint64_t dim0, uint64_t dim1, uint64_t stride1_bytes,
+              uint32_t box0, uint32_t box1, bool swizzle, CUtensorMapDataType dt) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return false;
   cuuint64_t dims[2] = {dim0, dim1};
   cuuint64_t strides[1] = {stride1_bytes};
   cuuint32_t box[2] = {box0, box1};
   cuuint32_t es[2] = {1, 1};
-  CUresult r = fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, (void*)base, dims, strides, box, es,
+  CUresult r = fn(m, dt, 2, const_cast<void*>(base), dims, strides, box, es,
                   CU_TENSOR_MAP_INTERLEAVE_NONE,
                   swizzle ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_NONE,
                   CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -375,51 +457,63 @@ bool make_map(CUtensorMap* m, const float* base, uint64_t dim0, uint64_t dim1, u
 bool tc_gemm_supported(const void* A, int64_t lda, int K) {
   if (!encode_fn()) return false;
   if ((reinterpret_cast<uintptr_t>(A) & 15) != 0) return false;
-  if (lda % 2 != 0) return false;         // column stride of the real view: multiple of 16 B
-  if (K % 16 != 0) return false;          // 2K real = whole 32-float K blocks
+  if (lda % 2 != 0) return false;  // column stride of the real view: multiple of 16 B
+  if (K % 32 != 0) return false;   // 2K halves = whole 64-half K stages
   return true;
+}
+
+// bytes of workspace tc_gemm_sub needs for an M x K by K x N update
+size_t tc_gemm_work_bytes(int64_t M, int64_t N, int K) {
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  return al((size_t)M * K * 8) + al((size_t)N * K * 4) + al((size_t)M * 4) + al((size_t)N * 4);
 }
 
 // C -= A B (complex64) for the LU trailing update:
 //   A at (rowA, colA) of the matrix, M x K;  B at (rowB = colA, colB), K x N;  C at (rowA, colB)
-// Mat: base of the full matrix (n_total x n_total, ld lda); work: >= 2M x 2K floats
-int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t n_total, int64_t rowA,
-                int64_t colA, int64_t colB, int64_t M, int64_t N, int K, float* work) {
+// Mat: base of the full matrix (ld lda); work: tc_gemm_work_bytes(M, N, K) bytes or more
+int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t colB,
+                int64_t M, int64_t N, int K, void* work, size_t work_bytes) {
   cudaStream_t st = ctx->stream;
-  // TMA: the first C' row (2 rowA floats) and the B' rows (2 colA) must start on 16 bytes
-  if ((2 * rowA) % 4 != 0 || (2 * colA) % 4 != 0 || 2 * (rowA + M) > INT32_MAX)
+  // TMA: the first C' row (2 rowA floats) must start on 16 bytes
+  if ((2 * rowA) % 4 != 0 || K % 32 != 0 || 2 * (rowA + M) > INT32_MAX || colB + N > INT32_MAX)
     return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: unaligned block");
+  if (tc_gemm_work_bytes(M, N, K) > work_bytes)
+    return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: workspace too small");
   static bool attr_done[64] = {false};
   int dev = ctx->device;
   if (!attr_done[dev]) {
     BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     attr_done[dev] = true;
   }
-  {
-    int64_t tot = M * (int64_t)K;
-    k_expand<<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(Mat + rowA + colA * lda, lda, (int)M, K, work);
-    ctx->launches += 1;
-  }
-  CUtensorMap tmA, tmB;
-  // A': 2K floats per row (x), 2M rows (y)
-  if (!make_map(&tmA, work, (uint64_t)2 * K, (uint64_t)2 * M, (uint64_t)2 * K * 4, TK, TM))
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  char* w = static_cast<char*>(work);
+  __half2* Ap = reinterpret_cast<__half2*>(w);
+  __half2* Bp = reinterpret_cast<__half2*>(w + al((size_t)M * K * 8));
+  float* inv_sa = reinterpret_cast<float*>(w + al((size_t)M * K * 8) + al((size_t)N * K * 4));
+  float* inv_sb = reinterpret_cast<float*>(reinterpret_cast<char*>(inv_sa) + al((size_t)M * 4));
+  k_expand_h<<<(unsigned)((M + 31) / 32), 256, 0, st>>>(Mat + rowA + colA * lda, lda, (int)M, K, Ap, inv_sa);
+  k_convert_bh<<<(unsigned)((N + 7) / 8), 256, 0, st>>>(Mat + colA + colB * lda, lda, K, (int)N, Bp, inv_sb);
+  ctx->launches += 2;
+  CUtensorMap tmA, tmB, tmC;
+  // A': 2K halves per row (x), 2M rows (y); B': 2K halves per column (x), N columns (y)
+  if (!make_map(&tmA, Ap, (uint64_t)2 * K, (uint64_t)2 * M, (uint64_t)2 * K * 2, TK, TM, true,
+                CU_TENSOR_MAP_DATA_TYPE_FLOAT16))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (A') failed");
-  // B': real view of the matrix, columns clipped at the end of the update block so that the
-  // tile columns beyond it load zeros (and contribute nothing)
-  const float* real = reinterpret_cast<const float*>(Mat);
-  if (!make_map(&tmB, real, (uint64_t)2 * n_total, (uint64_t)(colB + N), (uint64_t)2 * lda * 4, TK, TN))
+  if (!make_map(&tmB, Bp, (uint64_t)2 * K, (uint64_t)N, (uint64_t)2 * K * 2, TK, TN, true,
+                CU_TENSOR_MAP_DATA_TYPE_FLOAT16))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (B') failed");
   // C': real view clipped to the update block (rows up to 2(rowA+M), columns up to colB+N):
   // the bulk stores never touch anything outside it
-  CUtensorMap tmC;
-  if (!make_map(&tmC, real, (uint64_t)2 * (rowA + M), (uint64_t)(colB + N), (uint64_t)2 * lda * 4, TM, CCH, false))
+  const float* real = reinterpret_cast<const float*>(Mat);
+  if (!make_map(&tmC, real, (uint64_t)2 * (rowA + M), (uint64_t)(colB + N), (uint64_t)2 * lda * 4, TM, CCH, false,
+                CU_TENSOR_MAP_DATA_TYPE_FLOAT32))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (C') failed");
   const int m_rows = (int)(2 * M), n_cols = (int)N;
   const int ntiles = ((n_cols + TN - 1) / TN) * ((m_rows + TM - 1) / TM);
   const int grid = std::min(ntiles, std::max(1, ctx->num_sms));
   const int nk = (2 * K) / TK;
-  k_tc_gemm<<<grid, 192, SMEM_BYTES, st>>>(tmA, tmB, tmC, (int)(2 * rowA), (int)colB, m_rows, n_cols,
-                                           (int)(2 * colA), (int)colB, nk, ctx->d_flag);
+  k_tc_gemm<<<grid, 192, SMEM_BYTES, st>>>(tmA, tmB, tmC, (int)(2 * rowA), (int)colB, m_rows, n_cols, inv_sa,
+                                           inv_sb, nk, ctx->d_flag);
   BEAST_CUDA_TRY(ctx, cudaGetLastError());
   return BEAST_OK;
 }

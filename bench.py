@@ -304,7 +304,7 @@ def main():
     traffic = 7.18e-3 * work / nl if name == "lu_tc_gemm" else None
     roof = {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak, "unit": unit,
             "frac": achieved / peak, "peak_source": src,
-            "peak_note": "measured dense bf16 (sustained); the kernel runs TF32 operands",
+            "peak_note": "measured dense bf16 (sustained); the kernel runs FP16 operands with FP32 accumulation (same tensor rate as bf16)",
             "traffic": traffic, "launches": nl, "avg_launch_ms": kms / nl,
             "dominant_by_time": dominant}
     breakdown = {k: {"ms": v[0], "launches": v[1], "share": v[0] / sum(w[0] for w in prof.values())}

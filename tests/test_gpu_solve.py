@@ -69,8 +69,9 @@ def test_gmres_contract(efie):
 def test_lu_factors_exact(n, dtype):
     """P A = L U reproduced exactly: L has dyadic entries (k/64, |re|+|im| < 1, at most 7
     significant bits), U small integers with a dominant power-of-two diagonal, so every
-    product and partial sum of the factorisation is exact in TF32 x TF32 -> FP32 (the
-    tensor-core trailing update for c64) and in FP64, and partial pivoting keeps the
+    product and partial sum of the factorisation is exact in FP16 x FP16 -> FP32 after the
+    power-of-two row/column scaling (the tensor-core trailing update for c64) and in FP64,
+    and partial pivoting keeps the
     diagonal.  Any indexing or layout error of the GEMM shows up as a nonzero error."""
     import ctypes as C
     import torch
