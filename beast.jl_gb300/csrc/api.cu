@@ -795,8 +795,8 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
       }
       if (rc) break;
       it_max = std::max(it_max, it);
-      res_max = std::max(res_max, rel);
-      if (rel > tol) {
+      res_max = std::isfinite(rel) ? std::max(res_max, rel) : rel;
+      if (!(rel <= tol)) {  // also a non-finite residual
         if (!pivot) retry = true;
         else rc = beast_fail(ctx, BEAST_ERR_NOCONV, "iterative refinement did not reach the tolerance");
       }

@@ -16,6 +16,8 @@
 //             gather: every output entry written once, no atomics, deterministic.
 #include <cuda_runtime.h>
 
+#include <type_traits>
+
 #include <cmath>
 
 #include "internal.h"
@@ -1108,52 +1110,90 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
 // ------------------------------------------------------------------------------------
 // gather: Z[m, n] = sum_{(p,r,a) of m} sum_{(q,s,b) of n} a b Zcell[nst p + r, nsb q' + s]
 // ------------------------------------------------------------------------------------
+// A thread owns one test function m and a run of GATHER_NCOL consecutive trial functions: its
+// test entries (Zcell row, coefficient) are loaded once into registers, the trial entries are
+// warp-uniform loads, and each output is a sum of (#test x #trial) products.  With a complex
+// FP32 Zcell and output (the mixed path) the sums are FP32; otherwise FP64.
+constexpr int GATHER_NCOL = 16, GATHER_MAXE = 8;
 template <int ZC64, int OC64>
-__global__ void k_gather(GatherArgs G, const int64_t* tptr, const int* tcell, const int* tshape,
-                         const double* tcoef, const int64_t* bptr, const int* bcell,
-                         const int* bshape, const double* bcoef, int nst, int nsb,
-                         int64_t nrows) {
+__global__ void __launch_bounds__(256) k_gather(GatherArgs G, const int64_t* tptr, const int* tcell,
+                                                const int* tshape, const double* tcoef,
+                                                const int64_t* bptr, const int* bcell, const int* bshape,
+                                                const double* bcoef, int nst, int nsb, int64_t nrows) {
+  typedef typename std::conditional<ZC64 && OC64, float, double>::type A;
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  for (int64_t n = G.n0 + blockIdx.y; n < G.n1; n += gridDim.y) {
-    if (m >= nrows) continue;
-    double re = 0, im = 0;
+  if (m >= nrows) return;
+  const int64_t e0 = tptr[m], ne = tptr[m + 1] - e0;
+  int64_t trow[GATHER_MAXE];
+  A tc[GATHER_MAXE];
+#pragma unroll
+  for (int j = 0; j < GATHER_MAXE; ++j) {
+    trow[j] = 0;
+    tc[j] = 0;
+    if (j < ne) {
+      trow[j] = (int64_t)nst * tcell[e0 + j] + tshape[e0 + j];
+      tc[j] = (A)tcoef[e0 + j];
+    }
+  }
+  const int64_t nb0 = G.n0 + (int64_t)blockIdx.y * GATHER_NCOL;
+  const int64_t nb1 = nb0 + GATHER_NCOL < G.n1 ? nb0 + GATHER_NCOL : G.n1;
+  for (int64_t n = nb0; n < nb1; ++n) {
+    A re = 0, im = 0;
     for (int64_t f = bptr[n]; f < bptr[n + 1]; ++f) {
-      int ql = G.qlocal[bcell[f]];
-      int64_t col = (int64_t)nsb * ql + bshape[f];
-      double b = bcoef[f];
-      for (int64_t e = tptr[m]; e < tptr[m + 1]; ++e) {
-        int64_t row = (int64_t)nst * tcell[e] + tshape[e];
-        double ab = tcoef[e] * b;
-        int64_t idx = col * G.ldc + row;
-        if (ZC64) {
-          float2 z = reinterpret_cast<const float2*>(G.zcell)[idx];
-          re += ab * z.x;
-          im += ab * z.y;
-        } else {
-          double2 z = reinterpret_cast<const double2*>(G.zcell)[idx];
-          re += ab * z.x;
-          im += ab * z.y;
+      const int ql = G.qlocal[bcell[f]];
+      const int64_t col = ((int64_t)nsb * ql + bshape[f]) * G.ldc;
+      const A b = (A)bcoef[f];
+      if (ne <= GATHER_MAXE) {
+#pragma unroll
+        for (int j = 0; j < GATHER_MAXE; ++j) {
+          if (j < ne) {
+            const A ab = tc[j] * b;
+            if (ZC64) {
+              const float2 z = reinterpret_cast<const float2*>(G.zcell)[col + trow[j]];
+              re += ab * (A)z.x;
+              im += ab * (A)z.y;
+            } else {
+              const double2 z = reinterpret_cast<const double2*>(G.zcell)[col + trow[j]];
+              re += ab * (A)z.x;
+              im += ab * (A)z.y;
+            }
+          }
+        }
+      } else {
+        for (int64_t e = e0; e < e0 + ne; ++e) {
+          const A ab = (A)tcoef[e] * b;
+          const int64_t idx = col + (int64_t)nst * tcell[e] + tshape[e];
+          if (ZC64) {
+            const float2 z = reinterpret_cast<const float2*>(G.zcell)[idx];
+            re += ab * (A)z.x;
+            im += ab * (A)z.y;
+          } else {
+            const double2 z = reinterpret_cast<const double2*>(G.zcell)[idx];
+            re += ab * (A)z.x;
+            im += ab * (A)z.y;
+          }
         }
       }
     }
-    double vr = G.cr * re - G.ci * im, vi = G.cr * im + G.ci * re;
-    int64_t o = (G.row_off + m) + (G.col_off + n) * G.ldz;
+    const A cr = (A)G.cr, ci = (A)G.ci;
+    A vr = cr * re - ci * im, vi = cr * im + ci * re;
+    const int64_t o = (G.row_off + m) + (G.col_off + n) * G.ldz;
     if (OC64) {
       float2* Z = reinterpret_cast<float2*>(G.Z);
       if (G.accumulate) {
-        float2 old = Z[o];
-        vr += old.x;
-        vi += old.y;
+        const float2 old = Z[o];
+        vr += (A)old.x;
+        vi += (A)old.y;
       }
       Z[o] = make_float2((float)vr, (float)vi);
     } else {
       double2* Z = reinterpret_cast<double2*>(G.Z);
       if (G.accumulate) {
-        double2 old = Z[o];
-        vr += old.x;
-        vi += old.y;
+        const double2 old = Z[o];
+        vr += (A)old.x;
+        vi += (A)old.y;
       }
-      Z[o] = make_double2(vr, vi);
+      Z[o] = make_double2((double)vr, (double)vi);
     }
   }
 }
@@ -1450,7 +1490,9 @@ cudaError_t launch_gather(const GatherArgs& g, cudaStream_t st) {
   int64_t nrows = ts->nfuncs;
   if (nrows == 0 || g.n1 <= g.n0) return cudaSuccess;
   int th = 256;
-  dim3 grid((unsigned)((nrows + th - 1) / th), (unsigned)std::min<int64_t>(g.n1 - g.n0, 65535));
+  const int64_t ncb = (g.n1 - g.n0 + GATHER_NCOL - 1) / GATHER_NCOL;
+  if (ncb > 65535) return cudaErrorInvalidConfiguration;
+  dim3 grid((unsigned)((nrows + th - 1) / th), (unsigned)ncb);
   int nst = ts->kind == BEAST_P0 ? 1 : 3, nsb = bs->kind == BEAST_P0 ? 1 : 3;
 #define GATHER(ZC, OC)                                                                       \
   k_gather<ZC, OC><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_cell, ts->fn_shape, ts->fn_coeff, \

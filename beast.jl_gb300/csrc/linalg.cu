@@ -288,8 +288,14 @@ __global__ void k_laswp(T* A, int64_t lda, int64_t c0, int64_t c1, int64_t p0, i
 
 // ---- LU of a diagonal block without pivoting (mixed path) --------------------------------
 // A[j0:j0+kb, j0:j0+kb] = L11 U11 in place, kb <= 64, one CTA of 256 threads in shared
-// memory; thread t updates column t % 64 of the rows congruent to t / 64 modulo 4.  A zero
-// pivot sets *info (1-based column) and the kernel stops.
+// memory, two pivots per pass (two barriers per pair of columns):
+//   A: every thread forms l_{k+1,k} and the second pivot u_{k+1,k+1} itself; threads 0..63
+//      finish the multipliers of columns k and k+1 for one row each, threads 64..127 update
+//      row k+1 for one column each;
+//   B: rank-2 update of the trailing block, thread t on column t % 64 and the rows congruent
+//      to t / 64 modulo 4 (the two updates applied one after the other, as the one-pivot
+//      recurrence does).
+// A zero pivot sets *info (1-based column) and the kernel stops.
 constexpr int TRI = 64;
 
 template <typename T>
@@ -299,10 +305,26 @@ __device__ __forceinline__ void cfms(T& acc, T a, T b) {  // acc -= a b, four fu
   acc.y = fma(-a.x, b.y, acc.y);
   acc.y = fma(-a.y, b.x, acc.y);
 }
+template <typename T>
+__device__ __forceinline__ T cmulx(T a, T b) {
+  T r;
+  r.x = a.x * b.x - a.y * b.y;
+  r.y = a.x * b.y + a.y * b.x;
+  return r;
+}
+template <typename T>
+__device__ __forceinline__ bool crecip(T p, T& r) {  // r = 1 / p; false for p = 0
+  typedef decltype(T().x) RT;
+  const RT den = p.x * p.x + p.y * p.y;
+  if (den == (RT)0) return false;
+  const RT id = (RT)1 / den;
+  r.x = p.x * id;
+  r.y = -p.y * id;
+  return true;
+}
 
 template <typename T>
 __global__ void __launch_bounds__(256) k_getrf64(T* A, int64_t lda, int64_t j0, int kb, int* info) {
-  typedef decltype(T().x) RT;
   constexpr int LD = TRI + 1;
   extern __shared__ unsigned char smraw[];
   T* D = reinterpret_cast<T*>(smraw);  // row-major, ld LD
@@ -312,36 +334,65 @@ __global__ void __launch_bounds__(256) k_getrf64(T* A, int64_t lda, int64_t j0, 
     D[r * LD + k] = A[(j0 + r) + (j0 + k) * lda];
   }
   __syncthreads();
-  for (int k = 0; k < kb; ++k) {
-    const T p = D[k * LD + k];
-    const RT den = p.x * p.x + p.y * p.y;
-    if (den == (RT)0) {  // uniform
+  for (int k = 0; k < kb; k += 2) {
+    T i0;
+    if (!crecip(D[k * LD + k], i0)) {  // uniform
       if (tid == 0) atomicCAS(info, 0, (int)(j0 + k + 1));
       return;
     }
-    const int i = k + 1 + tid;
-    if (i < kb) {
-      const RT ir = p.x / den, ii = -p.y / den;
-      const T a = D[i * LD + k];
-      T l;
-      l.x = a.x * ir - a.y * ii;
-      l.y = a.x * ii + a.y * ir;
-      D[i * LD + k] = l;
+    if (k + 1 == kb) break;
+    const T l1k = cmulx(D[(k + 1) * LD + k], i0);
+    const T u01 = D[k * LD + k + 1];
+    T p1 = D[(k + 1) * LD + k + 1], i1;
+    cfms(p1, l1k, u01);
+    if (!crecip(p1, i1)) {
+      if (tid == 0) atomicCAS(info, 0, (int)(j0 + k + 2));
+      return;
+    }
+    // phase A
+    if (tid < TRI) {
+      const int i = k + 2 + tid;
+      if (i < kb) {
+        const T lk = cmulx(D[i * LD + k], i0);
+        T t1 = D[i * LD + k + 1];
+        cfms(t1, lk, u01);
+        D[i * LD + k] = lk;
+        D[i * LD + k + 1] = cmulx(t1, i1);
+      }
+    } else if (tid < 2 * TRI) {
+      const int cc = k + 2 + (tid - TRI);
+      if (cc < kb) cfms(D[(k + 1) * LD + cc], l1k, D[k * LD + cc]);
     }
     __syncthreads();
-    if (c > k && c < kb) {
-      // rows i = rg + 4 j > k: all 16 candidates at once (predicated) so the loads overlap
-      const T u = D[k * LD + c];
-      T l[16];
+    // phase B (row k+1 left of the trailing block: multiplier and the second pivot, written
+    // here because every thread read them before the barrier)
+    if (tid == 0) {
+      D[(k + 1) * LD + k] = l1k;
+      D[(k + 1) * LD + k + 1] = p1;
+    }
+    if (c >= k + 2 && c < kb) {
+      const T u0 = D[k * LD + c], u1 = D[(k + 1) * LD + c];
+      const int jb = (k + 2 - rg + 3) >> 2;  // first j with rg + 4 j >= k + 2
+      for (int jj = jb; jj < 16; jj += 4) {
+        T l0[4], l1[4], v[4];
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int i2 = rg + 4 * j;
-        l[j] = (i2 > k && i2 < kb) ? D[i2 * LD + k] : T{0, 0};
-      }
+        for (int q = 0; q < 4; ++q) {
+          const int i = rg + 4 * (jj + q);
+          if (jj + q < 16 && i < kb) {
+            l0[q] = D[i * LD + k];
+            l1[q] = D[i * LD + k + 1];
+            v[q] = D[i * LD + c];
+          }
+        }
 #pragma unroll
-      for (int j = 0; j < 16; ++j) {
-        const int i2 = rg + 4 * j;
-        if (i2 > k && i2 < kb) cfms(D[i2 * LD + c], l[j], u);
+        for (int q = 0; q < 4; ++q) {
+          const int i = rg + 4 * (jj + q);
+          if (jj + q < 16 && i < kb) {
+            cfms(v[q], l0[q], u0);
+            cfms(v[q], l1[q], u1);
+            D[i * LD + c] = v[q];
+          }
+        }
       }
     }
     __syncthreads();

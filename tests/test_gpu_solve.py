@@ -118,3 +118,27 @@ def test_mixed_falls_back_to_pivoting():
     b = rng.normal(size=n) + 0j
     x, it, res = bg.solve(A.astype(np.complex64), b, precision=bg.MIXED, tol=1e-10)
     assert np.linalg.norm(A.astype(np.complex64).astype(np.complex128) @ x - b) / np.linalg.norm(b) < 1e-9
+
+
+@pytest.mark.parametrize("n", [1101, 1536])
+def test_mixed_unpivoted_path_converges_without_fallback(n):
+    """a diagonally dominant c64 matrix: the unpivoted factorisation (diagonal-block LU two
+    pivots per pass, odd last block for n = 1101) must itself reach the tolerance -- no
+    hand-over to partial pivoting (no row interchanges recorded by the profiler)"""
+    import torch
+    ctx = bg.get_context(0)
+    rng = np.random.default_rng(5)
+    A = (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)) + 4 * n ** 0.5 * np.eye(n)).astype(np.complex64)
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda().T
+    ctx.prof_enable(True)
+    try:
+        x, it, res = bg.solve(At, b, precision=bg.MIXED, tol=1e-12, ctx=ctx)
+        prof = ctx.prof_read()
+    finally:
+        ctx.prof_enable(False)
+    assert "lu_laswp" not in prof and "lu_panel" in prof
+    assert prof["lu_panel"][1] == (n + 63) // 64  # one factorisation: one record per panel
+    assert it <= 4 and res < 1e-12
+    r = A.astype(np.complex128) @ x - b
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-12
