@@ -898,6 +898,65 @@ DEV void ss_node(int cls, int n, int64_t item, const double* glx, const double* 
   *w = wt;
 }
 
+// ss_node in FP32 for the mixed path, with D = X - Y formed from the maps' own factors (it
+// scales with xi, so x - y keeps its relative precision near the singularity)
+DEV void ss_node_f(int cls, int n, int item, const float* glx, const float* glw, float* X, float* Y,
+                   float* D, float* w) {
+  const int nreg = cls == 1 ? 2 : 6;
+  const int reg = item % nreg;
+  int k = item / nreg;
+  const int i4 = k % n;
+  k /= n;
+  const int i3 = k % n;
+  k /= n;
+  const int i2 = k % n;
+  const int i1 = k / n;
+  const float xi = glx[i1], e1 = glx[i2], e2 = glx[i3], e3 = glx[i4];
+  const float ww = glw[i1] * glw[i2] * glw[i3] * glw[i4];
+  float A[2], B[2], AB[2], wt;
+  const int sub = reg >> 1;
+  const bool swap = reg & 1;
+  if (cls == 1) {  // common vertex
+    wt = ww * xi * xi * xi * e2;
+    A[0] = xi; A[1] = xi * e1;
+    B[0] = xi * e2; B[1] = xi * e2 * e3;
+    AB[0] = xi * (1.0f - e2); AB[1] = xi * (e1 - e2 * e3);
+  } else if (cls == 2) {  // common edge
+    float ap, bb, cc;
+    if (sub == 0) { ap = e1; bb = e1 * e2; cc = e1 * e3; }
+    else if (sub == 1) { bb = e1; ap = e1 * e2; cc = e1 * e3; }
+    else { cc = e1; ap = e1 * e2; bb = e1 * e3; }
+    wt = ww * xi * xi * xi * (1.0f - ap) * e1 * e1;
+    A[0] = xi; A[1] = xi * bb;
+    B[0] = xi * (1.0f - ap); B[1] = xi * (1.0f - ap) * cc;
+    AB[0] = xi * ap; AB[1] = xi * (bb - (1.0f - ap) * cc);
+  } else {  // common face
+    const float s = e1, t = e2, u = e3;
+    wt = ww * xi * xi * xi * s * (1.0f - s);
+    if (sub == 0) {
+      const float ap = s * t, e = s * (1.0f - t), b = (1.0f - s) * u;
+      A[0] = xi; A[1] = xi * b;
+      B[0] = xi * (1.0f - ap); B[1] = xi * (b + e);
+      AB[0] = xi * ap; AB[1] = -xi * e;
+    } else {
+      const float ap = sub == 1 ? s : s * t, ep = sub == 1 ? s * t : s, cp = (1.0f - s) * u;
+      A[0] = xi; A[1] = xi * (cp + ep);
+      B[0] = xi * (1.0f - ap); B[1] = xi * cp;
+      AB[0] = xi * ap; AB[1] = xi * ep;
+    }
+  }
+  if (swap) {
+    X[0] = B[0]; X[1] = B[1]; Y[0] = A[0]; Y[1] = A[1];
+    D[0] = -AB[0]; D[1] = -AB[1];
+  } else {
+    X[0] = A[0]; X[1] = A[1]; Y[0] = B[0]; Y[1] = B[1];
+    D[0] = AB[0]; D[1] = AB[1];
+  }
+  *w = wt;
+}
+
+DEV V3<float> v3f(V3<double> a) { return V3<float>{(float)a.x, (float)a.y, (float)a.z}; }
+
 struct NearParams {
   OpParams op;
   beast_qs_desc qs;
@@ -909,6 +968,7 @@ struct NearParams {
   int nnear;
   void* zcell;
   int c64;
+  int ss32;  // Sauter-Schwab moments of RT Maxwell pairs in FP32 (mixed precision)
   int64_t ldc;
   int* flag;
   TriRuleDev ro, ri;
@@ -920,9 +980,12 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
   // Gauss-Legendre nodes in shared memory (lanes read different nodes: a constant-memory
   // read would serialise)
   __shared__ double s_glx[210], s_glw[210];
+  __shared__ float s_glxf[210], s_glwf[210];
   for (int k = threadIdx.x; k < 210; k += blockDim.x) {
     s_glx[k] = c_gl_x[k];
     s_glw[k] = c_gl_w[k];
+    s_glxf[k] = (float)c_gl_x[k];
+    s_glwf[k] = (float)c_gl_w[k];
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -985,7 +1048,66 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
 #pragma unroll
       for (int k = 0; k < 22; ++k) m[k] = 0.0;
       const V3<double> d = cp - cq;
-      for (int64_t it = lane; it < items; it += 32) {
+      if (P.ss32) {
+        // FP32: x - y = X0 Et1 + X1 Et2 - Y0 Es1 - Y1 Es2 over the edge vectors of the two
+        // charts from the shared first vertex (common terms folded into D = X - Y)
+        const V3<float> a0 = v3f(t.v[pt[0]] - cp), et1 = v3f(t.v[pt[1]] - t.v[pt[0]]),
+                        et2 = v3f(t.v[pt[2]] - t.v[pt[1]]);
+        const V3<float> b0 = v3f(s.v[ps[0]] - cq), es1 = v3f(s.v[ps[1]] - s.v[ps[0]]),
+                        es2 = v3f(s.v[ps[2]] - s.v[ps[1]]);
+        const V3<float> df = v3f(d);
+        const float gif = (float)gi, grf = (float)gr;
+        const float* glxf = s_glxf + c_gl_off[n - 1];
+        const float* glwf = s_glwf + c_gl_off[n - 1];
+        float mf[22];
+#pragma unroll
+        for (int k = 0; k < 22; ++k) mf[k] = 0.0f;
+        for (int it = lane; it < (int)items; it += 32) {
+          float X[2], Y[2], D[2], w;
+          ss_node_f(np_.cls, n, it, glxf, glwf, X, Y, D, &w);
+          const V3<float> xi = a0 + X[0] * et1 + X[1] * et2;
+          const V3<float> eta = b0 + Y[0] * es1 + Y[1] * es2;
+          V3<float> r;
+          if (np_.cls == 3)
+            r = D[0] * et1 + D[1] * et2;
+          else if (np_.cls == 2)
+            r = D[0] * et1 + (X[1] * et2 - Y[1] * es2);
+          else
+            r = (X[0] * et1 + X[1] * et2) - (Y[0] * es1 + Y[1] * es2);
+          const float R = sqrtf(dot(r, r));
+          const float iR = 1.0f / R;
+          float sn, cs;
+          sincosf(gif * R, &sn, &cs);
+          const float amp = (grf == 0.0f ? 1.0f : expf(-grf * R)) * (float)I4PI * iR * w;
+          float cr = amp * cs, ci = -amp * sn;
+          V3<float> a, b, c3;
+          float s0;
+          if (sl) {
+            s0 = dot(xi, eta);
+            a = xi;
+            b = eta;
+            c3 = V3<float>{0, 0, 0};
+            mf[0] += cr;
+            mf[1] += ci;
+          } else {
+            const float pr = -(grf + iR) * iR, pi = -gif * iR;
+            const float nr = pr * cr - pi * ci, ni = pr * ci + pi * cr;
+            cr = nr;
+            ci = ni;
+            s0 = dot(xi, cross(df, eta));
+            a = cross(xi, r);
+            b = cross(r, eta);
+            c3 = r;
+          }
+          mf[2] += s0 * cr; mf[3] += s0 * ci;
+          mf[4] += a.x * cr; mf[5] += a.x * ci; mf[6] += a.y * cr; mf[7] += a.y * ci; mf[8] += a.z * cr; mf[9] += a.z * ci;
+          mf[10] += b.x * cr; mf[11] += b.x * ci; mf[12] += b.y * cr; mf[13] += b.y * ci; mf[14] += b.z * cr; mf[15] += b.z * ci;
+          mf[16] += c3.x * cr; mf[17] += c3.x * ci; mf[18] += c3.y * cr; mf[19] += c3.y * ci; mf[20] += c3.z * cr; mf[21] += c3.z * ci;
+        }
+#pragma unroll
+        for (int k = 0; k < 22; ++k) m[k] = (double)mf[k];
+      }
+      for (int64_t it = P.ss32 ? items : (int64_t)lane; it < items; it += 32) {
         double X[2], Y[2], w;
         ss_node(np_.cls, n, it, glx, glw, X, Y, &w);
         const double lt[3] = {1.0 - X[0], X[0] - X[1], X[1]}, ls[3] = {1.0 - Y[0], Y[0] - Y[1], Y[1]};
@@ -1475,6 +1597,7 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   P.nnear = nnear;
   P.zcell = a.zcell;
   P.c64 = a.zcell_c64;
+  P.ss32 = a.precision == BEAST_MIXED;
   P.ldc = a.ldc;
   P.flag = a.flag;
   P.ro = ro;
