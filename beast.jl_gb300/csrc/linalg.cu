@@ -1112,7 +1112,7 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   while (nb > 8 && (size_t)(rows0 * (nb + 1) + nb) * sizeof(T) > smem_cap) nb /= 2;
   if ((size_t)(rows0 * (nb + 1) + nb) * sizeof(T) > smem_cap)
     return beast_fail(ctx, BEAST_ERR_ARG, "matrix too large for the shared-memory panel");
-  const int NB = 8 * nb;
+  const int NB = 16 * nb;
   const size_t panel_smem = (size_t)(rows0 * (nb + 1) + nb) * sizeof(T);
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_getrf64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,

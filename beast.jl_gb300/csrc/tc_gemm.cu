@@ -18,7 +18,8 @@
 // Kernel k_tc_gemm: persistent CTAs over 128 x 256 tiles of C'; a single thread issues the
 // TMA loads (128-byte swizzle, 4-stage ring over K) and the tcgen05.mma instructions (M=128,
 // N=256, K=16 per instruction) into a 256-column TMEM accumulator; four epilogue warps read
-// their 32 TMEM lanes with tcgen05.ld and apply C' -= D / (s t) through TMA bulk copies.
+// their 32 TMEM lanes with tcgen05.ld and apply C' -= D / (s t) as TMA reduce-adds of
+// shared-memory chunks (C' is read and written by the TMA unit only).
 // Every mbarrier wait is bounded by a clock budget: on expiry the CTA raises a status bit,
 // still frees its TMEM and returns (the host turns the bit into BEAST_ERR_TIMEOUT).
 #include <cuda.h>
@@ -96,7 +97,16 @@ __device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int 
                "r"(x), "r"(y), "r"(src)
                : "memory");
 }
+// C' += (chunk in shared memory), element-wise FP32 add performed by the TMA unit
+__device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
+  asm volatile(
+      "cp.reduce.async.bulk.tensor.2d.global.shared::cta.add.tile.bulk_group [%0, {%1, %2}], [%3];" ::"l"(
+          (uint64_t)map),
+      "r"(x), "r"(y), "r"(src)
+      : "memory");
+}
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
@@ -160,12 +170,12 @@ __global__ void __launch_bounds__(192, 1)
   unsigned char* gbase = smraw + (base - smem_u32(smraw));
   uint64_t* bars = reinterpret_cast<uint64_t*>(gbase + STAGES * STAGE_BYTES);
   // C' chunk buffers follow the operand ring; then the barriers:
-  // full[STAGES], empty[STAGES], tfull[2], tempty[2], done, cload[2]
+  // full[STAGES], empty[STAGES], tfull[2], tempty[2], done
   const uint32_t cbuf0 = base + STAGES * STAGE_BYTES;
   float* cbuf_g = reinterpret_cast<float*>(gbase + STAGES * STAGE_BYTES);
   bars = reinterpret_cast<uint64_t*>(gbase + STAGES * STAGE_BYTES + 2 * C_BYTES);
   const int B_FULL = 0, B_EMPTY = STAGES, B_TFULL = 2 * STAGES, B_TEMPTY = 2 * STAGES + 2,
-            B_DONE = 2 * STAGES + 4, B_CLOAD = 2 * STAGES + 5;
+            B_DONE = 2 * STAGES + 4;
   uint32_t* tmem_slot = reinterpret_cast<uint32_t*>(bars + 2 * STAGES + 7);
   __shared__ int s_abort_mem;
   volatile int* s_abort = &s_abort_mem;
@@ -184,8 +194,6 @@ __global__ void __launch_bounds__(192, 1)
       mbar_init(smem_u32(bars + B_TEMPTY + a), 4);  // one arrival per epilogue warp
     }
     mbar_init(smem_u32(bars + B_DONE), 1);
-    mbar_init(smem_u32(bars + B_CLOAD), 1);
-    mbar_init(smem_u32(bars + B_CLOAD + 1), 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -251,33 +259,24 @@ __global__ void __launch_bounds__(192, 1)
     int no_abort = 0;
     mbar_wait(smem_u32(bars + B_DONE), 0, status, &no_abort);
   } else if (warp >= 2) {
-    // ---- epilogue: warp w owns TMEM lanes 32*(w%4) .. +31 (= tile rows).  C' streams
-    // through two shared-memory chunk buffers (128 rows x 32 columns, column-major like C'):
-    // TMA load -> subtract the accumulator -> TMA store; the load of chunk c+2 is issued
-    // once the store of chunk c has read its buffer.
+    // ---- epilogue: warp w owns TMEM lanes 32*(w%4) .. +31 (= tile rows).  Each 128 x 32
+    // chunk of -D / (s t) goes through one of two shared-memory buffers (column-major like
+    // C') and is added to C' by a TMA reduce-add: C' is never loaded into the SM.  A buffer
+    // is rewritten once the reduce issued from it two chunks earlier has read it.
     const int q = warp & 3;
     const bool leader = (warp == 2 && lane == 0);
     const int nch = TN / CCH;
-    uint32_t cuse[2] = {0, 0};  // completed phases of the chunk-load barriers
     int t = 0;
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
       const int a = t & 1;
       const uint32_t aph = (t >> 1) & 1;
       const int m0 = (tile / ntn) * TM, n0 = (tile % ntn) * TN;
-      if (leader) {
-        for (int c = 0; c < 2; ++c) {
-          const uint32_t cl = smem_u32(bars + B_CLOAD + c);
-          mbar_expect_tx(cl, C_BYTES);
-          tma_load_2d(cbuf0 + c * C_BYTES, &tmC, c_row0 + m0, c_col0 + n0 + c * CCH, cl);
-        }
-      }
       if (!mbar_wait(smem_u32(bars + B_TFULL + a), aph, status, s_abort)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * TN);
       const int row = q * 32 + lane;
-      // 1 / s of this thread's row (rows beyond the block are clipped by the TMA store)
-      const float rs = m0 + row < m_rows ? inv_sa[(m0 + row) >> 1] : 0.f;
-      bool ok = true;
+      // -1 / s of this thread's row (rows beyond the block are clipped by the TMA reduce)
+      const float rs = m0 + row < m_rows ? -inv_sa[(m0 + row) >> 1] : 0.f;
       for (int c = 0; c < nch; ++c) {
         const int b = c & 1;
         float v[CCH];
@@ -290,36 +289,21 @@ __global__ void __launch_bounds__(192, 1)
           if (lane == 0)
             asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bars + B_TEMPTY + a)) : "memory");
         }
-        if (!mbar_wait(smem_u32(bars + B_CLOAD + b), cuse[b] & 1, status, s_abort)) {
-          ok = false;
-          break;
-        }
-        cuse[b]++;
-        float* cb = cbuf_g + b * (TM * CCH);
         // 1 / t of the chunk's columns, one per lane, broadcast by shuffles
         const int gcol = n0 + c * CCH + lane;
         const float cs = gcol < n_cols ? inv_sb[gcol] : 0.f;
+        if (leader) bulk_wait_read1();  // the reduce of chunk c-2 has read buffer b
+        asm volatile("bar.sync 1, 128;" ::: "memory");
+        float* cb = cbuf_g + b * (TM * CCH);
 #pragma unroll
-        for (int i = 0; i < CCH; ++i) {
-          const float ci = __shfl_sync(0xffffffffu, cs, i);
-          cb[i * TM + row] = fmaf(-(v[i] * ci), rs, cb[i * TM + row]);
-        }
+        for (int i = 0; i < CCH; ++i) cb[i * TM + row] = v[i] * __shfl_sync(0xffffffffu, cs, i) * rs;
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("bar.sync 1, 128;" ::: "memory");
         if (leader) {
-          tma_store_2d(&tmC, c_row0 + m0, c_col0 + n0 + c * CCH, cbuf0 + b * C_BYTES);
+          tma_reduce_add_2d(&tmC, c_row0 + m0, c_col0 + n0 + c * CCH, cbuf0 + b * C_BYTES);
           bulk_commit();
-          if (c + 2 < nch) {
-            bulk_wait_read0();
-            const uint32_t cl = smem_u32(bars + B_CLOAD + b);
-            mbar_expect_tx(cl, C_BYTES);
-            tma_load_2d(cbuf0 + b * C_BYTES, &tmC, c_row0 + m0, c_col0 + n0 + (c + 2) * CCH, cl);
-          }
         }
       }
-      if (!ok) break;
-      if (leader) bulk_wait_read0();  // both buffers are reloaded for the next tile
-      asm volatile("bar.sync 1, 128;" ::: "memory");
     }
     if (leader) bulk_wait0();
   }
