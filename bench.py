@@ -298,10 +298,10 @@ def main():
         achieved = work / (kms * 1e-3) / 1e12
         peak, unit, bound = pk.get("bf16_tflops_sustained", pk["bf16_tflops"]), "TFLOP/s", "tensor"
     # DRAM traffic per launch: bytes per algorithmic flop measured by ncu on one k_tc_gemm
-    # launch of the level-4 EFIE (348 MB for 4.85e10 flops, profiles/k_tc_gemm_level4_efie.md),
-    # scaled to this run's average launch; the update streams C once, so traffic scales with
-    # the flops of a launch (C area x K, K fixed per update)
-    traffic = 7.18e-3 * work / nl if name == "lu_tc_gemm" else None
+    # launch (the first trailing update of the level-4 EFIE: 744 MB of DRAM traffic for
+    # 3.63e11 flops, C' read and written once by the TMA reduce-add), scaled to this run's
+    # average launch by its flops
+    traffic = 2.05e-3 * work / nl if name == "lu_tc_gemm" else None
     roof = {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak, "unit": unit,
             "frac": achieved / peak, "peak_source": src,
             "peak_note": "measured dense bf16 (sustained); the kernel runs FP16 operands with FP32 accumulation (same tensor rate as bf16)",
