@@ -329,9 +329,19 @@ __global__ void __launch_bounds__(256) k_getrf64(T* A, int64_t lda, int64_t j0, 
   extern __shared__ unsigned char smraw[];
   T* D = reinterpret_cast<T*>(smraw);  // row-major, ld LD
   const int tid = threadIdx.x, c = tid % TRI, rg = tid / TRI;
-  for (int e = tid; e < kb * kb; e += 256) {
-    const int r = e % kb, k = e / kb;
-    D[r * LD + k] = A[(j0 + r) + (j0 + k) * lda];
+  // the block, 16 loads per thread issued before their stores so that they overlap
+  {
+    T v[TRI * TRI / 256];
+#pragma unroll
+    for (int j = 0; j < TRI * TRI / 256; ++j) {
+      const int e = tid + 256 * j, r = e % TRI, k = e / TRI;
+      v[j] = (r < kb && k < kb) ? A[(j0 + r) + (j0 + k) * lda] : T{0, 0};
+    }
+#pragma unroll
+    for (int j = 0; j < TRI * TRI / 256; ++j) {
+      const int e = tid + 256 * j;
+      D[(e % TRI) * LD + e / TRI] = v[j];
+    }
   }
   __syncthreads();
   for (int k = 0; k < kb; k += 2) {
@@ -1175,9 +1185,13 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
               A, lda, j0, kb, j0 + kb, n);
         BEAST_CUDA_TRY(ctx, cudaGetLastError());
       }
-      // TRSM + GEMM for the rest of the block
-      if ((rc = S.trsm(j0, kb, j0 + kb, J1))) break;
+      // TRSM + GEMM for the rest of the block.  Unpivoted, no later interchange touches
+      // these rows, so U12 of this panel is solved for every column to its right at once and
+      // the block's rows of the columns beyond the block are updated here too (what the
+      // pivoted path does per panel after the block).
+      if ((rc = S.trsm(j0, kb, j0 + kb, pivot ? J1 : n))) break;
       if ((rc = S.gemm(j0 + kb, n - j0 - kb, j0 + kb, J1 - j0 - kb, j0, kb, tcwork))) break;
+      if (!pivot && J1 < n && (rc = S.gemm(j0 + kb, J1 - j0 - kb, J1, n - J1, j0, kb, tcwork))) break;
     }
     if (rc) break;
     // the block's interchanges on the columns left and right of it
@@ -1186,8 +1200,9 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       if ((rc = S.laswp(J1, n, J0, J1))) break;
     }
     if (J1 < n) {
-      // U12 = L11^{-1} A12 (blocked: nb-row TRSM, then GEMM on the rows below inside the block)
-      for (int64_t j0 = J0; j0 < J1 && rc == BEAST_OK; j0 += nb) {
+      // U12 = L11^{-1} A12 (blocked: nb-row TRSM, then GEMM on the rows below inside the
+      // block); done per panel above when unpivoted
+      for (int64_t j0 = J0; pivot && j0 < J1 && rc == BEAST_OK; j0 += nb) {
         int kb = (int)std::min<int64_t>(nb, J1 - j0);
         if ((rc = S.trsm(j0, kb, J1, n))) break;
         if ((rc = S.gemm(j0 + kb, J1 - j0 - kb, J1, n - J1, j0, kb, tcwork))) break;
