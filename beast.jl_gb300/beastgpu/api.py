@@ -171,6 +171,42 @@ def assemble(op, X, Y=None, quadstrat=None, precision=L.FP64, out=None, dtype=No
     return result
 
 
+def blockassembler(op, X, Y=None, quadstrat=None, precision=L.FP64, ctx=None):
+    """BEAST.blockassembler (src/integralop.jl:228-320) for an integral operator: returns
+    f(test_ids, trial_ids) -> the block a(test_ids[i], trial_ids[j]) as a host array, with
+    0-based function indices; every entry equals the full assembly's"""
+    ctx = ctx or get_context()
+    Y = X if Y is None else Y
+    if isinstance(op, (O.LinearCombination, O.LocalOperator)):
+        raise ValueError("blockassembler: integral operators only")
+    qs = quadstrat if quadstrat is not None else O.defaultquadstrat(op, X, Y)
+    od, qd = _op_desc(op), _qs_desc(qs)
+    dtype = L.C64 if precision == L.MIXED else L.C128
+
+    def block(test_ids, trial_ids):
+        I = np.ascontiguousarray(np.atleast_1d(test_ids), dtype=np.int64)
+        J = np.ascontiguousarray(np.atleast_1d(trial_ids), dtype=np.int64)
+        Z = np.zeros((len(I), len(J)), dtype=np.complex64 if dtype == L.C64 else np.complex128, order="F")
+        ctx.check(ctx.lib.beast_assemble_block(ctx.handle, C.byref(od), C.byref(qd), ctx.space_handle(X),
+                                               ctx.space_handle(Y), I.ctypes.data, len(I), J.ctypes.data,
+                                               len(J), 0, precision, Z.ctypes.data, len(I), dtype, L.HOST,
+                                               1.0, 0.0, 0))
+        return Z
+    return block
+
+
+def assemblerow(op, X, Y, m, **kw):
+    """row m of the matrix (BEAST.assemblerow on the one-function test space subset(X, m))"""
+    Y = X if Y is None else Y
+    return blockassembler(op, X, Y, **kw)([m], np.arange(Y.numfunctions()))
+
+
+def assemblecol(op, X, Y, n, **kw):
+    """column n of the matrix (BEAST.assemblecol)"""
+    Y = X if Y is None else Y
+    return blockassembler(op, X, Y, **kw)(np.arange(X.numfunctions()), [n])
+
+
 def _zero_block(result, loc, r0, c0, nr, nc):
     if loc == L.HOST:
         result[r0:r0 + nr, c0:c0 + nc] = 0

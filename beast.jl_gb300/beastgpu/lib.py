@@ -41,7 +41,7 @@ EXPORTS = [
     "beast_ctx_create", "beast_ctx_destroy", "beast_last_error", "beast_ctx_set_stream",
     "beast_ctx_set_workspace_limit", "beast_ctx_synchronize", "beast_mesh_upload",
     "beast_mesh_free", "beast_space_upload", "beast_space_free", "beast_assemble",
-    "beast_assemble_local", "beast_rhs_planewave", "beast_lu_factor", "beast_lu_solve",
+    "beast_assemble_block", "beast_assemble_local", "beast_rhs_planewave", "beast_lu_factor", "beast_lu_solve",
     "beast_lu_free", "beast_lu_solve_noalloc", "beast_solve_dense", "beast_gmres", "beast_farfield", "beast_solve_job",
     "beast_prof_enable", "beast_prof_read", "beast_prof_launches", "beast_version",
 ]
@@ -74,6 +74,8 @@ def load(build_if_needed=True):
     L.beast_space_free.argtypes = [vp]
     L.beast_assemble.argtypes = [vp, C.POINTER(OpDesc), C.POINTER(QsDesc), vp, vp, i, vp, i64, i, i,
                                  i64, i64, d, d, i]
+    L.beast_assemble_block.argtypes = [vp, C.POINTER(OpDesc), C.POINTER(QsDesc), vp, vp, vp, i64, vp, i64,
+                                       i, i, vp, i64, i, i, d, d, i]
     L.beast_assemble_local.argtypes = [vp, i, vp, vp, i, vp, i64, i, i, i64, i64, d, d]
     L.beast_rhs_planewave.argtypes = [vp, i, vp, vp, vp, d, d, d, d, i, vp, i]
     L.beast_lu_factor.argtypes = [vp, i64, vp, i64, i, pp]

@@ -530,6 +530,74 @@ int beast_assemble(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc*
   return rc;
 }
 
+// ---------------------------------------------------------------------------------------
+// block assembly (blockassembler / assemblerow / assemblecol)
+// ---------------------------------------------------------------------------------------
+// The space restricted to the functions ids[0..nids): the active cells they touch (kept in
+// the original active order) and one function per id with its (cell, shape, coefficient)
+// entries in the original order, so every entry of the block is computed and summed exactly
+// as in the full assembly.  Mirrors reduce_assembly_data (src/bases/basis.jl:486-499), with
+// repeated ids kept as separate rows.
+static int make_subspace(beast_ctx* ctx, const beast_space* s, const int64_t* ids, int64_t nids,
+                         int index_base, beast_space** out) {
+  std::vector<int> newc(s->ncells, -1);
+  for (int64_t i = 0; i < nids; ++i) {
+    const int64_t d = ids[i] - index_base;
+    if (d < 0 || d >= s->nfuncs) return beast_fail(ctx, BEAST_ERR_ARG, "block index out of range");
+    for (int64_t e = s->h_fn_ptr[d]; e < s->h_fn_ptr[d + 1]; ++e) newc[s->h_fn_cell[e]] = 0;
+  }
+  std::vector<int> h_cells(s->ncells);
+  BEAST_CUDA_TRY(ctx, cudaMemcpy(h_cells.data(), s->cells, sizeof(int) * s->ncells, cudaMemcpyDeviceToHost));
+  std::vector<int64_t> mesh_cells;
+  for (int64_t c = 0; c < s->ncells; ++c)
+    if (newc[c] == 0) {
+      newc[c] = (int)mesh_cells.size();
+      mesh_cells.push_back(h_cells[c]);
+    }
+  const int64_t nc = (int64_t)mesh_cells.size();
+  if (nc == 0) return beast_fail(ctx, BEAST_ERR_ARG, "block functions have no support");
+  const int ns = s->nshapes;
+  // (new function, coefficient) per (new cell, shape); each function's entries then come out
+  // of the upload's CSR in the full space's (cell, shape) order
+  std::vector<std::vector<std::pair<int64_t, double>>> slot(nc * ns);
+  for (int64_t i = 0; i < nids; ++i) {
+    const int64_t d = ids[i] - index_base;
+    for (int64_t e = s->h_fn_ptr[d]; e < s->h_fn_ptr[d + 1]; ++e)
+      slot[(int64_t)newc[s->h_fn_cell[e]] * ns + s->h_fn_shape[e]].push_back({i, s->h_fn_coeff[e]});
+  }
+  int maxfn = 1;
+  for (auto& v : slot) maxfn = std::max<int>(maxfn, (int)v.size());
+  std::vector<int64_t> ad(nc * ns * maxfn, -1);
+  std::vector<double> ac(nc * ns * maxfn, 0.0);
+  for (int64_t cs = 0; cs < nc * ns; ++cs)
+    for (size_t k = 0; k < slot[cs].size(); ++k) {
+      ad[cs * maxfn + k] = slot[cs][k].first;
+      ac[cs * maxfn + k] = slot[cs][k].second;
+    }
+  return beast_space_upload(ctx, s->mesh, s->kind, nc, mesh_cells.data(), maxfn, ns, ad.data(), ac.data(),
+                            nids, 0, out);
+}
+
+int beast_assemble_block(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs,
+                         const beast_space* test, const beast_space* trial, const int64_t* test_ids,
+                         int64_t ntest, const int64_t* trial_ids, int64_t ntrial, int index_base,
+                         int precision, void* Z, int64_t ldz, int z_dtype, int z_loc, double coeff_re,
+                         double coeff_im, int accumulate) {
+  ARG_CHECK(ctx, ctx && op && qs && test && trial && test_ids && trial_ids && Z, "null argument");
+  ARG_CHECK(ctx, ntest > 0 && ntrial > 0 && ldz >= ntest, "invalid block sizes");
+  ARG_CHECK(ctx, index_base == 0 || index_base == 1, "index_base must be 0 or 1");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  beast_space *ts = nullptr, *bs = nullptr;
+  int rc = make_subspace(ctx, test, test_ids, ntest, index_base, &ts);
+  if (rc == BEAST_OK) rc = make_subspace(ctx, trial, trial_ids, ntrial, index_base, &bs);
+  if (rc == BEAST_OK)
+    rc = beast_assemble(ctx, op, qs, ts, bs, precision, Z, ldz, z_dtype, z_loc, 0, 0, coeff_re, coeff_im,
+                        accumulate);
+  beast_space_free(ts);
+  beast_space_free(bs);
+  return rc;
+}
+
 int beast_assemble_local(beast_ctx* ctx, int which, const beast_space* ts, const beast_space* bs,
                          int degree, void* Z, int64_t ldz, int z_dtype, int z_loc, int64_t row_off,
                          int64_t col_off, double cr, double ci) {

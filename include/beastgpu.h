@@ -145,6 +145,18 @@ int beast_assemble(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc*
                    int64_t ldz, int z_dtype, int z_loc, int64_t row_off, int64_t col_off,
                    double coeff_re, double coeff_im, int accumulate);
 
+/* replaces blockassembler(op, tfs, bfs)(test_ids, trial_ids, store) and assemblerow! /
+ * assemblecol! (src/integralop.jl:228-320, 593-702; reduce_assembly_data,
+ * src/bases/basis.jl:486-499): the block a(test_ids[i], trial_ids[j]) for i < ntest,
+ * j < ntrial into Z[i, j] (block-local rows / columns, ldz, like beast_assemble with zero
+ * offsets).  Ids are function indices of the two spaces with the given index_base; a
+ * repeated id gives a repeated row / column.  Every entry equals the full assembly's. */
+int beast_assemble_block(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs,
+                         const beast_space* test, const beast_space* trial, const int64_t* test_ids,
+                         int64_t ntest, const int64_t* trial_ids, int64_t ntrial, int index_base,
+                         int precision, void* Z, int64_t ldz, int z_dtype, int z_loc, double coeff_re,
+                         double coeff_im, int accumulate);
+
 /* replaces assemble!(::LocalOperator, ...) for Identity (which = 0) and NCross
  * (which = 1) on RT x RT (src/identityop.jl:7-24, 66-67; src/localop.jl:107-155):
  * adds coeff * block into Z (same addressing as beast_assemble).  degree: SingleNumQStrat. */

@@ -132,3 +132,41 @@ def test_rhs_and_farfield(ctx):
     ff = bg.farfield(X, u, dirs, 1j * k)
     ffo = O.farfield(X, u, dirs, 1j * k)
     assert np.abs(ff - ffo).max() <= 1e-12 * np.abs(ffo).max()
+
+
+def test_blockassembler_full_block_equals_assemble(ctx):
+    """test_blockassembler.jl: the block over all functions equals the full matrix
+    (double layer on the sphere5 mesh) to one ulp of the largest entry"""
+    X = bg.raviartthomas(bg.readmesh(mesh_path("sphere5.in")))
+    op = bg.Maxwell3D.doublelayer(wavenumber=2 * np.pi / 20.0)
+    A = bg.assemble(op, X, X, ctx=ctx)
+    blk = bg.blockassembler(op, X, X, ctx=ctx)
+    n = X.numfunctions()
+    B = blk(np.arange(n), np.arange(n))
+    assert np.abs(A - B).max() <= np.finfo(np.float64).eps * np.abs(A).max()
+
+
+@pytest.mark.parametrize("precision", [bg.FP64, bg.MIXED])
+def test_assemblerow_subset_blocks(ctx, precision):
+    """test_assemblerow.jl: rows of subset(X, I) against the full matrix, plus columns and
+    scattered blocks with repeated ids (Maxwell single layer on sphere35; Helmholtz P0)"""
+    X = bg.raviartthomas(bg.readmesh(mesh_path("sphere35.in")))
+    op = bg.Maxwell3D.singlelayer(wavenumber=1.0)
+    A = bg.assemble(op, X, X, precision=precision, ctx=ctx)
+    scale = np.abs(A).max()
+    tol = 1e-14 if precision == bg.FP64 else 1e-6
+    r = bg.assemblerow(op, X, X, 0, precision=precision, ctx=ctx)
+    assert np.abs(r[0] - A[0]).max() <= tol * scale
+    c = bg.assemblecol(op, X, X, 5, precision=precision, ctx=ctx)
+    assert np.abs(c[:, 0] - A[:, 5]).max() <= tol * scale
+    I, J = [3, 2, 7], [11, 0, 11, 40]
+    B = bg.blockassembler(op, X, X, precision=precision, ctx=ctx)(I, J)
+    assert np.abs(B - A[np.ix_(I, J)]).max() <= tol * scale
+    Y = bg.lagrangecxd0(bg.icosphere(2))
+    hh = bg.Helmholtz3D.singlelayer(wavenumber=1.5)
+    H = bg.assemble(hh, Y, Y, precision=precision, ctx=ctx)
+    rng = np.random.default_rng(2)
+    I = rng.integers(0, Y.numfunctions(), 17)
+    J = rng.integers(0, Y.numfunctions(), 9)
+    Hb = bg.blockassembler(hh, Y, Y, precision=precision, ctx=ctx)(I, J)
+    assert np.abs(Hb - H[np.ix_(I, J)]).max() <= tol * np.abs(H).max()
