@@ -170,6 +170,35 @@ function BEAST.assemble(op::GPUOps, tfs::BEAST.Space, bfs::BEAST.Space; quadstra
 end
 
 """
+    blockassembler(op, tfs, bfs, qs::GPUQStrat) -> (test_ids, trial_ids, store) -> nothing
+
+`BEAST.blockassembler` on the device: the block a(test_ids[i], trial_ids[j]) is assembled
+into a block-local buffer by `beast_assemble_block` and handed to `store(v, i, j)` entry by
+entry, like the reference's functor (block-local 1-based indices).
+"""
+function blockassembler(op::GPUOps, tfs::BEAST.Space, bfs::BEAST.Space, qs::GPUQStrat)
+    ctx = context()
+    inner = qs.inner isa Function ? qs.inner(op, tfs, bfs) : qs.inner
+    od = Ref(opdesc(op)); qd = Ref(qsdesc(inner))
+    return function (test_ids, trial_ids, store)
+        I = collect(Int64, test_ids); J = collect(Int64, trial_ids)
+        B = zeros(ComplexF64, length(I), length(J))
+        GC.@preserve I J B begin
+            check(ctx.ptr, ccall((:beast_assemble_block, libbeastgpu), Cint,
+                (Ptr{Cvoid}, Ref{OpDesc}, Ref{QsDesc}, Ptr{Cvoid}, Ptr{Cvoid}, Ptr{Int64}, Int64,
+                 Ptr{Int64}, Int64, Cint, Cint, Ptr{ComplexF64}, Int64, Cint, Cint, Cdouble, Cdouble,
+                 Cint),
+                ctx.ptr, od, qd, space_handle(ctx, tfs), space_handle(ctx, bfs), I, length(I), J,
+                length(J), 1, qs.precision, B, length(I), C128, HOST, 1.0, 0.0, 0))
+        end
+        for j in axes(B, 2), i in axes(B, 1)
+            store(B[i, j], i, j)
+        end
+        return nothing
+    end
+end
+
+"""
     solve(Z, b; precision=FP64, tol=1e-12) -> x
 
 `Z \\ b` on the device: FP64 LU, or (MIXED) FP32 LU with tensor-core updates and FP64
