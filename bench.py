@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--compare-fp64", action="store_true",
+                    help="instead of the bench line: one plain FP64 solve and one mixed solve of the "
+                         "workload, their solves/s and the relative difference of the surface currents")
     return ap.parse_args()
 
 
@@ -63,7 +66,8 @@ def config_dict(args, X, m):
             "triangles": int(m.numcells()), "unknowns": int(X.numfunctions()),
             "quadstrat": "DoubleNumWiltonSauterQStrat(2,3,6,7,5,5,4,3)",
             "precision": args.precision, "refinement_tol": args.tol,
-            "l2": "inputs larger than L2 (matrix 7.5 GB c64 / 15 GB c128)",
+            "l2": f"inputs larger than L2 (matrix {X.numfunctions() ** 2 * 8 / 1e9:.2f} GB c64 / "
+                  f"{X.numfunctions() ** 2 * 16 / 1e9:.2f} GB c128)",
             "parallelism": f"replicas x{args.gpus}"}
 
 
@@ -170,6 +174,58 @@ def run_reference(args, rank, world):
     print(json.dumps(out))
 
 
+def compare_fp64(args):
+    """Plain FP64 (c128 matrix, FP64 quadrature, FP64 LU) against the mixed path on the same
+    workload: solves/s of each (CUDA events around assemble + excitation + solve; the mixed
+    path after one warm-up solve, the FP64 path as one run after it, its LU alone taking
+    minutes) and the relative difference of the two surface-current vectors."""
+    import torch
+    import beastgpu as bg
+    from beastgpu import lib as L
+    m, X, op, E = workload(args)
+    n = X.numfunctions()
+    ctx = bg.Context(0)
+    sh = ctx.space_handle(X)
+    qs = bg.defaultquadstrat(op, X, X)
+    od, qd = bg.api._op_desc(op), bg.api._qs_desc(qs)
+    d, pol, g = np.array([1.0, 0, 0]), np.array([0, 0, 1.0]), complex(E.gamma)
+    out, xs = {}, {}
+    for name, prec, dt, tdt, warm in (("mixed", L.MIXED, L.C64, torch.complex64, 1),
+                                      ("fp64", L.FP64, L.C128, torch.complex128, 0)):
+        Z = torch.empty((n, n), dtype=tdt, device="cuda")
+        b = torch.empty(n, dtype=torch.complex128, device="cuda")
+        x = torch.empty(n, dtype=torch.complex128, device="cuda")
+        it, res = C.c_int(0), C.c_double(0)
+
+        def step():
+            ctx.check(ctx.lib.beast_assemble(ctx.handle, C.byref(od), C.byref(qd), sh, sh, prec, Z.data_ptr(),
+                                             n, dt, L.DEVICE, 0, 0, 1.0, 0.0, 0))
+            ctx.check(ctx.lib.beast_rhs_planewave(ctx.handle, 0, sh, d.ctypes.data, pol.ctypes.data, g.real,
+                                                  g.imag, 1.0, 0.0, 8, b.data_ptr(), L.DEVICE))
+            ctx.check(ctx.lib.beast_solve_dense(ctx.handle, n, Z.data_ptr(), n, dt, prec, b.data_ptr(),
+                                                x.data_ptr(), 1, L.DEVICE, args.tol, 30, C.byref(it),
+                                                C.byref(res)))
+        for _ in range(warm):
+            step()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        step()
+        e1.record()
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        out[name] = {"solves_per_s": 1000.0 / ms, "ms_per_solve": ms, "refinement_iters": it.value,
+                     "rel_residual": res.value}
+        xs[name] = x.cpu().numpy()
+        del Z, b, x
+        torch.cuda.empty_cache()
+    err = float(np.linalg.norm(xs["mixed"] - xs["fp64"]) / np.linalg.norm(xs["fp64"]))
+    print(json.dumps({"compare": "mixed vs plain FP64", "config": config_dict(args, X, m),
+                      "mixed": out["mixed"], "fp64": out["fp64"],
+                      "speedup_mixed_over_fp64": out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"],
+                      "surface_current_rel_diff": err}))
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -177,6 +233,8 @@ def main():
     local = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         return run_reference(args, rank, world)
+    if args.compare_fp64:
+        return compare_fp64(args)
     import torch
     import beastgpu as bg
     from beastgpu import lib as L
