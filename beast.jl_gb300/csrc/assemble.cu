@@ -262,6 +262,66 @@ struct FarParams {
   TriRuleDev ro, ri;
 };
 
+// ---- reference phase of a far pair in FP32 pairs (hi + lo) ----------------------------
+// In FP32 the phase k R of a distant pair carries an absolute error of about 1e-7 k R: at
+// k R = 20 that is a 2e-6 relative error of every entry.  The FP32 far kernel therefore
+// factors exp(-gamma R) = exp(-gamma Rc) exp(-gamma (R - Rc)) with Rc = |c_p - c_q|: the pair
+// factor is formed once per pair with error-free transformations (two_sum / two_prod, as in
+// double-double arithmetic, Dekker 1971), and R - Rc = (2 d.delta + delta.delta) / (R + Rc)
+// (delta = x - y - d, small) keeps the per-point phase small and accurate.
+DEV void two_sum_f(float a, float b, float& s, float& e) {
+  s = a + b;
+  const float bb = s - a;
+  e = (a - (s - bb)) + (b - bb);
+}
+DEV void two_prod_f(float a, float b, float& p, float& e) {
+  p = a * b;
+  e = fmaf(a, b, -p);
+}
+// exp(-(gr + i gi) Rc) for the pair whose centroid difference is (hi - hiq) + (lo - loq)
+DEV C2<float> pair_phase_f(V3<float> chp, V3<float> clp, const float* rq, float grh, float grl, float gih,
+                           float gil, float* Rc_out) {
+  const float ph[3] = {chp.x, chp.y, chp.z}, pl[3] = {clp.x, clp.y, clp.z};
+  float sh = 0.f, sl = 0.f;
+  for (int k = 0; k < 3; ++k) {
+    float dh, e;
+    two_sum_f(ph[k], -rq[9 + k], dh, e);
+    const float dl = e + (pl[k] - rq[12 + k]);
+    float p, pe, t;
+    two_prod_f(dh, dh, p, pe);
+    two_sum_f(sh, p, sh, t);
+    sl += t + pe + 2.f * dh * dl;
+  }
+  float S, Sl;
+  two_sum_f(sh, sl, S, Sl);
+  const float r0 = sqrtf(S);
+  float q, qe;
+  two_prod_f(r0, r0, q, qe);
+  const float rl = (((S - q) - qe) + Sl) / (2.f * r0);
+  *Rc_out = r0 + rl;
+  // phase gi Rc, reduced modulo 2 pi (2 pi = TPH + TPL)
+  const float TPH = 6.28318548202514648f, TPL = -1.74845553e-7f;
+  float ph0, phe;
+  two_prod_f(gih, r0, ph0, phe);
+  const float phl = phe + gih * rl + gil * r0;
+  const float n = rintf(ph0 * 0.159154943091895336f);
+  float nq, nqe, th, the;
+  two_prod_f(n, TPH, nq, nqe);
+  two_sum_f(ph0, -nq, th, the);
+  const float tl = the + (phl - nqe - n * TPL);
+  float sn, cs;
+  sincosf(th, &sn, &cs);
+  const float sinp = sn + cs * tl, cosp = cs - sn * tl;
+  float amp = 1.f;
+  if (grh != 0.f || grl != 0.f) {
+    float ah, ae;
+    two_prod_f(grh, r0, ah, ae);
+    const float al = ae + grh * rl + grl * r0;
+    amp = expf(-ah) * (1.f - al);
+  }
+  return {amp * cosp, -amp * sinp};
+}
+
 constexpr int FAR_THREADS = 128;
 constexpr int FAR_QT = 16;  // trial cells staged per CTA
 
@@ -344,6 +404,8 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
   const double Ap = tg[15];
   const R radp = (R)P.tgeof[4 * p + 3];
   const R gr = (R)P.op.gr, gi = (R)P.op.gi;
+  constexpr bool F32 = sizeof(R) == 4;
+  const float grl = (float)(P.op.gr - (double)(float)P.op.gr), gil = (float)(P.op.gi - (double)(float)P.op.gi);
   const C2<R> alpha{(R)P.op.ar, (R)P.op.ai}, beta{(R)P.op.br, (R)P.op.bi};
   const R ApR = (R)Ap;
   const int nst = (TK == BEAST_P0) ? 1 : 3, nsb = (BK == BEAST_P0) ? 1 : 3;
@@ -377,6 +439,17 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
     }
     const R Aq = rq[18];
     const R* pts = rq + QREC_HDR;
+    // FP32: the pair's reference distance and phase factor (applied to the finished block)
+    R Rc = 0;
+    C2<R> Pf{1, 0};
+    if (F32) {
+      float rcf;
+      const C2<float> pf = pair_phase_f(mk((float)chp.x, (float)chp.y, (float)chp.z),
+                                        mk((float)clp.x, (float)clp.y, (float)clp.z),
+                                        reinterpret_cast<const float*>(rq), (float)gr, grl, (float)gi, gil, &rcf);
+      Rc = (R)rcf;
+      Pf = C2<R>{(R)pf.re, (R)pf.im};
+    }
 
     if (OPK == BEAST_MW_SL || OPK == BEAST_MW_DL || OPK == BEAST_MW_NXDL) {
       // ---- RT x RT with moment reduction
@@ -403,7 +476,10 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
           const R R2 = dot(r, r);
           const R iR = rsq<R>(R2);
           const R Rr = R2 * iR;
-          C2<R> G = green<R>(gr, gi, Rr, iR);
+          // FP32: phase and attenuation relative to the pair's reference distance
+          const V3<R> del = xi - eta;
+          const R Rp = F32 ? ((R)2 * dot(d, del) + dot(del, del)) / (Rr + Rc) : Rr;
+          C2<R> G = green<R>(gr, gi, Rp, iR);
           C2<R> K;
           if (OPK == BEAST_MW_SL) {
             K = cscale(wb, G);
@@ -503,6 +579,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
             f = csub(f, cscale(dot(ti, sj), M3));
             z = cscale((R)0.25, f);
           }
+          if (F32) z = cmul(z, Pf);
           store_c<R>(P.zcell, (int64_t)(3 * ql + j) * P.ldc + 3 * p + i, z, C64);
         }
       }
@@ -527,7 +604,9 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
           const R R2 = dot(r, r);
           const R iR = rsq<R>(R2);
           const R Rr = R2 * iR;
-          C2<R> G = green<R>(gr, gi, Rr, iR);
+          const V3<R> del = xi - eta;
+          const R Rp = F32 ? ((R)2 * dot(d, del) + dot(del, del)) / (Rr + Rc) : Rr;
+          C2<R> G = green<R>(gr, gi, Rp, iR);
           C2<R> K;
           const C2<R> al = alpha;
           if (OPK == BEAST_HH_SL) {
@@ -554,7 +633,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
       for (int i = 0; i < nst; ++i)
         for (int j = 0; j < nsb; ++j)
           store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * p + i,
-                     cscale(ApAq, acc[i * nsb + j]), C64);
+                     cscale(ApAq, F32 ? cmul(acc[i * nsb + j], Pf) : acc[i * nsb + j]), C64);
     }
   }
 }
@@ -1051,17 +1130,26 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
       if (P.ss32) {
         // FP32: x - y = X0 Et1 + X1 Et2 - Y0 Es1 - Y1 Es2 over the edge vectors of the two
         // charts from the shared first vertex (common terms folded into D = X - Y)
-        const V3<float> a0 = v3f(t.v[pt[0]] - cp), et1 = v3f(t.v[pt[1]] - t.v[pt[0]]),
-                        et2 = v3f(t.v[pt[2]] - t.v[pt[1]]);
-        const V3<float> b0 = v3f(s.v[ps[0]] - cq), es1 = v3f(s.v[ps[1]] - s.v[ps[0]]),
-                        es2 = v3f(s.v[ps[2]] - s.v[ps[1]]);
+        // edge vectors as FP32 pairs hi + lo: the rounding of the geometry to FP32 would
+        // otherwise be one systematic perturbation of every point of the pair
+        const V3<double> Et1 = t.v[pt[1]] - t.v[pt[0]], Et2 = t.v[pt[2]] - t.v[pt[1]];
+        const V3<double> Es1 = s.v[ps[1]] - s.v[ps[0]], Es2 = s.v[ps[2]] - s.v[ps[1]];
+        const V3<float> a0 = v3f(t.v[pt[0]] - cp), et1 = v3f(Et1), et2 = v3f(Et2);
+        const V3<float> b0 = v3f(s.v[ps[0]] - cq), es1 = v3f(Es1), es2 = v3f(Es2);
+        const V3<float> et1l = v3f(Et1 - mk<double>(et1.x, et1.y, et1.z)),
+                        et2l = v3f(Et2 - mk<double>(et2.x, et2.y, et2.z)),
+                        es1l = v3f(Es1 - mk<double>(es1.x, es1.y, es1.z)),
+                        es2l = v3f(Es2 - mk<double>(es2.x, es2.y, es2.z));
         const V3<float> df = v3f(d);
         const float gif = (float)gi, grf = (float)gr;
         const float* glxf = s_glxf + c_gl_off[n - 1];
         const float* glwf = s_glwf + c_gl_off[n - 1];
+        // FP32 partial moments over at most 16 points, flushed into the FP64 moments m[] so
+        // that the FP32 rounding of the sums stays at the level of a 16-term sum
         float mf[22];
 #pragma unroll
         for (int k = 0; k < 22; ++k) mf[k] = 0.0f;
+        int cnt = 0;
         for (int it = lane; it < (int)items; it += 32) {
           float X[2], Y[2], D[2], w;
           ss_node_f(np_.cls, n, it, glxf, glwf, X, Y, D, &w);
@@ -1069,11 +1157,12 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
           const V3<float> eta = b0 + Y[0] * es1 + Y[1] * es2;
           V3<float> r;
           if (np_.cls == 3)
-            r = D[0] * et1 + D[1] * et2;
+            r = (D[0] * et1 + D[1] * et2) + (D[0] * et1l + D[1] * et2l);
           else if (np_.cls == 2)
-            r = D[0] * et1 + (X[1] * et2 - Y[1] * es2);
+            r = (D[0] * et1 + (X[1] * et2 - Y[1] * es2)) + (D[0] * et1l + (X[1] * et2l - Y[1] * es2l));
           else
-            r = (X[0] * et1 + X[1] * et2) - (Y[0] * es1 + Y[1] * es2);
+            r = ((X[0] * et1 + X[1] * et2) - (Y[0] * es1 + Y[1] * es2)) +
+                ((X[0] * et1l + X[1] * et2l) - (Y[0] * es1l + Y[1] * es2l));
           const float R = sqrtf(dot(r, r));
           const float iR = 1.0f / R;
           float sn, cs;
@@ -1103,9 +1192,17 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
           mf[4] += a.x * cr; mf[5] += a.x * ci; mf[6] += a.y * cr; mf[7] += a.y * ci; mf[8] += a.z * cr; mf[9] += a.z * ci;
           mf[10] += b.x * cr; mf[11] += b.x * ci; mf[12] += b.y * cr; mf[13] += b.y * ci; mf[14] += b.z * cr; mf[15] += b.z * ci;
           mf[16] += c3.x * cr; mf[17] += c3.x * ci; mf[18] += c3.y * cr; mf[19] += c3.y * ci; mf[20] += c3.z * cr; mf[21] += c3.z * ci;
+          if (++cnt == 16) {
+#pragma unroll
+            for (int k = 0; k < 22; ++k) {
+              m[k] += (double)mf[k];
+              mf[k] = 0.0f;
+            }
+            cnt = 0;
+          }
         }
 #pragma unroll
-        for (int k = 0; k < 22; ++k) m[k] = (double)mf[k];
+        for (int k = 0; k < 22; ++k) m[k] += (double)mf[k];
       }
       for (int64_t it = P.ss32 ? items : (int64_t)lane; it < items; it += 32) {
         double X[2], Y[2], w;
