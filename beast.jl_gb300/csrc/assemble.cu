@@ -262,66 +262,6 @@ struct FarParams {
   TriRuleDev ro, ri;
 };
 
-// ---- reference phase of a far pair in FP32 pairs (hi + lo) ----------------------------
-// In FP32 the phase k R of a distant pair carries an absolute error of about 1e-7 k R: at
-// k R = 20 that is a 2e-6 relative error of every entry.  The FP32 far kernel therefore
-// factors exp(-gamma R) = exp(-gamma Rc) exp(-gamma (R - Rc)) with Rc = |c_p - c_q|: the pair
-// factor is formed once per pair with error-free transformations (two_sum / two_prod, as in
-// double-double arithmetic, Dekker 1971), and R - Rc = (2 d.delta + delta.delta) / (R + Rc)
-// (delta = x - y - d, small) keeps the per-point phase small and accurate.
-DEV void two_sum_f(float a, float b, float& s, float& e) {
-  s = a + b;
-  const float bb = s - a;
-  e = (a - (s - bb)) + (b - bb);
-}
-DEV void two_prod_f(float a, float b, float& p, float& e) {
-  p = a * b;
-  e = fmaf(a, b, -p);
-}
-// exp(-(gr + i gi) Rc) for the pair whose centroid difference is (hi - hiq) + (lo - loq)
-DEV C2<float> pair_phase_f(V3<float> chp, V3<float> clp, const float* rq, float grh, float grl, float gih,
-                           float gil, float* Rc_out) {
-  const float ph[3] = {chp.x, chp.y, chp.z}, pl[3] = {clp.x, clp.y, clp.z};
-  float sh = 0.f, sl = 0.f;
-  for (int k = 0; k < 3; ++k) {
-    float dh, e;
-    two_sum_f(ph[k], -rq[9 + k], dh, e);
-    const float dl = e + (pl[k] - rq[12 + k]);
-    float p, pe, t;
-    two_prod_f(dh, dh, p, pe);
-    two_sum_f(sh, p, sh, t);
-    sl += t + pe + 2.f * dh * dl;
-  }
-  float S, Sl;
-  two_sum_f(sh, sl, S, Sl);
-  const float r0 = sqrtf(S);
-  float q, qe;
-  two_prod_f(r0, r0, q, qe);
-  const float rl = (((S - q) - qe) + Sl) / (2.f * r0);
-  *Rc_out = r0 + rl;
-  // phase gi Rc, reduced modulo 2 pi (2 pi = TPH + TPL)
-  const float TPH = 6.28318548202514648f, TPL = -1.74845553e-7f;
-  float ph0, phe;
-  two_prod_f(gih, r0, ph0, phe);
-  const float phl = phe + gih * rl + gil * r0;
-  const float n = rintf(ph0 * 0.159154943091895336f);
-  float nq, nqe, th, the;
-  two_prod_f(n, TPH, nq, nqe);
-  two_sum_f(ph0, -nq, th, the);
-  const float tl = the + (phl - nqe - n * TPL);
-  float sn, cs;
-  sincosf(th, &sn, &cs);
-  const float sinp = sn + cs * tl, cosp = cs - sn * tl;
-  float amp = 1.f;
-  if (grh != 0.f || grl != 0.f) {
-    float ah, ae;
-    two_prod_f(grh, r0, ah, ae);
-    const float al = ae + grh * rl + grl * r0;
-    amp = expf(-ah) * (1.f - al);
-  }
-  return {amp * cosp, -amp * sinp};
-}
-
 constexpr int FAR_THREADS = 128;
 constexpr int FAR_QT = 16;  // trial cells staged per CTA
 
@@ -404,8 +344,6 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
   const double Ap = tg[15];
   const R radp = (R)P.tgeof[4 * p + 3];
   const R gr = (R)P.op.gr, gi = (R)P.op.gi;
-  constexpr bool F32 = sizeof(R) == 4;
-  const float grl = (float)(P.op.gr - (double)(float)P.op.gr), gil = (float)(P.op.gi - (double)(float)P.op.gi);
   const C2<R> alpha{(R)P.op.ar, (R)P.op.ai}, beta{(R)P.op.br, (R)P.op.bi};
   const R ApR = (R)Ap;
   const int nst = (TK == BEAST_P0) ? 1 : 3, nsb = (BK == BEAST_P0) ? 1 : 3;
@@ -439,17 +377,6 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
     }
     const R Aq = rq[18];
     const R* pts = rq + QREC_HDR;
-    // FP32: the pair's reference distance and phase factor (applied to the finished block)
-    R Rc = 0;
-    C2<R> Pf{1, 0};
-    if (F32) {
-      float rcf;
-      const C2<float> pf = pair_phase_f(mk((float)chp.x, (float)chp.y, (float)chp.z),
-                                        mk((float)clp.x, (float)clp.y, (float)clp.z),
-                                        reinterpret_cast<const float*>(rq), (float)gr, grl, (float)gi, gil, &rcf);
-      Rc = (R)rcf;
-      Pf = C2<R>{(R)pf.re, (R)pf.im};
-    }
 
     if (OPK == BEAST_MW_SL || OPK == BEAST_MW_DL || OPK == BEAST_MW_NXDL) {
       // ---- RT x RT with moment reduction
@@ -476,10 +403,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
           const R R2 = dot(r, r);
           const R iR = rsq<R>(R2);
           const R Rr = R2 * iR;
-          // FP32: phase and attenuation relative to the pair's reference distance
-          const V3<R> del = xi - eta;
-          const R Rp = F32 ? ((R)2 * dot(d, del) + dot(del, del)) / (Rr + Rc) : Rr;
-          C2<R> G = green<R>(gr, gi, Rp, iR);
+          C2<R> G = green<R>(gr, gi, Rr, iR);
           C2<R> K;
           if (OPK == BEAST_MW_SL) {
             K = cscale(wb, G);
@@ -579,7 +503,6 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
             f = csub(f, cscale(dot(ti, sj), M3));
             z = cscale((R)0.25, f);
           }
-          if (F32) z = cmul(z, Pf);
           store_c<R>(P.zcell, (int64_t)(3 * ql + j) * P.ldc + 3 * p + i, z, C64);
         }
       }
@@ -604,9 +527,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
           const R R2 = dot(r, r);
           const R iR = rsq<R>(R2);
           const R Rr = R2 * iR;
-          const V3<R> del = xi - eta;
-          const R Rp = F32 ? ((R)2 * dot(d, del) + dot(del, del)) / (Rr + Rc) : Rr;
-          C2<R> G = green<R>(gr, gi, Rp, iR);
+          C2<R> G = green<R>(gr, gi, Rr, iR);
           C2<R> K;
           const C2<R> al = alpha;
           if (OPK == BEAST_HH_SL) {
@@ -633,7 +554,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
       for (int i = 0; i < nst; ++i)
         for (int j = 0; j < nsb; ++j)
           store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * p + i,
-                     cscale(ApAq, F32 ? cmul(acc[i * nsb + j], Pf) : acc[i * nsb + j]), C64);
+                     cscale(ApAq, acc[i * nsb + j]), C64);
     }
   }
 }
