@@ -35,8 +35,8 @@ void* lu_dinv(const int* ipiv, int64_t n) {
 
 bool tc_gemm_supported(const void* A, int64_t lda, int K);
 size_t tc_gemm_work_bytes(int64_t M, int64_t N, int K);
-int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t colB, int64_t M,
-                int64_t N, int K, void* work, size_t work_bytes);
+int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t colB,
+                int64_t M0, int64_t N0, int64_t M1, int64_t N1, int K, void* work, size_t work_bytes);
 
 namespace {
 
@@ -1094,18 +1094,30 @@ struct LUSteps {
   }
   // A[r0:r0+m, c0:c0+nc] -= A[r0:r0+m, k0:k0+k] A[k0:k0+k, c0:c0+nc]
   int gemm(int64_t r0, int64_t m, int64_t c0, int64_t nc, int64_t k0, int k, void* tcwork) {
-    if (m <= 0 || nc <= 0 || k <= 0) return BEAST_OK;
-    const bool tc = sizeof(T) == 8 && tcwork && m >= 64 && nc >= 64 && k % 32 == 0;
-    ProfScope ps(ctx, tc ? PK_TCGEMM : PK_GEMM, 8.0 * (double)m * nc * k);
-    if (tc) {
-      return tc_gemm_sub(ctx, reinterpret_cast<float2*>(A), lda, r0, k0, c0, m, nc, k, tcwork, tcwork_bytes);
+    return gemm2(r0, m, c0, nc, 0, 0, k0, k, tcwork);
+  }
+  // the same on an L-shaped region: rows [r0, r0+m0) of columns [c0, c0+n0), then rows
+  // [r0, r0+m1) (m1 <= m0) of the next n1 columns -- one tensor-core launch for both
+  int gemm2(int64_t r0, int64_t m0, int64_t c0, int64_t n0, int64_t m1, int64_t n1, int64_t k0, int k,
+            void* tcwork) {
+    if (m0 <= 0 || k <= 0) return BEAST_OK;
+    if (n0 <= 0 && (m1 <= 0 || n1 <= 0)) return BEAST_OK;
+    const bool tc = sizeof(T) == 8 && tcwork && m0 >= 64 && n0 + n1 >= 64 && k % 32 == 0;
+    ProfScope ps(ctx, tc ? PK_TCGEMM : PK_GEMM, 8.0 * (double)k * ((double)m0 * n0 + (double)m1 * n1));
+    if (tc)
+      return tc_gemm_sub(ctx, reinterpret_cast<float2*>(A), lda, r0, k0, c0, m0, n0, m1, n1, k, tcwork,
+                         tcwork_bytes);
+    const int64_t ms[2] = {m0, m1}, cs[2] = {c0, c0 + n0}, ns[2] = {n0, n1};
+    for (int r = 0; r < 2; ++r) {
+      if (ms[r] <= 0 || ns[r] <= 0) continue;
+      dim3 g((unsigned)((ms[r] + GT - 1) / GT), (unsigned)((ns[r] + GT - 1) / GT));
+      k_gemm_sub<T, R><<<g, 256, 0, st>>>(A + r0 + cs[r] * lda, lda, A + r0 + k0 * lda, lda, A + k0 + cs[r] * lda,
+                                          lda, ms[r], ns[r], k);
+      BEAST_CUDA_TRY(ctx, cudaGetLastError());
     }
-    dim3 g((unsigned)((m + GT - 1) / GT), (unsigned)((nc + GT - 1) / GT));
-    k_gemm_sub<T, R><<<g, 256, 0, st>>>(A + r0 + c0 * lda, lda, A + r0 + k0 * lda, lda, A + k0 + c0 * lda,
-                                        lda, m, nc, k);
-    BEAST_CUDA_TRY(ctx, cudaGetLastError());
     return BEAST_OK;
   }
+
 };
 
 // Two-level right-looking LU: column blocks of NB are factored with nb-wide panels (panel,
@@ -1190,8 +1202,11 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       // the block's rows of the columns beyond the block are updated here too (what the
       // pivoted path does per panel after the block).
       if ((rc = S.trsm(j0, kb, j0 + kb, pivot ? J1 : n))) break;
-      if ((rc = S.gemm(j0 + kb, n - j0 - kb, j0 + kb, J1 - j0 - kb, j0, kb, tcwork))) break;
-      if (!pivot && J1 < n && (rc = S.gemm(j0 + kb, J1 - j0 - kb, J1, n - J1, j0, kb, tcwork))) break;
+      // in-block update (all rows below, block columns) and, unpivoted, the block rows of
+      // the columns beyond the block, as one L-shaped update
+      if ((rc = S.gemm2(j0 + kb, n - j0 - kb, j0 + kb, J1 - j0 - kb, pivot ? 0 : J1 - j0 - kb,
+                        pivot ? 0 : n - J1, j0, kb, tcwork)))
+        break;
     }
     if (rc) break;
     // the block's interchanges on the columns left and right of it

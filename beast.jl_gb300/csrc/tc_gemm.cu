@@ -8,8 +8,9 @@
 //   C'  = the real view of C (no copy: element (r, c) of the complex matrix occupies rows
 //         2r, 2r+1 of column c of the real view)
 //   A'  = A expanded into 2x2 real blocks [[ar, -ai], [ai, ar]], K-major, row pair of complex
-//         row m scaled by a power of two s_m (k_expand_h)
-//   B'  = the real view of B, column j scaled by a power of two t_j (k_convert_bh)
+//         row m scaled by a power of two s_m (expand_h)
+//   B'  = the real view of B, column j scaled by a power of two t_j (convert_bh; both in
+//         one launch, k_prep_h)
 // Both operands are rounded to FP16 (11 significant bits, the precision of TF32) after the
 // scaling puts each row's / column's largest magnitude in [2^13, 2^14), so the FP16 range
 // never clips; the products accumulate in FP32 in TMEM and the epilogue multiplies by the
@@ -161,10 +162,21 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 // accumulator (tcgen05.ld -> C' -= D) so that the epilogue of tile t overlaps the loads and
 // MMAs of tile t+1.  Barriers: full/empty per stage (TMA <-> MMA), tfull/tempty per
 // accumulator (MMA <-> epilogue).  Tiles are visited N-fastest (B' stays in L2).
+// The update region is one or two rectangles of C' that share the operands: rectangle r
+// covers the first m_rows[r] rows of A' and the n_cols[r] columns of B' from b_col[r], and
+// writes C' through its own (clipped) tensor map at (c_row0, c_col0[r]).  Tiles of
+// rectangle 0 come first in the tile order.
+struct TcRegion {
+  int m_rows[2], n_cols[2], b_col[2], c_col0[2];
+  int c_row0;
+  int ntn[2], ntiles0, ntiles;
+};
+
 __global__ void __launch_bounds__(192, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-              const __grid_constant__ CUtensorMap tmC, int c_row0, int c_col0, int m_rows, int n_cols,
-              const float* __restrict__ inv_sa, const float* __restrict__ inv_sb, int nk, int* status) {
+              const __grid_constant__ CUtensorMap tmC0, const __grid_constant__ CUtensorMap tmC1,
+              const TcRegion Rg, const float* __restrict__ inv_sa, const float* __restrict__ inv_sb, int nk,
+              int* status) {
   extern __shared__ unsigned char smraw[];
   const uint32_t base = (smem_u32(smraw) + 1023u) & ~1023u;
   unsigned char* gbase = smraw + (base - smem_u32(smraw));
@@ -180,8 +192,14 @@ __global__ void __launch_bounds__(192, 1)
   __shared__ int s_abort_mem;
   volatile int* s_abort = &s_abort_mem;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntn = (n_cols + TN - 1) / TN, ntm = (m_rows + TM - 1) / TM;
-  const int ntiles = ntn * ntm;
+  const int ntiles = Rg.ntiles;
+  // tile -> (rectangle, first row, first column within the rectangle)
+  auto tile_at = [&](int tile, int& r, int& m0, int& n0) {
+    r = tile < Rg.ntiles0 ? 0 : 1;
+    const int lt = r ? tile - Rg.ntiles0 : tile;
+    m0 = (lt / Rg.ntn[r]) * TM;
+    n0 = (lt % Rg.ntn[r]) * TN;
+  };
 
   if (threadIdx.x == 0) {
     *s_abort = 0;
@@ -211,7 +229,8 @@ __global__ void __launch_bounds__(192, 1)
     // ---- TMA producer
     uint32_t it = 0;
     for (int tile = blockIdx.x; tile < ntiles && !*s_abort; tile += gridDim.x) {
-      const int m0 = (tile / ntn) * TM, n0 = (tile % ntn) * TN;
+      int rr, m0, n0;
+      tile_at(tile, rr, m0, n0);
       for (int kb = 0; kb < nk; ++kb, ++it) {
         const int s = it % STAGES;
         const uint32_t ph = (it / STAGES) & 1;
@@ -220,7 +239,7 @@ __global__ void __launch_bounds__(192, 1)
         const uint32_t full = smem_u32(bars + B_FULL + s);
         mbar_expect_tx(full, STAGE_BYTES);
         tma_load_2d(sa, &tmA, kb * TK, m0, full);
-        tma_load_2d(sb, &tmB, kb * TK, n0, full);
+        tma_load_2d(sb, &tmB, kb * TK, Rg.b_col[rr] + n0, full);
       }
     }
     // no copy may still be landing in shared memory when the CTA exits: wait (bounded,
@@ -270,7 +289,10 @@ __global__ void __launch_bounds__(192, 1)
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++t) {
       const int a = t & 1;
       const uint32_t aph = (t >> 1) & 1;
-      const int m0 = (tile / ntn) * TM, n0 = (tile % ntn) * TN;
+      int rr, m0, n0;
+      tile_at(tile, rr, m0, n0);
+      const CUtensorMap* tmC = rr ? &tmC1 : &tmC0;
+      const int m_rows = Rg.m_rows[rr], n_cols = Rg.n_cols[rr];
       if (!mbar_wait(smem_u32(bars + B_TFULL + a), aph, status, s_abort)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t tbase = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(a * TN);
@@ -291,7 +313,7 @@ __global__ void __launch_bounds__(192, 1)
         }
         // 1 / t of the chunk's columns, one per lane, broadcast by shuffles
         const int gcol = n0 + c * CCH + lane;
-        const float cs = gcol < n_cols ? inv_sb[gcol] : 0.f;
+        const float cs = gcol < n_cols ? inv_sb[Rg.b_col[rr] + gcol] : 0.f;
         if (leader) bulk_wait_read1();  // the reduce of chunk c-2 has read buffer b
         asm volatile("bar.sync 1, 128;" ::: "memory");
         float* cb = cbuf_g + b * (TM * CCH);
@@ -300,7 +322,7 @@ __global__ void __launch_bounds__(192, 1)
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         asm volatile("bar.sync 1, 128;" ::: "memory");
         if (leader) {
-          tma_reduce_add_2d(&tmC, c_row0 + m0, c_col0 + n0 + c * CCH, cbuf0 + b * C_BYTES);
+          tma_reduce_add_2d(tmC, Rg.c_row0 + m0, Rg.c_col0[rr] + n0 + c * CCH, cbuf0 + b * C_BYTES);
           bulk_commit();
         }
       }
@@ -326,13 +348,13 @@ __device__ __forceinline__ int scale_shift(float mx) {
 // A' (K-major; rows 2m, 2m+1 hold 2K halves): [[ar, -ai], [ai, ar]] blocks times s_m;
 // inv_sa[m] = 1 / s_m.  A CTA takes 32 rows: the row maxima first, then 64-column slices
 // transposed through shared memory so that every warp writes whole row segments.
-__global__ void __launch_bounds__(256) k_expand_h(const float2* A, int64_t lda, int M, int K, __half2* Ap,
-                                                  float* inv_sa) {
+__device__ __forceinline__ void expand_h(int bid, const float2* A, int64_t lda, int M, int K, __half2* Ap,
+                                         float* inv_sa) {
   __shared__ float red[8][33];
   __shared__ float2 tile[32][65];
   __shared__ float s_scale[32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int m0 = blockIdx.x * 32, m = m0 + lane;
+  const int m0 = bid * 32, m = m0 + lane;
   float mx = 0.f;
   if (m < M)
     for (int k = w; k < K; k += 8) {
@@ -378,10 +400,10 @@ __global__ void __launch_bounds__(256) k_expand_h(const float2* A, int64_t lda, 
 }
 
 // B' (column j: 2K halves, (re, im) per k) times t_j; inv_sb[j] = 1 / t_j.  One warp per column.
-__global__ void __launch_bounds__(256) k_convert_bh(const float2* B, int64_t lda, int K, int N, __half2* Bp,
-                                                    float* inv_sb) {
+__device__ __forceinline__ void convert_bh(int bid, const float2* B, int64_t lda, int K, int N, __half2* Bp,
+                                           float* inv_sb) {
   const int lane = threadIdx.x & 31;
-  const int j = blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int j = bid * 8 + (threadIdx.x >> 5);
   if (j >= N) return;
   const float2* col = B + (int64_t)j * lda;
   float mx = 0.f;
@@ -399,6 +421,16 @@ __global__ void __launch_bounds__(256) k_convert_bh(const float2* B, int64_t lda
     const float2 a = col[k];
     out[k] = __floats2half2_rn(a.x * sc, a.y * sc);
   }
+}
+
+// both operands in one launch: CTAs [0, nA) expand 32 rows of A each, the rest convert 8
+// columns of B each
+__global__ void __launch_bounds__(256) k_prep_h(const float2* A, const float2* B, int64_t lda, int M, int N, int K,
+                                                __half2* Ap, float* inv_sa, __half2* Bp, float* inv_sb, int nA) {
+  if ((int)blockIdx.x < nA)
+    expand_h(blockIdx.x, A, lda, M, K, Ap, inv_sa);
+  else
+    convert_bh(blockIdx.x - nA, B, lda, K, N, Bp, inv_sb);
 }
 
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
@@ -452,16 +484,20 @@ size_t tc_gemm_work_bytes(int64_t M, int64_t N, int K) {
   return al((size_t)M * K * 8) + al((size_t)N * K * 4) + al((size_t)M * 4) + al((size_t)N * 4);
 }
 
-// C -= A B (complex64) for the LU trailing update:
-//   A at (rowA, colA) of the matrix, M x K;  B at (rowB = colA, colB), K x N;  C at (rowA, colB)
-// Mat: base of the full matrix (ld lda); work: tc_gemm_work_bytes(M, N, K) bytes or more
+// C -= A B (complex64) for the LU updates, over an L-shaped region of C:
+//   A at (rowA, colA) of the matrix, M0 x K;  B at (colA, colB), K x (N0 + N1);
+//   rectangle 0: C[rowA : rowA+M0, colB : colB+N0]     = A[0:M0]  B[:, 0:N0]
+//   rectangle 1: C[rowA : rowA+M1, colB+N0 : +N1]      = A[0:M1]  B[:, N0:N0+N1]   (M1 <= M0)
+// (N1 = 0: one rectangle).  Mat: base of the full matrix (ld lda); work:
+// tc_gemm_work_bytes(M0, N0 + N1, K) bytes or more.
 int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t colB,
-                int64_t M, int64_t N, int K, void* work, size_t work_bytes) {
+                int64_t M0, int64_t N0, int64_t M1, int64_t N1, int K, void* work, size_t work_bytes) {
   cudaStream_t st = ctx->stream;
+  const int64_t N = N0 + N1;
   // TMA: the first C' row (2 rowA floats) must start on 16 bytes
-  if ((2 * rowA) % 4 != 0 || K % 32 != 0 || 2 * (rowA + M) > INT32_MAX || colB + N > INT32_MAX)
+  if ((2 * rowA) % 4 != 0 || K % 32 != 0 || M1 > M0 || 2 * (rowA + M0) > INT32_MAX || colB + N > INT32_MAX)
     return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: unaligned block");
-  if (tc_gemm_work_bytes(M, N, K) > work_bytes)
+  if (tc_gemm_work_bytes(M0, N, K) > work_bytes)
     return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: workspace too small");
   static bool attr_done[64] = {false};
   int dev = ctx->device;
@@ -472,32 +508,53 @@ int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t 
   auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
   char* w = static_cast<char*>(work);
   __half2* Ap = reinterpret_cast<__half2*>(w);
-  __half2* Bp = reinterpret_cast<__half2*>(w + al((size_t)M * K * 8));
-  float* inv_sa = reinterpret_cast<float*>(w + al((size_t)M * K * 8) + al((size_t)N * K * 4));
-  float* inv_sb = reinterpret_cast<float*>(reinterpret_cast<char*>(inv_sa) + al((size_t)M * 4));
-  k_expand_h<<<(unsigned)((M + 31) / 32), 256, 0, st>>>(Mat + rowA + colA * lda, lda, (int)M, K, Ap, inv_sa);
-  k_convert_bh<<<(unsigned)((N + 7) / 8), 256, 0, st>>>(Mat + colA + colB * lda, lda, K, (int)N, Bp, inv_sb);
-  ctx->launches += 2;
-  CUtensorMap tmA, tmB, tmC;
-  // A': 2K halves per row (x), 2M rows (y); B': 2K halves per column (x), N columns (y)
-  if (!make_map(&tmA, Ap, (uint64_t)2 * K, (uint64_t)2 * M, (uint64_t)2 * K * 2, TK, TM, true,
+  __half2* Bp = reinterpret_cast<__half2*>(w + al((size_t)M0 * K * 8));
+  float* inv_sa = reinterpret_cast<float*>(w + al((size_t)M0 * K * 8) + al((size_t)N * K * 4));
+  float* inv_sb = reinterpret_cast<float*>(reinterpret_cast<char*>(inv_sa) + al((size_t)M0 * 4));
+  const int nA = (int)((M0 + 31) / 32), nB = (int)((N + 7) / 8);
+  k_prep_h<<<(unsigned)(nA + nB), 256, 0, st>>>(Mat + rowA + colA * lda, Mat + colA + colB * lda, lda, (int)M0,
+                                                (int)N, K, Ap, inv_sa, Bp, inv_sb, nA);
+  ctx->launches += 1;
+  CUtensorMap tmA, tmB, tmC0, tmC1;
+  // A': 2K halves per row (x), 2 M0 rows (y); B': 2K halves per column (x), N columns (y)
+  if (!make_map(&tmA, Ap, (uint64_t)2 * K, (uint64_t)2 * M0, (uint64_t)2 * K * 2, TK, TM, true,
                 CU_TENSOR_MAP_DATA_TYPE_FLOAT16))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (A') failed");
   if (!make_map(&tmB, Bp, (uint64_t)2 * K, (uint64_t)N, (uint64_t)2 * K * 2, TK, TN, true,
                 CU_TENSOR_MAP_DATA_TYPE_FLOAT16))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (B') failed");
-  // C': real view clipped to the update block (rows up to 2(rowA+M), columns up to colB+N):
-  // the bulk stores never touch anything outside it
+  // C': real view clipped to each rectangle (rows up to 2(rowA + M_r), columns up to its last
+  // column): the reduce-adds never touch anything outside the rectangle
   const float* real = reinterpret_cast<const float*>(Mat);
-  if (!make_map(&tmC, real, (uint64_t)2 * (rowA + M), (uint64_t)(colB + N), (uint64_t)2 * lda * 4, TM, CCH, false,
+  if (!make_map(&tmC0, real, (uint64_t)2 * (rowA + M0), (uint64_t)(colB + N0), (uint64_t)2 * lda * 4, TM, CCH,
+                false, CU_TENSOR_MAP_DATA_TYPE_FLOAT32))
+    return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (C') failed");
+  tmC1 = tmC0;
+  if (N1 > 0 && M1 > 0 &&
+      !make_map(&tmC1, real, (uint64_t)2 * (rowA + M1), (uint64_t)(colB + N), (uint64_t)2 * lda * 4, TM, CCH, false,
                 CU_TENSOR_MAP_DATA_TYPE_FLOAT32))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (C') failed");
-  const int m_rows = (int)(2 * M), n_cols = (int)N;
-  const int ntiles = ((n_cols + TN - 1) / TN) * ((m_rows + TM - 1) / TM);
-  const int grid = std::min(ntiles, std::max(1, ctx->num_sms));
+  TcRegion Rg;
+  Rg.c_row0 = (int)(2 * rowA);
+  Rg.m_rows[0] = (int)(2 * M0);
+  Rg.n_cols[0] = (int)N0;
+  Rg.b_col[0] = 0;
+  Rg.c_col0[0] = (int)colB;
+  Rg.m_rows[1] = (int)(2 * M1);
+  Rg.n_cols[1] = (int)N1;
+  Rg.b_col[1] = (int)N0;
+  Rg.c_col0[1] = (int)(colB + N0);
+  int ntl[2];
+  for (int r = 0; r < 2; ++r) {
+    Rg.ntn[r] = std::max(1, (Rg.n_cols[r] + TN - 1) / TN);
+    ntl[r] = (Rg.m_rows[r] > 0 && Rg.n_cols[r] > 0) ? Rg.ntn[r] * ((Rg.m_rows[r] + TM - 1) / TM) : 0;
+  }
+  Rg.ntiles0 = ntl[0];
+  Rg.ntiles = ntl[0] + ntl[1];
+  if (Rg.ntiles == 0) return BEAST_OK;
+  const int grid = std::min(Rg.ntiles, std::max(1, ctx->num_sms));
   const int nk = (2 * K) / TK;
-  k_tc_gemm<<<grid, 192, SMEM_BYTES, st>>>(tmA, tmB, tmC, (int)(2 * rowA), (int)colB, m_rows, n_cols, inv_sa,
-                                           inv_sb, nk, ctx->d_flag);
+  k_tc_gemm<<<grid, 192, SMEM_BYTES, st>>>(tmA, tmB, tmC0, tmC1, Rg, inv_sa, inv_sb, nk, ctx->d_flag);
   BEAST_CUDA_TRY(ctx, cudaGetLastError());
   return BEAST_OK;
 }
