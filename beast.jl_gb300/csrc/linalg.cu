@@ -288,13 +288,11 @@ __global__ void k_laswp(T* A, int64_t lda, int64_t c0, int64_t c1, int64_t p0, i
 
 // ---- LU of a diagonal block without pivoting (mixed path) --------------------------------
 // A[j0:j0+kb, j0:j0+kb] = L11 U11 in place, kb <= 64, one CTA of 256 threads in shared
-// memory, two pivots per pass (two barriers per pair of columns):
-//   A: every thread forms l_{k+1,k} and the second pivot u_{k+1,k+1} itself; threads 0..63
-//      finish the multipliers of columns k and k+1 for one row each, threads 64..127 update
-//      row k+1 for one column each;
-//   B: rank-2 update of the trailing block, thread t on column t % 64 and the rows congruent
-//      to t / 64 modulo 4 (the two updates applied one after the other, as the one-pivot
-//      recurrence does).
+// memory, blocked by 16 columns (three barriers per 16 pivots):
+//   1. warp 0 factors the 64 x 16 column slab in registers (lane l holds rows l and l + 32;
+//      the pivot row is broadcast with shuffles, so the 16 pivot steps need no block barrier);
+//   2. U12 of the slab's rows, one column per thread (unit lower 16 x 16 substitution);
+//   3. rank-16 update of the trailing block by all threads.
 // A zero pivot sets *info (1-based column) and the kernel stops.
 constexpr int TRI = 64;
 
@@ -324,11 +322,20 @@ __device__ __forceinline__ bool crecip(T p, T& r) {  // r = 1 / p; false for p =
 }
 
 template <typename T>
+__device__ __forceinline__ T shfl_c(T v, int src) {
+  T r;
+  r.x = __shfl_sync(0xffffffffu, v.x, src);
+  r.y = __shfl_sync(0xffffffffu, v.y, src);
+  return r;
+}
+
+template <typename T>
 __global__ void __launch_bounds__(256) k_getrf64(T* A, int64_t lda, int64_t j0, int kb, int* info) {
-  constexpr int LD = TRI + 1;
+  constexpr int LD = TRI + 1, PB = 16;
   extern __shared__ unsigned char smraw[];
-  T* D = reinterpret_cast<T*>(smraw);  // row-major, ld LD
-  const int tid = threadIdx.x, c = tid % TRI, rg = tid / TRI;
+  T* D = reinterpret_cast<T*>(smraw);  // row-major, ld LD, zero outside kb x kb
+  __shared__ int s_zero;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   // the block, 16 loads per thread issued before their stores so that they overlap
   {
     T v[TRI * TRI / 256];
@@ -343,67 +350,77 @@ __global__ void __launch_bounds__(256) k_getrf64(T* A, int64_t lda, int64_t j0, 
       D[(e % TRI) * LD + e / TRI] = v[j];
     }
   }
+  if (tid == 0) s_zero = 0;
   __syncthreads();
-  for (int k = 0; k < kb; k += 2) {
-    T i0;
-    if (!crecip(D[k * LD + k], i0)) {  // uniform
-      if (tid == 0) atomicCAS(info, 0, (int)(j0 + k + 1));
-      return;
-    }
-    if (k + 1 == kb) break;
-    const T l1k = cmulx(D[(k + 1) * LD + k], i0);
-    const T u01 = D[k * LD + k + 1];
-    T p1 = D[(k + 1) * LD + k + 1], i1;
-    cfms(p1, l1k, u01);
-    if (!crecip(p1, i1)) {
-      if (tid == 0) atomicCAS(info, 0, (int)(j0 + k + 2));
-      return;
-    }
-    // phase A
-    if (tid < TRI) {
-      const int i = k + 2 + tid;
-      if (i < kb) {
-        const T lk = cmulx(D[i * LD + k], i0);
-        T t1 = D[i * LD + k + 1];
-        cfms(t1, lk, u01);
-        D[i * LD + k] = lk;
-        D[i * LD + k + 1] = cmulx(t1, i1);
+  for (int k0 = 0; k0 < kb; k0 += PB) {
+    const int nbk = min(PB, kb - k0);
+    // 1. the column slab k0 .. k0+15 by warp 0
+    if (warp == 0) {
+      T a[2][PB];
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int c = 0; c < PB; ++c) a[h][c] = D[(lane + 32 * h) * LD + k0 + c];
+      int zero_at = 0;
+#pragma unroll
+      for (int k = 0; k < PB; ++k) {
+        if (k < nbk && zero_at == 0) {  // uniform over the warp
+          const int pr = k0 + k, ow = pr & 31, oh = pr >> 5;
+          T u[PB];
+#pragma unroll
+          for (int c = k; c < PB; ++c) u[c] = shfl_c(oh ? a[1][c] : a[0][c], ow);
+          T ip;
+          if (!crecip(u[k], ip)) {
+            zero_at = pr + 1;
+          } else {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+              const int i = lane + 32 * h;
+              if (i > pr && i < kb) {
+                const T l = cmulx(a[h][k], ip);
+                a[h][k] = l;
+#pragma unroll
+                for (int c = k + 1; c < PB; ++c) cfms(a[h][c], l, u[c]);
+              }
+            }
+          }
+        }
       }
-    } else if (tid < 2 * TRI) {
-      const int cc = k + 2 + (tid - TRI);
-      if (cc < kb) cfms(D[(k + 1) * LD + cc], l1k, D[k * LD + cc]);
+#pragma unroll
+      for (int h = 0; h < 2; ++h)
+#pragma unroll
+        for (int c = 0; c < PB; ++c) D[(lane + 32 * h) * LD + k0 + c] = a[h][c];
+      if (lane == 0 && zero_at) s_zero = zero_at;
     }
     __syncthreads();
-    // phase B (row k+1 left of the trailing block: multiplier and the second pivot, written
-    // here because every thread read them before the barrier)
-    if (tid == 0) {
-      D[(k + 1) * LD + k] = l1k;
-      D[(k + 1) * LD + k + 1] = p1;
+    if (s_zero) {  // uniform
+      if (tid == 0) atomicCAS(info, 0, (int)(j0 + s_zero));
+      return;
     }
-    if (c >= k + 2 && c < kb) {
-      const T u0 = D[k * LD + c], u1 = D[(k + 1) * LD + c];
-      const int jb = (k + 2 - rg + 3) >> 2;  // first j with rg + 4 j >= k + 2
-      for (int jj = jb; jj < 16; jj += 4) {
-        T l0[4], l1[4], v[4];
+    const int c1 = k0 + PB;  // first column right of the slab (the slab is complete here)
+    if (c1 >= kb) break;
+    // 2. U12 = L11^{-1} A12 for the slab's 16 rows, one column per thread
+    if (tid < kb - c1) {
+      const int c = c1 + tid;
+      T x[PB];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int i = rg + 4 * (jj + q);
-          if (jj + q < 16 && i < kb) {
-            l0[q] = D[i * LD + k];
-            l1[q] = D[i * LD + k + 1];
-            v[q] = D[i * LD + c];
-          }
-        }
+      for (int i = 0; i < PB; ++i) x[i] = D[(k0 + i) * LD + c];
 #pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          const int i = rg + 4 * (jj + q);
-          if (jj + q < 16 && i < kb) {
-            cfms(v[q], l0[q], u0);
-            cfms(v[q], l1[q], u1);
-            D[i * LD + c] = v[q];
-          }
-        }
-      }
+      for (int i = 1; i < PB; ++i)
+#pragma unroll
+        for (int j = 0; j < i; ++j) cfms(x[i], D[(k0 + i) * LD + k0 + j], x[j]);
+#pragma unroll
+      for (int i = 1; i < PB; ++i) D[(k0 + i) * LD + c] = x[i];
+    }
+    __syncthreads();
+    // 3. rank-16 update of the trailing block
+    const int w = kb - c1;
+    for (int e = tid; e < w * w; e += 256) {
+      const int r = c1 + e / w, c = c1 + e % w;
+      T acc = D[r * LD + c];
+#pragma unroll
+      for (int j = 0; j < PB; ++j) cfms(acc, D[r * LD + k0 + j], D[(k0 + j) * LD + c]);
+      D[r * LD + c] = acc;
     }
     __syncthreads();
   }
