@@ -106,6 +106,17 @@ int beast_ctx_create(int device, beast_ctx** out) {
     return BEAST_ERR_CUDA;
   }
   cudaDeviceGetAttribute(&c->num_sms, cudaDevAttrMultiProcessorCount, device);
+  // workspace (factor copies, Zcell chunks, tensor-core operands) is stream-ordered memory
+  // of the device's default pool: keep what is freed in the pool instead of returning it at
+  // every synchronisation, so that repeated solves do not map gigabytes again each time
+  // (the pool is trimmed when the context is destroyed)
+  {
+    cudaMemPool_t pool;
+    if (cudaDeviceGetDefaultMemPool(&pool, device) == cudaSuccess) {
+      uint64_t keep = UINT64_MAX;
+      cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
+  }
   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete c;
     return BEAST_ERR_CUDA;
@@ -130,6 +141,8 @@ int beast_ctx_destroy(beast_ctx* ctx) {
   if (ctx->ws) cudaFree(ctx->ws);
   if (ctx->d_flag) cudaFree(ctx->d_flag);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
+  cudaMemPool_t pool;
+  if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
   delete ctx;
   return BEAST_OK;
 }
