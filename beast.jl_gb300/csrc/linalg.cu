@@ -769,26 +769,66 @@ __global__ void k_invert_diag(const T* A, int64_t lda, int64_t n, T* dinv) {
 }
 
 // ---- triangular solve on one right-hand side as a wavefront ------------------------------
-// Block rows of 64 are owned round-robin by co-resident CTAs (cooperative launch).  A block
-// row depends on every block solved before it, so blocks are published strictly in solve
-// order and one counter (flags[0] = blocks published) tells a CTA which solved blocks it may
-// read.  A CTA walks its dependencies in order: the 64 x 64 factor block of the next
-// dependency and its slice of the diagonal block's inverse are loaded before it waits, the
-// counter is polled only when the next dependency is beyond the last value seen, then it
-// solves its diagonal block (inverse matvec) and publishes.  lower = 1: unit lower,
-// forward; lower = 0: upper, backward.  Arithmetic in RT (the factors' precision).  Waits
-// are bounded; on expiry a status bit is set and the CTA returns.
+// Block rows of 64 are owned round-robin by co-resident CTAs (cooperative launch).  The
+// solution is written to `out`, which starts filled with a sentinel (a NaN bit pattern that
+// arithmetic does not produce), so a solved value is its own "ready" flag: a thread that
+// needs block k spins (bounded) on exactly the 16 values it multiplies, with no counter, no
+// fence and no block barrier inside the dependency walk.  The factor block of the next
+// dependency and the thread's slice of the diagonal block's inverse are loaded ahead.  After
+// the walk the CTA solves its diagonal block (inverse matvec) and stores its 64 values.
+// lower = 1: unit lower, forward; lower = 0: upper, backward.  rhs: the right-hand side
+// (read only).  Arithmetic in RT.  A wait that runs out sets status bit 8 and uses zeros.
+constexpr unsigned long long SENT32 = 0x7FC0DEAD7FC0DEADull;  // two FP32 NaNs, payload 0xDEAD
+constexpr unsigned long long SENT64 = 0x7FF8DEADBEEF0001ull;  // one FP64 NaN with a payload
+constexpr long long TRSV_SPIN_MAX = 1LL << 22;
+
+// a solved value as it is in memory (read from L2, never from a stale L1 line), and whether
+// it is still the sentinel (for c128 each 8-byte half is checked: a 16-byte store may land
+// in two parts)
+__device__ __forceinline__ float2 ld_raw(const float2* p) {
+  const unsigned long long u = *reinterpret_cast<const volatile unsigned long long*>(p);
+  float2 v;
+  v.x = __uint_as_float((unsigned)(u & 0xffffffffull));
+  v.y = __uint_as_float((unsigned)(u >> 32));
+  return v;
+}
+__device__ __forceinline__ double2 ld_raw(const double2* p) {
+  const volatile unsigned long long* q = reinterpret_cast<const volatile unsigned long long*>(p);
+  double2 v;
+  v.x = __longlong_as_double((long long)q[0]);
+  v.y = __longlong_as_double((long long)q[1]);
+  return v;
+}
+__device__ __forceinline__ bool is_sent(float2 v) {
+  return (((unsigned long long)__float_as_uint(v.y) << 32) | __float_as_uint(v.x)) == SENT32;
+}
+__device__ __forceinline__ bool is_sent(double2 v) {
+  return (unsigned long long)__double_as_longlong(v.x) == SENT64 ||
+         (unsigned long long)__double_as_longlong(v.y) == SENT64;
+}
+
+template <typename T>
+__global__ void k_fill_sentinel(T* v, int64_t n) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  unsigned long long* u = reinterpret_cast<unsigned long long*>(v + i);
+  if (sizeof(T) == 8) {
+    u[0] = SENT32;
+  } else {
+    u[0] = SENT64;
+    u[1] = SENT64;
+  }
+}
+
 template <typename T, typename RT>
-__global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int64_t n, T* x, int lower,
-                                                   int* flags, int* status, const T* dinv) {
+__global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int64_t n, const T* rhs, T* out,
+                                                   int lower, int* status, const T* dinv) {
   __shared__ RT sr[64], si[64];
   __shared__ RT pr[4][64], pim[4][64];
-  __shared__ int s_avail[2];
   const int nblk = (int)((n + 63) / 64);
   const int tid = threadIdx.x, r = tid & 63, q = tid >> 6;
-  int* done = flags;
   const T zero = {0, 0};
-  int avail = 0, polls = 0;
+  bool timed_out = false;
   for (int t = blockIdx.x; t < nblk; t += gridDim.x) {
     const int b = lower ? t : nblk - 1 - t;
     const int64_t r0 = (int64_t)b * 64;
@@ -810,48 +850,64 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
         dst[c] = (r < rb && col < cb) ? Ar[col * lda] : zero;
       }
     };
-    RT ar = 0, ai = 0;
-    T nxt[16];
-    if (t > 0) load_blk(0, nxt);
-    for (int s = 0; s < t; ++s) {
-      T cur[16];
-#pragma unroll
-      for (int c = 0; c < 16; ++c) cur[c] = nxt[c];
-      if (s + 1 < t) load_blk(s + 1, nxt);
-      if (s >= avail) {
-        // wait until block s (in solve order) is published; two alternating slots so that
-        // a slot is rewritten only after every thread has passed the next barrier
-        const int slot = polls & 1;
-        if (tid == 0) {
-          long long it = 0;
-          int v;
-          while ((v = atomicAdd(done, 0)) <= s) {
-            if (++it > (1LL << 24)) {
-              atomicOr(status, 8);
-              v = -1;
-              break;
-            }
-            __nanosleep(32);
-          }
-          __threadfence();
-          s_avail[slot] = v;
-        }
-        __syncthreads();
-        avail = s_avail[slot];
-        ++polls;
-        if (avail < 0) return;
-      }
+    // this thread's 16 solved values of dependency s, read as they are (maybe sentinels)
+    auto load_x = [&](int s, T* dst) {
       const int k = lower ? s : nblk - 1 - s;
       const int64_t c0 = (int64_t)k * 64;
       const int cb = (int)(n - c0 < 64 ? n - c0 : 64);
 #pragma unroll
+      for (int c = 0; c < 16; ++c) dst[c] = q * 16 + c < cb ? ld_raw(out + c0 + q * 16 + c) : zero;
+    };
+    RT ar = 0, ai = 0;
+    T nxt[16], xn[16];
+    if (t > 0) {
+      load_blk(0, nxt);
+      load_x(0, xn);
+    }
+    for (int s = 0; s < t; ++s) {
+      T cur[16], xv[16];
+#pragma unroll
       for (int c = 0; c < 16; ++c) {
-        const int col = q * 16 + c;
-        if (col < cb) {
-          const T xv = __ldcg(x + c0 + col);
-          ar += (RT)cur[c].x * (RT)xv.x - (RT)cur[c].y * (RT)xv.y;
-          ai += (RT)cur[c].x * (RT)xv.y + (RT)cur[c].y * (RT)xv.x;
+        cur[c] = nxt[c];
+        xv[c] = xn[c];
+      }
+      // the next dependency's factor entries and solved values are requested before this
+      // one is used
+      if (s + 1 < t) {
+        load_blk(s + 1, nxt);
+        load_x(s + 1, xn);
+      }
+      const int k = lower ? s : nblk - 1 - s;
+      const T* xk = out + (int64_t)k * 64 + q * 16;
+      unsigned pend = 0;
+#pragma unroll
+      for (int c = 0; c < 16; ++c)
+        if (is_sent(xv[c])) pend |= 1u << c;
+      long long it = 0;
+      while (pend) {
+        // spin on one value (one load per warp per round keeps the polling traffic low),
+        // then re-read the ones still missing
+        const int last = 31 - __clz(pend);
+        while (is_sent(ld_raw(xk + last)) && ++it <= TRSV_SPIN_MAX) __nanosleep(64);
+        if (it > TRSV_SPIN_MAX) {
+          if (!timed_out) atomicOr(status, 8);
+          timed_out = true;
+#pragma unroll
+          for (int c = 0; c < 16; ++c)
+            if (pend & (1u << c)) xv[c] = zero;
+          break;
         }
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+          if (pend & (1u << c)) {
+            xv[c] = ld_raw(xk + c);
+            if (!is_sent(xv[c])) pend &= ~(1u << c);
+          }
+      }
+#pragma unroll
+      for (int c = 0; c < 16; ++c) {
+        ar += (RT)cur[c].x * (RT)xv[c].x - (RT)cur[c].y * (RT)xv[c].y;
+        ai += (RT)cur[c].x * (RT)xv[c].y + (RT)cur[c].y * (RT)xv[c].x;
       }
     }
     pr[q][r] = ar;
@@ -860,7 +916,7 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
     if (tid < 64) {
       RT vr = 0, vi = 0;
       if (tid < rb) {
-        T bv = __ldcg(x + r0 + tid);
+        const T bv = rhs[r0 + tid];
         vr = (RT)bv.x - (pr[0][tid] + pr[1][tid] + pr[2][tid] + pr[3][tid]);
         vi = (RT)bv.y - (pim[0][tid] + pim[1][tid] + pim[2][tid] + pim[3][tid]);
       }
@@ -885,11 +941,9 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
       T o;
       o.x = pr[0][tid] + pr[1][tid] + pr[2][tid] + pr[3][tid];
       o.y = pim[0][tid] + pim[1][tid] + pim[2][tid] + pim[3][tid];
-      x[r0 + tid] = o;
+      __stcg(out + r0 + tid, o);
     }
-    __threadfence();
-    __syncthreads();
-    if (tid == 0) atomicAdd(done, 1);
+    __syncthreads();  // pr / pim are rewritten by the next block row
   }
 }
 
@@ -1273,75 +1327,64 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   return BEAST_OK;
 }
 
+// P b -> forward sweep -> backward sweep, per right-hand side: tmp (n values) is the
+// permuted right-hand side, then the backward sweep's output, copied back into b
+template <typename T, typename RT>
+int trsv_pair(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* perm, T* B, int64_t ldb,
+              int64_t nrhs, T* tmp, const T* dinv) {
+  cudaStream_t st = ctx->stream;
+  const int nblk = (int)((n + 63) / 64);
+  int occ = 0;
+  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, 0));
+  const int G = std::max(1, std::min(nblk, ctx->num_sms * std::max(occ, 1)));
+  int* status = ctx->d_flag;
+  const unsigned ge = (unsigned)((n + 255) / 256);
+  for (int64_t rr = 0; rr < nrhs; ++rr) {
+    T* b = B + rr * ldb;
+    // the two triangular solves read the factors once: n^2 elements
+    ProfScope ps(ctx, PK_TRSV, (double)n * n * sizeof(T), 5);
+    k_permute<T><<<ge, 256, 0, st>>>(b, tmp, perm, n);
+    k_fill_sentinel<T><<<ge, 256, 0, st>>>(b, n);
+    int lower = 1;
+    const T* in = tmp;
+    T* outp = b;
+    void* args[] = {&A, &lda, &n, &in, &outp, &lower, &status, &dinv};
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
+    k_fill_sentinel<T><<<ge, 256, 0, st>>>(tmp, n);
+    lower = 0;
+    in = b;
+    outp = tmp;
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
+    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(b, tmp, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, st));
+  }
+  BEAST_CUDA_TRY(ctx, cudaGetLastError());
+  return BEAST_OK;
+}
+
 template <typename T, typename RT>
 int lu_solve_t(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* perm, T* B,
                int64_t ldb, int64_t nrhs, const T* dinv) {
   cudaStream_t st = ctx->stream;
-  const int nblk = (int)((n + 63) / 64);
   T* tmp = nullptr;
-  int* flags = nullptr;
   BEAST_CUDA_TRY(ctx, cudaMallocAsync(&tmp, (size_t)n * sizeof(T), st));
-  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&flags, (size_t)2 * nblk * sizeof(int) + 16, st));
-  int occ = 0;
-  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, 0));
-  int G = std::max(1, std::min(nblk, ctx->num_sms * std::max(occ, 1)));
-  int* status = ctx->d_flag;
-  for (int64_t r = 0; r < nrhs; ++r) {
-    T* b = B + r * ldb;
-    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(tmp, b, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, st));
-    BEAST_CUDA_TRY(ctx, cudaMemsetAsync(flags, 0, (size_t)2 * nblk * sizeof(int), st));
-    // the two triangular solves read the factors once: n^2 elements
-    ProfScope ps(ctx, PK_TRSV, (double)n * n * sizeof(T), 3);
-    k_permute<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tmp, b, perm, n);
-    int lower = 1;
-    int* fl = flags;
-    void* args[] = {&A, &lda, &n, &b, &lower, &fl, &status, &dinv};
-    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
-    lower = 0;
-    fl = flags + nblk;
-    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
-  }
-  BEAST_CUDA_TRY(ctx, cudaGetLastError());
+  int rc = trsv_pair<T, RT>(ctx, n, A, lda, perm, B, ldb, nrhs, tmp, dinv);
   BEAST_CUDA_TRY(ctx, cudaFreeAsync(tmp, st));
-  BEAST_CUDA_TRY(ctx, cudaFreeAsync(flags, st));
-  return BEAST_OK;
+  return rc;
 }
 
 // ---- allocation-free triangular solve ----------------------------------------------------
-// Scratch of beast_lu_solve_noalloc: one permuted right-hand side of up to
-// NOALLOC_MAX_N complex128 values, then the per-block flags of the two wavefront sweeps.
+// Scratch of beast_lu_solve_noalloc: one right-hand side of up to NOALLOC_MAX_N complex128
+// values (the permuted right-hand side, then the backward sweep's output).
 // Held by every GPU that loads the library, for the life of the process.
 constexpr int64_t NOALLOC_MAX_N = 65536;
-constexpr int64_t NOALLOC_FLAGS = 2 * ((NOALLOC_MAX_N + 63) / 64);
-static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_MAX_N * 16 + NOALLOC_FLAGS * 4];
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NOALLOC_MAX_N * 16];
 
 template <typename T, typename RT>
 int lu_solve_fixed_scratch(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* perm, T* B,
                            int64_t ldb, int64_t nrhs, unsigned char* scratch, const T* dinv) {
-  cudaStream_t st = ctx->stream;
-  const int nblk = (int)((n + 63) / 64);
-  T* tmp = reinterpret_cast<T*>(scratch);
-  int* flags = reinterpret_cast<int*>(scratch + NOALLOC_MAX_N * 16);
-  int occ = 0;
-  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, 0));
-  int G = std::max(1, std::min(nblk, ctx->num_sms * std::max(occ, 1)));
-  int* status = ctx->d_flag;
-  for (int64_t r = 0; r < nrhs; ++r) {
-    T* b = B + r * ldb;
-    BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(tmp, b, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, st));
-    // the array keeps the previous call's flags: clear them for this solve
-    BEAST_CUDA_TRY(ctx, cudaMemsetAsync(flags, 0, (size_t)2 * nblk * sizeof(int), st));
-    k_permute<T><<<(unsigned)((n + 255) / 256), 256, 0, st>>>(tmp, b, perm, n);
-    int lower = 1;
-    int* fl = flags;
-    void* args[] = {&A, &lda, &n, &b, &lower, &fl, &status, &dinv};
-    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
-    lower = 0;
-    fl = flags + nblk;
-    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
-  }
-  BEAST_CUDA_TRY(ctx, cudaGetLastError());
-  return BEAST_OK;
+  // the scratch keeps the previous call's values; every value it is read for is written
+  // first in this call (the permutation, then the sentinel fill)
+  return trsv_pair<T, RT>(ctx, n, A, lda, perm, B, ldb, nrhs, reinterpret_cast<T*>(scratch), dinv);
 }
 
 }  // namespace
