@@ -838,6 +838,8 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
     T dv[16];
 #pragma unroll
     for (int c = 0; c < 16; ++c) dv[c] = Di[(q * 16 + c) * 64 + r];
+    // the block's right-hand side, needed right after the last dependency
+    const T bv = (tid < rb) ? rhs[r0 + tid] : zero;
     // this thread's 16 entries of the factor block of dependency s (row r0 + r)
     auto load_blk = [&](int s, T* dst) {
       const int k = lower ? s : nblk - 1 - s;
@@ -888,7 +890,7 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
         // spin on one value (one load per warp per round keeps the polling traffic low),
         // then re-read the ones still missing
         const int last = 31 - __clz(pend);
-        while (is_sent(ld_raw(xk + last)) && ++it <= TRSV_SPIN_MAX) __nanosleep(64);
+        while (is_sent(ld_raw(xk + last)) && ++it <= TRSV_SPIN_MAX) __nanosleep(32);
         if (it > TRSV_SPIN_MAX) {
           if (!timed_out) atomicOr(status, 8);
           timed_out = true;
@@ -916,7 +918,6 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
     if (tid < 64) {
       RT vr = 0, vi = 0;
       if (tid < rb) {
-        const T bv = rhs[r0 + tid];
         vr = (RT)bv.x - (pr[0][tid] + pr[1][tid] + pr[2][tid] + pr[3][tid]);
         vi = (RT)bv.y - (pim[0][tid] + pim[1][tid] + pim[2][tid] + pim[3][tid]);
       }
