@@ -820,9 +820,34 @@ __global__ void k_fill_sentinel(T* v, int64_t n) {
   }
 }
 
+// ring of factor blocks for the wavefront solve: stages of 16 x 256 elements
+template <typename T>
+struct TrsvRing {
+  static constexpr int STG = sizeof(T) == 8 ? 4 : 3;
+  static constexpr size_t BYTES = (size_t)STG * 16 * 256 * sizeof(T);
+};
+// one element global -> shared, asynchronously (zero-filled when !in: nothing is read)
+__device__ __forceinline__ void cp_async_el(float2* dst, const float2* src, bool in) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8, %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+               "l"(src), "r"(in ? 8 : 0)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_el(double2* dst, const double2* src, bool in) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"((unsigned)__cvta_generic_to_shared(dst)),
+               "l"(src), "r"(in ? 16 : 0)
+               : "memory");
+}
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 template <typename T, typename RT>
 __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int64_t n, const T* rhs, T* out,
                                                    int lower, int* status, const T* dinv) {
+  constexpr int STG = TrsvRing<T>::STG;
+  extern __shared__ __align__(16) unsigned char trsv_smraw[];
+  T* ring = reinterpret_cast<T*>(trsv_smraw);  // STG x 16 x 256 elements
   __shared__ RT sr[64], si[64];
   __shared__ RT pr[4][64], pim[4][64];
   const int nblk = (int)((n + 63) / 64);
@@ -840,17 +865,24 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
     for (int c = 0; c < 16; ++c) dv[c] = Di[(q * 16 + c) * 64 + r];
     // the block's right-hand side, needed right after the last dependency
     const T bv = (tid < rb) ? rhs[r0 + tid] : zero;
-    // this thread's 16 entries of the factor block of dependency s (row r0 + r)
-    auto load_blk = [&](int s, T* dst) {
-      const int k = lower ? s : nblk - 1 - s;
-      const int64_t c0 = (int64_t)k * 64;
-      const int cb = (int)(n - c0 < 64 ? n - c0 : 64);
-      const T* Ar = A + (r0 + r) + c0 * lda;
+    // this thread's 16 entries of the factor block of dependency s (row r0 + r) go into ring
+    // stage s % TRSV_STG by cp.async: each thread reads back only what it copied itself, so
+    // the walk needs no barrier
+    auto issue_blk = [&](int s) {
+      if (s < t) {
+        const int k = lower ? s : nblk - 1 - s;
+        const int64_t c0 = (int64_t)k * 64;
+        const int cb = (int)(n - c0 < 64 ? n - c0 : 64);
+        const T* Ar = A + (r0 + r) + c0 * lda;
+        T* st = ring + (size_t)(s % STG) * 16 * 256;
 #pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        const int col = q * 16 + c;
-        dst[c] = (r < rb && col < cb) ? Ar[col * lda] : zero;
+        for (int c = 0; c < 16; ++c) {
+          const int col = q * 16 + c;
+          const bool in = r < rb && col < cb;
+          cp_async_el(st + c * 256 + tid, in ? Ar + (int64_t)col * lda : A, in);
+        }
       }
+      asm volatile("cp.async.commit_group;" ::: "memory");
     };
     // this thread's 16 solved values of dependency s, read as they are (maybe sentinels)
     auto load_x = [&](int s, T* dst) {
@@ -861,24 +893,26 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
       for (int c = 0; c < 16; ++c) dst[c] = q * 16 + c < cb ? ld_raw(out + c0 + q * 16 + c) : zero;
     };
     RT ar = 0, ai = 0;
-    T nxt[16], xn[16];
-    if (t > 0) {
-      load_blk(0, nxt);
-      load_x(0, xn);
-    }
+    T xn1[16], xn2[16];
+#pragma unroll
+    for (int j = 0; j < STG - 1; ++j) issue_blk(j);
+    if (t > 0) load_x(0, xn1);
+    if (t > 1) load_x(1, xn2);
     for (int s = 0; s < t; ++s) {
-      T cur[16], xv[16];
+      issue_blk(s + STG - 1);
+      T xv[16];
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
-        cur[c] = nxt[c];
-        xv[c] = xn[c];
+        xv[c] = xn1[c];
+        xn1[c] = xn2[c];
       }
-      // the next dependency's factor entries and solved values are requested before this
-      // one is used
-      if (s + 1 < t) {
-        load_blk(s + 1, nxt);
-        load_x(s + 1, xn);
-      }
+      // solved values two dependencies ahead are requested before this one is used
+      if (s + 2 < t) load_x(s + 2, xn2);
+      cp_async_wait<STG - 1>();  // this thread's copies of dependency s have landed
+      const T* st = ring + (size_t)(s % STG) * 16 * 256;
+      T cur[16];
+#pragma unroll
+      for (int c = 0; c < 16; ++c) cur[c] = st[c * 256 + tid];
       const int k = lower ? s : nblk - 1 - s;
       const T* xk = out + (int64_t)k * 64 + q * 16;
       unsigned pend = 0;
@@ -912,6 +946,7 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
         ai += (RT)cur[c].x * (RT)xv[c].y + (RT)cur[c].y * (RT)xv[c].x;
       }
     }
+    cp_async_wait<0>();
     pr[q][r] = ar;
     pim[q][r] = ai;
     __syncthreads();
@@ -1335,8 +1370,10 @@ int trsv_pair(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* per
               int64_t nrhs, T* tmp, const T* dinv) {
   cudaStream_t st = ctx->stream;
   const int nblk = (int)((n + 63) / 64);
+  const size_t ring = TrsvRing<T>::BYTES;
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsv_wave<T, RT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ring));
   int occ = 0;
-  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, 0));
+  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, ring));
   const int G = std::max(1, std::min(nblk, ctx->num_sms * std::max(occ, 1)));
   int* status = ctx->d_flag;
   const unsigned ge = (unsigned)((n + 255) / 256);
@@ -1350,12 +1387,12 @@ int trsv_pair(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* per
     const T* in = tmp;
     T* outp = b;
     void* args[] = {&A, &lda, &n, &in, &outp, &lower, &status, &dinv};
-    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, ring, st));
     k_fill_sentinel<T><<<ge, 256, 0, st>>>(tmp, n);
     lower = 0;
     in = b;
     outp = tmp;
-    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, 0, st));
+    BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, ring, st));
     BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(b, tmp, (size_t)n * sizeof(T), cudaMemcpyDeviceToDevice, st));
   }
   BEAST_CUDA_TRY(ctx, cudaGetLastError());
