@@ -823,7 +823,7 @@ __global__ void k_fill_sentinel(T* v, int64_t n) {
 // ring of factor blocks for the wavefront solve: stages of 16 x 256 elements
 template <typename T>
 struct TrsvRing {
-  static constexpr int STG = sizeof(T) == 8 ? 4 : 3;
+  static constexpr int STG = sizeof(T) == 8 ? 3 : 2;
   static constexpr size_t BYTES = (size_t)STG * 16 * 256 * sizeof(T);
 };
 // one element global -> shared, asynchronously (zero-filled when !in: nothing is read)
@@ -884,66 +884,48 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
       }
       asm volatile("cp.async.commit_group;" ::: "memory");
     };
-    // this thread's 16 solved values of dependency s, read as they are (maybe sentinels)
-    auto load_x = [&](int s, T* dst) {
+    // the solved values of dependency s: lane l of a warp (all its lanes share q) reads value
+    // q*16 + (l & 15) as it is in memory (maybe still the sentinel): the warp's 16 values
+    // are one 128-byte line, so one request per warp per poll, and they are passed to every
+    // lane with shuffles once all are written
+    const int lane = tid & 31;
+    auto load_x = [&](int s) -> T {
       const int k = lower ? s : nblk - 1 - s;
-      const int64_t c0 = (int64_t)k * 64;
-      const int cb = (int)(n - c0 < 64 ? n - c0 : 64);
-#pragma unroll
-      for (int c = 0; c < 16; ++c) dst[c] = q * 16 + c < cb ? ld_raw(out + c0 + q * 16 + c) : zero;
+      const int c = q * 16 + (lane & 15);
+      return c < (int)(n - (int64_t)k * 64) ? ld_raw(out + (int64_t)k * 64 + c) : zero;
     };
     RT ar = 0, ai = 0;
-    T xn1[16], xn2[16];
+    T x1 = zero, x2 = zero;
 #pragma unroll
     for (int j = 0; j < STG - 1; ++j) issue_blk(j);
-    if (t > 0) load_x(0, xn1);
-    if (t > 1) load_x(1, xn2);
+    if (t > 0) x1 = load_x(0);
+    if (t > 1) x2 = load_x(1);
     for (int s = 0; s < t; ++s) {
       issue_blk(s + STG - 1);
-      T xv[16];
-#pragma unroll
-      for (int c = 0; c < 16; ++c) {
-        xv[c] = xn1[c];
-        xn1[c] = xn2[c];
-      }
       // solved values two dependencies ahead are requested before this one is used
-      if (s + 2 < t) load_x(s + 2, xn2);
+      T v = x1;
+      x1 = x2;
+      if (s + 2 < t) x2 = load_x(s + 2);
       cp_async_wait<STG - 1>();  // this thread's copies of dependency s have landed
       const T* st = ring + (size_t)(s % STG) * 16 * 256;
       T cur[16];
 #pragma unroll
       for (int c = 0; c < 16; ++c) cur[c] = st[c * 256 + tid];
-      const int k = lower ? s : nblk - 1 - s;
-      const T* xk = out + (int64_t)k * 64 + q * 16;
-      unsigned pend = 0;
-#pragma unroll
-      for (int c = 0; c < 16; ++c)
-        if (is_sent(xv[c])) pend |= 1u << c;
       long long it = 0;
-      while (pend) {
-        // spin on one value (one load per warp per round keeps the polling traffic low),
-        // then re-read the ones still missing
-        const int last = 31 - __clz(pend);
-        while (is_sent(ld_raw(xk + last)) && ++it <= TRSV_SPIN_MAX) __nanosleep(32);
-        if (it > TRSV_SPIN_MAX) {
+      while (!__all_sync(0xffffffffu, !is_sent(v))) {  // warp-uniform
+        if (++it > TRSV_SPIN_MAX) {
           if (!timed_out) atomicOr(status, 8);
           timed_out = true;
-#pragma unroll
-          for (int c = 0; c < 16; ++c)
-            if (pend & (1u << c)) xv[c] = zero;
+          if (is_sent(v)) v = zero;
           break;
         }
-#pragma unroll
-        for (int c = 0; c < 16; ++c)
-          if (pend & (1u << c)) {
-            xv[c] = ld_raw(xk + c);
-            if (!is_sent(xv[c])) pend &= ~(1u << c);
-          }
+        if (is_sent(v)) v = load_x(s);
       }
 #pragma unroll
       for (int c = 0; c < 16; ++c) {
-        ar += (RT)cur[c].x * (RT)xv[c].x - (RT)cur[c].y * (RT)xv[c].y;
-        ai += (RT)cur[c].x * (RT)xv[c].y + (RT)cur[c].y * (RT)xv[c].x;
+        const T xc = shfl_c(v, c);
+        ar += (RT)cur[c].x * (RT)xc.x - (RT)cur[c].y * (RT)xc.y;
+        ai += (RT)cur[c].x * (RT)xc.y + (RT)cur[c].y * (RT)xc.x;
       }
     }
     cp_async_wait<0>();
