@@ -435,16 +435,18 @@ __global__ void __launch_bounds__(256) k_getrf64(T* A, int64_t lda, int64_t j0, 
 // share one triangle of the factored diagonal block at (j0, j0):
 //   left  (U12 = L11^{-1} A12): one system per column of A12, unit lower L11;
 //   right (unpivoted path, L21 = A21 U11^{-1}): one system per row of A21, upper U11.
-// A CTA stages NS systems (coalesced global loads) as X[k][s] in shared memory, one system
-// per thread, and the triangle as M[k][c] = coefficient of x_k in equation c (k < c).  Each
-// thread then substitutes in blocks of 16 unknowns held in registers,
-//   x_c = (a_c - sum_{k<c} M[k][c] x_k) * d_c     (d_c = 1 or 1/U_cc),
-// reading its solved unknowns back from its own shared-memory column; the triangle rows are
-// warp-wide broadcasts, prefetched one row ahead.
+// A CTA stages NS = 64 systems (coalesced global loads) as X[k][s] in shared memory and the
+// triangle as M[k][c] = coefficient of x_k in equation c (k < c).  Four neighbouring lanes
+// share a system and substitute in blocks of 16 unknowns, lane j of the four owning unknowns
+// 4j .. 4j+3 of each block:
+//   x_c = (a_c - sum_{k<c} M[k][c] x_k) * d_c     (d_c = 1 or 1/U_cc);
+// the terms of earlier blocks are split over the four lanes, and inside a block each solved
+// unknown is passed to the other three lanes by a shuffle.
 template <typename T>
 struct TrsmTile {
-  static constexpr int NS = 64;                          // systems (threads) per CTA
-  static constexpr int MLD = sizeof(T) == 8 ? 66 : 65;   // row stride of M: 16-byte rows
+  static constexpr int NS = 64;                          // systems per CTA
+  static constexpr int NT = 4 * NS;                      // threads per CTA
+  static constexpr int MLD = sizeof(T) == 8 ? 66 : 65;   // row stride of M
 };
 
 template <typename T>
@@ -453,9 +455,9 @@ size_t trsm_tile_smem() {
 }
 
 template <typename T, typename RT, bool RIGHT>
-__global__ void __launch_bounds__(TrsmTile<T>::NS) k_trsm_tile(T* A, int64_t lda, int64_t j0, int kb,
+__global__ void __launch_bounds__(TrsmTile<T>::NT) k_trsm_tile(T* A, int64_t lda, int64_t j0, int kb,
                                                                int64_t s0, int64_t s1) {
-  constexpr int NS = TrsmTile<T>::NS, MLD = TrsmTile<T>::MLD, LDX = NS + 1;
+  constexpr int NS = TrsmTile<T>::NS, NT = TrsmTile<T>::NT, MLD = TrsmTile<T>::MLD, LDX = NS + 1;
   extern __shared__ __align__(16) unsigned char smraw[];
   T* M = reinterpret_cast<T*>(smraw);  // TRI x MLD
   T* dinv = M + TRI * MLD;             // TRI
@@ -465,20 +467,20 @@ __global__ void __launch_bounds__(TrsmTile<T>::NS) k_trsm_tile(T* A, int64_t lda
   const T zero = {0, 0};
 
   // the triangle (zero outside kb x kb and on/below the diagonal of M) and the systems
-  // X[k][s]; the loads of a thread are issued in batches of LB before their stores
-  constexpr int LB = 16;
-  static_assert((TRI * TRI / NS) % LB == 0 && TRI % LB == 0, "load batches");
-  for (int m0 = 0; m0 < TRI * TRI / NS; m0 += LB) {
+  // X[k][s]; each thread issues its 16 + 16 loads before the stores
+  constexpr int LB = TRI * TRI / NT;
+  static_assert(LB * NT == TRI * TRI && LB * NT == TRI * NS, "staging");
+  {
     T v[LB];
 #pragma unroll
     for (int j = 0; j < LB; ++j) {
-      const int e = tid + NS * (m0 + j);
+      const int e = tid + NT * j;
       const int r = e % TRI, k = e / TRI;  // global element (j0 + r, j0 + k), coalesced along r
       v[j] = (r < kb && k < kb) ? A[(j0 + r) + (j0 + k) * lda] : zero;
     }
 #pragma unroll
     for (int j = 0; j < LB; ++j) {
-      const int e = tid + NS * (m0 + j);
+      const int e = tid + NT * j;
       const int r = e % TRI, k = e / TRI;
       if (RIGHT) {
         M[r * MLD + k] = r < k ? v[j] : zero;  // U[r][k]: coefficient of x_r in equation k
@@ -496,11 +498,11 @@ __global__ void __launch_bounds__(TrsmTile<T>::NS) k_trsm_tile(T* A, int64_t lda
       }
     }
   }
-  for (int m0 = 0; m0 < TRI; m0 += LB) {
+  {
     T v[LB];
 #pragma unroll
     for (int j = 0; j < LB; ++j) {
-      const int e = tid + NS * (m0 + j);
+      const int e = tid + NT * j;
       if (RIGHT) {
         const int s = e % NS, k = e / NS;  // row sb + s, column j0 + k: coalesced along s
         v[j] = (k < kb && sb + s < s1) ? A[(sb + s) + (j0 + k) * lda] : zero;
@@ -511,7 +513,7 @@ __global__ void __launch_bounds__(TrsmTile<T>::NS) k_trsm_tile(T* A, int64_t lda
     }
 #pragma unroll
     for (int j = 0; j < LB; ++j) {
-      const int e = tid + NS * (m0 + j);
+      const int e = tid + NT * j;
       if (RIGHT)
         X[(e / NS) * LDX + e % NS] = v[j];
       else
@@ -520,60 +522,47 @@ __global__ void __launch_bounds__(TrsmTile<T>::NS) k_trsm_tile(T* A, int64_t lda
   }
   __syncthreads();
 
-  // substitution, 16 unknowns at a time
+  // substitution: lane quad (4 s .. 4 s + 3) of the warp owns system s, lane j owns
+  // unknowns 4 j .. 4 j + 3 of each block of 16
+  const int s = tid >> 2, j = tid & 3, qbase = (tid & 31) & ~3;
+  T* x = X + s;
   const int nblk = (kb + 15) / 16;
-  T* x = X + tid;
   for (int B = 0; B < nblk; ++B) {
-    const int c0 = 16 * B;
-    T acc[16];
+    const int c0 = 16 * B, cj = c0 + 4 * j;
+    T acc[4];
 #pragma unroll
-    for (int c = 0; c < 16; ++c) acc[c] = x[(c0 + c) * LDX];
-    if (c0 > 0) {
-      // acc_c -= sum_{k < c0} M[k][c0 + c] x_k, the next row of M prefetched
-      T mc[16], xc = x[0];
+    for (int i = 0; i < 4; ++i) acc[i] = x[(cj + i) * LDX];
+    for (int k = 0; k < c0; ++k) {
+      const T xk = x[k * LDX];
+      const T* mk = M + k * MLD + cj;
 #pragma unroll
-      for (int c = 0; c < 16; ++c) mc[c] = M[c0 + c];
-      for (int k = 0; k < c0; ++k) {
-        const int kn = k + 1 < c0 ? k + 1 : k;
-        T mn[16];
-#pragma unroll
-        for (int c = 0; c < 16; ++c) mn[c] = M[kn * MLD + c0 + c];
-        const T xn = x[kn * LDX];
-#pragma unroll
-        for (int c = 0; c < 16; ++c) cfms(acc[c], mc[c], xc);
-#pragma unroll
-        for (int c = 0; c < 16; ++c) mc[c] = mn[c];
-        xc = xn;
-      }
+      for (int i = 0; i < 4; ++i) cfms(acc[i], mk[i], xk);
     }
 #pragma unroll
-    for (int c = 0; c < 16; ++c) {
-#pragma unroll
-      for (int k = 0; k < c; ++k) cfms(acc[c], M[(c0 + k) * MLD + c0 + c], acc[k]);
-      if (RIGHT) {
-        const T d = dinv[c0 + c];
-        T q;
-        q.x = acc[c].x * d.x - acc[c].y * d.y;
-        q.y = acc[c].x * d.y + acc[c].y * d.x;
-        acc[c] = q;
+    for (int cc = 0; cc < 16; ++cc) {
+      const int jo = cc >> 2, io = cc & 3;
+      if (RIGHT && j == jo) {
+        const T d = dinv[c0 + cc];
+        acc[io] = cmulx(acc[io], d);
       }
-      x[(c0 + c) * LDX] = acc[c];
+      const T xc = shfl_c(acc[io], qbase + jo);  // the solved unknown c0 + cc
+      if (j == jo) x[(c0 + cc) * LDX] = xc;
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+        if (4 * j + i > cc) cfms(acc[i], M[(c0 + cc) * MLD + cj + i], xc);
     }
   }
   __syncthreads();
 
   // write the solved systems back
-  for (int m0 = 0; m0 < TRI; m0 += LB) {
-#pragma unroll
-    for (int j = 0; j < LB; ++j) {
-      const int e = tid + NS * (m0 + j);
-      if (RIGHT) {
-        const int s = e % NS, k = e / NS;
-        if (k < kb && sb + s < s1) A[(sb + s) + (j0 + k) * lda] = X[k * LDX + s];
-      } else {
-        const int k = e % TRI, s = e / TRI;
-        if (k < kb && sb + s < s1) A[(j0 + k) + (sb + s) * lda] = X[k * LDX + s];
-      }
+  for (int m0 = 0; m0 < TRI * NS / NT; ++m0) {
+    const int e = tid + NT * m0;
+    if (RIGHT) {
+      const int s2 = e % NS, k = e / NS;
+      if (k < kb && sb + s2 < s1) A[(sb + s2) + (j0 + k) * lda] = X[k * LDX + s2];
+    } else {
+      const int k = e % TRI, s2 = e / TRI;
+      if (k < kb && sb + s2 < s1) A[(j0 + k) + (sb + s2) * lda] = X[k * LDX + s2];
     }
   }
 }
@@ -1176,7 +1165,7 @@ struct LUSteps {
     if (c1 <= c0) return BEAST_OK;
     ProfScope ps(ctx, PK_TRSM, 4.0 * (double)(c1 - c0) * kb * kb);
     constexpr int NS = TrsmTile<T>::NS;
-    k_trsm_tile<T, R, false><<<(unsigned)((c1 - c0 + NS - 1) / NS), NS, trsm_tile_smem<T>(), st>>>(
+    k_trsm_tile<T, R, false><<<(unsigned)((c1 - c0 + NS - 1) / NS), TrsmTile<T>::NT, trsm_tile_smem<T>(), st>>>(
         A, lda, j0, kb, c0, c1);
     BEAST_CUDA_TRY(ctx, cudaGetLastError());
     return BEAST_OK;
@@ -1282,7 +1271,7 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
         k_getrf64<T><<<1, 256, (size_t)TRI * (TRI + 1) * sizeof(T), st>>>(A, lda, j0, kb, dinfo);
         const int64_t rb = n - j0 - kb;
         if (rb > 0)
-          k_trsm_tile<T, R, true><<<(unsigned)((rb + NS - 1) / NS), NS, trsm_tile_smem<T>(), st>>>(
+          k_trsm_tile<T, R, true><<<(unsigned)((rb + NS - 1) / NS), TrsmTile<T>::NT, trsm_tile_smem<T>(), st>>>(
               A, lda, j0, kb, j0 + kb, n);
         BEAST_CUDA_TRY(ctx, cudaGetLastError());
       }
