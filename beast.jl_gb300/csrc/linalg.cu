@@ -310,12 +310,26 @@ __device__ __forceinline__ T cmulx(T a, T b) {
   r.y = a.x * b.y + a.y * b.x;
   return r;
 }
-template <typename T>
-__device__ __forceinline__ bool crecip(T p, T& r) {  // r = 1 / p; false for p = 0
-  typedef decltype(T().x) RT;
-  const RT den = p.x * p.x + p.y * p.y;
-  if (den == (RT)0) return false;
-  const RT id = (RT)1 / den;
+// r = 1 / p; false for p = 0.  FP32: the hardware reciprocal (rcp.approx, within 1 ulp) --
+// this is on the serial pivot chain of the unpivoted mixed-precision LU, whose result is
+// refined in FP64 anyway; FP64: IEEE division
+__device__ __forceinline__ float rcp_f(float x) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
+}
+__device__ __forceinline__ bool crecip(float2 p, float2& r) {
+  const float den = p.x * p.x + p.y * p.y;
+  if (den == 0.f) return false;
+  const float id = rcp_f(den);
+  r.x = p.x * id;
+  r.y = -p.y * id;
+  return true;
+}
+__device__ __forceinline__ bool crecip(double2 p, double2& r) {
+  const double den = p.x * p.x + p.y * p.y;
+  if (den == 0.0) return false;
+  const double id = 1.0 / den;
   r.x = p.x * id;
   r.y = -p.y * id;
   return true;
@@ -532,11 +546,19 @@ __global__ void __launch_bounds__(TrsmTile<T>::NT) k_trsm_tile(T* A, int64_t lda
     T acc[4];
 #pragma unroll
     for (int i = 0; i < 4; ++i) acc[i] = x[(cj + i) * LDX];
-    for (int k = 0; k < c0; ++k) {
-      const T xk = x[k * LDX];
-      const T* mk = M + k * MLD + cj;
+    // c0 is a multiple of 16: four earlier unknowns per pass, their loads issued together
+    for (int k = 0; k < c0; k += 4) {
+      T xk[4], mk[4][4];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) cfms(acc[i], mk[i], xk);
+      for (int u = 0; u < 4; ++u) {
+        xk[u] = x[(k + u) * LDX];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) mk[u][i] = M[(k + u) * MLD + cj + i];
+      }
+#pragma unroll
+      for (int u = 0; u < 4; ++u)
+#pragma unroll
+        for (int i = 0; i < 4; ++i) cfms(acc[i], mk[u][i], xk[u]);
     }
 #pragma unroll
     for (int cc = 0; cc < 16; ++cc) {
