@@ -1269,10 +1269,17 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   LUSteps<T, R> S{ctx, A, lda, n, ipiv, st, tcwork_bytes};
 
   int rc = BEAST_OK;
+  // unpivoted, the outer block is factored in mid blocks of NB2 columns: the panels update
+  // only their mid block (and its rows beyond it), the mid block updates the rest of the
+  // outer block with K = NB2, and the outer block the trailing matrix with K = NB -- fewer
+  // passes of narrow (K = nb) updates over the same columns
+  const int64_t NB2 = pivot ? NB : 4 * nb;
   for (int64_t J0 = 0; J0 < n && rc == BEAST_OK; J0 += NB) {
     const int64_t J1 = std::min<int64_t>(n, J0 + NB);
-    for (int64_t j0 = J0; j0 < J1 && rc == BEAST_OK; j0 += nb) {
-      int kb = (int)std::min<int64_t>(nb, J1 - j0);
+    for (int64_t M0 = J0; M0 < J1 && rc == BEAST_OK; M0 += NB2) {
+    const int64_t M1 = std::min<int64_t>(J1, M0 + NB2);
+    for (int64_t j0 = M0; j0 < M1 && rc == BEAST_OK; j0 += nb) {
+      int kb = (int)std::min<int64_t>(nb, M1 - j0);
       int64_t M = n - j0;
       int rows_per = (int)((M + G0 - 1) / G0);
       int G = (int)((M + rows_per - 1) / rows_per);
@@ -1302,11 +1309,16 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       // the block's rows of the columns beyond the block are updated here too (what the
       // pivoted path does per panel after the block).
       if ((rc = S.trsm(j0, kb, j0 + kb, pivot ? J1 : n))) break;
-      // in-block update (all rows below, block columns) and, unpivoted, the block rows of
-      // the columns beyond the block, as one L-shaped update
-      if ((rc = S.gemm2(j0 + kb, n - j0 - kb, j0 + kb, J1 - j0 - kb, pivot ? 0 : J1 - j0 - kb,
-                        pivot ? 0 : n - J1, j0, kb, tcwork)))
+      // in-block update (all rows below, mid-block columns) and, unpivoted, the mid block's
+      // rows of the columns beyond it, as one L-shaped update
+      if ((rc = S.gemm2(j0 + kb, n - j0 - kb, j0 + kb, M1 - j0 - kb, pivot ? 0 : M1 - j0 - kb,
+                        pivot ? 0 : n - M1, j0, kb, tcwork)))
         break;
+    }
+    if (rc) break;
+    // mid-block update: rows below x the rest of the outer block, and the rest of the outer
+    // block's rows x the columns beyond it (K = NB2; nothing when pivoting: NB2 = NB)
+    if (M1 < J1 && (rc = S.gemm2(M1, n - M1, M1, J1 - M1, J1 - M1, n - J1, M0, (int)(M1 - M0), tcwork))) break;
     }
     if (rc) break;
     // the block's interchanges on the columns left and right of it
