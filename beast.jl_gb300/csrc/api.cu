@@ -327,6 +327,20 @@ int beast_space_upload(beast_ctx* ctx, const beast_mesh* mesh, int kind, int64_t
   up((void**)&s->fn_cell, s->h_fn_cell.data(), sizeof(int) * s->h_fn_cell.size());
   up((void**)&s->fn_shape, s->h_fn_shape.data(), sizeof(int) * s->h_fn_shape.size());
   up((void**)&s->fn_coeff, s->h_fn_coeff.data(), sizeof(double) * s->h_fn_coeff.size());
+  // Zcell row order on the test side: active cells by their first (lowest) function, so that
+  // consecutive functions read nearby Zcell rows in the gather
+  {
+    std::vector<int64_t> key(ncells, INT64_MAX);
+    for (int64_t f = 0; f < nfuncs; ++f)
+      for (int64_t e = s->h_fn_ptr[f]; e < s->h_fn_ptr[f + 1]; ++e)
+        key[s->h_fn_cell[e]] = std::min<int64_t>(key[s->h_fn_cell[e]], f);
+    std::vector<int> perm(ncells), pos(ncells);
+    for (int64_t c = 0; c < ncells; ++c) perm[c] = (int)c;
+    std::stable_sort(perm.begin(), perm.end(), [&](int a, int b) { return key[a] < key[b]; });
+    for (int64_t i = 0; i < ncells; ++i) pos[perm[i]] = (int)i;
+    up((void**)&s->tperm, perm.data(), sizeof(int) * ncells);
+    up((void**)&s->tpos, pos.data(), sizeof(int) * ncells);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&s->geo, sizeof(double) * GEO_STRIDE * ncells);
   if (e == cudaSuccess) e = cudaMalloc(&s->geof, sizeof(float) * 4 * ncells);
   if (e == cudaSuccess) e = launch_geometry(s, st);
@@ -344,7 +358,7 @@ int beast_space_free(beast_space* s) {
   cudaSetDevice(s->ctx->device);
   cudaStreamSynchronize(s->ctx->stream);
   void* ptrs[] = {s->cells, s->cell2act, s->ad_dof, s->ad_coeff, s->geo, s->geof,
-                  s->fn_ptr, s->fn_cell, s->fn_shape, s->fn_coeff};
+                  s->fn_ptr, s->fn_cell, s->fn_shape, s->fn_coeff, s->tperm, s->tpos};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete s;
@@ -478,6 +492,7 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
     g.zcell_c64 = zc64;
     g.ldc = ldc;
     g.qlocal = qlocal_d;
+    g.tpos = ts->tpos;
     g.n0 = ch.n0;
     g.n1 = ch.n1;
     g.Z = Z;

@@ -246,6 +246,7 @@ struct FarParams {
   OpParams op;
   int qs_kind;
   double k2;
+  const int* tperm;  // Zcell position -> test active cell
   const double* tgeo;
   const float* tgeof;
   int64_t np;
@@ -331,8 +332,11 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
     }
   }
   __syncthreads();
-  const int64_t p = blockIdx.x * (int64_t)FAR_THREADS + threadIdx.x;
-  if (p >= P.np) return;
+  // pp: the test cell's Zcell position (cells in the order of their first function, so that
+  // the rows a warp of the gather reads are close together); p: the active cell
+  const int64_t pp = blockIdx.x * (int64_t)FAR_THREADS + threadIdx.x;
+  if (pp >= P.np) return;
+  const int64_t p = P.tperm[pp];
   const double* tg = P.tgeo + p * GEO_STRIDE;
   const double cpx = tg[9], cpy = tg[10], cpz = tg[11];
   const V3<R> chp = mk((R)cpx, (R)cpy, (R)cpz);
@@ -365,12 +369,12 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
         if (cls != 0) {
           int idx = atomicAdd(P.near_count, 1);
           if (idx < P.near_cap)
-            P.near[idx] = NearPair{(int)p, ql, cls, 0};
+            P.near[idx] = NearPair{(int)pp, ql, cls, 0};
           else
             atomicOr(P.flag, 1);
           for (int i = 0; i < nst; ++i)
             for (int j = 0; j < nsb; ++j)
-              store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * p + i, C2<R>{0, 0}, C64);
+              store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * pp + i, C2<R>{0, 0}, C64);
           continue;
         }
       }
@@ -503,7 +507,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
             f = csub(f, cscale(dot(ti, sj), M3));
             z = cscale((R)0.25, f);
           }
-          store_c<R>(P.zcell, (int64_t)(3 * ql + j) * P.ldc + 3 * p + i, z, C64);
+          store_c<R>(P.zcell, (int64_t)(3 * ql + j) * P.ldc + 3 * pp + i, z, C64);
         }
       }
     } else {
@@ -553,7 +557,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
       const R ApAq = ApR * Aq;
       for (int i = 0; i < nst; ++i)
         for (int j = 0; j < nsb; ++j)
-          store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * p + i,
+          store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * pp + i,
                      cscale(ApAq, acc[i * nsb + j]), C64);
     }
   }
@@ -961,6 +965,7 @@ struct NearParams {
   OpParams op;
   beast_qs_desc qs;
   int tk, bk;
+  const int* tperm;  // Zcell position -> test active cell
   const double* tgeo;
   const double* bgeo;
   const int* qcells;
@@ -992,7 +997,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
   const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
   if (e >= P.nnear) return;
   const NearPair np_ = P.near[e];
-  const Geo t = load_geo(P.tgeo + (int64_t)np_.p * GEO_STRIDE);
+  const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
   const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
   const int nt = P.tk == BEAST_P0 ? 1 : 3, nb = P.bk == BEAST_P0 ? 1 : 3;
   C2<double> acc[9];
@@ -1271,7 +1276,7 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs G, const int64_t* tpt
     trow[j] = 0;
     tc[j] = 0;
     if (j < ne) {
-      trow[j] = (int64_t)nst * tcell[e0 + j] + tshape[e0 + j];
+      trow[j] = (int64_t)nst * G.tpos[tcell[e0 + j]] + tshape[e0 + j];
       tc[j] = (A)tcoef[e0 + j];
     }
   }
@@ -1302,7 +1307,7 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs G, const int64_t* tpt
       } else {
         for (int64_t e = e0; e < e0 + ne; ++e) {
           const A ab = (A)tcoef[e] * b;
-          const int64_t idx = col + (int64_t)nst * tcell[e] + tshape[e];
+          const int64_t idx = col + (int64_t)nst * G.tpos[tcell[e]] + tshape[e];
           if (ZC64) {
             const float2 z = reinterpret_cast<const float2*>(G.zcell)[idx];
             re += ab * (A)z.x;
@@ -1552,6 +1557,7 @@ cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev&
   P.tgeo = a.ts->geo;
   P.tgeof = a.ts->geof;
   P.np = a.ts->ncells;
+  P.tperm = a.ts->tperm;
   P.bgeo = a.bs->geo;
   P.bgeof = a.bs->geof;
   P.qcells = a.qcells;
@@ -1608,6 +1614,7 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   P.qs = a.qs;
   P.tk = a.ts->kind;
   P.bk = a.bs->kind;
+  P.tperm = a.ts->tperm;
   P.tgeo = a.ts->geo;
   P.bgeo = a.bs->geo;
   P.qcells = a.qcells;

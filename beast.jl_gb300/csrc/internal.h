@@ -85,6 +85,9 @@ struct beast_space {
   std::vector<int64_t> h_fn_ptr;
   std::vector<int> h_fn_cell, h_fn_shape;
   std::vector<double> h_fn_coeff;
+  // Zcell row order of the test side: active cells sorted by their first function
+  int* tperm = nullptr;        // position -> active cell
+  int* tpos = nullptr;         // active cell -> position
   std::vector<int> h_ad_dof;   // host copy of the assembly data
   std::vector<double> h_ad_coeff;
 };
@@ -152,6 +155,7 @@ struct GatherArgs {
   int zcell_c64;
   int64_t ldc;
   const int* qlocal;      // device: trial active cell -> chunk-local index (-1 absent)
+  const int* tpos;        // device: test active cell -> Zcell position
   int64_t n0, n1;         // trial dof range of this chunk
   void* Z;
   int64_t ldz;
