@@ -981,14 +981,18 @@ struct NearParams {
 
 constexpr int NEAR_WARPS = 4;
 
-__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
-  // Gauss-Legendre nodes in shared memory (lanes read different nodes: a constant-memory
-  // read would serialise)
-  __shared__ double s_glx[210], s_glw[210];
+// Sauter-Schwab pairs of RT x RT Maxwell single / double layers on the mixed path: the 22
+// moments in FP32 (FP64 partial sums every 16 points), the 3 x 3 block from them in FP64.
+// A kernel of its own so that its register budget (and occupancy) is not set by the FP64
+// paths of k_near; k_near skips these pairs.
+DEV bool near_is_ss32(const NearParams& P, int cls) {
+  return P.ss32 && cls >= 1 && P.tk == BEAST_RT && P.bk == BEAST_RT &&
+         (P.op.kind == BEAST_MW_SL || (P.op.kind == BEAST_MW_DL && cls != 3));
+}
+
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss32(NearParams P) {
   __shared__ float s_glxf[210], s_glwf[210];
   for (int k = threadIdx.x; k < 210; k += blockDim.x) {
-    s_glx[k] = c_gl_x[k];
-    s_glw[k] = c_gl_w[k];
     s_glxf[k] = (float)c_gl_x[k];
     s_glwf[k] = (float)c_gl_w[k];
   }
@@ -997,15 +1001,10 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
   const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
   if (e >= P.nnear) return;
   const NearPair np_ = P.near[e];
+  if (!near_is_ss32(P, np_.cls)) return;
   const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
   const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
-  const int nt = P.tk == BEAST_P0 ? 1 : 3, nb = P.bk == BEAST_P0 ? 1 : 3;
-  C2<double> acc[9];
-  for (int k = 0; k < 9; ++k) acc[k] = C2<double>{0, 0};
-  Shp f, g;
-  bool dl_face = np_.cls == 3 && (P.op.kind == BEAST_MW_DL || P.op.kind == BEAST_HH_DL ||
-                                  P.op.kind == BEAST_HH_DLT);
-  if (np_.cls >= 1 && !dl_face) {
+  {
     // ---- Sauter-Schwab: shared vertices first, same order (SauterSchwabQuadrature.reorder)
     const double dtol = 1.0e3 * 2.220446049250313e-16;
     int pt[3], ps[3], hits = 0, ti[3], si[3];
@@ -1035,25 +1034,14 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
     const int n = np_.cls == 3 ? P.qs.ss_face : (np_.cls == 2 ? P.qs.ss_edge : P.qs.ss_vert);
     const int nreg = np_.cls == 1 ? 2 : 6;
     const int64_t items = (int64_t)nreg * n * n * n * n;
-    const double jac = 4.0 * t.area * s.area;
-    const double* glx = s_glx + c_gl_off[n - 1];
-    const double* glw = s_glw + c_gl_off[n - 1];
-    const bool mw_rt = P.tk == BEAST_RT && P.bk == BEAST_RT &&
-                       (P.op.kind == BEAST_MW_SL || P.op.kind == BEAST_MW_DL);
-    if (mw_rt) {
-      // moment form: with xi = x - c_p, eta = y - c_q and W = node weight x kernel,
-      //  single layer: z_ij = alpha (Mxe - s_j.Mx - t_i.Me + (t_i.s_j) M0) + 4 beta M0
-      //  double layer: z_ij = D0 - s_j.Dxr - t_i.Dre + (s_j x t_i).Dr
-      // (t_i = v_i - c_p, s_j = w_j - c_q; the shape normalisations cancel the Jacobian)
-      const bool sl = P.op.kind == BEAST_MW_SL;
-      const V3<double> cp = t.c, cq = s.c;
-      const double gi = P.op.gi, gr = P.op.gr;
-      // m[0..1] M0, m[2..3] M1 (SL) ; m[4..9] V1, m[10..15] V2, m[16..21] V3 as (re, im) per axis
-      double m[22];
+    const bool sl = P.op.kind == BEAST_MW_SL;
+    const V3<double> cp = t.c, cq = s.c;
+    const double gi = P.op.gi, gr = P.op.gr;
+    double m[22];
 #pragma unroll
-      for (int k = 0; k < 22; ++k) m[k] = 0.0;
-      const V3<double> d = cp - cq;
-      if (P.ss32) {
+    for (int k = 0; k < 22; ++k) m[k] = 0.0;
+    const V3<double> d = cp - cq;
+    {
         // FP32: x - y = X0 Et1 + X1 Et2 - Y0 Es1 - Y1 Es2 over the edge vectors of the two
         // charts from the shared first vertex (common terms folded into D = X - Y)
         // edge vectors as FP32 pairs hi + lo: the rounding of the geometry to FP32 would
@@ -1129,8 +1117,111 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
         }
 #pragma unroll
         for (int k = 0; k < 22; ++k) m[k] += (double)mf[k];
+          }
+#pragma unroll
+      for (int k = 0; k < 22; ++k) {
+        double v = m[k];
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        m[k] = v;
       }
-      for (int64_t it = P.ss32 ? items : (int64_t)lane; it < items; it += 32) {
+      const C2<double> M0{m[0], m[1]}, M1{m[2], m[3]};
+      CV<double> V1, V2, V3_;
+      V1.x = {m[4], m[5]}; V1.y = {m[6], m[7]}; V1.z = {m[8], m[9]};
+      V2.x = {m[10], m[11]}; V2.y = {m[12], m[13]}; V2.z = {m[14], m[15]};
+      V3_.x = {m[16], m[17]}; V3_.y = {m[18], m[19]}; V3_.z = {m[20], m[21]};
+      if (lane == 0) {
+        const C2<double> al{P.op.ar, P.op.ai}, be{P.op.br, P.op.bi};
+        for (int i = 0; i < 3; ++i) {
+          const V3<double> ti = t.v[i] - cp;
+          for (int j = 0; j < 3; ++j) {
+            const V3<double> sj = s.v[j] - cq;
+            C2<double> z;
+            if (sl) {
+              C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
+              fm = cadd(fm, cscale(dot(ti, sj), M0));
+              z = cadd(cmul(al, fm), cscale(4.0, cmul(be, M0)));
+            } else {
+              C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
+              z = cadd(fm, rdot(cross(sj, ti), V3_));
+            }
+            store_c<double>(P.zcell, (int64_t)(3 * np_.q + j) * P.ldc + 3 * (int64_t)np_.p + i, z, P.c64);
+          }
+        }
+      }
+  }
+}
+
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
+  // Gauss-Legendre nodes in shared memory (lanes read different nodes: a constant-memory
+  // read would serialise)
+  __shared__ double s_glx[210], s_glw[210];
+  for (int k = threadIdx.x; k < 210; k += blockDim.x) {
+    s_glx[k] = c_gl_x[k];
+    s_glw[k] = c_gl_w[k];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
+  if (e >= P.nnear) return;
+  const NearPair np_ = P.near[e];
+  if (near_is_ss32(P, np_.cls)) return;  // k_near_ss32
+  const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
+  const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
+  const int nt = P.tk == BEAST_P0 ? 1 : 3, nb = P.bk == BEAST_P0 ? 1 : 3;
+  C2<double> acc[9];
+  for (int k = 0; k < 9; ++k) acc[k] = C2<double>{0, 0};
+  Shp f, g;
+  bool dl_face = np_.cls == 3 && (P.op.kind == BEAST_MW_DL || P.op.kind == BEAST_HH_DL ||
+                                  P.op.kind == BEAST_HH_DLT);
+  if (np_.cls >= 1 && !dl_face) {
+    // ---- Sauter-Schwab: shared vertices first, same order (SauterSchwabQuadrature.reorder)
+    const double dtol = 1.0e3 * 2.220446049250313e-16;
+    int pt[3], ps[3], hits = 0, ti[3], si[3];
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        V3<double> dd = t.v[i] - s.v[j];
+        if (sqrt(dot(dd, dd)) < dtol && hits < 3) {
+          ti[hits] = i;
+          si[hits] = j;
+          ++hits;
+        }
+      }
+    int k = 0;
+    for (int h = 0; h < hits; ++h) pt[k++] = ti[h];
+    for (int i = 0; i < 3; ++i) {
+      bool used = false;
+      for (int h = 0; h < hits; ++h) used |= ti[h] == i;
+      if (!used) pt[k++] = i;
+    }
+    k = 0;
+    for (int h = 0; h < hits; ++h) ps[k++] = si[h];
+    for (int j = 0; j < 3; ++j) {
+      bool used = false;
+      for (int h = 0; h < hits; ++h) used |= si[h] == j;
+      if (!used) ps[k++] = j;
+    }
+    const int n = np_.cls == 3 ? P.qs.ss_face : (np_.cls == 2 ? P.qs.ss_edge : P.qs.ss_vert);
+    const int nreg = np_.cls == 1 ? 2 : 6;
+    const int64_t items = (int64_t)nreg * n * n * n * n;
+    const double jac = 4.0 * t.area * s.area;
+    const double* glx = s_glx + c_gl_off[n - 1];
+    const double* glw = s_glw + c_gl_off[n - 1];
+    const bool mw_rt = P.tk == BEAST_RT && P.bk == BEAST_RT &&
+                       (P.op.kind == BEAST_MW_SL || P.op.kind == BEAST_MW_DL);
+    if (mw_rt) {
+      // moment form: with xi = x - c_p, eta = y - c_q and W = node weight x kernel,
+      //  single layer: z_ij = alpha (Mxe - s_j.Mx - t_i.Me + (t_i.s_j) M0) + 4 beta M0
+      //  double layer: z_ij = D0 - s_j.Dxr - t_i.Dre + (s_j x t_i).Dr
+      // (t_i = v_i - c_p, s_j = w_j - c_q; the shape normalisations cancel the Jacobian)
+      const bool sl = P.op.kind == BEAST_MW_SL;
+      const V3<double> cp = t.c, cq = s.c;
+      const double gi = P.op.gi, gr = P.op.gr;
+      // m[0..1] M0, m[2..3] M1 (SL) ; m[4..9] V1, m[10..15] V2, m[16..21] V3 as (re, im) per axis
+      double m[22];
+#pragma unroll
+      for (int k = 0; k < 22; ++k) m[k] = 0.0;
+      const V3<double> d = cp - cq;
+      for (int64_t it = lane; it < items; it += 32) {
         double X[2], Y[2], w;
         ss_node(np_.cls, n, it, glx, glw, X, Y, &w);
         const double lt[3] = {1.0 - X[0], X[0] - X[1], X[1]}, ls[3] = {1.0 - Y[0], Y[0] - Y[1], Y[1]};
@@ -1628,6 +1719,7 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   P.ro = ro;
   P.ri = ri;
   unsigned blocks = (unsigned)((nnear + NEAR_WARPS - 1) / NEAR_WARPS);
+  if (P.ss32) k_near_ss32<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   k_near<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   return cudaGetLastError();
 }
