@@ -1057,6 +1057,58 @@ __global__ void k_gemv_partial_c64_df(int64_t n, const float2* A, int64_t lda, c
   part[2 * (s * n + i) + 1] = (double)shi + (double)sli;
 }
 
+// the same with two rows per thread: one 16-byte load brings a[i, j] and a[i+1, j] (even i,
+// even lda), and the two rows are independent accumulation chains
+__device__ __forceinline__ void cdf_acc(float ar, float ai, float4 xv, float& shr, float& slr, float& shi,
+                                        float& sli) {
+  float p, e;
+  p = __fmul_rn(ar, xv.x);
+  e = fmaf(ar, xv.x, -p);
+  two_sum_acc(shr, slr, p);
+  slr = __fadd_rn(slr, e);
+  p = __fmul_rn(-ai, xv.y);
+  e = fmaf(-ai, xv.y, -p);
+  two_sum_acc(shr, slr, p);
+  slr = __fadd_rn(slr, e);
+  slr = __fadd_rn(slr, __fsub_rn(__fmul_rn(ar, xv.z), __fmul_rn(ai, xv.w)));
+  p = __fmul_rn(ar, xv.y);
+  e = fmaf(ar, xv.y, -p);
+  two_sum_acc(shi, sli, p);
+  sli = __fadd_rn(sli, e);
+  p = __fmul_rn(ai, xv.x);
+  e = fmaf(ai, xv.x, -p);
+  two_sum_acc(shi, sli, p);
+  sli = __fadd_rn(sli, e);
+  sli = __fadd_rn(sli, __fadd_rn(__fmul_rn(ar, xv.w), __fmul_rn(ai, xv.z)));
+}
+__global__ void k_gemv_partial_c64_df2(int64_t n, const float2* A, int64_t lda, const float4* xs,
+                                       double* part) {
+  const int64_t i = 2 * (blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+  const int s = blockIdx.y;
+  const int64_t c0 = n * s / MV_SLABS, c1 = n * (s + 1) / MV_SLABS;
+  if (i >= n) return;
+  const bool two = i + 1 < n;
+  float h0r = 0.f, l0r = 0.f, h0i = 0.f, l0i = 0.f, h1r = 0.f, l1r = 0.f, h1i = 0.f, l1i = 0.f;
+  for (int64_t j = c0; j < c1; ++j) {
+    const float4 xv = xs[j];
+    float4 a;
+    if (two) {
+      a = *reinterpret_cast<const float4*>(A + i + j * lda);
+    } else {
+      const float2 a0 = A[i + j * lda];
+      a = make_float4(a0.x, a0.y, 0.f, 0.f);
+    }
+    cdf_acc(a.x, a.y, xv, h0r, l0r, h0i, l0i);
+    cdf_acc(a.z, a.w, xv, h1r, l1r, h1i, l1i);
+  }
+  part[2 * (s * n + i)] = (double)h0r + (double)l0r;
+  part[2 * (s * n + i) + 1] = (double)h0i + (double)l0i;
+  if (two) {
+    part[2 * (s * n + i + 1)] = (double)h1r + (double)l1r;
+    part[2 * (s * n + i + 1) + 1] = (double)h1i + (double)l1i;
+  }
+}
+
 __global__ void k_gemv_reduce(int64_t n, const double* part, double* y, double alpha, double beta) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (i >= n) return;
@@ -1468,7 +1520,12 @@ cudaError_t gemv_dev(int64_t n, const void* A, int64_t lda, int a_c64, const dou
   if (a_c64) {
     float4* xs = reinterpret_cast<float4*>(g_part + (size_t)MV_SLABS * n * 2);
     k_split_x<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x, xs);
-    k_gemv_partial_c64_df<<<g, 128, 0, st>>>(n, (const float2*)A, lda, xs, g_part);
+    if (lda % 2 == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0) {
+      dim3 g2((unsigned)((n + 255) / 256), MV_SLABS);
+      k_gemv_partial_c64_df2<<<g2, 128, 0, st>>>(n, (const float2*)A, lda, xs, g_part);
+    } else {
+      k_gemv_partial_c64_df<<<g, 128, 0, st>>>(n, (const float2*)A, lda, xs, g_part);
+    }
   } else
     k_gemv_partial<double2><<<g, 128, 0, st>>>(n, (const double2*)A, lda, x, g_part);
   k_gemv_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, g_part, y, alpha, beta);
