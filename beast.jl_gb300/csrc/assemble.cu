@@ -16,6 +16,7 @@
 //             gather: every output entry written once, no atomics, deterministic.
 #include <cuda_runtime.h>
 
+#include <mutex>
 #include <type_traits>
 
 #include <cmath>
@@ -1678,6 +1679,8 @@ cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev&
 
 static cudaError_t upload_gl(cudaStream_t st) {
   static bool done[64] = {false};
+  static std::mutex mtx;
+  std::lock_guard<std::mutex> lk(mtx);
   int dev = 0;
   cudaGetDevice(&dev);
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;

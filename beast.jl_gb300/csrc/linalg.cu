@@ -1500,36 +1500,30 @@ int lu_solve_dev(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int dtyp
                                      (const double2*)lu_dinv(ipiv, n));
 }
 
-static double* g_part = nullptr;
-static size_t g_part_size = 0;
-
+// scratch per call from the device's stream-ordered pool (cheap once the pool holds memory;
+// nothing shared between contexts, streams or devices)
 cudaError_t gemv_dev(int64_t n, const void* A, int64_t lda, int a_c64, const double* x, double* y,
                      double alpha, double beta, cudaStream_t st) {
-  size_t need = (size_t)MV_SLABS * n * 2 * sizeof(double) + (size_t)n * sizeof(float4) + 256;
-  if (need > g_part_size) {
-    if (g_part) cudaFree(g_part);
-    cudaError_t e = cudaMalloc(&g_part, need);
-    if (e != cudaSuccess) {
-      g_part = nullptr;
-      g_part_size = 0;
-      return e;
-    }
-    g_part_size = need;
-  }
+  const size_t need = (size_t)MV_SLABS * n * 2 * sizeof(double) + (size_t)n * sizeof(float4) + 256;
+  double* part = nullptr;
+  cudaError_t e = cudaMallocAsync(&part, need, st);
+  if (e != cudaSuccess) return e;
   dim3 g((unsigned)((n + 127) / 128), MV_SLABS);
   if (a_c64) {
-    float4* xs = reinterpret_cast<float4*>(g_part + (size_t)MV_SLABS * n * 2);
+    float4* xs = reinterpret_cast<float4*>(part + (size_t)MV_SLABS * n * 2);
     k_split_x<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x, xs);
     if (lda % 2 == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0) {
       dim3 g2((unsigned)((n + 255) / 256), MV_SLABS);
-      k_gemv_partial_c64_df2<<<g2, 128, 0, st>>>(n, (const float2*)A, lda, xs, g_part);
+      k_gemv_partial_c64_df2<<<g2, 128, 0, st>>>(n, (const float2*)A, lda, xs, part);
     } else {
-      k_gemv_partial_c64_df<<<g, 128, 0, st>>>(n, (const float2*)A, lda, xs, g_part);
+      k_gemv_partial_c64_df<<<g, 128, 0, st>>>(n, (const float2*)A, lda, xs, part);
     }
   } else
-    k_gemv_partial<double2><<<g, 128, 0, st>>>(n, (const double2*)A, lda, x, g_part);
-  k_gemv_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, g_part, y, alpha, beta);
-  return cudaGetLastError();
+    k_gemv_partial<double2><<<g, 128, 0, st>>>(n, (const double2*)A, lda, x, part);
+  k_gemv_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, part, y, alpha, beta);
+  e = cudaGetLastError();
+  cudaFreeAsync(part, st);
+  return e;
 }
 
 cudaError_t convert_c128_to_c64(int64_t rows, int64_t cols, const double* src, int64_t lds, float* dst,
@@ -1551,15 +1545,15 @@ cudaError_t vec_axpy(int64_t n, double ar, double ai, const double* x, double* y
 cudaError_t vec_copy(int64_t n, const double* x, double* y, cudaStream_t st) {
   return cudaMemcpyAsync(y, x, (size_t)n * 2 * sizeof(double), cudaMemcpyDeviceToDevice, st);
 }
-static double* g_npart = nullptr;
 cudaError_t vec_norm2(int64_t n, const double* x, double* out, cudaStream_t st) {
-  if (!g_npart) {
-    cudaError_t e = cudaMalloc(&g_npart, 256 * sizeof(double));
-    if (e != cudaSuccess) return e;
-  }
-  k_norm2_part<<<256, 256, 0, st>>>(n, x, g_npart);
-  k_sum_part<<<1, 256, 0, st>>>(256, g_npart, out);
-  return cudaGetLastError();
+  double* npart = nullptr;
+  cudaError_t e = cudaMallocAsync(&npart, 256 * sizeof(double), st);
+  if (e != cudaSuccess) return e;
+  k_norm2_part<<<256, 256, 0, st>>>(n, x, npart);
+  k_sum_part<<<1, 256, 0, st>>>(256, npart, out);
+  e = cudaGetLastError();
+  cudaFreeAsync(npart, st);
+  return e;
 }
 cudaError_t vec_dots(int64_t n, int m, const double* V, int64_t ldv, const double* w, double* h,
                      cudaStream_t st) {
