@@ -1359,6 +1359,28 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs G, const int64_t* tpt
                                                 const double* bcoef, int nst, int nsb, int64_t nrows) {
   typedef typename std::conditional<ZC64 && OC64, float, double>::type A;
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nb0 = G.n0 + (int64_t)blockIdx.y * GATHER_NCOL;
+  const int64_t nb1 = nb0 + GATHER_NCOL < G.n1 ? nb0 + GATHER_NCOL : G.n1;
+  // the CTA's trial functions with at most two entries: Zcell column offsets and coefficients
+  // staged once in shared memory (s_cnt = -1: more entries, taken by the general loop)
+  __shared__ int64_t s_col[GATHER_NCOL][2];
+  __shared__ float s_b[GATHER_NCOL][2];
+  __shared__ int s_cnt[GATHER_NCOL];
+  if (ZC64 && OC64 && threadIdx.x < GATHER_NCOL) {
+    const int64_t n = nb0 + threadIdx.x;
+    int cnt = 0;
+    if (n < nb1) {
+      const int64_t f0 = bptr[n];
+      const int c = (int)(bptr[n + 1] - f0);
+      cnt = c <= 2 ? c : -1;
+      for (int k = 0; k < 2 && k < c; ++k) {
+        s_col[threadIdx.x][k] = ((int64_t)nsb * G.qlocal[bcell[f0 + k]] + bshape[f0 + k]) * G.ldc;
+        s_b[threadIdx.x][k] = (float)bcoef[f0 + k];
+      }
+    }
+    s_cnt[threadIdx.x] = cnt;
+  }
+  if (ZC64 && OC64) __syncthreads();
   if (m >= nrows) return;
   const int64_t e0 = tptr[m], ne = tptr[m + 1] - e0;
   int64_t trow[GATHER_MAXE];
@@ -1372,9 +1394,56 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs G, const int64_t* tpt
       tc[j] = (A)tcoef[e0 + j];
     }
   }
-  const int64_t nb0 = G.n0 + (int64_t)blockIdx.y * GATHER_NCOL;
-  const int64_t nb1 = nb0 + GATHER_NCOL < G.n1 ? nb0 + GATHER_NCOL : G.n1;
-  for (int64_t n = nb0; n < nb1; ++n) {
+  int64_t nstart = nb0;
+  if (ZC64 && OC64 && ne <= 2) {
+    // fast path: the Zcell values of 8 trial functions (<= 2 x 2 each) are requested before
+    // any is used
+    bool all2 = true;
+    for (int nn = 0; nn < nb1 - nb0; ++nn) all2 &= s_cnt[nn] >= 0;
+    if (all2) {
+      const float2* zc = reinterpret_cast<const float2*>(G.zcell);
+      for (int g0 = 0; g0 < (int)(nb1 - nb0); g0 += 8) {
+        float2 z[8][2][2];
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+#pragma unroll
+          for (int k = 0; k < 2; ++k)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+              const int nn = g0 + u;
+              const bool ok = nn < nb1 - nb0 && k < s_cnt[nn] && j < ne;
+              z[u][k][j] = ok ? zc[s_col[nn][k] + trow[j]] : make_float2(0.f, 0.f);
+            }
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int nn = g0 + u;
+          if (nn >= nb1 - nb0) break;
+          float re = 0.f, im = 0.f;
+#pragma unroll
+          for (int k = 0; k < 2; ++k)
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+              if (k < s_cnt[nn] && j < ne) {
+                const float ab = (float)tc[j] * s_b[nn][k];
+                re += ab * z[u][k][j].x;
+                im += ab * z[u][k][j].y;
+              }
+          const float cr = (float)G.cr, ci = (float)G.ci;
+          float vr = cr * re - ci * im, vi = cr * im + ci * re;
+          float2* Z = reinterpret_cast<float2*>(G.Z);
+          const int64_t o = (G.row_off + m) + (G.col_off + nb0 + nn) * G.ldz;
+          if (G.accumulate) {
+            const float2 old = Z[o];
+            vr += old.x;
+            vi += old.y;
+          }
+          Z[o] = make_float2(vr, vi);
+        }
+      }
+      nstart = nb1;
+    }
+  }
+  for (int64_t n = nstart; n < nb1; ++n) {
     A re = 0, im = 0;
     for (int64_t f = bptr[n]; f < bptr[n + 1]; ++f) {
       const int ql = G.qlocal[bcell[f]];
