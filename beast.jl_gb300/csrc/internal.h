@@ -205,3 +205,19 @@ cudaError_t vec_dots(int64_t n, int m, const double* V, int64_t ldv, const doubl
 // w -= V h (m columns)
 cudaError_t vec_gemv_sub(int64_t n, int m, const double* V, int64_t ldv, const double* h,
                          double* w, cudaStream_t st);
+
+// ---- FP16 operands of the tensor-core LU update (tc_gemm.cu)
+// work layout of an M x K by K x N update: A' (2M rows of K half2), B' (N columns of K half2),
+// the row scales 1/s (M floats), the column scales 1/t (N floats)
+void tc_gemm_operands(void* work, int64_t M, int64_t N, int K, void** Ap, float** inv_sa, void** Bp,
+                      float** inv_sb);
+#ifdef __CUDACC__
+// power-of-two scale 2^sh that brings a largest magnitude mx into [2^13, 2^14) (sh = 0 for
+// mx = 0): the FP16 operands then never clip and keep 11 significant bits
+__device__ __forceinline__ int tc_scale_shift(float mx) {
+  if (!(mx > 0.f)) return 0;
+  int e;
+  frexpf(mx, &e);  // mx = f 2^e, f in [0.5, 1)
+  return max(-120, min(120, 14 - e));
+}
+#endif

@@ -9,8 +9,11 @@
 //   k_laswp    the panel's row interchanges applied to the other columns
 //   k_trsm_tile   U12 = L11^{-1} A12 and (unpivoted path, after k_getrf64 on the diagonal
 //                 block) L21 = A21 U11^{-1}
+//   k_lu_inv64 + k_panel_apply   the unpivoted c64 panel: diagonal block LU with the
+//                 inverses of its triangles, then both triangular solves as products
 //   k_gemm     A22 -= L21 U12 (complex, tiled through shared memory)
 // The element type is complex FP64 (c128) or complex FP32 (c64).
+#include <cuda_fp16.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -36,7 +39,8 @@ void* lu_dinv(const int* ipiv, int64_t n) {
 bool tc_gemm_supported(const void* A, int64_t lda, int K);
 size_t tc_gemm_work_bytes(int64_t M, int64_t N, int K);
 int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t colB,
-                int64_t M0, int64_t N0, int64_t M1, int64_t N1, int K, void* work, size_t work_bytes);
+                int64_t M0, int64_t N0, int64_t M1, int64_t N1, int K, void* work, size_t work_bytes,
+                bool prepped);
 
 namespace {
 
@@ -304,6 +308,13 @@ __device__ __forceinline__ void cfms(T& acc, T a, T b) {  // acc -= a b, four fu
   acc.y = fma(-a.y, b.x, acc.y);
 }
 template <typename T>
+__device__ __forceinline__ void cfma(T& acc, T a, T b) {  // acc += a b
+  acc.x = fma(a.x, b.x, acc.x);
+  acc.x = fma(-a.y, b.y, acc.x);
+  acc.y = fma(a.x, b.y, acc.y);
+  acc.y = fma(a.y, b.x, acc.y);
+}
+template <typename T>
 __device__ __forceinline__ T cmulx(T a, T b) {
   T r;
   r.x = a.x * b.x - a.y * b.y;
@@ -441,6 +452,163 @@ __global__ void __launch_bounds__(256) k_getrf64(T* A, int64_t lda, int64_t j0, 
   for (int e = tid; e < kb * kb; e += 256) {
     const int r = e % kb, k = e / kb;
     A[(j0 + r) + (j0 + k) * lda] = D[r * LD + k];
+  }
+}
+
+// ---- diagonal block LU together with the inverses of its triangles ---------------------
+// For the unpivoted c64 path: the 64 x 64 block at (j0, j0) (kb x kb, the rest padded with
+// the identity) is factored by forward elimination on [A | I] -- eliminating below the pivot
+// turns the identity part of the rows into L^{-1} (it lives in the strictly lower positions
+// the elimination has just emptied), while the upper part becomes U -- and in the same pass
+// X = (U^T)^{-1} = (U^{-1})^T is built by forward elimination on U^T, whose multipliers
+// U[k][r] are the pivot row itself.  Step k (rows r > k), with d = 1 / U[k][k]:
+//   S1[r][c] -= (A[r][k] d) P1[c]   (P1 = row k of S1 with 0 at column k)
+//   S1[r][k]  = -A[r][k] d          (L^{-1}[r][k] after this step; L[r][k] = A[r][k] d)
+//   S2[r][c] -= (U[k][r] d) P2[c]   (P2 = row k of S2, before its own scaling)
+//   S2[k][c] *= d
+// Each thread holds a 4 x 4 tile of S1 and of S2 in registers (rows 4 rb.., columns 4 cb..;
+// a warp = 2 row blocks x 16 column blocks).  After each step the owners of row k+1, of
+// column k+1 and of the pivot publish P1, P2, the column and 1 / pivot in shared memory
+// (double-buffered by step parity): one block barrier per step.  The step loop is unrolled
+// by 4, so the tile slot of row / column k is known at compile time and the code is short
+// (this kernel runs alone on one SM between wide launches: it is latency-bound and starts
+// with cold instruction caches).  Output: the factors in A, Linv and Uinv (column-major
+// 64 x 64, identity beyond kb) in inv.  A zero pivot sets *info (1-based column) and the
+// kernel stops.
+template <typename T>
+__device__ __forceinline__ int pidx(int c) {  // conflict-free index of the published rows
+  return c + (c >> 2);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0, int kb, int* info, T* inv) {
+  constexpr int LD = TRI + 1, PL = TRI + TRI / 4;
+  extern __shared__ unsigned char smraw[];
+  T* Ls = reinterpret_cast<T*>(smraw);  // 64 x LD: staging, then the L factor, then Linv
+  __shared__ T p1[2][PL], p2[2][PL], lc[2][TRI];
+  __shared__ T dv[2];
+  __shared__ int s_zero[2];  // 1-based column of a zero pivot, by step parity
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int cb = lane & 15, rb = 2 * warp + (lane >> 4);
+  const int r0 = 4 * rb, c0 = 4 * cb;
+  const T zero = cmk<T>(0.0, 0.0), one = cmk<T>(1.0, 0.0);
+  // coalesced load through shared memory (identity padding beyond kb)
+  for (int e = tid; e < TRI * TRI; e += 256) {
+    const int r = e & (TRI - 1), c = e >> 6;
+    Ls[r * LD + c] = (r < kb && c < kb) ? A[(j0 + r) + (j0 + c) * lda] : (r == c ? one : zero);
+  }
+  if (tid < 2) s_zero[tid] = 0;
+  __syncthreads();
+  T s1[4][4], s2[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      s1[i][j] = Ls[(r0 + i) * LD + c0 + j];
+      s2[i][j] = (r0 + i == c0 + j) ? one : zero;
+    }
+  // publish row 0, column 0 and the first pivot's reciprocal
+  if (rb == 0)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      p1[0][pidx<T>(c0 + j)] = (c0 + j == 0) ? zero : s1[0][j];
+      p2[0][pidx<T>(c0 + j)] = s2[0][j];
+    }
+  if (cb == 0)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) lc[0][r0 + i] = s1[i][0];
+  if (rb == 0 && cb == 0) {
+    T d;
+    if (!crecip(s1[0][0], d)) s_zero[0] = 1;
+    dv[0] = d;
+  }
+  __syncthreads();  // the staging buffer is free from here on (L factor)
+  for (int kq = 0; kq < TRI / 4; ++kq) {
+#pragma unroll
+    for (int kk = 0; kk < 4; ++kk) {
+      const int k = 4 * kq + kk, b = kk & 1;
+      if (s_zero[b]) {  // uniform
+        if (tid == 0) atomicCAS(info, 0, (int)(j0 + s_zero[b]));
+        return;
+      }
+      const T d = dv[b];
+      if (r0 + 3 > k) {  // some row of the tile is below the pivot
+        T l1[4], l2[4], q1[4], q2[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          l1[i] = cmulx(lc[b][r0 + i], d);
+          l2[i] = cmulx(p1[b][pidx<T>(r0 + i)], d);
+        }
+#pragma unroll
+        for (int j = 0; j < 4; ++j) {
+          q1[j] = p1[b][pidx<T>(c0 + j)];
+          q2[j] = p2[b][pidx<T>(c0 + j)];
+        }
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+          if (r0 + i > k) {
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              cfms(s1[i][j], l1[i], q1[j]);
+              cfms(s2[i][j], l2[i], q2[j]);
+            }
+            if (cb == kq) {  // column k: L^{-1}[r][k] = -l, and the L factor
+              s1[i][kk].x = -l1[i].x;
+              s1[i][kk].y = -l1[i].y;
+              Ls[(r0 + i) * LD + k] = l1[i];
+            }
+          }
+      }
+      if (rb == kq)  // row k of X is final
+#pragma unroll
+        for (int j = 0; j < 4; ++j) s2[kk][j] = cmulx(s2[kk][j], d);
+      // publish step k + 1
+      if (k + 1 < TRI) {
+        const int kn = k + 1, bn = b ^ 1, qn = kn >> 2, in = kn & 3;
+        if (rb == qn)
+#pragma unroll
+          for (int j = 0; j < 4; ++j) {
+            p1[bn][pidx<T>(c0 + j)] = (c0 + j == kn) ? zero : s1[in][j];
+            p2[bn][pidx<T>(c0 + j)] = s2[in][j];
+          }
+        if (cb == qn)
+#pragma unroll
+          for (int i = 0; i < 4; ++i) lc[bn][r0 + i] = s1[i][in];
+        if (rb == qn && cb == qn) {
+          T dn;
+          if (!crecip(s1[in][in], dn)) s_zero[bn] = kn + 1;
+          dv[bn] = dn;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  // U (upper part of S1) joins the L factor in Ls; the factored block goes back to A
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+      if (c0 + j >= r0 + i) Ls[(r0 + i) * LD + c0 + j] = s1[i][j];
+  __syncthreads();
+  for (int e = tid; e < kb * kb; e += 256) {
+    const int r = e % kb, c = e / kb;
+    A[(j0 + r) + (j0 + c) * lda] = Ls[r * LD + c];
+  }
+  __syncthreads();
+  // Linv (column-major, inv[c * 64 + r] = Linv[r][c]) through Ls; Uinv = X^T, so row r of X
+  // is column r of Uinv (inv[4096 + r * 64 + c] = X[r][c]), written by the tile owners
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int r = r0 + i, c = c0 + j;
+      Ls[r * LD + c] = c < r ? s1[i][j] : (c == r ? one : zero);
+      inv[TRI * TRI + r * TRI + c] = s2[i][j];
+    }
+  __syncthreads();
+  for (int e = tid; e < TRI * TRI; e += 256) {
+    const int r = e & (TRI - 1), c = e >> 6;
+    inv[e] = Ls[r * LD + c];
   }
 }
 
@@ -585,6 +753,204 @@ __global__ void __launch_bounds__(TrsmTile<T>::NT) k_trsm_tile(T* A, int64_t lda
     } else {
       const int k = e % TRI, s2 = e / TRI;
       if (k < kb && sb + s2 < s1) A[(j0 + k) + (sb + s2) * lda] = X[k * LDX + s2];
+    }
+  }
+}
+
+// ---- unpivoted c64 panel: both triangular solves as products with the inverses ----------
+// After k_lu_inv64 (kb = 64, inverses in inv: Linv then Uinv, column-major 64 x 64), with
+// s0 = j0 + 64:
+//   CTA b <  nR:  L21 rows s0 + 64 b .. +63:          X = A21 Uinv  (a system per row)
+//   CTA b >= nR:  U12 columns s0 + 64 (b - nR) .. +63: X = Linv A12  (a system per column)
+// Both are C[x][y] = sum_k W[k][s] N[k][v] over 64 x 64 x 64: s runs over the 64 systems
+// (W: A21 / A12), v over the inverse's free index (N: Uinv / Linv), and N[k][v] = 0 for
+// k > v (the triangle).  A complex multiply-add is two packed FP32 FMAs,
+//   acc += (a.x, a.x) (b.x, b.y) + (-a.y, a.y) (b.y, b.x),
+// so W is staged as float4 (a.x, a.x, -a.y, a.y) and N as float4 (b.x, b.y, b.y, b.x): one
+// 16-byte load per operand and no register shuffling.  K is staged in two halves of 32.
+// A thread owns 4 systems (lanes 0..15 of a half-warp at stride 16) times 4 free indices,
+// dealt out so that every warp does the same work: warp w takes 4w .. 4w+3 and
+// 60-4w .. 63-4w (half-warp h the pairs at +2h), all four up to k = 4w+4, the upper two up
+// to 64-4w -- 544 complex multiply-adds per thread in every warp.  The result is staged
+// system-major in shared memory, stored coalesced and, when the tensor-core update follows
+// (Ap / Bp not null), written once more as its FP16 operands with 16-byte stores: L21 rows
+// expanded and row-scaled as A', U12 columns scaled as B' (layout and scale rule of the
+// update's own operand preparation).
+constexpr int PA_KH = 32;   // k per staged half
+constexpr int PA_LD4 = 65;  // staged operand rows: 64 float4 + 1
+constexpr int PA_CLD = 65;  // staged result columns
+size_t panel_apply_smem() { return (size_t)2 * PA_KH * PA_LD4 * sizeof(float4) + 4 * 64 * sizeof(float); }
+
+__device__ __forceinline__ void cmac2(float2& acc, float4 a, float4 b) {
+  acc = __ffma2_rn(make_float2(a.x, a.y), make_float2(b.x, b.y), acc);
+  acc = __ffma2_rn(make_float2(a.z, a.w), make_float2(b.z, b.w), acc);
+}
+
+__global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, int64_t j0, int64_t n,
+                                                        const float2* __restrict__ inv, int nR, __half2* Ap,
+                                                        float* inv_sa, __half2* Bp, float* inv_sb) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float4* Ws = reinterpret_cast<float4*>(smraw);  // W[k][s], k of the current half
+  float4* Ns = Ws + PA_KH * PA_LD4;               // N[k][v]
+  float* red = reinterpret_cast<float*>(Ns + PA_KH * PA_LD4);  // 4 x 64 partial maxima
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const bool right = (int)blockIdx.x < nR;
+  const int64_t s0 = j0 + TRI;
+  const int64_t b0 = s0 + (int64_t)(right ? (int)blockIdx.x : (int)blockIdx.x - nR) * 64;  // first system
+  const float2 zero = make_float2(0.f, 0.f);
+  const int sl = lane & 15, h = lane >> 4;
+  const int vlo = 4 * warp + 2 * h, vhi = 60 - 4 * warp + 2 * h;  // free indices vlo, vlo+1, vhi, vhi+1
+  const int k1 = 4 * warp + 4, k2 = 64 - 4 * warp;
+  float2 acc[4][4];  // [system u][free index: vlo, vlo+1, vhi, vhi+1]
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[u][j] = zero;
+
+  for (int kh = 0; kh < 2; ++kh) {
+    const int kb0 = kh * PA_KH;
+    if (kh) __syncthreads();  // the first half is consumed
+    {
+      // 8 + 8 elements per thread, e = tid + 256 t; coalesced along the contiguous index:
+      //   right W: s = e & 63, k = e >> 6 (A21 column k)   N: k = e & 31, v = e >> 5 (Uinv column v)
+      //   left  W: k = e & 31, s = e >> 5 (A12 column s)   N: v = e & 63, k = e >> 6 (Linv column k)
+      float2 w[8], v[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int e = tid + 256 * t;
+        if (right) {
+          const int s = e & 63, k = e >> 6;
+          w[t] = b0 + s < n ? A[(b0 + s) + (j0 + kb0 + k) * lda] : zero;
+          v[t] = inv[4096 + (e >> 5) * 64 + kb0 + (e & 31)];
+        } else {
+          const int k = e & 31, s = e >> 5;
+          w[t] = b0 + s < n ? A[(j0 + kb0 + k) + (b0 + s) * lda] : zero;
+          v[t] = inv[(kb0 + (e >> 6)) * 64 + (e & 63)];
+        }
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int e = tid + 256 * t;
+        const float4 wv = make_float4(w[t].x, w[t].x, -w[t].y, w[t].y);
+        const float4 nv = make_float4(v[t].x, v[t].y, v[t].y, v[t].x);
+        if (right) {
+          Ws[(e >> 6) * PA_LD4 + (e & 63)] = wv;
+          Ns[(e & 31) * PA_LD4 + (e >> 5)] = nv;
+        } else {
+          Ws[(e & 31) * PA_LD4 + (e >> 5)] = wv;
+          Ns[(e >> 6) * PA_LD4 + (e & 63)] = nv;
+        }
+      }
+    }
+    __syncthreads();
+    // all four free indices for k < k1 (inside the first half), the upper two for k < k2
+    const int e1 = kh == 0 ? k1 : kb0, e2 = min(k2, kb0 + PA_KH);
+#pragma unroll 2
+    for (int k = kb0; k < e1; ++k) {
+      const float4* wr = Ws + (k - kb0) * PA_LD4 + sl;
+      const float4* nr = Ns + (k - kb0) * PA_LD4;
+      const float4 n0 = nr[vlo], n1 = nr[vlo + 1], n2 = nr[vhi], n3 = nr[vhi + 1];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float4 a = wr[16 * u];
+        cmac2(acc[u][0], a, n0);
+        cmac2(acc[u][1], a, n1);
+        cmac2(acc[u][2], a, n2);
+        cmac2(acc[u][3], a, n3);
+      }
+    }
+#pragma unroll 2
+    for (int k = e1; k < e2; ++k) {
+      const float4* wr = Ws + (k - kb0) * PA_LD4 + sl;
+      const float4* nr = Ns + (k - kb0) * PA_LD4;
+      const float4 n2 = nr[vhi], n3 = nr[vhi + 1];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const float4 a = wr[16 * u];
+        cmac2(acc[u][2], a, n2);
+        cmac2(acc[u][3], a, n3);
+      }
+    }
+  }
+  __syncthreads();  // every warp is done with Ws / Ns
+  // stage C system-major, Cs[s][v] (s: system, v: free index)
+  float2* Cs = reinterpret_cast<float2*>(smraw);
+  __shared__ float s_scale[64];
+  const int vv[4] = {vlo, vlo + 1, vhi, vhi + 1};
+#pragma unroll
+  for (int u = 0; u < 4; ++u)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) Cs[(sl + 16 * u) * PA_CLD + vv[j]] = acc[u][j];
+  __syncthreads();
+  // the solved systems, coalesced: right -- A[b0 + s, j0 + v] (along s); left -- A[j0 + v,
+  // b0 + s] (along v)
+#pragma unroll 4
+  for (int t = 0; t < 16; ++t) {
+    const int e = tid + 256 * t;
+    if (right) {
+      const int sy = e & 63, v = e >> 6;
+      if (b0 + sy < n) A[(b0 + sy) + (j0 + v) * lda] = Cs[sy * PA_CLD + v];
+    } else {
+      const int v = e & 63, sy = e >> 6;
+      if (b0 + sy < n) A[(j0 + v) + (b0 + sy) * lda] = Cs[sy * PA_CLD + v];
+    }
+  }
+  // FP16 operands of the update: right -- the A' row pair of each system (2 x 64 half2);
+  // left -- the B' column of each system (64 half2).  Scale: 2^sh from the system's largest
+  // |re|, |im| (partial maxima over quarters of v, then one per system).
+  __half2* const dst = right ? Ap : Bp;
+  if (dst == nullptr) return;  // uniform over the CTA
+  {
+    const int sy = tid & 63, q = tid >> 6;
+    float mx = 0.f;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const float2 a = Cs[sy * PA_CLD + 16 * q + i];
+      mx = fmaxf(mx, fmaxf(fabsf(a.x), fabsf(a.y)));
+    }
+    red[q * 64 + sy] = mx;
+    __syncthreads();
+    if (q == 0) {
+      mx = fmaxf(fmaxf(red[sy], red[64 + sy]), fmaxf(red[128 + sy], red[192 + sy]));
+      const int sh = tc_scale_shift(mx);
+      s_scale[sy] = ldexpf(1.f, sh);
+      if (b0 + sy < n) (right ? inv_sa : inv_sb)[b0 + sy - s0] = ldexpf(1.f, -sh);
+    }
+    __syncthreads();
+  }
+  // 16-byte stores: a lane converts 4 consecutive v of one system; right -- one system per
+  // warp pass (lanes 0..15 row 2m, 16..31 row 2m+1: 512 contiguous bytes), left -- two
+  // systems per pass (256 bytes each)
+  const int v0 = 4 * (lane & 15);
+  if (right) {
+    for (int sy = warp; sy < 64; sy += 8) {
+      if (b0 + sy >= n) break;
+      const float sc = s_scale[sy];
+      const float2* cr = Cs + sy * PA_CLD + v0;
+      __half2 hv[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float2 a = cr[i];
+        hv[i] = (lane < 16) ? __floats2half2_rn(a.x * sc, -a.y * sc) : __floats2half2_rn(a.y * sc, a.x * sc);
+      }
+      const int64_t m = b0 + sy - s0;
+      *reinterpret_cast<uint4*>(Ap + (2 * m + (lane >> 4)) * TRI + v0) = *reinterpret_cast<const uint4*>(hv);
+    }
+  } else {
+    for (int sp = 2 * warp; sp < 64; sp += 16) {
+      const int sy = sp + (lane >> 4);
+      if (b0 + sy < n) {
+        const float sc = s_scale[sy];
+        const float2* cr = Cs + sy * PA_CLD + v0;
+        __half2 hv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float2 a = cr[i];
+          hv[i] = __floats2half2_rn(a.x * sc, a.y * sc);
+        }
+        const int64_t m = b0 + sy - s0;
+        *reinterpret_cast<uint4*>(Bp + m * TRI + v0) = *reinterpret_cast<const uint4*>(hv);
+      }
     }
   }
 }
@@ -1250,15 +1616,22 @@ struct LUSteps {
   }
   // the same on an L-shaped region: rows [r0, r0+m0) of columns [c0, c0+n0), then rows
   // [r0, r0+m1) (m1 <= m0) of the next n1 columns -- one tensor-core launch for both
+  // whether gemm2 with these sizes runs (and on the tensor cores)
+  static bool gemm2_runs(int64_t m0, int64_t n0, int64_t m1, int64_t n1, int k) {
+    return m0 > 0 && k > 0 && (n0 > 0 || (m1 > 0 && n1 > 0));
+  }
+  bool gemm2_tc(int64_t m0, int64_t n0, int64_t n1, int k, const void* tcwork) const {
+    return sizeof(T) == 8 && tcwork && m0 >= 64 && n0 + n1 >= 64 && k % 32 == 0;
+  }
+  // prepped: the FP16 operands are already in tcwork (k_panel_apply wrote them)
   int gemm2(int64_t r0, int64_t m0, int64_t c0, int64_t n0, int64_t m1, int64_t n1, int64_t k0, int k,
-            void* tcwork) {
-    if (m0 <= 0 || k <= 0) return BEAST_OK;
-    if (n0 <= 0 && (m1 <= 0 || n1 <= 0)) return BEAST_OK;
-    const bool tc = sizeof(T) == 8 && tcwork && m0 >= 64 && n0 + n1 >= 64 && k % 32 == 0;
+            void* tcwork, bool prepped = false) {
+    if (!gemm2_runs(m0, n0, m1, n1, k)) return BEAST_OK;
+    const bool tc = gemm2_tc(m0, n0, n1, k, tcwork);
     ProfScope ps(ctx, tc ? PK_TCGEMM : PK_GEMM, 8.0 * (double)k * ((double)m0 * n0 + (double)m1 * n1));
     if (tc)
       return tc_gemm_sub(ctx, reinterpret_cast<float2*>(A), lda, r0, k0, c0, m0, n0, m1, n1, k, tcwork,
-                         tcwork_bytes);
+                         tcwork_bytes, prepped);
     const int64_t ms[2] = {m0, m1}, cs[2] = {c0, c0 + n0}, ns[2] = {n0, n1};
     for (int r = 0; r < 2; ++r) {
       if (ms[r] <= 0 || ns[r] <= 0) continue;
@@ -1289,8 +1662,15 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   const int NB = 16 * nb;
   const size_t panel_smem = (size_t)(rows0 * (nb + 1) + nb) * sizeof(T);
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
-  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_getrf64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                           (int)((size_t)TRI * (TRI + 1) * sizeof(T))));
+  // unpivoted c64 with 64-wide panels: k_lu_inv64 also inverts the block's triangles and
+  // k_panel_apply does both triangular solves (and the FP16 operands of the in-block update)
+  const bool apply_path = !pivot && sizeof(T) == 8 && nb == TRI;
+  const size_t getrf_sm = (size_t)TRI * (TRI + 1) * sizeof(T);
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_getrf64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
+  if (apply_path)
+    BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)panel_apply_smem()));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_tile<T, R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)trsm_tile_smem<T>()));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_tile<T, R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1345,27 +1725,47 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
         // interchanges inside the column block
         if ((rc = S.laswp(J0, j0, j0, j0 + kb))) break;
         if ((rc = S.laswp(j0 + kb, J1, j0, j0 + kb))) break;
-      } else {
+      }
+      // the in-block update (all rows below, mid-block columns) and, unpivoted, the mid
+      // block's rows of the columns beyond it, as one L-shaped update
+      const int64_t u_m0 = n - j0 - kb, u_n0 = M1 - j0 - kb, u_m1 = pivot ? 0 : M1 - j0 - kb,
+                    u_n1 = pivot ? 0 : n - M1;
+      bool applied = false, prepped = false;
+      if (!pivot) {
         // no pivoting: diagonal block LU, then L21 = A21 U11^{-1} for every row below
-        ProfScope ps(ctx, PK_PANEL, 8.0 * (double)M * kb * kb / 2, 2);
+        ProfScope ps(ctx, PK_PANEL, 8.0 * (double)M * kb * kb / 2, apply_path ? 1 : 2);
         constexpr int NS = TrsmTile<T>::NS;
-        k_getrf64<T><<<1, 256, (size_t)TRI * (TRI + 1) * sizeof(T), st>>>(A, lda, j0, kb, dinfo);
         const int64_t rb = n - j0 - kb;
-        if (rb > 0)
+        T* dblk = apply_path ? reinterpret_cast<T*>(lu_dinv(ipiv, n)) + (j0 / TRI) * 2 * TRI * TRI : nullptr;
+        if (apply_path)
+          k_lu_inv64<T><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk);
+        else
+          k_getrf64<T><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo);
+        if (apply_path && kb == TRI && rb > 0) {
+          // L21 and U12 (every column to the right: no later interchange touches these rows)
+          // in one launch, with the FP16 operands of the update below when it runs on the
+          // tensor cores
+          prepped = S.gemm2_runs(u_m0, u_n0, u_m1, u_n1, kb) && S.gemm2_tc(u_m0, u_n0, u_n1, kb, tcwork);
+          void *Apv = nullptr, *Bpv = nullptr;
+          float *isa = nullptr, *isb = nullptr;
+          if (prepped) tc_gemm_operands(tcwork, u_m0, u_n0 + u_n1, kb, &Apv, &isa, &Bpv, &isb);
+          const int nR = (int)((rb + 63) / 64);
+          k_panel_apply<<<(unsigned)(2 * nR), 256, panel_apply_smem(), st>>>(
+              reinterpret_cast<float2*>(A), lda, j0, n, reinterpret_cast<const float2*>(dblk), nR,
+              static_cast<__half2*>(Apv), isa, static_cast<__half2*>(Bpv), isb);
+          applied = true;
+        } else if (rb > 0) {
           k_trsm_tile<T, R, true><<<(unsigned)((rb + NS - 1) / NS), TrsmTile<T>::NT, trsm_tile_smem<T>(), st>>>(
               A, lda, j0, kb, j0 + kb, n);
+        }
         BEAST_CUDA_TRY(ctx, cudaGetLastError());
       }
       // TRSM + GEMM for the rest of the block.  Unpivoted, no later interchange touches
       // these rows, so U12 of this panel is solved for every column to its right at once and
       // the block's rows of the columns beyond the block are updated here too (what the
       // pivoted path does per panel after the block).
-      if ((rc = S.trsm(j0, kb, j0 + kb, pivot ? J1 : n))) break;
-      // in-block update (all rows below, mid-block columns) and, unpivoted, the mid block's
-      // rows of the columns beyond it, as one L-shaped update
-      if ((rc = S.gemm2(j0 + kb, n - j0 - kb, j0 + kb, M1 - j0 - kb, pivot ? 0 : M1 - j0 - kb,
-                        pivot ? 0 : n - M1, j0, kb, tcwork)))
-        break;
+      if (!applied && (rc = S.trsm(j0, kb, j0 + kb, pivot ? J1 : n))) break;
+      if ((rc = S.gemm2(j0 + kb, u_m0, j0 + kb, u_n0, u_m1, u_n1, j0, kb, tcwork, prepped))) break;
     }
     if (rc) break;
     // mid-block update: rows below x the rest of the outer block, and the rest of the outer
@@ -1412,7 +1812,9 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
     BEAST_CUDA_TRY(ctx, cudaMemcpy(ipiv, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice));
   }
   BEAST_CUDA_TRY(ctx, cudaMemcpy(ipiv + n, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice));
-  // inverses of the diagonal blocks for the triangular solves
+  // inverses of the diagonal blocks for the triangular solves (already written by k_lu_inv64
+  // on the apply path)
+  if (apply_path) return BEAST_OK;
   const size_t ism = (size_t)2 * 64 * 65 * sizeof(T);
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_invert_diag<T, R>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ism));
   k_invert_diag<T, R><<<(unsigned)((n + 63) / 64), 64, ism, st>>>(A, lda, n, reinterpret_cast<T*>(lu_dinv(ipiv, n)));

@@ -337,14 +337,6 @@ __global__ void __launch_bounds__(192, 1)
   }
 }
 
-// scale 2^sh that brings a largest magnitude mx into [2^13, 2^14) (1 for mx = 0)
-__device__ __forceinline__ int scale_shift(float mx) {
-  if (!(mx > 0.f)) return 0;
-  int e;
-  frexpf(mx, &e);  // mx = f 2^e, f in [0.5, 1)
-  return max(-120, min(120, 14 - e));
-}
-
 // A' (K-major; rows 2m, 2m+1 hold 2K halves): [[ar, -ai], [ai, ar]] blocks times s_m;
 // inv_sa[m] = 1 / s_m.  A CTA takes 32 rows: the row maxima first, then 64-column slices
 // transposed through shared memory so that every warp writes whole row segments.
@@ -365,7 +357,7 @@ __device__ __forceinline__ void expand_h(int bid, const float2* A, int64_t lda, 
   __syncthreads();
   if (w == 0) {
     for (int j = 1; j < 8; ++j) mx = fmaxf(mx, red[j][lane]);
-    const int sh = scale_shift(mx);
+    const int sh = tc_scale_shift(mx);
     s_scale[lane] = ldexpf(1.f, sh);
     if (m < M) inv_sa[m] = ldexpf(1.f, -sh);
   }
@@ -413,7 +405,7 @@ __device__ __forceinline__ void convert_bh(int bid, const float2* B, int64_t lda
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  const int sh = scale_shift(mx);
+  const int sh = tc_scale_shift(mx);
   const float sc = ldexpf(1.f, sh);
   if (lane == 0) inv_sb[j] = ldexpf(1.f, -sh);
   __half2* out = Bp + (int64_t)j * K;
@@ -484,14 +476,26 @@ size_t tc_gemm_work_bytes(int64_t M, int64_t N, int K) {
   return al((size_t)M * K * 8) + al((size_t)N * K * 4) + al((size_t)M * 4) + al((size_t)N * 4);
 }
 
+void tc_gemm_operands(void* work, int64_t M, int64_t N, int K, void** Ap, float** inv_sa, void** Bp,
+                      float** inv_sb) {
+  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
+  char* w = static_cast<char*>(work);
+  *Ap = w;
+  *Bp = w + al((size_t)M * K * 8);
+  *inv_sa = reinterpret_cast<float*>(w + al((size_t)M * K * 8) + al((size_t)N * K * 4));
+  *inv_sb = reinterpret_cast<float*>(reinterpret_cast<char*>(*inv_sa) + al((size_t)M * 4));
+}
+
 // C -= A B (complex64) for the LU updates, over an L-shaped region of C:
 //   A at (rowA, colA) of the matrix, M0 x K;  B at (colA, colB), K x (N0 + N1);
 //   rectangle 0: C[rowA : rowA+M0, colB : colB+N0]     = A[0:M0]  B[:, 0:N0]
 //   rectangle 1: C[rowA : rowA+M1, colB+N0 : +N1]      = A[0:M1]  B[:, N0:N0+N1]   (M1 <= M0)
 // (N1 = 0: one rectangle).  Mat: base of the full matrix (ld lda); work:
-// tc_gemm_work_bytes(M0, N0 + N1, K) bytes or more.
+// tc_gemm_work_bytes(M0, N0 + N1, K) bytes or more.  prepped: the FP16 operands are already
+// in work (tc_gemm_operands layout, written by the kernel that produced A and B).
 int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t colB,
-                int64_t M0, int64_t N0, int64_t M1, int64_t N1, int K, void* work, size_t work_bytes) {
+                int64_t M0, int64_t N0, int64_t M1, int64_t N1, int K, void* work, size_t work_bytes,
+                bool prepped) {
   cudaStream_t st = ctx->stream;
   const int64_t N = N0 + N1;
   // TMA: the first C' row (2 rowA floats) must start on 16 bytes
@@ -505,16 +509,17 @@ int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t 
     BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     attr_done[dev] = true;
   }
-  auto al = [](size_t b) { return (b + 255) & ~(size_t)255; };
-  char* w = static_cast<char*>(work);
-  __half2* Ap = reinterpret_cast<__half2*>(w);
-  __half2* Bp = reinterpret_cast<__half2*>(w + al((size_t)M0 * K * 8));
-  float* inv_sa = reinterpret_cast<float*>(w + al((size_t)M0 * K * 8) + al((size_t)N * K * 4));
-  float* inv_sb = reinterpret_cast<float*>(reinterpret_cast<char*>(inv_sa) + al((size_t)M0 * 4));
-  const int nA = (int)((M0 + 31) / 32), nB = (int)((N + 7) / 8);
-  k_prep_h<<<(unsigned)(nA + nB), 256, 0, st>>>(Mat + rowA + colA * lda, Mat + colA + colB * lda, lda, (int)M0,
-                                                (int)N, K, Ap, inv_sa, Bp, inv_sb, nA);
-  ctx->launches += 1;
+  void *Apv, *Bpv;
+  float *inv_sa, *inv_sb;
+  tc_gemm_operands(work, M0, N, K, &Apv, &inv_sa, &Bpv, &inv_sb);
+  __half2* Ap = static_cast<__half2*>(Apv);
+  __half2* Bp = static_cast<__half2*>(Bpv);
+  if (!prepped) {
+    const int nA = (int)((M0 + 31) / 32), nB = (int)((N + 7) / 8);
+    k_prep_h<<<(unsigned)(nA + nB), 256, 0, st>>>(Mat + rowA + colA * lda, Mat + colA + colB * lda, lda,
+                                                  (int)M0, (int)N, K, Ap, inv_sa, Bp, inv_sb, nA);
+    ctx->launches += 1;
+  }
   CUtensorMap tmA, tmB, tmC0, tmC1;
   // A': 2K halves per row (x), 2 M0 rows (y); B': 2K halves per column (x), N columns (y)
   if (!make_map(&tmA, Ap, (uint64_t)2 * K, (uint64_t)2 * M0, (uint64_t)2 * K * 2, TK, TM, true,
