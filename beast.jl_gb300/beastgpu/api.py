@@ -70,6 +70,12 @@ class Context:
         self.check(self.lib.beast_prof_launches(self.handle, C.byref(n)))
         return n.value
 
+    def last_factor_mode(self):
+        """factorisation of the last dense solve: 0 pivoted LU, 1 unpivoted LU, 2 symmetric"""
+        m = C.c_int(-1)
+        self.check(self.lib.beast_last_factor_mode(self.handle, C.byref(m)))
+        return m.value
+
     def set_workspace_limit(self, nbytes):
         self.check(self.lib.beast_ctx_set_workspace_limit(self.handle, int(nbytes)))
 

@@ -202,6 +202,12 @@ int beast_prof_read(beast_ctx* ctx, int kind, double* ms, int64_t* launches, dou
   return BEAST_OK;
 }
 
+int beast_last_factor_mode(beast_ctx* ctx, int* mode) {
+  if (!ctx || !mode) return BEAST_ERR_ARG;
+  *mode = ctx->last_factor_mode;
+  return BEAST_OK;
+}
+
 int beast_prof_launches(beast_ctx* ctx, int64_t* n) {
   ARG_CHECK(ctx, ctx && n, "null argument");
   *n = ctx->launches;
@@ -773,7 +779,7 @@ static double dev_norm(beast_ctx* ctx, int64_t n, const double* x, double* scrat
 
 // copy A into F (c64 for the mixed path, c128 otherwise) and factor F in place
 static int factor_copy(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dtype, void* F,
-                       int fdt, bool pivot, beast_lu** out) {
+                       int fdt, bool pivot, bool sym, beast_lu** out) {
   cudaStream_t st = ctx->stream;
   if (fdt == BEAST_C64) {
     if (a_dtype == BEAST_C64)
@@ -797,7 +803,7 @@ static int factor_copy(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, in
     delete lu;
     return beast_fail(ctx, BEAST_ERR_OOM, "pivot allocation failed");
   }
-  int rc = lu_factor_dev(ctx, n, F, n, fdt, lu->ipiv, &lu->info, pivot);
+  int rc = lu_factor_dev(ctx, n, F, n, fdt, lu->ipiv, &lu->info, pivot, sym);
   if (rc == BEAST_OK && lu->info > 0)
     rc = beast_fail(ctx, BEAST_ERR_SINGULAR, "zero pivot in column " + std::to_string(lu->info));
   if (rc) {
@@ -810,9 +816,12 @@ static int factor_copy(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, in
 
 // core of the dense solve on device vectors (b, x: c128 [n x nrhs], ld n)
 // FP64: partial-pivoting LU in complex FP64 (zgetrf semantics) + one solve.
-// MIXED: complex FP32 LU (tensor-core trailing updates) of a c64 copy, first without row
-// interchanges; FP64 iterative refinement against A as stored.  A zero pivot, a diverging
-// or stagnating refinement triggers one refactorisation with partial pivoting.
+// MIXED: complex FP32 factorisation (tensor-core trailing updates) of a c64 copy, FP64
+// iterative refinement against A as stored.  Factorisations tried in turn, each taking over
+// when the previous one meets a zero pivot or its refinement diverges or stagnates:
+//   symmetric (LDL^T-type, half the work; only when A is complex symmetric to within 1e-2
+//   in a sampled Frobenius measure -- e.g. a Galerkin EFIE matrix, symmetric up to quadrature),
+//   unpivoted LU, LU with partial pivoting.
 static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dtype,
                               int precision, const double* b, double* x, int64_t nrhs, double tol,
                               int maxiter, int* iters, double* resid) {
@@ -832,15 +841,20 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
   double res_max = 0;
   int rc = BEAST_OK;
   beast_lu* lu = nullptr;
-  bool pivot = !mixed;
-  for (int attempt = 0; attempt < 2; ++attempt) {
+  // factorisation modes: 2 symmetric, 1 unpivoted LU, 0 LU with partial pivoting
+  int mode = 0;
+  if (mixed) mode = asym_sample(ctx, n, A, lda, a_dtype) <= 1e-2 ? 2 : 1;
+  ctx->last_factor_mode = mode;
+  for (;;) {
     if (lu) {
       beast_lu_free(lu);
       lu = nullptr;
     }
-    rc = factor_copy(ctx, n, A, lda, a_dtype, F, fdt, pivot, &lu);
+    const bool pivot = mode == 0;
+    ctx->last_factor_mode = mode;
+    rc = factor_copy(ctx, n, A, lda, a_dtype, F, fdt, pivot, mode == 2, &lu);
     if (rc == BEAST_ERR_SINGULAR && !pivot) {
-      pivot = true;
+      --mode;
       continue;
     }
     if (rc) break;
@@ -898,7 +912,7 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
       }
     }
     if (retry && rc == BEAST_OK) {
-      pivot = true;
+      --mode;
       continue;
     }
     break;

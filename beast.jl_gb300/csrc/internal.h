@@ -44,6 +44,7 @@ struct beast_ctx {
   std::vector<ProfRec> prof;
   std::vector<cudaEvent_t> evpool;
   int64_t launches = 0;   // kernels launched by this context (counted always)
+  int last_factor_mode = -1;  // factorisation of the last dense solve (beast_last_factor_mode)
 };
 
 // brackets one or more launches of class `kind`; `work` = algorithmic flops or bytes
@@ -183,8 +184,12 @@ size_t lu_aux_bytes(int64_t n, int dtype);
 void* lu_dinv(const int* ipiv, int64_t n);
 // pivot = false: no row interchanges (the mixed path; guarded by refinement and a
 // fall-back to partial pivoting in the caller)
+// sym (c64, unpivoted): the symmetric variant for a near complex-symmetric A (only its lower
+// triangle is used; the factors approximate those of (A + A^T) / 2)
 int lu_factor_dev(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, int* ipiv,
-                  int* info, bool pivot = true);
+                  int* info, bool pivot = true, bool sym = false);
+// relative asymmetry ||A - A^T|| / ||A|| (Frobenius) estimated on about 10^6 sampled pairs
+double asym_sample(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int dtype);
 int lu_solve_dev(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int dtype,
                  const int* ipiv, void* B, int64_t ldb, int64_t nrhs);
 // y = alpha * A x + beta * y (FP64 arithmetic, A c128 or c64, x/y c128)

@@ -41,6 +41,8 @@ size_t tc_gemm_work_bytes(int64_t M, int64_t N, int K);
 int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t colB,
                 int64_t M0, int64_t N0, int64_t M1, int64_t N1, int K, void* work, size_t work_bytes,
                 bool prepped);
+int tc_gemm_sym(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t rowB, int64_t M0,
+                int64_t N0, int K, bool lower, void* work, size_t work_bytes, bool prepped);
 
 namespace {
 
@@ -480,8 +482,11 @@ __device__ __forceinline__ int pidx(int c) {  // conflict-free index of the publ
   return c + (c >> 2);
 }
 
+// sym = 1: only the lower triangle of the block is current (symmetric updates); the upper
+// one is taken from it by symmetry.
 template <typename T>
-__global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0, int kb, int* info, T* inv) {
+__global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0, int kb, int* info, T* inv,
+                                                  int sym) {
   constexpr int LD = TRI + 1, PL = TRI + TRI / 4;
   extern __shared__ unsigned char smraw[];
   T* Ls = reinterpret_cast<T*>(smraw);  // 64 x LD: staging, then the L factor, then Linv
@@ -495,7 +500,8 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
   // coalesced load through shared memory (identity padding beyond kb)
   for (int e = tid; e < TRI * TRI; e += 256) {
     const int r = e & (TRI - 1), c = e >> 6;
-    Ls[r * LD + c] = (r < kb && c < kb) ? A[(j0 + r) + (j0 + c) * lda] : (r == c ? one : zero);
+    const int rr = (sym && c > r) ? c : r, cc = (sym && c > r) ? r : c;
+    Ls[r * LD + c] = (r < kb && c < kb) ? A[(j0 + rr) + (j0 + cc) * lda] : (r == c ? one : zero);
   }
   if (tid < 2) s_zero[tid] = 0;
   __syncthreads();
@@ -786,9 +792,12 @@ __device__ __forceinline__ void cmac2(float2& acc, float4 a, float4 b) {
   acc = __ffma2_rn(make_float2(a.z, a.w), make_float2(b.z, b.w), acc);
 }
 
+// Symmetric factorisation (nB >= 0; launched with nR CTAs, right side only): U12 = D L21^T
+// is not stored; its FP16 B' columns for the first nB systems (the rest of the mid block)
+// are written from L21 and the pivots D = diag(U11) instead.
 __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, int64_t j0, int64_t n,
                                                         const float2* __restrict__ inv, int nR, __half2* Ap,
-                                                        float* inv_sa, __half2* Bp, float* inv_sb) {
+                                                        float* inv_sa, __half2* Bp, float* inv_sb, int nB) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float4* Ws = reinterpret_cast<float4*>(smraw);  // W[k][s], k of the current half
   float4* Ns = Ws + PA_KH * PA_LD4;               // N[k][v]
@@ -918,6 +927,44 @@ __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, 
     }
     __syncthreads();
   }
+  if (right && nB > (int)(b0 - s0)) {
+    // symmetric: B' column of system s (< nB) = D (row s of L21), its own scale
+    __shared__ float2 s_d[64];
+    __shared__ float s_tsc[64];
+    if (tid < 64) s_d[tid] = A[(j0 + tid) + (j0 + tid) * lda];
+    __syncthreads();
+    const int sy = tid & 63, q = tid >> 6;
+    float mx = 0.f;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      const float2 a = cmulx(Cs[sy * PA_CLD + 16 * q + i], s_d[16 * q + i]);
+      mx = fmaxf(mx, fmaxf(fabsf(a.x), fabsf(a.y)));
+    }
+    red[q * 64 + sy] = mx;
+    __syncthreads();
+    if (q == 0) {
+      mx = fmaxf(fmaxf(red[sy], red[64 + sy]), fmaxf(red[128 + sy], red[192 + sy]));
+      const int sh = tc_scale_shift(mx);
+      s_tsc[sy] = ldexpf(1.f, sh);
+      if (b0 + sy - s0 < nB) inv_sb[b0 + sy - s0] = ldexpf(1.f, -sh);
+    }
+    __syncthreads();
+    const int v0 = 4 * (lane & 15);
+    for (int sp = 2 * warp; sp < 64; sp += 16) {
+      const int s2 = sp + (lane >> 4);
+      if (b0 + s2 - s0 < nB) {
+        const float sc = s_tsc[s2];
+        const float2* cr = Cs + s2 * PA_CLD + v0;
+        __half2 hv[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+          const float2 a = cmulx(cr[i], s_d[v0 + i]);
+          hv[i] = __floats2half2_rn(a.x * sc, a.y * sc);
+        }
+        *reinterpret_cast<uint4*>(Bp + (b0 + s2 - s0) * TRI + v0) = *reinterpret_cast<const uint4*>(hv);
+      }
+    }
+  }
   // 16-byte stores: a lane converts 4 consecutive v of one system; right -- one system per
   // warp pass (lanes 0..15 row 2m, 16..31 row 2m+1: 512 contiguous bytes), left -- two
   // systems per pass (256 bytes each)
@@ -952,6 +999,64 @@ __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, 
         *reinterpret_cast<uint4*>(Bp + m * TRI + v0) = *reinterpret_cast<const uint4*>(hv);
       }
     }
+  }
+}
+
+// ---- symmetric factorisation helpers ---------------------------------------------------
+// B (K x N, ld K) = D L^T with L = rows of the matrix (N x K at L, ld lda) and D the pivots on
+// the diagonal at dg (stride lda + 1): the explicit operand of the CUDA-core fallback update
+template <typename T>
+__global__ void k_dlt(const T* L, const T* dg, int64_t lda, int K, int N, T* B) {
+  const int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  if (e >= (int64_t)K * N) return;
+  const int k = (int)(e % K), c = (int)(e / K);
+  B[e] = cmulx(dg[(int64_t)k * (lda + 1)], L[c + (int64_t)k * lda]);
+}
+
+// U = D L^T above the 64 x 64 diagonal blocks: block (I, J), I < J, from the transposed block
+// (J, I) of L and the pivots of rows 64 I..: U[i][j] = d_i L[j][i] (the diagonal blocks
+// already hold U11 from k_lu_inv64)
+template <typename T>
+__global__ void __launch_bounds__(256) k_sym_upper(T* A, int64_t lda, int64_t n) {
+  const int J = blockIdx.x, I = blockIdx.y;
+  if (I >= J) return;
+  __shared__ T t[64][65];
+  __shared__ T d[64];
+  const int64_t r0 = 64 * (int64_t)I, c0 = 64 * (int64_t)J;
+  const int tid = threadIdx.x;
+  if (tid < 64) d[tid] = r0 + tid < n ? A[(r0 + tid) * (lda + 1)] : T{0, 0};
+  for (int e = tid; e < 64 * 64; e += 256) {
+    const int j = e & 63, i = e >> 6;  // L[c0 + j][r0 + i], coalesced along j
+    t[i][j] = (c0 + j < n && r0 + i < n) ? A[(c0 + j) + (r0 + i) * lda] : T{0, 0};
+  }
+  __syncthreads();
+  for (int e = tid; e < 64 * 64; e += 256) {
+    const int i = e & 63, j = e >> 6;  // U[r0 + i][c0 + j], coalesced along i
+    if (r0 + i < n && c0 + j < n) A[(r0 + i) + (c0 + j) * lda] = cmulx(d[i], t[i][j]);
+  }
+}
+
+// sampled asymmetry: sums of |a_ij - a_ji|^2 and |a_ij|^2 + |a_ji|^2 over rows i = s p, columns
+// j = s q < i (FP64 sums, atomically added)
+template <typename T>
+__global__ void k_asym_sample(const T* A, int64_t lda, int64_t n, int64_t s, double* out) {
+  const int64_t np = (n + s - 1) / s;
+  double dsum = 0, nsum = 0;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < np * np; e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t i = (e % np) * s, j = (e / np) * s;
+    if (j >= i) continue;
+    const T a = A[i + j * lda], b = A[j + i * lda];
+    const double dr = (double)a.x - (double)b.x, di = (double)a.y - (double)b.y;
+    dsum += dr * dr + di * di;
+    nsum += (double)a.x * a.x + (double)a.y * a.y + (double)b.x * b.x + (double)b.y * b.y;
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+    nsum += __shfl_xor_sync(0xffffffffu, nsum, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd(out, dsum);
+    atomicAdd(out + 1, nsum);
   }
 }
 
@@ -1642,15 +1747,47 @@ struct LUSteps {
     }
     return BEAST_OK;
   }
-
+  // symmetric update: A[rowA.., rowB..] (m x nc) -= L1 D L2^T, L1 = A[rowA.., colA..],
+  // L2 = A[rowB.., colA..], D the pivots on the diagonal at colA..; lower: only the tiles on or
+  // below the diagonal (tensor cores; the CUDA-core fallback updates the whole rectangle)
+  bool symgemm_tc(int64_t m, int64_t nc, int k, const void* tcwork) const {
+    return sizeof(T) == 8 && tcwork && m >= 64 && nc >= 64 && k % 32 == 0;
+  }
+  int symgemm(int64_t rowA, int64_t m, int64_t rowB, int64_t nc, int64_t colA, int k, bool lower, void* tcwork,
+              bool prepped = false) {
+    if (m <= 0 || nc <= 0 || k <= 0) return BEAST_OK;
+    const bool tc = symgemm_tc(m, nc, k, tcwork);
+    ProfScope ps(ctx, tc ? PK_TCGEMM : PK_GEMM, 8.0 * (double)k * (double)m * nc * (lower ? 0.5 : 1.0));
+    if (tc)
+      return tc_gemm_sym(ctx, reinterpret_cast<float2*>(A), lda, rowA, colA, rowB, m, nc, k, lower, tcwork,
+                         tcwork_bytes, prepped);
+    T* B = nullptr;
+    BEAST_CUDA_TRY(ctx, cudaMallocAsync(&B, (size_t)k * nc * sizeof(T), st));
+    const int64_t tot = (int64_t)k * nc;
+    k_dlt<T><<<(unsigned)((tot + 255) / 256), 256, 0, st>>>(A + rowB + colA * lda, A + colA + colA * lda, lda, k,
+                                                            (int)nc, B);
+    dim3 g((unsigned)((m + GT - 1) / GT), (unsigned)((nc + GT - 1) / GT));
+    k_gemm_sub<T, R><<<g, 256, 0, st>>>(A + rowA + rowB * lda, lda, A + rowA + colA * lda, lda, B, k, m, nc, k);
+    BEAST_CUDA_TRY(ctx, cudaGetLastError());
+    BEAST_CUDA_TRY(ctx, cudaFreeAsync(B, st));
+    return BEAST_OK;
+  }
 };
 
 // Two-level right-looking LU: column blocks of NB are factored with nb-wide panels (panel,
 // interchanges, TRSM and GEMM restricted to the block); then the block's interchanges are
 // applied to the other columns and the trailing matrix gets one rank-NB update
 // (TRSM for U12, GEMM with K = NB -- on the tensor cores for complex FP32).
+//
+// sym (unpivoted c64 with 64-wide panels; A near complex-symmetric, the factors serving as the
+// preconditioner of a refined solve): an LDL^T-type factorisation that keeps only the lower
+// triangle current -- the diagonal blocks are factored from their lower triangle mirrored,
+// U12 = D L21^T is never formed in FP32 (the updates take it from L21 and the pivots), the
+// in-block and mid-block updates cover only the rows below, the trailing update only the
+// tiles on or below the diagonal: about half the work.  At the end U = D L^T is written above
+// the diagonal blocks, so the factors have the layout of the LU.
 template <typename T, typename R>
-int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* info, bool pivot) {
+int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* info, bool pivot, bool sym) {
   cudaStream_t st = ctx->stream;
   const int G0 = std::max(1, ctx->num_sms);
   const size_t smem_cap = 220 * 1024;
@@ -1665,6 +1802,7 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   // unpivoted c64 with 64-wide panels: k_lu_inv64 also inverts the block's triangles and
   // k_panel_apply does both triangular solves (and the FP16 operands of the in-block update)
   const bool apply_path = !pivot && sizeof(T) == 8 && nb == TRI;
+  sym = sym && apply_path;
   const size_t getrf_sm = (size_t)TRI * (TRI + 1) * sizeof(T);
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_getrf64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
@@ -1738,21 +1876,24 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
         const int64_t rb = n - j0 - kb;
         T* dblk = apply_path ? reinterpret_cast<T*>(lu_dinv(ipiv, n)) + (j0 / TRI) * 2 * TRI * TRI : nullptr;
         if (apply_path)
-          k_lu_inv64<T><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk);
+          k_lu_inv64<T><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk, sym ? 1 : 0);
         else
           k_getrf64<T><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo);
         if (apply_path && kb == TRI && rb > 0) {
           // L21 and U12 (every column to the right: no later interchange touches these rows)
           // in one launch, with the FP16 operands of the update below when it runs on the
           // tensor cores
-          prepped = S.gemm2_runs(u_m0, u_n0, u_m1, u_n1, kb) && S.gemm2_tc(u_m0, u_n0, u_n1, kb, tcwork);
+          // (symmetric: L21 only, and the update is rows below x the rest of the mid block)
+          const int64_t nBs = sym ? u_n0 : 0;
+          prepped = sym ? (nBs > 0 && S.symgemm_tc(u_m0, nBs, kb, tcwork))
+                        : (S.gemm2_runs(u_m0, u_n0, u_m1, u_n1, kb) && S.gemm2_tc(u_m0, u_n0, u_n1, kb, tcwork));
           void *Apv = nullptr, *Bpv = nullptr;
           float *isa = nullptr, *isb = nullptr;
-          if (prepped) tc_gemm_operands(tcwork, u_m0, u_n0 + u_n1, kb, &Apv, &isa, &Bpv, &isb);
+          if (prepped) tc_gemm_operands(tcwork, u_m0, sym ? nBs : u_n0 + u_n1, kb, &Apv, &isa, &Bpv, &isb);
           const int nR = (int)((rb + 63) / 64);
-          k_panel_apply<<<(unsigned)(2 * nR), 256, panel_apply_smem(), st>>>(
+          k_panel_apply<<<(unsigned)(sym ? nR : 2 * nR), 256, panel_apply_smem(), st>>>(
               reinterpret_cast<float2*>(A), lda, j0, n, reinterpret_cast<const float2*>(dblk), nR,
-              static_cast<__half2*>(Apv), isa, static_cast<__half2*>(Bpv), isb);
+              static_cast<__half2*>(Apv), isa, static_cast<__half2*>(Bpv), isb, prepped ? (int)nBs : 0);
           applied = true;
         } else if (rb > 0) {
           k_trsm_tile<T, R, true><<<(unsigned)((rb + NS - 1) / NS), TrsmTile<T>::NT, trsm_tile_smem<T>(), st>>>(
@@ -1764,13 +1905,21 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       // these rows, so U12 of this panel is solved for every column to its right at once and
       // the block's rows of the columns beyond the block are updated here too (what the
       // pivoted path does per panel after the block).
+      if (sym) {
+        if ((rc = S.symgemm(j0 + kb, u_m0, j0 + kb, u_n0, j0, kb, false, tcwork, prepped))) break;
+        continue;
+      }
       if (!applied && (rc = S.trsm(j0, kb, j0 + kb, pivot ? J1 : n))) break;
       if ((rc = S.gemm2(j0 + kb, u_m0, j0 + kb, u_n0, u_m1, u_n1, j0, kb, tcwork, prepped))) break;
     }
     if (rc) break;
     // mid-block update: rows below x the rest of the outer block, and the rest of the outer
     // block's rows x the columns beyond it (K = NB2; nothing when pivoting: NB2 = NB)
-    if (M1 < J1 && (rc = S.gemm2(M1, n - M1, M1, J1 - M1, J1 - M1, n - J1, M0, (int)(M1 - M0), tcwork))) break;
+    if (M1 < J1) {
+      rc = sym ? S.symgemm(M1, n - M1, M1, J1 - M1, M0, (int)(M1 - M0), false, tcwork)
+               : S.gemm2(M1, n - M1, M1, J1 - M1, J1 - M1, n - J1, M0, (int)(M1 - M0), tcwork);
+      if (rc) break;
+    }
     }
     if (rc) break;
     // the block's interchanges on the columns left and right of it
@@ -1778,7 +1927,9 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       if ((rc = S.laswp(0, J0, J0, J1))) break;
       if ((rc = S.laswp(J1, n, J0, J1))) break;
     }
-    if (J1 < n) {
+    if (J1 < n && sym) {
+      rc = S.symgemm(J1, n - J1, J1, n - J1, J0, (int)(J1 - J0), true, tcwork);
+    } else if (J1 < n) {
       // U12 = L11^{-1} A12 (blocked: nb-row TRSM, then GEMM on the rows below inside the
       // block); done per panel above when unpivoted
       for (int64_t j0 = J0; pivot && j0 < J1 && rc == BEAST_OK; j0 += nb) {
@@ -1812,6 +1963,12 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
     BEAST_CUDA_TRY(ctx, cudaMemcpy(ipiv, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice));
   }
   BEAST_CUDA_TRY(ctx, cudaMemcpy(ipiv + n, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice));
+  if (sym) {  // U = D L^T above the diagonal blocks
+    const unsigned nbk = (unsigned)((n + 63) / 64);
+    ProfScope ps(ctx, PK_CONVERT, (double)n * n * sizeof(T));
+    k_sym_upper<T><<<dim3(nbk, nbk), 256, 0, st>>>(A, lda, n);
+    BEAST_CUDA_TRY(ctx, cudaGetLastError());
+  }
   // inverses of the diagonal blocks for the triangular solves (already written by k_lu_inv64
   // on the apply path)
   if (apply_path) return BEAST_OK;
@@ -1887,9 +2044,26 @@ int lu_solve_fixed_scratch(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, c
 }  // namespace
 
 int lu_factor_dev(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, int* ipiv, int* info,
-                  bool pivot) {
-  if (dtype == BEAST_C64) return lu_factor_t<float2, float>(ctx, n, (float2*)A, lda, ipiv, info, pivot);
-  return lu_factor_t<double2, double>(ctx, n, (double2*)A, lda, ipiv, info, pivot);
+                  bool pivot, bool sym) {
+  if (dtype == BEAST_C64) return lu_factor_t<float2, float>(ctx, n, (float2*)A, lda, ipiv, info, pivot, sym);
+  return lu_factor_t<double2, double>(ctx, n, (double2*)A, lda, ipiv, info, pivot, false);
+}
+
+double asym_sample(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int dtype) {
+  if (n < 2) return 0.0;
+  const int64_t s = std::max<int64_t>(1, n / 1400);  // about 10^6 pairs
+  double* d = nullptr;
+  if (cudaMallocAsync(&d, 2 * sizeof(double), ctx->stream) != cudaSuccess) return 1.0;
+  cudaMemsetAsync(d, 0, 2 * sizeof(double), ctx->stream);
+  if (dtype == BEAST_C64)
+    k_asym_sample<float2><<<1024, 256, 0, ctx->stream>>>((const float2*)A, lda, n, s, d);
+  else
+    k_asym_sample<double2><<<1024, 256, 0, ctx->stream>>>((const double2*)A, lda, n, s, d);
+  double h[2] = {0, 0};
+  cudaMemcpyAsync(h, d, sizeof(h), cudaMemcpyDeviceToHost, ctx->stream);
+  cudaFreeAsync(d, ctx->stream);
+  if (cudaStreamSynchronize(ctx->stream) != cudaSuccess) return 1.0;
+  return h[1] > 0 ? std::sqrt(2.0 * h[0] / h[1]) : 0.0;
 }
 
 // ipiv holds 2n ints: the pivots, then the permutation built by lu_factor_dev

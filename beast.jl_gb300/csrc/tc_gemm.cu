@@ -166,10 +166,15 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 // covers the first m_rows[r] rows of A' and the n_cols[r] columns of B' from b_col[r], and
 // writes C' through its own (clipped) tensor map at (c_row0, c_col0[r]).  Tiles of
 // rectangle 0 come first in the tile order.
+// lower = 1 (one square rectangle on the diagonal, symmetric updates): only the tiles that
+// hold an element on or below the diagonal, i.e. column tile n <= m / 4 for row tile m
+// (128 real rows = 64 complex rows against 256 columns); rows come in groups of four with
+// g + 1 tiles each, so tile t of group g = floor((sqrt(2t + 1) - 1) / 2) is found in closed form.
 struct TcRegion {
   int m_rows[2], n_cols[2], b_col[2], c_col0[2];
   int c_row0;
   int ntn[2], ntiles0, ntiles;
+  int lower;
 };
 
 __global__ void __launch_bounds__(192, 1)
@@ -195,6 +200,16 @@ __global__ void __launch_bounds__(192, 1)
   const int ntiles = Rg.ntiles;
   // tile -> (rectangle, first row, first column within the rectangle)
   auto tile_at = [&](int tile, int& r, int& m0, int& n0) {
+    if (Rg.lower) {
+      r = 0;
+      int g = (int)((sqrtf(2.f * (float)tile + 1.f) - 1.f) * 0.5f);
+      while (2 * g * (g + 1) > tile) --g;
+      while (2 * (g + 1) * (g + 2) <= tile) ++g;
+      const int t = tile - 2 * g * (g + 1);
+      m0 = (4 * g + t / (g + 1)) * TM;
+      n0 = (t % (g + 1)) * TN;
+      return;
+    }
     r = tile < Rg.ntiles0 ? 0 : 1;
     const int lt = r ? tile - Rg.ntiles0 : tile;
     m0 = (lt / Rg.ntn[r]) * TM;
@@ -415,6 +430,70 @@ __device__ __forceinline__ void convert_bh(int bid, const float2* B, int64_t lda
   }
 }
 
+// B' of a symmetric update, B = D L^T: column j of B' is row j of L (K complex, read through
+// shared memory in 32 x 64 tiles: coalesced along the rows of L) times the pivots d_k =
+// Mat[colA + k, colA + k], scaled by t_j (largest |re|, |im| of the column into [2^13, 2^14)).
+// A CTA takes 32 columns of B'.  L: the block of rows rowB.., columns colA.. of Mat.
+__device__ __forceinline__ void convert_bt(int bid, const float2* L, const float2* dg, int64_t lda, int K, int N,
+                                           __half2* Bp, float* inv_sb) {
+  __shared__ float red[8][33];
+  __shared__ float2 tile[32][65];
+  __shared__ float s_scale[32];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int j0 = bid * 32, j = j0 + lane;
+  auto dk = [&](int k) { return dg[(int64_t)k * (lda + 1)]; };
+  float mx = 0.f;
+  if (j < N)
+    for (int k = w; k < K; k += 8) {
+      const float2 a = L[j + (int64_t)k * lda], d = dk(k);
+      const float re = a.x * d.x - a.y * d.y, im = a.x * d.y + a.y * d.x;
+      mx = fmaxf(mx, fmaxf(fabsf(re), fabsf(im)));
+    }
+  red[w][lane] = mx;
+  __syncthreads();
+  if (w == 0) {
+    for (int q = 1; q < 8; ++q) mx = fmaxf(mx, red[q][lane]);
+    const int sh = tc_scale_shift(mx);
+    s_scale[lane] = ldexpf(1.f, sh);
+    if (j < N) inv_sb[j] = ldexpf(1.f, -sh);
+  }
+  __syncthreads();
+  for (int k0 = 0; k0 < K; k0 += 64) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int k = k0 + w + 8 * q;
+      tile[lane][w + 8 * q] = (j < N && k < K) ? L[j + (int64_t)k * lda] : make_float2(0.f, 0.f);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const int jr = w + 8 * i, jc = j0 + jr;
+      if (jc < N) {
+        const float sc = s_scale[jr];
+        __half2* col = Bp + (int64_t)jc * K;
+#pragma unroll
+        for (int hh = 0; hh < 2; ++hh) {
+          const int kk = lane + 32 * hh, k = k0 + kk;
+          if (k < K) {
+            const float2 a = tile[jr][kk], d = dk(k);
+            col[k] = __floats2half2_rn((a.x * d.x - a.y * d.y) * sc, (a.x * d.y + a.y * d.x) * sc);
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void __launch_bounds__(256) k_prep_sym(const float2* A, const float2* L, const float2* dg, int64_t lda,
+                                                  int M, int N, int K, __half2* Ap, float* inv_sa, __half2* Bp,
+                                                  float* inv_sb, int nA) {
+  if ((int)blockIdx.x < nA)
+    expand_h(blockIdx.x, A, lda, M, K, Ap, inv_sa);
+  else
+    convert_bt(blockIdx.x - nA, L, dg, lda, K, N, Bp, inv_sb);
+}
+
 // both operands in one launch: CTAs [0, nA) expand 32 rows of A each, the rest convert 8
 // columns of B each
 __global__ void __launch_bounds__(256) k_prep_h(const float2* A, const float2* B, int64_t lda, int M, int N, int K,
@@ -486,21 +565,30 @@ void tc_gemm_operands(void* work, int64_t M, int64_t N, int K, void** Ap, float*
   *inv_sb = reinterpret_cast<float*>(reinterpret_cast<char*>(*inv_sa) + al((size_t)M * 4));
 }
 
-// C -= A B (complex64) for the LU updates, over an L-shaped region of C:
-//   A at (rowA, colA) of the matrix, M0 x K;  B at (colA, colB), K x (N0 + N1);
-//   rectangle 0: C[rowA : rowA+M0, colB : colB+N0]     = A[0:M0]  B[:, 0:N0]
-//   rectangle 1: C[rowA : rowA+M1, colB+N0 : +N1]      = A[0:M1]  B[:, N0:N0+N1]   (M1 <= M0)
-// (N1 = 0: one rectangle).  Mat: base of the full matrix (ld lda); work:
-// tc_gemm_work_bytes(M0, N0 + N1, K) bytes or more.  prepped: the FP16 operands are already
-// in work (tc_gemm_operands layout, written by the kernel that produced A and B).
-int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t colB,
-                int64_t M0, int64_t N0, int64_t M1, int64_t N1, int K, void* work, size_t work_bytes,
-                bool prepped) {
+// One tensor-core update of the matrix Mat (ld lda), C -= A B over one or two rectangles of C
+// sharing the operands (see TcRegion), A = Mat[rowA.., colA..] (M0 x K).
+//   LU:        B = Mat[colA.., colB..] (K x (N0 + N1))
+//   symmetric: B = D L^T with L = Mat[rowB.., colA..] (N0 x K) and D the pivots
+//              Mat[colA + k, colA + k]; C columns from colB = rowB; lower: only the tiles on or
+//              below the diagonal (rowA = rowB, M0 = N0, one rectangle)
+// prepped: the FP16 operands are already in work (tc_gemm_operands layout, written by the
+// kernel that produced A and B).
+struct TcUpdate {
+  int64_t rowA, colA, colB, M0, N0, M1, N1;
+  int K;
+  bool sym, lower, prepped;
+};
+
+static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate& u, void* work, size_t work_bytes) {
   cudaStream_t st = ctx->stream;
+  const int64_t rowA = u.rowA, colA = u.colA, colB = u.colB, M0 = u.M0, N0 = u.N0, M1 = u.M1, N1 = u.N1;
+  const int K = u.K;
   const int64_t N = N0 + N1;
   // TMA: the first C' row (2 rowA floats) must start on 16 bytes
   if ((2 * rowA) % 4 != 0 || K % 32 != 0 || M1 > M0 || 2 * (rowA + M0) > INT32_MAX || colB + N > INT32_MAX)
     return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: unaligned block");
+  if (u.lower && (u.sym == false || rowA != colB || M0 != N0 || N1 != 0))
+    return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: lower-triangle tiles need a diagonal square");
   if (tc_gemm_work_bytes(M0, N, K) > work_bytes)
     return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: workspace too small");
   static bool attr_done[64] = {false};
@@ -514,10 +602,18 @@ int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t 
   tc_gemm_operands(work, M0, N, K, &Apv, &inv_sa, &Bpv, &inv_sb);
   __half2* Ap = static_cast<__half2*>(Apv);
   __half2* Bp = static_cast<__half2*>(Bpv);
-  if (!prepped) {
-    const int nA = (int)((M0 + 31) / 32), nB = (int)((N + 7) / 8);
-    k_prep_h<<<(unsigned)(nA + nB), 256, 0, st>>>(Mat + rowA + colA * lda, Mat + colA + colB * lda, lda,
-                                                  (int)M0, (int)N, K, Ap, inv_sa, Bp, inv_sb, nA);
+  if (!u.prepped) {
+    const int nA = (int)((M0 + 31) / 32);
+    if (u.sym) {
+      const int nB = (int)((N + 31) / 32);
+      k_prep_sym<<<(unsigned)(nA + nB), 256, 0, st>>>(Mat + rowA + colA * lda, Mat + colB + colA * lda,
+                                                      Mat + colA + colA * lda, lda, (int)M0, (int)N, K, Ap, inv_sa,
+                                                      Bp, inv_sb, nA);
+    } else {
+      const int nB = (int)((N + 7) / 8);
+      k_prep_h<<<(unsigned)(nA + nB), 256, 0, st>>>(Mat + rowA + colA * lda, Mat + colA + colB * lda, lda,
+                                                    (int)M0, (int)N, K, Ap, inv_sa, Bp, inv_sb, nA);
+    }
     ctx->launches += 1;
   }
   CUtensorMap tmA, tmB, tmC0, tmC1;
@@ -540,6 +636,7 @@ int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t 
                 CU_TENSOR_MAP_DATA_TYPE_FLOAT32))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (C') failed");
   TcRegion Rg;
+  Rg.lower = u.lower ? 1 : 0;
   Rg.c_row0 = (int)(2 * rowA);
   Rg.m_rows[0] = (int)(2 * M0);
   Rg.n_cols[0] = (int)N0;
@@ -556,10 +653,38 @@ int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t 
   }
   Rg.ntiles0 = ntl[0];
   Rg.ntiles = ntl[0] + ntl[1];
+  if (Rg.lower) {  // tiles n <= m / 4 of every row tile m
+    const int ntm = (Rg.m_rows[0] + TM - 1) / TM;
+    int64_t cnt = 0;
+    for (int m = 0; m < ntm; ++m) cnt += std::min(m / 4 + 1, Rg.ntn[0]);
+    Rg.ntiles0 = Rg.ntiles = (int)cnt;
+  }
   if (Rg.ntiles == 0) return BEAST_OK;
   const int grid = std::min(Rg.ntiles, std::max(1, ctx->num_sms));
   const int nk = (2 * K) / TK;
   k_tc_gemm<<<grid, 192, SMEM_BYTES, st>>>(tmA, tmB, tmC0, tmC1, Rg, inv_sa, inv_sb, nk, ctx->d_flag);
   BEAST_CUDA_TRY(ctx, cudaGetLastError());
   return BEAST_OK;
+}
+
+// C -= A B (complex64) for the LU updates, over an L-shaped region of C:
+//   A at (rowA, colA) of the matrix, M0 x K;  B at (colA, colB), K x (N0 + N1);
+//   rectangle 0: C[rowA : rowA+M0, colB : colB+N0]     = A[0:M0]  B[:, 0:N0]
+//   rectangle 1: C[rowA : rowA+M1, colB+N0 : +N1]      = A[0:M1]  B[:, N0:N0+N1]   (M1 <= M0)
+// (N1 = 0: one rectangle).  work: tc_gemm_work_bytes(M0, N0 + N1, K) bytes or more.
+int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t colB,
+                int64_t M0, int64_t N0, int64_t M1, int64_t N1, int K, void* work, size_t work_bytes,
+                bool prepped) {
+  TcUpdate u{rowA, colA, colB, M0, N0, M1, N1, K, false, false, prepped};
+  return tc_gemm_run(ctx, Mat, lda, u, work, work_bytes);
+}
+
+// Symmetric update of an LDL^T-type factorisation: C[rowA.., rowB..] (M0 x N0) -= L1 D L2^T
+// with L1 = Mat[rowA.., colA..] (M0 x K), L2 = Mat[rowB.., colA..] (N0 x K), D the pivots on
+// the diagonal of Mat at colA..; lower: only the tiles on or below the diagonal (rowA = rowB,
+// M0 = N0).
+int tc_gemm_sym(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t rowB, int64_t M0,
+                int64_t N0, int K, bool lower, void* work, size_t work_bytes, bool prepped) {
+  TcUpdate u{rowA, colA, rowB, M0, N0, 0, 0, K, true, lower, prepped};
+  return tc_gemm_run(ctx, Mat, lda, u, work, work_bytes);
 }

@@ -568,7 +568,10 @@ def main():
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": "c64+f64" if prec == L.MIXED else "c128", "data": "synthetic icosphere mesh",
            "config": config_dict(args, X, m), "refinement": {"iters": it.value,
-                                                            "rel_residual": res.value},
+                                                            "rel_residual": res.value,
+                                                            "factorisation": ["LU with partial pivoting",
+                                                                              "unpivoted LU", "symmetric LDL^T-type"][
+                                                                max(0, ctx.last_factor_mode())]},
            "roofline": roof, "kernel_breakdown": breakdown, "gpu_launches": int(launches),
            "clocks": clocks, "e2e": e2e}
     if not args.no_cpu_baseline:

@@ -237,6 +237,10 @@ int beast_prof_enable(beast_ctx* ctx, int on);
 int beast_prof_read(beast_ctx* ctx, int kind, double* ms, int64_t* launches, double* work);
 /* kernels launched by this context since the last beast_prof_enable (counted always) */
 int beast_prof_launches(beast_ctx* ctx, int64_t* n);
+/* factorisation that produced the result of the last beast_solve_dense / beast_solve_job on
+ * this context: 0 LU with partial pivoting, 1 unpivoted LU (mixed), 2 symmetric LDL^T-type
+ * (mixed, near complex-symmetric matrix), -1 none yet */
+int beast_last_factor_mode(beast_ctx* ctx, int* mode);
 
 /* library version string */
 const char* beast_version(void);

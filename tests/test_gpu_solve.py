@@ -39,9 +39,13 @@ def test_lu_random_matrix_pivoting():
 
 
 def test_mixed_refinement(efie):
+    """the EFIE Galerkin matrix is complex symmetric up to quadrature: the mixed solve takes
+    the symmetric (LDL^T-type) factorisation and still refines to the FP64 solution"""
     X, op, E, Z, b = efie
     xo = O.lu_solve(Z, b)
-    x, it, res = bg.solve(Z, b, precision=bg.MIXED, tol=1e-12)
+    ctx = bg.get_context(0)
+    x, it, res = bg.solve(Z, b, precision=bg.MIXED, tol=1e-12, ctx=ctx)
+    assert ctx.last_factor_mode() == 2
     assert res < 1e-12 and it >= 1
     assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-10
 
@@ -137,8 +141,39 @@ def test_mixed_unpivoted_path_converges_without_fallback(n):
         prof = ctx.prof_read()
     finally:
         ctx.prof_enable(False)
+    assert ctx.last_factor_mode() == 1  # not symmetric: the unpivoted LU
     assert "lu_laswp" not in prof and "lu_panel" in prof
     assert prof["lu_panel"][1] == (n + 63) // 64  # one factorisation: one record per panel
     assert it <= 4 and res < 1e-12
+    r = A.astype(np.complex128) @ x - b
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-12
+
+
+@pytest.mark.parametrize("n", [1101, 2600])
+def test_mixed_symmetric_path(n):
+    """a complex-symmetric matrix up to a 1e-6 perturbation: the mixed solve uses the symmetric
+    factorisation (diagonal-block LU from the lower triangle, L21 products only, updates of
+    the lower triangle with lower-triangle tiles in the trailing update -- two outer blocks
+    for n = 2600, odd last panel for both sizes) and refines to an FP64 residual without
+    handing over to an LU"""
+    import torch
+    ctx = bg.get_context(0)
+    rng = np.random.default_rng(21)
+    R = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    A = (R + R.T) / 2 + 4 * n ** 0.5 * np.eye(n)
+    A = A + 1e-6 * (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)))
+    A = A.astype(np.complex64)
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda().T
+    ctx.prof_enable(True)
+    try:
+        x, it, res = bg.solve(At, b, precision=bg.MIXED, tol=1e-12, ctx=ctx)
+        prof = ctx.prof_read()
+    finally:
+        ctx.prof_enable(False)
+    assert ctx.last_factor_mode() == 2
+    assert "lu_laswp" not in prof and "lu_trsm" not in prof
+    assert prof["lu_panel"][1] == (n + 63) // 64
+    assert it <= 5 and res < 1e-12
     r = A.astype(np.complex128) @ x - b
     assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-12
