@@ -482,11 +482,12 @@ __device__ __forceinline__ int pidx(int c) {  // conflict-free index of the publ
   return c + (c >> 2);
 }
 
-// sym = 1: only the lower triangle of the block is current (symmetric updates); the upper
-// one is taken from it by symmetry.
-template <typename T>
-__global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0, int kb, int* info, T* inv,
-                                                  int sym) {
+// SYM: only the lower triangle of the block is current (symmetric updates); the upper one
+// is taken from it by symmetry, the elimination on U^T is skipped and, U = D L^T,
+// U^{-1} = (L^{-1})^T D^{-1} is formed from L^{-1} and the pivots at the end.
+template <typename T, bool SYM>
+__global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0, int kb, int* info, T* inv) {
+  constexpr bool sym = SYM;
   constexpr int LD = TRI + 1, PL = TRI + TRI / 4;
   extern __shared__ unsigned char smraw[];
   T* Ls = reinterpret_cast<T*>(smraw);  // 64 x LD: staging, then the L factor, then Linv
@@ -518,7 +519,7 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
       p1[0][pidx<T>(c0 + j)] = (c0 + j == 0) ? zero : s1[0][j];
-      p2[0][pidx<T>(c0 + j)] = s2[0][j];
+      if (!SYM) p2[0][pidx<T>(c0 + j)] = s2[0][j];
     }
   if (cb == 0)
 #pragma unroll
@@ -556,7 +557,7 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
               cfms(s1[i][j], l1[i], q1[j]);
-              cfms(s2[i][j], l2[i], q2[j]);
+              if (!SYM) cfms(s2[i][j], l2[i], q2[j]);
             }
             if (cb == kq) {  // column k: L^{-1}[r][k] = -l, and the L factor
               s1[i][kk].x = -l1[i].x;
@@ -565,7 +566,7 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
             }
           }
       }
-      if (rb == kq)  // row k of X is final
+      if (!SYM && rb == kq)  // row k of X is final
 #pragma unroll
         for (int j = 0; j < 4; ++j) s2[kk][j] = cmulx(s2[kk][j], d);
       // publish step k + 1
@@ -575,7 +576,7 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
             p1[bn][pidx<T>(c0 + j)] = (c0 + j == kn) ? zero : s1[in][j];
-            p2[bn][pidx<T>(c0 + j)] = s2[in][j];
+            if (!SYM) p2[bn][pidx<T>(c0 + j)] = s2[in][j];
           }
         if (cb == qn)
 #pragma unroll
@@ -602,7 +603,28 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
   }
   __syncthreads();
   // Linv (column-major, inv[c * 64 + r] = Linv[r][c]) through Ls; Uinv = X^T, so row r of X
-  // is column r of Uinv (inv[4096 + r * 64 + c] = X[r][c]), written by the tile owners
+  // is column r of Uinv (inv[4096 + r * 64 + c] = X[r][c]), written by the tile owners;
+  // symmetric: X[r][c] = Linv[r][c] / d_r
+  if (SYM) {
+    __shared__ T s_dinv[TRI];
+    if (rb == cb)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        T di;
+        crecip(s1[i][i], di);  // nonzero: the elimination checked every pivot
+        s_dinv[r0 + i] = di;
+      }
+    __syncthreads();
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      const T di = s_dinv[r0 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int r = r0 + i, c = c0 + j;
+        s2[i][j] = c < r ? cmulx(s1[i][j], di) : (c == r ? di : zero);
+      }
+    }
+  }
 #pragma unroll
   for (int i = 0; i < 4; ++i)
 #pragma unroll
@@ -1805,7 +1827,8 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   sym = sym && apply_path;
   const size_t getrf_sm = (size_t)TRI * (TRI + 1) * sizeof(T);
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_getrf64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
-  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
   if (apply_path)
     BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)panel_apply_smem()));
@@ -1875,8 +1898,10 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
         constexpr int NS = TrsmTile<T>::NS;
         const int64_t rb = n - j0 - kb;
         T* dblk = apply_path ? reinterpret_cast<T*>(lu_dinv(ipiv, n)) + (j0 / TRI) * 2 * TRI * TRI : nullptr;
-        if (apply_path)
-          k_lu_inv64<T><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk, sym ? 1 : 0);
+        if (apply_path && sym)
+          k_lu_inv64<T, true><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk);
+        else if (apply_path)
+          k_lu_inv64<T, false><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk);
         else
           k_getrf64<T><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo);
         if (apply_path && kb == TRI && rb > 0) {
