@@ -51,8 +51,13 @@ class Context:
         except Exception:
             pass
 
-    def prof_enable(self, on=True):
-        self.check(self.lib.beast_prof_enable(self.handle, 1 if on else 0))
+    def prof_enable(self, on=True, kinds=None):
+        """start (or stop) recording; kinds: names of L.PROF_KINDS to record (default all)"""
+        if on and kinds is not None:
+            mask = sum(1 << L.PROF_KINDS.index(k) for k in kinds)
+            self.check(self.lib.beast_prof_enable_kinds(self.handle, mask))
+        else:
+            self.check(self.lib.beast_prof_enable(self.handle, 1 if on else 0))
 
     def prof_read(self):
         """{kind: (ms, launches, work)} for the records since prof_enable"""

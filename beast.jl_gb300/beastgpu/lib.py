@@ -43,7 +43,7 @@ EXPORTS = [
     "beast_mesh_free", "beast_space_upload", "beast_space_free", "beast_assemble",
     "beast_assemble_block", "beast_assemble_local", "beast_rhs_planewave", "beast_lu_factor", "beast_lu_solve",
     "beast_lu_free", "beast_lu_solve_noalloc", "beast_solve_dense", "beast_gmres", "beast_farfield", "beast_solve_job",
-    "beast_prof_enable", "beast_prof_read", "beast_prof_launches", "beast_last_factor_mode", "beast_version",
+    "beast_prof_enable", "beast_prof_enable_kinds", "beast_prof_read", "beast_prof_launches", "beast_last_factor_mode", "beast_version",
 ]
 
 
@@ -94,6 +94,7 @@ def load(build_if_needed=True):
                                   C.POINTER(C.c_double)]
     L.beast_prof_launches.argtypes = [vp, C.POINTER(C.c_int64)]
     L.beast_last_factor_mode.argtypes = [vp, C.POINTER(C.c_int)]
+    L.beast_prof_enable_kinds.argtypes = [vp, C.c_uint]
     L.beast_version.restype = C.c_char_p
     for name in EXPORTS:
         if name != "beast_version":

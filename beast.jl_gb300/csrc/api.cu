@@ -25,7 +25,7 @@ static cudaEvent_t ev_get(beast_ctx* c) {
 
 ProfScope::ProfScope(beast_ctx* c, int k, double w, int nlaunch) : ctx(c), kind(k), work(w) {
   ctx->launches += nlaunch;
-  if (ctx->prof_on) {
+  if (ctx->prof_on && ((ctx->prof_mask >> kind) & 1u)) {
     a = ev_get(ctx);
     cudaEventRecord(a, ctx->stream);
   }
@@ -179,8 +179,15 @@ int beast_prof_enable(beast_ctx* ctx, int on) {
   }
   ctx->prof.clear();
   ctx->prof_on = on != 0;
+  ctx->prof_mask = 0xffffffffu;
   ctx->launches = 0;
   return BEAST_OK;
+}
+
+int beast_prof_enable_kinds(beast_ctx* ctx, unsigned int mask) {
+  int rc = beast_prof_enable(ctx, mask != 0);
+  if (rc == BEAST_OK) ctx->prof_mask = mask;
+  return rc;
 }
 
 int beast_prof_read(beast_ctx* ctx, int kind, double* ms, int64_t* launches, double* work) {

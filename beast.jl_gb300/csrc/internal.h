@@ -41,6 +41,7 @@ struct beast_ctx {
   int* d_flag = nullptr;  // device error / status word
   // profiler: CUDA events around instrumented launches on `stream`
   bool prof_on = false;
+  uint32_t prof_mask = 0xffffffffu;  // kinds recorded while prof_on
   std::vector<ProfRec> prof;
   std::vector<cudaEvent_t> evpool;
   int64_t launches = 0;   // kernels launched by this context (counted always)

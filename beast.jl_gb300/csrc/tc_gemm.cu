@@ -430,68 +430,78 @@ __device__ __forceinline__ void convert_bh(int bid, const float2* B, int64_t lda
   }
 }
 
-// B' of a symmetric update, B = D L^T: column j of B' is row j of L (K complex, read through
-// shared memory in 32 x 64 tiles: coalesced along the rows of L) times the pivots d_k =
-// Mat[colA + k, colA + k], scaled by t_j (largest |re|, |im| of the column into [2^13, 2^14)).
-// A CTA takes 32 columns of B'.  L: the block of rows rowB.., columns colA.. of Mat.
-__device__ __forceinline__ void convert_bt(int bid, const float2* L, const float2* dg, int64_t lda, int K, int N,
-                                           __half2* Bp, float* inv_sb) {
-  __shared__ float red[8][33];
+// Both FP16 operands of a symmetric update C[r0.., r0..] -= L D L^T from the same rows of L
+// (M x K at L, ld lda; B' takes the first N <= M of them), D the pivots dg[k (lda + 1)]:
+//   A' rows 2m, 2m+1 = [[re, -im], [im, re]] of L[m][k] times s_m (as expand_h),
+//   B' column m = d_k L[m][k] times t_m (m < N);
+// s_m, t_m put the largest |re|, |im| of the row of L resp. D-scaled row into [2^13, 2^14).
+// A CTA takes 32 rows: one pass for both maxima, one pass through 32 x 64 shared-memory tiles
+// (coalesced along the rows of L) writing both operands; the pivots are staged once.
+__global__ void __launch_bounds__(256) k_prep_sym(const float2* L, const float2* dg, int64_t lda, int M, int N, int K,
+                                                  __half2* Ap, float* inv_sa, __half2* Bp, float* inv_sb) {
+  __shared__ float red[2][8][33];
   __shared__ float2 tile[32][65];
-  __shared__ float s_scale[32];
+  __shared__ float s_sa[32], s_sb[32];
+  __shared__ float2 s_d[1024];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int j0 = bid * 32, j = j0 + lane;
-  auto dk = [&](int k) { return dg[(int64_t)k * (lda + 1)]; };
-  float mx = 0.f;
-  if (j < N)
+  const int m0 = blockIdx.x * 32, m = m0 + lane;
+  for (int k = threadIdx.x; k < K; k += 256) s_d[k] = dg[(int64_t)k * (lda + 1)];
+  __syncthreads();
+  float ma = 0.f, mb = 0.f;
+  if (m < M)
     for (int k = w; k < K; k += 8) {
-      const float2 a = L[j + (int64_t)k * lda], d = dk(k);
+      const float2 a = L[m + (int64_t)k * lda], d = s_d[k];
       const float re = a.x * d.x - a.y * d.y, im = a.x * d.y + a.y * d.x;
-      mx = fmaxf(mx, fmaxf(fabsf(re), fabsf(im)));
+      ma = fmaxf(ma, fmaxf(fabsf(a.x), fabsf(a.y)));
+      mb = fmaxf(mb, fmaxf(fabsf(re), fabsf(im)));
     }
-  red[w][lane] = mx;
+  red[0][w][lane] = ma;
+  red[1][w][lane] = mb;
   __syncthreads();
   if (w == 0) {
-    for (int q = 1; q < 8; ++q) mx = fmaxf(mx, red[q][lane]);
-    const int sh = tc_scale_shift(mx);
-    s_scale[lane] = ldexpf(1.f, sh);
-    if (j < N) inv_sb[j] = ldexpf(1.f, -sh);
+    for (int q = 1; q < 8; ++q) {
+      ma = fmaxf(ma, red[0][q][lane]);
+      mb = fmaxf(mb, red[1][q][lane]);
+    }
+    const int sha = tc_scale_shift(ma), shb = tc_scale_shift(mb);
+    s_sa[lane] = ldexpf(1.f, sha);
+    s_sb[lane] = ldexpf(1.f, shb);
+    if (m < M) inv_sa[m] = ldexpf(1.f, -sha);
+    if (m < N) inv_sb[m] = ldexpf(1.f, -shb);
   }
   __syncthreads();
   for (int k0 = 0; k0 < K; k0 += 64) {
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       const int k = k0 + w + 8 * q;
-      tile[lane][w + 8 * q] = (j < N && k < K) ? L[j + (int64_t)k * lda] : make_float2(0.f, 0.f);
+      tile[lane][w + 8 * q] = (m < M && k < K) ? L[m + (int64_t)k * lda] : make_float2(0.f, 0.f);
     }
     __syncthreads();
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
-      const int jr = w + 8 * i, jc = j0 + jr;
-      if (jc < N) {
-        const float sc = s_scale[jr];
-        __half2* col = Bp + (int64_t)jc * K;
+      const int r = w + 8 * i, mr = m0 + r;
+      if (mr < M) {
+        const float sa = s_sa[r], sb = s_sb[r];
+        __half2* row0 = Ap + (int64_t)(2 * mr) * K;
+        __half2* row1 = row0 + K;
+        __half2* col = Bp + (int64_t)mr * K;
 #pragma unroll
         for (int hh = 0; hh < 2; ++hh) {
           const int kk = lane + 32 * hh, k = k0 + kk;
           if (k < K) {
-            const float2 a = tile[jr][kk], d = dk(k);
-            col[k] = __floats2half2_rn((a.x * d.x - a.y * d.y) * sc, (a.x * d.y + a.y * d.x) * sc);
+            const float2 a = tile[r][kk];
+            row0[k] = __floats2half2_rn(a.x * sa, -a.y * sa);
+            row1[k] = __floats2half2_rn(a.y * sa, a.x * sa);
+            if (mr < N) {
+              const float2 d = s_d[k];
+              col[k] = __floats2half2_rn((a.x * d.x - a.y * d.y) * sb, (a.x * d.y + a.y * d.x) * sb);
+            }
           }
         }
       }
     }
     __syncthreads();
   }
-}
-
-__global__ void __launch_bounds__(256) k_prep_sym(const float2* A, const float2* L, const float2* dg, int64_t lda,
-                                                  int M, int N, int K, __half2* Ap, float* inv_sa, __half2* Bp,
-                                                  float* inv_sb, int nA) {
-  if ((int)blockIdx.x < nA)
-    expand_h(blockIdx.x, A, lda, M, K, Ap, inv_sa);
-  else
-    convert_bt(blockIdx.x - nA, L, dg, lda, K, N, Bp, inv_sb);
 }
 
 // both operands in one launch: CTAs [0, nA) expand 32 rows of A each, the rest convert 8
@@ -605,10 +615,10 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
   if (!u.prepped) {
     const int nA = (int)((M0 + 31) / 32);
     if (u.sym) {
-      const int nB = (int)((N + 31) / 32);
-      k_prep_sym<<<(unsigned)(nA + nB), 256, 0, st>>>(Mat + rowA + colA * lda, Mat + colB + colA * lda,
-                                                      Mat + colA + colA * lda, lda, (int)M0, (int)N, K, Ap, inv_sa,
-                                                      Bp, inv_sb, nA);
+      if (colB != rowA || N > M0 || K > 1024)
+        return beast_fail(ctx, BEAST_ERR_ARG, "symmetric update: operands must come from the same rows");
+      k_prep_sym<<<(unsigned)nA, 256, 0, st>>>(Mat + rowA + colA * lda, Mat + colA + colA * lda, lda, (int)M0,
+                                               (int)N, K, Ap, inv_sa, Bp, inv_sb);
     } else {
       const int nB = (int)((N + 7) / 8);
       k_prep_h<<<(unsigned)(nA + nB), 256, 0, st>>>(Mat + rowA + colA * lda, Mat + colA + colB * lda, lda,

@@ -44,6 +44,9 @@ def parse():
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--prof-all", action="store_true",
+                    help="bracket every kernel class with CUDA events inside the timed steps "
+                         "(default: only the roofline class; the breakdown comes from one extra step)")
     ap.add_argument("--config", default="c2", choices=["c2", "c3", "c5"],
                     help="c2: the bench line (default); c3: 256 small Helmholtz P0 jobs, jobs/s; "
                          "c5: a Poisson stream of mixed solve requests, latency p50/p99")
@@ -476,7 +479,8 @@ def main():
     if dist:
         dist.barrier()
     clk = Clocks(dev)
-    ctx.prof_enable(True)
+    # timed steps: CUDA events only around the dominant class (the roofline kernel)
+    ctx.prof_enable(True, kinds=None if args.prof_all else ["lu_tc_gemm"])
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     e0.record(stream)
@@ -486,8 +490,15 @@ def main():
     torch.cuda.synchronize()
     ms = e0.elapsed_time(e1)
     clocks = clk.stop()
-    prof = ctx.prof_read()
+    prof_timed = ctx.prof_read()
     launches = ctx.launches()
+    # per-class breakdown: one more step with every class bracketed (not timed)
+    ctx.prof_enable(True)
+    step()
+    torch.cuda.synchronize()
+    prof = {k: (v[0] * args.steps, v[1] * args.steps, v[2] * args.steps) for k, v in ctx.prof_read().items()}
+    if "lu_tc_gemm" in prof_timed:
+        prof["lu_tc_gemm"] = prof_timed["lu_tc_gemm"]
     ctx.prof_enable(False)
     if dist:
         t = torch.tensor([ms], device=f"cuda:{dev}")

@@ -234,6 +234,8 @@ int beast_solve_job(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc
  * beast_prof_read sums event time (ms), bracketed launches and algorithmic work (flops for
  * compute kinds, bytes for memory kinds) over the records since the last enable. */
 int beast_prof_enable(beast_ctx* ctx, int on);
+/* as beast_prof_enable(ctx, 1), recording only the kinds whose bit (1 << kind) is set */
+int beast_prof_enable_kinds(beast_ctx* ctx, unsigned int mask);
 int beast_prof_read(beast_ctx* ctx, int kind, double* ms, int64_t* launches, double* work);
 /* kernels launched by this context since the last beast_prof_enable (counted always) */
 int beast_prof_launches(beast_ctx* ctx, int64_t* n);
