@@ -1551,28 +1551,33 @@ __global__ void k_gemv_partial_c64_df(int64_t n, const float2* A, int64_t lda, c
 }
 
 // the same with two rows per thread: one 16-byte load brings a[i, j] and a[i+1, j] (even i,
-// even lda), and the two rows are independent accumulation chains
-__device__ __forceinline__ void cdf_acc(float ar, float ai, float4 xv, float& shr, float& slr, float& shi,
-                                        float& sli) {
-  float p, e;
-  p = __fmul_rn(ar, xv.x);
-  e = fmaf(ar, xv.x, -p);
-  two_sum_acc(shr, slr, p);
-  slr = __fadd_rn(slr, e);
-  p = __fmul_rn(-ai, xv.y);
-  e = fmaf(-ai, xv.y, -p);
-  two_sum_acc(shr, slr, p);
-  slr = __fadd_rn(slr, e);
-  slr = __fadd_rn(slr, __fsub_rn(__fmul_rn(ar, xv.z), __fmul_rn(ai, xv.w)));
-  p = __fmul_rn(ar, xv.y);
-  e = fmaf(ar, xv.y, -p);
-  two_sum_acc(shi, sli, p);
-  sli = __fadd_rn(sli, e);
-  p = __fmul_rn(ai, xv.x);
-  e = fmaf(ai, xv.x, -p);
-  two_sum_acc(shi, sli, p);
-  sli = __fadd_rn(sli, e);
-  sli = __fadd_rn(sli, __fadd_rn(__fmul_rn(ar, xv.w), __fmul_rn(ai, xv.z)));
+// even lda), and the two rows are independent accumulation chains.  The real and imaginary
+// parts of a row travel as the two lanes of packed FP32 operations (sm_100 FFMA2 / FADD2 /
+// FMUL2, each lane rounded as its scalar counterpart):
+//   (re, im) += (a_r, a_r) (x_r, x_i) + (a_i, a_i) (-x_i, x_r),
+// every product kept exactly (TwoProduct: p and fma(a, x, -p)) and added to the high part with
+// its rounding error (TwoSum); the low-part terms (x's low half) in plain FP32.
+__device__ __forceinline__ float2 sub2(float2 a, float2 b) {  // a - b, one rounding
+  return __ffma2_rn(b, make_float2(-1.f, -1.f), a);
+}
+__device__ __forceinline__ void two_sum2(float2& sh, float2& sl, float2 p) {
+  const float2 t = __fadd2_rn(sh, p);
+  const float2 bb = sub2(t, sh);
+  sl = __fadd2_rn(sl, __fadd2_rn(sub2(sh, sub2(t, bb)), sub2(p, bb)));
+  sh = t;
+}
+__device__ __forceinline__ void cdf_acc2(float2 A, float2 B, float2 X1, float2 X2, float2 L1, float2 L2, float2& sh,
+                                         float2& sl) {
+  float2 p = __fmul2_rn(A, X1);
+  float2 e = __ffma2_rn(A, X1, make_float2(-p.x, -p.y));
+  two_sum2(sh, sl, p);
+  sl = __fadd2_rn(sl, e);
+  p = __fmul2_rn(B, X2);
+  e = __ffma2_rn(B, X2, make_float2(-p.x, -p.y));
+  two_sum2(sh, sl, p);
+  sl = __fadd2_rn(sl, e);
+  sl = __ffma2_rn(A, L1, sl);
+  sl = __ffma2_rn(B, L2, sl);
 }
 __global__ void k_gemv_partial_c64_df2(int64_t n, const float2* A, int64_t lda, const float4* xs,
                                        double* part) {
@@ -1581,9 +1586,12 @@ __global__ void k_gemv_partial_c64_df2(int64_t n, const float2* A, int64_t lda, 
   const int64_t c0 = n * s / MV_SLABS, c1 = n * (s + 1) / MV_SLABS;
   if (i >= n) return;
   const bool two = i + 1 < n;
-  float h0r = 0.f, l0r = 0.f, h0i = 0.f, l0i = 0.f, h1r = 0.f, l1r = 0.f, h1i = 0.f, l1i = 0.f;
+  float2 h0 = make_float2(0.f, 0.f), l0 = h0, h1 = h0, l1 = h0;
+#pragma unroll 4
   for (int64_t j = c0; j < c1; ++j) {
     const float4 xv = xs[j];
+    const float2 X1 = make_float2(xv.x, xv.y), X2 = make_float2(-xv.y, xv.x);
+    const float2 L1 = make_float2(xv.z, xv.w), L2 = make_float2(-xv.w, xv.z);
     float4 a;
     if (two) {
       a = *reinterpret_cast<const float4*>(A + i + j * lda);
@@ -1591,14 +1599,14 @@ __global__ void k_gemv_partial_c64_df2(int64_t n, const float2* A, int64_t lda, 
       const float2 a0 = A[i + j * lda];
       a = make_float4(a0.x, a0.y, 0.f, 0.f);
     }
-    cdf_acc(a.x, a.y, xv, h0r, l0r, h0i, l0i);
-    cdf_acc(a.z, a.w, xv, h1r, l1r, h1i, l1i);
+    cdf_acc2(make_float2(a.x, a.x), make_float2(a.y, a.y), X1, X2, L1, L2, h0, l0);
+    cdf_acc2(make_float2(a.z, a.z), make_float2(a.w, a.w), X1, X2, L1, L2, h1, l1);
   }
-  part[2 * (s * n + i)] = (double)h0r + (double)l0r;
-  part[2 * (s * n + i) + 1] = (double)h0i + (double)l0i;
+  part[2 * (s * n + i)] = (double)h0.x + (double)l0.x;
+  part[2 * (s * n + i) + 1] = (double)h0.y + (double)l0.y;
   if (two) {
-    part[2 * (s * n + i + 1)] = (double)h1r + (double)l1r;
-    part[2 * (s * n + i + 1) + 1] = (double)h1i + (double)l1i;
+    part[2 * (s * n + i + 1)] = (double)h1.x + (double)l1.x;
+    part[2 * (s * n + i + 1) + 1] = (double)h1.y + (double)l1.y;
   }
 }
 
