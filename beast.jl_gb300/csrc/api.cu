@@ -837,6 +837,23 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
   const int fdt = mixed ? BEAST_C64 : BEAST_C128;
   const size_t fel = mixed ? 8 : 16;
   void* F = nullptr;
+  {
+    // the assembly workspace (kept by the context) and the device pool's freed blocks stay
+    // mapped; when the factor copy would not fit next to them, hand them back first (the
+    // next assembly grows its workspace again)
+    size_t fr = 0, tot = 0;
+    const size_t want = (size_t)n * n * fel + ((size_t)1 << 31);
+    if (cudaMemGetInfo(&fr, &tot) == cudaSuccess && fr < want) {
+      cudaMemPool_t pool;
+      BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+      if (ctx->ws) {
+        cudaFree(ctx->ws);
+        ctx->ws = nullptr;
+        ctx->ws_size = 0;
+      }
+      if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
+    }
+  }
   BEAST_CUDA_TRY(ctx, cudaMallocAsync(&F, (size_t)n * n * fel, st));
   double *r = nullptr, *d = nullptr, *nrm = nullptr;
   float* d32 = nullptr;

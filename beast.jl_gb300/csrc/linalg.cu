@@ -1821,14 +1821,19 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   cudaStream_t st = ctx->stream;
   const int G0 = std::max(1, ctx->num_sms);
   const size_t smem_cap = 220 * 1024;
+  // panel width: 64; with pivoting the cooperative panel kernel holds its share of the panel's
+  // rows in shared memory, which narrows the panel for very tall matrices
   int nb = 64;
-  int64_t rows0 = (n + G0 - 1) / G0;
-  while (nb > 8 && (size_t)(rows0 * (nb + 1) + nb) * sizeof(T) > smem_cap) nb /= 2;
-  if ((size_t)(rows0 * (nb + 1) + nb) * sizeof(T) > smem_cap)
-    return beast_fail(ctx, BEAST_ERR_ARG, "matrix too large for the shared-memory panel");
+  const int64_t rows0 = (n + G0 - 1) / G0;
+  if (pivot) {
+    while (nb > 8 && (size_t)(rows0 * (nb + 1) + nb) * sizeof(T) > smem_cap) nb /= 2;
+    if ((size_t)(rows0 * (nb + 1) + nb) * sizeof(T) > smem_cap)
+      return beast_fail(ctx, BEAST_ERR_ARG, "matrix too large for the shared-memory panel");
+  }
   const int NB = 16 * nb;
   const size_t panel_smem = (size_t)(rows0 * (nb + 1) + nb) * sizeof(T);
-  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
+  if (pivot)
+    BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
   // unpivoted c64 with 64-wide panels: k_lu_inv64 also inverts the block's triangles and
   // k_panel_apply does both triangular solves (and the FP16 operands of the in-block update)
   const bool apply_path = !pivot && sizeof(T) == 8 && nb == TRI;
@@ -1844,9 +1849,11 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
                                            (int)trsm_tile_smem<T>()));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_tile<T, R, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)trsm_tile_smem<T>()));
-  int occ = 0;
-  BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_panel<T>, 256, panel_smem));
-  if (occ < 1) return beast_fail(ctx, BEAST_ERR_CUDA, "panel kernel does not fit on an SM");
+  if (pivot) {
+    int occ = 0;
+    BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_panel<T>, 256, panel_smem));
+    if (occ < 1) return beast_fail(ctx, BEAST_ERR_CUDA, "panel kernel does not fit on an SM");
+  }
   size_t need = 2 * G0 * sizeof(double) + 2 * G0 * sizeof(int) + (2 * (size_t)G0 * nb + 2 * nb) * sizeof(T) +
                 8 * sizeof(unsigned int) + 256;
   char* scr = nullptr;
