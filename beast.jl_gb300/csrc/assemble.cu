@@ -991,6 +991,14 @@ DEV bool near_is_ss32(const NearParams& P, int cls) {
          (P.op.kind == BEAST_MW_SL || (P.op.kind == BEAST_MW_DL && cls != 3));
 }
 
+// sh + sl += p, the rounding error of the addition kept (Knuth's TwoSum; no contraction)
+__device__ __forceinline__ void two_sum_f(float& sh, float& sl, float p) {
+  const float t = __fadd_rn(sh, p);
+  const float bb = __fsub_rn(t, sh);
+  sl = __fadd_rn(sl, __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bb)), __fsub_rn(p, bb)));
+  sh = t;
+}
+
 __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss32(NearParams P) {
   __shared__ float s_glxf[210], s_glwf[210];
   for (int k = threadIdx.x; k < 210; k += blockDim.x) {
@@ -1006,17 +1014,23 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss32(NearParams P) {
   const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
   const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
   {
-    // ---- Sauter-Schwab: shared vertices first, same order (SauterSchwabQuadrature.reorder)
+    // ---- Sauter-Schwab: shared vertices first, same order (SauterSchwabQuadrature.reorder).
+    // Lanes 0..8 test one vertex pair each (i = lane / 3, j = lane % 3; squared distances:
+    // shared vertices coincide exactly); the first three hits in (i, j) order from the ballot.
+    // (FP64 is a small fraction of the FP32 rate: per-pair FP64 work is spread over lanes.)
     const double dtol = 1.0e3 * 2.220446049250313e-16;
+    bool hit = false;
+    if (lane < 9) {
+      const V3<double> dd = t.v[lane / 3] - s.v[lane % 3];
+      hit = dot(dd, dd) < dtol * dtol;
+    }
+    const unsigned hmask = __ballot_sync(0xffffffffu, hit);
     int pt[3], ps[3], hits = 0, ti[3], si[3];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        V3<double> dd = t.v[i] - s.v[j];
-        if (sqrt(dot(dd, dd)) < dtol && hits < 3) {
-          ti[hits] = i;
-          si[hits] = j;
-          ++hits;
-        }
+    for (int b = 0; b < 9; ++b)
+      if (((hmask >> b) & 1u) && hits < 3) {
+        ti[hits] = b / 3;
+        si[hits] = b % 3;
+        ++hits;
       }
     int k = 0;
     for (int h = 0; h < hits; ++h) pt[k++] = ti[h];
@@ -1059,11 +1073,13 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss32(NearParams P) {
         const float gif = (float)gi, grf = (float)gr;
         const float* glxf = s_glxf + c_gl_off[n - 1];
         const float* glwf = s_glwf + c_gl_off[n - 1];
-        // FP32 partial moments over at most 16 points, flushed into the FP64 moments m[] so
-        // that the FP32 rounding of the sums stays at the level of a 16-term sum
-        float mf[22];
+        // FP32 partial moments over at most 16 points, flushed into double-float moments
+        // (mh + ml, the rounding error of each addition kept by TwoSum) so that the FP32
+        // rounding of the sums stays at the level of a 16-term sum -- without FP64
+        // arithmetic in the point loop (the FP64 pipe is a small fraction of the FP32 rate)
+        float mf[22], mh[22], ml[22];
 #pragma unroll
-        for (int k = 0; k < 22; ++k) mf[k] = 0.0f;
+        for (int k = 0; k < 22; ++k) mf[k] = mh[k] = ml[k] = 0.0f;
         int cnt = 0;
         for (int it = lane; it < (int)items; it += 32) {
           float X[2], Y[2], D[2], w;
@@ -1110,44 +1126,46 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss32(NearParams P) {
           if (++cnt == 16) {
 #pragma unroll
             for (int k = 0; k < 22; ++k) {
-              m[k] += (double)mf[k];
+              two_sum_f(mh[k], ml[k], mf[k]);
               mf[k] = 0.0f;
             }
             cnt = 0;
           }
         }
+        // the lanes' double-float moments summed across the warp in FP32 pairs (TwoSum per
+        // level), then one conversion to FP64
 #pragma unroll
-        for (int k = 0; k < 22; ++k) m[k] += (double)mf[k];
+        for (int k = 0; k < 22; ++k) {
+          two_sum_f(mh[k], ml[k], mf[k]);
+#pragma unroll
+          for (int o = 16; o > 0; o >>= 1) {
+            const float oh = __shfl_xor_sync(0xffffffffu, mh[k], o), ol = __shfl_xor_sync(0xffffffffu, ml[k], o);
+            two_sum_f(mh[k], ml[k], oh);
+            ml[k] = __fadd_rn(ml[k], ol);
           }
-#pragma unroll
-      for (int k = 0; k < 22; ++k) {
-        double v = m[k];
-        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-        m[k] = v;
-      }
+          m[k] = (double)mh[k] + (double)ml[k];
+        }
+          }
       const C2<double> M0{m[0], m[1]}, M1{m[2], m[3]};
       CV<double> V1, V2, V3_;
       V1.x = {m[4], m[5]}; V1.y = {m[6], m[7]}; V1.z = {m[8], m[9]};
       V2.x = {m[10], m[11]}; V2.y = {m[12], m[13]}; V2.z = {m[14], m[15]};
       V3_.x = {m[16], m[17]}; V3_.y = {m[18], m[19]}; V3_.z = {m[20], m[21]};
-      if (lane == 0) {
+      if (lane < 9) {  // lane 3 i + j: entry (i, j) of the 3 x 3 block
         const C2<double> al{P.op.ar, P.op.ai}, be{P.op.br, P.op.bi};
-        for (int i = 0; i < 3; ++i) {
-          const V3<double> ti = t.v[i] - cp;
-          for (int j = 0; j < 3; ++j) {
-            const V3<double> sj = s.v[j] - cq;
-            C2<double> z;
-            if (sl) {
-              C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
-              fm = cadd(fm, cscale(dot(ti, sj), M0));
-              z = cadd(cmul(al, fm), cscale(4.0, cmul(be, M0)));
-            } else {
-              C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
-              z = cadd(fm, rdot(cross(sj, ti), V3_));
-            }
-            store_c<double>(P.zcell, (int64_t)(3 * np_.q + j) * P.ldc + 3 * (int64_t)np_.p + i, z, P.c64);
-          }
+        const int i = lane / 3, j = lane % 3;
+        const V3<double> ti = t.v[i] - cp;
+        const V3<double> sj = s.v[j] - cq;
+        C2<double> z;
+        if (sl) {
+          C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
+          fm = cadd(fm, cscale(dot(ti, sj), M0));
+          z = cadd(cmul(al, fm), cscale(4.0, cmul(be, M0)));
+        } else {
+          C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
+          z = cadd(fm, rdot(cross(sj, ti), V3_));
         }
+        store_c<double>(P.zcell, (int64_t)(3 * np_.q + j) * P.ldc + 3 * (int64_t)np_.p + i, z, P.c64);
       }
   }
 }
