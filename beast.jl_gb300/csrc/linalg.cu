@@ -1763,10 +1763,10 @@ struct LUSteps {
             void* tcwork, bool prepped = false) {
     if (!gemm2_runs(m0, n0, m1, n1, k)) return BEAST_OK;
     const bool tc = gemm2_tc(m0, n0, n1, k, tcwork);
-    ProfScope ps(ctx, tc ? PK_TCGEMM : PK_GEMM, 8.0 * (double)k * ((double)m0 * n0 + (double)m1 * n1));
-    if (tc)
+    if (tc)  // brackets its operand preparation and its tensor-core launch separately
       return tc_gemm_sub(ctx, reinterpret_cast<float2*>(A), lda, r0, k0, c0, m0, n0, m1, n1, k, tcwork,
                          tcwork_bytes, prepped);
+    ProfScope ps(ctx, PK_GEMM, 8.0 * (double)k * ((double)m0 * n0 + (double)m1 * n1));
     const int64_t ms[2] = {m0, m1}, cs[2] = {c0, c0 + n0}, ns[2] = {n0, n1};
     for (int r = 0; r < 2; ++r) {
       if (ms[r] <= 0 || ns[r] <= 0) continue;
@@ -1787,10 +1787,10 @@ struct LUSteps {
               bool prepped = false) {
     if (m <= 0 || nc <= 0 || k <= 0) return BEAST_OK;
     const bool tc = symgemm_tc(m, nc, k, tcwork);
-    ProfScope ps(ctx, tc ? PK_TCGEMM : PK_GEMM, 8.0 * (double)k * (double)m * nc * (lower ? 0.5 : 1.0));
-    if (tc)
+    if (tc)  // brackets its operand preparation and its tensor-core launch separately
       return tc_gemm_sym(ctx, reinterpret_cast<float2*>(A), lda, rowA, colA, rowB, m, nc, k, lower, tcwork,
                          tcwork_bytes, prepped);
+    ProfScope ps(ctx, PK_GEMM, 8.0 * (double)k * (double)m * nc);
     T* B = nullptr;
     BEAST_CUDA_TRY(ctx, cudaMallocAsync(&B, (size_t)k * nc * sizeof(T), st));
     const int64_t tot = (int64_t)k * nc;

@@ -697,6 +697,8 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
   __half2* Ap = static_cast<__half2*>(Apv);
   __half2* Bp = static_cast<__half2*>(Bpv);
   if (!u.prepped) {
+    // FP16 operands: A read and A' written (2 x 4 B per complex element), B read and B' written
+    ProfScope ps(ctx, PK_CONVERT, (double)M0 * K * 16.0 + (double)N * K * 12.0);
     const int nA = (int)((M0 + 31) / 32);
     if (u.sym) {
       if (colB != rowA || N > M0 || K > 1024)
@@ -708,7 +710,7 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
       k_prep_h<<<(unsigned)(nA + nB), 256, 0, st>>>(Mat + rowA + colA * lda, Mat + colA + colB * lda, lda,
                                                     (int)M0, (int)N, K, Ap, inv_sa, Bp, inv_sb, nA);
     }
-    ctx->launches += 1;
+    BEAST_CUDA_TRY(ctx, cudaGetLastError());
   }
   CUtensorMap tmA, tmB, tmC0, tmC1;
   // A': 2K halves per row (x), 2 M0 rows (y); B': 2K halves per column (x), N columns (y)
@@ -759,6 +761,9 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
   }
   if (Rg.ntiles == 0) return BEAST_OK;
   const int nk = (2 * K) / TK;
+  // algorithmic work: 8 K per complex element of the region (the lower triangle: half the square)
+  ProfScope ps(ctx, PK_TCGEMM,
+               8.0 * K * (u.lower ? 0.5 * (double)M0 * N0 : (double)M0 * N0 + (double)M1 * N1));
   if (pair) {
     const int ncl = std::min(Rg.ntiles, pair_clusters[dev]);
     cudaLaunchConfig_t cfg = {};

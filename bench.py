@@ -563,10 +563,11 @@ def main():
         achieved = work / (kms * 1e-3) / 1e12
         peak, unit, bound = pk.get("bf16_tflops_sustained", pk["bf16_tflops"]), "TFLOP/s", "tensor"
     # DRAM traffic per launch: bytes per algorithmic flop measured by ncu on one k_tc_gemm
-    # launch (the first trailing update of the level-4 EFIE: 744 MB of DRAM traffic for
-    # 3.63e11 flops, C' read and written once by the TMA reduce-add), scaled to this run's
-    # average launch by its flops
-    traffic = 2.05e-3 * work / nl if name == "lu_tc_gemm" else None
+    # launch (the first lower-triangle trailing update of the level-4 EFIE: 400 MB of DRAM
+    # traffic for 1.81e11 flops, C' read and written once by the TMA reduce-adds), scaled to
+    # this run's average launch by its flops.  The class brackets the k_tc_gemm launches only
+    # (their FP16 operand preparation is counted as "convert").
+    traffic = 2.21e-3 * work / nl if name == "lu_tc_gemm" else None
     roof = {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak, "unit": unit,
             "frac": achieved / peak, "peak_source": src,
             "peak_note": "measured dense bf16 (sustained); the kernel runs FP16 operands with FP32 accumulation (same tensor rate as bf16)",
