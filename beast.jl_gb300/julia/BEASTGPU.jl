@@ -223,6 +223,19 @@ function solve(Z::Matrix{ComplexF64}, b::Vector{ComplexF64}; precision=FP64, tol
     return x
 end
 
+"""
+    last_factor_mode()
+
+Factorisation behind the last `solve`: 0 LU with partial pivoting, 1 unpivoted LU (mixed),
+2 symmetric LDL^T-type (mixed, near complex-symmetric matrix such as the Galerkin EFIE).
+"""
+function last_factor_mode()
+    ctx = context()
+    m = Ref{Cint}(-1)
+    check(ctx.ptr, ccall((:beast_last_factor_mode, libbeastgpu), Cint, (Ptr{Cvoid}, Ref{Cint}), ctx.ptr, m))
+    return Int(m[])
+end
+
 # device copy of a host matrix through the CUDA runtime (no CUDA.jl dependency)
 function device_copy(Z)
     p = Ref{Ptr{Cvoid}}(C_NULL)
