@@ -1001,6 +1001,8 @@ __device__ __forceinline__ void two_sum_f(float& sh, float& sl, float p) {
 
 __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss32(NearParams P) {
   __shared__ float s_glxf[210], s_glwf[210];
+  __shared__ float2 s_mom[NEAR_WARPS][22][33];  // per warp: each lane's double-float moments
+  __shared__ double s_tot[NEAR_WARPS][22];      // the warp's totals
   for (int k = threadIdx.x; k < 210; k += blockDim.x) {
     s_glxf[k] = (float)c_gl_x[k];
     s_glwf[k] = (float)c_gl_w[k];
@@ -1132,19 +1134,26 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss32(NearParams P) {
             cnt = 0;
           }
         }
-        // the lanes' double-float moments summed across the warp in FP32 pairs (TwoSum per
-        // level), then one conversion to FP64
+        // the lanes' double-float moments through shared memory: lane k < 22 sums moment k
+        // over the 32 lanes (TwoSum) and converts it to FP64 once
 #pragma unroll
         for (int k = 0; k < 22; ++k) {
           two_sum_f(mh[k], ml[k], mf[k]);
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) {
-            const float oh = __shfl_xor_sync(0xffffffffu, mh[k], o), ol = __shfl_xor_sync(0xffffffffu, ml[k], o);
-            two_sum_f(mh[k], ml[k], oh);
-            ml[k] = __fadd_rn(ml[k], ol);
-          }
-          m[k] = (double)mh[k] + (double)ml[k];
+          s_mom[warp][k][lane] = make_float2(mh[k], ml[k]);
         }
+        __syncwarp();
+        if (lane < 22) {
+          float th = 0.0f, tl = 0.0f;
+          for (int l = 0; l < 32; ++l) {
+            const float2 v = s_mom[warp][lane][l];
+            two_sum_f(th, tl, v.x);
+            tl = __fadd_rn(tl, v.y);
+          }
+          s_tot[warp][lane] = (double)th + (double)tl;
+        }
+        __syncwarp();
+#pragma unroll
+        for (int k = 0; k < 22; ++k) m[k] = s_tot[warp][k];
           }
       const C2<double> M0{m[0], m[1]}, M1{m[2], m[3]};
       CV<double> V1, V2, V3_;
