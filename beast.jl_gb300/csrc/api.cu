@@ -789,7 +789,10 @@ static int factor_copy(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, in
                        int fdt, bool pivot, bool sym, beast_lu** out) {
   cudaStream_t st = ctx->stream;
   if (fdt == BEAST_C64) {
-    if (a_dtype == BEAST_C64)
+    if (a_dtype == BEAST_C64 && sym) {  // the symmetric factorisation reads the block-lower part only
+      ProfScope ps(ctx, PK_CONVERT, (double)n * n * 8);
+      BEAST_CUDA_TRY(ctx, copy_lower_c64(n, A, lda, F, n, st));
+    } else if (a_dtype == BEAST_C64)
       BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(F, n * 8, A, lda * 8, n * 8, n, cudaMemcpyDeviceToDevice, st));
     else {
       ProfScope ps(ctx, PK_CONVERT, (double)n * n * 24);

@@ -1082,6 +1082,23 @@ __global__ void k_asym_sample(const T* A, int64_t lda, int64_t n, int64_t s, dou
   }
 }
 
+// copy of the block-lower part of a c64 matrix: column j from row 64 floor(j / 64) down (what
+// the symmetric factorisation reads; the rest of the copy is written at its end).  Two rows
+// per thread (16-byte accesses when lda and ldf are even and the bases 16-byte aligned).
+__global__ void k_copy_lower_c64(int64_t n, const float2* A, int64_t lda, float2* F, int64_t ldf, int vec) {
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+    const int64_t r0 = (j / 64) * 64;
+    const int64_t i = r0 + 2 * (blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
+    if (i >= n) continue;
+    if (vec && i + 1 < n)
+      *reinterpret_cast<float4*>(F + i + j * ldf) = *reinterpret_cast<const float4*>(A + i + j * lda);
+    else {
+      F[i + j * ldf] = A[i + j * lda];
+      if (i + 1 < n) F[i + 1 + j * ldf] = A[i + 1 + j * lda];
+    }
+  }
+}
+
 // ---- C -= A B  (complex; C m x n, A m x k, B k x n; all column-major with ld) -------------
 constexpr int GT = 64, GK = 8;
 template <typename T, typename R>
@@ -2140,6 +2157,17 @@ cudaError_t gemv_dev(int64_t n, const void* A, int64_t lda, int a_c64, const dou
   e = cudaGetLastError();
   cudaFreeAsync(part, st);
   return e;
+}
+
+cudaError_t copy_lower_c64(int64_t n, const void* A, int64_t lda, void* F, int64_t ldf, cudaStream_t st) {
+  const int vec = (lda % 2 == 0 && ldf % 2 == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0 &&
+                   (reinterpret_cast<uintptr_t>(F) & 15) == 0)
+                      ? 1
+                      : 0;
+  // grid.x covers the longest column (n rows, two per thread); shorter columns exit early
+  dim3 g((unsigned)((n + 511) / 512), (unsigned)std::min<int64_t>(n, 65535));
+  k_copy_lower_c64<<<g, 256, 0, st>>>(n, (const float2*)A, lda, (float2*)F, ldf, vec);
+  return cudaGetLastError();
 }
 
 cudaError_t convert_c128_to_c64(int64_t rows, int64_t cols, const double* src, int64_t lds, float* dst,
