@@ -12,7 +12,7 @@ from . import build as _build
 _LIB = None
 
 OK, ERR_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_NOCONV, ERR_SINGULAR, ERR_UNSUPPORTED = range(8)
-FP64, MIXED = 0, 1
+FP64, MIXED, MIXED_ACCURATE = 0, 1, 2
 C128, C64 = 0, 1
 HOST, DEVICE = 0, 1
 PROF_KINDS = ["geometry", "far", "near", "gather", "local", "rhs", "farfield", "lu_panel",

@@ -541,7 +541,9 @@ int beast_assemble(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc*
                    double cr, double ci, int accumulate) {
   ARG_CHECK(ctx, ctx && op && qs && ts && bs && Z, "null argument");
   ARG_CHECK(ctx, ts->mesh == bs->mesh, "test and trial spaces must share the mesh");
-  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED, "unknown precision");
+  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
+            "unknown precision");
+  if (precision == BEAST_MIXED_ACCURATE) precision = BEAST_FP64;  // assembly in FP64
   ARG_CHECK(ctx, z_dtype == BEAST_C128 || z_dtype == BEAST_C64, "unknown matrix dtype");
   ARG_CHECK(ctx, row_off >= 0 && col_off >= 0 && ldz >= row_off + ts->nfuncs, "bad Z addressing");
   ARG_CHECK(ctx, op->kind >= BEAST_MW_SL && op->kind <= BEAST_HH_DLT, "unknown operator kind");
@@ -960,7 +962,9 @@ int beast_solve_dense(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int
                       int precision, const double* b, double* x, int64_t nrhs, int bx_loc,
                       double tol, int maxiter, int* iters, double* resid) {
   ARG_CHECK(ctx, ctx && A && b && x && n > 0 && lda >= n && nrhs >= 1, "invalid solve arguments");
-  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED, "unknown precision");
+  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
+            "unknown precision");
+  if (precision == BEAST_MIXED_ACCURATE) precision = BEAST_MIXED;  // mixed factorisation
   if (set_device(ctx)) return BEAST_ERR_CUDA;
   if (maxiter <= 0) maxiter = 30;
   if (tol <= 0) tol = 1e-12;
@@ -1098,7 +1102,10 @@ int beast_solve_job(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc
   if (set_device(ctx)) return BEAST_ERR_CUDA;
   cudaStream_t st = ctx->stream;
   const int64_t n = space->nfuncs;
+  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
+            "unknown precision");
   const int dt = precision == BEAST_MIXED ? BEAST_C64 : BEAST_C128;
+  const int solve_prec = precision == BEAST_MIXED_ACCURATE ? BEAST_MIXED : precision;
   const size_t el = dt == BEAST_C64 ? 8 : 16;
   void* Z = nullptr;
   double *b = nullptr, *dx = nullptr;
@@ -1116,7 +1123,7 @@ int beast_solve_job(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc
     if (e != cudaSuccess) rc = beast_fail(ctx, BEAST_ERR_CUDA, cudaGetErrorString(e));
   }
   if (rc == BEAST_OK)
-    rc = solve_dense_device(ctx, n, Z, n, dt, precision, b, dx, 1, tol > 0 ? tol : 1e-12, 30, iters, resid);
+    rc = solve_dense_device(ctx, n, Z, n, dt, solve_prec, b, dx, 1, tol > 0 ? tol : 1e-12, 30, iters, resid);
   if (rc == BEAST_OK || rc == BEAST_ERR_NOCONV) {
     if (x_loc == BEAST_DEVICE)
       cudaMemcpyAsync(x, dx, n * 16, cudaMemcpyDeviceToDevice, st);

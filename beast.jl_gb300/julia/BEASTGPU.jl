@@ -23,7 +23,7 @@ const libbeastgpu = get(ENV, "BEASTGPU_LIB", joinpath(@__DIR__, "..", "beastgpu"
 const MW_SL, MW_DL, MW_NXDL, HH_SL, HH_DL, HH_DLT = 1, 2, 3, 4, 5, 6
 const P0, P1, RT = 0, 1, 2
 const QS_WILTON_SAUTER, QS_SAUTER, QS_DOUBLENUM = 1, 2, 3
-const FP64, MIXED = 0, 1
+const FP64, MIXED, MIXED_ACCURATE = 0, 1, 2
 const C128, C64 = 0, 1
 const HOST, DEVICE = 0, 1
 

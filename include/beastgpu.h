@@ -62,8 +62,13 @@ enum {
 /* ---- precision of assembly and solve */
 enum {
   BEAST_FP64 = 0, /* everything complex FP64 (the reference's arithmetic)                    */
-  BEAST_MIXED = 1 /* far pairs in FP32, singular/near pairs FP64, c64 storage, FP32 LU with
-                     tensor-core trailing updates, FP64 iterative refinement                 */
+  BEAST_MIXED = 1, /* far pairs in FP32, Sauter-Schwab RT Maxwell pairs with FP32 moments
+                      (double-float partial sums), other near pairs FP64, c64 storage; solve:
+                      FP32 panels with FP16-operand tensor-core trailing updates of a c64
+                      copy, FP64 iterative refinement against the c64 matrix                 */
+  BEAST_MIXED_ACCURATE = 2 /* assembly as BEAST_FP64 (c128 matrix); solve as BEAST_MIXED, the
+                      refinement residual taken against the c128 matrix, so the solution is
+                      the FP64 one to the refinement tolerance                               */
 };
 
 /* ---- element type of a dense matrix / vector argument */
@@ -139,7 +144,8 @@ int beast_space_free(beast_space* space);
  *   Z[row_off + m, col_off + n]  (=|+=)  coeff * a(m, n)
  * Z: ldz leading dimension, element type z_dtype (BEAST_C128/C64), location z_loc.
  * accumulate = 0 overwrites the addressed block, 1 adds (linear combinations,
- * src/operator.jl:294-304).  precision: BEAST_FP64 or BEAST_MIXED. */
+ * src/operator.jl:294-304).  precision: BEAST_FP64 or BEAST_MIXED (BEAST_MIXED_ACCURATE
+ * assembles as BEAST_FP64). */
 int beast_assemble(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs,
                    const beast_space* test, const beast_space* trial, int precision, void* Z,
                    int64_t ldz, int z_dtype, int z_loc, int64_t row_off, int64_t col_off,
@@ -194,8 +200,9 @@ int beast_lu_free(beast_lu* lu);
 int beast_lu_solve_noalloc(beast_ctx* ctx, const beast_lu* lu, int64_t nrhs, void* B, int64_t ldb);
 
 /* x = A \ b for a device matrix A (c128 or c64).  precision BEAST_FP64: FP64 LU;
- * BEAST_MIXED: FP32 LU of a c64 copy + FP64 iterative refinement to `tol` relative
- * residual (residual matvec and update in FP64, against A as stored).
+ * BEAST_MIXED (or BEAST_MIXED_ACCURATE, the same here): FP32 LU of a c64 copy + FP64
+ * iterative refinement to `tol` relative residual (residual matvec and update in FP64,
+ * against A as stored: c128 for the FP64 solution to the tolerance).
  * b, x: complex FP64 [n x nrhs], location bx_loc.  iters/resid (may be NULL) report the
  * refinement steps and the final relative residual. */
 int beast_solve_dense(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dtype,

@@ -59,6 +59,19 @@ def test_solve_job_matches_oracle(efie):
     assert np.linalg.norm(xm - xo) / np.linalg.norm(xo) < 1e-5
 
 
+def test_solve_job_mixed_accurate_is_the_fp64_solution(efie):
+    """FP64 assembly with the mixed factorisation: the refinement residual is taken against the
+    c128 matrix, so the solution is the FP64 one to the refinement tolerance"""
+    X, op, E, Z, b = efie
+    xo = O.lu_solve(Z, b)
+    ctx = bg.get_context(0)
+    x, it, res = bg.solve_job(op, X, bg.tangential_trace(E), precision=bg.MIXED_ACCURATE, tol=1e-12,
+                              ctx=ctx)
+    assert ctx.last_factor_mode() == 2
+    assert res < 1e-12 and it >= 1
+    assert np.linalg.norm(x - xo) / np.linalg.norm(xo) < 1e-10
+
+
 def test_gmres_contract(efie):
     # test/test_itsolver.jl:24-37
     X, op, E, Z, b = efie
