@@ -218,6 +218,8 @@ cudaError_t vec_gemv_sub(int64_t n, int m, const double* V, int64_t ldv, const d
 // ---- FP16 operands of the tensor-core LU update (tc_gemm.cu)
 // work layout of an M x K by K x N update: A' (2M rows of K half2), B' (N columns of K half2),
 // the row scales 1/s (M floats), the column scales 1/t (N floats)
+// largest K of a symmetric (D-scaled) tensor-core update: its pivots are staged in shared memory
+constexpr int TC_SYM_KMAX = 2048;
 void tc_gemm_operands(void* work, int64_t M, int64_t N, int K, void** Ap, float** inv_sa, void** Bp,
                       float** inv_sb);
 #ifdef __CUDACC__

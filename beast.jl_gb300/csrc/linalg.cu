@@ -1847,7 +1847,20 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
     if ((size_t)(rows0 * (nb + 1) + nb) * sizeof(T) > smem_cap)
       return beast_fail(ctx, BEAST_ERR_ARG, "matrix too large for the shared-memory panel");
   }
-  const int NB = 16 * nb;
+  // outer / mid block widths in columns: 16 and 4 panels (with pivoting a single level);
+  // unpivoted, BEAST_LU_NB / BEAST_LU_NB2 override them (multiples of the panel width, the
+  // mid width dividing the outer one, the outer one at most TC_SYM_KMAX)
+  int NB = 16 * nb;
+  int64_t NB2 = pivot ? NB : 4 * nb;
+  if (!pivot) {
+    const char* e1 = getenv("BEAST_LU_NB");
+    const char* e2 = getenv("BEAST_LU_NB2");
+    const int b1 = e1 ? atoi(e1) : NB, b2 = e2 ? atoi(e2) : (int)NB2;
+    if (b2 >= nb && b2 % nb == 0 && b1 >= b2 && b1 % b2 == 0 && b1 <= TC_SYM_KMAX) {
+      NB = b1;
+      NB2 = b2;
+    }
+  }
   const size_t panel_smem = (size_t)(rows0 * (nb + 1) + nb) * sizeof(T);
   if (pivot)
     BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)panel_smem));
@@ -1898,7 +1911,6 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   // only their mid block (and its rows beyond it), the mid block updates the rest of the
   // outer block with K = NB2, and the outer block the trailing matrix with K = NB -- fewer
   // passes of narrow (K = nb) updates over the same columns
-  const int64_t NB2 = pivot ? NB : 4 * nb;
   for (int64_t J0 = 0; J0 < n && rc == BEAST_OK; J0 += NB) {
     const int64_t J1 = std::min<int64_t>(n, J0 + NB);
     for (int64_t M0 = J0; M0 < J1 && rc == BEAST_OK; M0 += NB2) {

@@ -503,7 +503,7 @@ __global__ void __launch_bounds__(256) k_prep_sym(const float2* L, const float2*
   __shared__ float red[2][8][33];
   __shared__ float2 tile[32][65];
   __shared__ float s_sa[32], s_sb[32];
-  __shared__ float2 s_d[1024];
+  __shared__ float2 s_d[TC_SYM_KMAX];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int m0 = blockIdx.x * 32, m = m0 + lane;
   for (int k = threadIdx.x; k < K; k += 256) s_d[k] = dg[(int64_t)k * (lda + 1)];
@@ -701,7 +701,7 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
     ProfScope ps(ctx, PK_CONVERT, (double)M0 * K * 16.0 + (double)N * K * 12.0);
     const int nA = (int)((M0 + 31) / 32);
     if (u.sym) {
-      if (colB != rowA || N > M0 || K > 1024)
+      if (colB != rowA || N > M0 || K > TC_SYM_KMAX)
         return beast_fail(ctx, BEAST_ERR_ARG, "symmetric update: operands must come from the same rows");
       k_prep_sym<<<(unsigned)nA, 256, 0, st>>>(Mat + rowA + colA * lda, Mat + colA + colA * lda, lda, (int)M0,
                                                (int)N, K, Ap, inv_sa, Bp, inv_sb);
