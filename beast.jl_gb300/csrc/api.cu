@@ -23,6 +23,27 @@ static cudaEvent_t ev_get(beast_ctx* c) {
   return e;
 }
 
+bool ctx_lookahead_streams(beast_ctx* ctx) {
+  if (ctx->aux) return true;
+  int lo = 0, hi = 0;
+  if (cudaDeviceGetStreamPriorityRange(&lo, &hi) != cudaSuccess) hi = 0;
+  cudaStream_t s = nullptr;
+  if (cudaStreamCreateWithPriority(&s, cudaStreamNonBlocking, hi) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  for (auto& e : ctx->la_ev)
+    if (cudaEventCreateWithFlags(&e, cudaEventDisableTiming) != cudaSuccess) {
+      cudaGetLastError();
+      for (auto& f : ctx->la_ev)
+        if (f) cudaEventDestroy(f), f = nullptr;
+      cudaStreamDestroy(s);
+      return false;
+    }
+  ctx->aux = s;
+  return true;
+}
+
 ProfScope::ProfScope(beast_ctx* c, int k, double w, int nlaunch) : ctx(c), kind(k), work(w) {
   ctx->launches += nlaunch;
   if (ctx->prof_on && ((ctx->prof_mask >> kind) & 1u)) {
@@ -138,8 +159,19 @@ int beast_ctx_destroy(beast_ctx* ctx) {
   if (!ctx) return BEAST_OK;
   cudaSetDevice(ctx->device);
   cudaStreamSynchronize(ctx->stream);
+  if (ctx->aux) {
+    cudaStreamSynchronize(ctx->aux);
+    for (auto& e : ctx->la_ev)
+      if (e) cudaEventDestroy(e);
+    cudaStreamDestroy(ctx->aux);
+  }
   if (ctx->ws) cudaFree(ctx->ws);
   if (ctx->d_flag) cudaFree(ctx->d_flag);
+  for (auto& r : ctx->prof) {
+    cudaEventDestroy(r.a);
+    cudaEventDestroy(r.b);
+  }
+  for (auto e : ctx->evpool) cudaEventDestroy(e);
   if (ctx->own_stream) cudaStreamDestroy(ctx->stream);
   cudaMemPool_t pool;
   if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
@@ -178,6 +210,18 @@ int beast_prof_enable(beast_ctx* ctx, int on) {
     ctx->evpool.push_back(r.b);
   }
   ctx->prof.clear();
+  // events for the brackets to come, made here rather than at the first record of each: an
+  // event creation costs the issuing thread several microseconds, which the bracketed
+  // launches would otherwise wait for (about two thousand records per dense solve at n = 30720)
+  constexpr size_t kEventsReady = 8192;
+  while (on && ctx->evpool.size() < kEventsReady) {
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) {
+      cudaGetLastError();
+      break;
+    }
+    ctx->evpool.push_back(e);
+  }
   ctx->prof_on = on != 0;
   ctx->prof_mask = 0xffffffffu;
   ctx->launches = 0;

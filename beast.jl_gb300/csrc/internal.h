@@ -46,7 +46,13 @@ struct beast_ctx {
   std::vector<cudaEvent_t> evpool;
   int64_t launches = 0;   // kernels launched by this context (counted always)
   int last_factor_mode = -1;  // factorisation of the last dense solve (beast_last_factor_mode)
+  // second (high-priority) stream and events of the factorisation's lookahead, made on first use
+  cudaStream_t aux = nullptr;
+  cudaEvent_t la_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
 };
+
+// the lookahead stream and events of ctx (created once); false when they cannot be made
+bool ctx_lookahead_streams(beast_ctx* ctx);
 
 // brackets one or more launches of class `kind`; `work` = algorithmic flops or bytes
 struct ProfScope {

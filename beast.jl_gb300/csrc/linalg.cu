@@ -42,7 +42,7 @@ int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t 
                 int64_t M0, int64_t N0, int64_t M1, int64_t N1, int K, void* work, size_t work_bytes,
                 bool prepped);
 int tc_gemm_sym(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t rowB, int64_t M0,
-                int64_t N0, int K, bool lower, void* work, size_t work_bytes, bool prepped);
+                int64_t N0, int K, bool lower, void* work, size_t work_bytes, bool prepped, int64_t a_skip = 0);
 
 namespace {
 
@@ -817,17 +817,20 @@ __device__ __forceinline__ void cmac2(float2& acc, float4 a, float4 b) {
 // Symmetric factorisation (nB >= 0; launched with nR CTAs, right side only): U12 = D L21^T
 // is not stored; its FP16 B' columns for the first nB systems (the rest of the mid block)
 // are written from L21 and the pivots D = diag(U11) instead.
+// rb0: index of the first CTA's block (the grid covers blocks rb0 .. of the 2 nR, or nR)
 __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, int64_t j0, int64_t n,
                                                         const float2* __restrict__ inv, int nR, __half2* Ap,
-                                                        float* inv_sa, __half2* Bp, float* inv_sb, int nB) {
+                                                        float* inv_sa, __half2* Bp, float* inv_sb, int nB,
+                                                        int rb0) {
   extern __shared__ __align__(16) unsigned char smraw[];
   float4* Ws = reinterpret_cast<float4*>(smraw);  // W[k][s], k of the current half
   float4* Ns = Ws + PA_KH * PA_LD4;               // N[k][v]
   float* red = reinterpret_cast<float*>(Ns + PA_KH * PA_LD4);  // 4 x 64 partial maxima
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const bool right = (int)blockIdx.x < nR;
+  const int bi = (int)blockIdx.x + rb0;
+  const bool right = bi < nR;
   const int64_t s0 = j0 + TRI;
-  const int64_t b0 = s0 + (int64_t)(right ? (int)blockIdx.x : (int)blockIdx.x - nR) * 64;  // first system
+  const int64_t b0 = s0 + (int64_t)(right ? bi : bi - nR) * 64;  // first system
   const float2 zero = make_float2(0.f, 0.f);
   const int sl = lane & 15, h = lane >> 4;
   const int vlo = 4 * warp + 2 * h, vhi = 60 - 4 * warp + 2 * h;  // free indices vlo, vlo+1, vhi, vhi+1
@@ -1056,6 +1059,58 @@ __global__ void __launch_bounds__(256) k_sym_upper(T* A, int64_t lda, int64_t n)
     const int i = e & 63, j = e >> 6;  // U[r0 + i][c0 + j], coalesced along i
     if (r0 + i < n && c0 + j < n) A[(r0 + i) + (c0 + j) * lda] = cmulx(d[i], t[i][j]);
   }
+}
+
+// Lookahead of the symmetric factorisation: the diagonal block at p0 takes the previous
+// panel's contribution just before its elimination, block -= L D L^T with L = A[p0.., p0-64..]
+// (kb x 64, the block row the previous panel has just solved) and D that panel's pivots
+// A[p0-64+k, p0-64+k].  Only the lower triangle with the diagonal (what the symmetric
+// elimination reads), FP32 sums.  A thread owns a 4 x 4 tile; tiles above the diagonal idle.
+constexpr int SDU_LD = 65;
+size_t sym_diag_update_smem() { return (size_t)2 * 64 * SDU_LD * sizeof(float2); }
+__global__ void __launch_bounds__(256) k_sym_diag_update(float2* A, int64_t lda, int64_t p0, int kb) {
+  extern __shared__ __align__(16) unsigned char smraw[];
+  float2* Ls = reinterpret_cast<float2*>(smraw);  // Ls[k LD + r] = L[r][k]
+  float2* Ds = Ls + 64 * SDU_LD;                  // Ds[k LD + c] = d_k L[c][k]
+  const int tid = threadIdx.x;
+  const int64_t q0 = p0 - 64;
+  for (int e = tid; e < 64 * 64; e += 256) {
+    const int r = e & 63, k = e >> 6;  // column k of L, coalesced along r
+    const float2 l = r < kb ? A[(p0 + r) + (q0 + k) * lda] : make_float2(0.f, 0.f);
+    Ls[k * SDU_LD + r] = l;
+    Ds[k * SDU_LD + r] = cmulx(A[(q0 + k) * (lda + 1)], l);
+  }
+  __syncthreads();
+  const int tr = tid >> 4, tc = tid & 15;
+  if (tc > tr) return;
+  float2 acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = make_float2(0.f, 0.f);
+#pragma unroll 4
+  for (int k = 0; k < 64; ++k) {
+    float2 a[4], b[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      a[i] = Ls[k * SDU_LD + 4 * tr + i];
+      b[i] = Ds[k * SDU_LD + 4 * tc + i];
+    }
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int j = 0; j < 4; ++j) cfma(acc[i][j], a[i], b[j]);
+  }
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int r = 4 * tr + i, c = 4 * tc + j;
+      if (r >= c && r < kb) {
+        float2& x = A[(p0 + r) + (p0 + c) * lda];
+        x = make_float2(x.x - acc[i][j].x, x.y - acc[i][j].y);
+      }
+    }
 }
 
 // sampled asymmetry: sums of |a_ij - a_ji|^2 and |a_ij|^2 + |a_ji|^2 over rows i = s p, columns
@@ -1800,13 +1855,14 @@ struct LUSteps {
   bool symgemm_tc(int64_t m, int64_t nc, int k, const void* tcwork) const {
     return sizeof(T) == 8 && tcwork && m >= 64 && nc >= 64 && k % 32 == 0;
   }
+  // a_skip: the prepped operands were written for a_skip more rows above rowA
   int symgemm(int64_t rowA, int64_t m, int64_t rowB, int64_t nc, int64_t colA, int k, bool lower, void* tcwork,
-              bool prepped = false) {
+              bool prepped = false, int64_t a_skip = 0) {
     if (m <= 0 || nc <= 0 || k <= 0) return BEAST_OK;
     const bool tc = symgemm_tc(m, nc, k, tcwork);
     if (tc)  // brackets its operand preparation and its tensor-core launch separately
       return tc_gemm_sym(ctx, reinterpret_cast<float2*>(A), lda, rowA, colA, rowB, m, nc, k, lower, tcwork,
-                         tcwork_bytes, prepped);
+                         tcwork_bytes, prepped, prepped ? a_skip : 0);
     ProfScope ps(ctx, PK_GEMM, 8.0 * (double)k * (double)m * nc);
     T* B = nullptr;
     BEAST_CUDA_TRY(ctx, cudaMallocAsync(&B, (size_t)k * nc * sizeof(T), st));
@@ -1905,6 +1961,17 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
     BEAST_CUDA_TRY(ctx, cudaMallocAsync(&tcwork, tcwork_bytes, st));
   }
   LUSteps<T, R> S{ctx, A, lda, n, ipiv, st, tcwork_bytes};
+  // lookahead (symmetric path with tensor-core updates; BEAST_LU_LOOKAHEAD=1): while a panel's
+  // other rows and its update run on the context's stream, the second stream solves the next
+  // panel's block row, updates and eliminates the next diagonal block.  ahead: this panel's
+  // elimination has run there (event la_ev[lu_par]).
+  const char* la_env = getenv("BEAST_LU_LOOKAHEAD");
+  const bool la = sym && tcwork && la_env && la_env[0] == '1' && ctx_lookahead_streams(ctx);
+  if (la)
+    BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_sym_diag_update, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)sym_diag_update_smem()));
+  bool ahead = false;
+  int lu_par = 0;
 
   int rc = BEAST_OK;
   // unpivoted, the outer block is factored in mid blocks of NB2 columns: the panels update
@@ -1936,13 +2003,19 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       const int64_t u_m0 = n - j0 - kb, u_n0 = M1 - j0 - kb, u_m1 = pivot ? 0 : M1 - j0 - kb,
                     u_n1 = pivot ? 0 : n - M1;
       bool applied = false, prepped = false;
+      // lookahead for this panel: a full next panel inside the mid block with rows below it
+      const bool next = la && kb == TRI && j0 + 2 * TRI <= M1 && n - j0 - kb > TRI;
+      const int64_t skip = next ? TRI : 0;  // rows of the in-block update left to the second stream
       if (!pivot) {
         // no pivoting: diagonal block LU, then L21 = A21 U11^{-1} for every row below
-        ProfScope ps(ctx, PK_PANEL, 8.0 * (double)M * kb * kb / 2, apply_path ? 1 : 2);
+        ProfScope ps(ctx, PK_PANEL, 8.0 * (double)M * kb * kb / 2, 0);
         constexpr int NS = TrsmTile<T>::NS;
         const int64_t rb = n - j0 - kb;
         T* dblk = apply_path ? reinterpret_cast<T*>(lu_dinv(ipiv, n)) + (j0 / TRI) * 2 * TRI * TRI : nullptr;
-        if (apply_path && sym)
+        ctx->launches += ahead ? 0 : 1;
+        if (ahead)
+          BEAST_CUDA_TRY(ctx, cudaStreamWaitEvent(st, ctx->la_ev[lu_par], 0));
+        else if (apply_path && sym)
           k_lu_inv64<T, true><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk);
         else if (apply_path)
           k_lu_inv64<T, false><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk);
@@ -1954,19 +2027,51 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
           // tensor cores
           // (symmetric: L21 only, and the update is rows below x the rest of the mid block)
           const int64_t nBs = sym ? u_n0 : 0;
-          prepped = sym ? (nBs > 0 && S.symgemm_tc(u_m0, nBs, kb, tcwork))
+          prepped = sym ? (nBs > 0 && S.symgemm_tc(u_m0 - skip, nBs, kb, tcwork))
                         : (S.gemm2_runs(u_m0, u_n0, u_m1, u_n1, kb) && S.gemm2_tc(u_m0, u_n0, u_n1, kb, tcwork));
           void *Apv = nullptr, *Bpv = nullptr;
           float *isa = nullptr, *isb = nullptr;
           if (prepped) tc_gemm_operands(tcwork, u_m0, sym ? nBs : u_n0 + u_n1, kb, &Apv, &isa, &Bpv, &isb);
           const int nR = (int)((rb + 63) / 64);
-          k_panel_apply<<<(unsigned)(sym ? nR : 2 * nR), 256, panel_apply_smem(), st>>>(
-              reinterpret_cast<float2*>(A), lda, j0, n, reinterpret_cast<const float2*>(dblk), nR,
-              static_cast<__half2*>(Apv), isa, static_cast<__half2*>(Bpv), isb, prepped ? (int)nBs : 0);
+          float2* Af = reinterpret_cast<float2*>(A);
+          const float2* inv = reinterpret_cast<const float2*>(dblk);
+          const int nBp = prepped ? (int)nBs : 0;
+          if (next) {
+            // second stream: block row j0 + 64 (its L rows and operands), then the next diagonal
+            // block's update and elimination; it has to see this panel's elimination and the
+            // previous in-block update (both on it, or both here)
+            cudaStream_t ax = ctx->aux;
+            if (ahead) {
+              BEAST_CUDA_TRY(ctx, cudaStreamWaitEvent(ax, ctx->la_ev[3], 0));
+            } else {
+              BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[4], st));
+              BEAST_CUDA_TRY(ctx, cudaStreamWaitEvent(ax, ctx->la_ev[4], 0));
+            }
+            k_panel_apply<<<1, 256, panel_apply_smem(), ax>>>(Af, lda, j0, n, inv, nR, static_cast<__half2*>(Apv),
+                                                              isa, static_cast<__half2*>(Bpv), isb, nBp, 0);
+            BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[2], ax));
+            k_sym_diag_update<<<1, 256, sym_diag_update_smem(), ax>>>(Af, lda, j0 + TRI, TRI);
+            k_lu_inv64<T, true><<<1, 256, getrf_sm, ax>>>(A, lda, j0 + TRI, TRI, dinfo, dblk + 2 * TRI * TRI);
+            lu_par ^= 1;
+            BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[lu_par], ax));
+            ctx->launches += 3;
+            // here: the other block rows, then (after the second stream's operands) the update
+            if (nR > 1) {
+              k_panel_apply<<<(unsigned)(nR - 1), 256, panel_apply_smem(), st>>>(
+                  Af, lda, j0, n, inv, nR, static_cast<__half2*>(Apv), isa, static_cast<__half2*>(Bpv), isb, nBp, 1);
+              ctx->launches += 1;
+            }
+            BEAST_CUDA_TRY(ctx, cudaStreamWaitEvent(st, ctx->la_ev[2], 0));
+          } else {
+            k_panel_apply<<<(unsigned)(sym ? nR : 2 * nR), 256, panel_apply_smem(), st>>>(
+                Af, lda, j0, n, inv, nR, static_cast<__half2*>(Apv), isa, static_cast<__half2*>(Bpv), isb, nBp, 0);
+            ctx->launches += 1;
+          }
           applied = true;
         } else if (rb > 0) {
           k_trsm_tile<T, R, true><<<(unsigned)((rb + NS - 1) / NS), TrsmTile<T>::NT, trsm_tile_smem<T>(), st>>>(
               A, lda, j0, kb, j0 + kb, n);
+          ctx->launches += 1;
         }
         BEAST_CUDA_TRY(ctx, cudaGetLastError());
       }
@@ -1975,7 +2080,10 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       // the block's rows of the columns beyond the block are updated here too (what the
       // pivoted path does per panel after the block).
       if (sym) {
-        if ((rc = S.symgemm(j0 + kb, u_m0, j0 + kb, u_n0, j0, kb, false, tcwork, prepped))) break;
+        if ((rc = S.symgemm(j0 + kb + skip, u_m0 - skip, j0 + kb, u_n0, j0, kb, false, tcwork, prepped, skip)))
+          break;
+        if (next) BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[3], st));
+        ahead = next;
         continue;
       }
       if (!applied && (rc = S.trsm(j0, kb, j0 + kb, pivot ? J1 : n))) break;
@@ -2010,6 +2118,10 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       // trailing update with K = NB
       rc = S.gemm(J1, n - J1, J1, n - J1, J0, (int)(J1 - J0), tcwork);
     }
+  }
+  if (la) {  // nothing of the second stream outlives the factorisation
+    BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[4], ctx->aux));
+    BEAST_CUDA_TRY(ctx, cudaStreamWaitEvent(st, ctx->la_ev[4], 0));
   }
   if (tcwork) cudaFreeAsync(tcwork, st);
   int hinfo[3] = {0, 0, 0};

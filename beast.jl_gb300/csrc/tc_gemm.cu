@@ -644,10 +644,13 @@ void tc_gemm_operands(void* work, int64_t M, int64_t N, int K, void** Ap, float*
 //              below the diagonal (rowA = rowB, M0 = N0, one rectangle)
 // prepped: the FP16 operands are already in work (tc_gemm_operands layout, written by the
 // kernel that produced A and B).
+// a_skip (prepped only): the operands were written for a_skip + M0 rows of A and the update
+// uses the last M0 of them
 struct TcUpdate {
   int64_t rowA, colA, colB, M0, N0, M1, N1;
   int K;
   bool sym, lower, prepped;
+  int64_t a_skip = 0;
 };
 
 static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate& u, void* work, size_t work_bytes) {
@@ -660,7 +663,7 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
     return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: unaligned block");
   if (u.lower && (u.sym == false || rowA != colB || M0 != N0 || N1 != 0))
     return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: lower-triangle tiles need a diagonal square");
-  if (tc_gemm_work_bytes(M0, N, K) > work_bytes)
+  if (u.a_skip < 0 || (u.a_skip > 0 && !u.prepped) || tc_gemm_work_bytes(M0 + u.a_skip, N, K) > work_bytes)
     return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: workspace too small");
   static bool attr_done[64] = {false};
   static int pair_clusters[64] = {0};  // co-resident CTA pairs (0: the pair kernel is not used)
@@ -693,9 +696,10 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
   const bool pair = pair_clusters[dev] > 0;
   void *Apv, *Bpv;
   float *inv_sa, *inv_sb;
-  tc_gemm_operands(work, M0, N, K, &Apv, &inv_sa, &Bpv, &inv_sb);
-  __half2* Ap = static_cast<__half2*>(Apv);
+  tc_gemm_operands(work, M0 + u.a_skip, N, K, &Apv, &inv_sa, &Bpv, &inv_sb);
+  __half2* Ap = static_cast<__half2*>(Apv) + 2 * u.a_skip * K;  // A' rows 2m, 2m+1 of K half2 each
   __half2* Bp = static_cast<__half2*>(Bpv);
+  inv_sa += u.a_skip;
   if (!u.prepped) {
     // FP16 operands: A read and A' written (2 x 4 B per complex element), B read and B' written
     ProfScope ps(ctx, PK_CONVERT, (double)M0 * K * 16.0 + (double)N * K * 12.0);
@@ -805,7 +809,7 @@ int tc_gemm_sub(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t 
 // the diagonal of Mat at colA..; lower: only the tiles on or below the diagonal (rowA = rowB,
 // M0 = N0).
 int tc_gemm_sym(beast_ctx* ctx, float2* Mat, int64_t lda, int64_t rowA, int64_t colA, int64_t rowB, int64_t M0,
-                int64_t N0, int K, bool lower, void* work, size_t work_bytes, bool prepped) {
-  TcUpdate u{rowA, colA, rowB, M0, N0, 0, 0, K, true, lower, prepped};
+                int64_t N0, int K, bool lower, void* work, size_t work_bytes, bool prepped, int64_t a_skip) {
+  TcUpdate u{rowA, colA, rowB, M0, N0, 0, 0, K, true, lower, prepped, a_skip};
   return tc_gemm_run(ctx, Mat, lda, u, work, work_bytes);
 }

@@ -191,3 +191,35 @@ def test_mixed_symmetric_path(n):
     assert it <= 5 and res < 1e-12
     r = A.astype(np.complex128) @ x - b
     assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-12
+
+
+@pytest.mark.parametrize("n", [1101, 2600])
+def test_mixed_symmetric_lookahead(n, monkeypatch):
+    """the symmetric factorisation with lookahead (BEAST_LU_LOOKAHEAD=1: the next panel's block
+    row, diagonal-block update and elimination on a second stream) refines to the same FP64
+    solution as without it"""
+    import torch
+    ctx = bg.get_context(0)
+    rng = np.random.default_rng(23)
+    R = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    A = (R + R.T) / 2 + 4 * n ** 0.5 * np.eye(n)
+    A = A + 1e-6 * (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)))
+    A = A.astype(np.complex64)
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda().T
+    xs = {}
+    for la in ("0", "1"):
+        monkeypatch.setenv("BEAST_LU_LOOKAHEAD", la)
+        ctx.prof_enable(True)
+        try:
+            x, it, res = bg.solve(At, b, precision=bg.MIXED, tol=1e-12, ctx=ctx)
+            prof = ctx.prof_read()
+        finally:
+            ctx.prof_enable(False)
+        assert ctx.last_factor_mode() == 2
+        assert prof["lu_panel"][1] == (n + 63) // 64
+        assert it <= 5 and res < 1e-12
+        r = A.astype(np.complex128) @ x - b
+        assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-12
+        xs[la] = x
+    assert np.linalg.norm(xs["1"] - xs["0"]) / np.linalg.norm(xs["0"]) < 1e-10
