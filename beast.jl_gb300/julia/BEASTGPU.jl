@@ -201,8 +201,9 @@ end
 """
     solve(Z, b; precision=FP64, tol=1e-12) -> x
 
-`Z \\ b` on the device: FP64 LU, or (MIXED) FP32 LU with tensor-core updates and FP64
-iterative refinement to `tol`.
+`Z \\ b` on the device: FP64 LU, or (MIXED, or MIXED_ACCURATE -- the same here) FP32 LU
+with tensor-core updates and FP64 iterative refinement to `tol` against `Z` as given (an FP64
+assembly, `GPUQStrat(inner; precision=FP64)`, then gives the FP64 solution to the tolerance).
 """
 function solve(Z::Matrix{ComplexF64}, b::Vector{ComplexF64}; precision=FP64, tol=1e-12, maxiter=30)
     ctx = context()
