@@ -598,7 +598,6 @@ DEV void integrand(int kind, const OpParams& op, V3<double> x, V3<double> y, V3<
   V3<double> r = x - y;
   double R = sqrt(dot(r, r));
   double iR = 1.0 / R;
-  C2<double> gam{op.gr, op.gi};
   C2<double> gR{op.gr * R, op.gi * R};
   C2<double> al{op.ar, op.ai}, be{op.br, op.bi};
   switch (kind) {

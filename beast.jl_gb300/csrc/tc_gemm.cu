@@ -41,7 +41,6 @@ constexpr int A_BYTES = TM * TK * 2, B_BYTES = TN * TK * 2, STAGE_BYTES = A_BYTE
 constexpr int CCH = 32;                           // epilogue chunk: 128 rows x 32 columns of C'
 constexpr int C_BYTES = TM * CCH * 4;              // 16 KB per chunk buffer
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 2 * C_BYTES + 1024 + 256;
-constexpr int MAX_CTAS = 1024;
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
@@ -109,11 +108,6 @@ __device__ __forceinline__ void cluster_sync() {
   asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
 }
 
-__device__ __forceinline__ void tma_store_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
-  asm volatile("cp.async.bulk.tensor.2d.global.shared::cta.bulk_group [%0, {%1, %2}], [%3];" ::"l"((uint64_t)map),
-               "r"(x), "r"(y), "r"(src)
-               : "memory");
-}
 // C' += (chunk in shared memory), element-wise FP32 add performed by the TMA unit
 __device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
   asm volatile(
@@ -124,7 +118,6 @@ __device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, int x,
 }
 __device__ __forceinline__ void bulk_commit() { asm volatile("cp.async.bulk.commit_group;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait_read1() { asm volatile("cp.async.bulk.wait_group.read 1;" ::: "memory"); }
-__device__ __forceinline__ void bulk_wait_read0() { asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory"); }
 __device__ __forceinline__ void bulk_wait0() { asm volatile("cp.async.bulk.wait_group 0;" ::: "memory"); }
 
 // shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row atoms of 1024 B
