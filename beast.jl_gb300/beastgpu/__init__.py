@@ -13,5 +13,6 @@ from .operators import (Maxwell3D, Helmholtz3D, nxdoublelayer, Identity, NCross,
                         defaultquadstrat, tangential_trace, cross_trace_H, dirichlet_trace)
 from .api import (Context, get_context, assemble, assemble_rhs, solve, gmres, farfield,
                   solve_job, blockassembler, assemblerow, assemblecol)
+from .serve import Server, run_job, job_footprint
 
 __all__ = [n for n in dir() if not n.startswith("_")]

@@ -243,67 +243,16 @@ def compare_fp64(args):
 
 
 # ---- batched and served workloads -------------------------------------------------------
-def _job_runner(bg, L, ctx):
-    """one job through the C ABI on this context's stream: upload mesh + space, assemble on the
-    device, excitations, mixed solve with all right-hand sides, solution back to the host"""
-    import torch
-
-    def run(job):
-        m, X, op, waves, exc_kind = job["mesh"], job["space"], job["op"], job["waves"], job["exc_kind"]
-        lib = ctx.lib
-        ad = X.assemblydata()
-        verts = np.ascontiguousarray(m.vertices)
-        cells = np.ascontiguousarray(m.cells, dtype=np.int32)
-        mh, sh = C.c_void_p(), C.c_void_p()
-        ctx.check(lib.beast_mesh_upload(ctx.handle, verts.ctypes.data, verts.shape[0], cells.ctypes.data,
-                                        cells.shape[0], 0, C.byref(mh)))
-        ctx.check(lib.beast_space_upload(ctx.handle, mh, ad.kind, ad.cells.shape[0], ad.cells.ctypes.data,
-                                         ad.maxfn, ad.nshapes, ad.dof.ctypes.data, ad.coeff.ctypes.data,
-                                         X.numfunctions(), 0, C.byref(sh)))
-        n = X.numfunctions()
-        nr = len(waves)
-        qs = bg.defaultquadstrat(op, X, X)
-        od, qd = bg.api._op_desc(op), bg.api._qs_desc(qs)
-        dev = f"cuda:{ctx.device}"
-        Z = torch.empty((n, n), dtype=torch.complex64, device=dev)
-        B = torch.empty((nr, n), dtype=torch.complex128, device=dev)
-        Xs = torch.empty((nr, n), dtype=torch.complex128, device=dev)
-        ctx.check(lib.beast_assemble(ctx.handle, C.byref(od), C.byref(qd), sh, sh, L.MIXED, Z.data_ptr(), n,
-                                     L.C64, L.DEVICE, 0, 0, 1.0, 0.0, 0))
-        if job.get("local"):  # e.g. MFIE: n x K - Id/2
-            which, c = job["local"]
-            ctx.check(lib.beast_assemble_local(ctx.handle, which, sh, sh, 6, Z.data_ptr(), n, L.C64, L.DEVICE,
-                                               0, 0, c, 0.0))
-        for r, w in enumerate(waves):
-            d = np.ascontiguousarray(w.direction, dtype=np.float64)
-            pol = np.ascontiguousarray(getattr(w, "polarization", (0.0, 0.0, 0.0)), dtype=np.float64)
-            g, a = complex(w.gamma), complex(w.amplitude)
-            ctx.check(lib.beast_rhs_planewave(ctx.handle, exc_kind, sh, d.ctypes.data, pol.ctypes.data, g.real,
-                                              g.imag, a.real, a.imag, 8, B[r].data_ptr(), L.DEVICE))
-        it, res = C.c_int(0), C.c_double(0)
-        ctx.check(lib.beast_solve_dense(ctx.handle, n, Z.data_ptr(), n, L.C64, L.MIXED, B.data_ptr(),
-                                        Xs.data_ptr(), nr, L.DEVICE, 1e-10, 30, C.byref(it), C.byref(res)))
-        x = Xs.cpu().numpy()
-        lib.beast_space_free(sh)
-        lib.beast_mesh_free(mh)
-        return x, it.value, res.value
-    return run
-
-
-def _workers(args, bg, L):
-    import torch
-    ctxs = [bg.Context(0) for _ in range(args.workers)]
-    return ctxs, [_job_runner(bg, L, c) for c in ctxs]
+# Both run through the package's request loop (beastgpu.serve.Server): --workers contexts
+# (one CUDA stream and host thread each), jobs admitted as slots and HBM free up.
 
 
 def run_c3(args):
     """256 ellipsoids (semi-axes U[0.5, 2], level U{2, 3, 4}, vertices moved by N(0, 0.01 h)),
     Helmholtz single layer on P0, k U[0.5, 8], 4 plane waves each; jobs spread over
     --workers contexts (one stream each) from as many host threads; jobs/s over all 256"""
-    import threading
     import torch
     import beastgpu as bg
-    from beastgpu import lib as L
     rng = np.random.default_rng(2024)
     jobs = []
     for j in range(256):
@@ -316,32 +265,16 @@ def run_c3(args):
         waves = [bg.Helmholtz3D.planewave(tuple(d), wavenumber=k) for d in dirs]
         jobs.append({"mesh": m, "space": bg.lagrangecxd0(m), "op": bg.Helmholtz3D.singlelayer(wavenumber=k),
                      "waves": waves, "exc_kind": bg.dirichlet_trace(waves[0]).kind, "level": lvl})
-    ctxs, runners = _workers(args, bg, L)
-    for r in runners:  # warm-up: one small and one large job per context
-        r(jobs[0])
-    worst = [0.0]
-    lock = threading.Lock()
-    nxt = [0]
-
-    def worker(run):
-        while True:
-            with lock:
-                i = nxt[0]
-                nxt[0] += 1
-            if i >= len(jobs):
-                return
-            _, it, res = run(jobs[i])
-            with lock:
-                worst[0] = max(worst[0], res)
+    srv = bg.Server(slots=args.workers)
+    for f in [srv.submit(jobs[0]) for _ in range(args.workers)]:  # warm-up: one job per context
+        f.result()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    th = [threading.Thread(target=worker, args=(r,)) for r in runners]
-    for t in th:
-        t.start()
-    for t in th:
-        t.join()
+    futs = [srv.submit(j) for j in jobs]
+    worst = max(f.result()[2] for f in futs)
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
+    srv.close()
     lv = [j["level"] for j in jobs]
     print(json.dumps({"metric": "jobs/s", "value": len(jobs) / dt, "unit": "jobs/s", "n_gpus": 1,
                       "higher_is_better": True, "config": {
@@ -350,18 +283,15 @@ def run_c3(args):
                           "unknowns_max": int(max(j["space"].numfunctions() for j in jobs)),
                           "precision": "mixed", "workers": args.workers,
                           "job": "mesh + space upload, assembly, 4 excitations, solve (4 RHS), solution to host"},
-                      "seconds": dt, "worst_rel_residual": worst[0], "data": "synthetic seeded meshes"}))
+                      "seconds": dt, "worst_rel_residual": worst, "data": "synthetic seeded meshes"}))
 
 
 def run_c5(args):
     """a Poisson stream (--rate per second, --requests requests) of solve requests: operator
     U{EFIE, MFIE (n x K - Id/2), Helmholtz SL}, icosphere level U{3, 4, 5}, k U[1, 12], 1-8 plane
     waves; served by --workers contexts in arrival order; latency = completion - arrival"""
-    import threading
-    import queue
     import torch
     import beastgpu as bg
-    from beastgpu import lib as L
     rng = np.random.default_rng(7)
     meshes = {lv: bg.icosphere(lv) for lv in (3, 4, 5)}
     rt = {lv: bg.raviartthomas(meshes[lv]) for lv in meshes}
@@ -389,34 +319,30 @@ def run_c5(args):
                    "local": None if kind == "efie" else (0, -0.5)}
         job.update({"arrival": t, "kind": kind, "level": lv})
         reqs.append(job)
-    ctxs, runners = _workers(args, bg, L)
-    for r in runners:
-        r(reqs[0])
+    srv = bg.Server(slots=args.workers)
+    for f in [srv.submit(reqs[0]) for _ in range(args.workers)]:  # warm-up: one job per context
+        f.result()
     torch.cuda.synchronize()
-    q = queue.Queue()
     lat = [None] * len(reqs)
     t0 = time.perf_counter()
 
-    def worker(run):
-        while True:
-            i = q.get()
-            if i is None:
-                return
-            run(reqs[i])
+    def done(i):
+        def cb(_):
             lat[i] = time.perf_counter() - t0 - reqs[i]["arrival"]
-    th = [threading.Thread(target=worker, args=(r,)) for r in runners]
-    for w in th:
-        w.start()
+        return cb
+    futs = []
     for i, rq in enumerate(reqs):
         wait = rq["arrival"] - (time.perf_counter() - t0)
         if wait > 0:
             time.sleep(wait)
-        q.put(i)
-    for _ in th:
-        q.put(None)
-    for w in th:
-        w.join()
+        f = srv.submit(rq)
+        f.add_done_callback(done(i))
+        futs.append(f)
+    for f in futs:
+        f.result()
+    srv.drain()
     dt = time.perf_counter() - t0
+    srv.close()
     ms = np.array(lat) * 1e3
     print(json.dumps({"metric": "latency_ms", "p50": float(np.percentile(ms, 50)),
                       "p99": float(np.percentile(ms, 99)), "max": float(ms.max()), "unit": "ms",
@@ -424,7 +350,8 @@ def run_c5(args):
                           "workload": "C5: Poisson stream of EFIE / MFIE / Helmholtz-SL solve requests",
                           "rate_per_s": args.rate, "requests": args.requests, "workers": args.workers,
                           "levels": [3, 4, 5], "rhs_per_request": "1-8", "precision": "mixed",
-                          "request": "mesh + space upload, assembly, excitations, solve, solution to host"},
+                          "request": "mesh + space upload, assembly, excitations, solve, solution to host",
+                          "admission": "beastgpu.serve.Server: arrival order, a free slot and HBM footprint"},
                       "data": "synthetic seeded request stream"}))
 
 

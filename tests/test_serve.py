@@ -1,0 +1,100 @@
+"""Admission logic of the request loop (beastgpu.serve.Server) on the CPU: stand-in contexts
+and a stand-in job runner that records when each job runs."""
+import threading
+import time
+
+import pytest
+
+from beastgpu.serve import Server, job_footprint
+from beastgpu import lib as L
+
+
+class Recorder:
+    def __init__(self, hold=0.05):
+        self.hold = hold
+        self.lock = threading.Lock()
+        self.events = []  # (t, "start"/"end", name)
+
+    def __call__(self, ctx, job):
+        with self.lock:
+            self.events.append((time.perf_counter(), "start", job["name"]))
+        if job.get("fail"):
+            raise RuntimeError("job failed")
+        time.sleep(job.get("hold", self.hold))
+        with self.lock:
+            self.events.append((time.perf_counter(), "end", job["name"]))
+        return job["name"]
+
+    def order(self, kind):
+        return [n for _, k, n in sorted(self.events) if k == kind]
+
+    def concurrent(self, a, b):
+        ev = {(k, n): t for t, k, n in self.events}
+        return ev[("start", a)] < ev[("end", b)] and ev[("start", b)] < ev[("end", a)]
+
+
+def server(rec, slots, budget, allow_pass=False):
+    return Server(slots=slots, hbm_budget=budget, allow_pass=allow_pass, make_context=object,
+                  runner=rec, footprint=lambda job: job["fp"])
+
+
+def test_budget_holds_and_arrival_order_is_kept():
+    rec = Recorder()
+    jobs = [{"name": "a", "fp": 60}, {"name": "b", "fp": 60}, {"name": "c", "fp": 30}, {"name": "d", "fp": 30}]
+    with server(rec, slots=4, budget=100) as s:
+        futs = [s.submit(j) for j in jobs]
+        assert [f.result(timeout=10) for f in futs] == ["a", "b", "c", "d"]
+        assert s.peak_bytes <= 100
+    # b does not fit beside a, and c waits behind b; then b and c run together
+    assert rec.order("start") == ["a", "b", "c", "d"]
+    assert not rec.concurrent("a", "b") and not rec.concurrent("a", "c")
+    assert rec.concurrent("b", "c")
+
+
+def test_allow_pass_admits_a_later_job_that_fits():
+    rec = Recorder()
+    jobs = [{"name": "a", "fp": 60}, {"name": "b", "fp": 60}, {"name": "c", "fp": 30}]
+    with server(rec, slots=4, budget=100, allow_pass=True) as s:
+        for f in [s.submit(j) for j in jobs]:
+            f.result(timeout=10)
+        assert s.peak_bytes <= 100
+    assert rec.concurrent("a", "c")
+    assert not rec.concurrent("a", "b")
+
+
+def test_slots_bound_the_concurrency():
+    rec = Recorder()
+    jobs = [{"name": str(i), "fp": 1} for i in range(6)]
+    with server(rec, slots=2, budget=100) as s:
+        for f in [s.submit(j) for j in jobs]:
+            f.result(timeout=10)
+    running, peak = 0, 0
+    for _, k, _ in sorted(rec.events):
+        running += 1 if k == "start" else -1
+        peak = max(peak, running)
+    assert peak == 2
+
+
+def test_oversized_job_fails_at_submit_and_a_failing_job_does_not_stop_the_loop():
+    rec = Recorder()
+    with server(rec, slots=1, budget=100) as s:
+        big = s.submit({"name": "big", "fp": 101})
+        with pytest.raises(ValueError):
+            big.result(timeout=1)
+        bad = s.submit({"name": "bad", "fp": 10, "fail": True})
+        good = s.submit({"name": "good", "fp": 10})
+        with pytest.raises(RuntimeError):
+            bad.result(timeout=10)
+        assert good.result(timeout=10) == "good"
+        lat = s.latency_ms()
+    assert lat["jobs"] == 2 and lat["p50"] > 0 and lat["p99"] >= lat["p50"]
+
+
+def test_job_footprint_counts_the_matrix_and_its_factor_copy():
+    n = 30720
+    mixed = job_footprint(n, 1, L.MIXED)
+    acc = job_footprint(n, 1, L.MIXED_ACCURATE)
+    fp64 = job_footprint(n, 1, L.FP64)
+    assert 16 * n * n < mixed < 16 * n * n + (1 << 30)
+    assert 24 * n * n < acc < 24 * n * n + (1 << 30)
+    assert 32 * n * n < fp64 < 32 * n * n + (1 << 30)
