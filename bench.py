@@ -21,6 +21,7 @@ import ctypes as C
 import json
 import os
 import subprocess
+import tempfile
 import sys
 import time
 
@@ -94,8 +95,7 @@ class Clocks:
     """nvidia-smi sampling during the timed region"""
 
     def __init__(self, dev):
-        self.f = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
-        os.makedirs(os.path.dirname(self.f), exist_ok=True)
+        self.f = os.path.join(tempfile.gettempdir(), f"beast_clocks_{os.getpid()}.csv")
         q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
