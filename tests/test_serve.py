@@ -98,3 +98,15 @@ def test_job_footprint_counts_the_matrix_and_its_factor_copy():
     assert 16 * n * n < mixed < 16 * n * n + (1 << 30)
     assert 24 * n * n < acc < 24 * n * n + (1 << 30)
     assert 32 * n * n < fp64 < 32 * n * n + (1 << 30)
+
+
+def test_a_cancelled_pending_job_never_runs():
+    rec = Recorder(hold=0.1)
+    with server(rec, slots=1, budget=100) as s:
+        first = s.submit({"name": "first", "fp": 10})
+        waiting = s.submit({"name": "waiting", "fp": 10})
+        assert waiting.cancel()
+        last = s.submit({"name": "last", "fp": 10})
+        assert first.result(timeout=10) == "first" and last.result(timeout=10) == "last"
+        assert waiting.cancelled()
+    assert "waiting" not in rec.order("start")
