@@ -189,7 +189,8 @@ def compare_fp64(args):
     """Plain FP64 (c128 matrix, FP64 quadrature, FP64 LU) against the mixed path on the same
     workload: solves/s of each (CUDA events around assemble + excitation + solve; the mixed
     path after one warm-up solve, the FP64 path as one run after it, its LU alone taking
-    minutes) and the relative difference of the two surface-current vectors."""
+    minutes), and each arm's relative difference from the FP64 one in the surface current, the
+    far field (181 directions in the xz-plane) and, for the mixed arm, the matrix (Frobenius)."""
     import torch
     import beastgpu as bg
     from beastgpu import lib as L
@@ -200,7 +201,9 @@ def compare_fp64(args):
     qs = bg.defaultquadstrat(op, X, X)
     od, qd = bg.api._op_desc(op), bg.api._qs_desc(qs)
     d, pol, g = np.array([1.0, 0, 0]), np.array([0, 0, 1.0]), complex(E.gamma)
-    out, xs = {}, {}
+    out, xs, keep = {}, {}, {}
+    th = np.linspace(0.0, np.pi, 181)
+    dirs = np.stack([np.sin(th), np.zeros_like(th), np.cos(th)], axis=1)
     for name, prec, dt, tdt, warm in (("mixed", L.MIXED, L.C64, torch.complex64, 1),
                                       ("mixed_accurate", L.MIXED_ACCURATE, L.C128, torch.complex128, 1),
                                       ("fp64", L.FP64, L.C128, torch.complex128, 0)):
@@ -229,17 +232,37 @@ def compare_fp64(args):
         out[name] = {"solves_per_s": 1000.0 / ms, "ms_per_solve": ms, "refinement_iters": it.value,
                      "rel_residual": res.value}
         xs[name] = x.cpu().numpy()
+        if name != "fp64":
+            keep[name] = Z  # kept for the matrix comparison
+        else:
+            for a, Za in keep.items():
+                num = den = 0.0
+                for r0 in range(0, n, 2048):  # in row slabs: no full-size temporaries
+                    z64 = Z[r0:r0 + 2048]
+                    num += float(torch.linalg.norm(Za[r0:r0 + 2048].to(torch.complex128) - z64)) ** 2
+                    den += float(torch.linalg.norm(z64)) ** 2
+                out["matrix_rel_frobenius_" + a] = (num / den) ** 0.5
+            keep.clear()
         del Z, b, x
         torch.cuda.empty_cache()
+    ffs = {a: bg.farfield(X, xs[a], dirs, g, ctx=ctx) for a in xs}
+
     def rel(a):
         return float(np.linalg.norm(xs[a] - xs["fp64"]) / np.linalg.norm(xs["fp64"]))
+
+    def rel_ff(a):
+        return float(np.linalg.norm(ffs[a] - ffs["fp64"]) / np.linalg.norm(ffs["fp64"]))
     print(json.dumps({"compare": "mixed and mixed-accurate vs plain FP64", "config": config_dict(args, X, m),
                       "mixed": out["mixed"], "mixed_accurate": out["mixed_accurate"], "fp64": out["fp64"],
                       "speedup_mixed_over_fp64": out["mixed"]["solves_per_s"] / out["fp64"]["solves_per_s"],
                       "speedup_mixed_accurate_over_fp64":
                           out["mixed_accurate"]["solves_per_s"] / out["fp64"]["solves_per_s"],
                       "surface_current_rel_diff": rel("mixed"),
-                      "surface_current_rel_diff_mixed_accurate": rel("mixed_accurate")}))
+                      "surface_current_rel_diff_mixed_accurate": rel("mixed_accurate"),
+                      "farfield_rel_diff": rel_ff("mixed"),
+                      "farfield_rel_diff_mixed_accurate": rel_ff("mixed_accurate"),
+                      "matrix_rel_frobenius": out.pop("matrix_rel_frobenius_mixed"),
+                      "matrix_rel_frobenius_mixed_accurate": out.pop("matrix_rel_frobenius_mixed_accurate")}))
 
 
 # ---- batched and served workloads -------------------------------------------------------
