@@ -14,7 +14,7 @@ from conftest import ROOT
 CSRC = os.path.join(ROOT, "beast.jl_gb300", "csrc")
 
 HARNESS = r"""
-#include "dfloat.h"
+#include "far_df.h"
 #include <stdint.h>
 using namespace dfl;
 static df from(double x) { float h = (float)x; return {h, (float)(x - (double)h)}; }
@@ -39,6 +39,31 @@ void t_sincos(const double* th, int64_t n, double* s, double* c) {
 void t_green(const double* R, const double* k, int64_t n, double* out) {
   for (int64_t i = 0; i < n; ++i) { df re, im; green(from(R[i]), from(k[i]), &re, &im); out[2 * i] = to(re); out[2 * i + 1] = to(im); }
 }
+// EFIE far block of one cell pair from double geometry (staged as the kernel would: centroid
+// differences and rule points relative to the centroids in double, then split into pairs)
+void t_efie_pair(const double* tv, const double* bv, int no, const double* uvo, const double* wo, int ni,
+                 const double* uvi, const double* wi, double k, const double* al, const double* be, double* out) {
+  double cp[3], cq[3];
+  for (int c = 0; c < 3; ++c) { cp[c] = (tv[c] + tv[3 + c] + tv[6 + c]) / 3; cq[c] = (bv[c] + bv[3 + c] + bv[6 + c]) / 3; }
+  df d[3], tau[3][3], sig[3][3], xi[16][3], eta[16][3], w1[16], w2[16];
+  for (int c = 0; c < 3; ++c) d[c] = from(cp[c] - cq[c]);
+  for (int i = 0; i < 3; ++i)
+    for (int c = 0; c < 3; ++c) { tau[i][c] = from(tv[3 * i + c] - cp[c]); sig[i][c] = from(bv[3 * i + c] - cq[c]); }
+  for (int a = 0; a < no; ++a) {
+    const double u = uvo[2 * a], v = uvo[2 * a + 1], w = 1 - u - v;
+    for (int c = 0; c < 3; ++c) xi[a][c] = from(u * (tv[c] - cp[c]) + v * (tv[3 + c] - cp[c]) + w * (tv[6 + c] - cp[c]));
+    w1[a] = from(wo[a]);
+  }
+  for (int b = 0; b < ni; ++b) {
+    const double u = uvi[2 * b], v = uvi[2 * b + 1], w = 1 - u - v;
+    for (int c = 0; c < 3; ++c) eta[b][c] = from(u * (bv[c] - cq[c]) + v * (bv[3 + c] - cq[c]) + w * (bv[6 + c] - cq[c]));
+    w2[b] = from(wi[b]);
+  }
+  cdf z[9];
+  efie_far_pair(d, tau, sig, no, xi, w1, ni, eta, w2, from(k), cdf{from(al[0]), from(al[1])},
+                cdf{from(be[0]), from(be[1])}, z);
+  for (int e = 0; e < 9; ++e) { out[2 * e] = to(z[e].re); out[2 * e + 1] = to(z[e].im); }
+}
 }
 """
 
@@ -59,7 +84,7 @@ def lib(tmp_path_factory):
     subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I", CSRC, str(src), "-o", str(so)],
                    check=True)
     L = C.CDLL(str(so))
-    for f in ("t_two", "t_ops", "t_sincos", "t_green"):
+    for f in ("t_two", "t_ops", "t_sincos", "t_green", "t_efie_pair"):
         getattr(L, f).restype = None
     return L
 
@@ -121,10 +146,47 @@ def test_device_compile(tmp_path):
     if not os.path.exists(nvcc):
         pytest.skip("nvcc not available")
     src = tmp_path / "k.cu"
-    src.write_text('#include "dfloat.h"\n'
+    src.write_text('#include "far_df.h"\n'
                    "__global__ void k(const float* r, float* o) {\n"
-                   "  dfl::df re, im;\n"
-                   "  dfl::green(dfl::df{r[threadIdx.x], 0.f}, dfl::df{10.f, 0.f}, &re, &im);\n"
-                   "  o[threadIdx.x] = re.hi + im.lo;\n}\n")
+                   "  using namespace dfl;\n"
+                   "  df re, im;\n"
+                   "  green(df{r[threadIdx.x], 0.f}, df{10.f, 0.f}, &re, &im);\n"
+                   "  df d[3] = {re, im, re}, t[3][3] = {}, x[3][3] = {}, w[3] = {re, re, re};\n"
+                   "  cdf z[9];\n"
+                   "  efie_far_pair(d, t, t, 3, x, w, 3, x, w, re, cdf{re, im}, cdf{im, re}, z);\n"
+                   "  o[threadIdx.x] = z[4].re.hi + z[8].im.lo;\n}\n")
     subprocess.run([nvcc, "-gencode", "arch=compute_103a,code=sm_103a", "-c", "-I", CSRC, str(src), "-o",
                     str(tmp_path / "k.o")], check=True)
+
+
+def test_efie_far_pair_matches_the_fp64_oracle(lib):
+    """the double-float EFIE far block against the oracle's FP64 double quadrature (the
+    reference's DoubleQuadRule), on far pairs of a level-3 icosphere at k = 10"""
+    import beastgpu as bg
+    import oracle as O
+    m = bg.icosphere(3)
+    T = np.asarray(m.vertices)[np.asarray(m.cells)]
+    k = 10.0
+    g = 1j * k
+    al, be = -g, -1 / g
+    op = O.make_op(O.MW_SL, g, al, be)
+    qs = O.make_qs(O.QS_WILTON_SAUTER, 2, 3, 6, 7, 5, 5, 4, 3)
+    uvo, wo = O.trirule(2)
+    uvi, wi = O.trirule(3)
+    rng = np.random.default_rng(4)
+    worst, tested = 0.0, 0
+    for p, q in rng.integers(0, T.shape[0], size=(400, 2)):
+        if O.classify(op, qs, T[p], T[q]) != 0:
+            continue
+        ref = O.cellpair(op, O.RT, O.RT, T[p], T[q], O.RULE_DQ, 2, 3)
+        out = np.zeros(18)
+        args = [np.ascontiguousarray(a, np.float64) for a in (T[p].ravel(), T[q].ravel(), uvo.ravel(), wo,
+                                                              uvi.ravel(), wi, [al.real, al.imag],
+                                                              [be.real, be.imag])]
+        lib.t_efie_pair(_p(args[0]), _p(args[1]), C.c_int(len(wo)), _p(args[2]), _p(args[3]), C.c_int(len(wi)),
+                        _p(args[4]), _p(args[5]), C.c_double(k), _p(args[6]), _p(args[7]), _p(out))
+        z = (out[0::2] + 1j * out[1::2]).reshape(3, 3)
+        worst = max(worst, np.abs(z - ref).max() / np.abs(ref).max())
+        tested += 1
+    assert tested > 300
+    assert worst < 1e-10, worst
