@@ -14,5 +14,6 @@ from .operators import (Maxwell3D, Helmholtz3D, nxdoublelayer, Identity, NCross,
 from .api import (Context, get_context, assemble, assemble_rhs, solve, gmres, farfield,
                   solve_job, blockassembler, assemblerow, assemblecol)
 from .serve import Server, run_job, job_footprint
+from .refine import barycentric_refinement, buffachristiansen, refined
 
 __all__ = [n for n in dir() if not n.startswith("_")]
