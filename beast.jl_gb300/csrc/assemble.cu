@@ -22,6 +22,7 @@
 #include <cmath>
 
 #include "internal.h"
+#include "se_p1.h"
 
 namespace {
 
@@ -764,9 +765,10 @@ DEV void wilton(const Geo& s, V3<double> x, Wilton& W) {
   W.d = d;
 }
 
-// singular part at one test point x (weight dx); returns false if not available
+// singular part at one test point x (barycentrics bx in the test cell, weight dx); returns
+// false if not available
 DEV bool se_singular(const OpParams& op, int tk, int bk, const Geo& t, const Geo& s,
-                     V3<double> x, double dx, C2<double>* acc) {
+                     V3<double> x, const double* bx, double dx, C2<double>* acc) {
   Wilton W;
   wilton(s, x, W);
   V3<double> rho = x - W.d * W.n;
@@ -822,9 +824,26 @@ DEV bool se_singular(const OpParams& op, int tk, int bk, const Geo& t, const Geo
       return true;
     }
     case BEAST_HH_SL: {
-      if (tk != BEAST_P0 || bk != BEAST_P0) return false;
-      C2<double> iG = cscale(1.0 / (4 * PI), cadd(C2<double>{W.S[1], 0}, cscale(W.S[3], h)));
-      acc[0] = cadd(acc[0], cscale(dx, cmul(al, iG)));
+      // src/helmholtz3d/wiltonints.jl:19-135: P0 or P1 on either side; a P1 trial shape's
+      // integrals against 1/R and R come from the first-order potential integrals (se_p1.h),
+      // a P1 test shape is the barycentric coordinate of x
+      const int nt = tk == BEAST_P0 ? 1 : 3, nb = bk == BEAST_P0 ? 1 : 3;
+      C2<double> iG[3];
+      if (bk == BEAST_P0) {
+        iG[0] = cscale(1.0 / (4 * PI), cadd(C2<double>{W.S[1], 0}, cscale(W.S[3], h)));
+      } else {
+        const double v[3][3] = {{s.v[0].x, s.v[0].y, s.v[0].z}, {s.v[1].x, s.v[1].y, s.v[1].z},
+                                {s.v[2].x, s.v[2].y, s.v[2].z}};
+        const double nn[3] = {W.n.x, W.n.y, W.n.z}, rr[3] = {rho.x, rho.y, rho.z};
+        const double v1[3] = {W.V[1].x, W.V[1].y, W.V[1].z}, v3[3] = {W.V[3].x, W.V[3].y, W.V[3].z};
+        double i1[3], i3[3];
+        se_p1_moments(v, nn, rr, W.S[1], W.S[3], v1, v3, i1, i3);
+        for (int j = 0; j < 3; ++j) iG[j] = cscale(1.0 / (4 * PI), cadd(C2<double>{i1[j], 0}, cscale(i3[j], h)));
+      }
+      for (int i = 0; i < nt; ++i) {
+        const double ft = tk == BEAST_P0 ? 1.0 : bx[i];
+        for (int j = 0; j < nb; ++j) acc[i * nb + j] = cadd(acc[i * nb + j], cscale(dx * ft, cmul(al, iG[j])));
+      }
       return true;
     }
     case BEAST_HH_DL:
@@ -1350,7 +1369,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
     for (int a = lane; a < no; a += 32) {
       double bx[3] = {P.ro.u[a], P.ro.v[a], 1.0 - P.ro.u[a] - P.ro.v[a]};
       V3<double> x = bx[0] * t.v[0] + bx[1] * t.v[1] + bx[2] * t.v[2];
-      if (!se_singular(P.op, P.tk, P.bk, t, s, x, P.ro.w[a] * t.area, acc)) atomicOr(P.flag, 2);
+      if (!se_singular(P.op, P.tk, P.bk, t, s, x, bx, P.ro.w[a] * t.area, acc)) atomicOr(P.flag, 2);
     }
   }
   // ---- warp reduction and store

@@ -655,9 +655,29 @@ bool se_singular(const Op& op, int tk, int bk, const Tri& t, const Tri& s, V3 x,
       return true;
     }
     case ORC_HH_SL: {
-      if (tk != ORC_P0 || bk != ORC_P0) return false;
-      cplx iG = (scal[1] + 0.5 * g * g * scal[3]) / (4 * PI);
-      out[0] += op.alpha * iG * dx;
+      // src/helmholtz3d/wiltonints.jl:19-135: P0 or P1 on either side.  A P1 trial shape is
+      // affine in the plane, lambda_j(y) = lambda_j(rho) + grad lambda_j . (rho' - rho), so its
+      // integrals against 1/R and R follow from scal and vec (the reference takes them from
+      // WiltonInts84.higherorder); a P1 test shape is the barycentric coordinate of x.
+      const cplx h = 0.5 * g * g;
+      const int nt = tk == ORC_P0 ? 1 : 3, nb = bk == ORC_P0 ? 1 : 3;
+      cplx iG[3];
+      if (bk == ORC_P0) {
+        iG[0] = (scal[1] + h * scal[3]) / (4 * PI);
+      } else {
+        const double twoA = dot(cross(s.v[1] - s.v[0], s.v[2] - s.v[0]), ns);
+        for (int j = 0; j < 3; ++j) {
+          const V3 a = s.v[(j + 1) % 3], b = s.v[(j + 2) % 3];
+          const double lr = dot(cross(a - rho, b - rho), ns) / twoA;
+          const V3 gl = (1.0 / twoA) * cross(ns, b - a);
+          const double i1 = lr * scal[1] + dot(gl, VEC(1)), i3 = lr * scal[3] + dot(gl, VEC(3));
+          iG[j] = (i1 + h * i3) / (4 * PI);
+        }
+      }
+      for (int i = 0; i < nt; ++i) {
+        const double ft = tk == ORC_P0 ? 1.0 : bx[i];
+        for (int j = 0; j < nb; ++j) out[i * nb + j] += op.alpha * ft * iG[j] * dx;
+      }
       return true;
     }
     case ORC_HH_DL:
