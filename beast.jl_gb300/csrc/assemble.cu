@@ -848,17 +848,34 @@ DEV bool se_singular(const OpParams& op, int tk, int bk, const Geo& t, const Geo
     }
     case BEAST_HH_DL:
     case BEAST_HH_DLT: {
-      if (tk != BEAST_P0 || bk != BEAST_P0) return false;
-      CV<double> iDG;
-      iDG.x = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.x, 0}, cscale(gR.x, h)));
-      iDG.y = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.y, 0}, cscale(gR.y, h)));
-      iDG.z = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.z, 0}, cscale(gR.z, h)));
-      C2<double> v;
-      if (op.kind == BEAST_HH_DL)
-        v = cscale(-1.0, rdot(s.n, iDG));
-      else
-        v = rdot(t.n, iDG);
-      acc[0] = cadd(acc[0], cscale(dx, cmul(al, v)));
+      // P0 or P1 test shapes (a factor: the barycentric coordinate of x); P1 trial shapes for the
+      // double layer, whose source normal is constant on the flat trial triangle (se_p1.h).  The
+      // transposed double layer with P1 trial shapes needs in-plane second moments: unavailable.
+      if (op.kind == BEAST_HH_DLT && bk != BEAST_P0) return false;
+      const int nt = tk == BEAST_P0 ? 1 : 3, nb = bk == BEAST_P0 ? 1 : 3;
+      C2<double> v[3];
+      if (bk == BEAST_P0) {
+        CV<double> iDG;
+        iDG.x = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.x, 0}, cscale(gR.x, h)));
+        iDG.y = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.y, 0}, cscale(gR.y, h)));
+        iDG.z = cscale(-1.0 / (4 * PI), cadd(C2<double>{gm1.z, 0}, cscale(gR.z, h)));
+        if (op.kind == BEAST_HH_DL)
+          v[0] = cscale(-1.0, rdot(s.n, iDG));
+        else
+          v[0] = rdot(t.n, iDG);
+      } else {
+        const double sv[3][3] = {{s.v[0].x, s.v[0].y, s.v[0].z}, {s.v[1].x, s.v[1].y, s.v[1].z},
+                                 {s.v[2].x, s.v[2].y, s.v[2].z}};
+        const double nn[3] = {W.n.x, W.n.y, W.n.z}, rr[3] = {rho.x, rho.y, rho.z};
+        const double v0[3] = {W.V[0].x, W.V[0].y, W.V[0].z}, v1[3] = {W.V[1].x, W.V[1].y, W.V[1].z};
+        double iA[3], iB[3];
+        se_p1_dl_moments(sv, nn, rr, W.d, W.S[0], W.S[1], v0, v1, iA, iB);
+        for (int j = 0; j < 3; ++j) v[j] = cscale(1.0 / (4 * PI), csub(C2<double>{iA[j], 0}, cscale(iB[j], h)));
+      }
+      for (int i = 0; i < nt; ++i) {
+        const double ft = tk == BEAST_P0 ? 1.0 : bx[i];
+        for (int j = 0; j < nb; ++j) acc[i * nb + j] = cadd(acc[i * nb + j], cscale(dx * ft, cmul(al, v[j])));
+      }
       return true;
     }
   }

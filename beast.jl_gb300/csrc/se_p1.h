@@ -46,3 +46,22 @@ SEP1_HD void se_p1_moments(const double (*v)[3], const double* n, const double* 
     out3[j] = lr * S3 + (g[0] * V3[0] + g[1] * V3[1] + g[2] * V3[2]) / a2;
   }
 }
+
+// Double layer (normal derivative at the source, flat trial triangle): with d = n.(x - y), the
+// same for every y of the triangle, n.grad_y(1/R) = d/R^3 and n.grad_y R = -d/R, so
+//   outA[j] = int lambda_j d / R^3 = lambda_j(rho) S0 + d grad lambda_j . V0,
+//   outB[j] = int lambda_j d / R   = d (lambda_j(rho) S1 + grad lambda_j . V1),
+// S0 = int d / R^3 (the signed solid angle), V0 = int (rho' - rho) / R^3.
+SEP1_HD void se_p1_dl_moments(const double (*v)[3], const double* n, const double* rho, double d, double S0,
+                              double S1, const double* V0, const double* V1, double* outA, double* outB) {
+  double l1[3], l3[3];
+  // lambda_j(rho) and grad lambda_j . V through se_p1_moments with (S, V) = (S0, V0), (S1, V1)
+  se_p1_moments(v, n, rho, S0, S1, V0, V1, l1, l3);
+  // l1[j] = lambda_j(rho) S0 + g.V0 and l3[j] = lambda_j(rho) S1 + g.V1: scale the V0 part by d
+  double z3[3] = {0, 0, 0}, lr0[3], lr1[3];
+  se_p1_moments(v, n, rho, 1.0, 0.0, z3, z3, lr0, lr1);  // lr0[j] = lambda_j(rho)
+  for (int j = 0; j < 3; ++j) {
+    outA[j] = lr0[j] * S0 + d * (l1[j] - lr0[j] * S0);
+    outB[j] = d * l3[j];
+  }
+}

@@ -682,19 +682,39 @@ bool se_singular(const Op& op, int tk, int bk, const Tri& t, const Tri& s, V3 x,
     }
     case ORC_HH_DL:
     case ORC_HH_DLT: {
-      if (tk != ORC_P0 || bk != ORC_P0) return false;
-      cplx h = 0.5 * g * g;
-      CV3 iDG;
-      iDG.x = -(gm1.x + h * gR.x) / (4 * PI);
-      iDG.y = -(gm1.y + h * gR.y) / (4 * PI);
-      iDG.z = -(gm1.z + h * gR.z) / (4 * PI);
-      if (op.kind == ORC_HH_DL) {
-        cplx ndg = ns.x * iDG.x + ns.y * iDG.y + ns.z * iDG.z;
-        out[0] += op.alpha * (-ndg) * dx;
+      // P0 or P1 test shapes (a factor: the barycentric coordinate of x).  Trial P1 for the
+      // double layer: the source normal is constant on the flat trial triangle, so
+      // n.grad'(1/R) = d/R^3 and n.grad' R = -d/R with d = n.(x - y) fixed, and the shape
+      // moments follow from scal / vec as for the single layer.  The transposed double layer
+      // with P1 trial shapes needs in-plane second moments (the reference's
+      // WiltonInts84.higherorder): not available.
+      if (op.kind == ORC_HH_DLT && bk != ORC_P0) return false;
+      const cplx h = 0.5 * g * g;
+      const int nt = tk == ORC_P0 ? 1 : 3, nb = bk == ORC_P0 ? 1 : 3;
+      cplx v[3];
+      if (bk == ORC_P0) {
+        CV3 iDG;
+        iDG.x = -(gm1.x + h * gR.x) / (4 * PI);
+        iDG.y = -(gm1.y + h * gR.y) / (4 * PI);
+        iDG.z = -(gm1.z + h * gR.z) / (4 * PI);
+        const V3 nn = op.kind == ORC_HH_DL ? ns : t.n;
+        const cplx ndg = nn.x * iDG.x + nn.y * iDG.y + nn.z * iDG.z;
+        v[0] = op.kind == ORC_HH_DL ? -ndg : ndg;
       } else {
-        V3 nt = t.n;
-        cplx ndg = nt.x * iDG.x + nt.y * iDG.y + nt.z * iDG.z;
-        out[0] += op.alpha * ndg * dx;
+        const double twoA = dot(cross(s.v[1] - s.v[0], s.v[2] - s.v[0]), ns);
+        const double d = dot(x - s.v[0], ns);
+        for (int j = 0; j < 3; ++j) {
+          const V3 a = s.v[(j + 1) % 3], b = s.v[(j + 2) % 3];
+          const double lr = dot(cross(a - rho, b - rho), ns) / twoA;
+          const V3 gl = (1.0 / twoA) * cross(ns, b - a);
+          const double iA = lr * scal[0] + d * dot(gl, VEC(0));  // int lambda_j d / R^3
+          const double iB = d * (lr * scal[1] + dot(gl, VEC(1)));  // int lambda_j d / R
+          v[j] = (iA - h * iB) / (4 * PI);
+        }
+      }
+      for (int i = 0; i < nt; ++i) {
+        const double ft = tk == ORC_P0 ? 1.0 : bx[i];
+        for (int j = 0; j < nb; ++j) out[i * nb + j] += op.alpha * ft * v[j] * dx;
       }
       return true;
     }

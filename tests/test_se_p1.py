@@ -25,16 +25,20 @@ def moments(tmp_path_factory):
     (d / "h.cpp").write_text('#include "se_p1.h"\n'
                              'extern "C" void t(const double* v, const double* n, const double* rho, double S1, '
                              'double S3, const double* V1, const double* V3, double* o1, double* o3) {\n'
-                             '  se_p1_moments((const double (*)[3])v, n, rho, S1, S3, V1, V3, o1, o3);\n}\n')
+                             '  se_p1_moments((const double (*)[3])v, n, rho, S1, S3, V1, V3, o1, o3);\n}\n'
+                             'extern "C" void t_dl(const double* v, const double* n, const double* rho, double d, '
+                             'double S0, double S1, const double* V0, const double* V1, double* oa, double* ob) {\n'
+                             '  se_p1_dl_moments((const double (*)[3])v, n, rho, d, S0, S1, V0, V1, oa, ob);\n}\n')
     subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-I", CSRC, str(d / "h.cpp"), "-o", str(d / "h.so")],
                    check=True)
     L = C.CDLL(str(d / "h.so"))
     L.t.restype = None
+    L.t_dl.restype = None
     return L
 
 
-def _brute(v, x, levels=6):
-    """int lambda_j / R and int lambda_j R over the triangle: degree-8 rule on 4^levels pieces"""
+def _brute(v, x, levels=6, powers=(-1, 1)):
+    """int lambda_j R^p over the triangle for p in powers: degree-8 rule on 4^levels pieces"""
     uv, w = O.trirule(8)
     N = 2 ** levels
     pts, wts = [], []
@@ -53,7 +57,7 @@ def _brute(v, x, levels=6):
     lam = np.c_[p, 1 - p.sum(1)]
     y = lam @ v
     R = np.linalg.norm(x - y, axis=1)
-    return (wt / R) @ lam, (wt * R) @ lam
+    return tuple((wt * R ** p) @ lam for p in powers)
 
 
 def test_p1_moments_against_quadrature(moments):
@@ -70,9 +74,16 @@ def test_p1_moments_against_quadrature(moments):
         o1, o3 = np.zeros(3), np.zeros(3)
         moments.t(P(v), P(n), P(rho), C.c_double(s[1]), C.c_double(s[3]), P(vec[1]), P(vec[3]),
                   o1.ctypes.data_as(C.c_void_p), o3.ctypes.data_as(C.c_void_p))
-        b1, b3 = _brute(v, x)
+        b1, b3, bm3 = _brute(v, x, powers=(-1, 1, -3))
         assert np.abs(o1 - b1).max() < 1e-8 * np.abs(b1).max()
         assert np.abs(o3 - b3).max() < 1e-8 * np.abs(b3).max()
+        # double layer: int lambda_j d / R^3 and int lambda_j d / R
+        dd = float(np.dot(x - v[0], n))
+        oa, ob = np.zeros(3), np.zeros(3)
+        moments.t_dl(P(v), P(n), P(rho), C.c_double(dd), C.c_double(s[0]), C.c_double(s[1]), P(vec[0]),
+                     P(vec[1]), oa.ctypes.data_as(C.c_void_p), ob.ctypes.data_as(C.c_void_p))
+        assert np.abs(oa - dd * bm3).max() < 1e-8 * np.abs(dd * bm3).max()
+        assert np.abs(ob - dd * b1).max() < 1e-8 * np.abs(dd * b1).max()
 
 
 def _children(v):
@@ -119,3 +130,30 @@ def test_oracle_p1_singularity_extraction():
         assert abs(se[O.P0, O.P1].sum() - z00) < 1e-12 * abs(z00)
         assert abs(se[O.P1, O.P0].sum() - z00) < 1e-12 * abs(z00)
         assert np.abs(se[O.P1, O.P1].sum(1) - se[O.P1, O.P0][:, 0]).max() < 1e-12 * abs(z00)
+
+
+@pytest.mark.parametrize("kind", [O.HH_DL, O.HH_DLT])
+def test_oracle_p1_double_layer_singularity_extraction(kind):
+    """double layer with P1 on either side (n.grad' of the kernel is d/R^3, -d/R on the flat trial
+    triangle) and the transposed double layer with P1 test shapes: exact partition of unity, and
+    the same accuracy class as the pinned P0 x P0 extraction against converged subdivided
+    quadrature"""
+    rng = np.random.default_rng(5)
+    op = O.make_op(kind, 2j, 1.0)
+    tv = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0.]])
+    combos = [(O.P0, O.P0), (O.P1, O.P0)] + ([(O.P0, O.P1), (O.P1, O.P1)] if kind == O.HH_DL else [])
+    for trial in range(2):
+        bv = tv + np.array([0.3 * rng.uniform(), 0.3 * rng.uniform(), 0.12 + 0.1 * trial]) + \
+            0.05 * rng.normal(size=(3, 3))
+        se, err = {}, {}
+        for tk, bk in combos:
+            se[tk, bk] = O.cellpair(op, tk, bk, tv, bv, O.RULE_SE, 10, 10)
+            ref = _dq_subdivided(op, tk, bk, tv, bv)
+            err[tk, bk] = np.abs(se[tk, bk] - ref).max() / np.abs(ref).max()
+        for c in combos[1:]:
+            assert err[c] < max(5 * err[O.P0, O.P0], 1e-4), (c, err)
+        z00 = se[O.P0, O.P0][0, 0]
+        assert abs(se[O.P1, O.P0].sum() - z00) < 1e-12 * abs(z00)
+        if kind == O.HH_DL:
+            assert abs(se[O.P0, O.P1].sum() - z00) < 1e-12 * abs(z00)
+            assert np.abs(se[O.P1, O.P1].sum(1) - se[O.P1, O.P0][:, 0]).max() < 1e-12 * abs(z00)
