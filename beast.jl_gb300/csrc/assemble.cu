@@ -848,10 +848,9 @@ DEV bool se_singular(const OpParams& op, int tk, int bk, const Geo& t, const Geo
     }
     case BEAST_HH_DL:
     case BEAST_HH_DLT: {
-      // P0 or P1 test shapes (a factor: the barycentric coordinate of x); P1 trial shapes for the
-      // double layer, whose source normal is constant on the flat trial triangle (se_p1.h).  The
-      // transposed double layer with P1 trial shapes needs in-plane second moments: unavailable.
-      if (op.kind == BEAST_HH_DLT && bk != BEAST_P0) return false;
+      // P0 or P1 test shapes (a factor: the barycentric coordinate of x).  P1 trial shapes
+      // (se_p1.h): for the double layer the source normal is constant on the flat trial triangle;
+      // the transposed double layer adds the in-plane second moments of rho' - rho.
       const int nt = tk == BEAST_P0 ? 1 : 3, nb = bk == BEAST_P0 ? 1 : 3;
       C2<double> v[3];
       if (bk == BEAST_P0) {
@@ -869,8 +868,15 @@ DEV bool se_singular(const OpParams& op, int tk, int bk, const Geo& t, const Geo
         const double nn[3] = {W.n.x, W.n.y, W.n.z}, rr[3] = {rho.x, rho.y, rho.z};
         const double v0[3] = {W.V[0].x, W.V[0].y, W.V[0].z}, v1[3] = {W.V[1].x, W.V[1].y, W.V[1].z};
         double iA[3], iB[3];
-        se_p1_dl_moments(sv, nn, rr, W.d, W.S[0], W.S[1], v0, v1, iA, iB);
-        for (int j = 0; j < 3; ++j) v[j] = cscale(1.0 / (4 * PI), csub(C2<double>{iA[j], 0}, cscale(iB[j], h)));
+        if (op.kind == BEAST_HH_DL) {
+          se_p1_dl_moments(sv, nn, rr, W.d, W.S[0], W.S[1], v0, v1, iA, iB);
+          for (int j = 0; j < 3; ++j) v[j] = cscale(1.0 / (4 * PI), csub(C2<double>{iA[j], 0}, cscale(iB[j], h)));
+        } else {
+          // -(nx . int lambda_j grad'(1/R) + h nx . int lambda_j grad' R) / (4 pi)
+          const double nx[3] = {t.n.x, t.n.y, t.n.z};
+          se_p1_dlt_moments(sv, nn, rr, W.d, W.S[0], W.S[1], W.S[3], v0, v1, nx, iA, iB);
+          for (int j = 0; j < 3; ++j) v[j] = cscale(-1.0 / (4 * PI), cadd(C2<double>{iA[j], 0}, cscale(iB[j], h)));
+        }
       }
       for (int i = 0; i < nt; ++i) {
         const double ft = tk == BEAST_P0 ? 1.0 : bx[i];

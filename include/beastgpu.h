@@ -146,9 +146,8 @@ int beast_space_free(beast_space* space);
  * accumulate = 0 overwrites the addressed block, 1 adds (linear combinations,
  * src/operator.jl:294-304).  precision: BEAST_FP64 or BEAST_MIXED (BEAST_MIXED_ACCURATE
  * assembles as BEAST_FP64).  Singularity-extraction pairs (DoubleNumWiltonSauterQStrat) are
- * available for the Maxwell operators on RT and the Helmholtz single and double layers on any
- * P0 / P1 combination; the transposed double layer with P1 trial shapes returns
- * BEAST_ERR_UNSUPPORTED when such a pair occurs (DoubleNumSauterQstrat avoids them). */
+ * available for the Maxwell operators on RT and the Helmholtz single, double and transposed
+ * double layers on any P0 / P1 combination. */
 int beast_assemble(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs,
                    const beast_space* test, const beast_space* trial, int precision, void* Z,
                    int64_t ldz, int z_dtype, int z_loc, int64_t row_off, int64_t col_off,

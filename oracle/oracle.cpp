@@ -686,9 +686,8 @@ bool se_singular(const Op& op, int tk, int bk, const Tri& t, const Tri& s, V3 x,
       // double layer: the source normal is constant on the flat trial triangle, so
       // n.grad'(1/R) = d/R^3 and n.grad' R = -d/R with d = n.(x - y) fixed, and the shape
       // moments follow from scal / vec as for the single layer.  The transposed double layer
-      // with P1 trial shapes needs in-plane second moments (the reference's
-      // WiltonInts84.higherorder): not available.
-      if (op.kind == ORC_HH_DLT && bk != ORC_P0) return false;
+      // with P1 trial shapes needs in-plane second moments (the reference takes them from
+      // WiltonInts84.higherorder): built here from the divergence theorem in the plane.
       const cplx h = 0.5 * g * g;
       const int nt = tk == ORC_P0 ? 1 : 3, nb = bk == ORC_P0 ? 1 : 3;
       cplx v[3];
@@ -703,13 +702,47 @@ bool se_singular(const Op& op, int tk, int bk, const Tri& t, const Tri& s, V3 x,
       } else {
         const double twoA = dot(cross(s.v[1] - s.v[0], s.v[2] - s.v[0]), ns);
         const double d = dot(x - s.v[0], ns);
+        // transposed double layer: in-plane second moments of u = rho' - rho,
+        //   Q3 = int u u^T / R^3 = P S1 - sum_e (int_e u / R) m_e^T,
+        //   Q1 = int u u^T / R   = sum_e (int_e u R) m_e^T - P S3
+        // (divergence theorem on d_l(u_k / R) and d_l(u_k R)); their products with a vector w
+        V3 q3w[3], q1w[3];
+        const V3 nt = t.n;
+        auto Q = [&](V3 w, V3* o3, V3* o1) {
+          const V3 pw = w - dot(w, ns) * ns;
+          *o3 = scal[1] * pw;
+          *o1 = (-scal[3]) * pw;
+          for (int e = 0; e < 3; ++e) {
+            const V3 a = s.v[e], b = s.v[(e + 1) % 3];
+            const double len = norm(b - a);
+            const V3 te = (1.0 / len) * (b - a);
+            const V3 me = cross(te, ns);
+            const double sa = dot(a - rho, te), sb = dot(b - rho, te), pe = dot(a - rho, me);
+            const double w2 = pe * pe + d * d;
+            const double ra = std::sqrt(sa * sa + w2), rb = std::sqrt(sb * sb + w2);
+            const double lg = (sa + sb >= 0) ? std::log((sb + rb) / (sa + ra)) : std::log((ra - sa) / (rb - sb));
+            const double ir = 0.5 * (sb * rb - sa * ra + w2 * lg);
+            const V3 f1 = (pe * lg) * me + (rb - ra) * te;
+            const V3 f3 = (pe * ir) * me + ((rb * rb * rb - ra * ra * ra) / 3.0) * te;
+            *o3 = *o3 - dot(me, w) * f1;
+            *o1 = *o1 + dot(me, w) * f3;
+          }
+        };
         for (int j = 0; j < 3; ++j) {
           const V3 a = s.v[(j + 1) % 3], b = s.v[(j + 2) % 3];
           const double lr = dot(cross(a - rho, b - rho), ns) / twoA;
           const V3 gl = (1.0 / twoA) * cross(ns, b - a);
           const double iA = lr * scal[0] + d * dot(gl, VEC(0));  // int lambda_j d / R^3
           const double iB = d * (lr * scal[1] + dot(gl, VEC(1)));  // int lambda_j d / R
-          v[j] = (iA - h * iB) / (4 * PI);
+          if (op.kind == ORC_HH_DL) {
+            v[j] = (iA - h * iB) / (4 * PI);
+          } else {
+            Q(gl, &q3w[j], &q1w[j]);
+            // int lambda_j grad'(1/R) = -(lr V0 + Q3 gl) + n iA ; int lambda_j grad' R = (lr V1 + Q1 gl) - n iB
+            const V3 g1 = (-1.0) * (lr * VEC(0) + q3w[j]) + iA * ns;
+            const V3 gr = (lr * VEC(1) + q1w[j]) - iB * ns;
+            v[j] = -(dot(nt, g1) + h * dot(nt, gr)) / (4 * PI);
+          }
         }
       }
       for (int i = 0; i < nt; ++i) {

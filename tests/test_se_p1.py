@@ -28,12 +28,17 @@ def moments(tmp_path_factory):
                              '  se_p1_moments((const double (*)[3])v, n, rho, S1, S3, V1, V3, o1, o3);\n}\n'
                              'extern "C" void t_dl(const double* v, const double* n, const double* rho, double d, '
                              'double S0, double S1, const double* V0, const double* V1, double* oa, double* ob) {\n'
-                             '  se_p1_dl_moments((const double (*)[3])v, n, rho, d, S0, S1, V0, V1, oa, ob);\n}\n')
+                             '  se_p1_dl_moments((const double (*)[3])v, n, rho, d, S0, S1, V0, V1, oa, ob);\n}\n'
+                             'extern "C" void t_dlt(const double* v, const double* n, const double* rho, double d, '
+                             'double S0, double S1, double S3, const double* V0, const double* V1, const double* nx, '
+                             'double* oa, double* ob) {\n'
+                             '  se_p1_dlt_moments((const double (*)[3])v, n, rho, d, S0, S1, S3, V0, V1, nx, oa, ob);\n}\n')
     subprocess.run(["g++", "-O2", "-fPIC", "-shared", "-I", CSRC, str(d / "h.cpp"), "-o", str(d / "h.so")],
                    check=True)
     L = C.CDLL(str(d / "h.so"))
     L.t.restype = None
     L.t_dl.restype = None
+    L.t_dlt.restype = None
     return L
 
 
@@ -60,6 +65,28 @@ def _brute(v, x, levels=6, powers=(-1, 1)):
     return tuple((wt * R ** p) @ lam for p in powers)
 
 
+def _brute_grad(v, x, nx, levels=6):
+    """nx . int lambda_j grad_y(1/R) and nx . int lambda_j grad_y R (same pieces as _brute)"""
+    uv, w = O.trirule(8)
+    N = 2 ** levels
+    pts, wts = [], []
+    for i in range(N):
+        for j in range(N - i):
+            tris = [((i, j), (i + 1, j), (i, j + 1))]
+            if i + j + 1 < N:
+                tris.append(((i + 1, j), (i, j + 1), (i + 1, j + 1)))
+            for corners in tris:
+                cb = np.array(corners, float) / N
+                pts.append(uv[:, :1] * cb[0] + uv[:, 1:] * cb[1] + (1 - uv.sum(1, keepdims=True)) * cb[2])
+                wts.append(w / (N * N))
+    p = np.concatenate(pts)
+    wt = np.concatenate(wts) * np.linalg.norm(np.cross(v[1] - v[0], v[2] - v[0])) / 2
+    lam = np.c_[p, 1 - p.sum(1)]
+    r = x - lam @ v
+    R = np.linalg.norm(r, axis=1)
+    return (wt * (r @ nx) / R ** 3) @ lam, (wt * -(r @ nx) / R) @ lam
+
+
 def test_p1_moments_against_quadrature(moments):
     rng = np.random.default_rng(0)
     P = lambda a: np.ascontiguousarray(a, np.float64).ctypes.data_as(C.c_void_p)
@@ -84,6 +111,15 @@ def test_p1_moments_against_quadrature(moments):
                      P(vec[1]), oa.ctypes.data_as(C.c_void_p), ob.ctypes.data_as(C.c_void_p))
         assert np.abs(oa - dd * bm3).max() < 1e-8 * np.abs(dd * bm3).max()
         assert np.abs(ob - dd * b1).max() < 1e-8 * np.abs(dd * b1).max()
+        # transposed double layer: nx . int lambda_j grad_y(1/R), nx . int lambda_j grad_y R
+        nx = rng.normal(size=3)
+        nx /= np.linalg.norm(nx)
+        ta, tb = np.zeros(3), np.zeros(3)
+        moments.t_dlt(P(v), P(n), P(rho), C.c_double(dd), C.c_double(s[0]), C.c_double(s[1]), C.c_double(s[3]),
+                      P(vec[0]), P(vec[1]), P(nx), ta.ctypes.data_as(C.c_void_p), tb.ctypes.data_as(C.c_void_p))
+        ga, gb = _brute_grad(v, x, nx)
+        assert np.abs(ta - ga).max() < 1e-8 * np.abs(ga).max()
+        assert np.abs(tb - gb).max() < 1e-8 * np.abs(gb).max()
 
 
 def _children(v):
@@ -134,14 +170,14 @@ def test_oracle_p1_singularity_extraction():
 
 @pytest.mark.parametrize("kind", [O.HH_DL, O.HH_DLT])
 def test_oracle_p1_double_layer_singularity_extraction(kind):
-    """double layer with P1 on either side (n.grad' of the kernel is d/R^3, -d/R on the flat trial
-    triangle) and the transposed double layer with P1 test shapes: exact partition of unity, and
-    the same accuracy class as the pinned P0 x P0 extraction against converged subdivided
-    quadrature"""
+    """double layer (n.grad' of the kernel is d/R^3, -d/R on the flat trial triangle) and
+    transposed double layer (plus the in-plane second moments) with P1 on either side: exact
+    partition of unity, and the same accuracy class as the pinned P0 x P0 extraction against
+    converged subdivided quadrature"""
     rng = np.random.default_rng(5)
     op = O.make_op(kind, 2j, 1.0)
     tv = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0.]])
-    combos = [(O.P0, O.P0), (O.P1, O.P0)] + ([(O.P0, O.P1), (O.P1, O.P1)] if kind == O.HH_DL else [])
+    combos = [(O.P0, O.P0), (O.P1, O.P0), (O.P0, O.P1), (O.P1, O.P1)]
     for trial in range(2):
         bv = tv + np.array([0.3 * rng.uniform(), 0.3 * rng.uniform(), 0.12 + 0.1 * trial]) + \
             0.05 * rng.normal(size=(3, 3))
@@ -154,6 +190,5 @@ def test_oracle_p1_double_layer_singularity_extraction(kind):
             assert err[c] < max(5 * err[O.P0, O.P0], 1e-4), (c, err)
         z00 = se[O.P0, O.P0][0, 0]
         assert abs(se[O.P1, O.P0].sum() - z00) < 1e-12 * abs(z00)
-        if kind == O.HH_DL:
-            assert abs(se[O.P0, O.P1].sum() - z00) < 1e-12 * abs(z00)
-            assert np.abs(se[O.P1, O.P1].sum(1) - se[O.P1, O.P0][:, 0]).max() < 1e-12 * abs(z00)
+        assert abs(se[O.P0, O.P1].sum() - z00) < 1e-12 * abs(z00)
+        assert np.abs(se[O.P1, O.P1].sum(1) - se[O.P1, O.P0][:, 0]).max() < 1e-12 * abs(z00)
