@@ -23,6 +23,7 @@
 
 #include "internal.h"
 #include "se_p1.h"
+#include "far_df.h"
 
 namespace {
 
@@ -1769,6 +1770,118 @@ static cudaError_t far_prec(const FarParams& P, int precision, int c64, cudaStre
   return far_t<OPK, TK, BK, double, 0>(P, st);
 }
 
+// ---- EFIE far pairs in double-float arithmetic (FP64-quality values on the FP32 pipes) -------
+// Same pair loop, near filter and Zcell layout (c128) as k_far<MW_SL, RT, RT, double, 0>; the
+// block of a far pair comes from dfl::efie_far_pair (far_df.h) on pair-split geometry.
+struct FarDfRecord {
+  dfl::df sig[3][3];  // trial vertices minus centroid
+  dfl::df c[3];       // trial centroid
+  float lim;          // near-test radius (radius + threshold distance)
+  float pad;
+  dfl::df eta[RULE_MAXPTS][3];  // inner rule points minus centroid
+  dfl::df w[RULE_MAXPTS];       // inner rule weights
+};
+
+DEV dfl::df df_of(double x) {
+  const float h = (float)x;
+  return dfl::df{h, (float)(x - (double)h)};
+}
+
+__global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
+  __shared__ FarDfRecord rec[FAR_QT];
+  const int ni = P.ri.n, no = P.ro.n;
+  const int q0 = blockIdx.y * FAR_QT;
+  const int nqt = min(FAR_QT, P.nq - q0);
+  for (int k = threadIdx.x; k < nqt * (1 + ni); k += blockDim.x) {
+    const int qi = k / (1 + ni), b = k % (1 + ni);
+    const int qc = P.qcells[q0 + qi];
+    const double* g = P.bgeo + (int64_t)qc * GEO_STRIDE;
+    FarDfRecord& r = rec[qi];
+    const double cx = g[9], cy = g[10], cz = g[11];
+    if (b == 0) {
+      for (int j = 0; j < 3; ++j) {
+        r.sig[j][0] = df_of(g[3 * j] - cx);
+        r.sig[j][1] = df_of(g[3 * j + 1] - cy);
+        r.sig[j][2] = df_of(g[3 * j + 2] - cz);
+      }
+      r.c[0] = df_of(cx);
+      r.c[1] = df_of(cy);
+      r.c[2] = df_of(cz);
+      const double thr2 = near_threshold2(P.qs_kind, P.k2, g[15]);
+      r.lim = (float)((double)P.bgeof[4 * qc + 3] + sqrt(fmax(thr2, 0.0)));
+    } else {
+      const int bb = b - 1;
+      const double u = P.ri.u[bb], v = P.ri.v[bb], w = 1.0 - u - v;
+      r.eta[bb][0] = df_of(u * (g[0] - cx) + v * (g[3] - cx) + w * (g[6] - cx));
+      r.eta[bb][1] = df_of(u * (g[1] - cy) + v * (g[4] - cy) + w * (g[7] - cy));
+      r.eta[bb][2] = df_of(u * (g[2] - cz) + v * (g[5] - cz) + w * (g[8] - cz));
+      r.w[bb] = df_of(P.ri.w[bb]);
+    }
+  }
+  __syncthreads();
+  const int64_t pp = blockIdx.x * (int64_t)FAR_THREADS + threadIdx.x;
+  if (pp >= P.np) return;
+  const int64_t p = P.tperm[pp];
+  const double* tg = P.tgeo + p * GEO_STRIDE;
+  const double cpx = tg[9], cpy = tg[10], cpz = tg[11];
+  const dfl::df cp[3] = {df_of(cpx), df_of(cpy), df_of(cpz)};
+  dfl::df tau[3][3], xi[RULE_MAXPTS][3], wo[RULE_MAXPTS];
+  for (int i = 0; i < 3; ++i) {
+    tau[i][0] = df_of(tg[3 * i] - cpx);
+    tau[i][1] = df_of(tg[3 * i + 1] - cpy);
+    tau[i][2] = df_of(tg[3 * i + 2] - cpz);
+  }
+  for (int a = 0; a < no; ++a) {
+    const double u = P.ro.u[a], v = P.ro.v[a], w = 1.0 - u - v;
+    xi[a][0] = df_of(u * (tg[0] - cpx) + v * (tg[3] - cpx) + w * (tg[6] - cpx));
+    xi[a][1] = df_of(u * (tg[1] - cpy) + v * (tg[4] - cpy) + w * (tg[7] - cpy));
+    xi[a][2] = df_of(u * (tg[2] - cpz) + v * (tg[5] - cpz) + w * (tg[8] - cpz));
+    wo[a] = df_of(P.ro.w[a]);
+  }
+  const float radp = P.tgeof[4 * p + 3];
+  const dfl::df kk = df_of(P.op.gi);
+  const dfl::cdf alpha{df_of(P.op.ar), df_of(P.op.ai)}, beta{df_of(P.op.br), df_of(P.op.bi)};
+  for (int qi = 0; qi < nqt; ++qi) {
+    const FarDfRecord& r = rec[qi];
+    const int ql = q0 + qi;
+    const dfl::df d[3] = {dfl::sub(cp[0], r.c[0]), dfl::sub(cp[1], r.c[1]), dfl::sub(cp[2], r.c[2])};
+    if (P.qs_kind != BEAST_QS_DOUBLENUM) {
+      const float lim = radp + r.lim;
+      const float dd = d[0].hi * d[0].hi + d[1].hi * d[1].hi + d[2].hi * d[2].hi;
+      if (dd <= lim * lim * 1.0001f + 1e-30f) {
+        Geo t = load_geo(tg);
+        Geo s = load_geo(P.bgeo + (int64_t)P.qcells[ql] * GEO_STRIDE);
+        const int cls = classify_exact(t, s, P.qs_kind, P.k2);
+        if (cls != 0) {
+          const int idx = atomicAdd(P.near_count, 1);
+          if (idx < P.near_cap)
+            P.near[idx] = NearPair{(int)pp, ql, cls, 0};
+          else
+            atomicOr(P.flag, 1);
+          for (int i = 0; i < 3; ++i)
+            for (int j = 0; j < 3; ++j)
+              reinterpret_cast<double2*>(P.zcell)[(int64_t)(3 * ql + j) * P.ldc + 3 * pp + i] = make_double2(0, 0);
+          continue;
+        }
+      }
+    }
+    dfl::cdf z[9];
+    dfl::efie_far_pair(d, tau, r.sig, no, xi, wo, ni, r.eta, r.w, kk, alpha, beta, z);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) {
+        const dfl::cdf& v = z[3 * i + j];
+        reinterpret_cast<double2*>(P.zcell)[(int64_t)(3 * ql + j) * P.ldc + 3 * pp + i] =
+            make_double2((double)v.re.hi + (double)v.re.lo, (double)v.im.hi + (double)v.im.lo);
+      }
+  }
+}
+
+static cudaError_t far_efie_df(const FarParams& P, cudaStream_t st) {
+  dim3 grid((unsigned)((P.np + FAR_THREADS - 1) / FAR_THREADS), (unsigned)((P.nq + FAR_QT - 1) / FAR_QT));
+  k_far_efie_df<<<grid, FAR_THREADS, 0, st>>>(P);
+  return cudaGetLastError();
+}
+
 template <int OPK>
 static cudaError_t far_hh(const FarParams& P, int tk, int bk, int precision, int c64, cudaStream_t st) {
   if (tk == BEAST_P0 && bk == BEAST_P0) return far_prec<OPK, BEAST_P0, BEAST_P0>(P, precision, c64, st);
@@ -1804,6 +1917,12 @@ cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev&
   const int kind = a.op.kind;
   if (kind == BEAST_MW_SL || kind == BEAST_MW_DL || kind == BEAST_MW_NXDL) {
     if (tk != BEAST_RT || bk != BEAST_RT) return cudaErrorInvalidValue;
+    if (kind == BEAST_MW_SL && a.precision == BEAST_FP64 && !a.zcell_c64 && P.op.gr == 0.0) {
+      // opt-in (BEAST_FAR_DF=1): the double-float kernel for FP64 EFIE assemblies (real
+      // wavenumber), at a fraction of the FP64 kernel's time on GB300
+      const char* e = getenv("BEAST_FAR_DF");
+      if (e && e[0] == '1') return far_efie_df(P, st);
+    }
     if (kind == BEAST_MW_SL) return far_prec<BEAST_MW_SL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_c64, st);
     if (kind == BEAST_MW_DL) return far_prec<BEAST_MW_DL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_c64, st);
     return far_prec<BEAST_MW_NXDL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_c64, st);
