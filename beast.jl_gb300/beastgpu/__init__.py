@@ -15,5 +15,6 @@ from .api import (Context, get_context, assemble, assemble_rhs, solve, gmres, fa
                   solve_job, blockassembler, assemblerow, assemblecol)
 from .serve import Server, run_job, job_footprint
 from .refine import barycentric_refinement, buffachristiansen, refined
+from . import tune
 
 __all__ = [n for n in dir() if not n.startswith("_")]
