@@ -39,18 +39,8 @@ def job_footprint(n, nrhs=1, precision=L.MIXED, workspace=0):
     return int(zel * n * n + fel * n * n + tc + 16 * n * (2 * nrhs + 4) + workspace + (64 << 20))
 
 
-def run_job(ctx, job):
-    """one job through the C ABI on ctx's stream: mesh + space upload, assembly on the device
-    (plus an optional local operator: `local` = (which, coefficient), e.g. (0, -0.5) for the
-    MFIE's -Id/2), one excitation per plane wave, dense solve with all right-hand sides,
-    solution back to the host.  job: mesh, space, op, waves, exc_kind, and optionally local,
-    precision (default MIXED), tol (default 1e-10).  Returns (x [nrhs, n], iters, resid)."""
-    import torch
-    from . import api
-    from .operators import defaultquadstrat
-    m, X, op, waves, exc_kind = job["mesh"], job["space"], job["op"], job["waves"], job["exc_kind"]
-    prec = job.get("precision", L.MIXED)
-    tol = job.get("tol", 1e-10)
+def _upload(ctx, m, X):
+    """mesh + space handles of (m, X) on ctx"""
     lib = ctx.lib
     ad = X.assemblydata()
     verts = np.ascontiguousarray(m.vertices)
@@ -58,10 +48,68 @@ def run_job(ctx, job):
     mh, sh = C.c_void_p(), C.c_void_p()
     ctx.check(lib.beast_mesh_upload(ctx.handle, verts.ctypes.data, verts.shape[0], cells.ctypes.data,
                                     cells.shape[0], 0, C.byref(mh)))
+    rc = lib.beast_space_upload(ctx.handle, mh, ad.kind, ad.cells.shape[0], ad.cells.ctypes.data, ad.maxfn,
+                                ad.nshapes, ad.dof.ctypes.data, ad.coeff.ctypes.data, X.numfunctions(), 0,
+                                C.byref(sh))
+    if rc != 0:
+        lib.beast_mesh_free(mh)
+        ctx.check(rc)
+    return mh, sh
+
+
+class ResidentSpaces:
+    """the last `capacity` (mesh, space) pairs a context served, kept on the device (least
+    recently used first out), so that requests on a mesh already seen skip the upload"""
+
+    def __init__(self, ctx, capacity):
+        self.ctx = ctx
+        self.capacity = int(capacity)
+        self.entries = collections.OrderedDict()  # id(space) -> (space, mesh handle, space handle)
+        self.uploads = 0
+
+    def handles(self, m, X):
+        e = self.entries.get(id(X))
+        if e is not None and e[0] is X:
+            self.entries.move_to_end(id(X))
+            return e[1], e[2]
+        if e is not None:  # a dead object's id was reused
+            self._free(self.entries.pop(id(X)))
+        mh, sh = _upload(self.ctx, m, X)
+        self.uploads += 1
+        self.entries[id(X)] = (X, mh, sh)
+        while len(self.entries) > self.capacity:
+            self._free(self.entries.popitem(last=False)[1])
+        return mh, sh
+
+    def _free(self, e):
+        self.ctx.lib.beast_space_free(e[2])
+        self.ctx.lib.beast_mesh_free(e[1])
+
+    def close(self):
+        while self.entries:
+            self._free(self.entries.popitem(last=False)[1])
+
+
+def run_job(ctx, job):
+    """one job through the C ABI on ctx's stream: mesh + space upload (or the handles kept by
+    ctx.resident, a ResidentSpaces), assembly on the device (plus an optional local operator:
+    `local` = (which, coefficient), e.g. (0, -0.5) for the MFIE's -Id/2), one excitation per
+    plane wave, dense solve with all right-hand sides, solution back to the host.  job: mesh,
+    space, op, waves, exc_kind, and optionally local, precision (default MIXED), tol (default
+    1e-10).  Returns (x [nrhs, n], iters, resid)."""
+    import torch
+    from . import api
+    from .operators import defaultquadstrat
+    m, X, op, waves, exc_kind = job["mesh"], job["space"], job["op"], job["waves"], job["exc_kind"]
+    prec = job.get("precision", L.MIXED)
+    tol = job.get("tol", 1e-10)
+    lib = ctx.lib
+    resident = getattr(ctx, "resident", None)
+    if resident is not None:
+        mh, sh = resident.handles(m, X)
+    else:
+        mh, sh = _upload(ctx, m, X)
     try:
-        ctx.check(lib.beast_space_upload(ctx.handle, mh, ad.kind, ad.cells.shape[0], ad.cells.ctypes.data,
-                                         ad.maxfn, ad.nshapes, ad.dof.ctypes.data, ad.coeff.ctypes.data,
-                                         X.numfunctions(), 0, C.byref(sh)))
         try:
             n = X.numfunctions()
             nr = len(waves)
@@ -89,19 +137,22 @@ def run_job(ctx, job):
                                             nr, L.DEVICE, tol, 30, C.byref(it), C.byref(res)))
             x = Xs.cpu().numpy()
         finally:
-            lib.beast_space_free(sh)
+            if resident is None:
+                lib.beast_space_free(sh)
     finally:
-        lib.beast_mesh_free(mh)
+        if resident is None:
+            lib.beast_mesh_free(mh)
     return x, it.value, res.value
 
 
 class Server:
     """worker slots (one context and host thread each) behind an admission queue bounded by an
-    HBM budget.  make_context / runner are replaceable (tests drive the admission logic on the
-    CPU with stand-ins); footprint(job) defaults to job_footprint of the job's space."""
+    HBM budget.  resident > 0 keeps that many (mesh, space) pairs on each slot's device context
+    (ResidentSpaces).  make_context / runner are replaceable (tests drive the admission logic on
+    the CPU with stand-ins); footprint(job) defaults to job_footprint of the job's space."""
 
     def __init__(self, slots=2, hbm_budget=None, device=0, allow_pass=False, workspace=None,
-                 make_context=None, runner=None, footprint=None):
+                 make_context=None, runner=None, footprint=None, resident=0):
         if slots < 1:
             raise ValueError("slots must be >= 1")
         if hbm_budget is None:
@@ -122,6 +173,8 @@ class Server:
             def make_context():
                 c = Context(device)
                 c.set_workspace_limit(self.workspace)
+                if resident > 0:  # meshes / spaces kept on the device per slot
+                    c.resident = ResidentSpaces(c, resident)
                 return c
         self._cv = threading.Condition()
         self._pending = collections.deque()
@@ -217,6 +270,8 @@ class Server:
         for t in self._threads:
             t.join()
         for c in self._ctxs:
+            if getattr(c, "resident", None) is not None:
+                c.resident.close()
             if hasattr(c, "close"):
                 c.close()
 

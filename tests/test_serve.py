@@ -110,3 +110,59 @@ def test_a_cancelled_pending_job_never_runs():
         assert first.result(timeout=10) == "first" and last.result(timeout=10) == "last"
         assert waiting.cancelled()
     assert "waiting" not in rec.order("start")
+
+
+class _FakeLib:
+    """stand-in for the C library's mesh / space upload and free calls"""
+
+    def __init__(self):
+        self.next = 1
+        self.live = set()
+        self.uploads = 0
+
+    def _new(self, ref):
+        ref._obj.value = self.next
+        self.live.add(self.next)
+        self.next += 1
+        return 0
+
+    def beast_mesh_upload(self, ctx, verts, nv, cells, nc, base, ref):
+        self.uploads += 1
+        return self._new(ref)
+
+    def beast_space_upload(self, ctx, mh, kind, ncells, cells, maxfn, nshapes, dof, coeff, nf, base, ref):
+        return self._new(ref)
+
+    def beast_space_free(self, h):
+        self.live.remove(h.value)
+
+    def beast_mesh_free(self, h):
+        self.live.remove(h.value)
+
+
+class _FakeCtx:
+    def __init__(self):
+        self.lib = _FakeLib()
+        self.handle = None
+
+    def check(self, rc):
+        assert rc == 0
+
+
+def test_resident_spaces_keep_the_last_used_meshes():
+    from beastgpu.serve import ResidentSpaces
+    import beastgpu as bg
+    ctx = _FakeCtx()
+    meshes = [bg.icosphere(1) for _ in range(3)]
+    spaces = [bg.raviartthomas(m) for m in meshes]
+    res = ResidentSpaces(ctx, capacity=2)
+    h0 = res.handles(meshes[0], spaces[0])
+    assert res.handles(meshes[0], spaces[0]) == h0 and ctx.lib.uploads == 1   # hit: no upload
+    res.handles(meshes[1], spaces[1])
+    res.handles(meshes[0], spaces[0])                                         # 0 most recent
+    res.handles(meshes[2], spaces[2])                                         # evicts 1
+    assert ctx.lib.uploads == 3 and len(ctx.lib.live) == 4                    # 2 pairs of handles
+    res.handles(meshes[1], spaces[1])                                         # upload again
+    assert ctx.lib.uploads == 4 and len(res.entries) == 2
+    res.close()
+    assert not ctx.lib.live
