@@ -48,7 +48,9 @@ def test_efie_icosphere(ctx):
 
 
 def test_efie_reference_mesh_with_near_pairs(ctx):
-    # sphere45 is irregular enough to produce Wilton singularity-extraction pairs
+    # sphere45: an irregular reference mesh (Sauter-Schwab pairs of all three kinds; at k = 3 its
+    # non-touching pairs are all far -- the singularity-extraction pairs are covered in
+    # test_gpu_pending.py on a strongly perturbed ellipsoid)
     X = bg.raviartthomas(bg.readmesh(mesh_path("sphere45.in")))
     op = bg.Maxwell3D.singlelayer(wavenumber=3.0)
     _check(op, X, X, ctx)

@@ -1,5 +1,6 @@
 """GPU parity tests of parts built after the last GPU run (Helmholtz P1 singularity extraction,
-the BC-tested MFIE on the barycentric refinement, the double-float EFIE far kernel).  Staged
+the BC-tested MFIE on the barycentric refinement, the double-float EFIE far kernel) and of the
+Maxwell singularity extraction, which no mesh of the `gpu` tests exercises.  Staged
 under their own marker: `pytest -m gpu_pending` on a GB300; each moves to the `gpu` marker
 once it has passed there.  Without a GPU they skip."""
 import numpy as np
@@ -54,3 +55,10 @@ def test_double_float_efie_far_kernel(ctx, monkeypatch):
     monkeypatch.setenv("BEAST_FAR_DF", "1")
     X = bg.raviartthomas(bg.icosphere(2))
     _check(bg.Maxwell3D.singlelayer(wavenumber=2.0), X, X, ctx)
+
+
+@pytest.mark.parametrize("which", ["singlelayer", "doublelayer"])
+def test_maxwell_singularity_extraction(ctx, which):
+    # the perturbed ellipsoid at k = 0.3 has seven Wilton pairs for the Maxwell strategy
+    X = bg.raviartthomas(bg.ellipsoid(2, (1.0, 0.7, 1.3), perturb=0.3, rng=3))
+    _check(getattr(bg.Maxwell3D, which)(wavenumber=0.3), X, X, ctx)
