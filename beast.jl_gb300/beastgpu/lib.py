@@ -39,7 +39,7 @@ class QsDesc(C.Structure):
 
 EXPORTS = [
     "beast_ctx_create", "beast_ctx_destroy", "beast_last_error", "beast_ctx_set_stream",
-    "beast_ctx_set_workspace_limit", "beast_ctx_synchronize", "beast_mesh_upload",
+    "beast_ctx_set_workspace_limit", "beast_ctx_synchronize", "beast_ctx_set_wait_limit", "beast_mesh_upload",
     "beast_mesh_free", "beast_space_upload", "beast_space_free", "beast_assemble",
     "beast_assemble_block", "beast_assemble_local", "beast_rhs_planewave", "beast_lu_factor", "beast_lu_solve",
     "beast_lu_free", "beast_lu_solve_noalloc", "beast_solve_dense", "beast_gmres", "beast_farfield", "beast_solve_job",
@@ -68,6 +68,7 @@ def load(build_if_needed=True):
     L.beast_ctx_set_stream.argtypes = [vp, vp]
     L.beast_ctx_set_workspace_limit.argtypes = [vp, C.c_size_t]
     L.beast_ctx_synchronize.argtypes = [vp]
+    L.beast_ctx_set_wait_limit.argtypes = [vp, i64]
     L.beast_mesh_upload.argtypes = [vp, vp, i64, vp, i64, i, pp]
     L.beast_mesh_free.argtypes = [vp]
     L.beast_space_upload.argtypes = [vp, vp, i, i64, vp, i, i, vp, vp, i64, i, pp]

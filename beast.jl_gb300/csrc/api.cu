@@ -265,6 +265,12 @@ int beast_prof_launches(beast_ctx* ctx, int64_t* n) {
   return BEAST_OK;
 }
 
+int beast_ctx_set_wait_limit(beast_ctx* ctx, int64_t polls) {
+  ARG_CHECK(ctx, ctx && polls >= 0, "invalid wait limit");
+  ctx->trsv_spin_max = polls;
+  return BEAST_OK;
+}
+
 int beast_ctx_synchronize(beast_ctx* ctx) {
   ARG_CHECK(ctx, ctx, "null context");
   BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
@@ -809,8 +815,7 @@ int beast_lu_solve(beast_ctx* ctx, const beast_lu* lu, int64_t nrhs, void* B, in
   if (set_device(ctx)) return BEAST_ERR_CUDA;
   int rc = lu_solve_dev(ctx, lu->n, lu->A, lu->lda, lu->dtype, lu->ipiv, B, ldb, nrhs);
   if (rc) return rc;
-  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  return BEAST_OK;
+  return trsv_check(ctx);
 }
 
 int beast_lu_free(beast_lu* lu) {
@@ -948,6 +953,7 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
           BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, 0, xk, r, -1.0, 1.0, st));
         }
         double rn = dev_norm(ctx, n, r, nrm);
+        if ((rc = trsv_check(ctx))) break;
         res_max = std::max(res_max, bn > 0 ? rn / bn : rn);
         continue;
       }
@@ -969,6 +975,7 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
         }
         ++it;
         double rn = dev_norm(ctx, n, r, nrm);
+        if ((rc = trsv_check(ctx))) break;
         rel = bn > 0 ? rn / bn : rn;
         if (rel <= tol || it >= maxiter) break;
         // contraction slower than 1/2 per step twice in a row: the factors are not good enough

@@ -46,6 +46,7 @@ struct beast_ctx {
   std::vector<cudaEvent_t> evpool;
   int64_t launches = 0;   // kernels launched by this context (counted always)
   int last_factor_mode = -1;  // factorisation of the last dense solve (beast_last_factor_mode)
+  long long trsv_spin_max = 0;  // polls of one triangular-solve flag wait (0: library default)
   // second (high-priority) stream and events of the factorisation's lookahead, made on first use
   cudaStream_t aux = nullptr;
   cudaEvent_t la_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
@@ -199,6 +200,9 @@ int lu_factor_dev(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, in
 double asym_sample(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int dtype);
 int lu_solve_dev(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int dtype,
                  const int* ipiv, void* B, int64_t ldb, int64_t nrhs);
+// synchronises the context stream; BEAST_ERR_TIMEOUT when a triangular-solve wait of the
+// solves queued since the last lu_solve_dev gave up
+int trsv_check(beast_ctx* ctx);
 // y = alpha * A x + beta * y (FP64 arithmetic, A c128 or c64, x/y c128)
 cudaError_t gemv_dev(int64_t n, const void* A, int64_t lda, int a_c64, const double* x,
                      double* y, double alpha, double beta, cudaStream_t st);

@@ -1420,7 +1420,7 @@ __device__ __forceinline__ void cp_async_wait() {
 
 template <typename T, typename RT>
 __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int64_t n, const T* rhs, T* out,
-                                                   int lower, int* status, const T* dinv) {
+                                                   int lower, int* status, const T* dinv, long long spin_max) {
   constexpr int STG = TrsvRing<T>::STG;
   extern __shared__ __align__(16) unsigned char trsv_smraw[];
   T* ring = reinterpret_cast<T*>(trsv_smraw);  // STG x 16 x 256 elements
@@ -1489,7 +1489,7 @@ __global__ void __launch_bounds__(256) k_trsv_wave(const T* A, int64_t lda, int6
       for (int c = 0; c < 16; ++c) cur[c] = st[c * 256 + tid];
       long long it = 0;
       while (!__all_sync(0xffffffffu, !is_sent(v))) {  // warp-uniform
-        if (++it > TRSV_SPIN_MAX) {
+        if (++it > spin_max) {
           if (!timed_out) atomicOr(status, 8);
           timed_out = true;
           if (is_sent(v)) v = zero;
@@ -2173,7 +2173,10 @@ int trsv_pair(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* per
   BEAST_CUDA_TRY(ctx, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_trsv_wave<T, RT>, 256, ring));
   const int G = std::max(1, std::min(nblk, ctx->num_sms * std::max(occ, 1)));
   int* status = ctx->d_flag;
+  long long spin_max = ctx->trsv_spin_max > 0 ? ctx->trsv_spin_max : TRSV_SPIN_MAX;
   const unsigned ge = (unsigned)((n + 255) / 256);
+  // a stale status from an earlier call must not be reported for this one
+  BEAST_CUDA_TRY(ctx, cudaMemsetAsync(status, 0, sizeof(int), st));
   for (int64_t rr = 0; rr < nrhs; ++rr) {
     T* b = B + rr * ldb;
     // the two triangular solves read the factors once: n^2 elements
@@ -2183,7 +2186,7 @@ int trsv_pair(beast_ctx* ctx, int64_t n, const T* A, int64_t lda, const int* per
     int lower = 1;
     const T* in = tmp;
     T* outp = b;
-    void* args[] = {&A, &lda, &n, &in, &outp, &lower, &status, &dinv};
+    void* args[] = {&A, &lda, &n, &in, &outp, &lower, &status, &dinv, &spin_max};
     BEAST_CUDA_TRY(ctx, cudaLaunchCooperativeKernel((void*)k_trsv_wave<T, RT>, G, 256, args, ring, st));
     k_fill_sentinel<T><<<ge, 256, 0, st>>>(tmp, n);
     lower = 0;
@@ -2255,6 +2258,16 @@ int lu_solve_dev(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int dtyp
                                      (const float2*)lu_dinv(ipiv, n));
   return lu_solve_t<double2, double>(ctx, n, (const double2*)A, lda, ipiv + n, (double2*)B, ldb, nrhs,
                                      (const double2*)lu_dinv(ipiv, n));
+}
+
+// waits for the context stream and reports a triangular-solve flag wait that ran out (status
+// bit 8, cleared at the start of every solve by trsv_pair)
+int trsv_check(beast_ctx* ctx) {
+  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
+  int status = 0;
+  BEAST_CUDA_TRY(ctx, cudaMemcpy(&status, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (status & 8) return beast_fail(ctx, BEAST_ERR_TIMEOUT, "triangular solve: flag wait timed out");
+  return BEAST_OK;
 }
 
 // scratch per call from the device's stream-ordered pool (cheap once the pool holds memory;
@@ -2374,9 +2387,5 @@ extern "C" int beast_lu_solve_noalloc(beast_ctx* ctx, const beast_lu* lu, int64_
                                                  lu->ipiv + lu->n, (double2*)B, ldb, nrhs, scratch,
                                                  (const double2*)lu_dinv(lu->ipiv, lu->n));
   if (rc) return rc;
-  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  int status = 0;
-  BEAST_CUDA_TRY(ctx, cudaMemcpy(&status, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
-  if (status & 8) return beast_fail(ctx, BEAST_ERR_TIMEOUT, "triangular solve: flag wait timed out");
-  return BEAST_OK;
+  return trsv_check(ctx);
 }

@@ -30,6 +30,7 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
+#include <mutex>
 
 #include "internal.h"
 
@@ -93,21 +94,6 @@ __device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map
       : "memory");
 }
 
-// the same box into the same shared-memory offset of every CTA in ctaMask, each CTA's
-// mbarrier at the same offset receiving the bytes it got (this GPU's own memory only)
-__device__ __forceinline__ void tma_load_2d_mc(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar,
-                                               uint16_t mask) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes.multicast::cluster "
-      "[%0], [%1, {%2, %3}], [%4], %5;" ::"r"(dst),
-      "l"((uint64_t)map), "r"(x), "r"(y), "r"(bar), "h"(mask)
-      : "memory");
-}
-
-__device__ __forceinline__ void cluster_sync() {
-  asm volatile("barrier.cluster.arrive.release.aligned;\n\tbarrier.cluster.wait.acquire.aligned;" ::: "memory");
-}
-
 // C' += (chunk in shared memory), element-wise FP32 add performed by the TMA unit
 __device__ __forceinline__ void tma_reduce_add_2d(const CUtensorMap* map, int x, int y, uint32_t src) {
   asm volatile(
@@ -150,13 +136,6 @@ __device__ __forceinline__ void mma_commit(uint32_t bar) {
   asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar)
                : "memory");
 }
-// the same completion signalled on the mbarrier at this offset in every CTA of ctaMask
-__device__ __forceinline__ void mma_commit_mc(uint32_t bar, uint16_t mask) {
-  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.multicast::cluster.b64 [%0], %1;" ::"r"(
-                   bar),
-               "h"(mask)
-               : "memory");
-}
 
 __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
   uint32_t r[16];
@@ -186,12 +165,6 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 // hold an element on or below the diagonal, i.e. column tile n <= m / 4 for row tile m
 // (128 real rows = 64 complex rows against 256 columns); rows come in groups of four with
 // g + 1 tiles each, so tile t of group g = floor((sqrt(2t + 1) - 1) / 2) is found in closed form.
-// PAIR: CTA pairs (clusters of two) take the row tiles 2p, 2p+1 of the same column tile: each
-// CTA loads its own A' tile and half of the B' tile, multicast into both CTAs' shared
-// memory (the pair reads B' from L2 once), and a stage is refilled once both CTAs' MMAs have
-// consumed it (each MMA warp's commit arrives on the empty barrier of both).  Tile counts
-// (ntiles0, ntiles) then count pairs; a tile beyond its rectangle (odd row-tile count) is
-// computed -- its B' half is needed by the partner -- but not stored.
 struct TcRegion {
   int m_rows[2], n_cols[2], b_col[2], c_col0[2];
   int c_row0;
@@ -199,7 +172,6 @@ struct TcRegion {
   int lower;
 };
 
-template <bool PAIR>
 __global__ void __launch_bounds__(192, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const __grid_constant__ CUtensorMap tmC0, const __grid_constant__ CUtensorMap tmC1,
@@ -221,35 +193,24 @@ __global__ void __launch_bounds__(192, 1)
   volatile int* s_abort = &s_abort_mem;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = Rg.ntiles;
-  uint32_t rank = 0;
-  if (PAIR) asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(rank));
-  const int unit0 = PAIR ? (int)(blockIdx.x >> 1) : (int)blockIdx.x;  // first tile (pair) of this CTA
-  const int nunits = PAIR ? (int)(gridDim.x >> 1) : (int)gridDim.x;
+  const int unit0 = (int)blockIdx.x;  // first tile of this CTA
+  const int nunits = (int)gridDim.x;
   // tile -> (rectangle, first row, first column within the rectangle); false: the tile lies
-  // beyond its rectangle (the second of a pair)
+  // beyond its rectangle
   auto tile_at = [&](int tile, int& r, int& m0, int& n0) -> bool {
     if (Rg.lower) {
       r = 0;
-      if (PAIR) {  // row pairs 2g, 2g+1 with g + 1 tiles each: g (g + 1) before group g
-        int g = (int)((sqrtf(4.f * (float)tile + 1.f) - 1.f) * 0.5f);
-        while (g * (g + 1) > tile) --g;
-        while ((g + 1) * (g + 2) <= tile) ++g;
-        const int t = tile - g * (g + 1);
-        m0 = (2 * (2 * g + t / (g + 1)) + (int)rank) * TM;
-        n0 = (t % (g + 1)) * TN;
-      } else {
-        int g = (int)((sqrtf(2.f * (float)tile + 1.f) - 1.f) * 0.5f);
-        while (2 * g * (g + 1) > tile) --g;
-        while (2 * (g + 1) * (g + 2) <= tile) ++g;
-        const int t = tile - 2 * g * (g + 1);
-        m0 = (4 * g + t / (g + 1)) * TM;
-        n0 = (t % (g + 1)) * TN;
-      }
+      int g = (int)((sqrtf(2.f * (float)tile + 1.f) - 1.f) * 0.5f);
+      while (2 * g * (g + 1) > tile) --g;
+      while (2 * (g + 1) * (g + 2) <= tile) ++g;
+      const int t = tile - 2 * g * (g + 1);
+      m0 = (4 * g + t / (g + 1)) * TM;
+      n0 = (t % (g + 1)) * TN;
       return m0 < Rg.m_rows[0];
     }
     r = tile < Rg.ntiles0 ? 0 : 1;
     const int lt = r ? tile - Rg.ntiles0 : tile;
-    m0 = (PAIR ? 2 * (lt / Rg.ntn[r]) + (int)rank : lt / Rg.ntn[r]) * TM;
+    m0 = (lt / Rg.ntn[r]) * TM;
     n0 = (lt % Rg.ntn[r]) * TN;
     return m0 < Rg.m_rows[r];
   };
@@ -258,7 +219,7 @@ __global__ void __launch_bounds__(192, 1)
     *s_abort = 0;
     for (int s = 0; s < STAGES; ++s) {
       mbar_init(smem_u32(bars + B_FULL + s), 1);
-      mbar_init(smem_u32(bars + B_EMPTY + s), PAIR ? 2 : 1);
+      mbar_init(smem_u32(bars + B_EMPTY + s), 1);
     }
     for (int a = 0; a < 2; ++a) {
       mbar_init(smem_u32(bars + B_TFULL + a), 1);
@@ -275,7 +236,6 @@ __global__ void __launch_bounds__(192, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (PAIR) cluster_sync();  // both CTAs' barriers exist before the first multicast
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
@@ -291,13 +251,9 @@ __global__ void __launch_bounds__(192, 1)
         if (!mbar_wait(smem_u32(bars + B_EMPTY + s), ph ^ 1, status, s_abort)) break;
         const uint32_t sa = base + s * STAGE_BYTES, sb = sa + A_BYTES;
         const uint32_t full = smem_u32(bars + B_FULL + s);
-        mbar_expect_tx(full, STAGE_BYTES);  // PAIR: half of B' from the partner's multicast
+        mbar_expect_tx(full, STAGE_BYTES);
         tma_load_2d(sa, &tmA, kb * TK, m0, full);
-        if (PAIR)
-          tma_load_2d_mc(sb + rank * (B_BYTES / 2), &tmB, kb * TK, Rg.b_col[rr] + n0 + (int)rank * (TN / 2), full,
-                         (uint16_t)0x3);
-        else
-          tma_load_2d(sb, &tmB, kb * TK, Rg.b_col[rr] + n0, full);
+        tma_load_2d(sb, &tmB, kb * TK, Rg.b_col[rr] + n0, full);
       }
     }
     // no copy may still be landing in shared memory when the CTA exits: wait (bounded,
@@ -325,10 +281,7 @@ __global__ void __launch_bounds__(192, 1)
 #pragma unroll
         for (int kk = 0; kk < TK / 16; ++kk)
           mma_f16(acc, smem_desc(sa + kk * 32), smem_desc(sb + kk * 32), idesc, (kb | kk) ? 1u : 0u);
-        if (PAIR)
-          mma_commit_mc(smem_u32(bars + B_EMPTY + s), (uint16_t)0x3);
-        else
-          mma_commit(smem_u32(bars + B_EMPTY + s));
+        mma_commit(smem_u32(bars + B_EMPTY + s));
       }
       if (*s_abort) break;
       mma_commit(smem_u32(bars + B_TFULL + a));
@@ -399,7 +352,6 @@ __global__ void __launch_bounds__(192, 1)
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
-  if (PAIR) cluster_sync();  // the partner issues no more multicasts or commits into this CTA
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TN) : "memory");
@@ -573,17 +525,18 @@ typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t,
                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// looked up once per process; std::call_once makes concurrent first calls (several host
+// threads, one per serving slot) see the finished result
 EncodeTiledFn encode_fn() {
   static EncodeTiledFn fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  static std::once_flag once;
+  std::call_once(once, [] {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPoint("cuTensorMapEncodeTiled", &p, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
       fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
+  });
   return fn;
 }
 
@@ -658,35 +611,19 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
     return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: lower-triangle tiles need a diagonal square");
   if (u.a_skip < 0 || (u.a_skip > 0 && !u.prepped) || tc_gemm_work_bytes(M0 + u.a_skip, N, K) > work_bytes)
     return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: workspace too small");
-  static bool attr_done[64] = {false};
-  static int pair_clusters[64] = {0};  // co-resident CTA pairs (0: the pair kernel is not used)
-  int dev = ctx->device;
-  if (!attr_done[dev]) {
-    BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tc_gemm<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tc_gemm<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    const char* env = getenv("BEAST_TC_PAIR");
-    if (!(env && env[0] == '0')) {
-      cudaLaunchConfig_t cfg = {};
-      cudaLaunchAttribute at[1];
-      at[0].id = cudaLaunchAttributeClusterDimension;
-      at[0].val.clusterDim.x = 2;
-      at[0].val.clusterDim.y = 1;
-      at[0].val.clusterDim.z = 1;
-      cfg.gridDim = dim3(2 * std::max(1, ctx->num_sms / 2));
-      cfg.blockDim = dim3(192);
-      cfg.dynamicSmemBytes = SMEM_BYTES;
-      cfg.attrs = at;
-      cfg.numAttrs = 1;
-      int ncl = 0;
-      if (cudaOccupancyMaxActiveClusters(&ncl, (void*)k_tc_gemm<true>, &cfg) != cudaSuccess) {
-        cudaGetLastError();
-        ncl = 0;
-      }
-      pair_clusters[dev] = ncl;
+  {
+    // the kernel's shared-memory attribute, set once per device (serving slots may make their
+    // first factorisation concurrently from several host threads)
+    static std::mutex mtx;
+    static bool attr_done[64] = {false};
+    const int dev = ctx->device;
+    if (dev < 0 || dev >= 64) return beast_fail(ctx, BEAST_ERR_ARG, "tensor-core update: device index out of range");
+    std::lock_guard<std::mutex> lk(mtx);
+    if (!attr_done[dev]) {
+      BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_tc_gemm, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+      attr_done[dev] = true;
     }
-    attr_done[dev] = true;
   }
-  const bool pair = pair_clusters[dev] > 0;
   void *Apv, *Bpv;
   float *inv_sa, *inv_sb;
   tc_gemm_operands(work, M0 + u.a_skip, N, K, &Apv, &inv_sa, &Bpv, &inv_sb);
@@ -714,7 +651,7 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
   if (!make_map(&tmA, Ap, (uint64_t)2 * K, (uint64_t)2 * M0, (uint64_t)2 * K * 2, TK, TM, true,
                 CU_TENSOR_MAP_DATA_TYPE_FLOAT16))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (A') failed");
-  if (!make_map(&tmB, Bp, (uint64_t)2 * K, (uint64_t)N, (uint64_t)2 * K * 2, TK, pair ? TN / 2 : TN, true,
+  if (!make_map(&tmB, Bp, (uint64_t)2 * K, (uint64_t)N, (uint64_t)2 * K * 2, TK, TN, true,
                 CU_TENSOR_MAP_DATA_TYPE_FLOAT16))
     return beast_fail(ctx, BEAST_ERR_CUDA, "tensor map encode (B') failed");
   // C': real view clipped to each rectangle (rows up to 2(rowA + M_r), columns up to its last
@@ -743,17 +680,14 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
   for (int r = 0; r < 2; ++r) {
     Rg.ntn[r] = std::max(1, (Rg.n_cols[r] + TN - 1) / TN);
     const int ntm = (Rg.m_rows[r] + TM - 1) / TM;
-    ntl[r] = (Rg.m_rows[r] > 0 && Rg.n_cols[r] > 0) ? Rg.ntn[r] * (pair ? (ntm + 1) / 2 : ntm) : 0;
+    ntl[r] = (Rg.m_rows[r] > 0 && Rg.n_cols[r] > 0) ? Rg.ntn[r] * ntm : 0;
   }
   Rg.ntiles0 = ntl[0];
   Rg.ntiles = ntl[0] + ntl[1];
-  if (Rg.lower) {  // tiles n <= m / 4 of every row tile m (pairs: of every row pair p, n <= p / 2)
+  if (Rg.lower) {  // tiles n <= m / 4 of every row tile m
     const int ntm = (Rg.m_rows[0] + TM - 1) / TM;
     int64_t cnt = 0;
-    if (pair)
-      for (int p = 0; p < (ntm + 1) / 2; ++p) cnt += std::min(p / 2 + 1, Rg.ntn[0]);
-    else
-      for (int m = 0; m < ntm; ++m) cnt += std::min(m / 4 + 1, Rg.ntn[0]);
+    for (int m = 0; m < ntm; ++m) cnt += std::min(m / 4 + 1, Rg.ntn[0]);
     Rg.ntiles0 = Rg.ntiles = (int)cnt;
   }
   if (Rg.ntiles == 0) return BEAST_OK;
@@ -761,26 +695,8 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
   // algorithmic work: 8 K per complex element of the region (the lower triangle: half the square)
   ProfScope ps(ctx, PK_TCGEMM,
                8.0 * K * (u.lower ? 0.5 * (double)M0 * N0 : (double)M0 * N0 + (double)M1 * N1));
-  if (pair) {
-    const int ncl = std::min(Rg.ntiles, pair_clusters[dev]);
-    cudaLaunchConfig_t cfg = {};
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeClusterDimension;
-    at[0].val.clusterDim.x = 2;
-    at[0].val.clusterDim.y = 1;
-    at[0].val.clusterDim.z = 1;
-    cfg.gridDim = dim3(2 * ncl);
-    cfg.blockDim = dim3(192);
-    cfg.dynamicSmemBytes = SMEM_BYTES;
-    cfg.stream = st;
-    cfg.attrs = at;
-    cfg.numAttrs = 1;
-    BEAST_CUDA_TRY(ctx, cudaLaunchKernelEx(&cfg, k_tc_gemm<true>, tmA, tmB, tmC0, tmC1, Rg, (const float*)inv_sa,
-                                           (const float*)inv_sb, nk, ctx->d_flag));
-  } else {
-    const int grid = std::min(Rg.ntiles, std::max(1, ctx->num_sms));
-    k_tc_gemm<false><<<grid, 192, SMEM_BYTES, st>>>(tmA, tmB, tmC0, tmC1, Rg, inv_sa, inv_sb, nk, ctx->d_flag);
-  }
+  const int grid = std::min(Rg.ntiles, std::max(1, ctx->num_sms));
+  k_tc_gemm<<<grid, 192, SMEM_BYTES, st>>>(tmA, tmB, tmC0, tmC1, Rg, inv_sa, inv_sb, nk, ctx->d_flag);
   BEAST_CUDA_TRY(ctx, cudaGetLastError());
   return BEAST_OK;
 }

@@ -14,7 +14,8 @@ A step = one assemble + excitation + solve of that system.
 
 `--impl reference` times the reference's CPU algorithm (the oracle port; Julia is not
 available) on the host cores and prints the same line with "impl": "reference".
-Multi-GPU: replicas only (each rank solves its own copy; no collective on the data path).
+One GPU only: the path does not shard (a dense LU) and this library is built for a single
+GB300; --gpus other than 1, or a multi-rank launch, is refused.
 """
 import argparse
 import ctypes as C
@@ -382,7 +383,10 @@ def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.gpus != 1 or world != 1:
+        sys.stderr.write("bench.py runs on one GPU only (--gpus 1, no multi-rank launch): the dense "
+                         "solve does not shard and this library is single-GPU\n")
+        sys.exit(2)
     if args.impl == "reference":
         return run_reference(args, rank, world)
     if args.compare_fp64:
@@ -394,12 +398,7 @@ def main():
     import torch
     import beastgpu as bg
     from beastgpu import lib as L
-    dist = None
-    if world > 1:
-        import torch.distributed as dist
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
-    dev = local
+    dev = 0
     torch.cuda.set_device(dev)
     m, X, op, E = workload(args)
     n = X.numfunctions()
@@ -433,8 +432,6 @@ def main():
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
-    if dist:
-        dist.barrier()
     clk = Clocks(dev)
     # timed steps: CUDA events only around the dominant class (the roofline kernel)
     ctx.prof_enable(True, kinds=None if args.prof_all else ["lu_tc_gemm"])
@@ -457,13 +454,8 @@ def main():
     if "lu_tc_gemm" in prof_timed:
         prof["lu_tc_gemm"] = prof_timed["lu_tc_gemm"]
     ctx.prof_enable(False)
-    if dist:
-        t = torch.tensor([ms], device=f"cuda:{dev}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-        dist.barrier()
     ms_step = ms / args.steps
-    value = world * 1000.0 / ms_step
+    value = 1000.0 / ms_step
 
     # ---- end to end through the C ABI with host buffers
     e2e = None
@@ -498,15 +490,9 @@ def main():
             e2e_step()
         torch.cuda.synchronize()
         te = (time.perf_counter() - t0) / args.steps
-        if dist:
-            t = torch.tensor([te], device=f"cuda:{dev}")
-            dist.all_reduce(t, op=dist.ReduceOp.MAX)
-            te = float(t.item())
-        e2e = {"value": world / te, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+        e2e = {"value": 1.0 / te, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
                "d2h_bytes_per_step": int(d2h)}
         c2.close()
-    if rank != 0:
-        return
     # ---- roofline: the tensor-core trailing update of the LU (the dominant kernel class)
     pk, src = peaks()
     dominant = max(prof.items(), key=lambda kv: kv[1][0])[0]
@@ -532,7 +518,7 @@ def main():
             "dominant_by_time": dominant}
     breakdown = {k: {"ms": v[0], "launches": v[1], "share": v[0] / sum(w[0] for w in prof.values())}
                  for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
-    out = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": world,
+    out = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": 1,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
            "dtype": {L.MIXED: "c64+f64", L.MIXED_ACCURATE: "c128+c64"}.get(prec, "c128"),

@@ -119,6 +119,10 @@ int beast_ctx_set_stream(beast_ctx* ctx, void* stream);
 int beast_ctx_set_workspace_limit(beast_ctx* ctx, size_t bytes);
 /* wait for all work queued on the context stream */
 int beast_ctx_synchronize(beast_ctx* ctx);
+/* bound on the polls of one flag wait in the triangular solves (0 = the library default,
+ * about 4 million).  A wait that runs out makes the solve return BEAST_ERR_TIMEOUT; the
+ * context stays usable.  For tests of that error path; no reference counterpart. */
+int beast_ctx_set_wait_limit(beast_ctx* ctx, int64_t polls);
 
 /* ---- geometry and spaces ------------------------------------------------------------ */
 /* replaces the mesh arrays a CompScienceMeshes.Mesh carries into assemble (vertices,
@@ -185,7 +189,8 @@ int beast_rhs_planewave(beast_ctx* ctx, int kind, const beast_space* test, const
  * src/solvers/lusolver.jl:30).  A: n x n device matrix (dtype) factored IN PLACE with
  * partial pivoting; the handle keeps the pivots. */
 int beast_lu_factor(beast_ctx* ctx, int64_t n, void* A, int64_t lda, int dtype, beast_lu** out);
-/* solve with the factors: B (device, same dtype as the factors, n x nrhs) overwritten */
+/* solve with the factors: B (device, same dtype as the factors, n x nrhs) overwritten;
+ * blocks until done; BEAST_ERR_TIMEOUT if a bounded wait of the triangular solves ran out */
 int beast_lu_solve(beast_ctx* ctx, const beast_lu* lu, int64_t nrhs, void* B, int64_t ldb);
 int beast_lu_free(beast_lu* lu);
 
@@ -198,6 +203,8 @@ int beast_lu_free(beast_lu* lu);
  * looks up the array's device address; make that first call before any stream capture.
  * All calls share the one array and it keeps the previous call's contents: calls that
  * overlap on the GPU (other streams, other host threads) race -- serialise them.
+ * Like every call here it makes the context's device current on the calling thread, and it
+ * blocks that thread until the solve has finished (it reads the solve's status word).
  * No counterpart in the reference (it has no device memory). */
 int beast_lu_solve_noalloc(beast_ctx* ctx, const beast_lu* lu, int64_t nrhs, void* B, int64_t ldb);
 

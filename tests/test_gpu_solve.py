@@ -223,3 +223,47 @@ def test_mixed_symmetric_lookahead(n, monkeypatch):
         assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-12
         xs[la] = x
     assert np.linalg.norm(xs["1"] - xs["0"]) / np.linalg.norm(xs["0"]) < 1e-10
+
+
+@pytest.mark.parametrize("entry", ["lu_solve", "noalloc", "solve_dense"])
+def test_triangular_solve_wait_timeout_is_reported(entry):
+    """A flag wait of the wavefront triangular solve that runs out makes the call return
+    BEAST_ERR_TIMEOUT (not BEAST_OK with a wrong answer), and the next solve on the same
+    context, with the default wait budget, is clean.  The budget is cut to one poll: block
+    rows of a 4096-unknown solve wait on 63 predecessors, so some wait finds its value not
+    yet written.  Every wait is bounded; nothing faults or hangs."""
+    import ctypes as C
+    import torch
+    ctx = bg.get_context(0)
+    rng = np.random.default_rng(21)
+    n = 4096
+    A = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)) + 4 * n ** 0.5 * np.eye(n)
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+    h = C.c_void_p()
+    ctx.check(ctx.lib.beast_lu_factor(ctx.handle, n, At.data_ptr(), n, bg.C128, C.byref(h)))
+    try:
+        def run():
+            if entry == "solve_dense":
+                Ad = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()
+                bd = torch.from_numpy(b.copy()).cuda()
+                xd = torch.empty_like(bd)
+                it, res = C.c_int(0), C.c_double(0)
+                rc = ctx.lib.beast_solve_dense(ctx.handle, n, Ad.data_ptr(), n, bg.C128, bg.FP64, bd.data_ptr(),
+                                               xd.data_ptr(), 1, bg.lib.DEVICE, 1e-12, 30, C.byref(it), C.byref(res))
+                return rc, xd.cpu().numpy()
+            B = torch.from_numpy(b.copy()).cuda()
+            fn = ctx.lib.beast_lu_solve if entry == "lu_solve" else ctx.lib.beast_lu_solve_noalloc
+            rc = fn(ctx.handle, h, 1, B.data_ptr(), n)
+            return rc, B.cpu().numpy()
+
+        ctx.check(ctx.lib.beast_ctx_set_wait_limit(ctx.handle, 1))
+        rc, _ = run()
+        assert rc == bg.lib.ERR_TIMEOUT
+        ctx.check(ctx.lib.beast_ctx_set_wait_limit(ctx.handle, 0))
+        rc, x = run()
+        assert rc == bg.lib.OK
+        assert np.linalg.norm(A @ x - b) / np.linalg.norm(b) < 1e-12
+    finally:
+        ctx.lib.beast_ctx_set_wait_limit(ctx.handle, 0)
+        ctx.lib.beast_lu_free(h)
