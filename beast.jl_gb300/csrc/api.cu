@@ -593,7 +593,6 @@ int beast_assemble(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc*
   ARG_CHECK(ctx, ts->mesh == bs->mesh, "test and trial spaces must share the mesh");
   ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
             "unknown precision");
-  if (precision == BEAST_MIXED_ACCURATE) precision = BEAST_FP64;  // assembly in FP64
   ARG_CHECK(ctx, z_dtype == BEAST_C128 || z_dtype == BEAST_C64, "unknown matrix dtype");
   ARG_CHECK(ctx, row_off >= 0 && col_off >= 0 && ldz >= row_off + ts->nfuncs, "bad Z addressing");
   ARG_CHECK(ctx, op->kind >= BEAST_MW_SL && op->kind <= BEAST_HH_DLT, "unknown operator kind");
@@ -703,11 +702,19 @@ int beast_assemble_local(beast_ctx* ctx, int which, const beast_space* ts, const
   if (set_device(ctx)) return BEAST_ERR_CUDA;
   const int zc = z_dtype == BEAST_C64;
   const size_t elem = zc ? 8 : 16;
+  BEAST_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), ctx->stream));
+  auto flag_check = [&]() -> int {
+    int flag = 0;
+    BEAST_CUDA_TRY(ctx, cudaMemcpy(&flag, ctx->d_flag, sizeof(int), cudaMemcpyDeviceToHost));
+    if (flag & 16)
+      return beast_fail(ctx, BEAST_ERR_UNSUPPORTED, "local operator: a test function meets more than 64 trial functions");
+    return BEAST_OK;
+  };
   if (z_loc == BEAST_DEVICE) {
     BEAST_CUDA_TRY(ctx, launch_local_impl(which, ts, bs, bs->cell2act, r, Z, ldz, zc, row_off, col_off,
-                                          cr, ci, ctx->stream));
+                                          cr, ci, ctx->d_flag, ctx->stream));
     BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-    return BEAST_OK;
+    return flag_check();
   }
   void* dz = nullptr;
   BEAST_CUDA_TRY(ctx, cudaMallocAsync(&dz, (size_t)ts->nfuncs * bs->nfuncs * elem, ctx->stream));
@@ -715,12 +722,12 @@ int beast_assemble_local(beast_ctx* ctx, int which, const beast_space* ts, const
   BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(dz, ts->nfuncs * elem, hz, ldz * elem, ts->nfuncs * elem,
                                         bs->nfuncs, cudaMemcpyHostToDevice, ctx->stream));
   BEAST_CUDA_TRY(ctx, launch_local_impl(which, ts, bs, bs->cell2act, r, dz, ts->nfuncs, zc, 0, 0, cr,
-                                        ci, ctx->stream));
+                                        ci, ctx->d_flag, ctx->stream));
   BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(hz, ldz * elem, dz, ts->nfuncs * elem, ts->nfuncs * elem,
                                         bs->nfuncs, cudaMemcpyDeviceToHost, ctx->stream));
   BEAST_CUDA_TRY(ctx, cudaFreeAsync(dz, ctx->stream));
   BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(ctx->stream));
-  return BEAST_OK;
+  return flag_check();
 }
 
 int beast_rhs_planewave(beast_ctx* ctx, int kind, const beast_space* ts, const double* dir,

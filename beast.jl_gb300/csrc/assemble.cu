@@ -1138,10 +1138,14 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs G, const int64_t* tpt
   const int64_t nb1 = nb0 + GATHER_NCOL < G.n1 ? nb0 + GATHER_NCOL : G.n1;
   // the CTA's trial functions with at most two entries: Zcell column offsets and coefficients
   // staged once in shared memory (s_cnt = -1: more entries, taken by the general loop)
+  // (both for c64 -> c64, with FP32 sums, and c128 -> c128, with FP64 sums)
+  constexpr bool FAST = ZC64 == OC64;
+  typedef typename std::conditional<ZC64, float2, double2>::type Z2;
+  constexpr int GRP = ZC64 ? 8 : 4;  // trial functions whose Zcell values are requested together
   __shared__ int64_t s_col[GATHER_NCOL][2];
-  __shared__ float s_b[GATHER_NCOL][2];
+  __shared__ A s_b[GATHER_NCOL][2];
   __shared__ int s_cnt[GATHER_NCOL];
-  if (ZC64 && OC64 && threadIdx.x < GATHER_NCOL) {
+  if (FAST && threadIdx.x < GATHER_NCOL) {
     const int64_t n = nb0 + threadIdx.x;
     int cnt = 0;
     if (n < nb1) {
@@ -1150,12 +1154,12 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs G, const int64_t* tpt
       cnt = c <= 2 ? c : -1;
       for (int k = 0; k < 2 && k < c; ++k) {
         s_col[threadIdx.x][k] = ((int64_t)nsb * G.qlocal[bcell[f0 + k]] + bshape[f0 + k]) * G.ldc;
-        s_b[threadIdx.x][k] = (float)bcoef[f0 + k];
+        s_b[threadIdx.x][k] = (A)bcoef[f0 + k];
       }
     }
     s_cnt[threadIdx.x] = cnt;
   }
-  if (ZC64 && OC64) __syncthreads();
+  if (FAST) __syncthreads();
   if (m >= nrows) return;
   const int64_t e0 = tptr[m], ne = tptr[m + 1] - e0;
   int64_t trow[GATHER_MAXE];
@@ -1170,49 +1174,55 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs G, const int64_t* tpt
     }
   }
   int64_t nstart = nb0;
-  if (ZC64 && OC64 && ne <= 2) {
-    // fast path: the Zcell values of 8 trial functions (<= 2 x 2 each) are requested before
+  if (FAST && ne <= 2) {
+    // fast path: the Zcell values of GRP trial functions (<= 2 x 2 each) are requested before
     // any is used
     bool all2 = true;
     for (int nn = 0; nn < nb1 - nb0; ++nn) all2 &= s_cnt[nn] >= 0;
     if (all2) {
-      const float2* zc = reinterpret_cast<const float2*>(G.zcell);
-      for (int g0 = 0; g0 < (int)(nb1 - nb0); g0 += 8) {
-        float2 z[8][2][2];
+      const Z2* zc = reinterpret_cast<const Z2*>(G.zcell);
+      for (int g0 = 0; g0 < (int)(nb1 - nb0); g0 += GRP) {
+        Z2 z[GRP][2][2];
 #pragma unroll
-        for (int u = 0; u < 8; ++u)
+        for (int u = 0; u < GRP; ++u)
 #pragma unroll
           for (int k = 0; k < 2; ++k)
 #pragma unroll
             for (int j = 0; j < 2; ++j) {
               const int nn = g0 + u;
               const bool ok = nn < nb1 - nb0 && k < s_cnt[nn] && j < ne;
-              z[u][k][j] = ok ? zc[s_col[nn][k] + trow[j]] : make_float2(0.f, 0.f);
+              Z2 v;
+              v.x = 0;
+              v.y = 0;
+              z[u][k][j] = ok ? zc[s_col[nn][k] + trow[j]] : v;
             }
 #pragma unroll
-        for (int u = 0; u < 8; ++u) {
+        for (int u = 0; u < GRP; ++u) {
           const int nn = g0 + u;
           if (nn >= nb1 - nb0) break;
-          float re = 0.f, im = 0.f;
+          A re = 0, im = 0;
 #pragma unroll
           for (int k = 0; k < 2; ++k)
 #pragma unroll
             for (int j = 0; j < 2; ++j)
               if (k < s_cnt[nn] && j < ne) {
-                const float ab = (float)tc[j] * s_b[nn][k];
+                const A ab = tc[j] * s_b[nn][k];
                 re += ab * z[u][k][j].x;
                 im += ab * z[u][k][j].y;
               }
-          const float cr = (float)G.cr, ci = (float)G.ci;
-          float vr = cr * re - ci * im, vi = cr * im + ci * re;
-          float2* Z = reinterpret_cast<float2*>(G.Z);
+          const A cr = (A)G.cr, ci = (A)G.ci;
+          A vr = cr * re - ci * im, vi = cr * im + ci * re;
+          Z2* Z = reinterpret_cast<Z2*>(G.Z);
           const int64_t o = (G.row_off + m) + (G.col_off + nb0 + nn) * G.ldz;
           if (G.accumulate) {
-            const float2 old = Z[o];
+            const Z2 old = Z[o];
             vr += old.x;
             vi += old.y;
           }
-          Z[o] = make_float2(vr, vi);
+          Z2 out;
+          out.x = vr;
+          out.y = vi;
+          Z[o] = out;
         }
       }
       nstart = nb1;
@@ -1282,15 +1292,19 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs G, const int64_t* tpt
 // ------------------------------------------------------------------------------------
 // local operators (Identity / NCross on RT x RT), deterministic per test dof
 // ------------------------------------------------------------------------------------
+constexpr int LOCAL_MAXCOLS = 64;
+
 __global__ void k_local(int which, const int64_t* tptr, const int* tcell, const int* tshape,
                         const double* tcoef, const int* tcells_mesh, const double* tgeo,
                         const int* b_cell2act, const int* bad_dof, const double* bad_coef,
                         int bmaxfn, TriRuleDev r, int64_t nrows, void* Z, int64_t ldz, int zc64,
-                        int64_t row_off, int64_t col_off, double cr, double ci) {
+                        int64_t row_off, int64_t col_off, double cr, double ci, int* flag) {
   const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
   if (m >= nrows) return;
-  int64_t cols[16];
-  double vals[16];
+  // the distinct trial functions of this row (a Buffa-Christiansen row meets about 25 coarse
+  // RT functions written on the refinement; an RT row at most 5)
+  int cols[LOCAL_MAXCOLS];
+  double vals[LOCAL_MAXCOLS];
   int nc = 0;
   for (int64_t e = tptr[m]; e < tptr[m + 1]; ++e) {
     int pa = tcell[e], ra = tshape[e];
@@ -1316,12 +1330,16 @@ __global__ void k_local(int which, const int64_t* tptr, const int* tcell, const 
         int slot = -1;
         for (int s = 0; s < nc; ++s)
           if (cols[s] == n) slot = s;
-        if (slot < 0 && nc < 16) {
+        if (slot < 0) {
+          if (nc == LOCAL_MAXCOLS) {  // more distinct columns than the buffer holds: reported
+            atomicOr(flag, 16);
+            continue;
+          }
           slot = nc++;
           cols[slot] = n;
           vals[slot] = 0;
         }
-        if (slot >= 0) vals[slot] += v;
+        vals[slot] += v;
       }
   }
   for (int s = 0; s < nc; ++s) {
@@ -1623,11 +1641,12 @@ cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev&
   const int kind = a.op.kind;
   if (kind == BEAST_MW_SL || kind == BEAST_MW_DL || kind == BEAST_MW_NXDL) {
     if (tk != BEAST_RT || bk != BEAST_RT) return cudaErrorInvalidValue;
-    if (kind == BEAST_MW_SL && a.precision == BEAST_FP64 && !a.zcell_c64 && P.op.gr == 0.0) {
-      // opt-in (BEAST_FAR_DF=1): the double-float kernel for FP64 EFIE assemblies (real
-      // wavenumber), at a fraction of the FP64 kernel's time on GB300
+    if (kind == BEAST_MW_SL && a.precision == BEAST_MIXED_ACCURATE && !a.zcell_c64 && P.op.gr == 0.0) {
+      // mixed-accurate EFIE assemblies (real wavenumber): far pairs in double-float arithmetic
+      // on the FP32 pipes (about 1e-12 relative to the FP64 values, at a fraction of the FP64
+      // kernel's time on GB300); BEAST_FAR_DF=0 selects the FP64 kernel instead
       const char* e = getenv("BEAST_FAR_DF");
-      if (e && e[0] == '1') return far_efie_df(P, st);
+      if (!(e && e[0] == '0')) return far_efie_df(P, st);
     }
     if (kind == BEAST_MW_SL) return far_prec<BEAST_MW_SL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_c64, st);
     if (kind == BEAST_MW_DL) return far_prec<BEAST_MW_DL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_c64, st);
@@ -1736,13 +1755,13 @@ cudaError_t launch_farfield(const beast_space* s, const double* u, const double*
 cudaError_t launch_local_impl(int which, const beast_space* ts, const beast_space* bs,
                               const int* b_cell2act, const TriRuleDev& r, void* Z, int64_t ldz,
                               int z_c64, int64_t row_off, int64_t col_off, double cr, double ci,
-                              cudaStream_t st) {
+                              int* flag, cudaStream_t st) {
   int64_t n = ts->nfuncs;
   if (n == 0) return cudaSuccess;
   int th = 128;
   k_local<<<(unsigned)((n + th - 1) / th), th, 0, st>>>(which, ts->fn_ptr, ts->fn_cell, ts->fn_shape,
                                                       ts->fn_coeff, ts->cells, ts->geo, b_cell2act,
                                                       bs->ad_dof, bs->ad_coeff, bs->maxfn, r, n, Z,
-                                                      ldz, z_c64, row_off, col_off, cr, ci);
+                                                      ldz, z_c64, row_off, col_off, cr, ci, flag);
   return cudaGetLastError();
 }

@@ -177,7 +177,7 @@ cudaError_t launch_gather(const GatherArgs& g, cudaStream_t st);
 cudaError_t launch_local_impl(int which, const beast_space* ts, const beast_space* bs,
                               const int* b_cell2act, const TriRuleDev& r, void* Z, int64_t ldz,
                               int z_c64, int64_t row_off, int64_t col_off, double cr, double ci,
-                              cudaStream_t st);
+                              int* flag, cudaStream_t st);
 cudaError_t launch_rhs(int kind, const beast_space* ts, const double* dir, const double* pol,
                        double gr, double gi, double ar, double ai, const TriRuleDev& r,
                        double* b, cudaStream_t st);

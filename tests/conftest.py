@@ -13,8 +13,6 @@ GOLDEN = os.path.join(ROOT, "tests", "golden")
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
-    config.addinivalue_line("markers", "gpu_pending: GPU parity test of a part that has not run on a GPU "
-                                       "yet (run with -m gpu_pending; marked gpu once it has passed)")
 
 
 @pytest.fixture(scope="session")

@@ -192,3 +192,32 @@ def test_threading_and_row_invariance():
     n = X.numfunctions()
     R = O.assemble(op, qs, X, X, row_lo=n // 3, row_hi=n // 3 + 17)
     assert np.abs(R - A1[n // 3:n // 3 + 17]).max() <= 1e-12 * np.abs(A1).max()
+
+
+def _farfield_golden(golden):
+    """the reference's golden current on sphere824 in this package's dof order, with the
+    7 directions and magnitudes of test/test_farfield.jl:17-40"""
+    from beastgpu import mesh as M, spaces as S
+    ffg = golden["farfield_sphere824"]
+    m = M.readmesh(mesh_path("sphere824.in"))
+    X = S.raviartthomas(m)
+    u_ref = np.array(ffg["u_re"]) + 1j * np.array(ffg["u_im"])
+    u = np.zeros_like(u_ref)
+    u[np.array(ffg["dof_map"])] = np.array(ffg["sign"]) * u_ref
+    th = np.linspace(0.0, np.pi, 7)
+    dirs = np.stack([np.sin(th), np.zeros_like(th), np.cos(th)], axis=1)
+    return X, u, dirs, np.array(ffg["a"])
+
+
+def test_farfield_golden_vector(golden):
+    """test/test_farfield.jl: |potential(MWFarField3D(1im), points, u, X)| * omega / (4 pi c)
+    at 7 angles within 1e4 eps.  The golden magnitudes are those of the 4-point degree-3
+    triangle rule: with it they are reproduced to about 1e-15, while rules of degree 4 and
+    above converge to values 1.5e-7 away -- so this pins the dof map, the far-field kernel and
+    that rule's points and weights against the reference."""
+    X, u, dirs, a = _farfield_golden(golden)
+    tol = 1e4 * np.finfo(float).eps
+    ff = O.farfield(X, u, dirs, 1j, degree=3) / (4 * np.pi)
+    assert np.abs(np.linalg.norm(ff, axis=1) - a).max() < tol
+    ff10 = O.farfield(X, u, dirs, 1j, degree=10) / (4 * np.pi)
+    assert 1e-8 < np.abs(np.linalg.norm(ff10, axis=1) - a).max() < 1e-6
