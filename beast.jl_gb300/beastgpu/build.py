@@ -8,7 +8,7 @@ PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(os.path.dirname(PKG), "csrc")
 LIB = os.path.join(PKG, "libbeastgpu.so")
 SOURCES = ["api.cu", "assemble.cu", "linalg.cu", "tc_gemm.cu"]
-HEADERS = ["internal.h", "rules_gen.h", "se_core.h", "se_p1.h", "dfloat.h", "dftables.h", "far_df.h",
+HEADERS = ["internal.h", "rules_gen.h", "se_core.h", "se_p1.h", "dfloat.h", "dftables.h", "far_df.h", "fsplit.h",
            os.path.join("..", "..", "include", "beastgpu.h")]
 NVCC = os.environ.get("NVCC", "nvcc")
 FLAGS = ["-gencode", "arch=compute_103a,code=sm_103a", "-lineinfo", "-O3", "-std=c++17",

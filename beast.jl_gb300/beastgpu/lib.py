@@ -15,6 +15,7 @@ OK, ERR_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_NOCONV, ERR_SINGULAR, ERR_UNSUP
 FP64, MIXED, MIXED_ACCURATE = 0, 1, 2
 C128, C64 = 0, 1
 HOST, DEVICE = 0, 1
+EXC_TANGTRACE_E, EXC_CROSSTRACE_H, EXC_HH_DIRICHLET = 0, 1, 2
 PROF_KINDS = ["geometry", "far", "near", "gather", "local", "rhs", "farfield", "lu_panel",
               "lu_laswp", "lu_trsm", "lu_gemm", "trsv", "gemv", "vec", "convert", "lu_tc_gemm"]
 

@@ -438,13 +438,14 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
   cudaStream_t st = ctx->stream;
   const int nst = ts->kind == BEAST_P0 ? 1 : 3, nsb = bs->kind == BEAST_P0 ? 1 : 3;
   const int64_t ldc = (int64_t)nst * ts->ncells;
-  const int zc64 = precision == BEAST_MIXED ? 1 : 0;
-  const size_t elem = zc64 ? 8 : 16;
+  const int zfmt = precision == BEAST_MIXED ? ZCELL_C64 : precision == BEAST_MIXED_ACCURATE ? ZCELL_DF : ZCELL_C128;
+  const size_t elem = zfmt == ZCELL_C64 ? 8 : 16;
   // rules
   TriRuleDev ro, ri, ron, rin;
   ARG_CHECK(ctx, make_trirule(qs->outer_far, &ro) && make_trirule(qs->inner_far, &ri),
             "far rule degree not available (1..10)");
-  bool has_near = qs->kind == BEAST_QS_WILTON_SAUTER || qs->kind == BEAST_QS_SAUTER;
+  // DoubleNumQStrat pairs that come close are evaluated by the near kernel too (class 4)
+  const bool has_near = true;
   if (qs->kind == BEAST_QS_WILTON_SAUTER) {
     ARG_CHECK(ctx, make_trirule(qs->outer_near, &ron) && make_trirule(qs->inner_near, &rin),
               "near rule degree not available (1..10)");
@@ -452,7 +453,7 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
     ron = ro;
     rin = ri;
   }
-  if (has_near)
+  if (qs->kind != BEAST_QS_DOUBLENUM)
     ARG_CHECK(ctx, qs->ss_face >= 1 && qs->ss_face <= 20 && qs->ss_edge >= 1 && qs->ss_edge <= 20 &&
                        qs->ss_vert >= 1 && qs->ss_vert <= 20,
               "Sauter-Schwab orders must be in 1..20");
@@ -522,7 +523,7 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
     a.qcells = qcells_d;
     a.nq = (int)ch.cells.size();
     a.zcell = zcell;
-    a.zcell_c64 = zc64;
+    a.zcell_fmt = zfmt;
     a.ldc = ldc;
     a.near = nearl;
     a.near_cap = (int)near_cap;
@@ -552,7 +553,7 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
     g.ts = ts;
     g.bs = bs;
     g.zcell = zcell;
-    g.zcell_c64 = zc64;
+    g.zcell_fmt = zfmt;
     g.ldc = ldc;
     g.qlocal = qlocal_d;
     g.tpos = ts->tpos;

@@ -21,6 +21,7 @@
 
 #include <cmath>
 
+#include "fsplit.h"
 #include "internal.h"
 #include "se_p1.h"
 #include "far_df.h"
@@ -177,15 +178,24 @@ struct FarParams {
 constexpr int FAR_THREADS = 128;
 constexpr int FAR_QT = 16;  // trial cells staged per CTA
 
+// one cell-pair value into Zcell in its format (ZCELL_*); an FP64 value enters the
+// double-float format through the integer split of fsplit.h (no FP64 instruction)
 template <typename R>
-DEV void store_c(void* z, int64_t idx, C2<R> v, int c64);
-
-template <typename R>
-DEV void store_c(void* z, int64_t idx, C2<R> v, int c64) {
-  if (c64)
+DEV void store_c(void* z, int64_t idx, C2<R> v, int fmt) {
+  if (fmt == ZCELL_C64) {
     reinterpret_cast<float2*>(z)[idx] = make_float2((float)v.re, (float)v.im);
-  else
+  } else if (fmt == ZCELL_DF) {
+    float4 o;
+    if (sizeof(R) == 8) {
+      fsplit::split_f64((double)v.re, &o.x, &o.y);
+      fsplit::split_f64((double)v.im, &o.z, &o.w);
+    } else {
+      o = make_float4((float)v.re, 0.f, (float)v.im, 0.f);
+    }
+    reinterpret_cast<float4*>(z)[idx] = o;
+  } else {
     reinterpret_cast<double2*>(z)[idx] = make_double2((double)v.re, (double)v.im);
+  }
 }
 
 // shared trial-cell record (in the arithmetic type R): sigma_j = s_j - c (9), centroid hi
@@ -193,7 +203,7 @@ DEV void store_c(void* z, int64_t idx, C2<R> v, int c64) {
 // distance); then per inner rule point eta_b = y_b - c (3) and weight
 constexpr int QREC_HDR = 20;
 
-template <int OPK, int TK, int BK, typename R, int C64>
+template <int OPK, int TK, int BK, typename R, int FMT>
 __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
   extern __shared__ unsigned char smraw[];
   R* sm = reinterpret_cast<R*>(smraw);
@@ -270,13 +280,20 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
     // d = c_p - c_q from hi/lo parts
     const V3<R> d = mk((chp.x - rq[9]) + (clp.x - rq[12]), (chp.y - rq[10]) + (clp.y - rq[13]),
                        (chp.z - rq[11]) + (clp.z - rq[14]));
-    // ---- near test (candidate filter on centroid distance, exact FP64 classification)
-    if (P.qs_kind != BEAST_QS_DOUBLENUM) {
+    // ---- near test (candidate filter on centroid distance, exact FP64 classification).
+    // DoubleNumQStrat applies one rule to every pair; the pairs whose circumspheres about the
+    // centroids meet (every touching pair among them) go to k_near as class 4, the same rule
+    // evaluated point by point in FP64: the moment form loses digits when rule points of the
+    // two cells come close.
+    {
       const R lim = radp + rq[19];
       if (dot(d, d) <= lim * lim * (R)1.0001 + (R)1e-30) {
-        Geo t = load_geo(tg);
-        Geo s = load_geo(P.bgeo + (int64_t)P.qcells[ql] * GEO_STRIDE);
-        int cls = classify_exact(t, s, P.qs_kind, P.k2);
+        int cls = 4;
+        if (P.qs_kind != BEAST_QS_DOUBLENUM) {
+          Geo t = load_geo(tg);
+          Geo s = load_geo(P.bgeo + (int64_t)P.qcells[ql] * GEO_STRIDE);
+          cls = classify_exact(t, s, P.qs_kind, P.k2);
+        }
         if (cls != 0) {
           int idx = atomicAdd(P.near_count, 1);
           if (idx < P.near_cap)
@@ -285,7 +302,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
             atomicOr(P.flag, 1);
           for (int i = 0; i < nst; ++i)
             for (int j = 0; j < nsb; ++j)
-              store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * pp + i, C2<R>{0, 0}, C64);
+              store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * pp + i, C2<R>{0, 0}, FMT);
           continue;
         }
       }
@@ -418,7 +435,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
             f = csub(f, cscale(dot(ti, sj), M3));
             z = cscale((R)0.25, f);
           }
-          store_c<R>(P.zcell, (int64_t)(3 * ql + j) * P.ldc + 3 * pp + i, z, C64);
+          store_c<R>(P.zcell, (int64_t)(3 * ql + j) * P.ldc + 3 * pp + i, z, FMT);
         }
       }
     } else {
@@ -469,7 +486,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
       for (int i = 0; i < nst; ++i)
         for (int j = 0; j < nsb; ++j)
           store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * pp + i,
-                     cscale(ApAq, acc[i * nsb + j]), C64);
+                     cscale(ApAq, acc[i * nsb + j]), FMT);
     }
   }
 }
@@ -721,7 +738,7 @@ struct NearParams {
   const NearPair* near;
   int nnear;
   void* zcell;
-  int c64;
+  int zfmt;  // Zcell format (ZCELL_*)
   int ss32;  // Sauter-Schwab moments of RT Maxwell pairs in FP32 (mixed precision)
   int64_t ldc;
   int* flag;
@@ -735,7 +752,7 @@ constexpr int NEAR_WARPS = 4;
 // A kernel of its own so that its register budget (and occupancy) is not set by the FP64
 // paths of k_near; k_near skips these pairs.
 DEV bool near_is_ss32(const NearParams& P, int cls) {
-  return P.ss32 && cls >= 1 && P.tk == BEAST_RT && P.bk == BEAST_RT &&
+  return P.ss32 && cls >= 1 && cls <= 3 && P.tk == BEAST_RT && P.bk == BEAST_RT &&
          (P.op.kind == BEAST_MW_SL || (P.op.kind == BEAST_MW_DL && cls != 3));
 }
 
@@ -922,7 +939,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss32(NearParams P) {
           C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
           z = cadd(fm, rdot(cross(sj, ti), V3_));
         }
-        store_c<double>(P.zcell, (int64_t)(3 * np_.q + j) * P.ldc + 3 * (int64_t)np_.p + i, z, P.c64);
+        store_c<double>(P.zcell, (int64_t)(3 * np_.q + j) * P.ldc + 3 * (int64_t)np_.p + i, z, P.zfmt);
       }
   }
 }
@@ -949,7 +966,22 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
   Shp f, g;
   bool dl_face = np_.cls == 3 && (P.op.kind == BEAST_MW_DL || P.op.kind == BEAST_HH_DL ||
                                   P.op.kind == BEAST_HH_DLT);
-  if (np_.cls >= 1 && !dl_face) {
+  if (np_.cls == 4) {
+    // ---- DoubleNumQStrat pair close to its partner: the pair's own DoubleQuadRule
+    // (src/quadrature/doublenumints.jl:12-43) point by point in FP64, lanes over point pairs
+    const int no = P.ro.n, ni = P.ri.n;
+    for (int it = lane; it < no * ni; it += 32) {
+      const int a = it / ni, b = it % ni;
+      double bx[3] = {P.ro.u[a], P.ro.v[a], 1.0 - P.ro.u[a] - P.ro.v[a]};
+      double by[3] = {P.ri.u[b], P.ri.v[b], 1.0 - P.ri.u[b] - P.ri.v[b]};
+      V3<double> x = bx[0] * t.v[0] + bx[1] * t.v[1] + bx[2] * t.v[2];
+      V3<double> y = by[0] * s.v[0] + by[1] * s.v[1] + by[2] * s.v[2];
+      shapes(P.tk, t, x, bx, f);
+      shapes(P.bk, s, y, by, g);
+      integrand(P.op.kind, P.op, x, y, t.n, s.n, P.tk, f, P.bk, g, P.ro.w[a] * t.area * P.ri.w[b] * s.area,
+                acc);
+    }
+  } else if (np_.cls >= 1 && !dl_face) {
     // ---- Sauter-Schwab: shared vertices first, same order (SauterSchwabQuadrature.reorder)
     const double dtol = 1.0e3 * 2.220446049250313e-16;
     int pt[3], ps[3], hits = 0, ti[3], si[3];
@@ -1061,7 +1093,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
               C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
               z = cadd(fm, rdot(cross(sj, ti), V3_));
             }
-            store_c<double>(P.zcell, (int64_t)(3 * np_.q + j) * P.ldc + 3 * (int64_t)np_.p + i, z, P.c64);
+            store_c<double>(P.zcell, (int64_t)(3 * np_.q + j) * P.ldc + 3 * (int64_t)np_.p + i, z, P.zfmt);
           }
         }
       }
@@ -1115,7 +1147,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
     for (int i = 0; i < nt; ++i)
       for (int j = 0; j < nb; ++j)
         store_c<double>(P.zcell, (int64_t)(nb * np_.q + j) * P.ldc + nt * (int64_t)np_.p + i,
-                        acc[i * nb + j], P.c64);
+                        acc[i * nb + j], P.zfmt);
   }
 }
 
@@ -1286,6 +1318,137 @@ __global__ void __launch_bounds__(256) k_gather(GatherArgs G, const int64_t* tpt
       }
       Z[o] = make_double2((double)vr, (double)vi);
     }
+  }
+}
+
+// The same gather from double-float cell-pair blocks (ZCELL_DF, the mixed-accurate path): the
+// sums run on the FP32 pipes as sloppy pair sums, coefficients enter as pairs from the
+// integer split, and the result reaches the c128 output through exact integer float-to-double
+// conversions and one FP64 addition per real part (or rounds to c64).  The far entries of RT
+// functions cancel by about (h/R)^2 in these sums; the pair sums keep about 2^-44 of the
+// largest term, below the cell-pair values' own error.
+__device__ __forceinline__ dfl::df df_coef(double c) {
+  float h, l;
+  fsplit::split_f64(c, &h, &l);
+  return dfl::fast_two_sum(h, l);
+}
+__device__ __forceinline__ void df_acc(dfl::df& re, dfl::df& im, float4 z, dfl::df c) {
+  re = dfl::adds(re, dfl::mul(dfl::df{z.x, z.y}, c));
+  im = dfl::adds(im, dfl::mul(dfl::df{z.z, z.w}, c));
+}
+template <int OC64>
+__global__ void __launch_bounds__(256) k_gather_df(GatherArgs G, const int64_t* tptr, const int* tcell,
+                                                   const int* tshape, const double* tcoef, const int64_t* bptr,
+                                                   const int* bcell, const int* bshape, const double* bcoef, int nst,
+                                                   int nsb, int64_t nrows) {
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nb0 = G.n0 + (int64_t)blockIdx.y * GATHER_NCOL;
+  const int64_t nb1 = nb0 + GATHER_NCOL < G.n1 ? nb0 + GATHER_NCOL : G.n1;
+  __shared__ int64_t s_col[GATHER_NCOL][2];
+  __shared__ dfl::df s_b[GATHER_NCOL][2];
+  __shared__ int s_cnt[GATHER_NCOL];
+  if (threadIdx.x < GATHER_NCOL) {
+    const int64_t n = nb0 + threadIdx.x;
+    int cnt = 0;
+    if (n < nb1) {
+      const int64_t f0 = bptr[n];
+      const int c = (int)(bptr[n + 1] - f0);
+      cnt = c <= 2 ? c : -1;
+      for (int k = 0; k < 2 && k < c; ++k) {
+        s_col[threadIdx.x][k] = ((int64_t)nsb * G.qlocal[bcell[f0 + k]] + bshape[f0 + k]) * G.ldc;
+        s_b[threadIdx.x][k] = df_coef(bcoef[f0 + k]);
+      }
+    }
+    s_cnt[threadIdx.x] = cnt;
+  }
+  __syncthreads();
+  if (m >= nrows) return;
+  const int64_t e0 = tptr[m], ne = tptr[m + 1] - e0;
+  const float4* zc = reinterpret_cast<const float4*>(G.zcell);
+  const bool unit = G.cr == 1.0 && G.ci == 0.0;
+  auto finish = [&](int64_t n, dfl::df re, dfl::df im) {
+    const int64_t o = (G.row_off + m) + (G.col_off + n) * G.ldz;
+    if (OC64) {
+      float vr = dfl::add_rn(re.hi, re.lo), vi = dfl::add_rn(im.hi, im.lo);
+      if (!unit) {
+        const float cr = (float)G.cr, ci = (float)G.ci;
+        const float tr = cr * vr - ci * vi;
+        vi = cr * vi + ci * vr;
+        vr = tr;
+      }
+      float2* Z = reinterpret_cast<float2*>(G.Z);
+      if (G.accumulate) {
+        const float2 old = Z[o];
+        vr += old.x;
+        vi += old.y;
+      }
+      Z[o] = make_float2(vr, vi);
+    } else {
+      double vr = fsplit::f2d(re.hi) + fsplit::f2d(re.lo), vi = fsplit::f2d(im.hi) + fsplit::f2d(im.lo);
+      if (!unit) {
+        const double tr = G.cr * vr - G.ci * vi;
+        vi = G.cr * vi + G.ci * vr;
+        vr = tr;
+      }
+      double2* Z = reinterpret_cast<double2*>(G.Z);
+      if (G.accumulate) {
+        const double2 old = Z[o];
+        vr += old.x;
+        vi += old.y;
+      }
+      Z[o] = make_double2(vr, vi);
+    }
+  };
+  const dfl::df z0 = dfl::make(0.f);
+  int64_t nstart = nb0;
+  if (ne <= 2) {
+    bool all2 = true;
+    for (int nn = 0; nn < nb1 - nb0; ++nn) all2 &= s_cnt[nn] >= 0;
+    if (all2) {
+      int64_t trow[2] = {0, 0};
+      dfl::df tc[2] = {z0, z0};
+      for (int j = 0; j < ne; ++j) {
+        trow[j] = (int64_t)nst * G.tpos[tcell[e0 + j]] + tshape[e0 + j];
+        tc[j] = df_coef(tcoef[e0 + j]);
+      }
+      // the Zcell values of four trial functions (<= 2 x 2 each) are requested before any is used
+      for (int g0 = 0; g0 < (int)(nb1 - nb0); g0 += 4) {
+        float4 z[4][2][2];
+#pragma unroll
+        for (int u = 0; u < 4; ++u)
+#pragma unroll
+          for (int k = 0; k < 2; ++k)
+#pragma unroll
+            for (int j = 0; j < 2; ++j) {
+              const int nn = g0 + u;
+              const bool ok = nn < nb1 - nb0 && k < s_cnt[nn] && j < ne;
+              z[u][k][j] = ok ? zc[s_col[nn][k] + trow[j]] : make_float4(0.f, 0.f, 0.f, 0.f);
+            }
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int nn = g0 + u;
+          if (nn >= nb1 - nb0) break;
+          dfl::df re = z0, im = z0;
+#pragma unroll
+          for (int k = 0; k < 2; ++k)
+#pragma unroll
+            for (int j = 0; j < 2; ++j)
+              if (k < s_cnt[nn] && j < ne) df_acc(re, im, z[u][k][j], dfl::mul(tc[j], s_b[nn][k]));
+          finish(nb0 + nn, re, im);
+        }
+      }
+      nstart = nb1;
+    }
+  }
+  for (int64_t n = nstart; n < nb1; ++n) {
+    dfl::df re = z0, im = z0;
+    for (int64_t f = bptr[n]; f < bptr[n + 1]; ++f) {
+      const int64_t col = ((int64_t)nsb * G.qlocal[bcell[f]] + bshape[f]) * G.ldc;
+      const dfl::df b = df_coef(bcoef[f]);
+      for (int64_t e = e0; e < e0 + ne; ++e)
+        df_acc(re, im, zc[col + (int64_t)nst * G.tpos[tcell[e]] + tshape[e]], dfl::mul(df_coef(tcoef[e]), b));
+    }
+    finish(n, re, im);
   }
 }
 
@@ -1479,19 +1642,20 @@ cudaError_t launch_geometry(const beast_space* s, cudaStream_t st) {
   return cudaGetLastError();
 }
 
-template <int OPK, int TK, int BK, typename R, int C64>
+template <int OPK, int TK, int BK, typename R, int FMT>
 static cudaError_t far_t(const FarParams& P, cudaStream_t st) {
   dim3 grid((unsigned)((P.np + FAR_THREADS - 1) / FAR_THREADS), (unsigned)((P.nq + FAR_QT - 1) / FAR_QT));
   size_t sm = (size_t)FAR_QT * (QREC_HDR + 4 * P.ri.n) * sizeof(R);
-  k_far<OPK, TK, BK, R, C64><<<grid, FAR_THREADS, sm, st>>>(P);
+  k_far<OPK, TK, BK, R, FMT><<<grid, FAR_THREADS, sm, st>>>(P);
   return cudaGetLastError();
 }
 
 template <int OPK, int TK, int BK>
-static cudaError_t far_prec(const FarParams& P, int precision, int c64, cudaStream_t st) {
-  if (precision == BEAST_MIXED) return far_t<OPK, TK, BK, float, 1>(P, st);
-  if (c64) return far_t<OPK, TK, BK, double, 1>(P, st);
-  return far_t<OPK, TK, BK, double, 0>(P, st);
+static cudaError_t far_prec(const FarParams& P, int precision, int fmt, cudaStream_t st) {
+  if (precision == BEAST_MIXED) return far_t<OPK, TK, BK, float, ZCELL_C64>(P, st);
+  if (fmt == ZCELL_C64) return far_t<OPK, TK, BK, double, ZCELL_C64>(P, st);
+  if (fmt == ZCELL_DF) return far_t<OPK, TK, BK, double, ZCELL_DF>(P, st);
+  return far_t<OPK, TK, BK, double, ZCELL_C128>(P, st);
 }
 
 // ---- EFIE far pairs in double-float arithmetic (FP64-quality values on the FP32 pipes) -------
@@ -1504,15 +1668,24 @@ struct FarDfRecord {
   float pad;
   dfl::df eta[RULE_MAXPTS][3];  // inner rule points minus centroid
   dfl::df w[RULE_MAXPTS];       // inner rule weights
+  dfl::df eta2[RULE_MAXPTS];    // |eta_b|^2
 };
 
 DEV dfl::df df_of(double x) {
-  const float h = (float)x;
-  return dfl::df{h, (float)(x - (double)h)};
+  float h, l;
+  fsplit::split_f64(x, &h, &l);
+  return dfl::fast_two_sum(h, l);
 }
 
+// The EFIE far pairs of the mixed-accurate path: k_far's tiling (one test cell per thread,
+// FAR_QT trial cells staged in shared memory), every operation on FP32 pairs (dfloat.h), the
+// cell-pair blocks stored as double-float pairs (ZCELL_DF).  NO x NI > 0: the rule sizes known
+// at compile time (the default 3 x 4 far rules; efie_far_pair_fast), else the general core.
+template <int NO, int NI>
 __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
   __shared__ FarDfRecord rec[FAR_QT];
+  __shared__ float s_tab[64][4];  // sin / cos(m pi/32): lanes read different entries
+  for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
   const int ni = P.ri.n, no = P.ro.n;
   const int q0 = blockIdx.y * FAR_QT;
   const int nqt = min(FAR_QT, P.nq - q0);
@@ -1540,6 +1713,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
       r.eta[bb][1] = df_of(u * (g[1] - cy) + v * (g[4] - cy) + w * (g[7] - cy));
       r.eta[bb][2] = df_of(u * (g[2] - cz) + v * (g[5] - cz) + w * (g[8] - cz));
       r.w[bb] = df_of(P.ri.w[bb]);
+      r.eta2[bb] = dfl::dot3s(r.eta[bb], r.eta[bb]);
     }
   }
   __syncthreads();
@@ -1549,13 +1723,16 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
   const double* tg = P.tgeo + p * GEO_STRIDE;
   const double cpx = tg[9], cpy = tg[10], cpz = tg[11];
   const dfl::df cp[3] = {df_of(cpx), df_of(cpy), df_of(cpz)};
-  dfl::df tau[3][3], xi[RULE_MAXPTS][3], wo[RULE_MAXPTS];
+  constexpr int NOA = NO > 0 ? NO : RULE_MAXPTS;
+  dfl::df tau[3][3], xi[NOA][3], wo[NOA];
   for (int i = 0; i < 3; ++i) {
     tau[i][0] = df_of(tg[3 * i] - cpx);
     tau[i][1] = df_of(tg[3 * i + 1] - cpy);
     tau[i][2] = df_of(tg[3 * i + 2] - cpz);
   }
-  for (int a = 0; a < no; ++a) {
+#pragma unroll
+  for (int a = 0; a < NOA; ++a) {
+    if (NO == 0 && a >= no) break;
     const double u = P.ro.u[a], v = P.ro.v[a], w = 1.0 - u - v;
     xi[a][0] = df_of(u * (tg[0] - cpx) + v * (tg[3] - cpx) + w * (tg[6] - cpx));
     xi[a][1] = df_of(u * (tg[1] - cpy) + v * (tg[4] - cpy) + w * (tg[7] - cpy));
@@ -1565,6 +1742,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
   const float radp = P.tgeof[4 * p + 3];
   const dfl::df kk = df_of(P.op.gi);
   const dfl::cdf alpha{df_of(P.op.ar), df_of(P.op.ai)}, beta{df_of(P.op.br), df_of(P.op.bi)};
+  float4* zc = reinterpret_cast<float4*>(P.zcell);
   for (int qi = 0; qi < nqt; ++qi) {
     const FarDfRecord& r = rec[qi];
     const int ql = q0 + qi;
@@ -1583,35 +1761,39 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
           else
             atomicOr(P.flag, 1);
           for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j)
-              reinterpret_cast<double2*>(P.zcell)[(int64_t)(3 * ql + j) * P.ldc + 3 * pp + i] = make_double2(0, 0);
+            for (int j = 0; j < 3; ++j) zc[(int64_t)(3 * ql + j) * P.ldc + 3 * pp + i] = make_float4(0.f, 0.f, 0.f, 0.f);
           continue;
         }
       }
     }
     dfl::cdf z[9];
-    dfl::efie_far_pair(d, tau, r.sig, no, xi, wo, ni, r.eta, r.w, kk, alpha, beta, z);
+    if constexpr (NO > 0)
+      dfl::efie_far_pair_fast<NO, NI>(d, tau, r.sig, xi, wo, r.eta, r.w, r.eta2, kk, alpha, beta, s_tab, z);
+    else
+      dfl::efie_far_pair(d, tau, r.sig, no, xi, wo, ni, r.eta, r.w, kk, alpha, beta, z);
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) {
         const dfl::cdf& v = z[3 * i + j];
-        reinterpret_cast<double2*>(P.zcell)[(int64_t)(3 * ql + j) * P.ldc + 3 * pp + i] =
-            make_double2((double)v.re.hi + (double)v.re.lo, (double)v.im.hi + (double)v.im.lo);
+        zc[(int64_t)(3 * ql + j) * P.ldc + 3 * pp + i] = make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo);
       }
   }
 }
 
 static cudaError_t far_efie_df(const FarParams& P, cudaStream_t st) {
   dim3 grid((unsigned)((P.np + FAR_THREADS - 1) / FAR_THREADS), (unsigned)((P.nq + FAR_QT - 1) / FAR_QT));
-  k_far_efie_df<<<grid, FAR_THREADS, 0, st>>>(P);
+  if (P.ro.n == 3 && P.ri.n == 4)
+    k_far_efie_df<3, 4><<<grid, FAR_THREADS, 0, st>>>(P);
+  else
+    k_far_efie_df<0, 0><<<grid, FAR_THREADS, 0, st>>>(P);
   return cudaGetLastError();
 }
 
 template <int OPK>
-static cudaError_t far_hh(const FarParams& P, int tk, int bk, int precision, int c64, cudaStream_t st) {
-  if (tk == BEAST_P0 && bk == BEAST_P0) return far_prec<OPK, BEAST_P0, BEAST_P0>(P, precision, c64, st);
-  if (tk == BEAST_P0 && bk == BEAST_P1) return far_prec<OPK, BEAST_P0, BEAST_P1>(P, precision, c64, st);
-  if (tk == BEAST_P1 && bk == BEAST_P0) return far_prec<OPK, BEAST_P1, BEAST_P0>(P, precision, c64, st);
-  if (tk == BEAST_P1 && bk == BEAST_P1) return far_prec<OPK, BEAST_P1, BEAST_P1>(P, precision, c64, st);
+static cudaError_t far_hh(const FarParams& P, int tk, int bk, int precision, int fmt, cudaStream_t st) {
+  if (tk == BEAST_P0 && bk == BEAST_P0) return far_prec<OPK, BEAST_P0, BEAST_P0>(P, precision, fmt, st);
+  if (tk == BEAST_P0 && bk == BEAST_P1) return far_prec<OPK, BEAST_P0, BEAST_P1>(P, precision, fmt, st);
+  if (tk == BEAST_P1 && bk == BEAST_P0) return far_prec<OPK, BEAST_P1, BEAST_P0>(P, precision, fmt, st);
+  if (tk == BEAST_P1 && bk == BEAST_P1) return far_prec<OPK, BEAST_P1, BEAST_P1>(P, precision, fmt, st);
   return cudaErrorInvalidValue;
 }
 
@@ -1641,20 +1823,20 @@ cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev&
   const int kind = a.op.kind;
   if (kind == BEAST_MW_SL || kind == BEAST_MW_DL || kind == BEAST_MW_NXDL) {
     if (tk != BEAST_RT || bk != BEAST_RT) return cudaErrorInvalidValue;
-    if (kind == BEAST_MW_SL && a.precision == BEAST_MIXED_ACCURATE && !a.zcell_c64 && P.op.gr == 0.0) {
+    if (kind == BEAST_MW_SL && a.precision == BEAST_MIXED_ACCURATE && a.zcell_fmt == ZCELL_DF && P.op.gr == 0.0) {
       // mixed-accurate EFIE assemblies (real wavenumber): far pairs in double-float arithmetic
       // on the FP32 pipes (about 1e-12 relative to the FP64 values, at a fraction of the FP64
       // kernel's time on GB300); BEAST_FAR_DF=0 selects the FP64 kernel instead
       const char* e = getenv("BEAST_FAR_DF");
       if (!(e && e[0] == '0')) return far_efie_df(P, st);
     }
-    if (kind == BEAST_MW_SL) return far_prec<BEAST_MW_SL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_c64, st);
-    if (kind == BEAST_MW_DL) return far_prec<BEAST_MW_DL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_c64, st);
-    return far_prec<BEAST_MW_NXDL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_c64, st);
+    if (kind == BEAST_MW_SL) return far_prec<BEAST_MW_SL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_fmt, st);
+    if (kind == BEAST_MW_DL) return far_prec<BEAST_MW_DL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_fmt, st);
+    return far_prec<BEAST_MW_NXDL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_fmt, st);
   }
-  if (kind == BEAST_HH_SL) return far_hh<BEAST_HH_SL>(P, tk, bk, a.precision, a.zcell_c64, st);
-  if (kind == BEAST_HH_DL) return far_hh<BEAST_HH_DL>(P, tk, bk, a.precision, a.zcell_c64, st);
-  if (kind == BEAST_HH_DLT) return far_hh<BEAST_HH_DLT>(P, tk, bk, a.precision, a.zcell_c64, st);
+  if (kind == BEAST_HH_SL) return far_hh<BEAST_HH_SL>(P, tk, bk, a.precision, a.zcell_fmt, st);
+  if (kind == BEAST_HH_DL) return far_hh<BEAST_HH_DL>(P, tk, bk, a.precision, a.zcell_fmt, st);
+  if (kind == BEAST_HH_DLT) return far_hh<BEAST_HH_DLT>(P, tk, bk, a.precision, a.zcell_fmt, st);
   return cudaErrorInvalidValue;
 }
 
@@ -1696,7 +1878,7 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   P.near = a.near;
   P.nnear = nnear;
   P.zcell = a.zcell;
-  P.c64 = a.zcell_c64;
+  P.zfmt = a.zcell_fmt;
   P.ss32 = a.precision == BEAST_MIXED;
   P.ldc = a.ldc;
   P.flag = a.flag;
@@ -1722,7 +1904,14 @@ cudaError_t launch_gather(const GatherArgs& g, cudaStream_t st) {
   k_gather<ZC, OC><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_cell, ts->fn_shape, ts->fn_coeff, \
                                         bs->fn_ptr, bs->fn_cell, bs->fn_shape, bs->fn_coeff, nst, \
                                         nsb, nrows)
-  if (g.zcell_c64) {
+  if (g.zcell_fmt == ZCELL_DF) {
+    if (g.z_c64)
+      k_gather_df<1><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_cell, ts->fn_shape, ts->fn_coeff, bs->fn_ptr,
+                                          bs->fn_cell, bs->fn_shape, bs->fn_coeff, nst, nsb, nrows);
+    else
+      k_gather_df<0><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_cell, ts->fn_shape, ts->fn_coeff, bs->fn_ptr,
+                                          bs->fn_cell, bs->fn_shape, bs->fn_coeff, nst, nsb, nrows);
+  } else if (g.zcell_fmt == ZCELL_C64) {
     if (g.z_c64) GATHER(1, 1); else GATHER(1, 0);
   } else {
     if (g.z_c64) GATHER(0, 1); else GATHER(0, 0);

@@ -76,6 +76,13 @@ DF_HD df add(df a, float b) {
   return fast_two_sum(s.hi, add_rn(s.lo, a.lo));
 }
 DF_HD df sub(df a, df b) { return add(a, neg(b)); }
+// the "sloppy" pair sum of Hida, Li and Bailey: error below about 2^-44 (|a| + |b|) instead
+// of 2^-44 |a + b| -- for sums whose terms do not cancel to far below their size
+DF_HD df adds(df a, df b) {
+  const df s = two_sum(a.hi, b.hi);
+  return fast_two_sum(s.hi, add_rn(s.lo, add_rn(a.lo, b.lo)));
+}
+DF_HD df subs(df a, df b) { return adds(a, neg(b)); }
 DF_HD df mul(df a, df b) {
   const df p = two_prod(a.hi, b.hi);
   return fast_two_sum(p.hi, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo)));
@@ -93,6 +100,21 @@ DF_HD df sqrt(df a) {
   const float s = sqrtf(a.hi);
   const float e = add_rn(fmaf(-s, s, a.hi), a.lo);  // a - s^2
   return fast_two_sum(s, e / mul_rn(2.f, s));
+}
+// 1 / sqrt(a), a > 0: one Newton correction of the FP32 reciprocal square root,
+// y = y0 + y0 (1 - a y0^2) / 2 with a y0^2 formed exactly enough in pairs (about 2^-44).  The
+// FP32 start is the hardware estimate on the device and 1 / sqrtf on the host, so the two
+// builds agree to the pair accuracy here rather than bit for bit.
+DF_HD df rsqrt(df a) {
+#if defined(__CUDA_ARCH__)
+  const float y0 = rsqrtf(a.hi);
+#else
+  const float y0 = 1.f / sqrtf(a.hi);
+#endif
+  const df y2 = two_prod(y0, y0);
+  const df ay2 = mul(a, y2);
+  const float e = add_rn(sub_rn(1.f, ay2.hi), -ay2.lo);  // 1 - a y0^2, about 2^-22
+  return fast_two_sum(y0, mul_rn(mul_rn(y0, e), 0.5f));
 }
 // 1 / a: one Newton correction of the FP32 reciprocal
 DF_HD df rcp(df a) {
@@ -125,6 +147,25 @@ DF_HD void sincos(df th, df* s, df* c) {
   const df sm = {tab[m][0], tab[m][1]}, cm = {tab[m][2], tab[m][3]};
   *s = add(mul(sm, ct), mul(cm, st));
   *c = sub(mul(cm, ct), mul(sm, st));
+}
+
+// sincos with the table of m pi/32 passed in (shared memory in a kernel: lanes read different
+// entries) and pair sums that do not cancel taken as sloppy sums; the argument reduction keeps
+// the exact sums.  Same range and error class as sincos.
+DF_HD void sincos_tab(df th, const float (*tab)[4], df* s, df* c) {
+  const float n = rintf(mul_rn(th.hi, DF_32_OVER_PI));
+  df t = add(th, neg(two_prod(n, DF_PI32_0)));
+  t = add(t, neg(two_prod(n, DF_PI32_1)));
+  t = add(t, -mul_rn(n, DF_PI32_2));
+  const int m = ((int)n) & 63;
+  const float t2 = mul_rn(t.hi, t.hi);
+  const float q = fmaf(t2, fmaf(t2, -1.f / 5040.f, 1.f / 120.f), -1.f / 6.f);
+  const df st = add(t, mul_rn(mul_rn(t.hi, t2), q));
+  const float r4 = mul_rn(mul_rn(t2, t2), fmaf(t2, -1.f / 720.f, 1.f / 24.f));
+  const df ct = add(add(make(1.f), neg(scale(mul(t, t), 0.5f))), r4);
+  const df sm = {tab[m][0], tab[m][1]}, cm = {tab[m][2], tab[m][3]};
+  *s = adds(mul(sm, ct), mul(cm, st));
+  *c = subs(mul(cm, ct), mul(sm, st));
 }
 
 // Helmholtz / Maxwell Green's function exp(-i k R) / (4 pi R) for a real wavenumber k

@@ -76,4 +76,89 @@ DF_HD void efie_far_pair(const df* d, const df (*tau)[3], const df (*sig)[3], in
     }
 }
 
+// The same block for rule sizes known at compile time (the default far rules: NO = 3 test and
+// NI = 4 trial points), with the work per point pair cut down:
+//   * R^2 = (A_a + Q_b) - 2 P_ab with A_a = |d + xi_a|^2 (per test point), Q_b = |eta_b|^2 -
+//     2 d.eta_b (per trial point) and P_ab = xi_a.eta_b, which the M1 moment needs anyway;
+//   * 1 / R from a pair reciprocal square root, R = R^2 / R, the weight folded into 1/(4 pi R);
+//   * sums whose terms do not cancel far below their size (moments, dot products of small
+//     vectors, the angle sum of the sine / cosine) as sloppy pair sums;
+//   * the table of sin / cos(m pi/32) read from `tab` (shared memory in the kernel);
+//   * the 3 x 3 block from per-row and per-column parts: z_ij = C - S_j - T_i + (tau_i.sig_j) D
+//     with C = a4 M1 + beta M0, S_j = a4 sig_j.V1, T_i = a4 tau_i.V2, D = a4 M0, a4 = alpha/4.
+// eta2[b] = |eta_b|^2 (staged with the trial cell).  Matches efie_far_pair to the pair
+// arithmetic's accuracy.
+DF_HD cdf cadds(cdf a, cdf b) { return {adds(a.re, b.re), adds(a.im, b.im)}; }
+DF_HD cdf csubs(cdf a, cdf b) { return {subs(a.re, b.re), subs(a.im, b.im)}; }
+DF_HD cdf cmuls(cdf a, cdf b) {
+  return {subs(mul(a.re, b.re), mul(a.im, b.im)), adds(mul(a.re, b.im), mul(a.im, b.re))};
+}
+DF_HD df dot3s(const df* a, const df* b) { return adds(adds(mul(a[0], b[0]), mul(a[1], b[1])), mul(a[2], b[2])); }
+DF_HD cdf cdot3s(const cdf* v, const df* b) {
+  return cadds(cadds(cscale(v[0], b[0]), cscale(v[1], b[1])), cscale(v[2], b[2]));
+}
+
+template <int NO, int NI>
+DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3], const df (*xi)[3],
+                              const df* wo, const df (*eta)[3], const df* wi, const df* eta2, df k, cdf alpha,
+                              cdf beta, const float (*tab)[4], cdf* out) {
+  const df z0 = make(0.f);
+  const df i4pi{DF_I4PI_HI, DF_I4PI_LO};
+  df A[NO];
+  cdf U0[NO];
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int a = 0; a < NO; ++a) {
+    df dx[3];
+    for (int c = 0; c < 3; ++c) dx[c] = add(d[c], xi[a][c]);
+    A[a] = dot3s(dx, dx);
+    U0[a] = cdf{z0, z0};
+  }
+  cdf M0{z0, z0}, M1{z0, z0}, V2[3];
+  for (int c = 0; c < 3; ++c) V2[c] = cdf{z0, z0};
+  for (int b = 0; b < NI; ++b) {
+    const df Q = subs(eta2[b], scale(dot3s(d, eta[b]), 2.f));
+    const df wq = mul(wi[b], i4pi);
+    cdf T{z0, z0};
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+    for (int a = 0; a < NO; ++a) {
+      const df P = dot3s(xi[a], eta[b]);
+      const df R2 = subs(adds(A[a], Q), scale(P, 2.f));
+      const df iR = rsqrt(R2);
+      const df R = mul(R2, iR);
+      df sn, cs;
+      sincos_tab(mul(k, R), tab, &sn, &cs);
+      const df amp = mul(iR, wq);  // w_b / (4 pi R)
+      const cdf K{mul(amp, cs), neg(mul(amp, sn))};
+      U0[a] = cadds(U0[a], K);
+      const cdf wK = cscale(K, wo[a]);
+      T = cadds(T, wK);
+      M1 = cadds(M1, cscale(wK, P));
+    }
+    M0 = cadds(M0, T);
+    for (int c = 0; c < 3; ++c) V2[c] = cadds(V2[c], cscale(T, eta[b][c]));
+  }
+  cdf V1[3];
+  for (int c = 0; c < 3; ++c) V1[c] = cdf{z0, z0};
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int a = 0; a < NO; ++a) {
+    const cdf s = cscale(U0[a], wo[a]);
+    for (int c = 0; c < 3; ++c) V1[c] = cadds(V1[c], cscale(s, xi[a][c]));
+  }
+  const cdf a4{scale(alpha.re, 0.25f), scale(alpha.im, 0.25f)};
+  const cdf C = cadds(cmuls(a4, M1), cmuls(beta, M0));
+  const cdf D = cmuls(a4, M0);
+  cdf S[3], T[3];
+  for (int j = 0; j < 3; ++j) S[j] = cmuls(a4, cdot3s(V1, sig[j]));
+  for (int i = 0; i < 3; ++i) T[i] = cmuls(a4, cdot3s(V2, tau[i]));
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j)
+      out[3 * i + j] = cadds(csubs(csubs(C, S[j]), T[i]), cscale(D, dot3s(tau[i], sig[j])));
+}
+
 }  // namespace dfl

@@ -1,0 +1,101 @@
+// An FP64 value split into two floats with integer operations only: a ~= hi + lo to about
+// 2^-47 relative.  GB300 runs FP64 instructions, conversions included, at a small fraction of
+// its FP32 rate, so the refinement matvec of a c128 matrix reads each entry as FP64 bits and
+// works on the FP32 pipes.
+//   hi: the sign, the exponent and the top 23 stored mantissa bits (a truncation, so
+//       |lo| < 2^-23 |hi|);
+//   lo: the remaining 29 mantissa bits converted to float (rounded to 24 bits) and scaled by
+//       2^(e - 1075), with the sign of a.
+// |a| < 2^-97 gives 0 + 0, and lo is dropped below |a| = 2^-74: absolute errors below 1e-29,
+// far under the FP64 rounding of a matvec of boundary-element entries.  |a| >= 2^128 (not a
+// BEM matrix entry) overflows to +-inf, so the matvec reports it instead of hiding it.  Host
+// and device builds give identical bits.
+#pragma once
+#include <stdint.h>
+#include <string.h>
+
+#if defined(__CUDACC__)
+#define FS_HD __host__ __device__ __forceinline__
+#else
+#define FS_HD inline
+#endif
+
+namespace fsplit {
+
+FS_HD uint64_t bits64(double a) {
+#if defined(__CUDA_ARCH__)
+  return (uint64_t)__double_as_longlong(a);
+#else
+  uint64_t u;
+  memcpy(&u, &a, 8);
+  return u;
+#endif
+}
+FS_HD float from_bits(uint32_t u) {
+#if defined(__CUDA_ARCH__)
+  return __uint_as_float(u);
+#else
+  float f;
+  memcpy(&f, &u, 4);
+  return f;
+#endif
+}
+FS_HD uint32_t to_bits(float f) {
+#if defined(__CUDA_ARCH__)
+  return __float_as_uint(f);
+#else
+  uint32_t u;
+  memcpy(&u, &f, 4);
+  return u;
+#endif
+}
+
+// (hi, lo) of a
+FS_HD void split_f64(double a, float* hi, float* lo) {
+  const uint64_t u = bits64(a);
+  const uint32_t top = (uint32_t)(u >> 32);
+  const int e = (int)((top >> 20) & 0x7FF);
+  const uint32_t sgn = top & 0x80000000u;
+  if (e > 1150) {  // beyond the float range (NaN and infinity included): +-inf or NaN
+    *hi = (float)a;
+    *lo = 0.f;
+    return;
+  }
+  if (e < 926) {
+    *hi = 0.f;
+    *lo = 0.f;
+    return;
+  }
+  *hi = from_bits(sgn | ((uint32_t)(e - 896) << 23) | (uint32_t)((u >> 29) & 0x7FFFFFu));
+  *lo = 0.f;
+  if (e >= 949) {
+    const float scale = from_bits((uint32_t)(e - 948) << 23);  // 2^(e - 1075), exact
+    // the 29-bit integer rounds to 24 bits in the conversion; the power-of-two scaling is exact
+    const float m = (float)(uint32_t)(u & 0x1FFFFFFFu);
+    *lo = from_bits(to_bits(m * scale) | sgn);
+  }
+}
+
+}  // namespace fsplit
+
+namespace fsplit {
+
+// a float as a double with integer operations only (exact; subnormal floats, below 1.2e-38,
+// become 0; infinities and NaN take the conversion instruction)
+FS_HD double f2d(float f) {
+  const uint32_t u = to_bits(f);
+  const uint32_t e = (u >> 23) & 0xFF;
+  if (e == 0xFF) return (double)f;
+  if (e == 0) return 0.0;
+  const uint64_t b = ((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896) << 52) |
+                     ((uint64_t)(u & 0x7FFFFFu) << 29);
+#if defined(__CUDA_ARCH__)
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  memcpy(&d, &b, 8);
+  return d;
+#endif
+}
+
+}  // namespace fsplit

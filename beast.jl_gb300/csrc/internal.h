@@ -127,6 +127,11 @@ struct OpParams {
   double br, bi;   // beta
 };
 
+// element format of the cell-pair blocks (Zcell): complex FP64 (plain path), complex FP32
+// (mixed path), or double-float pairs (mixed-accurate path: re.hi, re.lo, im.hi, im.lo as one
+// float4, written and summed on the FP32 pipes)
+enum { ZCELL_C128 = 0, ZCELL_C64 = 1, ZCELL_DF = 2 };
+
 // near-pair list entry
 struct NearPair {
   int p, q;       // test active cell, trial cell (chunk-local index)
@@ -144,8 +149,8 @@ struct AsmArgs {
   // chunk description
   const int* qcells;   // device: trial active cell ids of this chunk [nq]
   int nq;
-  void* zcell;         // device Zcell [ns_t*ncells_t x ns_b*nq], c128 or c64
-  int zcell_c64;
+  void* zcell;         // device Zcell [ns_t*ncells_t x ns_b*nq], in format zcell_fmt
+  int zcell_fmt;       // ZCELL_C128, ZCELL_C64 or ZCELL_DF
   int64_t ldc;
   NearPair* near;      // device near list
   int near_cap;
@@ -161,7 +166,7 @@ struct GatherArgs {
   const beast_space* ts;
   const beast_space* bs;
   const void* zcell;
-  int zcell_c64;
+  int zcell_fmt;
   int64_t ldc;
   const int* qlocal;      // device: trial active cell -> chunk-local index (-1 absent)
   const int* tpos;        // device: test active cell -> Zcell position

@@ -22,6 +22,7 @@
 #include <string>
 #include <vector>
 
+#include "fsplit.h"
 #include "internal.h"
 
 // the pivot allocation of a factorisation: ipiv[n], perm[n], then (256-byte aligned) the
@@ -1550,22 +1551,6 @@ __global__ void k_permute(const T* in, T* out, const int* perm, int64_t n) {
 
 // ---- FP64 matvec y = alpha A x + beta y  (A c128 or c64) --------------------------------
 constexpr int MV_SLABS = 32;
-template <typename T>
-__global__ void k_gemv_partial(int64_t n, const T* A, int64_t lda, const double* x, double* part) {
-  int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-  int s = blockIdx.y;
-  int64_t c0 = n * s / MV_SLABS, c1 = n * (s + 1) / MV_SLABS;
-  if (i >= n) return;
-  double sr = 0, si = 0;
-  for (int64_t j = c0; j < c1; ++j) {
-    T a = A[i + j * lda];
-    double xr = x[2 * j], xi = x[2 * j + 1];
-    sr += (double)a.x * xr - (double)a.y * xi;
-    si += (double)a.x * xi + (double)a.y * xr;
-  }
-  part[2 * (s * n + i)] = sr;
-  part[2 * (s * n + i) + 1] = si;
-}
 // x (complex FP64) split into float hi + lo parts: (re_hi, im_hi, re_lo, im_lo)
 __global__ void k_split_x(int64_t n, const double* x, float4* xs) {
   int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -1680,6 +1665,35 @@ __global__ void k_gemv_partial_c64_df2(int64_t n, const float2* A, int64_t lda, 
     part[2 * (s * n + i + 1)] = (double)h1.x + (double)l1.x;
     part[2 * (s * n + i + 1) + 1] = (double)h1.y + (double)l1.y;
   }
+}
+
+// partial sums of A x for a c128 matrix on the FP32 pipes: each entry split into hi + lo
+// floats (fsplit.h), hi * x_hi kept exactly (TwoProduct) and added with TwoSum, the terms of
+// the low parts (hi * x_lo, lo * x_hi) accumulated in FP32 -- the compensated dot product of
+// k_gemv_partial_c64_df2 with the matrix's own low part added.  About 2^-47 relative per
+// product, against a few FP64 multiply-adds per entry at GB300's FP64 rate.
+__global__ void k_gemv_partial_c128_df(int64_t n, const double2* A, int64_t lda, const float4* xs,
+                                       double* part) {
+  const int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int s = blockIdx.y;
+  const int64_t c0 = n * s / MV_SLABS, c1 = n * (s + 1) / MV_SLABS;
+  if (i >= n) return;
+  float2 h = make_float2(0.f, 0.f), l = h;
+#pragma unroll 4
+  for (int64_t j = c0; j < c1; ++j) {
+    const float4 xv = xs[j];
+    const float2 X1 = make_float2(xv.x, xv.y), X2 = make_float2(-xv.y, xv.x);
+    const float2 L1 = make_float2(xv.z, xv.w), L2 = make_float2(-xv.w, xv.z);
+    const double2 a = A[i + j * lda];
+    float2 ar, ai;
+    fsplit::split_f64(a.x, &ar.x, &ar.y);
+    fsplit::split_f64(a.y, &ai.x, &ai.y);
+    cdf_acc2(make_float2(ar.x, ar.x), make_float2(ai.x, ai.x), X1, X2, L1, L2, h, l);
+    l = __ffma2_rn(make_float2(ar.y, ar.y), X1, l);
+    l = __ffma2_rn(make_float2(ai.y, ai.y), X2, l);
+  }
+  part[2 * (s * n + i)] = (double)h.x + (double)l.x;
+  part[2 * (s * n + i) + 1] = (double)h.y + (double)l.y;
 }
 
 __global__ void k_gemv_reduce(int64_t n, const double* part, double* y, double alpha, double beta) {
@@ -2279,9 +2293,9 @@ cudaError_t gemv_dev(int64_t n, const void* A, int64_t lda, int a_c64, const dou
   cudaError_t e = cudaMallocAsync(&part, need, st);
   if (e != cudaSuccess) return e;
   dim3 g((unsigned)((n + 127) / 128), MV_SLABS);
+  float4* xs = reinterpret_cast<float4*>(part + (size_t)MV_SLABS * n * 2);
+  k_split_x<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x, xs);
   if (a_c64) {
-    float4* xs = reinterpret_cast<float4*>(part + (size_t)MV_SLABS * n * 2);
-    k_split_x<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, x, xs);
     if (lda % 2 == 0 && (reinterpret_cast<uintptr_t>(A) & 15) == 0) {
       dim3 g2((unsigned)((n + 255) / 256), MV_SLABS);
       k_gemv_partial_c64_df2<<<g2, 128, 0, st>>>(n, (const float2*)A, lda, xs, part);
@@ -2289,7 +2303,7 @@ cudaError_t gemv_dev(int64_t n, const void* A, int64_t lda, int a_c64, const dou
       k_gemv_partial_c64_df<<<g, 128, 0, st>>>(n, (const float2*)A, lda, xs, part);
     }
   } else
-    k_gemv_partial<double2><<<g, 128, 0, st>>>(n, (const double2*)A, lda, x, part);
+    k_gemv_partial_c128_df<<<g, 128, 0, st>>>(n, (const double2*)A, lda, xs, part);
   k_gemv_reduce<<<(unsigned)((n + 255) / 256), 256, 0, st>>>(n, part, y, alpha, beta);
   e = cudaGetLastError();
   cudaFreeAsync(part, st);

@@ -1,16 +1,22 @@
 """Benchmark: EFIE solves/s on one GB300 (Galerkin assembly + excitation + dense solve).
 
-Workload (default): icosphere subdivided 5x (20480 triangles, 30720 RT unknowns), EFIE
+Workload (default, C2): icosphere subdivided 5x (20480 triangles, 30720 RT unknowns), EFIE
 (Maxwell3D.singlelayer, k = 10), plane wave x-hat / z-hat polarisation, default quadrature
-strategy DoubleNumWiltonSauterQStrat(2,3,6,7,5,5,4,3), mixed precision (FP32 far pairs +
-FP64 near/singular pairs, c64 matrix, FP32 LU, FP64 iterative refinement to 1e-10).
-A step = one assemble + excitation + solve of that system.
+strategy DoubleNumWiltonSauterQStrat(2,3,6,7,5,5,4,3), mixed-accurate precision: far pairs in
+double-float arithmetic on the FP32 pipes, Sauter-Schwab / singularity-extraction near pairs in
+FP64, c128 matrix, complex FP32 factorisation with FP16-operand tensor-core updates, FP64
+iterative refinement against the c128 matrix to 1e-10.  A step = one assemble + excitation +
+solve of that system.
 
-  value   steps/s with mesh and spaces resident on the device (timed with CUDA events)
-  e2e     the same through the C ABI from host buffers: mesh + assembly data uploaded and
-          the solution read back inside every step
+  value      steps/s with mesh and spaces resident on the device (CUDA events)
+  accuracy   surface current, far field and matrix (Frobenius) relative to the plain FP64 path
+             (FP64 assembly + FP64 LU, solved once in the same run; its solves/s is `fp64`)
+  modes      the fast mixed mode (FP32 far pairs, c64 matrix) for context: its speed and error
+  mfie       the MFIE leg (n x K - Id/2 on the same mesh): solves/s and accuracy
+  e2e        the headline mode through the C ABI from host buffers: mesh + assembly data
+             uploaded and the solution read back inside every step
   roofline, gpu_launches from the library's event instrumentation over the timed steps
-  cpu_baseline  the CPU oracle (a restatement of BEAST's algorithm) on a bounded sample
+  cpu_baseline  the reference's CPU path (oracle assembly + LAPACK solve) on a bounded sample
 
 `--impl reference` times the reference's CPU algorithm (the oracle port; Julia is not
 available) on the host cores and prints the same line with "impl": "reference".
@@ -37,14 +43,20 @@ for p in (os.path.join(ROOT, "beast.jl_gb300"), os.path.join(ROOT, "oracle")):
 def parse():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--level", type=int, default=5)
     ap.add_argument("--k", type=float, default=10.0)
-    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed-accurate", "fp64"],
-                    help="mixed-accurate: FP64 assembly (c128 matrix), mixed factorisation, "
-                         "refinement against the c128 matrix")
+    ap.add_argument("--precision", default="mixed-accurate", choices=["mixed", "mixed-accurate", "fp64"],
+                    help="mixed-accurate (default; meets the 1e-6 surface-current contract): double-float "
+                         "far pairs + FP64 near pairs into a c128 matrix, mixed factorisation, FP64 "
+                         "refinement against the c128 matrix; mixed: FP32 far pairs, c64 matrix")
+    ap.add_argument("--mfie-precision", default="mixed", choices=["mixed", "mixed-accurate", "fp64"])
+    ap.add_argument("--no-fp64", action="store_true",
+                    help="skip the plain FP64 solve (its solves/s and the accuracy figures)")
+    ap.add_argument("--no-mfie", action="store_true", help="skip the MFIE leg")
+    ap.add_argument("--no-modes", action="store_true", help="skip the other mixed mode")
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -75,13 +87,14 @@ def workload(args):
 def config_dict(args, X, m):
     return {"workload": f"EFIE k={args.k:g} on icosphere level {args.level} "
                         f"({m.numcells()} triangles, {X.numfunctions()} RT unknowns), "
-                        f"{args.precision} precision, 1 plane-wave RHS",
+                        f"{args.precision} precision, 1 plane-wave RHS; MFIE leg n x K - Id/2 "
+                        f"({args.mfie_precision})",
             "triangles": int(m.numcells()), "unknowns": int(X.numfunctions()),
             "quadstrat": "DoubleNumWiltonSauterQStrat(2,3,6,7,5,5,4,3)",
             "precision": args.precision, "refinement_tol": args.tol,
             "l2": f"inputs larger than L2 (matrix {X.numfunctions() ** 2 * 8 / 1e9:.2f} GB c64 / "
                   f"{X.numfunctions() ** 2 * 16 / 1e9:.2f} GB c128)",
-            "parallelism": f"replicas x{args.gpus}"}
+            "parallelism": "one GPU"}
 
 
 def peaks():
@@ -456,6 +469,316 @@ def run_c5(args):
                       "data": "synthetic seeded request stream"}))
 
 
+class Problem:
+    """one boundary-integral equation of the workload on the device, driven through the C ABI:
+    assemble (+ local term) + plane-wave excitation + dense solve, the `solve(eq)` path of
+    src/solvers/lusolver.jl:9-39"""
+
+    def __init__(self, ctx, X, op, exc_kind, local=None, quadstrat=None):
+        import beastgpu as bg
+        self.ctx, self.lib, self.X, self.n = ctx, ctx.lib, X, X.numfunctions()
+        self.sh = ctx.space_handle(X)
+        qs = quadstrat or bg.defaultquadstrat(op, X, X)
+        self.od, self.qd = bg.api._op_desc(op), bg.api._qs_desc(qs)
+        self.exc_kind, self.local = exc_kind, local
+        self.it, self.res = C.c_int(0), C.c_double(0)
+
+    def buffers(self, precision):
+        import torch
+        from beastgpu import lib as L
+        dt = L.C64 if precision == L.MIXED else L.C128
+        Z = torch.empty((self.n, self.n), dtype=torch.complex64 if dt == L.C64 else torch.complex128, device="cuda")
+        b = torch.empty(self.n, dtype=torch.complex128, device="cuda")
+        x = torch.empty(self.n, dtype=torch.complex128, device="cuda")
+        return Z, dt, b, x
+
+    def assemble(self, precision, Z, dt):
+        from beastgpu import lib as L
+        c, n = self.ctx, self.n
+        c.check(self.lib.beast_assemble(c.handle, C.byref(self.od), C.byref(self.qd), self.sh, self.sh, precision,
+                                        Z.data_ptr(), n, dt, L.DEVICE, 0, 0, 1.0, 0.0, 0))
+        if self.local is not None:
+            which, coeff = self.local
+            c.check(self.lib.beast_assemble_local(c.handle, which, self.sh, self.sh, 6, Z.data_ptr(), n, dt,
+                                                  L.DEVICE, 0, 0, coeff, 0.0))
+
+    def rhs(self, b, d, pol, g):
+        from beastgpu import lib as L
+        self.ctx.check(self.lib.beast_rhs_planewave(self.ctx.handle, self.exc_kind, self.sh, d.ctypes.data,
+                                                    pol.ctypes.data, g.real, g.imag, 1.0, 0.0, 8, b.data_ptr(),
+                                                    L.DEVICE))
+
+    def solve(self, precision, Z, dt, b, x, tol):
+        from beastgpu import lib as L
+        self.ctx.check(self.lib.beast_solve_dense(self.ctx.handle, self.n, Z.data_ptr(), self.n, dt, precision,
+                                                  b.data_ptr(), x.data_ptr(), 1, L.DEVICE, tol, 30,
+                                                  C.byref(self.it), C.byref(self.res)))
+
+    def step(self, precision, Z, dt, b, x, wave, tol):
+        self.assemble(precision, Z, dt)
+        self.rhs(b, *wave)
+        self.solve(precision, Z, dt, b, x, tol)
+
+
+def _events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+
+
+def _timed(fn, stream):
+    """(ms, result) of fn() between CUDA events on the stream"""
+    import torch
+    e0, e1 = _events()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    r = fn()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    return e0.elapsed_time(e1), r
+
+
+def _fro_diff(Za, Zb, slab=2048):
+    """||Za - Zb||_F / ||Zb||_F on the device, in row slabs (no full-size temporaries)"""
+    import torch
+    num = den = 0.0
+    for r0 in range(0, Zb.shape[0], slab):
+        zb = Zb[r0:r0 + slab]
+        num += float(torch.linalg.norm(Za[r0:r0 + slab].to(torch.complex128) - zb)) ** 2
+        den += float(torch.linalg.norm(zb)) ** 2
+    return (num / den) ** 0.5
+
+
+def _accuracy(bg, X, x, xref, dirs, g, Z=None, Zref=None, ctx=None):
+    """relative differences from the plain FP64 solution: surface current, far field
+    (directions `dirs`) and, when both matrices are given, the matrix (Frobenius)"""
+    fa, fr = bg.farfield(X, x, dirs, g, ctx=ctx), bg.farfield(X, xref, dirs, g, ctx=ctx)
+    out = {"surface_current": float(np.linalg.norm(x - xref) / np.linalg.norm(xref)),
+           "far_field": float(np.linalg.norm(fa - fr) / np.linalg.norm(fr))}
+    if Z is not None and Zref is not None:
+        out["matrix_frobenius"] = _fro_diff(Z, Zref)
+    return out
+
+
+PRECISIONS = {"mixed": 1, "mixed-accurate": 2, "fp64": 0}
+
+
+def run_c2(args):
+    """The bench line: C2 (EFIE k = 10 on the 20480-triangle icosphere, 30720 RT unknowns).
+    value = solves/s of the --precision mode (default mixed-accurate, the mode that meets the
+    1e-6 surface-current contract) with mesh and spaces resident; its accuracy, the plain FP64
+    path's solves/s on the same system and the fast mixed mode are measured in the same run;
+    the MFIE leg (n x K - Id/2 on the same mesh) is a second key."""
+    import torch
+    import beastgpu as bg
+    from beastgpu import lib as L
+    dev = 0
+    torch.cuda.set_device(dev)
+    m, X, op, E = workload(args)
+    n = X.numfunctions()
+    prec = PRECISIONS[args.precision]
+    ctx = bg.Context(dev)
+    stream = torch.cuda.current_stream()
+    ctx.check(ctx.lib.beast_ctx_set_stream(ctx.handle, C.c_void_p(stream.cuda_stream)))
+    efie = Problem(ctx, X, op, L.EXC_TANGTRACE_E)
+    wave = (np.array([1.0, 0, 0]), np.array([0, 0, 1.0]), complex(E.gamma))
+    g = complex(E.gamma)
+    th = np.linspace(0.0, np.pi, 181)
+    dirs = np.stack([np.sin(th), np.zeros_like(th), np.cos(th)], axis=1)
+    out_extra = {}
+
+    # ---- plain FP64 path on the same system (reference solution and denominator)
+    fp64 = None
+    if not args.no_fp64:
+        Z64, dt64, b64, x64 = efie.buffers(L.FP64)
+        efie.assemble(L.FP64, Z64, dt64)  # warm-up of the assembly kernels
+        ms_a, _ = _timed(lambda: efie.assemble(L.FP64, Z64, dt64), stream)
+        ms_s, _ = _timed(lambda: (efie.rhs(b64, *wave), efie.solve(L.FP64, Z64, dt64, b64, x64, args.tol)), stream)
+        fp64 = {"ms_per_solve": ms_a + ms_s, "solves_per_s": 1000.0 / (ms_a + ms_s),
+                "assembly_ms": ms_a, "excitation_and_lu_ms": ms_s,
+                "how": "one timed solve after a warm-up assembly: FP64 quadrature, c128 matrix, FP64 LU with "
+                       "partial pivoting, CUDA events"}
+        xref = x64.cpu().numpy()
+
+    # ---- the headline mode
+    Z, dt, b, x = efie.buffers(prec)
+    for _ in range(args.warmup):
+        efie.step(prec, Z, dt, b, x, wave, args.tol)
+    torch.cuda.synchronize()
+    clk = Clocks(dev)
+    ctx.prof_enable(True, kinds=None if args.prof_all else ["lu_tc_gemm"])
+    torch.cuda.synchronize()
+    evs = [_events() for _ in range(args.steps)]
+    e0, e1 = _events()
+    e0.record(stream)
+    for i in range(args.steps):
+        evs[i][0].record(stream)
+        efie.step(prec, Z, dt, b, x, wave, args.tol)
+        evs[i][1].record(stream)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1)
+    clocks = clk.stop()
+    step_ms = np.array([a.elapsed_time(c) for a, c in evs])
+    prof_timed = ctx.prof_read()
+    launches = ctx.launches()
+    it, res, mode = efie.it.value, efie.res.value, ctx.last_factor_mode()
+    # per-class breakdown: one more step with every class bracketed (not timed)
+    ctx.prof_enable(True)
+    efie.step(prec, Z, dt, b, x, wave, args.tol)
+    torch.cuda.synchronize()
+    prof = {k: (v[0] * args.steps, v[1] * args.steps, v[2] * args.steps) for k, v in ctx.prof_read().items()}
+    if "lu_tc_gemm" in prof_timed:
+        prof["lu_tc_gemm"] = prof_timed["lu_tc_gemm"]
+    ctx.prof_enable(False)
+    ms_step = ms / args.steps
+    value = 1000.0 / ms_step
+    accuracy = None
+    if fp64 is not None:
+        accuracy = _accuracy(bg, X, x.cpu().numpy(), xref, dirs, g, Z, Z64, ctx=ctx)
+        accuracy["reference"] = "plain FP64 path of this run (FP64 assembly + FP64 LU)"
+    del Z
+    torch.cuda.empty_cache()
+
+    # ---- the other mixed mode, for context (one timed solve after a warm-up)
+    modes = {}
+    if not args.no_modes:
+        for name in ("mixed", "mixed-accurate"):
+            p = PRECISIONS[name]
+            if p == prec:
+                continue
+            Zm, dtm, bm, xm = efie.buffers(p)
+            efie.step(p, Zm, dtm, bm, xm, wave, args.tol)
+            msm, _ = _timed(lambda: efie.step(p, Zm, dtm, bm, xm, wave, args.tol), stream)
+            modes[name] = {"solves_per_s": 1000.0 / msm, "ms_per_solve": msm}
+            if fp64 is not None:
+                modes[name]["accuracy"] = _accuracy(bg, X, xm.cpu().numpy(), xref, dirs, g, Zm, Z64, ctx=ctx)
+            del Zm
+            torch.cuda.empty_cache()
+    if fp64 is not None:
+        del Z64
+        torch.cuda.empty_cache()
+
+    # ---- MFIE leg: (n x K - Id/2) on the same mesh, examples/nxmfie.jl
+    mfie_out = None
+    if not args.no_mfie:
+        nxk = bg.nxdoublelayer(wavenumber=args.k)
+        mf = Problem(ctx, X, nxk, L.EXC_CROSSTRACE_H, local=(0, -0.5))
+        mprec = PRECISIONS[args.mfie_precision]
+        mfie_out = {"workload": f"MFIE (n x K - Id/2, DoubleNumQStrat(6,7) for every pair) k={args.k:g}, "
+                                f"same mesh, n x H of the same plane wave", "precision": args.mfie_precision}
+        if fp64 is not None:
+            Zr, dtr, br, xr = mf.buffers(L.FP64)
+            ms_a, _ = _timed(lambda: mf.assemble(L.FP64, Zr, dtr), stream)
+            mf.rhs(br, *wave)
+            xr = torch.zeros_like(br)
+            itg, resg = C.c_int(0), C.c_double(0)
+            ctx.check(ctx.lib.beast_gmres(ctx.handle, n, Zr.data_ptr(), n, dtr, br.data_ptr(), xr.data_ptr(),
+                                          L.DEVICE, 1e-13, 300, 3000, C.byref(itg), C.byref(resg)))
+            itg = itg.value
+            xr_h = xr.cpu().numpy()
+            mfie_out["fp64"] = {"assembly_ms": ms_a, "ms_per_solve": ms_a + fp64["excitation_and_lu_ms"],
+                                "solves_per_s": 1000.0 / (ms_a + fp64["excitation_and_lu_ms"]),
+                                "how": "FP64 n x K assembly timed here + the FP64 LU time of the EFIE system "
+                                       "(same n); reference solution by FP64 GMRES to 1e-13 "
+                                       f"({itg} iterations)"}
+        Zm, dtm, bm, xm = mf.buffers(mprec)
+        for _ in range(max(1, min(2, args.warmup))):
+            mf.step(mprec, Zm, dtm, bm, xm, wave, args.tol)
+        nst = max(1, min(5, args.steps))
+        msm, _ = _timed(lambda: [mf.step(mprec, Zm, dtm, bm, xm, wave, args.tol) for _ in range(nst)], stream)
+        mfie_out.update({"solves_per_s": 1000.0 * nst / msm, "ms_per_solve": msm / nst, "steps": nst,
+                         "refinement": {"iters": mf.it.value, "rel_residual": mf.res.value,
+                                        "factorisation": FACTOR_MODES[max(0, ctx.last_factor_mode())]}})
+        if fp64 is not None:
+            mfie_out["accuracy"] = _accuracy(bg, X, xm.cpu().numpy(), xr_h, dirs, g, Zm, Zr, ctx=ctx)
+            mfie_out["accuracy"]["reference"] = "plain FP64 assembly, FP64 GMRES solution"
+            mfie_out["speedup_over_fp64"] = mfie_out["solves_per_s"] / mfie_out["fp64"]["solves_per_s"]
+            del Zr
+        del Zm
+        torch.cuda.empty_cache()
+
+    # ---- end to end through the C ABI with host buffers (the headline mode)
+    e2e = None
+    if not args.no_e2e:
+        ad = X.assemblydata()
+        verts = np.ascontiguousarray(m.vertices)
+        cells = np.ascontiguousarray(m.cells, dtype=np.int32)
+        xh = np.zeros(n, dtype=np.complex128)
+        h2d = verts.nbytes + cells.nbytes + ad.cells.nbytes + ad.dof.nbytes + ad.coeff.nbytes
+        d2h = xh.nbytes
+        c2 = bg.Context(dev)
+        lib = c2.lib
+        d, pol = wave[0], wave[1]
+        it2, res2 = C.c_int(0), C.c_double(0)
+
+        def e2e_step():
+            mh, shh = C.c_void_p(), C.c_void_p()
+            c2.check(lib.beast_mesh_upload(c2.handle, verts.ctypes.data, verts.shape[0],
+                                           cells.ctypes.data, cells.shape[0], 0, C.byref(mh)))
+            c2.check(lib.beast_space_upload(c2.handle, mh, ad.kind, ad.cells.shape[0],
+                                            ad.cells.ctypes.data, ad.maxfn, ad.nshapes,
+                                            ad.dof.ctypes.data, ad.coeff.ctypes.data, n, 0,
+                                            C.byref(shh)))
+            c2.check(lib.beast_solve_job(c2.handle, C.byref(efie.od), C.byref(efie.qd), shh, 0,
+                                         d.ctypes.data, pol.ctypes.data, g.real, g.imag, prec,
+                                         args.tol, xh.ctypes.data, L.HOST, C.byref(it2),
+                                         C.byref(res2)))
+            lib.beast_space_free(shh)
+            lib.beast_mesh_free(mh)
+
+        e2e_step()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        te = (time.perf_counter() - t0) / args.steps
+        e2e = {"value": 1.0 / te, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
+               "d2h_bytes_per_step": int(d2h)}
+        c2.close()
+
+    # ---- roofline: the tensor-core trailing update of the LU
+    pk, src = peaks()
+    dominant = max(prof.items(), key=lambda kv: kv[1][0])[0]
+    name = "lu_tc_gemm" if "lu_tc_gemm" in prof else dominant
+    kms, nl, work = prof[name]
+    achieved = work / (kms * 1e-3) / 1e12
+    peak = pk.get("bf16_tflops_sustained", pk["bf16_tflops"])
+    # DRAM traffic per launch: bytes per algorithmic flop measured by ncu on one k_tc_gemm
+    # launch (the first lower-triangle trailing update of the level-4 EFIE: 400 MB of DRAM
+    # traffic for 1.81e11 flops, C' read and written once by the TMA reduce-adds), scaled to
+    # this run's average launch by its flops
+    traffic = 2.21e-3 * work / nl if name == "lu_tc_gemm" else None
+    roof = {"bound": "tensor", "kernel": name, "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": achieved / peak, "peak_source": src,
+            "peak_note": "measured dense bf16 (sustained); the kernel runs FP16 operands with FP32 "
+                         "accumulation (same tensor rate as bf16)",
+            "traffic": traffic, "launches": nl, "avg_launch_ms": kms / nl, "dominant_by_time": dominant}
+    breakdown = {k: {"ms": v[0], "launches": v[1], "share": v[0] / sum(w[0] for w in prof.values())}
+                 for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
+    out = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+           "latency_ms": {"p50": float(np.percentile(step_ms, 50)), "p99": float(np.percentile(step_ms, 99)),
+                          "max": float(step_ms.max()), "of": "the timed steps (one solve each, CUDA events)"},
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+           "dtype": {L.MIXED: "c64+f64", L.MIXED_ACCURATE: "c128+c64"}.get(prec, "c128"),
+           "data": "synthetic icosphere mesh",
+           "config": config_dict(args, X, m),
+           "accuracy": accuracy,
+           "fp64": fp64,
+           "speedup_over_fp64": (value / fp64["solves_per_s"]) if fp64 else None,
+           "refinement": {"iters": it, "rel_residual": res, "factorisation": FACTOR_MODES[max(0, mode)]},
+           "modes": modes, "mfie": mfie_out,
+           "roofline": roof, "kernel_breakdown": breakdown, "gpu_launches": int(launches),
+           "clocks": clocks, "e2e": e2e}
+    if not args.no_cpu_baseline:
+        out["cpu_baseline"] = cpu_baseline(args, X, m)
+    print(json.dumps(out))
+
+
+FACTOR_MODES = ["LU with partial pivoting", "unpivoted LU", "symmetric LDL^T-type"]
+
+
 def main():
     args = parse()
     rank = int(os.environ.get("RANK", "0"))
@@ -472,144 +795,7 @@ def main():
         return run_c3(args)
     if args.config == "c5":
         return run_c5(args)
-    import torch
-    import beastgpu as bg
-    from beastgpu import lib as L
-    dev = 0
-    torch.cuda.set_device(dev)
-    m, X, op, E = workload(args)
-    n = X.numfunctions()
-    prec = {"mixed": L.MIXED, "mixed-accurate": L.MIXED_ACCURATE, "fp64": L.FP64}[args.precision]
-    ctx = bg.Context(dev)
-    stream = torch.cuda.current_stream()
-    ctx.check(ctx.lib.beast_ctx_set_stream(ctx.handle, C.c_void_p(stream.cuda_stream)))
-    lib = ctx.lib
-    sh = ctx.space_handle(X)
-    qs = bg.defaultquadstrat(op, X, X)
-    od, qd = bg.api._op_desc(op), bg.api._qs_desc(qs)
-    dt = L.C64 if prec == L.MIXED else L.C128
-    Z = torch.empty((n, n), dtype=torch.complex64 if dt == L.C64 else torch.complex128,
-                    device=f"cuda:{dev}")
-    b = torch.empty(n, dtype=torch.complex128, device=f"cuda:{dev}")
-    x = torch.empty(n, dtype=torch.complex128, device=f"cuda:{dev}")
-    d = np.array([1.0, 0, 0])
-    pol = np.array([0, 0, 1.0])
-    g = complex(E.gamma)
-    it, res = C.c_int(0), C.c_double(0)
-
-    def step():
-        ctx.check(lib.beast_assemble(ctx.handle, C.byref(od), C.byref(qd), sh, sh, prec,
-                                     Z.data_ptr(), n, dt, L.DEVICE, 0, 0, 1.0, 0.0, 0))
-        ctx.check(lib.beast_rhs_planewave(ctx.handle, 0, sh, d.ctypes.data, pol.ctypes.data,
-                                          g.real, g.imag, 1.0, 0.0, 8, b.data_ptr(), L.DEVICE))
-        ctx.check(lib.beast_solve_dense(ctx.handle, n, Z.data_ptr(), n, dt, prec, b.data_ptr(),
-                                        x.data_ptr(), 1, L.DEVICE, args.tol, 30, C.byref(it),
-                                        C.byref(res)))
-
-    for _ in range(args.warmup):
-        step()
-    torch.cuda.synchronize()
-    clk = Clocks(dev)
-    # timed steps: CUDA events only around the dominant class (the roofline kernel)
-    ctx.prof_enable(True, kinds=None if args.prof_all else ["lu_tc_gemm"])
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1)
-    clocks = clk.stop()
-    prof_timed = ctx.prof_read()
-    launches = ctx.launches()
-    # per-class breakdown: one more step with every class bracketed (not timed)
-    ctx.prof_enable(True)
-    step()
-    torch.cuda.synchronize()
-    prof = {k: (v[0] * args.steps, v[1] * args.steps, v[2] * args.steps) for k, v in ctx.prof_read().items()}
-    if "lu_tc_gemm" in prof_timed:
-        prof["lu_tc_gemm"] = prof_timed["lu_tc_gemm"]
-    ctx.prof_enable(False)
-    ms_step = ms / args.steps
-    value = 1000.0 / ms_step
-
-    # ---- end to end through the C ABI with host buffers
-    e2e = None
-    if not args.no_e2e:
-        ad = X.assemblydata()
-        verts = np.ascontiguousarray(m.vertices)
-        cells = np.ascontiguousarray(m.cells, dtype=np.int32)
-        xh = np.zeros(n, dtype=np.complex128)
-        h2d = verts.nbytes + cells.nbytes + ad.cells.nbytes + ad.dof.nbytes + ad.coeff.nbytes
-        d2h = xh.nbytes
-        c2 = bg.Context(dev)
-
-        def e2e_step():
-            mh, shh = C.c_void_p(), C.c_void_p()
-            c2.check(lib.beast_mesh_upload(c2.handle, verts.ctypes.data, verts.shape[0],
-                                           cells.ctypes.data, cells.shape[0], 0, C.byref(mh)))
-            c2.check(lib.beast_space_upload(c2.handle, mh, ad.kind, ad.cells.shape[0],
-                                            ad.cells.ctypes.data, ad.maxfn, ad.nshapes,
-                                            ad.dof.ctypes.data, ad.coeff.ctypes.data, n, 0,
-                                            C.byref(shh)))
-            c2.check(lib.beast_solve_job(c2.handle, C.byref(od), C.byref(qd), shh, 0,
-                                         d.ctypes.data, pol.ctypes.data, g.real, g.imag, prec,
-                                         args.tol, xh.ctypes.data, L.HOST, C.byref(it),
-                                         C.byref(res)))
-            lib.beast_space_free(shh)
-            lib.beast_mesh_free(mh)
-
-        e2e_step()
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            e2e_step()
-        torch.cuda.synchronize()
-        te = (time.perf_counter() - t0) / args.steps
-        e2e = {"value": 1.0 / te, "unit": "solves/s", "h2d_bytes_per_step": int(h2d),
-               "d2h_bytes_per_step": int(d2h)}
-        c2.close()
-    # ---- roofline: the tensor-core trailing update of the LU (the dominant kernel class)
-    pk, src = peaks()
-    dominant = max(prof.items(), key=lambda kv: kv[1][0])[0]
-    name = "lu_tc_gemm" if "lu_tc_gemm" in prof else dominant
-    kms, nl, work = prof[name]
-    memory_bound = name in ("gather", "gemv", "trsv", "convert", "lu_laswp")
-    if memory_bound:
-        achieved = work / (kms * 1e-3) / 1e9
-        peak, unit, bound = pk["hbm_gbs"], "GB/s", "hbm"
-    else:
-        achieved = work / (kms * 1e-3) / 1e12
-        peak, unit, bound = pk.get("bf16_tflops_sustained", pk["bf16_tflops"]), "TFLOP/s", "tensor"
-    # DRAM traffic per launch: bytes per algorithmic flop measured by ncu on one k_tc_gemm
-    # launch (the first lower-triangle trailing update of the level-4 EFIE: 400 MB of DRAM
-    # traffic for 1.81e11 flops, C' read and written once by the TMA reduce-adds), scaled to
-    # this run's average launch by its flops.  The class brackets the k_tc_gemm launches only
-    # (their FP16 operand preparation is counted as "convert").
-    traffic = 2.21e-3 * work / nl if name == "lu_tc_gemm" else None
-    roof = {"bound": bound, "kernel": name, "achieved": achieved, "peak": peak, "unit": unit,
-            "frac": achieved / peak, "peak_source": src,
-            "peak_note": "measured dense bf16 (sustained); the kernel runs FP16 operands with FP32 accumulation (same tensor rate as bf16)",
-            "traffic": traffic, "launches": nl, "avg_launch_ms": kms / nl,
-            "dominant_by_time": dominant}
-    breakdown = {k: {"ms": v[0], "launches": v[1], "share": v[0] / sum(w[0] for w in prof.values())}
-                 for k, v in sorted(prof.items(), key=lambda kv: -kv[1][0])}
-    out = {"metric": "solves/s", "value": value, "unit": "solves/s", "n_gpus": 1,
-           "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
-           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-           "dtype": {L.MIXED: "c64+f64", L.MIXED_ACCURATE: "c128+c64"}.get(prec, "c128"),
-           "data": "synthetic icosphere mesh",
-           "config": config_dict(args, X, m), "refinement": {"iters": it.value,
-                                                            "rel_residual": res.value,
-                                                            "factorisation": ["LU with partial pivoting",
-                                                                              "unpivoted LU", "symmetric LDL^T-type"][
-                                                                max(0, ctx.last_factor_mode())]},
-           "roofline": roof, "kernel_breakdown": breakdown, "gpu_launches": int(launches),
-           "clocks": clocks, "e2e": e2e}
-    if not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(args, X, m)
-    print(json.dumps(out))
+    return run_c2(args)
 
 
 if __name__ == "__main__":

@@ -42,7 +42,8 @@ void t_green(const double* R, const double* k, int64_t n, double* out) {
 // EFIE far block of one cell pair from double geometry (staged as the kernel would: centroid
 // differences and rule points relative to the centroids in double, then split into pairs)
 void t_efie_pair(const double* tv, const double* bv, int no, const double* uvo, const double* wo, int ni,
-                 const double* uvi, const double* wi, double k, const double* al, const double* be, double* out) {
+                 const double* uvi, const double* wi, double k, const double* al, const double* be, double* out,
+                 int fast) {
   double cp[3], cq[3];
   for (int c = 0; c < 3; ++c) { cp[c] = (tv[c] + tv[3 + c] + tv[6 + c]) / 3; cq[c] = (bv[c] + bv[3 + c] + bv[6 + c]) / 3; }
   df d[3], tau[3][3], sig[3][3], xi[16][3], eta[16][3], w1[16], w2[16];
@@ -60,8 +61,15 @@ void t_efie_pair(const double* tv, const double* bv, int no, const double* uvo, 
     w2[b] = from(wi[b]);
   }
   cdf z[9];
-  efie_far_pair(d, tau, sig, no, xi, w1, ni, eta, w2, from(k), cdf{from(al[0]), from(al[1])},
-                cdf{from(be[0]), from(be[1])}, z);
+  if (fast && no == 3 && ni == 4) {
+    df e2[4];
+    for (int b = 0; b < 4; ++b) e2[b] = dot3s(eta[b], eta[b]);
+    efie_far_pair_fast<3, 4>(d, tau, sig, xi, w1, eta, w2, e2, from(k), cdf{from(al[0]), from(al[1])},
+                             cdf{from(be[0]), from(be[1])}, sincos_tab_host, z);
+  } else {
+    efie_far_pair(d, tau, sig, no, xi, w1, ni, eta, w2, from(k), cdf{from(al[0]), from(al[1])},
+                  cdf{from(be[0]), from(be[1])}, z);
+  }
   for (int e = 0; e < 9; ++e) { out[2 * e] = to(z[e].re); out[2 * e + 1] = to(z[e].im); }
 }
 }
@@ -159,9 +167,11 @@ def test_device_compile(tmp_path):
                     str(tmp_path / "k.o")], check=True)
 
 
-def test_efie_far_pair_matches_the_fp64_oracle(lib):
+@pytest.mark.parametrize("fast", [0, 1])
+def test_efie_far_pair_matches_the_fp64_oracle(lib, fast):
     """the double-float EFIE far block against the oracle's FP64 double quadrature (the
-    reference's DoubleQuadRule), on far pairs of a level-3 icosphere at k = 10"""
+    reference's DoubleQuadRule), on far pairs of a level-3 icosphere at k = 10: the general
+    core and the one for the default rule sizes (3 x 4 points) that the kernel runs"""
     import beastgpu as bg
     import oracle as O
     m = bg.icosphere(3)
@@ -184,7 +194,8 @@ def test_efie_far_pair_matches_the_fp64_oracle(lib):
                                                               uvi.ravel(), wi, [al.real, al.imag],
                                                               [be.real, be.imag])]
         lib.t_efie_pair(_p(args[0]), _p(args[1]), C.c_int(len(wo)), _p(args[2]), _p(args[3]), C.c_int(len(wi)),
-                        _p(args[4]), _p(args[5]), C.c_double(k), _p(args[6]), _p(args[7]), _p(out))
+                        _p(args[4]), _p(args[5]), C.c_double(k), _p(args[6]), _p(args[7]), _p(out),
+                        C.c_int(fast))
         z = (out[0::2] + 1j * out[1::2]).reshape(3, 3)
         worst = max(worst, np.abs(z - ref).max() / np.abs(ref).max())
         tested += 1

@@ -1,12 +1,14 @@
 """GPU parity: libbeastgpu (through the C ABI) against the CPU oracle.
 
 Tolerances:
-  FP64 path: 1e-10 relative PER ENTRY, |Z_ij - Zo_ij| <= 1e-10 (|Zo_ij| + 1e-12 max|Zo|) -- the
-      absolute floor only matters for entries that are (nearly) zero, such as double-layer
-      entries of coplanar pairs;
+  FP64 path: 1e-10 relative PER ENTRY with an absolute floor at FP64 rounding level,
+      |Z_ij - Zo_ij| <= 1e-10 |Zo_ij| + 1e-13 max|Zo|: relative for every entry above 1e-3 of
+      the largest.  Smaller entries are sums of cell-pair terms of about that size that cancel
+      (exactly zero on symmetric meshes, or the (h/R)^2 cancellation of RT divergence terms),
+      so two FP64 evaluations in different order agree there to a few ulps of those terms, not
+      of the entry: 1e-13 of the largest entry is 1e-10 relative to them;
   mixed-accurate path (double-float far pairs, FP64 near pairs, c128 storage): 1e-11 relative
-      in the Frobenius norm and 1e-8 per entry with the same floor (the far entries of RT
-      functions cancel by about (h/R)^2, which magnifies the double-float rounding there);
+      in the Frobenius norm and 1e-8 per entry with the same floor;
   mixed path (FP32 far pairs, c64 storage): 1e-6 relative in the Frobenius norm (the north
       star's matrix error measure; per entry the FP32 cancellation error is not bounded).
 """
@@ -31,9 +33,17 @@ def rel(a, b):
     return float(np.abs(a - b).max() / np.abs(b).max())
 
 
-def rel_entry(a, b, floor=1e-12):
+def rel_entry(a, b, floor=1e-3):
     """largest per-entry relative difference, with an absolute floor of floor * max|b|"""
     return float((np.abs(a - b) / (np.abs(b) + floor * np.abs(b).max())).max())
+
+
+def err_profile(a, b):
+    """for failure messages: relative to the largest entry, and per entry above 1e-3 of it"""
+    big = np.abs(b) > 1e-3 * np.abs(b).max()
+    per = np.abs(a - b)[big] / np.abs(b)[big]
+    return {"max_rel": rel(a, b), "entry_q50": float(np.median(per)), "entry_max": float(per.max()),
+            "floor": rel_entry(a, b)}
 
 
 def rel_fro(a, b):
@@ -54,7 +64,7 @@ def _check(op, X, Y, ctx, tol=1e-10, precision=bg.FP64, qs=None):
     Z = bg.assemble(op, X, Y, quadstrat=qs, precision=precision, ctx=ctx)
     Zo = O.assemble(_orc_op(op), _orc_qs(qs), X, Y)
     e = rel_entry(Z, Zo)
-    assert e < tol, (e, rel(Z, Zo))
+    assert e < tol, err_profile(Z, Zo)
     return Z, Zo
 
 
@@ -85,7 +95,7 @@ def test_mfie_double_layer(ctx):
 
 def test_nxk(ctx):
     X = bg.raviartthomas(bg.icosphere(1))
-    _check(bg.nxdoublelayer(wavenumber=2.0), X, X, ctx, tol=1e-9)
+    _check(bg.nxdoublelayer(wavenumber=2.0), X, X, ctx)
 
 
 @pytest.mark.parametrize("which", ["sl", "dl", "dlt"])
@@ -122,7 +132,7 @@ def test_mixed_accurate_assembly(ctx):
     assert Z.dtype == np.complex128
     Zo = O.assemble(_orc_op(op), _orc_qs(bg.defaultquadstrat(op, X, X)), X, X)
     assert rel_fro(Z, Zo) < 1e-11, rel_fro(Z, Zo)
-    assert rel_entry(Z, Zo) < 1e-8, rel_entry(Z, Zo)
+    assert rel_entry(Z, Zo) < 1e-8, err_profile(Z, Zo)
 
 
 def test_c1_efie_assembly(ctx):
@@ -146,7 +156,7 @@ def test_c2_efie_row_sample(ctx):
         Zo = O.assemble(_orc_op(op), _orc_qs(qs), X, X, row_lo=lo, row_hi=lo + 64)
         Z = blk(np.arange(lo, lo + 64), cols)
         e = rel_entry(Z, Zo)
-        assert e < 1e-10, (lo, e)
+        assert e < 1e-10, (lo, err_profile(Z, Zo))
 
 
 @pytest.mark.parametrize("which", ["singlelayer", "doublelayer", "doublelayer_transposed"])
@@ -200,7 +210,18 @@ def test_linear_combination_mfie(ctx):
     Z = bg.assemble(nxk - 0.5 * bg.Identity(), X, X, ctx=ctx)
     Zo = O.assemble(_orc_op(nxk), _orc_qs(bg.defaultquadstrat(nxk, X, X)), X, X)
     Zo = Zo - 0.5 * O.assemble_local(0, X, X, degree=6)
-    assert rel(Z, Zo) < 1e-9
+    assert rel_entry(Z, Zo) < 1e-10, err_profile(Z, Zo)
+
+
+def test_mfie_mixed_is_near_fp32_rounding(ctx):
+    """the MFIE (n x K - Id/2) assembled on the mixed path: far pairs in FP32, the pairs whose
+    rule points come close in FP64 -- within 1e-6 of the FP64 matrix (Frobenius)"""
+    X = bg.raviartthomas(bg.icosphere(2))
+    nxk = bg.nxdoublelayer(wavenumber=3.0)
+    op = nxk - 0.5 * bg.Identity()
+    Zm = bg.assemble(op, X, X, precision=bg.MIXED, ctx=ctx)
+    Z = bg.assemble(op, X, X, ctx=ctx)
+    assert rel_fro(Zm.astype(np.complex128), Z) < 1e-6, rel_fro(Zm.astype(np.complex128), Z)
 
 
 def test_rhs_and_farfield(ctx):
