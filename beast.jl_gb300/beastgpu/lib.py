@@ -44,6 +44,7 @@ EXPORTS = [
     "beast_mesh_free", "beast_space_upload", "beast_space_free", "beast_assemble",
     "beast_assemble_block", "beast_assemble_local", "beast_rhs_planewave", "beast_lu_factor", "beast_lu_solve",
     "beast_lu_free", "beast_lu_solve_noalloc", "beast_solve_dense", "beast_gmres", "beast_farfield", "beast_solve_job",
+    "beast_system_create", "beast_system_solve", "beast_system_bytes", "beast_system_free", "beast_pool_stats",
     "beast_prof_enable", "beast_prof_enable_kinds", "beast_prof_read", "beast_prof_launches", "beast_last_factor_mode", "beast_version",
 ]
 
@@ -91,6 +92,12 @@ def load(build_if_needed=True):
     L.beast_farfield.argtypes = [vp, vp, vp, vp, i64, d, d, i, vp, i]
     L.beast_solve_job.argtypes = [vp, C.POINTER(OpDesc), C.POINTER(QsDesc), vp, i, vp, vp, d, d, i,
                                   d, vp, i, C.POINTER(C.c_int), C.POINTER(C.c_double)]
+    L.beast_system_create.argtypes = [vp, C.POINTER(OpDesc), C.POINTER(QsDesc), vp, i, d, d, i, pp]
+    L.beast_system_solve.argtypes = [vp, vp, i, i64, vp, vp, d, d, d, vp, i, C.POINTER(C.c_int),
+                                     C.POINTER(C.c_double)]
+    L.beast_system_bytes.argtypes = [vp, C.POINTER(C.c_size_t)]
+    L.beast_system_free.argtypes = [vp]
+    L.beast_pool_stats.argtypes = [vp] + [C.POINTER(C.c_size_t)] * 4
     L.beast_prof_enable.argtypes = [vp, i]
     L.beast_prof_read.argtypes = [vp, i, C.POINTER(C.c_double), C.POINTER(C.c_int64),
                                   C.POINTER(C.c_double)]

@@ -7,6 +7,16 @@ assemble + excitation + dense-solve jobs of different sizes concurrently on one 
     srv.latency_ms()                        # p50 / p99 / max of submit -> completion
     srv.close()
 
+Residency.  Each slot keeps the meshes / spaces it served (`resident`, least recently used
+out) and, with `resident_systems`, whole factored systems (`beast_system_*`: the matrix and
+its factors) keyed by (space, operator, strategy, local term, precision): a request on a
+resident system only builds its excitations and solves against the kept factors.  A job is
+routed to the slot that holds its system when that slot is free.
+
+Memory.  All of a job's device memory comes from the CUDA stream-ordered pool the library
+allocates from (matrix, factors, vectors), so the admitted footprints, plus the bytes of the
+resident systems, bound what the pool holds.
+
 Admission.  A job is admitted when a worker slot is free and its device footprint fits in
 what the admitted jobs leave of the HBM budget (`job_footprint`: the N^2 complex entries of
 the matrix and of its factor copy dominate, plus the context's assembly workspace).  Jobs are
@@ -90,57 +100,131 @@ class ResidentSpaces:
             self._free(self.entries.popitem(last=False)[1])
 
 
+def system_key(job):
+    """what identifies a job's system: the space (by identity), the operator, the strategy,
+    the local term and the precision"""
+    from .operators import defaultquadstrat
+    op = job["op"]
+    qs = job.get("quadstrat") or defaultquadstrat(op, job["space"], job["space"])
+    return (id(job["space"]), op.kind, complex(op.gamma), complex(op.alpha), complex(op.beta), tuple(qs.orders()),
+            tuple(job.get("local") or ()), job.get("precision", L.MIXED))
+
+
+class ResidentSystems:
+    """factored systems kept on a slot's device (least recently used first out, at most
+    `capacity` of them), each with its own mesh and space handles; `bytes` is what the
+    systems hold"""
+
+    def __init__(self, ctx, capacity):
+        self.ctx = ctx
+        self.capacity = int(capacity)
+        self.entries = collections.OrderedDict()  # key -> (space, system, bytes, mesh h, space h)
+        self.created = 0
+
+    @property
+    def bytes(self):
+        return sum(e[2] for e in self.entries.values())
+
+    def __contains__(self, key):
+        return key in self.entries
+
+    def get(self, key, m, space, make):
+        """the system of key (make(space handle) creates it on a miss)"""
+        e = self.entries.get(key)
+        if e is not None and e[0] is space:
+            self.entries.move_to_end(key)
+            return e[1]
+        if e is not None:  # a dead space's id was reused
+            self._free(self.entries.pop(key))
+        mh, sh = _upload(self.ctx, m, space)
+        try:
+            h = make(sh)
+        except BaseException:
+            self.ctx.lib.beast_space_free(sh)
+            self.ctx.lib.beast_mesh_free(mh)
+            raise
+        nb = C.c_size_t(0)
+        self.ctx.check(self.ctx.lib.beast_system_bytes(h, C.byref(nb)))
+        self.entries[key] = (space, h, int(nb.value), mh, sh)
+        self.created += 1
+        while len(self.entries) > self.capacity:
+            self._free(self.entries.popitem(last=False)[1])
+        return h
+
+    def evict_oldest(self):
+        """frees the least recently used system; False when there is none"""
+        if not self.entries:
+            return False
+        self._free(self.entries.popitem(last=False)[1])
+        return True
+
+    def _free(self, e):
+        self.ctx.lib.beast_system_free(e[1])
+        self.ctx.lib.beast_space_free(e[4])
+        self.ctx.lib.beast_mesh_free(e[3])
+
+    def close(self):
+        while self.entries:
+            self._free(self.entries.popitem(last=False)[1])
+
+
 def run_job(ctx, job):
     """one job through the C ABI on ctx's stream: mesh + space upload (or the handles kept by
-    ctx.resident, a ResidentSpaces), assembly on the device (plus an optional local operator:
-    `local` = (which, coefficient), e.g. (0, -0.5) for the MFIE's -Id/2), one excitation per
-    plane wave, dense solve with all right-hand sides, solution back to the host.  job: mesh,
-    space, op, waves, exc_kind, and optionally local, precision (default MIXED), tol (default
-    1e-10).  Returns (x [nrhs, n], iters, resid)."""
-    import torch
+    ctx.resident, a ResidentSpaces), the factored system (beast_system_create: assembly on the
+    device, plus an optional local operator `local` = (which, coefficient), e.g. (0, -0.5) for
+    the MFIE's -Id/2, and the factorisation -- or the one kept by ctx.systems, a
+    ResidentSystems), one excitation per plane wave and the solve of all of them against the
+    factors, solution back to the host.  job: mesh, space, op, waves, exc_kind, and optionally
+    local, precision (default MIXED), tol (default 1e-10), quadstrat.  Returns
+    (x [nrhs, n], iters, resid)."""
     from . import api
     from .operators import defaultquadstrat
     m, X, op, waves, exc_kind = job["mesh"], job["space"], job["op"], job["waves"], job["exc_kind"]
     prec = job.get("precision", L.MIXED)
     tol = job.get("tol", 1e-10)
+    if len({complex(w.gamma) for w in waves}) != 1:
+        raise ValueError("the plane waves of one job share their wavenumber")
     lib = ctx.lib
     resident = getattr(ctx, "resident", None)
-    if resident is not None:
-        mh, sh = resident.handles(m, X)
-    else:
-        mh, sh = _upload(ctx, m, X)
+    systems = getattr(ctx, "systems", None)
+    n = X.numfunctions()
+    nr = len(waves)
+    qs = job.get("quadstrat") or defaultquadstrat(op, X, X)
+    od, qd = api._op_desc(op), api._qs_desc(qs)
+    which, lc = job.get("local") or (-1, 0.0)
+    lc = complex(lc)
+
+    def make(sh):
+        h = C.c_void_p()
+        ctx.check(lib.beast_system_create(ctx.handle, C.byref(od), C.byref(qd), sh, which, lc.real, lc.imag,
+                                          prec, C.byref(h)))
+        return h
+
+    mh = sh = None
+    if systems is None:
+        if resident is not None:
+            mh, sh = resident.handles(m, X)
+        else:
+            mh, sh = _upload(ctx, m, X)
     try:
+        sysh = systems.get(system_key(job), m, X, make) if systems is not None else make(sh)
         try:
-            n = X.numfunctions()
-            nr = len(waves)
-            qs = defaultquadstrat(op, X, X)
-            od, qd = api._op_desc(op), api._qs_desc(qs)
-            dev = f"cuda:{ctx.device}"
-            zdt = L.C64 if prec == L.MIXED else L.C128
-            Z = torch.empty((n, n), dtype=torch.complex64 if zdt == L.C64 else torch.complex128, device=dev)
-            B = torch.empty((nr, n), dtype=torch.complex128, device=dev)
-            Xs = torch.empty((nr, n), dtype=torch.complex128, device=dev)
-            ctx.check(lib.beast_assemble(ctx.handle, C.byref(od), C.byref(qd), sh, sh, prec, Z.data_ptr(), n,
-                                         zdt, L.DEVICE, 0, 0, 1.0, 0.0, 0))
-            if job.get("local"):
-                which, c = job["local"]
-                ctx.check(lib.beast_assemble_local(ctx.handle, which, sh, sh, 6, Z.data_ptr(), n, zdt, L.DEVICE,
-                                                   0, 0, c, 0.0))
-            for r, w in enumerate(waves):
-                d = np.ascontiguousarray(w.direction, dtype=np.float64)
-                pol = np.ascontiguousarray(getattr(w, "polarization", (0.0, 0.0, 0.0)), dtype=np.float64)
-                g, a = complex(w.gamma), complex(w.amplitude)
-                ctx.check(lib.beast_rhs_planewave(ctx.handle, exc_kind, sh, d.ctypes.data, pol.ctypes.data, g.real,
-                                                  g.imag, a.real, a.imag, 8, B[r].data_ptr(), L.DEVICE))
+            dirs = np.ascontiguousarray([w.direction for w in waves], dtype=np.float64)
+            pols = np.ascontiguousarray([getattr(w, "polarization", (0.0, 0.0, 0.0)) for w in waves],
+                                        dtype=np.float64)
+            g = complex(waves[0].gamma)
+            amps = [complex(w.amplitude) for w in waves]
+            x = np.zeros((nr, n), dtype=np.complex128)
             it, res = C.c_int(0), C.c_double(0)
-            ctx.check(lib.beast_solve_dense(ctx.handle, n, Z.data_ptr(), n, zdt, prec, B.data_ptr(), Xs.data_ptr(),
-                                            nr, L.DEVICE, tol, 30, C.byref(it), C.byref(res)))
-            x = Xs.cpu().numpy()
+            ctx.check(lib.beast_system_solve(ctx.handle, sysh, exc_kind, nr, dirs.ctypes.data, pols.ctypes.data,
+                                             g.real, g.imag, tol, x.ctypes.data, L.HOST, C.byref(it), C.byref(res)))
+            x *= np.asarray(amps)[:, None]  # the solve is linear in the wave's amplitude
         finally:
-            if resident is None:
-                lib.beast_space_free(sh)
+            if systems is None:
+                lib.beast_system_free(sysh)
     finally:
-        if resident is None:
+        if systems is None and resident is None:
+            lib.beast_space_free(sh)
             lib.beast_mesh_free(mh)
     return x, it.value, res.value
 
@@ -152,7 +236,8 @@ class Server:
     the CPU with stand-ins); footprint(job) defaults to job_footprint of the job's space."""
 
     def __init__(self, slots=2, hbm_budget=None, device=0, allow_pass=False, workspace=None,
-                 make_context=None, runner=None, footprint=None, resident=0):
+                 make_context=None, runner=None, footprint=None, resident=0, resident_systems=0,
+                 key=None):
         if slots < 1:
             raise ValueError("slots must be >= 1")
         if hbm_budget is None:
@@ -175,7 +260,10 @@ class Server:
                 c.set_workspace_limit(self.workspace)
                 if resident > 0:  # meshes / spaces kept on the device per slot
                     c.resident = ResidentSpaces(c, resident)
+                if resident_systems > 0:  # factored systems kept on the device per slot
+                    c.systems = ResidentSystems(c, resident_systems)
                 return c
+        self._key = key or (system_key if resident_systems > 0 else None)
         self._cv = threading.Condition()
         self._pending = collections.deque()
         self._free = []
@@ -185,6 +273,7 @@ class Server:
         self._closed = False
         self._lat = []
         self._ctxs = [make_context() for _ in range(slots)]
+        self._held = [0] * slots  # bytes of the resident systems of each slot
         self._queues = [collections.deque() for _ in range(slots)]
         self._threads = []
         for s in range(slots):
@@ -211,25 +300,51 @@ class Server:
             self._dispatch()
         return fut
 
+    def _slot_for(self, job):  # caller holds _cv: a free slot, the one holding the job's system first
+        if self._key is not None:
+            k = self._key(job)
+            for s in self._free:
+                systems = getattr(self._ctxs[s], "systems", None)
+                if systems is not None and k in systems:
+                    return s, True
+        return self._free[-1], False
+
+    def _make_room(self, need, keep):  # caller holds _cv: evict resident systems of idle slots
+        for s in list(self._free):
+            systems = getattr(self._ctxs[s], "systems", None)
+            while systems is not None and self._used + sum(self._held) + need > self.budget:
+                if s == keep and len(systems.entries) <= 1 or not systems.evict_oldest():
+                    break
+                self._held[s] = systems.bytes
+        return self._used + sum(self._held) + need <= self.budget
+
     def _dispatch(self):  # caller holds _cv
         while self._free and self._pending:
             pick = None
             for i, item in enumerate(self._pending):
-                if self._used + item[3] <= self.budget:
+                s, hit = self._slot_for(item[0])
+                need = self._resident_footprint(item[0]) if hit else item[3]
+                if self._used + sum(self._held) + need <= self.budget or (
+                        need <= self.budget and self._make_room(need, s if hit else -1)):
                     pick = i
                     break
                 if not self.allow_pass:
                     break
             if pick is None:
                 return
-            item = self._pending[pick]
+            job, fut, t0, _ = self._pending[pick]
             del self._pending[pick]
-            self._used += item[3]
-            self._peak = max(self._peak, self._used)
+            self._used += need
+            self._peak = max(self._peak, self._used + sum(self._held))
             self._running += 1
-            s = self._free.pop()
-            self._queues[s].append(item)
+            self._free.remove(s)
+            self._queues[s].append((job, fut, t0, need))
             self._cv.notify_all()
+
+    def _resident_footprint(self, job):
+        """a job on a resident system: the excitations, solutions and refinement vectors"""
+        n = job["space"].numfunctions()
+        return int(16 * n * (2 * (len(job.get("waves", ())) or 1) + 4) + (16 << 20))
 
     def _worker(self, s):
         ctx = self._ctxs[s]
@@ -250,6 +365,9 @@ class Server:
                 with self._cv:
                     self._lat.append(time.perf_counter() - t0)
                     self._used -= fp
+                    systems = getattr(ctx, "systems", None)
+                    self._held[s] = systems.bytes if systems is not None else 0
+                    self._peak = max(self._peak, self._used + sum(self._held))
                     self._running -= 1
                     self._free.append(s)
                     self._dispatch()
@@ -270,6 +388,8 @@ class Server:
         for t in self._threads:
             t.join()
         for c in self._ctxs:
+            if getattr(c, "systems", None) is not None:
+                c.systems.close()
             if getattr(c, "resident", None) is not None:
                 c.resident.close()
             if hasattr(c, "close"):
@@ -286,8 +406,17 @@ class Server:
 
     @property
     def peak_bytes(self):
-        """largest sum of admitted footprints seen (never above the budget)"""
+        """largest sum of admitted footprints and resident systems seen (never above the budget)"""
         return self._peak
+
+    def pool_stats(self):
+        """the device pool's reserved and used bytes now and at their highest"""
+        c = self._ctxs[0]
+        if not hasattr(c, "lib"):
+            return None
+        v = [C.c_size_t(0) for _ in range(4)]
+        c.check(c.lib.beast_pool_stats(c.handle, *[C.byref(x) for x in v]))
+        return dict(zip(("reserved", "reserved_high", "used", "used_high"), [x.value for x in v]))
 
     def __enter__(self):
         return self

@@ -265,6 +265,21 @@ int beast_prof_launches(beast_ctx* ctx, int64_t* n) {
   return BEAST_OK;
 }
 
+int beast_pool_stats(beast_ctx* ctx, size_t* reserved, size_t* reserved_high, size_t* used, size_t* used_high) {
+  ARG_CHECK(ctx, ctx && reserved && reserved_high && used && used_high, "null argument");
+  cudaMemPool_t pool;
+  BEAST_CUDA_TRY(ctx, cudaDeviceGetDefaultMemPool(&pool, ctx->device));
+  uint64_t v[4] = {0, 0, 0, 0};
+  const cudaMemPoolAttr at[4] = {cudaMemPoolAttrReservedMemCurrent, cudaMemPoolAttrReservedMemHigh,
+                                 cudaMemPoolAttrUsedMemCurrent, cudaMemPoolAttrUsedMemHigh};
+  for (int k = 0; k < 4; ++k) BEAST_CUDA_TRY(ctx, cudaMemPoolGetAttribute(pool, at[k], &v[k]));
+  *reserved = v[0];
+  *reserved_high = v[1];
+  *used = v[2];
+  *used_high = v[3];
+  return BEAST_OK;
+}
+
 int beast_ctx_set_wait_limit(beast_ctx* ctx, int64_t polls) {
   ARG_CHECK(ctx, ctx && polls >= 0, "invalid wait limit");
   ctx->trsv_spin_max = polls;
@@ -883,23 +898,41 @@ static int factor_copy(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, in
   return BEAST_OK;
 }
 
-// core of the dense solve on device vectors (b, x: c128 [n x nrhs], ld n)
-// FP64: partial-pivoting LU in complex FP64 (zgetrf semantics) + one solve.
+// ---- factored systems: the matrix A (as stored) and the factors of its copy F
+// FP64: partial-pivoting LU in complex FP64 (zgetrf semantics) of a c128 copy.
 // MIXED: complex FP32 factorisation (tensor-core trailing updates) of a c64 copy, FP64
 // iterative refinement against A as stored.  Factorisations tried in turn, each taking over
 // when the previous one meets a zero pivot or its refinement diverges or stagnates:
 //   symmetric (LDL^T-type, half the work; only when A is complex symmetric to within 1e-2
 //   in a sampled Frobenius measure -- e.g. a Galerkin EFIE matrix, symmetric up to quadrature),
 //   unpivoted LU, LU with partial pivoting.
-static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dtype,
-                              int precision, const double* b, double* x, int64_t nrhs, double tol,
-                              int maxiter, int* iters, double* resid) {
+struct DenseSystem {
+  int64_t n = 0, lda = 0;
+  const void* A = nullptr;
+  int a_dtype = 0;
+  bool mixed = false;
+  void* F = nullptr;        // factor copy (stream-ordered pool memory)
+  beast_lu* lu = nullptr;
+  int mode = 0;             // 2 symmetric, 1 unpivoted LU, 0 LU with partial pivoting
+};
+
+static void system_release(beast_ctx* ctx, DenseSystem& S) {
+  if (S.lu) beast_lu_free(S.lu);
+  S.lu = nullptr;
+  if (S.F) cudaFreeAsync(S.F, ctx->stream);
+  S.F = nullptr;
+}
+
+// the factor copy of A in mode S.mode (allocated on first use)
+static int system_factor(beast_ctx* ctx, DenseSystem& S) {
   cudaStream_t st = ctx->stream;
-  const bool mixed = precision == BEAST_MIXED;
-  const int fdt = mixed ? BEAST_C64 : BEAST_C128;
-  const size_t fel = mixed ? 8 : 16;
-  void* F = nullptr;
-  {
+  const int64_t n = S.n;
+  const size_t fel = S.mixed ? 8 : 16;
+  if (S.lu) {
+    beast_lu_free(S.lu);
+    S.lu = nullptr;
+  }
+  if (!S.F) {
     // the assembly workspace (kept by the context) and the device pool's freed blocks stay
     // mapped; when the factor copy would not fit next to them, hand them back first (the
     // next assembly grows its workspace again)
@@ -915,35 +948,50 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
       }
       if (cudaDeviceGetDefaultMemPool(&pool, ctx->device) == cudaSuccess) cudaMemPoolTrimTo(pool, 0);
     }
+    BEAST_CUDA_TRY(ctx, cudaMallocAsync(&S.F, (size_t)n * n * fel, st));
   }
-  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&F, (size_t)n * n * fel, st));
+  ctx->last_factor_mode = S.mode;
+  return factor_copy(ctx, n, S.A, S.lda, S.a_dtype, S.F, S.mixed ? BEAST_C64 : BEAST_C128, S.mode == 0, S.mode == 2,
+                     &S.lu);
+}
+
+// factor A: the first mode of the sequence that factors without a zero pivot
+static int system_setup(beast_ctx* ctx, DenseSystem& S, int64_t n, const void* A, int64_t lda, int a_dtype,
+                        bool mixed) {
+  S.n = n;
+  S.lda = lda;
+  S.A = A;
+  S.a_dtype = a_dtype;
+  S.mixed = mixed;
+  S.mode = mixed ? (asym_sample(ctx, n, A, lda, a_dtype) <= 1e-2 ? 2 : 1) : 0;
+  for (;;) {
+    int rc = system_factor(ctx, S);
+    if (rc == BEAST_ERR_SINGULAR && S.mode > 0) {
+      --S.mode;
+      continue;
+    }
+    return rc;
+  }
+}
+
+// x = A \ b for device vectors (b, x: c128 [n x nrhs], ld n) with the factors of S; on the
+// mixed path a refinement that stagnates or diverges moves S to the next factorisation mode
+// and starts over, so the result never depends on a cheaper factorisation being good
+static int system_solve(beast_ctx* ctx, DenseSystem& S, const double* b, double* x, int64_t nrhs, double tol,
+                        int maxiter, int* iters, double* resid) {
+  cudaStream_t st = ctx->stream;
+  const int64_t n = S.n;
   double *r = nullptr, *d = nullptr, *nrm = nullptr;
   float* d32 = nullptr;
   BEAST_CUDA_TRY(ctx, cudaMallocAsync(&r, n * 16, st));
   BEAST_CUDA_TRY(ctx, cudaMallocAsync(&d, n * 16, st));
   BEAST_CUDA_TRY(ctx, cudaMallocAsync(&nrm, 64, st));
-  if (mixed) BEAST_CUDA_TRY(ctx, cudaMallocAsync(&d32, n * 8, st));
+  if (S.mixed) BEAST_CUDA_TRY(ctx, cudaMallocAsync(&d32, n * 8, st));
   int it_max = 0;
   double res_max = 0;
   int rc = BEAST_OK;
-  beast_lu* lu = nullptr;
-  // factorisation modes: 2 symmetric, 1 unpivoted LU, 0 LU with partial pivoting
-  int mode = 0;
-  if (mixed) mode = asym_sample(ctx, n, A, lda, a_dtype) <= 1e-2 ? 2 : 1;
-  ctx->last_factor_mode = mode;
+  ctx->last_factor_mode = S.mode;
   for (;;) {
-    if (lu) {
-      beast_lu_free(lu);
-      lu = nullptr;
-    }
-    const bool pivot = mode == 0;
-    ctx->last_factor_mode = mode;
-    rc = factor_copy(ctx, n, A, lda, a_dtype, F, fdt, pivot, mode == 2, &lu);
-    if (rc == BEAST_ERR_SINGULAR && !pivot) {
-      --mode;
-      continue;
-    }
-    if (rc) break;
     it_max = 0;
     res_max = 0;
     bool retry = false;
@@ -951,14 +999,14 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
       const double* bk = b + 2 * k * n;
       double* xk = x + 2 * k * n;
       double bn = dev_norm(ctx, n, bk, nrm);
-      if (!mixed) {
+      if (!S.mixed) {
         BEAST_CUDA_TRY(ctx, vec_copy(n, bk, xk, st));
-        rc = lu_solve_dev(ctx, n, F, n, BEAST_C128, lu->ipiv, xk, n, 1);
+        rc = lu_solve_dev(ctx, n, S.F, n, BEAST_C128, S.lu->ipiv, xk, n, 1);
         if (rc) break;
         BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
         {
           ProfScope ps(ctx, PK_GEMV, (double)n * n * 16, 2);
-          BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, 0, xk, r, -1.0, 1.0, st));
+          BEAST_CUDA_TRY(ctx, gemv_dev(n, S.A, S.lda, 0, xk, r, -1.0, 1.0, st));
         }
         double rn = dev_norm(ctx, n, r, nrm);
         if ((rc = trsv_check(ctx))) break;
@@ -972,14 +1020,14 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
       int slow = 0;
       while (true) {
         BEAST_CUDA_TRY(ctx, convert_c128_to_c64(n, 1, r, n, d32, n, st));
-        rc = lu_solve_dev(ctx, n, F, n, BEAST_C64, lu->ipiv, d32, n, 1);
+        rc = lu_solve_dev(ctx, n, S.F, n, BEAST_C64, S.lu->ipiv, d32, n, 1);
         if (rc) break;
         BEAST_CUDA_TRY(ctx, convert_c64_to_c128(n, 1, d32, n, d, n, st));
         BEAST_CUDA_TRY(ctx, vec_axpy(n, 1.0, 0.0, d, xk, st));
         BEAST_CUDA_TRY(ctx, vec_copy(n, bk, r, st));
         {
-          ProfScope ps(ctx, PK_GEMV, (double)n * n * (a_dtype == BEAST_C64 ? 8 : 16), 2);
-          BEAST_CUDA_TRY(ctx, gemv_dev(n, A, lda, a_dtype == BEAST_C64, xk, r, -1.0, 1.0, st));
+          ProfScope ps(ctx, PK_GEMV, (double)n * n * (S.a_dtype == BEAST_C64 ? 8 : 16), 2);
+          BEAST_CUDA_TRY(ctx, gemv_dev(n, S.A, S.lda, S.a_dtype == BEAST_C64, xk, r, -1.0, 1.0, st));
         }
         ++it;
         double rn = dev_norm(ctx, n, r, nrm);
@@ -995,12 +1043,22 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
       it_max = std::max(it_max, it);
       res_max = std::isfinite(rel) ? std::max(res_max, rel) : rel;
       if (!(rel <= tol)) {  // also a non-finite residual
-        if (!pivot) retry = true;
+        if (S.mode > 0) retry = true;
         else rc = beast_fail(ctx, BEAST_ERR_NOCONV, "iterative refinement did not reach the tolerance");
       }
     }
     if (retry && rc == BEAST_OK) {
-      --mode;
+      // the next factorisation mode; a zero pivot there moves on again
+      for (;;) {
+        --S.mode;
+        rc = system_factor(ctx, S);
+        if (rc == BEAST_ERR_SINGULAR && S.mode > 0) {
+          rc = BEAST_OK;
+          continue;
+        }
+        break;
+      }
+      if (rc) break;
       continue;
     }
     break;
@@ -1009,11 +1067,20 @@ static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t 
   cudaFreeAsync(d, st);
   cudaFreeAsync(nrm, st);
   if (d32) cudaFreeAsync(d32, st);
-  if (lu) beast_lu_free(lu);
-  cudaFreeAsync(F, st);
-  cudaStreamSynchronize(st);
   if (iters) *iters = it_max;
   if (resid) *resid = res_max;
+  return rc;
+}
+
+// core of the dense solve on device vectors (b, x: c128 [n x nrhs], ld n)
+static int solve_dense_device(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dtype,
+                              int precision, const double* b, double* x, int64_t nrhs, double tol,
+                              int maxiter, int* iters, double* resid) {
+  DenseSystem S;
+  int rc = system_setup(ctx, S, n, A, lda, a_dtype, precision == BEAST_MIXED);
+  if (rc == BEAST_OK) rc = system_solve(ctx, S, b, x, nrhs, tol, maxiter, iters, resid);
+  system_release(ctx, S);
+  cudaStreamSynchronize(ctx->stream);
   return rc;
 }
 
@@ -1153,46 +1220,114 @@ int beast_gmres(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dty
   return BEAST_OK;
 }
 
+}  // extern "C"
+
+// an assembled and factored system kept on the device (beast_system_*)
+struct beast_system {
+  beast_ctx* ctx = nullptr;
+  const beast_space* space = nullptr;
+  int precision = 0;
+  int dtype = 0;
+  void* Z = nullptr;
+  DenseSystem S;
+  size_t bytes = 0;
+};
+
+extern "C" {
+
+int beast_system_create(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs, const beast_space* space,
+                        int local_which, double local_re, double local_im, int precision, beast_system** out) {
+  ARG_CHECK(ctx, ctx && op && qs && space && out, "null argument");
+  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
+            "unknown precision");
+  ARG_CHECK(ctx, local_which >= -1 && local_which <= 1, "local_which must be -1 (none), 0 (Identity) or 1 (NCross)");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  cudaStream_t st = ctx->stream;
+  const int64_t n = space->nfuncs;
+  beast_system* y = new beast_system();
+  y->ctx = ctx;
+  y->space = space;
+  y->precision = precision;
+  y->dtype = precision == BEAST_MIXED ? BEAST_C64 : BEAST_C128;
+  const size_t el = y->dtype == BEAST_C64 ? 8 : 16;
+  cudaError_t e = cudaMallocAsync(&y->Z, (size_t)n * n * el, st);
+  if (e != cudaSuccess) {
+    delete y;
+    return beast_fail(ctx, BEAST_ERR_OOM, "system matrix allocation failed");
+  }
+  int rc = beast_assemble(ctx, op, qs, space, space, precision, y->Z, n, y->dtype, BEAST_DEVICE, 0, 0, 1.0, 0.0, 0);
+  if (rc == BEAST_OK && local_which >= 0)
+    rc = beast_assemble_local(ctx, local_which, space, space, 6, y->Z, n, y->dtype, BEAST_DEVICE, 0, 0, local_re,
+                              local_im);
+  if (rc == BEAST_OK) rc = system_setup(ctx, y->S, n, y->Z, n, y->dtype, precision != BEAST_FP64);
+  if (rc == BEAST_OK) rc = beast_ctx_synchronize(ctx);
+  if (rc) {
+    beast_system_free(y);
+    return rc;
+  }
+  y->bytes = (size_t)n * n * el + (size_t)n * n * (precision == BEAST_FP64 ? 16 : 8) + lu_aux_bytes(n, y->S.mixed ? BEAST_C64 : BEAST_C128);
+  *out = y;
+  return BEAST_OK;
+}
+
+int beast_system_solve(beast_ctx* ctx, beast_system* y, int exc_kind, int64_t nrhs, const double* dirs,
+                       const double* pols, double egr, double egi, double tol, double* x, int x_loc, int* iters,
+                       double* resid) {
+  ARG_CHECK(ctx, ctx && y && dirs && x && nrhs >= 1, "invalid system solve arguments");
+  ARG_CHECK(ctx, y->ctx == ctx, "the system belongs to another context");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  cudaStream_t st = ctx->stream;
+  const int64_t n = y->S.n;
+  double *b = nullptr, *dx = nullptr;
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&b, n * nrhs * 16, st));
+  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&dx, n * nrhs * 16, st));
+  int rc = BEAST_OK;
+  TriRuleDev r;
+  make_trirule(8, &r);
+  for (int64_t k = 0; k < nrhs && rc == BEAST_OK; ++k) {
+    double p3[3] = {0, 0, 0};
+    if (pols) memcpy(p3, pols + 3 * k, sizeof(p3));
+    ProfScope ps(ctx, PK_RHS, (double)n);
+    cudaError_t e = launch_rhs(exc_kind, y->space, dirs + 3 * k, p3, egr, egi, 1.0, 0.0, r, b + 2 * k * n, st);
+    if (e != cudaSuccess) rc = beast_fail(ctx, BEAST_ERR_CUDA, cudaGetErrorString(e));
+  }
+  if (rc == BEAST_OK) rc = system_solve(ctx, y->S, b, dx, nrhs, tol > 0 ? tol : 1e-12, 30, iters, resid);
+  if (rc == BEAST_OK || rc == BEAST_ERR_NOCONV)
+    cudaMemcpyAsync(x, dx, n * nrhs * 16, x_loc == BEAST_DEVICE ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost,
+                    st);
+  cudaFreeAsync(b, st);
+  cudaFreeAsync(dx, st);
+  cudaStreamSynchronize(st);
+  return rc;
+}
+
+int beast_system_bytes(const beast_system* y, size_t* bytes) {
+  if (!y || !bytes) return BEAST_ERR_ARG;
+  *bytes = y->bytes;
+  return BEAST_OK;
+}
+
+int beast_system_free(beast_system* y) {
+  if (!y) return BEAST_OK;
+  beast_ctx* ctx = y->ctx;
+  cudaSetDevice(ctx->device);
+  system_release(ctx, y->S);
+  if (y->Z) cudaFreeAsync(y->Z, ctx->stream);
+  cudaStreamSynchronize(ctx->stream);
+  delete y;
+  return BEAST_OK;
+}
+
 int beast_solve_job(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs,
                     const beast_space* space, int exc_kind, const double* dir, const double* pol,
                     double egr, double egi, int precision, double tol, double* x, int x_loc,
                     int* iters, double* resid) {
   ARG_CHECK(ctx, ctx && op && qs && space && dir && x, "null argument");
-  if (set_device(ctx)) return BEAST_ERR_CUDA;
-  cudaStream_t st = ctx->stream;
-  const int64_t n = space->nfuncs;
-  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
-            "unknown precision");
-  const int dt = precision == BEAST_MIXED ? BEAST_C64 : BEAST_C128;
-  const int solve_prec = precision == BEAST_MIXED_ACCURATE ? BEAST_MIXED : precision;
-  const size_t el = dt == BEAST_C64 ? 8 : 16;
-  void* Z = nullptr;
-  double *b = nullptr, *dx = nullptr;
-  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&Z, (size_t)n * n * el, st));
-  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&b, n * 16, st));
-  BEAST_CUDA_TRY(ctx, cudaMallocAsync(&dx, n * 16, st));
-  int rc = beast_assemble(ctx, op, qs, space, space, precision, Z, n, dt, BEAST_DEVICE, 0, 0, 1.0, 0.0, 0);
-  if (rc == BEAST_OK) {
-    double p3[3] = {0, 0, 0};
-    if (pol) memcpy(p3, pol, sizeof(p3));
-    TriRuleDev r;
-    make_trirule(8, &r);
-    ProfScope ps(ctx, PK_RHS, (double)n);
-    cudaError_t e = launch_rhs(exc_kind, space, dir, p3, egr, egi, 1.0, 0.0, r, b, st);
-    if (e != cudaSuccess) rc = beast_fail(ctx, BEAST_ERR_CUDA, cudaGetErrorString(e));
-  }
-  if (rc == BEAST_OK)
-    rc = solve_dense_device(ctx, n, Z, n, dt, solve_prec, b, dx, 1, tol > 0 ? tol : 1e-12, 30, iters, resid);
-  if (rc == BEAST_OK || rc == BEAST_ERR_NOCONV) {
-    if (x_loc == BEAST_DEVICE)
-      cudaMemcpyAsync(x, dx, n * 16, cudaMemcpyDeviceToDevice, st);
-    else
-      cudaMemcpyAsync(x, dx, n * 16, cudaMemcpyDeviceToHost, st);
-  }
-  cudaFreeAsync(Z, st);
-  cudaFreeAsync(b, st);
-  cudaFreeAsync(dx, st);
-  cudaStreamSynchronize(st);
+  beast_system* y = nullptr;
+  int rc = beast_system_create(ctx, op, qs, space, -1, 0.0, 0.0, precision, &y);
+  if (rc) return rc;
+  rc = beast_system_solve(ctx, y, exc_kind, 1, dir, pol, egr, egi, tol, x, x_loc, iters, resid);
+  beast_system_free(y);
   return rc;
 }
 

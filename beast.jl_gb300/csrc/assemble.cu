@@ -968,8 +968,19 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
                                   P.op.kind == BEAST_HH_DLT);
   if (np_.cls == 4) {
     // ---- DoubleNumQStrat pair close to its partner: the pair's own DoubleQuadRule
-    // (src/quadrature/doublenumints.jl:12-43) point by point in FP64, lanes over point pairs
-    const int no = P.ro.n, ni = P.ri.n;
+    // (src/quadrature/doublenumints.jl:12-43) point by point in FP64, lanes over point pairs.
+    // Double-layer type kernels vanish identically on a common face (every vector of the
+    // triple product lies in the flat triangle): that block stays 0 rather than summed noise.
+    const bool dl_kind = P.op.kind == BEAST_MW_DL || P.op.kind == BEAST_MW_NXDL || P.op.kind == BEAST_HH_DL ||
+                         P.op.kind == BEAST_HH_DLT;
+    int hits = 0;
+    if (dl_kind)
+      for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) {
+          const V3<double> dd = t.v[i] - s.v[j];
+          hits += sqrt(dot(dd, dd)) < 1.0e3 * 2.220446049250313e-16;
+        }
+    const int no = P.ro.n, ni = (dl_kind && hits == 3) ? 0 : P.ri.n;
     for (int it = lane; it < no * ni; it += 32) {
       const int a = it / ni, b = it % ni;
       double bx[3] = {P.ro.u[a], P.ro.v[a], 1.0 - P.ro.u[a] - P.ro.v[a]};

@@ -57,6 +57,8 @@ def parse():
                     help="skip the plain FP64 solve (its solves/s and the accuracy figures)")
     ap.add_argument("--no-mfie", action="store_true", help="skip the MFIE leg")
     ap.add_argument("--no-modes", action="store_true", help="skip the other mixed mode")
+    ap.add_argument("--no-serving", action="store_true",
+                    help="skip the short request stream (40 C5 requests at 8/s) of the default line")
     ap.add_argument("--tol", type=float, default=1e-10)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -401,19 +403,26 @@ def run_c3(args):
 
 
 def run_c5(args):
+    print(json.dumps(serve_stream(args)))
+
+
+def serve_stream(args, requests=None, rate=None):
     """a Poisson stream (--rate per second, --requests requests) of solve requests: operator
     U{EFIE, MFIE (n x K - Id/2), Helmholtz SL}, icosphere level U{3, 4, 5}, k U[1, 12], 1-8 plane
-    waves; served by --workers contexts in arrival order; latency = completion - arrival"""
+    waves; served by --workers contexts in arrival order, meshes and spaces resident per slot;
+    latency = completion - arrival"""
     import torch
     import beastgpu as bg
+    requests = requests or args.requests
+    rate = rate or args.rate
     rng = np.random.default_rng(7)
     meshes = {lv: bg.icosphere(lv) for lv in (3, 4, 5)}
     rt = {lv: bg.raviartthomas(meshes[lv]) for lv in meshes}
     p0 = {lv: bg.lagrangecxd0(meshes[lv]) for lv in meshes}
     reqs = []
     t = 0.0
-    for i in range(args.requests):
-        t += rng.exponential(1.0 / args.rate)
+    for i in range(requests):
+        t += rng.exponential(1.0 / rate)
         kind = ["efie", "mfie", "hh"][int(rng.integers(3))]
         lv = int(rng.integers(3, 6))
         k = float(rng.uniform(1.0, 12.0))
@@ -433,7 +442,7 @@ def run_c5(args):
                    "local": None if kind == "efie" else (0, -0.5)}
         job.update({"arrival": t, "kind": kind, "level": lv})
         reqs.append(job)
-    srv = bg.Server(slots=args.workers)
+    srv = bg.Server(slots=args.workers, resident=3)
     for f in [srv.submit(reqs[0]) for _ in range(args.workers)]:  # warm-up: one job per context
         f.result()
     torch.cuda.synchronize()
@@ -457,16 +466,24 @@ def run_c5(args):
     srv.drain()
     dt = time.perf_counter() - t0
     srv.close()
+    pool = srv.pool_stats()
     ms = np.array(lat) * 1e3
-    print(json.dumps({"metric": "latency_ms", "p50": float(np.percentile(ms, 50)),
-                      "p99": float(np.percentile(ms, 99)), "max": float(ms.max()), "unit": "ms",
-                      "higher_is_better": False, "throughput_rps": len(reqs) / dt, "config": {
-                          "workload": "C5: Poisson stream of EFIE / MFIE / Helmholtz-SL solve requests",
-                          "rate_per_s": args.rate, "requests": args.requests, "workers": args.workers,
-                          "levels": [3, 4, 5], "rhs_per_request": "1-8", "precision": "mixed",
-                          "request": "mesh + space upload, assembly, excitations, solve, solution to host",
-                          "admission": "beastgpu.serve.Server: arrival order, a free slot and HBM footprint"},
-                      "data": "synthetic seeded request stream"}))
+    kinds = [r["kind"] for r in reqs]
+    return {"metric": "latency_ms", "p50": float(np.percentile(ms, 50)),
+            "p99": float(np.percentile(ms, 99)), "max": float(ms.max()), "unit": "ms",
+            "higher_is_better": False, "throughput_rps": len(reqs) / dt,
+            "solves_per_s": sum(len(r["waves"]) for r in reqs) / dt,
+            "peak_admitted_bytes": int(srv.peak_bytes), "budget_bytes": int(srv.budget),
+            "pool_reserved_high_bytes": int(pool["reserved_high"]) if pool else None,
+            "config": {
+                "workload": "C5: Poisson stream of EFIE / MFIE / Helmholtz-SL solve requests",
+                "rate_per_s": rate, "requests": requests, "workers": args.workers,
+                "mix": {k: kinds.count(k) for k in sorted(set(kinds))},
+                "levels": [3, 4, 5], "rhs_per_request": "1-8", "precision": "mixed",
+                "request": "assembly, excitations, factorisation, solve, solution to host (meshes and spaces "
+                           "resident per slot)",
+                "admission": "beastgpu.serve.Server: arrival order, a free slot and HBM footprint"},
+            "data": "synthetic seeded request stream"}
 
 
 class Problem:
@@ -771,6 +788,9 @@ def run_c2(args):
            "modes": modes, "mfie": mfie_out,
            "roofline": roof, "kernel_breakdown": breakdown, "gpu_launches": int(launches),
            "clocks": clocks, "e2e": e2e}
+    if not args.no_serving:
+        torch.cuda.empty_cache()
+        out["serving"] = serve_stream(args, requests=40, rate=8.0)
     if not args.no_cpu_baseline:
         out["cpu_baseline"] = cpu_baseline(args, X, m)
     print(json.dumps(out))

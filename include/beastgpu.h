@@ -88,6 +88,7 @@ typedef struct beast_ctx beast_ctx;
 typedef struct beast_mesh beast_mesh;
 typedef struct beast_space beast_space;
 typedef struct beast_lu beast_lu;
+typedef struct beast_system beast_system;
 
 /* operator parameters: MW_SL uses gamma, alpha, beta; MW_DL / MW_NXDL use gamma (alpha is
  * carried but, as in the reference integrands, not applied); HH_* use gamma and alpha. */
@@ -241,6 +242,26 @@ int beast_solve_job(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc
                     double exc_gamma_re, double exc_gamma_im, int precision, double tol,
                     double* x, int x_loc, int* iters, double* resid);
 
+/* ---- resident systems: the `solve(eq)` path split so that the matrix and its factors stay
+ * on the device between requests (serving: a request on a system already resident skips
+ * assembly and factorisation; src/solvers/lusolver.jl:9-39 assembles and factors per call).
+ * beast_system_create assembles op (+ local_coeff * Identity / NCross when local_which is 0 /
+ * 1; -1: none) on space x space in `precision` and factors it (the mixed factorisation for
+ * BEAST_MIXED / BEAST_MIXED_ACCURATE, FP64 LU for BEAST_FP64).  beast_system_solve builds nrhs
+ * plane-wave excitations (dirs, pols: [nrhs][3]; same gamma) and solves them against the
+ * kept factors (FP64 refinement to `tol` on the mixed paths); x: complex FP64 [nrhs][nfuncs],
+ * location x_loc.  beast_system_bytes: device memory the system holds (matrix, factors,
+ * pivots).  The space must outlive the system.  No reference counterpart for the handle. */
+int beast_system_create(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs,
+                        const beast_space* space, int local_which, double local_coeff_re,
+                        double local_coeff_im, int precision, beast_system** out);
+int beast_system_solve(beast_ctx* ctx, beast_system* sys, int exc_kind, int64_t nrhs,
+                       const double* dirs, const double* pols, double exc_gamma_re,
+                       double exc_gamma_im, double tol, double* x, int x_loc, int* iters,
+                       double* resid);
+int beast_system_bytes(const beast_system* sys, size_t* bytes);
+int beast_system_free(beast_system* sys);
+
 /* ---- instrumentation (no reference counterpart: the reference has no device) ---------
  * When enabled, every instrumented kernel launch on the context stream is bracketed by
  * CUDA events.  Kinds: 0 geometry, 1 far pairs, 2 near pairs, 3 gather/scatter, 4 local
@@ -259,6 +280,13 @@ int beast_prof_launches(beast_ctx* ctx, int64_t* n);
  * this context: 0 LU with partial pivoting, 1 unpivoted LU (mixed), 2 symmetric LDL^T-type
  * (mixed, near complex-symmetric matrix), -1 none yet */
 int beast_last_factor_mode(beast_ctx* ctx, int* mode);
+
+/* the device's stream-ordered memory pool that every allocation of the library's calls comes
+ * from: bytes reserved from the device and bytes in use, now and at their highest (since the
+ * process started).  Serving admission reads it to check that its footprint model bounds the
+ * device memory actually held.  No reference counterpart. */
+int beast_pool_stats(beast_ctx* ctx, size_t* reserved, size_t* reserved_high, size_t* used,
+                     size_t* used_high);
 
 /* library version string */
 const char* beast_version(void);

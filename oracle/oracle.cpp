@@ -926,6 +926,16 @@ int classify(const Op& op, const orc_qs& qs, const Tri& t, const Tri& s) {
 
 void pair_block(const Op& op, const orc_qs& qs, int tk, int bk, const Tri& t, const Tri& s, cplx* z) {
   int c = classify(op, qs, t, s);
+  // DoubleNumQStrat on a common face: the double-layer type kernels vanish identically there
+  // (as in ss_block); the plain rule would only sum rounding noise
+  if (qs.kind == ORC_QS_DOUBLENUM &&
+      (op.kind == ORC_MW_DL || op.kind == ORC_MW_NXDL || op.kind == ORC_HH_DL || op.kind == ORC_HH_DLT)) {
+    const double dtol = 1.0e3 * 2.220446049250313e-16;
+    int hits = 0;
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j) hits += norm(t.v[i] - s.v[j]) < dtol;
+    if (hits == 3) return;
+  }
   int outer_far = qs.outer_far, inner_far = qs.inner_far;
   if (c == 3)
     ss_block(op, tk, bk, t, s, ORC_RULE_SS_FACE, qs.ss_face, z);

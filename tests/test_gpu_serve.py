@@ -44,3 +44,73 @@ def test_each_result_is_the_same_alone_and_in_the_mix():
         assert xa.shape == (len(j["waves"]), j["space"].numfunctions())
         assert ra <= 1e-10 and rm <= 1e-10
         assert np.linalg.norm(xm - xa) / np.linalg.norm(xa) <= 1e-12
+
+
+def test_resident_system_solves_like_a_fresh_job():
+    """beast_system_*: assemble + factor once, solve twice with different plane waves; each
+    solve equals the one-shot job (beast_solve_job) on the same wave"""
+    import ctypes as C
+    ctx = bg.Context(0)
+    m = bg.icosphere(2)
+    X = bg.raviartthomas(m)
+    op = bg.Maxwell3D.singlelayer(wavenumber=3.0)
+    od, qd = bg.api._op_desc(op), bg.api._qs_desc(bg.defaultquadstrat(op, X, X))
+    sh = ctx.space_handle(X)
+    h = C.c_void_p()
+    ctx.check(ctx.lib.beast_system_create(ctx.handle, C.byref(od), C.byref(qd), sh, -1, 0.0, 0.0, bg.MIXED,
+                                          C.byref(h)))
+    nb = C.c_size_t(0)
+    ctx.check(ctx.lib.beast_system_bytes(h, C.byref(nb)))
+    n = X.numfunctions()
+    assert nb.value >= n * n * 16
+    rng = np.random.default_rng(8)
+    try:
+        for _ in range(2):
+            d = rng.normal(size=3)
+            d /= np.linalg.norm(d)
+            p = np.cross(d, rng.normal(size=3))
+            p /= np.linalg.norm(p)
+            dirs, pols = np.ascontiguousarray([d]), np.ascontiguousarray([p])
+            x = np.zeros(n, np.complex128)
+            it, res = C.c_int(0), C.c_double(0)
+            ctx.check(ctx.lib.beast_system_solve(ctx.handle, h, 0, 1, dirs.ctypes.data, pols.ctypes.data, 0.0, 3.0,
+                                                 1e-10, x.ctypes.data, bg.lib.HOST, C.byref(it), C.byref(res)))
+            E = bg.Maxwell3D.planewave(tuple(d), tuple(p), 3.0)
+            xo, _, _ = bg.solve_job(op, X, bg.tangential_trace(E), precision=bg.MIXED, tol=1e-10, ctx=ctx)
+            assert res.value <= 1e-10
+            assert np.linalg.norm(x - xo) / np.linalg.norm(xo) <= 1e-12
+    finally:
+        ctx.lib.beast_system_free(h)
+        ctx.close()
+
+
+def test_server_keeps_systems_resident():
+    """a second request on the same system (new right-hand sides) reuses the factored system
+    kept by the slot; its answer equals the one without residency, and the admitted
+    footprints plus the resident systems stay within the budget"""
+    jobs = _jobs()[:3]
+    rng = np.random.default_rng(9)
+    again = []
+    for j in jobs:  # the same systems, other plane waves of the same wavenumber
+        k = abs(complex(j["waves"][0].gamma))
+        d = rng.normal(size=3)
+        d /= np.linalg.norm(d)
+        if j.get("local") is None and j["space"].refspace_nshapes() == 1:
+            w = [bg.Helmholtz3D.planewave(tuple(d), wavenumber=k)]
+        else:
+            p = np.cross(d, rng.normal(size=3))
+            w = [bg.Maxwell3D.planewave(tuple(d), tuple(p / np.linalg.norm(p)), k)]
+        again.append(dict(j, waves=w))
+    with bg.Server(slots=1, hbm_budget=16 << 30) as s:
+        ref = [s.submit(j).result(timeout=600) for j in again]
+    with bg.Server(slots=2, hbm_budget=16 << 30, resident_systems=4) as s:
+        for f in [s.submit(j) for j in jobs]:
+            f.result(timeout=600)
+        created = sum(c.systems.created for c in s._ctxs)
+        got = [s.submit(j).result(timeout=600) for j in again]
+        assert sum(c.systems.created for c in s._ctxs) == created  # no new system
+        assert s.peak_bytes <= s.budget
+        pool = s.pool_stats()
+        assert pool["reserved_high"] <= s.budget + (2 << 30)
+    for (x, _, _), (xr, _, _) in zip(got, ref):
+        assert np.linalg.norm(x - xr) / np.linalg.norm(xr) <= 1e-12

@@ -166,3 +166,59 @@ def test_resident_spaces_keep_the_last_used_meshes():
     assert ctx.lib.uploads == 4 and len(res.entries) == 2
     res.close()
     assert not ctx.lib.live
+
+
+class Held:
+    """stand-in for a slot's ResidentSystems: keys with their bytes"""
+
+    def __init__(self):
+        self.entries = {}
+
+    def __contains__(self, k):
+        return k in self.entries
+
+    @property
+    def bytes(self):
+        return sum(self.entries.values())
+
+    def evict_oldest(self):
+        if not self.entries:
+            return False
+        self.entries.pop(next(iter(self.entries)))
+        return True
+
+    def close(self):
+        self.entries.clear()
+
+
+class HeldCtx:
+    def __init__(self):
+        self.systems = Held()
+
+
+def test_resident_systems_count_in_admission_and_are_evicted_for_room():
+    """a slot's resident systems count against the budget; a job that only fits without them
+    evicts them from idle slots; a job on a resident system is routed to its slot and admitted
+    with the small footprint of a solve"""
+    runs = []
+
+    def runner(ctx, job):
+        runs.append((job["name"], id(ctx)))
+        ctx.systems.entries[job["key"]] = job["keep"]  # the job leaves its system resident
+        return job["name"]
+
+    s = Server(slots=2, hbm_budget=100, make_context=HeldCtx, runner=runner, footprint=lambda j: j["fp"],
+               key=lambda j: j["key"])
+    s._resident_footprint = lambda j: 1
+    try:
+        assert s.submit({"name": "a", "fp": 50, "key": "A", "keep": 40}).result(timeout=10) == "a"
+        assert sum(s._held) == 40
+        # on A's system again: its slot, small footprint
+        assert s.submit({"name": "a2", "fp": 50, "key": "A", "keep": 40}).result(timeout=10) == "a2"
+        assert runs[1][1] == runs[0][1]
+        # 70 does not fit beside the 40 held: the idle slot's system is evicted
+        assert s.submit({"name": "b", "fp": 70, "key": "B", "keep": 10}).result(timeout=10) == "b"
+        assert "A" not in [k for c in s._ctxs for k in c.systems.entries]
+        assert s.peak_bytes <= 100
+    finally:
+        s.close()
