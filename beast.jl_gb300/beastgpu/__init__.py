@@ -14,6 +14,7 @@ from .operators import (Maxwell3D, Helmholtz3D, nxdoublelayer, Identity, NCross,
 from .api import (Context, get_context, assemble, assemble_rhs, solve, gmres, farfield,
                   solve_job, blockassembler, assemblerow, assemblecol)
 from .serve import Server, run_job, job_footprint
+from .batch import Batch
 from .refine import barycentric_refinement, buffachristiansen, refined
 from . import tune
 

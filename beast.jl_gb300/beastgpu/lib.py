@@ -45,6 +45,7 @@ EXPORTS = [
     "beast_assemble_block", "beast_assemble_local", "beast_rhs_planewave", "beast_lu_factor", "beast_lu_solve",
     "beast_lu_free", "beast_lu_solve_noalloc", "beast_solve_dense", "beast_gmres", "beast_farfield", "beast_solve_job",
     "beast_system_create", "beast_system_solve", "beast_system_bytes", "beast_system_free", "beast_pool_stats",
+    "beast_batch_create", "beast_batch_assemble", "beast_batch_free",
     "beast_prof_enable", "beast_prof_enable_kinds", "beast_prof_read", "beast_prof_launches", "beast_last_factor_mode", "beast_version",
 ]
 
@@ -98,6 +99,9 @@ def load(build_if_needed=True):
     L.beast_system_bytes.argtypes = [vp, C.POINTER(C.c_size_t)]
     L.beast_system_free.argtypes = [vp]
     L.beast_pool_stats.argtypes = [vp] + [C.POINTER(C.c_size_t)] * 4
+    L.beast_batch_create.argtypes = [vp, C.POINTER(QsDesc), i64, vp, vp, vp, i, i, i, i, pp]
+    L.beast_batch_assemble.argtypes = [vp, vp]
+    L.beast_batch_free.argtypes = [vp]
     L.beast_prof_enable.argtypes = [vp, i]
     L.beast_prof_read.argtypes = [vp, i, C.POINTER(C.c_double), C.POINTER(C.c_int64),
                                   C.POINTER(C.c_double)]

@@ -1,4 +1,5 @@
-"""Home-grown autotuner for the dense solve's tuning switches.
+"""Home-grown autotuners: the dense solve's tuning switches, and the batched assembly's tile
+shape and tile order.
 
 The factorisation reads its block widths and lookahead from the environment at every call
 (`BEAST_LU_NB`, `BEAST_LU_NB2`, `BEAST_LU_LOOKAHEAD`).  `autotune(n)` times
@@ -10,7 +11,13 @@ tuned setting without timing again.
     import beastgpu as bg
     best = bg.tune.autotune(30720)        # {'BEAST_LU_NB': '1024', 'BEAST_LU_NB2': '256', ...}
 
-The timer is replaceable: the tests drive the search, the cache and the apply step on the CPU.
+`autotune_batch(ops, spaces, precision)` times the batched assembly (beastgpu.batch) of the
+given jobs under each candidate tile shape (test cells x trial cells per CTA step) and tile
+order ("pair bucketing": job by job, largest jobs first, jobs interleaved) and caches the
+fastest per GPU model and batch signature (operator kind, precision, job count, size classes).
+
+The timers are replaceable: the tests drive the searches, the caches and the apply step on
+the CPU.
 """
 import json
 import math
@@ -117,4 +124,68 @@ def autotune(n, timer=None, candidates=None, cache_path=None, device=0, key=None
         os.replace(tmp, cache_path)
     if apply:
         os.environ.update(entry["params"])
+    return entry
+
+
+# candidate batched-assembly schedules: (test cells per CTA, trial cells staged per CTA, order)
+BATCH_CANDIDATES = [(tm, tq, order) for tm in (64, 128, 256) for tq in (8, 16, 32)
+                    for order in ("largest_first", "interleaved", "job")]
+
+
+def batch_signature(ops, spaces, precision):
+    """what a tuned batch schedule is keyed by: operator kind, precision, job count and the
+    histogram of size classes"""
+    classes = {}
+    for s in spaces:
+        c = size_class(s.numfunctions())
+        classes[c] = classes.get(c, 0) + 1
+    return f"k{ops[0].kind}|p{precision}|n{len(spaces)}|" + ",".join(f"{c}:{k}" for c, k in sorted(classes.items()))
+
+
+def batch_timer(ops, spaces, precision, device=0, repeats=3):
+    """(tile_m, tile_q, order) -> seconds of the fastest of `repeats` graph replays of the
+    batched assembly (after the capturing call)"""
+    import torch
+    from .batch import Batch
+
+    def timer(cand):
+        tm, tq, order = cand
+        b = Batch(ops, spaces, precision=precision, tile_m=tm, tile_q=tq, order=order)
+        try:
+            b.assemble()
+            best = float("inf")
+            for _ in range(repeats):
+                torch.cuda.synchronize(device)
+                t0 = time.perf_counter()
+                b.assemble()
+                torch.cuda.synchronize(device)
+                best = min(best, time.perf_counter() - t0)
+            return best
+        finally:
+            b.close()
+    return timer
+
+
+def autotune_batch(ops, spaces, precision, timer=None, candidates=None, cache_path=None, device=0, key=None,
+                   force=False):
+    """the fastest batched-assembly schedule for these jobs (from the cache when present):
+    {"tile_m", "tile_q", "order", "times"}"""
+    candidates = candidates or BATCH_CANDIDATES
+    cache_path = cache_path or default_cache_path()
+    key = key or f"{device_key(device)}|batch|{batch_signature(ops, spaces, precision)}"
+    cache = _load(cache_path)
+    entry = cache.get(key)
+    if entry is None or force:
+        timer = timer or batch_timer(ops, spaces, precision, device)
+        times = [float(timer(tuple(c))) for c in candidates]
+        best = min(range(len(candidates)), key=lambda i: times[i])
+        tm, tq, order = candidates[best]
+        entry = {"tile_m": int(tm), "tile_q": int(tq), "order": order,
+                 "times": {f"{c[0]}x{c[1]}:{c[2]}": t for c, t in zip(candidates, times)}}
+        cache[key] = entry
+        os.makedirs(os.path.dirname(os.path.abspath(cache_path)), exist_ok=True)
+        tmp = cache_path + ".tmp"
+        with open(tmp, "w") as fh:
+            json.dump(cache, fh, indent=1, sort_keys=True)
+        os.replace(tmp, cache_path)
     return entry

@@ -418,6 +418,20 @@ int beast_space_upload(beast_ctx* ctx, const beast_mesh* mesh, int kind, int64_t
     for (int64_t i = 0; i < ncells; ++i) pos[perm[i]] = (int)i;
     up((void**)&s->tperm, perm.data(), sizeof(int) * ncells);
     up((void**)&s->tpos, pos.data(), sizeof(int) * ncells);
+    // the entry of each (active cell, shape), and by Zcell position for the far kernels
+    s->h_cs2e.assign(ncells * nshapes, -1);
+    s->injective = true;
+    for (int64_t f = 0; f < (int64_t)s->h_fn_cell.size(); ++f) {
+      int& slot = s->h_cs2e[(int64_t)s->h_fn_cell[f] * nshapes + s->h_fn_shape[f]];
+      if (slot >= 0) s->injective = false;
+      slot = (int)f;
+    }
+    if (s->injective) {
+      std::vector<int> zr(ncells * nshapes);
+      for (int64_t i = 0; i < ncells; ++i)
+        for (int r = 0; r < nshapes; ++r) zr[i * nshapes + r] = s->h_cs2e[(int64_t)perm[i] * nshapes + r];
+      up((void**)&s->zrow_entry, zr.data(), sizeof(int) * zr.size());
+    }
   }
   if (e == cudaSuccess) e = cudaMalloc(&s->geo, sizeof(double) * GEO_STRIDE * ncells);
   if (e == cudaSuccess) e = cudaMalloc(&s->geof, sizeof(float) * 4 * ncells);
@@ -436,7 +450,7 @@ int beast_space_free(beast_space* s) {
   cudaSetDevice(s->ctx->device);
   cudaStreamSynchronize(s->ctx->stream);
   void* ptrs[] = {s->cells, s->cell2act, s->ad_dof, s->ad_coeff, s->geo, s->geof,
-                  s->fn_ptr, s->fn_cell, s->fn_shape, s->fn_coeff, s->tperm, s->tpos};
+                  s->fn_ptr, s->fn_cell, s->fn_shape, s->fn_coeff, s->tperm, s->tpos, s->zrow_entry};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete s;
@@ -452,7 +466,15 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
                            double ci, int accumulate) {
   cudaStream_t st = ctx->stream;
   const int nst = ts->kind == BEAST_P0 ? 1 : 3, nsb = bs->kind == BEAST_P0 ? 1 : 3;
-  const int64_t ldc = (int64_t)nst * ts->ncells;
+  // cell-pair blocks laid out by function entries when both spaces allow it (the gather then
+  // reads each function's rows and columns as contiguous runs); else by cells.
+  // BEAST_ZCELL_LAYOUT=cell forces the cell layout.
+  bool entry_layout = ts->injective && bs->injective;
+  {
+    const char* ev = getenv("BEAST_ZCELL_LAYOUT");
+    if (ev && ev[0] == 'c') entry_layout = false;
+  }
+  const int64_t ldc = entry_layout ? ts->h_fn_ptr[ts->nfuncs] : (int64_t)nst * ts->ncells;
   const int zfmt = precision == BEAST_MIXED ? ZCELL_C64 : precision == BEAST_MIXED_ACCURATE ? ZCELL_DF : ZCELL_C128;
   const size_t elem = zfmt == ZCELL_C64 ? 8 : 16;
   // rules
@@ -513,7 +535,7 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
   for (auto& c : chunks) maxq = std::max<int64_t>(maxq, (int64_t)c.cells.size());
   size_t zbytes = align256((size_t)ldc * nsb * maxq * elem);
   size_t need = zbytes + align256(near_cap * sizeof(NearPair)) + align256(sizeof(int) * maxq) +
-                align256(sizeof(int) * bs->ncells) + 256;
+                align256(sizeof(int) * bs->ncells) + 256 + align256(sizeof(int) * nsb * maxq);
   int rc = ws_reserve(ctx, need);
   if (rc) return rc;
   char* w = (char*)ctx->ws;
@@ -522,10 +544,23 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
   int* qcells_d = (int*)((char*)nearl + align256(near_cap * sizeof(NearPair)));
   int* qlocal_d = (int*)((char*)qcells_d + align256(sizeof(int) * maxq));
   int* counter = (int*)((char*)qlocal_d + align256(sizeof(int) * bs->ncells));
+  int* zcol_d = (int*)((char*)counter + 256);
   BEAST_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_flag, 0, 64, st));
-  std::vector<int> ql(bs->ncells, -1);
+  std::vector<int> ql(bs->ncells, -1), zcol_h;
   for (auto& ch : chunks) {
     for (size_t i = 0; i < ch.cells.size(); ++i) ql[ch.cells[i]] = (int)i;
+    // entry layout: the Zcell column of each (chunk cell, shape) -- its entry relative to the
+    // chunk's first, -1 for an entry of a function outside the chunk
+    const int64_t f0 = bs->h_fn_ptr[ch.n0], f1 = bs->h_fn_ptr[ch.n1];
+    if (entry_layout) {
+      zcol_h.assign(ch.cells.size() * nsb, -1);
+      for (size_t i = 0; i < ch.cells.size(); ++i)
+        for (int j = 0; j < nsb; ++j) {
+          const int e = bs->h_cs2e[(int64_t)ch.cells[i] * nsb + j];
+          if (e >= f0 && e < f1) zcol_h[i * nsb + j] = (int)(e - f0);
+        }
+      BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(zcol_d, zcol_h.data(), sizeof(int) * zcol_h.size(), cudaMemcpyHostToDevice, st));
+    }
     BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(qcells_d, ch.cells.data(), sizeof(int) * ch.cells.size(), cudaMemcpyHostToDevice, st));
     BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(qlocal_d, ql.data(), sizeof(int) * bs->ncells, cudaMemcpyHostToDevice, st));
     BEAST_CUDA_TRY(ctx, cudaMemsetAsync(counter, 0, sizeof(int), st));
@@ -544,6 +579,8 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
     a.near_cap = (int)near_cap;
     a.near_count = counter;
     a.flag = ctx->d_flag;
+    a.zrow = entry_layout ? ts->zrow_entry : nullptr;
+    a.zcol = entry_layout ? zcol_d : nullptr;
     cudaError_t e;
     {
       // algorithmic work: far pairs x flops per pair (EFIE 1200, MFIE 2040, n x K 29600,
@@ -582,6 +619,8 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
     g.cr = cr;
     g.ci = ci;
     g.accumulate = accumulate;
+    g.entry_layout = entry_layout ? 1 : 0;
+    g.f0 = f0;
     {
       // bytes: Zcell chunk read once + output block written (read too when accumulating)
       double by = (double)ldc * nsb * ch.cells.size() * elem +
@@ -1222,6 +1261,18 @@ int beast_gmres(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int a_dty
 
 }  // extern "C"
 
+// a batch of P0 jobs assembled by one persistent launch (beast_batch_*)
+struct beast_batch {
+  beast_ctx* ctx = nullptr;
+  BatchLaunch L;
+  BatchJobDev* jobs = nullptr;
+  BatchTile* tiles = nullptr;
+  NearPairB* near = nullptr;
+  int* counter = nullptr;  // [0] near-pair count, [1] status
+  std::vector<void*> zcols;  // the jobs' column maps
+  cudaGraphExec_t exec = nullptr;
+};
+
 // an assembled and factored system kept on the device (beast_system_*)
 struct beast_system {
   beast_ctx* ctx = nullptr;
@@ -1315,6 +1366,174 @@ int beast_system_free(beast_system* y) {
   if (y->Z) cudaFreeAsync(y->Z, ctx->stream);
   cudaStreamSynchronize(ctx->stream);
   delete y;
+  return BEAST_OK;
+}
+
+int beast_batch_create(beast_ctx* ctx, const beast_qs_desc* qs, int64_t njobs, const beast_space* const* spaces,
+                       const beast_op_desc* ops, void* const* Z, int precision, int tile_m, int tile_q, int order,
+                       beast_batch** out) {
+  ARG_CHECK(ctx, ctx && qs && spaces && ops && Z && out && njobs > 0, "null argument");
+  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
+            "unknown precision");
+  ARG_CHECK(ctx, order >= 0 && order <= 2, "order must be 0, 1 or 2");
+  if (tile_m <= 0) tile_m = 128;
+  if (tile_q <= 0) tile_q = 16;
+  ARG_CHECK(ctx, tile_m <= 1024 && tile_q <= 256, "tile shape out of range");
+  const int kind = ops[0].kind;
+  ARG_CHECK(ctx, kind == BEAST_HH_SL || kind == BEAST_HH_DLT,
+            "batched assembly: Helmholtz single layer or transposed double layer");
+  for (int64_t j = 0; j < njobs; ++j) {
+    const beast_space* s = spaces[j];
+    ARG_CHECK(ctx, s && Z[j] && ops[j].kind == kind, "every job needs a space, a matrix and the batch's operator");
+    ARG_CHECK(ctx, s->kind == BEAST_P0 && s->injective && s->maxfn == 1 &&
+                       (int64_t)s->h_fn_cell.size() == s->ncells && s->nfuncs == s->ncells,
+              "batched assembly: P0 spaces with one function per cell");
+    for (double c : s->h_fn_coeff) ARG_CHECK(ctx, c == 1.0, "batched assembly: P0 coefficients must be 1");
+  }
+  TriRuleDev ro, ri, ron, rin;
+  ARG_CHECK(ctx, make_trirule(qs->outer_far, &ro) && make_trirule(qs->inner_far, &ri), "far rule degree not available");
+  if (qs->kind == BEAST_QS_WILTON_SAUTER) {
+    ARG_CHECK(ctx, make_trirule(qs->outer_near, &ron) && make_trirule(qs->inner_near, &rin), "near rule degree not available");
+  } else {
+    ron = ro;
+    rin = ri;
+  }
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  beast_batch* b = new beast_batch();
+  b->ctx = ctx;
+  // job table and zcol (= the cell's entry: with one cell per function, its function)
+  std::vector<BatchJobDev> jt(njobs);
+  std::vector<std::vector<int>> cols(njobs);
+  int64_t near_cap = 0;
+  cudaError_t e = cudaSuccess;
+  for (int64_t j = 0; j < njobs && e == cudaSuccess; ++j) {
+    const beast_space* s = spaces[j];
+    int* zc = nullptr;
+    e = cudaMalloc(&zc, sizeof(int) * s->ncells);
+    if (e == cudaSuccess) {
+      b->zcols.push_back(zc);
+      e = cudaMemcpy(zc, s->h_cs2e.data(), sizeof(int) * s->ncells, cudaMemcpyHostToDevice);
+    }
+    BatchJobDev& J = jt[j];
+    J.op = to_params(&ops[j]);
+    J.k2 = ops[j].gamma_re * ops[j].gamma_re + ops[j].gamma_im * ops[j].gamma_im;
+    J.geo = s->geo;
+    J.geof = s->geof;
+    J.tperm = s->tperm;
+    J.zrow = s->zrow_entry;
+    J.zcol = zc;
+    J.ncells = s->ncells;
+    J.Z = Z[j];
+    J.ldz = s->nfuncs;
+    near_cap += 48 * s->ncells;
+  }
+  // tile list in the requested order
+  std::vector<int64_t> jord(njobs);
+  for (int64_t j = 0; j < njobs; ++j) jord[j] = j;
+  if (order == 1)
+    std::stable_sort(jord.begin(), jord.end(), [&](int64_t a, int64_t c) { return jt[a].ncells > jt[c].ncells; });
+  std::vector<BatchTile> tiles;
+  if (order == 2) {
+    std::vector<std::vector<BatchTile>> per(njobs);
+    size_t most = 0;
+    for (int64_t j = 0; j < njobs; ++j) {
+      for (int64_t p0 = 0; p0 < jt[j].ncells; p0 += tile_m)
+        for (int64_t q0 = 0; q0 < jt[j].ncells; q0 += tile_q) per[j].push_back(BatchTile{(int)j, (int)p0, (int)q0, 0});
+      most = std::max(most, per[j].size());
+    }
+    for (size_t k = 0; k < most; ++k)
+      for (int64_t j = 0; j < njobs; ++j)
+        if (k < per[j].size()) tiles.push_back(per[j][k]);
+  } else {
+    for (int64_t j : jord)
+      for (int64_t p0 = 0; p0 < jt[j].ncells; p0 += tile_m)
+        for (int64_t q0 = 0; q0 < jt[j].ncells; q0 += tile_q) tiles.push_back(BatchTile{(int)j, (int)p0, (int)q0, 0});
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&b->jobs, sizeof(BatchJobDev) * njobs);
+  if (e == cudaSuccess) e = cudaMemcpy(b->jobs, jt.data(), sizeof(BatchJobDev) * njobs, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&b->tiles, sizeof(BatchTile) * std::max<size_t>(1, tiles.size()));
+  if (e == cudaSuccess && !tiles.empty())
+    e = cudaMemcpy(b->tiles, tiles.data(), sizeof(BatchTile) * tiles.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMalloc(&b->near, sizeof(NearPairB) * near_cap);
+  if (e == cudaSuccess) e = cudaMalloc(&b->counter, 256);
+  b->L.jobs = b->jobs;
+  if (e != cudaSuccess) {
+    beast_batch_free(b);
+    return beast_fail(ctx, e == cudaErrorMemoryAllocation ? BEAST_ERR_OOM : BEAST_ERR_CUDA,
+                      std::string("batch setup: ") + cudaGetErrorString(e));
+  }
+  BatchLaunch& L = b->L;
+  L.tiles = b->tiles;
+  L.ntiles = (int)tiles.size();
+  L.qs_kind = qs->kind;
+  L.qs = *qs;
+  L.ro = ro;
+  L.ri = ri;
+  L.ron = ron;
+  L.rin = rin;
+  L.precision = precision;
+  L.zfmt = precision == BEAST_MIXED ? ZCELL_C64 : ZCELL_C128;
+  L.op_kind = kind;
+  L.near = b->near;
+  L.near_cap = (int)std::min<int64_t>(near_cap, INT32_MAX);
+  L.near_count = b->counter;
+  L.flag = b->counter + 1;
+  L.tile_m = tile_m;
+  L.tile_q = tile_q;
+  // persistent grids: a few CTAs per SM (the far kernel holds ~130 registers per thread)
+  L.grid_far = std::max(1, std::min(L.ntiles, ctx->num_sms * std::max(1, 512 / std::max(64, tile_m))));
+  L.grid_near = ctx->num_sms * 8;
+  *out = b;
+  return BEAST_OK;
+}
+
+int beast_batch_assemble(beast_ctx* ctx, beast_batch* b) {
+  ARG_CHECK(ctx, ctx && b && b->ctx == ctx, "invalid batch");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  cudaStream_t st = ctx->stream;
+  if (!b->exec) {
+    // capture on a stream of our own (a capture cannot run on the legacy default stream)
+    cudaStream_t cs;
+    BEAST_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->counter, 0, 2 * sizeof(int), cs);
+    if (e == cudaSuccess) e = launch_far_batch(b->L, cs);
+    if (e == cudaSuccess) e = launch_near_batch(b->L, cs);
+    cudaError_t e2 = cudaStreamEndCapture(cs, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->exec, g, 0);
+    if (g) cudaGraphDestroy(g);
+    cudaStreamDestroy(cs);
+    if (e != cudaSuccess) {
+      b->exec = nullptr;
+      return beast_fail(ctx, BEAST_ERR_CUDA, std::string("batch graph: ") + cudaGetErrorString(e));
+    }
+  }
+  {
+    ProfScope ps(ctx, PK_FAR, 228.0 * (double)b->L.ntiles * b->L.tile_m * b->L.tile_q, 2);
+    BEAST_CUDA_TRY(ctx, cudaGraphLaunch(b->exec, st));
+  }
+  int h[2] = {0, 0};
+  BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(h, b->counter, sizeof(h), cudaMemcpyDeviceToHost, st));
+  BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(st));
+  if ((h[1] & 1) || h[0] > b->L.near_cap) return beast_fail(ctx, BEAST_ERR_ARG, "batch near-pair list overflow");
+  if (h[1] & 2)
+    return beast_fail(ctx, BEAST_ERR_UNSUPPORTED, "singularity extraction not available for this operator/space pairing");
+  return BEAST_OK;
+}
+
+int beast_batch_free(beast_batch* b) {
+  if (!b) return BEAST_OK;
+  cudaSetDevice(b->ctx->device);
+  cudaStreamSynchronize(b->ctx->stream);
+  if (b->exec) cudaGraphExecDestroy(b->exec);
+  for (void* p : b->zcols) cudaFree(p);
+  if (b->jobs) cudaFree(b->jobs);
+  if (b->tiles) cudaFree(b->tiles);
+  if (b->near) cudaFree(b->near);
+  if (b->counter) cudaFree(b->counter);
+  delete b;
   return BEAST_OK;
 }
 

@@ -168,12 +168,19 @@ struct FarParams {
   int nq;
   void* zcell;
   int64_t ldc;
+  const int* zrow;  // Zcell row of (position, test shape) / column of (chunk cell, trial
+  const int* zcol;  // shape); null: the cell layout (see AsmArgs)
   NearPair* near;
   int near_cap;
   int* near_count;
   int* flag;
   TriRuleDev ro, ri;
 };
+
+// Zcell rows / columns (-1: the block entry is not stored)
+DEV int64_t zrow_of(const int* zrow, int64_t pp, int nst, int i) { return zrow ? zrow[pp * nst + i] : nst * pp + i; }
+DEV int64_t zcol_of(const int* zcol, int ql, int nsb, int j) { return zcol ? zcol[(int64_t)ql * nsb + j] : nsb * ql + j; }
+DEV int64_t zidx(int64_t row, int64_t col, int64_t ldc) { return (row < 0 || col < 0) ? -1 : col * ldc + row; }
 
 constexpr int FAR_THREADS = 128;
 constexpr int FAR_QT = 16;  // trial cells staged per CTA
@@ -182,6 +189,7 @@ constexpr int FAR_QT = 16;  // trial cells staged per CTA
 // double-float format through the integer split of fsplit.h (no FP64 instruction)
 template <typename R>
 DEV void store_c(void* z, int64_t idx, C2<R> v, int fmt) {
+  if (idx < 0) return;
   if (fmt == ZCELL_C64) {
     reinterpret_cast<float2*>(z)[idx] = make_float2((float)v.re, (float)v.im);
   } else if (fmt == ZCELL_DF) {
@@ -252,12 +260,17 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
       pt[3] = (R)P.ri.w[bb];
     }
   }
+  __shared__ int s_zc[FAR_QT][3];
+  for (int k = threadIdx.x; k < nqt * 3; k += blockDim.x)
+    s_zc[k / 3][k % 3] = (int)zcol_of(P.zcol, q0 + k / 3, (BK == BEAST_P0) ? 1 : 3, k % 3);
   __syncthreads();
   // pp: the test cell's Zcell position (cells in the order of their first function, so that
   // the rows a warp of the gather reads are close together); p: the active cell
   const int64_t pp = blockIdx.x * (int64_t)FAR_THREADS + threadIdx.x;
   if (pp >= P.np) return;
   const int64_t p = P.tperm[pp];
+  int64_t zr[3];
+  for (int i = 0; i < 3; ++i) zr[i] = i < ((TK == BEAST_P0) ? 1 : 3) ? zrow_of(P.zrow, pp, (TK == BEAST_P0) ? 1 : 3, i) : -1;
   const double* tg = P.tgeo + p * GEO_STRIDE;
   const double cpx = tg[9], cpy = tg[10], cpz = tg[11];
   const V3<R> chp = mk((R)cpx, (R)cpy, (R)cpz);
@@ -302,7 +315,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
             atomicOr(P.flag, 1);
           for (int i = 0; i < nst; ++i)
             for (int j = 0; j < nsb; ++j)
-              store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * pp + i, C2<R>{0, 0}, FMT);
+              store_c<R>(P.zcell, zidx(zr[i], s_zc[qi][j], P.ldc), C2<R>{0, 0}, FMT);
           continue;
         }
       }
@@ -435,7 +448,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
             f = csub(f, cscale(dot(ti, sj), M3));
             z = cscale((R)0.25, f);
           }
-          store_c<R>(P.zcell, (int64_t)(3 * ql + j) * P.ldc + 3 * pp + i, z, FMT);
+          store_c<R>(P.zcell, zidx(zr[i], s_zc[qi][j], P.ldc), z, FMT);
         }
       }
     } else {
@@ -485,8 +498,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
       const R ApAq = ApR * Aq;
       for (int i = 0; i < nst; ++i)
         for (int j = 0; j < nsb; ++j)
-          store_c<R>(P.zcell, (int64_t)(nsb * ql + j) * P.ldc + nst * pp + i,
-                     cscale(ApAq, acc[i * nsb + j]), FMT);
+          store_c<R>(P.zcell, zidx(zr[i], s_zc[qi][j], P.ldc), cscale(ApAq, acc[i * nsb + j]), FMT);
     }
   }
 }
@@ -741,6 +753,8 @@ struct NearParams {
   int zfmt;  // Zcell format (ZCELL_*)
   int ss32;  // Sauter-Schwab moments of RT Maxwell pairs in FP32 (mixed precision)
   int64_t ldc;
+  const int* zrow;  // as in FarParams
+  const int* zcol;
   int* flag;
   TriRuleDev ro, ri;
 };
@@ -939,27 +953,17 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss32(NearParams P) {
           C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
           z = cadd(fm, rdot(cross(sj, ti), V3_));
         }
-        store_c<double>(P.zcell, (int64_t)(3 * np_.q + j) * P.ldc + 3 * (int64_t)np_.p + i, z, P.zfmt);
+        store_c<double>(P.zcell, zidx(zrow_of(P.zrow, np_.p, 3, i), zcol_of(P.zcol, np_.q, 3, j), P.ldc), z, P.zfmt);
       }
   }
 }
 
-__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
-  // Gauss-Legendre nodes in shared memory (lanes read different nodes: a constant-memory
-  // read would serialise)
-  __shared__ double s_glx[210], s_glw[210];
-  for (int k = threadIdx.x; k < 210; k += blockDim.x) {
-    s_glx[k] = c_gl_x[k];
-    s_glw[k] = c_gl_w[k];
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
-  if (e >= P.nnear) return;
-  const NearPair np_ = P.near[e];
+// one near pair, by one warp (lane = its lane); s_glx / s_glw: the Gauss-Legendre table in
+// shared memory (lanes read different nodes: a constant-memory read would serialise)
+DEV void near_pair(const NearParams& P, const NearPair np_, const double* s_glx, const double* s_glw, int lane) {
   if (near_is_ss32(P, np_.cls)) return;  // k_near_ss32
   const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
-  const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
+  const Geo s = load_geo(P.bgeo + (int64_t)(P.qcells ? P.qcells[np_.q] : np_.q) * GEO_STRIDE);
   const int nt = P.tk == BEAST_P0 ? 1 : 3, nb = P.bk == BEAST_P0 ? 1 : 3;
   C2<double> acc[9];
   for (int k = 0; k < 9; ++k) acc[k] = C2<double>{0, 0};
@@ -1104,7 +1108,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
               C2<double> fm = csub(csub(M1, rdot(sj, V1)), rdot(ti, V2));
               z = cadd(fm, rdot(cross(sj, ti), V3_));
             }
-            store_c<double>(P.zcell, (int64_t)(3 * np_.q + j) * P.ldc + 3 * (int64_t)np_.p + i, z, P.zfmt);
+            store_c<double>(P.zcell, zidx(zrow_of(P.zrow, np_.p, 3, i), zcol_of(P.zcol, np_.q, 3, j), P.ldc), z, P.zfmt);
           }
         }
       }
@@ -1157,9 +1161,22 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
   if (lane == 0) {
     for (int i = 0; i < nt; ++i)
       for (int j = 0; j < nb; ++j)
-        store_c<double>(P.zcell, (int64_t)(nb * np_.q + j) * P.ldc + nt * (int64_t)np_.p + i,
+        store_c<double>(P.zcell, zidx(zrow_of(P.zrow, np_.p, nt, i), zcol_of(P.zcol, np_.q, nb, j), P.ldc),
                         acc[i * nb + j], P.zfmt);
   }
+}
+
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
+  __shared__ double s_glx[210], s_glw[210];
+  for (int k = threadIdx.x; k < 210; k += blockDim.x) {
+    s_glx[k] = c_gl_x[k];
+    s_glw[k] = c_gl_w[k];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
+  if (e >= P.nnear) return;
+  near_pair(P, P.near[e], s_glx, s_glw, lane);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1463,6 +1480,105 @@ __global__ void __launch_bounds__(256) k_gather_df(GatherArgs G, const int64_t* 
   }
 }
 
+// Gather from cell-pair blocks laid out by function entries (the entry layout of AsmArgs):
+//   Z[m, n] = sum over the entries e of m and f of n of c_e c_f Zcell[(f - f0) ldc + e].
+// A thread owns a test function m and GATHER_NCOL consecutive trial functions.  The entries of
+// a function are consecutive rows (columns), so for functions with the same number of entries
+// (RT: two) the rows a warp reads in one column are one contiguous run: every Zcell byte is
+// read once, in full sectors.  Sums in FP32 for c64 -> c64, in pairs of floats (sloppy sums,
+// as k_gather_df) for double-float blocks, else in FP64.
+constexpr int GATHER_E_MAX = 4;  // entries per function handled from registers
+template <int ZC, int OC64>
+__global__ void __launch_bounds__(256) k_gather_e(GatherArgs G, const int64_t* tptr, const double* tcoef,
+                                                  const int64_t* bptr, const double* bcoef, int64_t nrows) {
+  typedef typename std::conditional<ZC == ZCELL_C64 && OC64, float, double>::type A;
+  const int64_t m = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+  const int64_t nb0 = G.n0 + (int64_t)blockIdx.y * GATHER_NCOL;
+  const int64_t nb1 = nb0 + GATHER_NCOL < G.n1 ? nb0 + GATHER_NCOL : G.n1;
+  __shared__ int64_t s_c0[GATHER_NCOL];  // first Zcell column (element offset) of trial function n
+  __shared__ int s_nc[GATHER_NCOL];
+  __shared__ double s_b[GATHER_NCOL][GATHER_E_MAX];
+  if (threadIdx.x < GATHER_NCOL) {
+    const int64_t n = nb0 + threadIdx.x;
+    if (n < nb1) {
+      const int64_t f0 = bptr[n];
+      const int c = (int)(bptr[n + 1] - f0);
+      s_c0[threadIdx.x] = (f0 - G.f0) * G.ldc;
+      s_nc[threadIdx.x] = c;
+      for (int k = 0; k < GATHER_E_MAX; ++k) s_b[threadIdx.x][k] = k < c ? bcoef[f0 + k] : 0.0;
+    }
+  }
+  __syncthreads();
+  if (m >= nrows) return;
+  const int64_t e0 = tptr[m];
+  const int ne = (int)(tptr[m + 1] - e0);
+  const bool unit = G.cr == 1.0 && G.ci == 0.0;
+  auto out = [&](int64_t n, double vr, double vi) {
+    if (!unit) {
+      const double tr = G.cr * vr - G.ci * vi;
+      vi = G.cr * vi + G.ci * vr;
+      vr = tr;
+    }
+    const int64_t o = (G.row_off + m) + (G.col_off + n) * G.ldz;
+    if (OC64) {
+      float2* Z = reinterpret_cast<float2*>(G.Z);
+      float r = (float)vr, i = (float)vi;
+      if (G.accumulate) {
+        const float2 old = Z[o];
+        r += old.x;
+        i += old.y;
+      }
+      Z[o] = make_float2(r, i);
+    } else {
+      double2* Z = reinterpret_cast<double2*>(G.Z);
+      if (G.accumulate) {
+        const double2 old = Z[o];
+        vr += old.x;
+        vi += old.y;
+      }
+      Z[o] = make_double2(vr, vi);
+    }
+  };
+  for (int64_t n = nb0; n < nb1; ++n) {
+    const int nn = (int)(n - nb0);
+    const int nc = s_nc[nn];
+    const int64_t c0 = s_c0[nn] + e0;
+    if (ZC == ZCELL_DF) {
+      const float4* zc = reinterpret_cast<const float4*>(G.zcell);
+      dfl::df re = dfl::make(0.f), im = dfl::make(0.f);
+      for (int f = 0; f < nc; ++f) {
+        const dfl::df b = df_coef(f < GATHER_E_MAX ? s_b[nn][f] : bcoef[bptr[n] + f]);
+        for (int e = 0; e < ne; ++e) df_acc(re, im, zc[c0 + (int64_t)f * G.ldc + e], dfl::mul(df_coef(tcoef[e0 + e]), b));
+      }
+      if (OC64) {
+        out(n, (double)dfl::add_rn(re.hi, re.lo), (double)dfl::add_rn(im.hi, im.lo));
+      } else {
+        // exact float -> double by integer operations, one FP64 addition per part
+        const double vr = fsplit::f2d(re.hi) + fsplit::f2d(re.lo), vi = fsplit::f2d(im.hi) + fsplit::f2d(im.lo);
+        if (unit && !G.accumulate) {
+          reinterpret_cast<double2*>(G.Z)[(G.row_off + m) + (G.col_off + n) * G.ldz] = make_double2(vr, vi);
+        } else {
+          out(n, vr, vi);
+        }
+      }
+    } else {
+      typedef typename std::conditional<ZC == ZCELL_C64, float2, double2>::type Z2;
+      const Z2* zc = reinterpret_cast<const Z2*>(G.zcell);
+      A re = 0, im = 0;
+      for (int f = 0; f < nc; ++f) {
+        const A b = (A)(f < GATHER_E_MAX ? s_b[nn][f] : bcoef[bptr[n] + f]);
+        for (int e = 0; e < ne; ++e) {
+          const Z2 z = zc[c0 + (int64_t)f * G.ldc + e];
+          const A ab = (A)tcoef[e0 + e] * b;
+          re += ab * (A)z.x;
+          im += ab * (A)z.y;
+        }
+      }
+      out(n, (double)re, (double)im);
+    }
+  }
+}
+
 // ------------------------------------------------------------------------------------
 // local operators (Identity / NCross on RT x RT), deterministic per test dof
 // ------------------------------------------------------------------------------------
@@ -1653,6 +1769,166 @@ cudaError_t launch_geometry(const beast_space* s, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ------------------------------------------------------------------------------------
+// batched far pairs: many meshes in one persistent launch (Helmholtz operators, P0 spaces)
+// ------------------------------------------------------------------------------------
+// The grid walks a tile list (job, first test position, first trial cell), tile t on CTA
+// t mod gridDim.x: a CTA stages tile_q trial cells of the tile's job in shared memory and
+// each of its tile_m threads takes one test cell against them, as k_far does for one mesh.
+// P0 functions have one cell each, so every cell-pair value is a matrix entry and goes
+// straight to the job's matrix (row zrow[position], column zcol[trial cell]).  Near pairs go
+// to one list for the whole batch (k_near_batch).
+template <int OPK, typename R, int FMT>
+__global__ void k_far_batch(BatchLaunch L) {
+  extern __shared__ unsigned char smraw[];
+  R* sm = reinterpret_cast<R*>(smraw);
+  const int ni = L.ri.n, no = L.ro.n;
+  const int rec = 8 + 4 * ni;  // per trial cell: centroid hi (3) lo (3), area, near radius; points
+  int* s_col = reinterpret_cast<int*>(sm + (size_t)L.tile_q * rec);
+  __shared__ R ro_s[3 * RULE_MAXPTS];
+  for (int k = threadIdx.x; k < no; k += blockDim.x) {
+    ro_s[3 * k] = (R)L.ro.u[k];
+    ro_s[3 * k + 1] = (R)L.ro.v[k];
+    ro_s[3 * k + 2] = (R)L.ro.w[k];
+  }
+  for (int t = blockIdx.x; t < L.ntiles; t += gridDim.x) {
+    const BatchTile tile = L.tiles[t];
+    const BatchJobDev J = L.jobs[tile.job];
+    const int nqt = (int)min((int64_t)L.tile_q, J.ncells - tile.q0);
+    __syncthreads();  // the previous tile's records are no longer read
+    for (int k = threadIdx.x; k < nqt * (1 + ni); k += blockDim.x) {
+      const int qi = k / (1 + ni), b = k % (1 + ni);
+      const int qc = tile.q0 + qi;
+      const double* g = J.geo + (int64_t)qc * GEO_STRIDE;
+      R* r = sm + qi * rec;
+      const double cx = g[9], cy = g[10], cz = g[11];
+      if (b == 0) {
+        r[0] = (R)cx; r[1] = (R)cy; r[2] = (R)cz;
+        r[3] = (R)(cx - (double)(R)cx); r[4] = (R)(cy - (double)(R)cy); r[5] = (R)(cz - (double)(R)cz);
+        r[6] = (R)g[15];
+        const double thr2 = near_threshold2(L.qs_kind, J.k2, g[15]);
+        r[7] = (R)((double)J.geof[4 * qc + 3] + sqrt(fmax(thr2, 0.0)));
+        s_col[qi] = J.zcol[qc];
+      } else {
+        const int bb = b - 1;
+        const double u = L.ri.u[bb], v = L.ri.v[bb], w = 1.0 - u - v;
+        R* pt = r + 8 + 4 * bb;
+        pt[0] = (R)(u * (g[0] - cx) + v * (g[3] - cx) + w * (g[6] - cx));
+        pt[1] = (R)(u * (g[1] - cy) + v * (g[4] - cy) + w * (g[7] - cy));
+        pt[2] = (R)(u * (g[2] - cz) + v * (g[5] - cz) + w * (g[8] - cz));
+        pt[3] = (R)L.ri.w[bb];
+      }
+    }
+    __syncthreads();
+    const int64_t pp = tile.p0 + threadIdx.x;
+    if (pp >= J.ncells || threadIdx.x >= L.tile_m) continue;
+    const int64_t p = J.tperm[pp];
+    const double* tg = J.geo + p * GEO_STRIDE;
+    const double cpx = tg[9], cpy = tg[10], cpz = tg[11];
+    const V3<R> chp = mk((R)cpx, (R)cpy, (R)cpz);
+    const V3<R> clp = mk((R)(cpx - (double)(R)cpx), (R)(cpy - (double)(R)cpy), (R)(cpz - (double)(R)cpz));
+    V3<R> tau[3];
+    for (int i = 0; i < 3; ++i)
+      tau[i] = mk((R)(tg[3 * i] - cpx), (R)(tg[3 * i + 1] - cpy), (R)(tg[3 * i + 2] - cpz));
+    const V3<R> nn = mk((R)tg[12], (R)tg[13], (R)tg[14]);
+    const R ApR = (R)tg[15];
+    const R radp = (R)J.geof[4 * p + 3];
+    const R gr = (R)J.op.gr, gi = (R)J.op.gi;
+    const C2<R> al{(R)J.op.ar, (R)J.op.ai};
+    const int64_t zr = J.zrow[pp];
+    for (int qi = 0; qi < nqt; ++qi) {
+      const R* rq = sm + qi * rec;
+      const V3<R> d = mk((chp.x - rq[0]) + (clp.x - rq[3]), (chp.y - rq[1]) + (clp.y - rq[4]),
+                         (chp.z - rq[2]) + (clp.z - rq[5]));
+      const int64_t o = zidx(zr, s_col[qi], J.ldz);
+      const R lim = radp + rq[7];
+      if (dot(d, d) <= lim * lim * (R)1.0001 + (R)1e-30) {
+        int cls = 4;
+        if (L.qs_kind != BEAST_QS_DOUBLENUM) {
+          Geo ta = load_geo(tg);
+          Geo sb = load_geo(J.geo + (int64_t)(tile.q0 + qi) * GEO_STRIDE);
+          cls = classify_exact(ta, sb, L.qs_kind, J.k2);
+        }
+        if (cls != 0) {
+          const int idx = atomicAdd(L.near_count, 1);
+          if (idx < L.near_cap)
+            L.near[idx] = NearPairB{tile.job, (int)pp, tile.q0 + qi, cls};
+          else
+            atomicOr(L.flag, 1);
+          continue;  // k_near_batch writes the entry
+        }
+      }
+      const R* pts = rq + 8;
+      const V3<R> nq = mk((R)0, (R)0, (R)0);  // trial normal: only the double layer needs it
+      C2<R> acc{0, 0};
+      for (int a = 0; a < no; ++a) {
+        const R ua = ro_s[3 * a], va = ro_s[3 * a + 1], wa3 = (R)1 - ua - va;
+        const V3<R> xi = mk(ua * tau[0].x + va * tau[1].x + wa3 * tau[2].x,
+                            ua * tau[0].y + va * tau[1].y + wa3 * tau[2].y,
+                            ua * tau[0].z + va * tau[1].z + wa3 * tau[2].z);
+        const R wa = ro_s[3 * a + 2];
+        const V3<R> dx = d + xi;
+        for (int b = 0; b < ni; ++b) {
+          const R* pb = pts + 4 * b;
+          const V3<R> r = dx - mk(pb[0], pb[1], pb[2]);
+          const R R2 = dot(r, r);
+          const R iR = rsq<R>(R2);
+          const C2<R> G = green<R>(gr, gi, R2 * iR, iR);
+          C2<R> K;
+          if (OPK == BEAST_HH_SL) {
+            K = cmul(al, G);
+          } else {  // transposed double layer: n_x . grad G (the double layer takes the trial
+                    // normal from the geometry below)
+            const C2<R> c = cmul(al, cscale(iR, cmul(C2<R>{-(gr + iR), -gi}, G)));
+            K = cscale(dot(nn, r), c);
+          }
+          acc = cadd(acc, cscale(pb[3] * wa, K));
+        }
+      }
+      (void)nq;
+      store_c<R>(J.Z, o, cscale(ApR * rq[6], acc), FMT);
+    }
+  }
+}
+
+// near pairs of a batch: one warp per pair, pairs dealt over the warps of a fixed grid
+// (the list length is read on the device, so the launch needs no host round trip)
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_batch(BatchLaunch L) {
+  __shared__ double s_glx[210], s_glw[210];
+  for (int k = threadIdx.x; k < 210; k += blockDim.x) {
+    s_glx[k] = c_gl_x[k];
+    s_glw[k] = c_gl_w[k];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = min(*L.near_count, L.near_cap);
+  for (int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp; e < n; e += (int64_t)gridDim.x * NEAR_WARPS) {
+    const NearPairB nb = L.near[e];
+    const BatchJobDev J = L.jobs[nb.job];
+    NearParams P;
+    P.op = J.op;
+    P.qs = L.qs;
+    P.tk = BEAST_P0;
+    P.bk = BEAST_P0;
+    P.tperm = J.tperm;
+    P.tgeo = J.geo;
+    P.bgeo = J.geo;
+    P.qcells = nullptr;
+    P.near = nullptr;
+    P.nnear = 0;
+    P.zcell = J.Z;
+    P.zfmt = L.zfmt;
+    P.ss32 = 0;
+    P.ldc = J.ldz;
+    P.zrow = J.zrow;
+    P.zcol = J.zcol;
+    P.flag = L.flag;
+    P.ro = L.ron;
+    P.ri = L.rin;
+    near_pair(P, NearPair{nb.p, nb.q, nb.cls, 0}, s_glx, s_glw, lane);
+  }
+}
+
 template <int OPK, int TK, int BK, typename R, int FMT>
 static cudaError_t far_t(const FarParams& P, cudaStream_t st) {
   dim3 grid((unsigned)((P.np + FAR_THREADS - 1) / FAR_THREADS), (unsigned)((P.nq + FAR_QT - 1) / FAR_QT));
@@ -1696,6 +1972,7 @@ template <int NO, int NI>
 __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
   __shared__ FarDfRecord rec[FAR_QT];
   __shared__ float s_tab[64][4];  // sin / cos(m pi/32): lanes read different entries
+  __shared__ int s_zc[FAR_QT][3];
   for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
   const int ni = P.ri.n, no = P.ro.n;
   const int q0 = blockIdx.y * FAR_QT;
@@ -1727,10 +2004,13 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
       r.eta2[bb] = dfl::dot3s(r.eta[bb], r.eta[bb]);
     }
   }
+  for (int k = threadIdx.x; k < nqt * 3; k += blockDim.x) s_zc[k / 3][k % 3] = (int)zcol_of(P.zcol, q0 + k / 3, 3, k % 3);
   __syncthreads();
   const int64_t pp = blockIdx.x * (int64_t)FAR_THREADS + threadIdx.x;
   if (pp >= P.np) return;
   const int64_t p = P.tperm[pp];
+  int64_t zr[3];
+  for (int i = 0; i < 3; ++i) zr[i] = zrow_of(P.zrow, pp, 3, i);
   const double* tg = P.tgeo + p * GEO_STRIDE;
   const double cpx = tg[9], cpy = tg[10], cpz = tg[11];
   const dfl::df cp[3] = {df_of(cpx), df_of(cpy), df_of(cpz)};
@@ -1772,7 +2052,10 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
           else
             atomicOr(P.flag, 1);
           for (int i = 0; i < 3; ++i)
-            for (int j = 0; j < 3; ++j) zc[(int64_t)(3 * ql + j) * P.ldc + 3 * pp + i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            for (int j = 0; j < 3; ++j) {
+              const int64_t o = zidx(zr[i], s_zc[qi][j], P.ldc);
+              if (o >= 0) zc[o] = make_float4(0.f, 0.f, 0.f, 0.f);
+            }
           continue;
         }
       }
@@ -1785,7 +2068,8 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
     for (int i = 0; i < 3; ++i)
       for (int j = 0; j < 3; ++j) {
         const dfl::cdf& v = z[3 * i + j];
-        zc[(int64_t)(3 * ql + j) * P.ldc + 3 * pp + i] = make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo);
+        const int64_t o = zidx(zr[i], s_zc[qi][j], P.ldc);
+        if (o >= 0) zc[o] = make_float4(v.re.hi, v.re.lo, v.im.hi, v.im.lo);
       }
   }
 }
@@ -1823,6 +2107,8 @@ cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev&
   P.nq = a.nq;
   P.zcell = a.zcell;
   P.ldc = a.ldc;
+  P.zrow = a.zrow;
+  P.zcol = a.zcol;
   P.near = a.near;
   P.near_cap = a.near_cap;
   P.near_count = a.near_count;
@@ -1872,6 +2158,31 @@ static cudaError_t upload_gl(cudaStream_t st) {
   return e;
 }
 
+cudaError_t launch_far_batch(const BatchLaunch& L, cudaStream_t st) {
+  if (L.ntiles == 0) return cudaSuccess;
+  const size_t sm_f = (size_t)L.tile_q * (8 + 4 * L.ri.n) * sizeof(float) + sizeof(int) * L.tile_q;
+  const size_t sm_d = (size_t)L.tile_q * (8 + 4 * L.ri.n) * sizeof(double) + sizeof(int) * L.tile_q;
+  const int th = ((L.tile_m + 31) / 32) * 32;
+  const bool f32 = L.precision == BEAST_MIXED;
+  if (L.op_kind == BEAST_HH_SL) {
+    if (f32) k_far_batch<BEAST_HH_SL, float, ZCELL_C64><<<L.grid_far, th, sm_f, st>>>(L);
+    else k_far_batch<BEAST_HH_SL, double, ZCELL_C128><<<L.grid_far, th, sm_d, st>>>(L);
+  } else if (L.op_kind == BEAST_HH_DLT) {
+    if (f32) k_far_batch<BEAST_HH_DLT, float, ZCELL_C64><<<L.grid_far, th, sm_f, st>>>(L);
+    else k_far_batch<BEAST_HH_DLT, double, ZCELL_C128><<<L.grid_far, th, sm_d, st>>>(L);
+  } else {
+    return cudaErrorInvalidValue;
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_near_batch(const BatchLaunch& L, cudaStream_t st) {
+  cudaError_t e = upload_gl(st);
+  if (e != cudaSuccess) return e;
+  k_near_batch<<<L.grid_near, 32 * NEAR_WARPS, 0, st>>>(L);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const TriRuleDev& ri,
                         cudaStream_t st) {
   if (nnear <= 0) return cudaSuccess;
@@ -1892,6 +2203,8 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   P.zfmt = a.zcell_fmt;
   P.ss32 = a.precision == BEAST_MIXED;
   P.ldc = a.ldc;
+  P.zrow = a.zrow;
+  P.zcol = a.zcol;
   P.flag = a.flag;
   P.ro = ro;
   P.ri = ri;
@@ -1915,7 +2228,18 @@ cudaError_t launch_gather(const GatherArgs& g, cudaStream_t st) {
   k_gather<ZC, OC><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_cell, ts->fn_shape, ts->fn_coeff, \
                                         bs->fn_ptr, bs->fn_cell, bs->fn_shape, bs->fn_coeff, nst, \
                                         nsb, nrows)
-  if (g.zcell_fmt == ZCELL_DF) {
+  if (g.entry_layout) {
+#define GATHER_E(ZC, OC) \
+  k_gather_e<ZC, OC><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_coeff, bs->fn_ptr, bs->fn_coeff, nrows)
+    if (g.zcell_fmt == ZCELL_DF) {
+      if (g.z_c64) GATHER_E(ZCELL_DF, 1); else GATHER_E(ZCELL_DF, 0);
+    } else if (g.zcell_fmt == ZCELL_C64) {
+      if (g.z_c64) GATHER_E(ZCELL_C64, 1); else GATHER_E(ZCELL_C64, 0);
+    } else {
+      if (g.z_c64) GATHER_E(ZCELL_C128, 1); else GATHER_E(ZCELL_C128, 0);
+    }
+#undef GATHER_E
+  } else if (g.zcell_fmt == ZCELL_DF) {
     if (g.z_c64)
       k_gather_df<1><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_cell, ts->fn_shape, ts->fn_coeff, bs->fn_ptr,
                                           bs->fn_cell, bs->fn_shape, bs->fn_coeff, nst, nsb, nrows);

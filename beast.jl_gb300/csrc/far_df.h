@@ -102,14 +102,15 @@ template <int NO, int NI>
 DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3], const df (*xi)[3],
                               const df* wo, const df (*eta)[3], const df* wi, const df* eta2, df k, cdf alpha,
                               cdf beta, const float (*tab)[4], cdf* out) {
-  // The loops stay rolled: unrolled, the body of the 12 point pairs and the block finish come
-  // to several thousand instructions and the warps stall on instruction fetch.
+  // The loops over test points are unrolled (their per-point values stay in registers); the
+  // loops over trial points and over the block entries stay rolled: fully unrolled, the
+  // kernel comes to several thousand instructions and its warps stall on instruction fetch.
   const df z0 = make(0.f);
   const df i4pi{DF_I4PI_HI, DF_I4PI_LO};
   df A[NO];
   cdf U0[NO];
 #if defined(__CUDA_ARCH__)
-#pragma unroll 1
+#pragma unroll
 #endif
   for (int a = 0; a < NO; ++a) {
     df dx[3];
@@ -127,7 +128,7 @@ DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3
     const df wq = mul(wi[b], i4pi);
     cdf T{z0, z0};
 #if defined(__CUDA_ARCH__)
-#pragma unroll 1
+#pragma unroll
 #endif
     for (int a = 0; a < NO; ++a) {
       const df P = dot3s(xi[a], eta[b]);
@@ -149,7 +150,7 @@ DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3
   cdf V1[3];
   for (int c = 0; c < 3; ++c) V1[c] = cdf{z0, z0};
 #if defined(__CUDA_ARCH__)
-#pragma unroll 1
+#pragma unroll
 #endif
   for (int a = 0; a < NO; ++a) {
     const cdf s = cscale(U0[a], wo[a]);
@@ -158,20 +159,21 @@ DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3
   const cdf a4{scale(alpha.re, 0.25f), scale(alpha.im, 0.25f)};
   const cdf C = cadds(cmuls(a4, M1), cmuls(beta, M0));
   const cdf D = cmuls(a4, M0);
-  cdf S[3], T[3];
+  cdf S[3];
+#if defined(__CUDA_ARCH__)
+#pragma unroll
+#endif
+  for (int j = 0; j < 3; ++j) S[j] = cmuls(a4, cdot3s(V1, sig[j]));
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
-  for (int j = 0; j < 3; ++j) {
-    S[j] = cmuls(a4, cdot3s(V1, sig[j]));
-    T[j] = cmuls(a4, cdot3s(V2, tau[j]));
-  }
+  for (int i = 0; i < 3; ++i) {
+    const cdf Ti = cmuls(a4, cdot3s(V2, tau[i]));
+    const cdf Ci = csubs(C, Ti);
 #if defined(__CUDA_ARCH__)
-#pragma unroll 1
+#pragma unroll
 #endif
-  for (int e = 0; e < 9; ++e) {
-    const int i = e / 3, j = e % 3;
-    out[e] = cadds(csubs(csubs(C, S[j]), T[i]), cscale(D, dot3s(tau[i], sig[j])));
+    for (int j = 0; j < 3; ++j) out[3 * i + j] = cadds(csubs(Ci, S[j]), cscale(D, dot3s(tau[i], sig[j])));
   }
 }
 

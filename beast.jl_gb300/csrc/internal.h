@@ -97,6 +97,12 @@ struct beast_space {
   // Zcell row order of the test side: active cells sorted by their first function
   int* tperm = nullptr;        // position -> active cell
   int* tpos = nullptr;         // active cell -> position
+  // (active cell, shape) -> its entry in the function CSR (fn_*), -1 for none; `injective`
+  // when no (cell, shape) belongs to two entries (RT on a closed or open surface, P0, P1): the
+  // cell-pair blocks can then be laid out by entries (ZLAYOUT_ENTRY)
+  bool injective = false;
+  std::vector<int> h_cs2e;
+  int* zrow_entry = nullptr;   // [ncells][nshapes] by Zcell position: the entry, or -1
   std::vector<int> h_ad_dof;   // host copy of the assembly data
   std::vector<double> h_ad_coeff;
 };
@@ -156,6 +162,11 @@ struct AsmArgs {
   int near_cap;
   int* near_count;     // device counter
   int* flag;           // device error flag
+  // where the block of (test position pp, shape i) x (chunk trial cell ql, shape j) goes:
+  // row zrow[pp * nst + i], column zcol[ql * nsb + j] (-1: not stored); null: the cell layout,
+  // row nst pp + i, column nsb ql + j
+  const int* zrow;
+  const int* zcol;
 };
 cudaError_t launch_geometry(const beast_space* s, cudaStream_t st);
 cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev& ri,
@@ -177,6 +188,9 @@ struct GatherArgs {
   int64_t row_off, col_off;
   double cr, ci;
   int accumulate;
+  // entry layout (ZLAYOUT_ENTRY): Zcell row = test entry, column = trial entry - f0
+  int entry_layout;
+  int64_t f0;
 };
 cudaError_t launch_gather(const GatherArgs& g, cudaStream_t st);
 cudaError_t launch_local_impl(int which, const beast_space* ts, const beast_space* bs,
@@ -189,6 +203,46 @@ cudaError_t launch_rhs(int kind, const beast_space* ts, const double* dir, const
 cudaError_t launch_farfield(const beast_space* s, const double* u, const double* pts,
                             int64_t npts, double gr, double gi, const TriRuleDev& r, double* ff,
                             cudaStream_t st);
+
+// ---- batched assembly of many meshes (assemble.cu / api.cu): Helmholtz operators on P0
+// spaces, every cell-pair value written straight into its job's matrix
+struct BatchJobDev {
+  OpParams op;
+  double k2;
+  const double* geo;   // the job space's geometry ([ncells][GEO_STRIDE])
+  const float* geof;   // centroid and radius per cell
+  const int* tperm;    // position -> active cell
+  const int* zrow;     // [position]: matrix row (the space's entry of the cell)
+  const int* zcol;     // [active cell]: matrix column
+  int64_t ncells;
+  void* Z;             // the job's matrix (column-major, ld ldz)
+  int64_t ldz;
+};
+struct BatchTile {
+  int job, p0, q0, pad;  // test positions p0 .. p0 + tile_m, trial cells q0 .. q0 + tile_q
+};
+struct NearPairB {
+  int job, p, q, cls;
+};
+struct BatchLaunch {
+  const BatchJobDev* jobs;
+  const BatchTile* tiles;
+  int ntiles;
+  int qs_kind;
+  beast_qs_desc qs;
+  TriRuleDev ro, ri, ron, rin;  // far and near rules
+  int precision;
+  int zfmt;                     // matrix element format (ZCELL_C64 or ZCELL_C128)
+  int op_kind;                  // one operator kind for the whole batch
+  NearPairB* near;
+  int near_cap;
+  int* near_count;
+  int* flag;
+  int tile_m, tile_q;           // test cells per CTA (= threads), trial cells staged per CTA
+  int grid_far, grid_near;      // persistent CTAs
+};
+cudaError_t launch_far_batch(const BatchLaunch& L, cudaStream_t st);
+cudaError_t launch_near_batch(const BatchLaunch& L, cudaStream_t st);
 
 // ---- dense linear algebra (linalg.cu)
 // bytes of the auxiliary allocation of a factorisation (pivots, permutation, inverses of the

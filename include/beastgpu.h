@@ -242,6 +242,25 @@ int beast_solve_job(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc
                     double exc_gamma_re, double exc_gamma_im, int precision, double tol,
                     double* x, int x_loc, int* iters, double* resid);
 
+/* ---- batched assembly: many meshes in one persistent launch ---------------------------
+ * Helmholtz single layer (BEAST_HH_SL) or transposed double layer (BEAST_HH_DLT) on P0
+ * spaces (one cell per function, coefficient 1): job j assembles ops[j] on spaces[j] x
+ * spaces[j] into the device matrix Z[j] (column-major, ld = nfuncs, c64 for BEAST_MIXED, else
+ * c128; overwritten).  Every job shares the quadrature strategy `qs` and one operator kind.
+ * The far pairs of all jobs run as one persistent kernel over a tile list (tile_m test cells x
+ * tile_q trial cells of one job per CTA step; 0 = defaults 128 x 16) in the order `order`
+ * (0: job by job, 1: largest jobs first, 2: jobs interleaved), the near pairs of all jobs as a
+ * second one; the pair list length stays on the device.  beast_batch_assemble captures both
+ * launches in a CUDA graph on its first call and replays the graph afterwards (the calls
+ * replace, for a batch of meshes, one assemble(op, X, X) per mesh: src/operator.jl:100-116).
+ * No reference counterpart for the handle. */
+typedef struct beast_batch beast_batch;
+int beast_batch_create(beast_ctx* ctx, const beast_qs_desc* qs, int64_t njobs, const beast_space* const* spaces,
+                       const beast_op_desc* ops, void* const* Z, int precision, int tile_m, int tile_q, int order,
+                       beast_batch** out);
+int beast_batch_assemble(beast_ctx* ctx, beast_batch* batch);
+int beast_batch_free(beast_batch* batch);
+
 /* ---- resident systems: the `solve(eq)` path split so that the matrix and its factors stay
  * on the device between requests (serving: a request on a system already resident skips
  * assembly and factorisation; src/solvers/lusolver.jl:9-39 assembles and factors per call).

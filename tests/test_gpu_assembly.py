@@ -288,3 +288,15 @@ def test_assemblerow_subset_blocks(ctx, precision):
     J = rng.integers(0, Y.numfunctions(), 9)
     Hb = bg.blockassembler(hh, Y, Y, precision=precision, ctx=ctx)(I, J)
     assert np.abs(Hb - H[np.ix_(I, J)]).max() <= tol * np.abs(H).max()
+
+
+@pytest.mark.parametrize("precision", [bg.FP64, bg.MIXED, bg.MIXED_ACCURATE])
+def test_zcell_layouts_agree(ctx, monkeypatch, precision):
+    """the cell-pair blocks laid out by function entries (the default for RT / P0 / P1) and by
+    cells give the same matrix: the same sums in the same order"""
+    X = bg.raviartthomas(bg.icosphere(2))
+    op = bg.Maxwell3D.singlelayer(wavenumber=3.0)
+    Ze = bg.assemble(op, X, X, precision=precision, ctx=ctx)
+    monkeypatch.setenv("BEAST_ZCELL_LAYOUT", "cell")
+    Zc = bg.assemble(op, X, X, precision=precision, ctx=ctx)
+    assert np.array_equal(Ze, Zc)

@@ -50,3 +50,28 @@ def test_cache_is_reused_and_force_retimes(tmp_path, monkeypatch):
 def test_size_classes():
     assert bg.tune.size_class(30720) == bg.tune.size_class(30000)
     assert bg.tune.size_class(30720) != bg.tune.size_class(15360)
+
+
+def test_batch_autotuner_search_and_cache(tmp_path):
+    """the batch schedule search picks the fastest candidate, caches it by signature and
+    reads it back without timing again (a stand-in timer on the CPU)"""
+    from beastgpu import tune
+    from beastgpu.spaces import lagrangecxd0
+    from beastgpu.mesh import icosphere
+    from beastgpu.operators import Helmholtz3D
+    spaces = [lagrangecxd0(icosphere(1)), lagrangecxd0(icosphere(2))]
+    ops = [Helmholtz3D.singlelayer(wavenumber=1.0)] * 2
+    calls = []
+
+    def timer(c):
+        calls.append(c)
+        return 1.0 + abs(c[0] - 128) / 64 + abs(c[1] - 32) / 16 + (0 if c[2] == "interleaved" else 0.5)
+
+    path = str(tmp_path / "t.json")
+    e = tune.autotune_batch(ops, spaces, 1, timer=timer, cache_path=path, key="k")
+    assert (e["tile_m"], e["tile_q"], e["order"]) == (128, 32, "interleaved")
+    n = len(calls)
+    assert n == len(tune.BATCH_CANDIDATES)
+    e2 = tune.autotune_batch(ops, spaces, 1, timer=timer, cache_path=path, key="k")
+    assert len(calls) == n and e2["tile_q"] == 32
+    assert tune.batch_signature(ops, spaces, 1).startswith("k4|p1|n2|")
