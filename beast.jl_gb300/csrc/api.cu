@@ -1492,6 +1492,8 @@ int beast_batch_assemble(beast_ctx* ctx, beast_batch* b) {
   if (set_device(ctx)) return BEAST_ERR_CUDA;
   cudaStream_t st = ctx->stream;
   if (!b->exec) {
+    BEAST_CUDA_TRY(ctx, upload_tables(st));
+    BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(st));
     // capture on a stream of our own (a capture cannot run on the legacy default stream)
     cudaStream_t cs;
     BEAST_CUDA_TRY(ctx, cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));

@@ -2176,9 +2176,10 @@ cudaError_t launch_far_batch(const BatchLaunch& L, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+cudaError_t upload_tables(cudaStream_t st) { return upload_gl(st); }
+
 cudaError_t launch_near_batch(const BatchLaunch& L, cudaStream_t st) {
-  cudaError_t e = upload_gl(st);
-  if (e != cudaSuccess) return e;
+  // the Gauss-Legendre table is uploaded before (upload_tables): this launch may be captured
   k_near_batch<<<L.grid_near, 32 * NEAR_WARPS, 0, st>>>(L);
   return cudaGetLastError();
 }

@@ -242,6 +242,9 @@ struct BatchLaunch {
   int grid_far, grid_near;      // persistent CTAs
 };
 cudaError_t launch_far_batch(const BatchLaunch& L, cudaStream_t st);
+// the constant tables of the near-pair kernels (Gauss-Legendre nodes), once per device; must
+// run before a launch that is captured in a graph
+cudaError_t upload_tables(cudaStream_t st);
 cudaError_t launch_near_batch(const BatchLaunch& L, cudaStream_t st);
 
 // ---- dense linear algebra (linalg.cu)
