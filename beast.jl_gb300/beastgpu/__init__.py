@@ -6,11 +6,11 @@ mirror of the reference's interface: meshes, spaces, operators, quadrature strat
 """
 from . import lib
 from .lib import FP64, MIXED, MIXED_ACCURATE, C128, C64, BeastError
-from .mesh import Mesh, readmesh, icosphere, ellipsoid
+from .mesh import Mesh, readmesh, icosphere, ellipsoid, refines
 from .spaces import raviartthomas, lagrangecxd0, lagrangec0d1, P0, P1, RT
 from .operators import (Maxwell3D, Helmholtz3D, nxdoublelayer, Identity, NCross,
                         DoubleNumWiltonSauterQStrat, DoubleNumSauterQstrat, DoubleNumQStrat,
-                        defaultquadstrat, tangential_trace, cross_trace_H, dirichlet_trace)
+                        TestRefinesTrialQStrat, TrialRefinesTestQStrat, defaultquadstrat, tangential_trace, cross_trace_H, dirichlet_trace)
 from .api import (Context, get_context, assemble, assemble_rhs, solve, gmres, farfield,
                   solve_job, blockassembler, assemblerow, assemblecol)
 from .serve import Server, run_job, job_footprint

@@ -13,6 +13,7 @@ import ctypes as C
 import numpy as np
 
 from . import lib as L
+from . import mesh as M
 from . import operators as O
 from . import spaces as S
 
@@ -101,6 +102,15 @@ class Context:
             self._meshes[key] = ent
         return ent[0]
 
+    def register_children(self, coarse, refinement):
+        """the children of every cell of `coarse` (refinement.coarse) on the device, once"""
+        h = self.mesh_handle(coarse)
+        done = self.__dict__.setdefault("_children", {})
+        if done.get(id(coarse)) is not refinement:
+            cv = refinement.child_vertices()
+            self.check(self.lib.beast_mesh_set_children(self.handle, h, cv.shape[1], cv.ctypes.data))
+            done[id(coarse)] = refinement
+
     def space_handle(self, space):
         key = id(space)
         ent = self._spaces.get(key)
@@ -123,6 +133,30 @@ def get_context(device=0):
         ctx = Context(device)
         _CTX[device] = ctx
     return ctx
+
+
+def _quadstrat(ctx, op, X, Y, quadstrat):
+    """the strategy of an integral operator on X x Y: the given one or the default, wrapped in
+    TestRefinesTrialQStrat / TrialRefinesTestQStrat when one space lives on the refinement of
+    the other's mesh (src/operator.jl:256-262); the coarse mesh's children go to the device"""
+    qs = quadstrat if quadstrat is not None else O.defaultquadstrat(op, X, Y)
+    if M.refines(X.mesh, Y.mesh):
+        ctx.register_children(Y.mesh, X.mesh.refinement)
+        return qs if isinstance(qs, O.TestRefinesTrialQStrat) else O.TestRefinesTrialQStrat(qs)
+    if M.refines(Y.mesh, X.mesh):
+        ctx.register_children(X.mesh, Y.mesh.refinement)
+        return qs if isinstance(qs, O.TrialRefinesTestQStrat) else O.TrialRefinesTestQStrat(qs)
+    return qs
+
+
+def _local_spaces(X, Y):
+    """a local operator across a refinement: the coarse space written in the fine cells'
+    shapes, exactly (assemble_local_refines!, src/localop.jl:155-216)"""
+    if M.refines(X.mesh, Y.mesh):
+        return X, X.mesh.refinement.refined_space(Y)
+    if M.refines(Y.mesh, X.mesh):
+        return Y.mesh.refinement.refined_space(X), Y
+    return X, Y
 
 
 def _op_desc(op):
@@ -165,15 +199,17 @@ def assemble(op, X, Y=None, quadstrat=None, precision=L.FP64, out=None, dtype=No
     acc = accumulate
     for (c, term) in terms:
         c = complex(c) * complex(coeff)
-        th, bh = ctx.space_handle(X), ctx.space_handle(Y)
         if isinstance(term, O.LocalOperator):
+            tX, tY = _local_spaces(X, Y)
+            th, bh = ctx.space_handle(tX), ctx.space_handle(tY)
             if not acc:
                 # the local store adds; start from zero when it is the first term
                 _zero_block(result, loc, row_off, col_off, X.numfunctions(), Y.numfunctions())
             ctx.check(ctx.lib.beast_assemble_local(ctx.handle, term.which, th, bh, 6, ptr, ld, dtype,
                                                    loc, row_off, col_off, c.real, c.imag))
         else:
-            qs = quadstrat if quadstrat is not None else O.defaultquadstrat(term, X, Y)
+            qs = _quadstrat(ctx, term, X, Y, quadstrat)
+            th, bh = ctx.space_handle(X), ctx.space_handle(Y)
             od, qd = _op_desc(term), _qs_desc(qs)
             ctx.check(ctx.lib.beast_assemble(ctx.handle, C.byref(od), C.byref(qd), th, bh, precision,
                                              ptr, ld, dtype, loc, row_off, col_off, c.real, c.imag,
@@ -190,7 +226,7 @@ def blockassembler(op, X, Y=None, quadstrat=None, precision=L.FP64, ctx=None):
     Y = X if Y is None else Y
     if isinstance(op, (O.LinearCombination, O.LocalOperator)):
         raise ValueError("blockassembler: integral operators only")
-    qs = quadstrat if quadstrat is not None else O.defaultquadstrat(op, X, Y)
+    qs = _quadstrat(ctx, op, X, Y, quadstrat)
     od, qd = _op_desc(op), _qs_desc(qs)
     dtype = L.C64 if precision == L.MIXED else L.C128
 

@@ -41,7 +41,7 @@ class QsDesc(C.Structure):
 EXPORTS = [
     "beast_ctx_create", "beast_ctx_destroy", "beast_last_error", "beast_ctx_set_stream",
     "beast_ctx_set_workspace_limit", "beast_ctx_synchronize", "beast_ctx_set_wait_limit", "beast_mesh_upload",
-    "beast_mesh_free", "beast_space_upload", "beast_space_free", "beast_assemble",
+    "beast_mesh_free", "beast_mesh_set_children", "beast_space_upload", "beast_space_free", "beast_assemble",
     "beast_assemble_block", "beast_assemble_local", "beast_rhs_planewave", "beast_lu_factor", "beast_lu_solve",
     "beast_lu_free", "beast_lu_solve_noalloc", "beast_solve_dense", "beast_gmres", "beast_farfield", "beast_solve_job",
     "beast_system_create", "beast_system_solve", "beast_system_bytes", "beast_system_free", "beast_pool_stats",
@@ -74,6 +74,7 @@ def load(build_if_needed=True):
     L.beast_ctx_set_wait_limit.argtypes = [vp, i64]
     L.beast_mesh_upload.argtypes = [vp, vp, i64, vp, i64, i, pp]
     L.beast_mesh_free.argtypes = [vp]
+    L.beast_mesh_set_children.argtypes = [vp, vp, i, vp]
     L.beast_space_upload.argtypes = [vp, vp, i, i64, vp, i, i, vp, vp, i64, i, pp]
     L.beast_space_free.argtypes = [vp]
     L.beast_assemble.argtypes = [vp, C.POINTER(OpDesc), C.POINTER(QsDesc), vp, vp, i, vp, i64, i, i,

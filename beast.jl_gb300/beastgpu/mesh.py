@@ -18,6 +18,8 @@ class Mesh:
         self.cells = np.ascontiguousarray(cells, dtype=np.int32)
         assert self.vertices.ndim == 2 and self.vertices.shape[1] == 3
         assert self.cells.ndim == 2 and self.cells.shape[1] == 3
+        # the Refinement this mesh is the fine side of (CompScienceMeshes.parent), if any
+        self.refinement = None
 
     def numcells(self):
         return self.cells.shape[0]
@@ -41,6 +43,12 @@ class Mesh:
         v = self.vertices[self.cells]
         e = np.concatenate([v[:, 1] - v[:, 0], v[:, 2] - v[:, 1], v[:, 0] - v[:, 2]])
         return float(np.linalg.norm(e, axis=1).mean())
+
+
+def refines(fine, coarse):
+    """CompScienceMeshes.refines: `fine` is a refinement of `coarse` made here"""
+    R = getattr(fine, "refinement", None)
+    return R is not None and R.coarse is coarse
 
 
 def readmesh(path):

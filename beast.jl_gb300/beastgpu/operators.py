@@ -16,6 +16,7 @@ from . import spaces as _sp
 # operator kind codes shared with the C ABI (include/beastgpu.h)
 MW_SL, MW_DL, MW_NXDL, HH_SL, HH_DL, HH_DLT = 1, 2, 3, 4, 5, 6
 QS_WILTON_SAUTER, QS_SAUTER, QS_DOUBLENUM = 1, 2, 3
+QS_TEST_REFINES_TRIAL, QS_TRIAL_REFINES_TEST = 4, 5
 
 
 def gamma_wavenumber_handler(gamma, wavenumber):
@@ -223,6 +224,32 @@ class DoubleNumQStrat:
     def orders(self):
         return (QS_DOUBLENUM, self.outer_rule, self.inner_rule, self.outer_rule,
                 self.inner_rule, 0, 0, 0, 0)
+
+
+@dataclass(frozen=True)
+class TestRefinesTrialQStrat:
+    """src/quadrature/strategies/testrefinestrialqstrat.jl:1-17: the test space lives on a
+    refinement of the trial space's mesh; pairs that share a vertex integrate the trial cell's
+    children with the wrapped strategy (rules/testrefinestrialqrule.jl:6-52)"""
+    __test__ = False  # not a pytest class
+    conforming_qstrat: DoubleNumWiltonSauterQStrat
+
+    def orders(self):
+        if not isinstance(self.conforming_qstrat, DoubleNumWiltonSauterQStrat):
+            raise ValueError("TestRefinesTrialQStrat wraps a DoubleNumWiltonSauterQStrat")
+        return (QS_TEST_REFINES_TRIAL,) + self.conforming_qstrat.orders()[1:]
+
+
+@dataclass(frozen=True)
+class TrialRefinesTestQStrat:
+    """src/quadrature/strategies/trialrefinestestqstrat.jl:1-17: the same with the trial space
+    on the refinement (rules/trialrefinestestqrule.jl:6-40)"""
+    conforming_qstrat: DoubleNumWiltonSauterQStrat
+
+    def orders(self):
+        if not isinstance(self.conforming_qstrat, DoubleNumWiltonSauterQStrat):
+            raise ValueError("TrialRefinesTestQStrat wraps a DoubleNumWiltonSauterQStrat")
+        return (QS_TRIAL_REFINES_TEST,) + self.conforming_qstrat.orders()[1:]
 
 
 def defaultquadstrat(op, tspace, bspace):

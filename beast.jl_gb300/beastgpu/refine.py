@@ -41,6 +41,21 @@ class Refinement:
     def children(self, c):
         return range(6 * c, 6 * c + 6)
 
+    def child_vertices(self):
+        """[coarse cells][6][3][3]: the vertices of every coarse cell's children, in the
+        children's own orientation (that of the parent)"""
+        nc = self.coarse.numcells()
+        return np.ascontiguousarray(self.fine.vertices[self.fine.cells[:6 * nc]].reshape(nc, 6, 3, 3))
+
+    def refined_space(self, X):
+        """refined(X, self), built once per coarse space"""
+        cache = self.__dict__.setdefault("_refined", {})
+        ent = cache.get(id(X))
+        if ent is None or ent[0] is not X:
+            ent = (X, refined(X, self))
+            cache[id(X)] = ent
+        return ent[1]
+
 
 def barycentric_refinement(mesh):
     V = mesh.vertices
@@ -67,7 +82,10 @@ def barycentric_refinement(mesh):
         g = int(centroid[c])
         cells[6 * c:6 * c + 6] = [(a, m(a, b), g), (m(a, b), b, g), (b, m(b, d), g),
                                   (m(b, d), d, g), (d, m(d, a), g), (m(d, a), a, g)]
-    return Refinement(mesh, Mesh(verts, cells), np.repeat(np.arange(nc), 6), midpoint, centroid)
+    fine = Mesh(verts, cells)
+    R = Refinement(mesh, fine, np.repeat(np.arange(nc), 6), midpoint, centroid)
+    fine.refinement = R
+    return R
 
 
 def _vertex_to_cells(cells, nv):

@@ -328,7 +328,28 @@ int beast_mesh_free(beast_mesh* m) {
   cudaStreamSynchronize(m->ctx->stream);
   cudaFree(m->verts);
   cudaFree(m->cells);
+  if (m->children) cudaFree(m->children);
   delete m;
+  return BEAST_OK;
+}
+
+int beast_mesh_set_children(beast_ctx* ctx, beast_mesh* m, int nchild, const double* child_verts) {
+  ARG_CHECK(ctx, ctx && m && child_verts, "null argument");
+  ARG_CHECK(ctx, nchild >= 1 && nchild <= MAX_CHILDREN, "nchild must be in 1..8");
+  ARG_CHECK(ctx, m->ctx == ctx, "the mesh belongs to another context");
+  if (set_device(ctx)) return BEAST_ERR_CUDA;
+  const size_t bytes = sizeof(double) * 9 * (size_t)nchild * (size_t)m->nc;
+  double* d = nullptr;
+  cudaError_t e = cudaMalloc(&d, bytes);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d, child_verts, bytes, cudaMemcpyHostToDevice, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) {
+    if (d) cudaFree(d);
+    return beast_fail(ctx, BEAST_ERR_CUDA, std::string("children upload: ") + cudaGetErrorString(e));
+  }
+  if (m->children) cudaFree(m->children);
+  m->children = d;
+  m->nchild = nchild;
   return BEAST_OK;
 }
 
@@ -483,7 +504,8 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
             "far rule degree not available (1..10)");
   // DoubleNumQStrat pairs that come close are evaluated by the near kernel too (class 4)
   const bool has_near = true;
-  if (qs->kind == BEAST_QS_WILTON_SAUTER) {
+  if (qs->kind == BEAST_QS_WILTON_SAUTER || qs->kind == BEAST_QS_TEST_REFINES_TRIAL ||
+      qs->kind == BEAST_QS_TRIAL_REFINES_TEST) {
     ARG_CHECK(ctx, make_trirule(qs->outer_near, &ron) && make_trirule(qs->inner_near, &rin),
               "near rule degree not available (1..10)");
   } else {
@@ -599,7 +621,7 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
       BEAST_CUDA_TRY(ctx, cudaStreamSynchronize(st));
       if (nnear > near_cap) return beast_fail(ctx, BEAST_ERR_ARG, "near-pair list overflow");
       ProfScope ps(ctx, PK_NEAR, (double)nnear, nnear > 0);
-      BEAST_CUDA_TRY(ctx, launch_near(a, nnear, ron, rin, st));
+      BEAST_CUDA_TRY(ctx, launch_near(a, nnear, ron, rin, ro, ri, st));
     }
     GatherArgs g;
     g.ts = ts;
@@ -645,13 +667,20 @@ int beast_assemble(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc*
                    int64_t ldz, int z_dtype, int z_loc, int64_t row_off, int64_t col_off,
                    double cr, double ci, int accumulate) {
   ARG_CHECK(ctx, ctx && op && qs && ts && bs && Z, "null argument");
-  ARG_CHECK(ctx, ts->mesh == bs->mesh, "test and trial spaces must share the mesh");
+  if (qs->kind == BEAST_QS_TEST_REFINES_TRIAL)
+    ARG_CHECK(ctx, bs->mesh->children && ts->kind == BEAST_RT && bs->kind == BEAST_RT,
+              "TestRefinesTrialQStrat: RT spaces and the trial mesh's children (beast_mesh_set_children)");
+  else if (qs->kind == BEAST_QS_TRIAL_REFINES_TEST)
+    ARG_CHECK(ctx, ts->mesh->children && ts->kind == BEAST_RT && bs->kind == BEAST_RT,
+              "TrialRefinesTestQStrat: RT spaces and the test mesh's children (beast_mesh_set_children)");
+  else
+    ARG_CHECK(ctx, ts->mesh == bs->mesh, "test and trial spaces must share the mesh");
   ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
             "unknown precision");
   ARG_CHECK(ctx, z_dtype == BEAST_C128 || z_dtype == BEAST_C64, "unknown matrix dtype");
   ARG_CHECK(ctx, row_off >= 0 && col_off >= 0 && ldz >= row_off + ts->nfuncs, "bad Z addressing");
   ARG_CHECK(ctx, op->kind >= BEAST_MW_SL && op->kind <= BEAST_HH_DLT, "unknown operator kind");
-  ARG_CHECK(ctx, qs->kind >= 1 && qs->kind <= 3, "unknown quadrature strategy");
+  ARG_CHECK(ctx, qs->kind >= 1 && qs->kind <= 5, "unknown quadrature strategy");
   if (set_device(ctx)) return BEAST_ERR_CUDA;
   const int zc = z_dtype == BEAST_C64;
   if (z_loc == BEAST_DEVICE)

@@ -141,6 +141,16 @@ DEV int classify_exact(const Geo& t, const Geo& s, int qs_kind, double k2) {
   return 0;
 }
 
+// TestRefinesTrialQStrat / TrialRefinesTestQStrat (src/quadrature/strategies/
+// testrefinestrialqstrat.jl:9-17, trialrefinestestqstrat.jl:9-17): a pair that shares a vertex
+// becomes class 5 (split the trial cell into its children) or 6 (split the test cell); every
+// other pair keeps the wrapped strategy's class
+DEV int refines_class(int cls, int qs_kind) {
+  if (cls > 0 && qs_kind == BEAST_QS_TEST_REFINES_TRIAL) return 5;
+  if (cls > 0 && qs_kind == BEAST_QS_TRIAL_REFINES_TEST) return 6;
+  return cls;
+}
+
 // squared distance below which a pair can be near (strategy threshold of the trial cell)
 DEV double near_threshold2(int qs_kind, double k2, double area) {
   if (qs_kind == BEAST_QS_DOUBLENUM) return -1.0;
@@ -305,7 +315,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far(FarParams P) {
         if (P.qs_kind != BEAST_QS_DOUBLENUM) {
           Geo t = load_geo(tg);
           Geo s = load_geo(P.bgeo + (int64_t)P.qcells[ql] * GEO_STRIDE);
-          cls = classify_exact(t, s, P.qs_kind, P.k2);
+          cls = refines_class(classify_exact(t, s, P.qs_kind, P.k2), P.qs_kind);
         }
         if (cls != 0) {
           int idx = atomicAdd(P.near_count, 1);
@@ -535,8 +545,11 @@ DEV void integrand(int kind, const OpParams& op, V3<double> x, V3<double> y, V3<
                    C2<double>* acc) {
   const int nt = tk == BEAST_P0 ? 1 : 3, nb = bk == BEAST_P0 ? 1 : 3;
   V3<double> r = x - y;
-  double R = sqrt(dot(r, r));
-  double iR = 1.0 / R;
+  // one reciprocal square root instead of a square root and a division (both long FP64
+  // sequences on GB300)
+  const double R2 = dot(r, r);
+  const double iR = rsqrt(R2);
+  const double R = R2 * iR;
   C2<double> gR{op.gr * R, op.gi * R};
   C2<double> al{op.ar, op.ai}, be{op.br, op.bi};
   switch (kind) {
@@ -550,7 +563,7 @@ DEV void integrand(int kind, const OpParams& op, V3<double> x, V3<double> y, V3<
         C2<double> e = cexpm1_d(C2<double>{-gR.re, -gR.im});
         C2<double> g2 = cmul(gR, gR);
         G = cadd(e, csub(gR, cscale(0.5, g2)));
-        G = cscale(1.0 / (4.0 * PI * R), G);
+        G = cscale(I4PI * iR, G);
       }
       C2<double> aG = cmul(al, G), bG = cmul(be, G);
       for (int i = 0; i < 3; ++i)
@@ -757,6 +770,15 @@ struct NearParams {
   const int* zcol;
   int* flag;
   TriRuleDev ro, ri;
+  // the refines strategies: the wrapped strategy's far rules (children far from the other
+  // cell), the coarse side's active cell -> mesh cell and the coarse mesh's children
+  TriRuleDev fro, fri;
+  const int* bcells;        // trial active cell -> trial mesh cell
+  const double* bchildren;  // [trial mesh cell][bnchild][9]
+  int bnchild;
+  const int* tcells;        // test active cell -> test mesh cell
+  const double* tchildren;  // [test mesh cell][tnchild][9]
+  int tnchild;
 };
 
 constexpr int NEAR_WARPS = 4;
@@ -958,6 +980,139 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss32(NearParams P) {
   }
 }
 
+// ---- per-node paths of a near pair, shared by near_pair and the children of the refines
+// strategies.  Each adds its lane's share of the block (lanes over nodes) to acc[i * nb + j].
+
+// DoubleQuadRule (src/quadrature/doublenumints.jl:12-43) of rules ro x ri point by point in
+// FP64 with the integrand of `kind` (REG + kind: the regular part of singularity extraction)
+DEV void dq_points(const NearParams& P, int kind, const Geo& t, const Geo& s, const TriRuleDev& ro,
+                   const TriRuleDev& ri, int lane, C2<double>* acc) {
+  Shp f, g;
+  const int no = ro.n, ni = ri.n;
+  for (int it = lane; it < no * ni; it += 32) {
+    const int a = it / ni, b = it % ni;
+    double bx[3] = {ro.u[a], ro.v[a], 1.0 - ro.u[a] - ro.v[a]};
+    double by[3] = {ri.u[b], ri.v[b], 1.0 - ri.u[b] - ri.v[b]};
+    V3<double> x = bx[0] * t.v[0] + bx[1] * t.v[1] + bx[2] * t.v[2];
+    V3<double> y = by[0] * s.v[0] + by[1] * s.v[1] + by[2] * s.v[2];
+    shapes(P.tk, t, x, bx, f);
+    shapes(P.bk, s, y, by, g);
+    integrand(kind, P.op, x, y, t.n, s.n, P.tk, f, P.bk, g, ro.w[a] * t.area * ri.w[b] * s.area, acc);
+  }
+}
+
+// Sauter-Schwab vertex order: shared vertices first, same order (SauterSchwabQuadrature.reorder)
+DEV void ss_order(const Geo& t, const Geo& s, int* pt, int* ps) {
+  const double dtol = 1.0e3 * 2.220446049250313e-16;
+  int hits = 0, ti[3], si[3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      V3<double> dd = t.v[i] - s.v[j];
+      if (sqrt(dot(dd, dd)) < dtol && hits < 3) {
+        ti[hits] = i;
+        si[hits] = j;
+        ++hits;
+      }
+    }
+  int k = 0;
+  for (int h = 0; h < hits; ++h) pt[k++] = ti[h];
+  for (int i = 0; i < 3; ++i) {
+    bool used = false;
+    for (int h = 0; h < hits; ++h) used |= ti[h] == i;
+    if (!used) pt[k++] = i;
+  }
+  k = 0;
+  for (int h = 0; h < hits; ++h) ps[k++] = si[h];
+  for (int j = 0; j < 3; ++j) {
+    bool used = false;
+    for (int h = 0; h < hits; ++h) used |= si[h] == j;
+    if (!used) ps[k++] = j;
+  }
+}
+
+// Sauter-Schwab rule of class cls (3 face, 2 edge, 1 vertex) node by node
+DEV void ss_points(const NearParams& P, const Geo& t, const Geo& s, int cls, const int* pt, const int* ps,
+                   const double* s_glx, const double* s_glw, int lane, C2<double>* acc) {
+  Shp f, g;
+  const int n = cls == 3 ? P.qs.ss_face : (cls == 2 ? P.qs.ss_edge : P.qs.ss_vert);
+  const int nreg = cls == 1 ? 2 : 6;
+  const int64_t items = (int64_t)nreg * n * n * n * n;
+  const double jac = 4.0 * t.area * s.area;
+  const double* glx = s_glx + c_gl_off[n - 1];
+  const double* glw = s_glw + c_gl_off[n - 1];
+  for (int64_t it = lane; it < items; it += 32) {
+    double X[2], Y[2], w;
+    ss_node(cls, n, it, glx, glw, X, Y, &w);
+    double lt[3] = {1.0 - X[0], X[0] - X[1], X[1]}, ls[3] = {1.0 - Y[0], Y[0] - Y[1], Y[1]};
+    double bx[3], by[3];
+    for (int q = 0; q < 3; ++q) {
+      bx[pt[q]] = lt[q];
+      by[ps[q]] = ls[q];
+    }
+    V3<double> x = lt[0] * t.v[pt[0]] + lt[1] * t.v[pt[1]] + lt[2] * t.v[pt[2]];
+    V3<double> y = ls[0] * s.v[ps[0]] + ls[1] * s.v[ps[1]] + ls[2] * s.v[ps[2]];
+    shapes(P.tk, t, x, bx, f);
+    shapes(P.bk, s, y, by, g);
+    integrand(P.op.kind, P.op, x, y, t.n, s.n, P.tk, f, P.bk, g, w * jac, acc);
+  }
+}
+
+// singularity extraction: the regular part by the near rules, the analytic inner part per
+// outer point
+DEV void se_points(const NearParams& P, const Geo& t, const Geo& s, int lane, C2<double>* acc) {
+  dq_points(P, REG + P.op.kind, t, s, P.ro, P.ri, lane, acc);
+  for (int a = lane; a < P.ro.n; a += 32) {
+    double bx[3] = {P.ro.u[a], P.ro.v[a], 1.0 - P.ro.u[a] - P.ro.v[a]};
+    V3<double> x = bx[0] * t.v[0] + bx[1] * t.v[1] + bx[2] * t.v[2];
+    if (!se_singular(P.op, P.tk, P.bk, t, s, x, bx, P.ro.w[a] * t.area, acc)) atomicOr(P.flag, 2);
+  }
+}
+
+// double-layer type kernels vanish identically on a flat common face
+DEV bool dl_type(int kind) { return kind == BEAST_MW_DL || kind == BEAST_HH_DL || kind == BEAST_HH_DLT; }
+
+// the wrapped DoubleNumWiltonSauterQStrat on one pair of triangles, any class
+DEV void pair_points(const NearParams& P, const Geo& t, const Geo& s, int cls, const double* s_glx,
+                     const double* s_glw, int lane, C2<double>* acc) {
+  if (cls == 0) {
+    dq_points(P, P.op.kind, t, s, P.fro, P.fri, lane, acc);
+  } else if (cls > 0) {
+    if (cls == 3 && dl_type(P.op.kind)) return;
+    int pt[3], ps[3];
+    ss_order(t, s, pt, ps);
+    ss_points(P, t, s, cls, pt, ps, s_glx, s_glw, lane, acc);
+  } else {
+    se_points(P, t, s, lane, acc);
+  }
+}
+
+// the triangle of 9 vertex coordinates as a Geo
+DEV Geo geo_of_triangle(const double* v) {
+  Geo g;
+  for (int i = 0; i < 3; ++i) g.v[i] = mk(v[3 * i], v[3 * i + 1], v[3 * i + 2]);
+  const V3<double> cr = cross(g.v[0] - g.v[2], g.v[1] - g.v[2]);
+  const double j = sqrt(dot(cr, cr));
+  g.c = (1.0 / 3.0) * (g.v[0] + g.v[1] + g.v[2]);
+  g.n = (1.0 / j) * cr;
+  g.area = 0.5 * j;
+  return g;
+}
+
+// RT shape j of `parent` on its child `ch`: sum_k Q[j][k] (child shape k), Q[j][k] the flux of
+// shape j through the child's edge k (an RT shape has unit outward flux through its own edge):
+// |e_k| (m_k - v_j).n_k / (2 A), n_k the edge's outward unit normal, m_k a point of the edge
+// (the RT interpolation of src/bases/local/rtlocal.jl:82-111)
+DEV void rt_restriction(const Geo& parent, const Geo& ch, double Q[3][3]) {
+  for (int k = 0; k < 3; ++k) {
+    const V3<double> a = ch.v[(k + 1) % 3], b = ch.v[(k + 2) % 3];
+    V3<double> nk = cross(b - a, ch.n);
+    nk = (1.0 / sqrt(dot(nk, nk))) * nk;
+    if (dot(ch.v[k] - a, nk) > 0) nk = -1.0 * nk;
+    const double len = sqrt(dot(b - a, b - a));
+    for (int j = 0; j < 3; ++j) Q[j][k] = len * dot(a - parent.v[j], nk) / (2.0 * parent.area);
+  }
+}
+
 // one near pair, by one warp (lane = its lane); s_glx / s_glw: the Gauss-Legendre table in
 // shared memory (lanes read different nodes: a constant-memory read would serialise)
 DEV void near_pair(const NearParams& P, const NearPair np_, const double* s_glx, const double* s_glw, int lane) {
@@ -967,16 +1122,14 @@ DEV void near_pair(const NearParams& P, const NearPair np_, const double* s_glx,
   const int nt = P.tk == BEAST_P0 ? 1 : 3, nb = P.bk == BEAST_P0 ? 1 : 3;
   C2<double> acc[9];
   for (int k = 0; k < 9; ++k) acc[k] = C2<double>{0, 0};
-  Shp f, g;
-  bool dl_face = np_.cls == 3 && (P.op.kind == BEAST_MW_DL || P.op.kind == BEAST_HH_DL ||
-                                  P.op.kind == BEAST_HH_DLT);
+  const bool dl_face = np_.cls == 3 && dl_type(P.op.kind);
+  if (np_.cls >= 5) return;  // k_near_refines
   if (np_.cls == 4) {
     // ---- DoubleNumQStrat pair close to its partner: the pair's own DoubleQuadRule
     // (src/quadrature/doublenumints.jl:12-43) point by point in FP64, lanes over point pairs.
     // Double-layer type kernels vanish identically on a common face (every vector of the
     // triple product lies in the flat triangle): that block stays 0 rather than summed noise.
-    const bool dl_kind = P.op.kind == BEAST_MW_DL || P.op.kind == BEAST_MW_NXDL || P.op.kind == BEAST_HH_DL ||
-                         P.op.kind == BEAST_HH_DLT;
+    const bool dl_kind = dl_type(P.op.kind) || P.op.kind == BEAST_MW_NXDL;
     int hits = 0;
     if (dl_kind)
       for (int i = 0; i < 3; ++i)
@@ -984,49 +1137,13 @@ DEV void near_pair(const NearParams& P, const NearPair np_, const double* s_glx,
           const V3<double> dd = t.v[i] - s.v[j];
           hits += sqrt(dot(dd, dd)) < 1.0e3 * 2.220446049250313e-16;
         }
-    const int no = P.ro.n, ni = (dl_kind && hits == 3) ? 0 : P.ri.n;
-    for (int it = lane; it < no * ni; it += 32) {
-      const int a = it / ni, b = it % ni;
-      double bx[3] = {P.ro.u[a], P.ro.v[a], 1.0 - P.ro.u[a] - P.ro.v[a]};
-      double by[3] = {P.ri.u[b], P.ri.v[b], 1.0 - P.ri.u[b] - P.ri.v[b]};
-      V3<double> x = bx[0] * t.v[0] + bx[1] * t.v[1] + bx[2] * t.v[2];
-      V3<double> y = by[0] * s.v[0] + by[1] * s.v[1] + by[2] * s.v[2];
-      shapes(P.tk, t, x, bx, f);
-      shapes(P.bk, s, y, by, g);
-      integrand(P.op.kind, P.op, x, y, t.n, s.n, P.tk, f, P.bk, g, P.ro.w[a] * t.area * P.ri.w[b] * s.area,
-                acc);
-    }
+    if (!(dl_kind && hits == 3)) dq_points(P, P.op.kind, t, s, P.ro, P.ri, lane, acc);
   } else if (np_.cls >= 1 && !dl_face) {
-    // ---- Sauter-Schwab: shared vertices first, same order (SauterSchwabQuadrature.reorder)
-    const double dtol = 1.0e3 * 2.220446049250313e-16;
-    int pt[3], ps[3], hits = 0, ti[3], si[3];
-    for (int i = 0; i < 3; ++i)
-      for (int j = 0; j < 3; ++j) {
-        V3<double> dd = t.v[i] - s.v[j];
-        if (sqrt(dot(dd, dd)) < dtol && hits < 3) {
-          ti[hits] = i;
-          si[hits] = j;
-          ++hits;
-        }
-      }
-    int k = 0;
-    for (int h = 0; h < hits; ++h) pt[k++] = ti[h];
-    for (int i = 0; i < 3; ++i) {
-      bool used = false;
-      for (int h = 0; h < hits; ++h) used |= ti[h] == i;
-      if (!used) pt[k++] = i;
-    }
-    k = 0;
-    for (int h = 0; h < hits; ++h) ps[k++] = si[h];
-    for (int j = 0; j < 3; ++j) {
-      bool used = false;
-      for (int h = 0; h < hits; ++h) used |= si[h] == j;
-      if (!used) ps[k++] = j;
-    }
+    int pt[3], ps[3];
+    ss_order(t, s, pt, ps);
     const int n = np_.cls == 3 ? P.qs.ss_face : (np_.cls == 2 ? P.qs.ss_edge : P.qs.ss_vert);
     const int nreg = np_.cls == 1 ? 2 : 6;
     const int64_t items = (int64_t)nreg * n * n * n * n;
-    const double jac = 4.0 * t.area * s.area;
     const double* glx = s_glx + c_gl_off[n - 1];
     const double* glw = s_glw + c_gl_off[n - 1];
     const bool mw_rt = P.tk == BEAST_RT && P.bk == BEAST_RT &&
@@ -1051,8 +1168,9 @@ DEV void near_pair(const NearParams& P, const NearPair np_, const double* s_glx,
         const V3<double> xi = lt[0] * (t.v[pt[0]] - cp) + lt[1] * (t.v[pt[1]] - cp) + lt[2] * (t.v[pt[2]] - cp);
         const V3<double> eta = ls[0] * (s.v[ps[0]] - cq) + ls[1] * (s.v[ps[1]] - cq) + ls[2] * (s.v[ps[2]] - cq);
         const V3<double> r = (d + xi) - eta;
-        const double R = sqrt(dot(r, r));
-        const double iR = 1.0 / R;
+        const double R2 = dot(r, r);
+        const double iR = rsqrt(R2);
+        const double R = R2 * iR;
         double sn, cs;
         sincos(gi * R, &sn, &cs);
         const double amp = (gr == 0.0 ? 1.0 : exp(-gr * R)) * I4PI * iR * w;
@@ -1114,40 +1232,9 @@ DEV void near_pair(const NearParams& P, const NearPair np_, const double* s_glx,
       }
       return;
     }
-    for (int64_t it = lane; it < items; it += 32) {
-      double X[2], Y[2], w;
-      ss_node(np_.cls, n, it, glx, glw, X, Y, &w);
-      double lt[3] = {1.0 - X[0], X[0] - X[1], X[1]}, ls[3] = {1.0 - Y[0], Y[0] - Y[1], Y[1]};
-      double bx[3], by[3];
-      for (int q = 0; q < 3; ++q) {
-        bx[pt[q]] = lt[q];
-        by[ps[q]] = ls[q];
-      }
-      V3<double> x = lt[0] * t.v[pt[0]] + lt[1] * t.v[pt[1]] + lt[2] * t.v[pt[2]];
-      V3<double> y = ls[0] * s.v[ps[0]] + ls[1] * s.v[ps[1]] + ls[2] * s.v[ps[2]];
-      shapes(P.tk, t, x, bx, f);
-      shapes(P.bk, s, y, by, g);
-      integrand(P.op.kind, P.op, x, y, t.n, s.n, P.tk, f, P.bk, g, w * jac, acc);
-    }
+    ss_points(P, t, s, np_.cls, pt, ps, s_glx, s_glw, lane, acc);
   } else if (np_.cls == -1) {
-    // ---- singularity extraction: regular part by DQ (near rules) + analytic inner part
-    const int no = P.ro.n, ni = P.ri.n;
-    for (int it = lane; it < no * ni; it += 32) {
-      int a = it / ni, b = it % ni;
-      double bx[3] = {P.ro.u[a], P.ro.v[a], 1.0 - P.ro.u[a] - P.ro.v[a]};
-      double by[3] = {P.ri.u[b], P.ri.v[b], 1.0 - P.ri.u[b] - P.ri.v[b]};
-      V3<double> x = bx[0] * t.v[0] + bx[1] * t.v[1] + bx[2] * t.v[2];
-      V3<double> y = by[0] * s.v[0] + by[1] * s.v[1] + by[2] * s.v[2];
-      shapes(P.tk, t, x, bx, f);
-      shapes(P.bk, s, y, by, g);
-      integrand(REG + P.op.kind, P.op, x, y, t.n, s.n, P.tk, f, P.bk, g,
-                P.ro.w[a] * t.area * P.ri.w[b] * s.area, acc);
-    }
-    for (int a = lane; a < no; a += 32) {
-      double bx[3] = {P.ro.u[a], P.ro.v[a], 1.0 - P.ro.u[a] - P.ro.v[a]};
-      V3<double> x = bx[0] * t.v[0] + bx[1] * t.v[1] + bx[2] * t.v[2];
-      if (!se_singular(P.op, P.tk, P.bk, t, s, x, bx, P.ro.w[a] * t.area, acc)) atomicOr(P.flag, 2);
-    }
+    se_points(P, t, s, lane, acc);
   }
   // ---- warp reduction and store
   for (int k = 0; k < nt * nb; ++k) {
@@ -1177,6 +1264,66 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near(NearParams P) {
   const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
   if (e >= P.nnear) return;
   near_pair(P, P.near[e], s_glx, s_glw, lane);
+}
+
+// the pairs of the refines strategies (classes 5 and 6), one per warp: a kernel of their own
+// so that the children loop does not set k_near's register budget
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_refines(NearParams P) {
+  __shared__ double s_glx[210], s_glw[210];
+  for (int k = threadIdx.x; k < 210; k += blockDim.x) {
+    s_glx[k] = c_gl_x[k];
+    s_glw[k] = c_gl_w[k];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
+  if (e >= P.nnear) return;
+  const NearPair np_ = P.near[e];
+  if (np_.cls < 5) return;
+  const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
+  const Geo s = load_geo(P.bgeo + (int64_t)(P.qcells ? P.qcells[np_.q] : np_.q) * GEO_STRIDE);
+  C2<double> acc[9];
+  for (int k = 0; k < 9; ++k) acc[k] = C2<double>{0, 0};
+  // ---- the refines strategies (src/quadrature/rules/testrefinestrialqrule.jl:6-52,
+  // trialrefinestestqrule.jl:6-40): the pair shares a vertex, so the coarse cell (trial for
+  // class 5, test for class 6) is split into its children, each child integrated against the
+  // other cell with the wrapped strategy (its own class), the coarse RT shapes restricted to
+  // the child.  The restriction is linear, so it applies to each lane's share.
+  const bool split_trial = np_.cls == 5;
+  const Geo& parent = split_trial ? s : t;
+  const int nchild = split_trial ? P.bnchild : P.tnchild;
+  const double* ch = split_trial
+                         ? P.bchildren + (int64_t)P.bcells[P.qcells ? P.qcells[np_.q] : np_.q] * nchild * 9
+                         : P.tchildren + (int64_t)P.tcells[P.tperm[np_.p]] * nchild * 9;
+  const double k2 = P.op.gr * P.op.gr + P.op.gi * P.op.gi;
+  for (int c = 0; c < nchild; ++c) {
+    const Geo g = geo_of_triangle(ch + 9 * c);
+    const Geo& tt = split_trial ? t : g;
+    const Geo& ss = split_trial ? g : s;
+    C2<double> B[9];
+    for (int k = 0; k < 9; ++k) B[k] = C2<double>{0, 0};
+    pair_points(P, tt, ss, classify_exact(tt, ss, BEAST_QS_WILTON_SAUTER, k2), s_glx, s_glw, lane, B);
+    double Q[3][3];
+    rt_restriction(parent, g, Q);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k)
+          acc[i * 3 + j] = cadd(acc[i * 3 + j], split_trial ? cscale(Q[j][k], B[i * 3 + k])
+                                                            : cscale(Q[i][k], B[k * 3 + j]));
+  }
+  for (int k = 0; k < 9; ++k) {
+    double re = acc[k].re, im = acc[k].im;
+    for (int o = 16; o > 0; o >>= 1) {
+      re += __shfl_xor_sync(0xffffffffu, re, o);
+      im += __shfl_xor_sync(0xffffffffu, im, o);
+    }
+    acc[k] = C2<double>{re, im};
+  }
+  if (lane == 0)
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        store_c<double>(P.zcell, zidx(zrow_of(P.zrow, np_.p, 3, i), zcol_of(P.zcol, np_.q, 3, j), P.ldc),
+                        acc[i * 3 + j], P.zfmt);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1498,6 +1645,7 @@ __global__ void __launch_bounds__(256) k_gather_e(GatherArgs G, const int64_t* t
   __shared__ int64_t s_c0[GATHER_NCOL];  // first Zcell column (element offset) of trial function n
   __shared__ int s_nc[GATHER_NCOL];
   __shared__ double s_b[GATHER_NCOL][GATHER_E_MAX];
+  __shared__ dfl::df s_bd[GATHER_NCOL][GATHER_E_MAX];  // the same as pairs (double-float blocks)
   if (threadIdx.x < GATHER_NCOL) {
     const int64_t n = nb0 + threadIdx.x;
     if (n < nb1) {
@@ -1505,13 +1653,19 @@ __global__ void __launch_bounds__(256) k_gather_e(GatherArgs G, const int64_t* t
       const int c = (int)(bptr[n + 1] - f0);
       s_c0[threadIdx.x] = (f0 - G.f0) * G.ldc;
       s_nc[threadIdx.x] = c;
-      for (int k = 0; k < GATHER_E_MAX; ++k) s_b[threadIdx.x][k] = k < c ? bcoef[f0 + k] : 0.0;
+      for (int k = 0; k < GATHER_E_MAX; ++k) {
+        s_b[threadIdx.x][k] = k < c ? bcoef[f0 + k] : 0.0;
+        if (ZC == ZCELL_DF) s_bd[threadIdx.x][k] = df_coef(s_b[threadIdx.x][k]);
+      }
     }
   }
   __syncthreads();
   if (m >= nrows) return;
   const int64_t e0 = tptr[m];
   const int ne = (int)(tptr[m + 1] - e0);
+  dfl::df tcd[GATHER_E_MAX];  // the test coefficients as pairs, split once per thread
+  if (ZC == ZCELL_DF)
+    for (int e = 0; e < GATHER_E_MAX; ++e) tcd[e] = e < ne ? df_coef(tcoef[e0 + e]) : dfl::make(0.f);
   const bool unit = G.cr == 1.0 && G.ci == 0.0;
   auto out = [&](int64_t n, double vr, double vi) {
     if (!unit) {
@@ -1547,8 +1701,10 @@ __global__ void __launch_bounds__(256) k_gather_e(GatherArgs G, const int64_t* t
       const float4* zc = reinterpret_cast<const float4*>(G.zcell);
       dfl::df re = dfl::make(0.f), im = dfl::make(0.f);
       for (int f = 0; f < nc; ++f) {
-        const dfl::df b = df_coef(f < GATHER_E_MAX ? s_b[nn][f] : bcoef[bptr[n] + f]);
-        for (int e = 0; e < ne; ++e) df_acc(re, im, zc[c0 + (int64_t)f * G.ldc + e], dfl::mul(df_coef(tcoef[e0 + e]), b));
+        const dfl::df b = f < GATHER_E_MAX ? s_bd[nn][f] : df_coef(bcoef[bptr[n] + f]);
+        for (int e = 0; e < ne; ++e)
+          df_acc(re, im, zc[c0 + (int64_t)f * G.ldc + e],
+                 dfl::mul(e < GATHER_E_MAX ? tcd[e] : df_coef(tcoef[e0 + e]), b));
       }
       if (OC64) {
         out(n, (double)dfl::add_rn(re.hi, re.lo), (double)dfl::add_rn(im.hi, im.lo));
@@ -1925,6 +2081,9 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_batch(BatchLaunch L) {
     P.flag = L.flag;
     P.ro = L.ron;
     P.ri = L.rin;
+    P.bcells = P.tcells = nullptr;  // no refines strategies in a batch
+    P.bchildren = P.tchildren = nullptr;
+    P.bnchild = P.tnchild = 0;
     near_pair(P, NearPair{nb.p, nb.q, nb.cls, 0}, s_glx, s_glw, lane);
   }
 }
@@ -2044,7 +2203,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
       if (dd <= lim * lim * 1.0001f + 1e-30f) {
         Geo t = load_geo(tg);
         Geo s = load_geo(P.bgeo + (int64_t)P.qcells[ql] * GEO_STRIDE);
-        const int cls = classify_exact(t, s, P.qs_kind, P.k2);
+        const int cls = refines_class(classify_exact(t, s, P.qs_kind, P.k2), P.qs_kind);
         if (cls != 0) {
           const int idx = atomicAdd(P.near_count, 1);
           if (idx < P.near_cap)
@@ -2185,7 +2344,7 @@ cudaError_t launch_near_batch(const BatchLaunch& L, cudaStream_t st) {
 }
 
 cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const TriRuleDev& ri,
-                        cudaStream_t st) {
+                        const TriRuleDev& fro, const TriRuleDev& fri, cudaStream_t st) {
   if (nnear <= 0) return cudaSuccess;
   cudaError_t e = upload_gl(st);
   if (e != cudaSuccess) return e;
@@ -2209,9 +2368,19 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   P.flag = a.flag;
   P.ro = ro;
   P.ri = ri;
+  P.fro = fro;
+  P.fri = fri;
+  P.bcells = a.bs->cells;
+  P.bchildren = a.bs->mesh->children;
+  P.bnchild = a.bs->mesh->nchild;
+  P.tcells = a.ts->cells;
+  P.tchildren = a.ts->mesh->children;
+  P.tnchild = a.ts->mesh->nchild;
   unsigned blocks = (unsigned)((nnear + NEAR_WARPS - 1) / NEAR_WARPS);
   if (P.ss32) k_near_ss32<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   k_near<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
+  if (P.qs.kind == BEAST_QS_TEST_REFINES_TRIAL || P.qs.kind == BEAST_QS_TRIAL_REFINES_TEST)
+    k_near_refines<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   return cudaGetLastError();
 }
 

@@ -4,8 +4,8 @@
 // works on the FP32 pipes.
 //   hi: the sign, the exponent and the top 23 stored mantissa bits (a truncation, so
 //       |lo| < 2^-23 |hi|);
-//   lo: the remaining 29 mantissa bits converted to float (rounded to 24 bits) and scaled by
-//       2^(e - 1075), with the sign of a.
+//   lo: the remaining 29 mantissa bits times 2^(e - 1075), truncated to 24 significant bits,
+//       with the sign of a, built from the bits with integer instructions only.
 // |a| < 2^-97 gives 0 + 0, and lo is dropped below |a| = 2^-74: absolute errors below 1e-29,
 // far under the FP64 rounding of a matvec of boundary-element entries.  |a| >= 2^128 (not a
 // BEM matrix entry) overflows to +-inf, so the matvec reports it instead of hiding it.  Host
@@ -50,6 +50,15 @@ FS_HD uint32_t to_bits(float f) {
 #endif
 }
 
+// leading zeros of a nonzero 32-bit word
+FS_HD int clz32(uint32_t x) {
+#if defined(__CUDA_ARCH__)
+  return __clz((int)x);
+#else
+  return __builtin_clz(x);
+#endif
+}
+
 // (hi, lo) of a
 FS_HD void split_f64(double a, float* hi, float* lo) {
   const uint64_t u = bits64(a);
@@ -68,11 +77,13 @@ FS_HD void split_f64(double a, float* hi, float* lo) {
   }
   *hi = from_bits(sgn | ((uint32_t)(e - 896) << 23) | (uint32_t)((u >> 29) & 0x7FFFFFu));
   *lo = 0.f;
-  if (e >= 949) {
-    const float scale = from_bits((uint32_t)(e - 948) << 23);  // 2^(e - 1075), exact
-    // the 29-bit integer rounds to 24 bits in the conversion; the power-of-two scaling is exact
-    const float m = (float)(uint32_t)(u & 0x1FFFFFFFu);
-    *lo = from_bits(to_bits(m * scale) | sgn);
+  const uint32_t m = (uint32_t)(u & 0x1FFFFFFFu);
+  if (m != 0) {
+    // m = 2^p (1 + f): biased float exponent p + (e - 1075) + 127, mantissa the 23 bits below
+    // the leading one (truncated); results below the normal float range are dropped
+    const int p = 31 - clz32(m);
+    const int be = p + e - 948;
+    if (be >= 1) *lo = from_bits(sgn | ((uint32_t)be << 23) | (((m << (31 - p)) >> 8) & 0x7FFFFFu));
   }
 }
 

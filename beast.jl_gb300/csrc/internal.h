@@ -65,11 +65,15 @@ struct ProfScope {
   ~ProfScope();
 };
 
+constexpr int MAX_CHILDREN = 8;
 struct beast_mesh {
   beast_ctx* ctx = nullptr;
   int64_t nv = 0, nc = 0;
   double* verts = nullptr;   // [nv][3]
   int* cells = nullptr;      // [nc][3] 0-based
+  // the cells' children in a refinement (beast_mesh_set_children): [nc][nchild][9] or null
+  double* children = nullptr;
+  int nchild = 0;
 };
 
 // per active cell geometry, 16 doubles: v0 v1 v2 (9) | centroid (3) | unit normal (3) | area
@@ -171,8 +175,10 @@ struct AsmArgs {
 cudaError_t launch_geometry(const beast_space* s, cudaStream_t st);
 cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev& ri,
                        cudaStream_t st);
+// ro_far / ri_far: the far rules, for the children of the refines strategies
 cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro_near,
-                        const TriRuleDev& ri_near, cudaStream_t st);
+                        const TriRuleDev& ri_near, const TriRuleDev& ro_far, const TriRuleDev& ri_far,
+                        cudaStream_t st);
 struct GatherArgs {
   const beast_space* ts;
   const beast_space* bs;

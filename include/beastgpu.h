@@ -56,7 +56,20 @@ enum {
 enum {
   BEAST_QS_WILTON_SAUTER = 1, /* DoubleNumWiltonSauterQStrat src/quadrature/doublenumwiltonsauterqstrat.jl:1-69 */
   BEAST_QS_SAUTER = 2,        /* DoubleNumSauterQstrat src/quadrature/doublenumsauterqstrat.jl:1-27          */
-  BEAST_QS_DOUBLENUM = 3      /* DoubleNumQStrat src/quadrature/doublenumqstrat.jl:1-32                     */
+  BEAST_QS_DOUBLENUM = 3,     /* DoubleNumQStrat src/quadrature/doublenumqstrat.jl:1-32                     */
+  BEAST_QS_TEST_REFINES_TRIAL = 4, /* TestRefinesTrialQStrat(DoubleNumWiltonSauterQStrat(...)),
+                                 src/quadrature/strategies/testrefinestrialqstrat.jl:1-17 with
+                                 rules/testrefinestrialqrule.jl:1-52: the test space lives on a
+                                 refinement of the trial space's mesh (beast_mesh_set_children on
+                                 the trial mesh); a pair that shares a vertex integrates the trial
+                                 cell's children with the wrapped strategy, every other pair the
+                                 wrapped strategy on the trial cell itself.  RT x RT; orders as for
+                                 DoubleNumWiltonSauter. */
+  BEAST_QS_TRIAL_REFINES_TEST = 5  /* TrialRefinesTestQStrat(DoubleNumWiltonSauterQStrat(...)),
+                                 src/quadrature/strategies/trialrefinestestqstrat.jl:1-17 with
+                                 rules/trialrefinestestqrule.jl:1-40: the same with the roles
+                                 swapped (the trial space on the refinement, the test cell split
+                                 into its children; children registered on the test mesh). */
 };
 
 /* ---- precision of assembly and solve */
@@ -131,6 +144,12 @@ int beast_ctx_set_wait_limit(beast_ctx* ctx, int64_t polls);
 int beast_mesh_upload(beast_ctx* ctx, const double* verts, int64_t nv, const int32_t* cells,
                       int64_t nc, int index_base, beast_mesh** out);
 int beast_mesh_free(beast_mesh* mesh);
+/* the children of every cell of `coarse` in a refinement (CompScienceMeshes.children of the
+ * barycentric refinement that Buffa-Christiansen spaces live on): child_verts [nc][nchild][3][3]
+ * float64, the vertices of each child triangle, oriented like its parent; nchild <= 8.
+ * Needed by BEAST_QS_TEST_REFINES_TRIAL (trial space on `coarse`) and
+ * BEAST_QS_TRIAL_REFINES_TEST (test space on `coarse`).  A second call replaces the first. */
+int beast_mesh_set_children(beast_ctx* ctx, beast_mesh* coarse, int nchild, const double* child_verts);
 
 /* replaces assemblydata(basis) (src/bases/basis.jl:235-294): the active cells
  * (act_to_global, `cells`, [ncells]) and AssemblyData.data split into two arrays of

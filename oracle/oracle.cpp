@@ -960,6 +960,48 @@ Tri mesh_tri(const orc_mesh* m, int64_t c) {
   return make_tri(p);
 }
 
+// RT shapes of `parent` on its child `ch` (src/bases/local/interpolate.jl:61-75 with the RT
+// interpolation of src/bases/local/rtlocal.jl:82-111): Q[j][k] = f_j(m_k) . (t_k x n), the
+// flux of parent shape j through the child's edge k (t_k the edge vector, so |t_k x n| = |e_k|,
+// oriented outward).
+void rt_restrict(const Tri& parent, const Tri& ch, double Q[3][3]) {
+  for (int k = 0; k < 3; ++k) {
+    const V3 a = ch.v[(k + 1) % 3], b = ch.v[(k + 2) % 3];
+    V3 m = cross(b - a, ch.n);
+    if (dot(ch.v[k] - a, m) > 0) m = -1.0 * m;
+    const V3 mid = 0.5 * (a + b);
+    for (int j = 0; j < 3; ++j) Q[j][k] = dot((1.0 / (2.0 * parent.area)) * (mid - parent.v[j]), m);
+  }
+}
+
+// TestRefinesTrialQStrat / TrialRefinesTestQStrat (src/quadrature/strategies/
+// testrefinestrialqstrat.jl:9-17, trialrefinestestqstrat.jl:9-17): a pair sharing a vertex
+// integrates the coarse cell's children one by one with the wrapped strategy and maps the
+// child blocks back through the restriction (rules/testrefinestrialqrule.jl:6-52,
+// rules/trialrefinestestqrule.jl:6-40); every other pair uses the wrapped strategy whole.
+// `children`: [coarse mesh cell][nchild][9]; split_test selects the trial-refines-test form.
+void refines_block(const Op& op, const orc_qs& qs, const Tri& t, const Tri& s, int64_t coarse_cell,
+                   const double* children, int nchild, int split_test, cplx* z) {
+  if (classify(op, qs, t, s) <= 0) {
+    pair_block(op, qs, ORC_RT, ORC_RT, t, s, z);
+    return;
+  }
+  const Tri& parent = split_test ? t : s;
+  for (int c = 0; c < nchild; ++c) {
+    const Tri ch = make_tri(children + (coarse_cell * nchild + c) * 9);
+    cplx b[9] = {};
+    if (split_test)
+      pair_block(op, qs, ORC_RT, ORC_RT, ch, s, b);
+    else
+      pair_block(op, qs, ORC_RT, ORC_RT, t, ch, b);
+    double Q[3][3];
+    rt_restrict(parent, ch, Q);
+    for (int i = 0; i < 3; ++i)
+      for (int j = 0; j < 3; ++j)
+        for (int k = 0; k < 3; ++k) z[i * 3 + j] += split_test ? Q[i][k] * b[k * 3 + j] : b[i * 3 + k] * Q[j][k];
+  }
+}
+
 }  // namespace
 
 extern "C" int orc_trirule(int degree, double* uv, double* w, int cap) {
@@ -1062,6 +1104,59 @@ extern "C" int orc_assemble(const orc_op* o, const orc_qs* qs, const orc_mesh* m
   for (int t = 0; t < nthreads; ++t) th.emplace_back(worker, t);
   for (auto& t : th) t.join();
   return bad.load();
+}
+
+// Dense assembly of RT x RT pairs across a refinement: the test space on `tmesh`, the trial
+// space on `bmesh`, one of them the barycentric refinement of the other (operator.jl:256-262
+// picks the strategy from which mesh refines which).  Layout and threading as orc_assemble.
+extern "C" int orc_assemble_refines(const orc_op* o, const orc_qs* qs, const orc_mesh* tmesh,
+                                    const orc_mesh* bmesh, const orc_space* ts, const orc_space* bs,
+                                    const double* children, int nchild, int split_test, double* Z,
+                                    int64_t ldz, int nthreads) {
+  if (ts->kind != ORC_RT || bs->kind != ORC_RT || qs->kind != ORC_QS_WILTON_SAUTER) return -1;
+  Op op = make_op(o);
+  if (nthreads < 1) nthreads = 1;
+  std::vector<Tri> ttri(ts->ncells), btri(bs->ncells);
+  for (int64_t c = 0; c < ts->ncells; ++c) ttri[c] = mesh_tri(tmesh, ts->cells[c]);
+  for (int64_t c = 0; c < bs->ncells; ++c) btri[c] = mesh_tri(bmesh, bs->cells[c]);
+  const int64_t nrows = ts->nfuncs;
+  auto worker = [&](int tid) {
+    const int64_t lo = nrows * tid / nthreads, hi = nrows * (tid + 1) / nthreads;
+    if (hi <= lo) return;
+    for (int64_t p = 0; p < ts->ncells; ++p) {
+      bool act = false;
+      for (int r = 0; r < 3 && !act; ++r)
+        for (int k = 0; k < ts->maxfn; ++k) {
+          const int64_t m = ts->ad_dof[(p * 3 + r) * ts->maxfn + k];
+          if (m >= lo && m < hi) act = true;
+        }
+      if (!act) continue;
+      for (int64_t q = 0; q < bs->ncells; ++q) {
+        cplx z[9] = {};
+        refines_block(op, *qs, ttri[p], btri[q], split_test ? ts->cells[p] : bs->cells[q], children, nchild,
+                      split_test, z);
+        for (int j = 0; j < 3; ++j)
+          for (int kb = 0; kb < bs->maxfn; ++kb) {
+            const int64_t n = bs->ad_dof[(q * 3 + j) * bs->maxfn + kb];
+            if (n < 0) continue;
+            const double b = bs->ad_coeff[(q * 3 + j) * bs->maxfn + kb];
+            for (int i = 0; i < 3; ++i)
+              for (int ka = 0; ka < ts->maxfn; ++ka) {
+                const int64_t m = ts->ad_dof[(p * 3 + i) * ts->maxfn + ka];
+                if (m < lo || m >= hi) continue;
+                const cplx v = ts->ad_coeff[(p * 3 + i) * ts->maxfn + ka] * z[i * 3 + j] * b;
+                double* e = Z + 2 * (m + n * ldz);
+                e[0] += v.real();
+                e[1] += v.imag();
+              }
+          }
+      }
+    }
+  };
+  std::vector<std::thread> th;
+  for (int t = 0; t < nthreads; ++t) th.emplace_back(worker, t);
+  for (auto& t : th) t.join();
+  return 0;
 }
 
 // Identity / NCross on RT x RT (src/identityop.jl:7-24, SingleNumQStrat(6) identityop.jl:66-67;

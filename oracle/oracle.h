@@ -111,6 +111,15 @@ int orc_assemble(const orc_op* op, const orc_qs* qs, const orc_mesh* mesh,
                  const orc_space* tspace, const orc_space* bspace,
                  double* Z, int64_t ldz, int64_t row_lo, int64_t row_hi, int nthreads);
 
+/* TestRefinesTrialQStrat (split_test 0: test space on the refinement of the trial mesh) or
+ * TrialRefinesTestQStrat (split_test 1) wrapping the DoubleNumWiltonSauterQStrat `qs`, RT x RT.
+ * children: [coarse mesh cell][nchild][3][3] vertices of each coarse cell's children.
+ * Z as orc_assemble (all rows), zeroed by the caller. */
+int orc_assemble_refines(const orc_op* op, const orc_qs* qs, const orc_mesh* tmesh,
+                         const orc_mesh* bmesh, const orc_space* tspace, const orc_space* bspace,
+                         const double* children, int nchild, int split_test, double* Z, int64_t ldz,
+                         int nthreads);
+
 /* local identity / ncross operator on same-cell pairs (src/identityop.jl), RT x RT.
  * which: 0 Identity, 1 NCross.  Adds coeff * block into Z. */
 int orc_assemble_local(int which, const orc_mesh* mesh, const orc_space* tspace,

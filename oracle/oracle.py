@@ -58,6 +58,9 @@ def lib():
         _LIB.orc_trirule.argtypes = [C.c_int, d, d, C.c_int]
         _LIB.orc_gausslegendre.argtypes = [C.c_int, d, d]
         _LIB.orc_wiltonints.argtypes = [d, d, d, d, d, d, d]
+        vp = C.c_void_p
+        _LIB.orc_assemble_refines.argtypes = [vp, vp, vp, vp, vp, vp, d, C.c_int, C.c_int, d, C.c_int64,
+                                              C.c_int]
         _LIB.orc_wiltonints.restype = None
         _LIB.orc_cellpair.argtypes = [C.POINTER(OrcOp), C.c_int, C.c_int, d, d, C.c_int,
                                       C.c_int, C.c_int, C.c_int, d]
@@ -180,6 +183,22 @@ def assemble(op, qs, tspace, bspace, row_lo=0, row_hi=-1, nthreads=None):
     lib().orc_assemble(C.byref(op), C.byref(qs), C.byref(m), C.byref(ts), C.byref(bs),
                        _dp(Z.view(np.float64)), nrows, row_lo, row_hi, nthreads)
     return Z.T  # rows x cols view of column-major storage
+
+
+def assemble_refines(op, qs, tspace, bspace, children, split_test=False, nthreads=None):
+    """RT x RT matrix across a barycentric refinement (TestRefinesTrialQStrat, or with
+    split_test TrialRefinesTestQStrat): children [coarse cells][nchild][3][3]"""
+    keep = _Keep()
+    tm, bm = _mesh_struct(tspace.mesh, keep), _mesh_struct(bspace.mesh, keep)
+    ts, bs = _space_struct(tspace, keep), _space_struct(bspace, keep)
+    ch = np.ascontiguousarray(children, dtype=np.float64)
+    n = tspace.numfunctions()
+    Z = np.zeros((bspace.numfunctions(), n), dtype=np.complex128)
+    rc = lib().orc_assemble_refines(C.byref(op), C.byref(qs), C.byref(tm), C.byref(bm), C.byref(ts),
+                                    C.byref(bs), _dp(ch), ch.shape[1], 1 if split_test else 0,
+                                    _dp(Z.view(np.float64)), n, nthreads or os.cpu_count() or 1)
+    assert rc == 0, "RT spaces and a DoubleNumWiltonSauterQStrat are required"
+    return Z.T
 
 
 def assemble_local(which, tspace, bspace, degree=6, coeff=1.0):

@@ -88,8 +88,9 @@ def test_bc_mfie_against_the_reference_quadrature_scheme():
     (src/quadrature/strategies/testrefinestrialqstrat.jl, rules/testrefinestrialqrule.jl): a fine
     test cell against a coarse trial cell, split into the trial cell's children (conforming rule
     on each, coarse shapes restricted to the child) only when the two share a vertex, the
-    conforming rule on the whole coarse cell otherwise.  Restated here on the oracle's cell-pair
-    blocks; the fine-mesh assembly (children for every pair) differs from it by quadrature only:
+    conforming rule on the whole coarse cell otherwise (TrialRefinesTestQStrat: the same with the
+    roles swapped).  Restated here on the oracle's cell-pair blocks, which pins the oracle's
+    own restatement (orc_assemble_refines); the fine-mesh assembly (children for every pair) differs from it by quadrature only:
     measured 4.6e-3 (matrix), 2.6e-3 (surface current), 3.0e-3 (far field) at level 1 and 2.5e-3,
     9.0e-4, 1.0e-3 at level 2"""
     import oracle as O
@@ -126,21 +127,32 @@ def test_bc_mfie_against_the_reference_quadrature_scheme():
 
     ncs = m.numcells()
     Zloc = np.zeros((R.fine.numcells(), ncs, 3, 3), complex)
+    Zloc_t = np.zeros((ncs, R.fine.numcells(), 3, 3), complex)  # coarse test, fine trial
     for tf in range(R.fine.numcells()):
         tv = Vf[Cf[tf]]
         shared = {int(x) for x in Cf[tf] if x < nv}
         for c in range(ncs):
             if shared & {int(x) for x in Cc[c]}:
                 Zloc[tf, c] = sum(block(tv, Vf[Cf[t]]) @ restriction(c, t).T for t in R.children(c))
+                Zloc_t[c, tf] = sum(restriction(c, t) @ block(Vf[Cf[t]], tv) for t in R.children(c))
             else:
                 Zloc[tf, c] = block(tv, Vc[Cc[c]])
+                Zloc_t[c, tf] = block(Vc[Cc[c]], tv)
     n = X.numfunctions()
     Zref = np.zeros((n, n), complex)
+    Zref_t = np.zeros((n, n), complex)
     for i, fn in enumerate(Y.fns):
         for tf, r, w in fn:
             for j, fx in enumerate(X.fns):
                 for c, rr, wx in fx:
                     Zref[i, j] += w * wx * Zloc[tf, c, r, rr]
+                    Zref_t[j, i] += w * wx * Zloc_t[c, tf, rr, r]
+    # the oracle's C restatement of both strategies agrees with this one to rounding
+    cv = R.child_vertices()
+    Zo = O.assemble_refines(op, qs, Y, X, cv)
+    Zo_t = O.assemble_refines(op, qs, X, Y, cv, split_test=True)
+    assert np.abs(Zo - Zref).max() < 1e-13 * np.abs(Zref).max()
+    assert np.abs(Zo_t - Zref_t).max() < 1e-13 * np.abs(Zref_t).max()
     Zfine = O.assemble(op, qs, Y, Xf)
     assert np.linalg.norm(Zfine - Zref) / np.linalg.norm(Zref) < 1e-2
     N = O.assemble_local(1, Y, Xf)

@@ -192,6 +192,55 @@ def test_bc_mfie_on_the_refinement(ctx):
     assert rel_entry(N, O.assemble_local(1, Y, Xf)) < 1e-12
 
 
+@pytest.mark.parametrize("which,precision,tol", [("doublelayer", bg.FP64, 1e-10), ("singlelayer", bg.FP64, 1e-10),
+                                                  ("singlelayer", bg.MIXED_ACCURATE, 1e-8)])
+def test_refines_strategies(ctx, which, precision, tol):
+    """BC test functions on the refinement against RT trial functions on the coarse mesh: the
+    library picks TestRefinesTrialQStrat (and TrialRefinesTestQStrat with the roles swapped)
+    from the meshes, as src/operator.jl:256-262 does, and matches the oracle's restatement"""
+    m = bg.icosphere(1)
+    X = bg.raviartthomas(m)
+    R = bg.barycentric_refinement(m)
+    Y, _ = bg.buffachristiansen(m, R, X)
+    op = getattr(bg.Maxwell3D, which)(wavenumber=1.0)
+    qs = _orc_qs(bg.defaultquadstrat(op, Y, X))
+    cv = R.child_vertices()
+    Z = bg.assemble(op, Y, X, precision=precision, ctx=ctx)
+    Zo = O.assemble_refines(_orc_op(op), qs, Y, X, cv)
+    assert rel_entry(Z, Zo) < tol, err_profile(Z, Zo)
+    Zt = bg.assemble(op, X, Y, precision=precision, ctx=ctx)
+    Zto = O.assemble_refines(_orc_op(op), qs, X, Y, cv, split_test=True)
+    assert rel_entry(Zt, Zto) < tol, err_profile(Zt, Zto)
+
+
+def test_bc_mfie_across_the_refinement(ctx):
+    """(K + N/2)[BC, RT] of examples/mfie.jl with the RT space on the coarse mesh: the double
+    layer through TestRefinesTrialQStrat, NCross through the refined trial space (exact, as
+    assemble_local_refines!); its far field agrees with the EFIE's"""
+    m = bg.icosphere(2)
+    X = bg.raviartthomas(m)
+    R = bg.barycentric_refinement(m)
+    Y, _ = bg.buffachristiansen(m, R, X)
+    k = 1.0
+    K = bg.Maxwell3D.doublelayer(wavenumber=k)
+    A = bg.assemble(K + 0.5 * bg.NCross(), Y, X, ctx=ctx)
+    N = O.assemble_local(1, Y, bg.refined(X, R))
+    Ko = O.assemble_refines(_orc_op(K), _orc_qs(bg.defaultquadstrat(K, Y, X)), Y, X, R.child_vertices())
+    assert rel_entry(A, Ko + 0.5 * N) < 1e-10
+    # MFIE right-hand side ((n x H) x n)[BC] with H = d x p for this wave, EFIE ((n x E) x n)[RT]
+    d, p = np.array([0, 0, 1.0]), np.array([1.0, 0, 0])
+    H = bg.Maxwell3D.planewave(direction=d, polarization=np.cross(d, p), wavenumber=k)
+    E = bg.Maxwell3D.planewave(direction=d, polarization=p, wavenumber=k)
+    u_m = np.linalg.solve(A, bg.assemble_rhs(bg.tangential_trace(H), Y, ctx=ctx))
+    T = bg.assemble(bg.Maxwell3D.singlelayer(wavenumber=k), X, X, ctx=ctx)
+    u_e = np.linalg.solve(T, bg.assemble_rhs(bg.tangential_trace(E), X, ctx=ctx))
+    th = np.linspace(0, np.pi, 91)
+    dirs = np.stack([np.sin(th), 0 * th, np.cos(th)], 1)
+    ff_m, ff_e = bg.farfield(X, u_m, dirs, 1j * k, ctx=ctx), bg.farfield(X, u_e, dirs, 1j * k, ctx=ctx)
+    assert np.linalg.norm(ff_m - ff_e) / np.linalg.norm(ff_e) < 2e-3  # 3.1e-4 from the oracle
+    assert np.linalg.cond(A) < 10
+
+
 def test_chunked_assembly_identical(ctx):
     X = bg.raviartthomas(bg.icosphere(2))
     op = bg.Maxwell3D.singlelayer(wavenumber=2.0)

@@ -1,5 +1,5 @@
 """GPU: the batched assembly of many P0 meshes in one persistent launch (beast_batch_*) gives
-each job the matrix its own assembly gives, on the first (graph-capturing) call and on a
+each job the matrix its own assembly gives (to a few ulps), on the first (graph-capturing) call and on a
 replay."""
 import numpy as np
 import pytest
@@ -30,7 +30,10 @@ def test_batch_matches_per_job_assembly(precision, order):
             Zs = [Z.cpu().numpy() for Z in b.assemble()]
             for op, X, Z in zip(ops, spaces, Zs):
                 ref = bg.assemble(op, X, X, precision=precision)
-                assert np.array_equal(Z, ref), (call, float(np.abs(Z - ref).max()))
+                # the batched and per-mesh far kernels sum a pair's points in the same order but
+                # may contract the FP64 moment updates differently: allow a few ulps of the block
+                err = float(np.abs(Z - ref).max())
+                assert err <= 1e-14 * float(np.abs(ref).max()), (call, err)
     finally:
         b.close()
 
