@@ -46,8 +46,8 @@ def parse():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--level", type=int, default=5)
-    ap.add_argument("--k", type=float, default=10.0)
+    ap.add_argument("--level", type=int, default=None, help="icosphere level (c2: 5, c4: 6)")
+    ap.add_argument("--k", type=float, default=None, help="wavenumber (c2: 10, c4: 20)")
     ap.add_argument("--precision", default="mixed-accurate", choices=["mixed", "mixed-accurate", "fp64"],
                     help="mixed-accurate (default; meets the 1e-6 surface-current contract): double-float "
                          "far pairs + FP64 near pairs into a c128 matrix, mixed factorisation, FP64 "
@@ -65,8 +65,9 @@ def parse():
     ap.add_argument("--prof-all", action="store_true",
                     help="bracket every kernel class with CUDA events inside the timed steps "
                          "(default: only the roofline class; the breakdown comes from one extra step)")
-    ap.add_argument("--config", default="c2", choices=["c2", "c3", "c5"],
+    ap.add_argument("--config", default="c2", choices=["c2", "c3", "c4", "c5"],
                     help="c2: the bench line (default); c3: 256 small Helmholtz P0 jobs, jobs/s; "
+                         "c4: mixed EFIE k=20 on level 6 with its FP64-GMRES calibration at level 5; "
                          "c5: a Poisson stream of mixed solve requests, latency p50/p99")
     ap.add_argument("--workers", type=int, default=4, help="c3/c5: concurrent contexts (streams)")
     ap.add_argument("--rate", type=float, default=4.0, help="c5: requests per second")
@@ -74,7 +75,12 @@ def parse():
     ap.add_argument("--compare-fp64", action="store_true",
                     help="instead of the bench line: one plain FP64 solve and one mixed solve of the "
                          "workload, their solves/s and the relative difference of the surface currents")
-    return ap.parse_args()
+    a = ap.parse_args()
+    if a.level is None:
+        a.level = 6 if a.config == "c4" else 5
+    if a.k is None:
+        a.k = 20.0 if a.config == "c4" else 10.0
+    return a
 
 
 def workload(args):
@@ -649,6 +655,95 @@ def _accuracy(bg, X, x, xref, dirs, g, Z=None, Zref=None, ctx=None):
 PRECISIONS = {"mixed": 1, "mixed-accurate": 2, "fp64": 0}
 
 
+def run_c4(args):
+    """C4: mixed-precision EFIE (c64 matrix, mixed factorisation, FP64 refinement) on icosphere
+    level --level (default 6: 81920 triangles, 122880 RT unknowns, a 121 GB matrix) at k = --k
+    (default 20), with its error calibrated at level 5 (30720 unknowns, where the FP64 matrix
+    fits) against FP64 GMRES on the FP64 matrix, the reference's iterative solver
+    (src/solvers/itsolver.jl:5-176): the mixed solve of the level-5 system is compared with
+    the GMRES solution (surface current and far field)."""
+    import torch
+    import beastgpu as bg
+    from beastgpu import lib as L
+    dev = 0
+    torch.cuda.set_device(dev)
+    k = args.k
+    g = 1j * k
+    wave = (np.array([1.0, 0, 0]), np.array([0, 0, 1.0]), g)
+    th = np.linspace(0.0, np.pi, 181)
+    dirs = np.stack([np.sin(th), np.zeros_like(th), np.cos(th)], axis=1)
+    op = bg.Maxwell3D.singlelayer(wavenumber=k)
+    stream = torch.cuda.current_stream()
+
+    # ---- calibration at level 5: FP64 GMRES on the FP64 matrix vs the mixed solve
+    ctx = bg.Context(dev)
+    ctx.check(ctx.lib.beast_ctx_set_stream(ctx.handle, C.c_void_p(stream.cuda_stream)))
+    X5 = bg.raviartthomas(bg.icosphere(5))
+    n5 = X5.numfunctions()
+    p5 = Problem(ctx, X5, op, L.EXC_TANGTRACE_E)
+    Z64, dt64, b64, x64 = p5.buffers(L.FP64)
+    p5.assemble(L.FP64, Z64, dt64)
+    p5.rhs(b64, *wave)
+    it, res = C.c_int(0), C.c_double(0)
+    gm_tol, gm_restart, gm_max = 1e-10, 200, 20000
+    ms_gm, _ = _timed(lambda: ctx.check(ctx.lib.beast_gmres(
+        ctx.handle, n5, Z64.data_ptr(), n5, dt64, b64.data_ptr(), x64.data_ptr(), L.DEVICE, gm_tol, gm_restart,
+        gm_max, C.byref(it), C.byref(res))), stream)
+    gm_iters, gm_res = int(it.value), float(res.value)
+    xg = x64.cpu().numpy()
+    del Z64
+    torch.cuda.empty_cache()
+    Zm, dtm, bm, xm = p5.buffers(L.MIXED)
+    p5.step(L.MIXED, Zm, dtm, bm, xm, wave, args.tol)
+    torch.cuda.synchronize()
+    calib = _accuracy(bg, X5, xm.cpu().numpy(), xg, dirs, g, ctx=ctx)
+    calib.update({"unknowns": int(n5), "reference": "FP64 GMRES on the FP64 (c128) matrix, x0 = 0",
+                  "gmres": {"iterations": gm_iters, "rel_residual": gm_res, "reltol": gm_tol,
+                            "restart": gm_restart, "ms": ms_gm, "converged": bool(gm_res <= gm_tol)},
+                  "mixed_refinement": {"iters": int(p5.it.value), "rel_residual": float(p5.res.value)}})
+    del Zm, bm, xm, b64, x64
+    ctx.close()
+    torch.cuda.empty_cache()
+
+    # ---- the timed large solve
+    ctx = bg.Context(dev)
+    ctx.check(ctx.lib.beast_ctx_set_stream(ctx.handle, C.c_void_p(stream.cuda_stream)))
+    m = bg.icosphere(args.level)
+    X = bg.raviartthomas(m)
+    n = X.numfunctions()
+    prob = Problem(ctx, X, op, L.EXC_TANGTRACE_E)
+    Z, dt, b, x = prob.buffers(L.MIXED)
+    for _ in range(args.warmup):
+        prob.step(L.MIXED, Z, dt, b, x, wave, args.tol)
+    torch.cuda.synchronize()
+    clk = Clocks(dev)
+    evs = [_events() for _ in range(args.steps)]
+    for i in range(args.steps):
+        evs[i][0].record(stream)
+        prob.step(L.MIXED, Z, dt, b, x, wave, args.tol)
+        evs[i][1].record(stream)
+    torch.cuda.synchronize()
+    clocks = clk.stop()
+    ms = [a.elapsed_time(b_) for a, b_ in evs]
+    mode = C.c_int(-1)
+    ctx.lib.beast_last_factor_mode(ctx.handle, C.byref(mode))
+    t = float(np.sum(ms)) / 1000.0
+    out = {"metric": "solves/s", "value": args.steps / t, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": 1000.0 * t / args.steps, "step_ms": ms,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64+f64",
+           "data": "synthetic (icosphere, plane wave)",
+           "config": {"workload": f"C4: mixed-precision EFIE k={k:g} on icosphere level {args.level} "
+                                  f"({m.numcells()} triangles, {n} RT unknowns)",
+                      "matrix_gb": n * n * 8 / 1e9, "precision": "mixed", "refinement_tol": args.tol,
+                      "step": "assembly (c64) + excitation + mixed factorisation + FP64 refinement",
+                      "l2": "inputs larger than L2", "parallelism": "one GPU"},
+           "refinement": {"iters": int(prob.it.value), "rel_residual": float(prob.res.value),
+                          "factorisation": FACTOR_MODES[max(0, mode.value)]},
+           "calibration": calib, "clocks": clocks}
+    ctx.close()
+    print(json.dumps(out))
+
+
 def run_c2(args):
     """The bench line: C2 (EFIE k = 10 on the 20480-triangle icosphere, 30720 RT unknowns).
     value = solves/s of the --precision mode (default mixed-accurate, the mode that meets the
@@ -888,6 +983,8 @@ def main():
         return run_c3(args)
     if args.config == "c5":
         return run_c5(args)
+    if args.config == "c4":
+        return run_c4(args)
     return run_c2(args)
 
 
