@@ -167,6 +167,7 @@ int beast_ctx_destroy(beast_ctx* ctx) {
   }
   if (ctx->ws) cudaFree(ctx->ws);
   if (ctx->d_flag) cudaFree(ctx->d_flag);
+  for (auto& kv : ctx->ss_tabs) cudaFree(kv.second);
   for (auto& r : ctx->prof) {
     cudaEventDestroy(r.a);
     cudaEventDestroy(r.b);
@@ -587,6 +588,7 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
     BEAST_CUDA_TRY(ctx, cudaMemcpyAsync(qlocal_d, ql.data(), sizeof(int) * bs->ncells, cudaMemcpyHostToDevice, st));
     BEAST_CUDA_TRY(ctx, cudaMemsetAsync(counter, 0, sizeof(int), st));
     AsmArgs a;
+    a.ss_tabs = &ctx->ss_tabs;
     a.op = to_params(op);
     a.qs = *qs;
     a.ts = ts;

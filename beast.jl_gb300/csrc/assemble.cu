@@ -750,6 +750,63 @@ DEV void ss_node_f(int cls, int n, int item, const float* glx, const float* glw,
   *w = wt;
 }
 
+// ss_node_f's maps in FP64 (X, Y, D = X - Y from the maps' own factors, weight): the node
+// tables of k_near_ss_df are built from it once
+DEV void ss_node_fd(int cls, int n, int item, const double* glx, const double* glw, double* X, double* Y,
+                    double* D, double* w) {
+  const int nreg = cls == 1 ? 2 : 6;
+  const int reg = item % nreg;
+  int k = item / nreg;
+  const int i4 = k % n;
+  k /= n;
+  const int i3 = k % n;
+  k /= n;
+  const int i2 = k % n;
+  const int i1 = k / n;
+  const double xi = glx[i1], e1 = glx[i2], e2 = glx[i3], e3 = glx[i4];
+  const double ww = glw[i1] * glw[i2] * glw[i3] * glw[i4];
+  double A[2], B[2], AB[2], wt;
+  const int sub = reg >> 1;
+  const bool swap = reg & 1;
+  if (cls == 1) {
+    wt = ww * xi * xi * xi * e2;
+    A[0] = xi; A[1] = xi * e1;
+    B[0] = xi * e2; B[1] = xi * e2 * e3;
+    AB[0] = xi * (1.0 - e2); AB[1] = xi * (e1 - e2 * e3);
+  } else if (cls == 2) {
+    double ap, bb, cc;
+    if (sub == 0) { ap = e1; bb = e1 * e2; cc = e1 * e3; }
+    else if (sub == 1) { bb = e1; ap = e1 * e2; cc = e1 * e3; }
+    else { cc = e1; ap = e1 * e2; bb = e1 * e3; }
+    wt = ww * xi * xi * xi * (1.0 - ap) * e1 * e1;
+    A[0] = xi; A[1] = xi * bb;
+    B[0] = xi * (1.0 - ap); B[1] = xi * (1.0 - ap) * cc;
+    AB[0] = xi * ap; AB[1] = xi * (bb - (1.0 - ap) * cc);
+  } else {
+    const double s = e1, t = e2, u = e3;
+    wt = ww * xi * xi * xi * s * (1.0 - s);
+    if (sub == 0) {
+      const double ap = s * t, e = s * (1.0 - t), b = (1.0 - s) * u;
+      A[0] = xi; A[1] = xi * b;
+      B[0] = xi * (1.0 - ap); B[1] = xi * (b + e);
+      AB[0] = xi * ap; AB[1] = -xi * e;
+    } else {
+      const double ap = sub == 1 ? s : s * t, ep = sub == 1 ? s * t : s, cp = (1.0 - s) * u;
+      A[0] = xi; A[1] = xi * (cp + ep);
+      B[0] = xi * (1.0 - ap); B[1] = xi * cp;
+      AB[0] = xi * ap; AB[1] = xi * ep;
+    }
+  }
+  if (swap) {
+    X[0] = B[0]; X[1] = B[1]; Y[0] = A[0]; Y[1] = A[1];
+    D[0] = -AB[0]; D[1] = -AB[1];
+  } else {
+    X[0] = A[0]; X[1] = A[1]; Y[0] = B[0]; Y[1] = B[1];
+    D[0] = AB[0]; D[1] = AB[1];
+  }
+  *w = wt;
+}
+
 DEV V3<float> v3f(V3<double> a) { return V3<float>{(float)a.x, (float)a.y, (float)a.z}; }
 
 struct NearParams {
@@ -765,6 +822,9 @@ struct NearParams {
   void* zcell;
   int zfmt;  // Zcell format (ZCELL_*)
   int ss32;  // Sauter-Schwab moments of RT Maxwell pairs in FP32 (mixed precision)
+  int ssdf;  // Sauter-Schwab pairs of RT Maxwell operators in double-float (k_near_ss_df)
+  const float2* ssdf_tab[4];  // per class 1..3: node table [7][items] (ss_table)
+  int ssdf_items[4];
   int64_t ldc;
   const int* zrow;  // as in FarParams
   const int* zcol;
@@ -789,6 +849,13 @@ constexpr int NEAR_WARPS = 4;
 // paths of k_near; k_near skips these pairs.
 DEV bool near_is_ss32(const NearParams& P, int cls) {
   return P.ss32 && cls >= 1 && cls <= 3 && P.tk == BEAST_RT && P.bk == BEAST_RT &&
+         (P.op.kind == BEAST_MW_SL || (P.op.kind == BEAST_MW_DL && cls != 3));
+}
+
+// the same pairs in double-float arithmetic on the mixed-accurate path (real wavenumber):
+// k_near_ss_df; the double layer's common-face blocks (identically zero) stay with k_near
+DEV bool near_is_ssdf(const NearParams& P, int cls) {
+  return P.ssdf && cls >= 1 && cls <= 3 && P.tk == BEAST_RT && P.bk == BEAST_RT &&
          (P.op.kind == BEAST_MW_SL || (P.op.kind == BEAST_MW_DL && cls != 3));
 }
 
@@ -1116,7 +1183,7 @@ DEV void rt_restriction(const Geo& parent, const Geo& ch, double Q[3][3]) {
 // one near pair, by one warp (lane = its lane); s_glx / s_glw: the Gauss-Legendre table in
 // shared memory (lanes read different nodes: a constant-memory read would serialise)
 DEV void near_pair(const NearParams& P, const NearPair np_, const double* s_glx, const double* s_glw, int lane) {
-  if (near_is_ss32(P, np_.cls)) return;  // k_near_ss32
+  if (near_is_ss32(P, np_.cls) || near_is_ssdf(P, np_.cls)) return;  // k_near_ss32 / k_near_ss_df
   const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
   const Geo s = load_geo(P.bgeo + (int64_t)(P.qcells ? P.qcells[np_.q] : np_.q) * GEO_STRIDE);
   const int nt = P.tk == BEAST_P0 ? 1 : 3, nb = P.bk == BEAST_P0 ? 1 : 3;
@@ -2081,6 +2148,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_batch(BatchLaunch L) {
     P.flag = L.flag;
     P.ro = L.ron;
     P.ri = L.rin;
+    P.ssdf = 0;
     P.bcells = P.tcells = nullptr;  // no refines strategies in a batch
     P.bchildren = P.tchildren = nullptr;
     P.bnchild = P.tnchild = 0;
@@ -2343,6 +2411,226 @@ cudaError_t launch_near_batch(const BatchLaunch& L, cudaStream_t st) {
   return cudaGetLastError();
 }
 
+// ---- Sauter-Schwab pairs in double-float arithmetic (mixed-accurate path)
+// The node table of class cls and order n: for node `it` of the pair's rule (ss_node's order),
+// tab[k * items + it] = (hi, lo) of X0, X1, Y0, Y1, D0, D1, w (k = 0..6), built once in FP64.
+constexpr int SSDF_VALS = 7;
+__global__ void k_ss_table(int cls, int n, int items, float2* tab) {
+  const int it = blockIdx.x * blockDim.x + threadIdx.x;
+  if (it >= items) return;
+  double X[2], Y[2], D[2], w;
+  ss_node_fd(cls, n, it, c_gl_x + c_gl_off[n - 1], c_gl_w + c_gl_off[n - 1], X, Y, D, &w);
+  const double v[SSDF_VALS] = {X[0], X[1], Y[0], Y[1], D[0], D[1], w};
+  for (int k = 0; k < SSDF_VALS; ++k) {
+    const dfl::df p = df_of(v[k]);
+    tab[(int64_t)k * items + it] = make_float2(p.hi, p.lo);
+  }
+}
+
+// the table of (cls, n) from the context's cache, built on first use (after upload_gl)
+static cudaError_t ss_table(std::map<int, void*>* cache, int cls, int n, cudaStream_t st, const float2** out,
+                            int* items) {
+  const int nreg = cls == 1 ? 2 : 6;
+  *items = nreg * n * n * n * n;
+  const int key = 64 * cls + n;
+  auto f = cache->find(key);
+  if (f != cache->end()) {
+    *out = (const float2*)f->second;
+    return cudaSuccess;
+  }
+  void* p = nullptr;
+  cudaError_t e = cudaMalloc(&p, sizeof(float2) * SSDF_VALS * (size_t)*items);
+  if (e != cudaSuccess) return e;
+  k_ss_table<<<(*items + 255) / 256, 256, 0, st>>>(cls, n, *items, (float2*)p);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    cudaFree(p);
+    return e;
+  }
+  (*cache)[key] = p;
+  *out = (const float2*)p;
+  return cudaSuccess;
+}
+
+DEV void dfv3(const V3<double>& a, dfl::df* o) {
+  o[0] = df_of(a.x);
+  o[1] = df_of(a.y);
+  o[2] = df_of(a.z);
+}
+
+// The moment form of k_near's Sauter-Schwab path for RT x RT Maxwell pairs, every node in
+// double-float arithmetic on the FP32 pipes (GB300's FP64 pipe is a small fraction of its FP32
+// rate): one warp per pair, lanes over the nodes, x - y from the maps' own factors (D = X - Y)
+// on double-float edge vectors, 1/R by the pair reciprocal square root, exp(-ikR) from the
+// shared-memory sine table; per-lane moments as sloppy pair sums, the warp's totals as exact
+// pair sums, the 3 x 3 block from them in FP64 (nine lanes).  Real wavenumbers (the caller
+// keeps complex ones on k_near).
+template <bool SL>
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
+  __shared__ float s_tab[64][4];  // sin / cos(m pi/32)
+  for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
+  if (e >= P.nnear) return;
+  const NearPair np_ = P.near[e];
+  if (!near_is_ssdf(P, np_.cls)) return;
+  const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
+  const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
+  // shared vertices first, in the same order (as k_near_ss32: lanes 0..8 test one pair each)
+  const double dtol = 1.0e3 * 2.220446049250313e-16;
+  bool hit = false;
+  if (lane < 9) {
+    const V3<double> dd = t.v[lane / 3] - s.v[lane % 3];
+    hit = dot(dd, dd) < dtol * dtol;
+  }
+  const unsigned hmask = __ballot_sync(0xffffffffu, hit);
+  int pt[3], ps[3], hits = 0, ti[3], si[3];
+  for (int b = 0; b < 9; ++b)
+    if (((hmask >> b) & 1u) && hits < 3) {
+      ti[hits] = b / 3;
+      si[hits] = b % 3;
+      ++hits;
+    }
+  int k = 0;
+  for (int h = 0; h < hits; ++h) pt[k++] = ti[h];
+  for (int i = 0; i < 3; ++i) {
+    bool used = false;
+    for (int h = 0; h < hits; ++h) used |= ti[h] == i;
+    if (!used) pt[k++] = i;
+  }
+  k = 0;
+  for (int h = 0; h < hits; ++h) ps[k++] = si[h];
+  for (int j = 0; j < 3; ++j) {
+    bool used = false;
+    for (int h = 0; h < hits; ++h) used |= si[h] == j;
+    if (!used) ps[k++] = j;
+  }
+  const int cls = np_.cls;
+  const float2* tab = P.ssdf_tab[cls];
+  const int items = P.ssdf_items[cls];
+  const V3<double> cp = t.c, cq = s.c;
+  dfl::df a0[3], et1[3], et2[3], b0[3], es1[3], es2[3], dd[3];
+  dfv3(t.v[pt[0]] - cp, a0);
+  dfv3(t.v[pt[1]] - t.v[pt[0]], et1);
+  dfv3(t.v[pt[2]] - t.v[pt[1]], et2);
+  dfv3(s.v[ps[0]] - cq, b0);
+  dfv3(s.v[ps[1]] - s.v[ps[0]], es1);
+  dfv3(s.v[ps[2]] - s.v[ps[1]], es2);
+  dfv3(cp - cq, dd);
+  const dfl::df kk = df_of(P.op.gi);
+  const dfl::df i4pi{DF_I4PI_HI, DF_I4PI_LO};
+  constexpr int NM = SL ? 16 : 22;  // M0 (SL only), M1, V1, V2 (+ V3 for the double layer)
+  dfl::df m[22];
+#pragma unroll
+  for (int q = 0; q < 22; ++q) m[q] = dfl::make(0.f);
+  for (int it = lane; it < items; it += 32) {
+    dfl::df v[SSDF_VALS];
+#pragma unroll
+    for (int q = 0; q < SSDF_VALS; ++q) {
+      const float2 f = tab[(int64_t)q * items + it];
+      v[q] = dfl::df{f.x, f.y};
+    }
+    const dfl::df X0 = v[0], X1 = v[1], Y0 = v[2], Y1 = v[3], D0 = v[4], D1 = v[5], w = v[6];
+    dfl::df xi[3], eta[3], r[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      xi[c] = dfl::adds(a0[c], dfl::adds(dfl::mul(X0, et1[c]), dfl::mul(X1, et2[c])));
+      eta[c] = dfl::adds(b0[c], dfl::adds(dfl::mul(Y0, es1[c]), dfl::mul(Y1, es2[c])));
+      if (cls == 3)
+        r[c] = dfl::adds(dfl::mul(D0, et1[c]), dfl::mul(D1, et2[c]));
+      else if (cls == 2)
+        r[c] = dfl::adds(dfl::mul(D0, et1[c]), dfl::subs(dfl::mul(X1, et2[c]), dfl::mul(Y1, es2[c])));
+      else
+        r[c] = dfl::subs(dfl::adds(dfl::mul(X0, et1[c]), dfl::mul(X1, et2[c])),
+                         dfl::adds(dfl::mul(Y0, es1[c]), dfl::mul(Y1, es2[c])));
+    }
+    const dfl::df R2 = dfl::dot3s(r, r);
+    const dfl::df iR = dfl::rsqrt(R2);
+    const dfl::df R = dfl::mul(R2, iR);
+    dfl::df sn, cs;
+    dfl::sincos_tab(dfl::mul(kk, R), s_tab, &sn, &cs);
+    const dfl::df amp = dfl::mul(dfl::mul(iR, w), i4pi);  // w / (4 pi R)
+    dfl::df cr = dfl::mul(amp, cs), ci = dfl::neg(dfl::mul(amp, sn));
+    dfl::df s0, a[3], b[3];
+    if (SL) {
+      s0 = dfl::dot3s(xi, eta);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        a[c] = xi[c];
+        b[c] = eta[c];
+      }
+      m[0] = dfl::adds(m[0], cr);
+      m[1] = dfl::adds(m[1], ci);
+    } else {
+      // grad G = c r, c = -(i k + 1/R) G / R
+      const dfl::df pr = dfl::neg(dfl::mul(iR, iR)), pi = dfl::neg(dfl::mul(kk, iR));
+      const dfl::df nr = dfl::subs(dfl::mul(pr, cr), dfl::mul(pi, ci));
+      const dfl::df ni = dfl::adds(dfl::mul(pr, ci), dfl::mul(pi, cr));
+      cr = nr;
+      ci = ni;
+      // xi.(r x eta) = xi.(d x eta); a = xi x r, b = r x eta
+      const dfl::df de[3] = {dfl::subs(dfl::mul(dd[1], eta[2]), dfl::mul(dd[2], eta[1])),
+                             dfl::subs(dfl::mul(dd[2], eta[0]), dfl::mul(dd[0], eta[2])),
+                             dfl::subs(dfl::mul(dd[0], eta[1]), dfl::mul(dd[1], eta[0]))};
+      s0 = dfl::dot3s(xi, de);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
+        a[c] = dfl::subs(dfl::mul(xi[c1], r[c2]), dfl::mul(xi[c2], r[c1]));
+        b[c] = dfl::subs(dfl::mul(r[c1], eta[c2]), dfl::mul(r[c2], eta[c1]));
+      }
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        m[16 + 2 * c] = dfl::adds(m[16 + 2 * c], dfl::mul(r[c], cr));
+        m[17 + 2 * c] = dfl::adds(m[17 + 2 * c], dfl::mul(r[c], ci));
+      }
+    }
+    m[2] = dfl::adds(m[2], dfl::mul(s0, cr));
+    m[3] = dfl::adds(m[3], dfl::mul(s0, ci));
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      m[4 + 2 * c] = dfl::adds(m[4 + 2 * c], dfl::mul(a[c], cr));
+      m[5 + 2 * c] = dfl::adds(m[5 + 2 * c], dfl::mul(a[c], ci));
+      m[10 + 2 * c] = dfl::adds(m[10 + 2 * c], dfl::mul(b[c], cr));
+      m[11 + 2 * c] = dfl::adds(m[11 + 2 * c], dfl::mul(b[c], ci));
+    }
+  }
+  // the warp's totals (exact pair sums), then FP64
+  double md[22];
+#pragma unroll
+  for (int q = 0; q < 22; ++q) {
+    dfl::df x = m[q];
+    if (q < 2 && !SL) x = dfl::make(0.f);
+    if (q >= NM && SL) x = dfl::make(0.f);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const dfl::df y{__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)};
+      x = dfl::add(x, y);
+    }
+    md[q] = fsplit::f2d(x.hi) + fsplit::f2d(x.lo);
+  }
+  if (lane < 9) {  // lane 3 i + j: entry (i, j) of the 3 x 3 block, as k_near's moment form
+    const C2<double> M0{md[0], md[1]}, M1{md[2], md[3]};
+    CV<double> V1, V2, V3_;
+    V1.x = {md[4], md[5]}; V1.y = {md[6], md[7]}; V1.z = {md[8], md[9]};
+    V2.x = {md[10], md[11]}; V2.y = {md[12], md[13]}; V2.z = {md[14], md[15]};
+    V3_.x = {md[16], md[17]}; V3_.y = {md[18], md[19]}; V3_.z = {md[20], md[21]};
+    const int i = lane / 3, j = lane % 3;
+    const V3<double> tv = t.v[i] - cp, sv = s.v[j] - cq;
+    C2<double> z;
+    C2<double> fm = csub(csub(M1, rdot(sv, V1)), rdot(tv, V2));
+    if (SL) {
+      const C2<double> al{P.op.ar, P.op.ai}, be{P.op.br, P.op.bi};
+      fm = cadd(fm, cscale(dot(tv, sv), M0));
+      z = cadd(cmul(al, fm), cscale(4.0, cmul(be, M0)));
+    } else {
+      z = cadd(fm, rdot(cross(sv, tv), V3_));
+    }
+    store_c<double>(P.zcell, zidx(zrow_of(P.zrow, np_.p, 3, i), zcol_of(P.zcol, np_.q, 3, j), P.ldc), z, P.zfmt);
+  }
+}
+
 cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const TriRuleDev& ri,
                         const TriRuleDev& fro, const TriRuleDev& fri, cudaStream_t st) {
   if (nnear <= 0) return cudaSuccess;
@@ -2370,6 +2658,22 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   P.ri = ri;
   P.fro = fro;
   P.fri = fri;
+  // Sauter-Schwab pairs of RT Maxwell operators on the mixed-accurate path (real wavenumber)
+  // in double-float arithmetic: their node tables first
+  P.ssdf = a.zcell_fmt == ZCELL_DF && a.op.gr == 0.0 && a.ts->kind == BEAST_RT && a.bs->kind == BEAST_RT &&
+           (a.op.kind == BEAST_MW_SL || a.op.kind == BEAST_MW_DL) && a.ss_tabs != nullptr &&
+           a.qs.kind != BEAST_QS_DOUBLENUM;
+  for (int c = 0; c < 4; ++c) {
+    P.ssdf_tab[c] = nullptr;
+    P.ssdf_items[c] = 0;
+  }
+  if (P.ssdf) {
+    const int ord[4] = {0, a.qs.ss_vert, a.qs.ss_edge, a.qs.ss_face};
+    for (int c = 1; c <= 3; ++c) {
+      e = ss_table(a.ss_tabs, c, ord[c], st, &P.ssdf_tab[c], &P.ssdf_items[c]);
+      if (e != cudaSuccess) return e;
+    }
+  }
   P.bcells = a.bs->cells;
   P.bchildren = a.bs->mesh->children;
   P.bnchild = a.bs->mesh->nchild;
@@ -2378,6 +2682,12 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   P.tnchild = a.ts->mesh->nchild;
   unsigned blocks = (unsigned)((nnear + NEAR_WARPS - 1) / NEAR_WARPS);
   if (P.ss32) k_near_ss32<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
+  if (P.ssdf) {
+    if (a.op.kind == BEAST_MW_SL)
+      k_near_ss_df<true><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
+    else
+      k_near_ss_df<false><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
+  }
   k_near<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   if (P.qs.kind == BEAST_QS_TEST_REFINES_TRIAL || P.qs.kind == BEAST_QS_TRIAL_REFINES_TEST)
     k_near_refines<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);

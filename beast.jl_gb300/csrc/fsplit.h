@@ -8,8 +8,9 @@
 //       with the sign of a, built from the bits with integer instructions only.
 // |a| < 2^-97 gives 0 + 0, and lo is dropped below |a| = 2^-74: absolute errors below 1e-29,
 // far under the FP64 rounding of a matvec of boundary-element entries.  |a| >= 2^128 (not a
-// BEM matrix entry) overflows to +-inf, so the matvec reports it instead of hiding it.  Host
-// and device builds give identical bits.
+// BEM matrix entry) overflows to +-inf, so the matvec reports it instead of hiding it.  No
+// branch converts (a conversion instruction, even on a path not taken, would be if-converted
+// into every call and run on the FP64 pipe).  Host and device builds give identical bits.
 #pragma once
 #include <stdint.h>
 #include <string.h>
@@ -65,8 +66,9 @@ FS_HD void split_f64(double a, float* hi, float* lo) {
   const uint32_t top = (uint32_t)(u >> 32);
   const int e = (int)((top >> 20) & 0x7FF);
   const uint32_t sgn = top & 0x80000000u;
-  if (e > 1150) {  // beyond the float range (NaN and infinity included): +-inf or NaN
-    *hi = (float)a;
+  if (e > 1150) {  // beyond the float range: +-inf, NaN stays NaN (bits, not a conversion)
+    const bool nan = e == 2047 && (u & 0x000FFFFFFFFFFFFFull) != 0;
+    *hi = from_bits(sgn | 0x7F800000u | (nan ? 0x00400000u : 0u));
     *lo = 0.f;
     return;
   }
@@ -91,15 +93,29 @@ FS_HD void split_f64(double a, float* hi, float* lo) {
 
 namespace fsplit {
 
+// a double rounded to the nearest float (ties to even) with integer operations only: the same
+// bits as the conversion instruction for results in the normal float range; results below it
+// (|a| < 2^-126) become 0, results above it +-inf, NaN stays NaN
+FS_HD float to_float_rn(double a) {
+  const uint64_t u = bits64(a);
+  const uint32_t top = (uint32_t)(u >> 32);
+  const int e = (int)((top >> 20) & 0x7FF);
+  const uint32_t sgn = top & 0x80000000u;
+  if (e > 1150) return from_bits(sgn | 0x7F800000u | (e == 2047 && (u & 0x000FFFFFFFFFFFFFull) ? 0x00400000u : 0u));
+  if (e < 897) return from_bits(sgn);
+  uint32_t f = ((uint32_t)(e - 896) << 23) | (uint32_t)((u >> 29) & 0x7FFFFFu);
+  const uint32_t r = (uint32_t)(u & 0x1FFFFFFFu);
+  f += (r > 0x10000000u || (r == 0x10000000u && (f & 1u))) ? 1u : 0u;  // a carry into the exponent is right
+  return from_bits(sgn | f);
+}
+
 // a float as a double with integer operations only (exact; subnormal floats, below 1.2e-38,
-// become 0; infinities and NaN take the conversion instruction)
+// become 0; infinities and NaN keep their class)
 FS_HD double f2d(float f) {
   const uint32_t u = to_bits(f);
   const uint32_t e = (u >> 23) & 0xFF;
-  if (e == 0xFF) return (double)f;
-  if (e == 0) return 0.0;
-  const uint64_t b = ((uint64_t)(u & 0x80000000u) << 32) | ((uint64_t)(e + 896) << 52) |
-                     ((uint64_t)(u & 0x7FFFFFu) << 29);
+  const uint64_t s = (uint64_t)(u & 0x80000000u) << 32;
+  const uint64_t b = e == 0 ? s : s | ((uint64_t)(e == 0xFF ? 2047u : e + 896) << 52) | ((uint64_t)(u & 0x7FFFFFu) << 29);
 #if defined(__CUDA_ARCH__)
   return __longlong_as_double((long long)b);
 #else

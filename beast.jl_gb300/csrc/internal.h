@@ -3,6 +3,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <map>
 #include <string>
 #include <vector>
 
@@ -50,6 +51,8 @@ struct beast_ctx {
   // second (high-priority) stream and events of the factorisation's lookahead, made on first use
   cudaStream_t aux = nullptr;
   cudaEvent_t la_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+  // Sauter-Schwab node tables as double-float pairs, built on first use: key 64 class + order
+  std::map<int, void*> ss_tabs;
 };
 
 // the lookahead stream and events of ctx (created once); false when they cannot be made
@@ -171,6 +174,7 @@ struct AsmArgs {
   // row nst pp + i, column nsb ql + j
   const int* zrow;
   const int* zcol;
+  std::map<int, void*>* ss_tabs = nullptr;  // the context's Sauter-Schwab node tables
 };
 cudaError_t launch_geometry(const beast_space* s, cudaStream_t st);
 cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev& ri,

@@ -1715,8 +1715,9 @@ __global__ void k_c128_to_c64(int64_t rows, int64_t cols, const double* s, int64
   int64_t c = blockIdx.y;
   for (; c < cols; c += gridDim.y)
     if (i < rows) {
-      d[2 * (i + c * ldd)] = (float)s[2 * (i + c * lds)];
-      d[2 * (i + c * ldd) + 1] = (float)s[2 * (i + c * lds) + 1];
+      // rounded by integer operations: a conversion instruction runs on GB300's FP64 pipe
+      d[2 * (i + c * ldd)] = fsplit::to_float_rn(s[2 * (i + c * lds)]);
+      d[2 * (i + c * ldd) + 1] = fsplit::to_float_rn(s[2 * (i + c * lds) + 1]);
     }
 }
 __global__ void k_c64_to_c128(int64_t rows, int64_t cols, const float* s, int64_t lds, double* d,
@@ -1725,8 +1726,8 @@ __global__ void k_c64_to_c128(int64_t rows, int64_t cols, const float* s, int64_
   int64_t c = blockIdx.y;
   for (; c < cols; c += gridDim.y)
     if (i < rows) {
-      d[2 * (i + c * ldd)] = s[2 * (i + c * lds)];
-      d[2 * (i + c * ldd) + 1] = s[2 * (i + c * lds) + 1];
+      d[2 * (i + c * ldd)] = fsplit::f2d(s[2 * (i + c * lds)]);
+      d[2 * (i + c * ldd) + 1] = fsplit::f2d(s[2 * (i + c * lds) + 1]);
     }
 }
 

@@ -33,6 +33,7 @@ order), so the result drops into `T \\ e`, GMRES or any later BEAST code unchang
 module BEASTGPU
 
 using BEAST
+using CompScienceMeshes
 using LinearAlgebra
 
 const libbeastgpu = get(ENV, "BEASTGPU_LIB", joinpath(@__DIR__, "..", "beastgpu", "libbeastgpu.so"))
@@ -41,6 +42,7 @@ const libbeastgpu = get(ENV, "BEASTGPU_LIB", joinpath(@__DIR__, "..", "beastgpu"
 const MW_SL, MW_DL, MW_NXDL, HH_SL, HH_DL, HH_DLT = 1, 2, 3, 4, 5, 6
 const P0, P1, RT = 0, 1, 2
 const QS_WILTON_SAUTER, QS_SAUTER, QS_DOUBLENUM = 1, 2, 3
+const QS_TEST_REFINES_TRIAL, QS_TRIAL_REFINES_TEST = 4, 5
 const FP64, MIXED, MIXED_ACCURATE = 0, 1, 2
 const C128, C64 = 0, 1
 const HOST, DEVICE = 0, 1
@@ -193,6 +195,40 @@ end
 on_device(tfs, bfs) = spacekind(BEAST.refspace(tfs)) !== nothing &&
     spacekind(BEAST.refspace(bfs)) !== nothing && BEAST.geometry(tfs) === BEAST.geometry(bfs)
 
+# the children of every cell of `coarse` in its refinement `fine` (CompScienceMeshes.parent /
+# children, as rules/testrefinestrialqrule.jl:23-24 reads them), registered once per mesh
+const CHILDREN = IdDict{Any,Bool}()
+function register_children!(ctx, coarse, fine)
+    get!(CHILDREN, coarse) do
+        pm = CompScienceMeshes.parent(fine)
+        kids = [collect(CompScienceMeshes.children(pm, c)) for c in 1:length(coarse)]
+        nchild = length(kids[1])
+        all(length(k) == nchild for k in kids) || error("refinement with a varying number of children")
+        CV = Float64[]
+        for k in kids, p in k, v in CompScienceMeshes.chart(fine, p).vertices
+            append!(CV, v)
+        end
+        check(ctx.ptr, ccall((:beast_mesh_set_children, libbeastgpu), Cint,
+            (Ptr{Cvoid}, Ptr{Cvoid}, Cint, Ptr{Float64}), ctx.ptr, mesh_handle(ctx, coarse), nchild, CV))
+        true
+    end
+end
+
+# RT x RT across a barycentric refinement with the Wilton-Sauter strategy: the strategy the
+# reference's assemble! wraps it in (src/operator.jl:256-262), children registered; else nothing
+function refines_qsdesc(ctx, tfs, bfs, qs)
+    qs isa BEAST.DoubleNumWiltonSauterQStrat || return nothing
+    (spacekind(BEAST.refspace(tfs)) == RT && spacekind(BEAST.refspace(bfs)) == RT) || return nothing
+    tg, bg = BEAST.geometry(tfs), BEAST.geometry(bfs)
+    kind = CompScienceMeshes.refines(tg, bg) ? QS_TEST_REFINES_TRIAL :
+           CompScienceMeshes.refines(bg, tg) ? QS_TRIAL_REFINES_TEST : 0
+    kind == 0 && return nothing
+    kind == QS_TEST_REFINES_TRIAL ? register_children!(ctx, bg, tg) : register_children!(ctx, tg, bg)
+    d = qsdesc(qs)
+    return QsDesc(kind, d.outer_far, d.inner_far, d.outer_near, d.inner_near, d.ss_tetr, d.ss_face,
+                  d.ss_edge, d.ss_vert)
+end
+
 # integral operators (src/operator.jl:207-281, one method per threading trait so that each
 # is at least as specific as the reference's in every argument)
 for T in (:multi, :single, :cellcoloring)
@@ -204,6 +240,8 @@ for T in (:multi, :single, :cellcoloring)
         if qd !== nothing && on_device(tfs, bfs)
             return gpu_assemble!(store, op, tfs, bfs, qd)
         end
+        qr = BEAST.geometry(tfs) === BEAST.geometry(bfs) ? nothing : refines_qsdesc(context(), tfs, bfs, qs)
+        qr !== nothing && return gpu_assemble!(store, op, tfs, bfs, qr)
         return invoke(BEAST.assemble!, Tuple{BEAST.Operator, BEAST.Space, BEAST.Space, Any,
                                              Type{BEAST.Threading{$(QuoteNode(T))}}},
                       op, tfs, bfs, store, threading; quadstrat=(a...) -> qs, kwargs...)

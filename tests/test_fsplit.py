@@ -55,13 +55,15 @@ def test_split_is_accurate_over_the_entry_range(split):
 
 
 def test_split_special_ranges(split):
-    a = np.array([0.0, -0.0, 1e-300, -3e-30, 2.0 ** -80, 2.0 ** 200, -2.0 ** 130, 1.0, -1.0])
+    a = np.array([0.0, -0.0, 1e-300, -3e-30, 2.0 ** -80, 2.0 ** 200, -2.0 ** 130, 1.0, -1.0,
+                  np.inf, -np.inf, np.nan])
     hi, lo = split(a)
     s = hi.astype(np.float64) + lo.astype(np.float64)
     assert s[0] == 0.0 and s[1] == 0.0 and s[2] == 0.0 and s[3] == 0.0   # below 2^-97: zero
     assert abs(s[4] - a[4]) <= 2.0 ** -80 * 2.0 ** -23                    # low part dropped
-    assert np.isinf(s[5]) and np.isinf(s[6])                              # FP64 conversion
+    assert s[5] == np.inf and s[6] == -np.inf                             # overflow to +-inf
     assert s[7] == 1.0 and s[8] == -1.0 and lo[7] == 0.0
+    assert s[9] == np.inf and s[10] == -np.inf and np.isnan(s[11])       # classes kept
 
 
 def test_float_to_double_by_integer_ops(tmp_path):
@@ -82,6 +84,39 @@ def test_float_to_double_by_integer_ops(tmp_path):
     d = np.zeros(f.size)
     L.t_f2d(f.ctypes.data, f.size, d.ctypes.data)
     assert np.array_equal(d, f.astype(np.float64))
+    assert np.array_equal(np.signbit(d), np.signbit(f))
+    nan = np.array([np.nan], np.float32)
+    L.t_f2d(nan.ctypes.data, 1, d.ctypes.data)
+    assert np.isnan(d[0])
     sub = np.array([1e-40, -3e-45], np.float32)  # subnormal floats become zero
     L.t_f2d(sub.ctypes.data, 2, d.ctypes.data)
     assert d[0] == 0.0 and d[1] == 0.0
+
+
+def test_round_to_float_by_integer_ops(tmp_path):
+    """fsplit::to_float_rn gives the conversion's bits (round to nearest, ties to even) over the
+    normal float range, including the ties, overflow to infinity and NaN"""
+    if shutil.which("g++") is None:
+        pytest.skip("g++ not available")
+    src = tmp_path / "r.cpp"
+    src.write_text('#include "fsplit.h"\n'
+                   'extern "C" void t_rn(const double* a, long n, float* f) {\n'
+                   '  for (long i = 0; i < n; ++i) f[i] = fsplit::to_float_rn(a[i]);\n}\n')
+    so = tmp_path / "r.so"
+    subprocess.check_call(["g++", "-O2", "-shared", "-fPIC", "-I", CSRC, str(src), "-o", str(so)])
+    L = C.CDLL(str(so))
+    L.t_rn.argtypes = [C.c_void_p, C.c_long, C.c_void_p]
+    rng = np.random.default_rng(2)
+    a = rng.uniform(1, 2, 200000) * 2.0 ** rng.integers(-125, 127, 200000)
+    a *= rng.choice([-1.0, 1.0], a.size)
+    # exact ties: a float plus half its ulp, both parities of the last mantissa bit
+    f0 = rng.uniform(1, 2, 1000).astype(np.float32)
+    ties = f0.astype(np.float64) + np.spacing(f0).astype(np.float64) / 2
+    big = np.array([3.4028235677973366e38, 3.4028235e38 * 1.0000001, 1e300, -1e300, np.inf, -np.inf, np.nan, 0.0, -0.0])
+    a = np.concatenate([a, ties, -ties, big])
+    f = np.zeros(a.size, np.float32)
+    L.t_rn(a.ctypes.data, a.size, f.ctypes.data)
+    with np.errstate(over="ignore"):
+        ref = a.astype(np.float32)
+    ok = (f.view(np.uint32) == ref.view(np.uint32)) | (np.isnan(f) & np.isnan(ref))
+    assert ok.all(), a[~ok][:5]

@@ -124,8 +124,8 @@ def test_mixed_precision_assembly(ctx):
 
 
 def test_mixed_accurate_assembly(ctx):
-    """the mixed-accurate EFIE assembly: far pairs in double-float arithmetic on the FP32
-    pipes, near pairs in FP64, c128 storage"""
+    """the mixed-accurate EFIE assembly: far pairs and Sauter-Schwab pairs in double-float
+    arithmetic on the FP32 pipes, c128 storage"""
     X = bg.raviartthomas(bg.icosphere(2))
     op = bg.Maxwell3D.singlelayer(wavenumber=2.0)
     Z = bg.assemble(op, X, X, precision=bg.MIXED_ACCURATE, ctx=ctx)
@@ -133,6 +133,20 @@ def test_mixed_accurate_assembly(ctx):
     Zo = O.assemble(_orc_op(op), _orc_qs(bg.defaultquadstrat(op, X, X)), X, X)
     assert rel_fro(Z, Zo) < 1e-11, rel_fro(Z, Zo)
     assert rel_entry(Z, Zo) < 1e-8, err_profile(Z, Zo)
+
+
+@pytest.mark.parametrize("which", ["singlelayer", "doublelayer"])
+def test_mixed_accurate_near_pairs(ctx, which):
+    """the double-float Sauter-Schwab pairs (face, edge and vertex classes) of the RT Maxwell
+    operators on a perturbed ellipsoid: every entry against the oracle's FP64"""
+    X = bg.raviartthomas(bg.ellipsoid(2, (1.0, 0.7, 1.3), perturb=0.1, rng=5))
+    op = getattr(bg.Maxwell3D, which)(wavenumber=4.0)
+    Z = bg.assemble(op, X, X, precision=bg.MIXED_ACCURATE, ctx=ctx)
+    Zo = O.assemble(_orc_op(op), _orc_qs(bg.defaultquadstrat(op, X, X)), X, X)
+    assert rel_fro(Z, Zo) < 1e-11, rel_fro(Z, Zo)
+    assert rel_entry(Z, Zo) < 1e-8, err_profile(Z, Zo)
+    Z64 = bg.assemble(op, X, X, precision=bg.FP64, ctx=ctx)
+    assert rel_entry(Z, Z64) < 1e-8, err_profile(Z, Z64)
 
 
 def test_c1_efie_assembly(ctx):
