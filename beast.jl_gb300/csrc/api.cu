@@ -1514,6 +1514,17 @@ int beast_batch_create(beast_ctx* ctx, const beast_qs_desc* qs, int64_t njobs, c
   // persistent grids: a few CTAs per SM (the far kernel holds ~130 registers per thread)
   L.grid_far = std::max(1, std::min(L.ntiles, ctx->num_sms * std::max(1, 512 / std::max(64, tile_m))));
   L.grid_near = ctx->num_sms * 8;
+  // the single layer's Sauter-Schwab pairs in double-float off the FP64 path: node tables now
+  // (graph capture comes later)
+  if (kind == BEAST_HH_SL && precision != BEAST_FP64 && qs->kind != BEAST_QS_DOUBLENUM) {
+    cudaError_t e = ss_tables(&ctx->ss_tabs, *qs, ctx->stream, L.ssdf_tab, L.ssdf_items);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) {
+      beast_batch_free(b);
+      return beast_fail(ctx, BEAST_ERR_CUDA, std::string("batch node tables: ") + cudaGetErrorString(e));
+    }
+    L.ssdf = 1;
+  }
   *out = b;
   return BEAST_OK;
 }

@@ -853,10 +853,14 @@ DEV bool near_is_ss32(const NearParams& P, int cls) {
 }
 
 // the same pairs in double-float arithmetic on the mixed-accurate path (real wavenumber):
-// k_near_ss_df; the double layer's common-face blocks (identically zero) stay with k_near
+// k_near_ss_df; the double layer's common-face blocks (identically zero) stay with k_near;
+// (k_near_ss_df), and the Helmholtz single layer's Sauter-Schwab pairs on P0 / P1 on the
+// mixed and mixed-accurate paths (k_near_hh_df, k_near_batch_df)
 DEV bool near_is_ssdf(const NearParams& P, int cls) {
-  return P.ssdf && cls >= 1 && cls <= 3 && P.tk == BEAST_RT && P.bk == BEAST_RT &&
-         (P.op.kind == BEAST_MW_SL || (P.op.kind == BEAST_MW_DL && cls != 3));
+  if (!P.ssdf || cls < 1 || cls > 3) return false;
+  if (P.tk == BEAST_RT && P.bk == BEAST_RT)
+    return P.op.kind == BEAST_MW_SL || (P.op.kind == BEAST_MW_DL && cls != 3);
+  return P.op.kind == BEAST_HH_SL && P.tk != BEAST_RT && P.bk != BEAST_RT;
 }
 
 // sh + sl += p, the rounding error of the addition kept (Knuth's TwoSum; no contraction)
@@ -2148,7 +2152,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_batch(BatchLaunch L) {
     P.flag = L.flag;
     P.ro = L.ron;
     P.ri = L.rin;
-    P.ssdf = 0;
+    P.ssdf = L.ssdf && J.op.gr == 0.0;  // those pairs run in k_near_batch_df
     P.bcells = P.tcells = nullptr;  // no refines strategies in a batch
     P.bchildren = P.tchildren = nullptr;
     P.bnchild = P.tnchild = 0;
@@ -2405,9 +2409,12 @@ cudaError_t launch_far_batch(const BatchLaunch& L, cudaStream_t st) {
 
 cudaError_t upload_tables(cudaStream_t st) { return upload_gl(st); }
 
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_batch_df(BatchLaunch L);  // below
+
 cudaError_t launch_near_batch(const BatchLaunch& L, cudaStream_t st) {
   // the Gauss-Legendre table is uploaded before (upload_tables): this launch may be captured
   k_near_batch<<<L.grid_near, 32 * NEAR_WARPS, 0, st>>>(L);
+  if (L.ssdf) k_near_batch_df<<<L.grid_near, 32 * NEAR_WARPS, 0, st>>>(L);
   return cudaGetLastError();
 }
 
@@ -2452,6 +2459,20 @@ static cudaError_t ss_table(std::map<int, void*>* cache, int cls, int n, cudaStr
   return cudaSuccess;
 }
 
+cudaError_t ss_tables(std::map<int, void*>* cache, const beast_qs_desc& qs, cudaStream_t st, const float2** tab,
+                      int* items) {
+  cudaError_t e = upload_gl(st);
+  if (e != cudaSuccess) return e;
+  const int ord[4] = {0, qs.ss_vert, qs.ss_edge, qs.ss_face};
+  tab[0] = nullptr;
+  items[0] = 0;
+  for (int c = 1; c <= 3; ++c) {
+    e = ss_table(cache, c, ord[c], st, &tab[c], &items[c]);
+    if (e != cudaSuccess) return e;
+  }
+  return cudaSuccess;
+}
+
 DEV void dfv3(const V3<double>& a, dfl::df* o) {
   o[0] = df_of(a.x);
   o[1] = df_of(a.y);
@@ -2465,19 +2486,10 @@ DEV void dfv3(const V3<double>& a, dfl::df* o) {
 // shared-memory sine table; per-lane moments as sloppy pair sums, the warp's totals as exact
 // pair sums, the 3 x 3 block from them in FP64 (nine lanes).  Real wavenumbers (the caller
 // keeps complex ones on k_near).
-template <bool SL>
-__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
-  __shared__ float s_tab[64][4];  // sin / cos(m pi/32)
-  for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
-  if (e >= P.nnear) return;
-  const NearPair np_ = P.near[e];
-  if (!near_is_ssdf(P, np_.cls)) return;
-  const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
-  const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
-  // shared vertices first, in the same order (as k_near_ss32: lanes 0..8 test one pair each)
+// shared vertices of a touching pair first, in the same order (SauterSchwabQuadrature.reorder):
+// lanes 0..8 test one vertex pair each (shared vertices coincide exactly), the first three
+// hits in (i, j) order from the ballot
+DEV void ss_order_warp(const Geo& t, const Geo& s, int lane, int* pt, int* ps) {
   const double dtol = 1.0e3 * 2.220446049250313e-16;
   bool hit = false;
   if (lane < 9) {
@@ -2485,7 +2497,7 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
     hit = dot(dd, dd) < dtol * dtol;
   }
   const unsigned hmask = __ballot_sync(0xffffffffu, hit);
-  int pt[3], ps[3], hits = 0, ti[3], si[3];
+  int hits = 0, ti[3], si[3];
   for (int b = 0; b < 9; ++b)
     if (((hmask >> b) & 1u) && hits < 3) {
       ti[hits] = b / 3;
@@ -2506,6 +2518,150 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
     for (int h = 0; h < hits; ++h) used |= si[h] == j;
     if (!used) ps[k++] = j;
   }
+}
+
+// the warp's total of a double-float value (exact pair sums over the butterfly), as FP64
+DEV double warp_total_df(dfl::df x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const dfl::df y{__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)};
+    x = dfl::add(x, y);
+  }
+  return fsplit::f2d(x.hi) + fsplit::f2d(x.lo);
+}
+
+// The Helmholtz single layer alpha G on a touching pair of P0 / P1 cells by the Sauter-Schwab
+// rule of class cls, every node in double-float arithmetic (real wavenumber kk): lanes over the
+// nodes, per shape pair (a, b) of the reordered vertices the moment sum_k w_k G_k lt_a ls_b
+// (P0: one moment, shape value 1), the warp's totals in FP64 on every lane.  z[i * nb + j]:
+// the block in the cells' own vertex order (alpha and the Jacobian 4 A_t A_s included).
+template <int TP1, int BP1>
+DEV void hh_sl_ss_df(const OpParams& op, const Geo& t, const Geo& s, int cls, const float2* tab, int items,
+                     const float (*s_tab)[4], int lane, C2<double>* z) {
+  constexpr int NT = TP1 ? 3 : 1, NB = BP1 ? 3 : 1;
+  int pt[3], ps[3];
+  ss_order_warp(t, s, lane, pt, ps);
+  dfl::df et1[3], et2[3], es1[3], es2[3];
+  dfv3(t.v[pt[1]] - t.v[pt[0]], et1);
+  dfv3(t.v[pt[2]] - t.v[pt[1]], et2);
+  dfv3(s.v[ps[1]] - s.v[ps[0]], es1);
+  dfv3(s.v[ps[2]] - s.v[ps[1]], es2);
+  const dfl::df kk = df_of(op.gi);
+  const dfl::df i4pi{DF_I4PI_HI, DF_I4PI_LO};
+  const dfl::df one = dfl::make(1.f);
+  dfl::df m[NT * NB][2];
+#pragma unroll
+  for (int q = 0; q < NT * NB; ++q) m[q][0] = m[q][1] = dfl::make(0.f);
+  for (int it = lane; it < items; it += 32) {
+    dfl::df v[SSDF_VALS];
+#pragma unroll
+    for (int q = 0; q < SSDF_VALS; ++q) {
+      const float2 f = tab[(int64_t)q * items + it];
+      v[q] = dfl::df{f.x, f.y};
+    }
+    const dfl::df X0 = v[0], X1 = v[1], Y0 = v[2], Y1 = v[3], D0 = v[4], D1 = v[5], w = v[6];
+    dfl::df r[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+      if (cls == 3)
+        r[c] = dfl::adds(dfl::mul(D0, et1[c]), dfl::mul(D1, et2[c]));
+      else if (cls == 2)
+        r[c] = dfl::adds(dfl::mul(D0, et1[c]), dfl::subs(dfl::mul(X1, et2[c]), dfl::mul(Y1, es2[c])));
+      else
+        r[c] = dfl::subs(dfl::adds(dfl::mul(X0, et1[c]), dfl::mul(X1, et2[c])),
+                         dfl::adds(dfl::mul(Y0, es1[c]), dfl::mul(Y1, es2[c])));
+    }
+    const dfl::df R2 = dfl::dot3s(r, r);
+    const dfl::df iR = dfl::rsqrt(R2);
+    const dfl::df R = dfl::mul(R2, iR);
+    dfl::df sn, cs;
+    dfl::sincos_tab(dfl::mul(kk, R), s_tab, &sn, &cs);
+    const dfl::df amp = dfl::mul(dfl::mul(iR, w), i4pi);  // w / (4 pi R)
+    const dfl::df cr = dfl::mul(amp, cs), ci = dfl::neg(dfl::mul(amp, sn));
+    // shape values at the node in the reordered vertex order: lt = (1 - X0, X0 - X1, X1)
+    const dfl::df lt[3] = {dfl::sub(one, X0), dfl::sub(X0, X1), X1};
+    const dfl::df ls[3] = {dfl::sub(one, Y0), dfl::sub(Y0, Y1), Y1};
+#pragma unroll
+    for (int a = 0; a < NT; ++a)
+#pragma unroll
+      for (int b = 0; b < NB; ++b) {
+        dfl::df f = TP1 ? lt[a] : one;
+        if (BP1) f = BP1 && TP1 ? dfl::mul(f, ls[b]) : ls[b];
+        m[a * NB + b][0] = dfl::adds(m[a * NB + b][0], TP1 || BP1 ? dfl::mul(f, cr) : cr);
+        m[a * NB + b][1] = dfl::adds(m[a * NB + b][1], TP1 || BP1 ? dfl::mul(f, ci) : ci);
+      }
+  }
+  const C2<double> al{op.ar, op.ai};
+  const double jac = 4.0 * t.area * s.area;
+#pragma unroll
+  for (int a = 0; a < NT; ++a)
+#pragma unroll
+    for (int b = 0; b < NB; ++b) {
+      const C2<double> M{warp_total_df(m[a * NB + b][0]), warp_total_df(m[a * NB + b][1])};
+      const int i = TP1 ? pt[a] : 0, j = BP1 ? ps[b] : 0;
+      z[i * NB + j] = cscale(jac, cmul(al, M));
+    }
+}
+
+// the Helmholtz single layer's Sauter-Schwab pairs (P0 / P1) of one assembly in double-float
+// (near_is_ssdf), one warp per pair
+template <int TP1, int BP1>
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_hh_df(NearParams P) {
+  __shared__ float s_tab[64][4];
+  for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
+  if (e >= P.nnear) return;
+  const NearPair np_ = P.near[e];
+  if (!near_is_ssdf(P, np_.cls)) return;
+  const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
+  const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
+  constexpr int NT = TP1 ? 3 : 1, NB = BP1 ? 3 : 1;
+  C2<double> z[NT * NB];
+  hh_sl_ss_df<TP1, BP1>(P.op, t, s, np_.cls, P.ssdf_tab[np_.cls], P.ssdf_items[np_.cls], s_tab, lane, z);
+  if (lane == 0)
+    for (int i = 0; i < NT; ++i)
+      for (int j = 0; j < NB; ++j)
+        store_c<double>(P.zcell, zidx(zrow_of(P.zrow, np_.p, NT, i), zcol_of(P.zcol, np_.q, NB, j), P.ldc),
+                        z[i * NB + j], P.zfmt);
+}
+
+// the batch's P0 single-layer Sauter-Schwab pairs in double-float (the pairs k_near_batch
+// skips), persistent over the device-counted near list
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_batch_df(BatchLaunch L) {
+  __shared__ float s_tab[64][4];
+  for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int n = min(*L.near_count, L.near_cap);
+  for (int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp; e < n; e += (int64_t)gridDim.x * NEAR_WARPS) {
+    const NearPairB nb = L.near[e];
+    const BatchJobDev& J = L.jobs[nb.job];
+    if (!(J.op.gr == 0.0 && nb.cls >= 1 && nb.cls <= 3)) continue;
+    const Geo t = load_geo(J.geo + (int64_t)J.tperm[nb.p] * GEO_STRIDE);
+    const Geo s = load_geo(J.geo + (int64_t)nb.q * GEO_STRIDE);
+    C2<double> z[1];
+    hh_sl_ss_df<0, 0>(J.op, t, s, nb.cls, L.ssdf_tab[nb.cls], L.ssdf_items[nb.cls], s_tab, lane, z);
+    if (lane == 0)
+      store_c<double>(J.Z, zidx(zrow_of(J.zrow, nb.p, 1, 0), zcol_of(J.zcol, nb.q, 1, 0), J.ldz), z[0], L.zfmt);
+  }
+}
+
+template <bool SL>
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
+  __shared__ float s_tab[64][4];  // sin / cos(m pi/32)
+  for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
+  if (e >= P.nnear) return;
+  const NearPair np_ = P.near[e];
+  if (!near_is_ssdf(P, np_.cls)) return;
+  const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
+  const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
+  int pt[3], ps[3];
+  ss_order_warp(t, s, lane, pt, ps);
   const int cls = np_.cls;
   const float2* tab = P.ssdf_tab[cls];
   const int items = P.ssdf_items[cls];
@@ -2658,21 +2814,21 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   P.ri = ri;
   P.fro = fro;
   P.fri = fri;
-  // Sauter-Schwab pairs of RT Maxwell operators on the mixed-accurate path (real wavenumber)
-  // in double-float arithmetic: their node tables first
-  P.ssdf = a.zcell_fmt == ZCELL_DF && a.op.gr == 0.0 && a.ts->kind == BEAST_RT && a.bs->kind == BEAST_RT &&
-           (a.op.kind == BEAST_MW_SL || a.op.kind == BEAST_MW_DL) && a.ss_tabs != nullptr &&
-           a.qs.kind != BEAST_QS_DOUBLENUM;
+  // Sauter-Schwab pairs in double-float arithmetic (real wavenumber): RT Maxwell single and
+  // double layers on the mixed-accurate path, the Helmholtz single layer on P0 / P1 off the
+  // FP64 path; their node tables first
+  const bool rt_mw = a.zcell_fmt == ZCELL_DF && a.ts->kind == BEAST_RT && a.bs->kind == BEAST_RT &&
+                     (a.op.kind == BEAST_MW_SL || a.op.kind == BEAST_MW_DL);
+  const bool hh_sl = a.precision != BEAST_FP64 && a.op.kind == BEAST_HH_SL && a.ts->kind != BEAST_RT &&
+                     a.bs->kind != BEAST_RT;
+  P.ssdf = (rt_mw || hh_sl) && a.op.gr == 0.0 && a.ss_tabs != nullptr && a.qs.kind != BEAST_QS_DOUBLENUM;
   for (int c = 0; c < 4; ++c) {
     P.ssdf_tab[c] = nullptr;
     P.ssdf_items[c] = 0;
   }
   if (P.ssdf) {
-    const int ord[4] = {0, a.qs.ss_vert, a.qs.ss_edge, a.qs.ss_face};
-    for (int c = 1; c <= 3; ++c) {
-      e = ss_table(a.ss_tabs, c, ord[c], st, &P.ssdf_tab[c], &P.ssdf_items[c]);
-      if (e != cudaSuccess) return e;
-    }
+    e = ss_tables(a.ss_tabs, a.qs, st, P.ssdf_tab, P.ssdf_items);
+    if (e != cudaSuccess) return e;
   }
   P.bcells = a.bs->cells;
   P.bchildren = a.bs->mesh->children;
@@ -2683,10 +2839,18 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   unsigned blocks = (unsigned)((nnear + NEAR_WARPS - 1) / NEAR_WARPS);
   if (P.ss32) k_near_ss32<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   if (P.ssdf) {
-    if (a.op.kind == BEAST_MW_SL)
+    if (rt_mw && a.op.kind == BEAST_MW_SL)
       k_near_ss_df<true><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
-    else
+    else if (rt_mw)
       k_near_ss_df<false><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
+    else if (P.tk == BEAST_P1 && P.bk == BEAST_P1)
+      k_near_hh_df<1, 1><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
+    else if (P.tk == BEAST_P1)
+      k_near_hh_df<1, 0><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
+    else if (P.bk == BEAST_P1)
+      k_near_hh_df<0, 1><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
+    else
+      k_near_hh_df<0, 0><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   }
   k_near<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   if (P.qs.kind == BEAST_QS_TEST_REFINES_TRIAL || P.qs.kind == BEAST_QS_TRIAL_REFINES_TEST)

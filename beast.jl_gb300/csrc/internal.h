@@ -250,7 +250,16 @@ struct BatchLaunch {
   int* flag;
   int tile_m, tile_q;           // test cells per CTA (= threads), trial cells staged per CTA
   int grid_far, grid_near;      // persistent CTAs
+  // single-layer Sauter-Schwab pairs in double-float (not on the FP64 path): node tables per
+  // class 1..3 (ss_tables)
+  int ssdf = 0;
+  const float2* ssdf_tab[4] = {nullptr, nullptr, nullptr, nullptr};
+  int ssdf_items[4] = {0, 0, 0, 0};
 };
+// the double-float Sauter-Schwab node tables of the strategy's orders (class 1..3: vertex,
+// edge, face), from the context's cache or built now on `st` (not inside a graph capture)
+cudaError_t ss_tables(std::map<int, void*>* cache, const beast_qs_desc& qs, cudaStream_t st,
+                      const float2** tab, int* items);
 cudaError_t launch_far_batch(const BatchLaunch& L, cudaStream_t st);
 // the constant tables of the near-pair kernels (Gauss-Legendre nodes), once per device; must
 // run before a launch that is captured in a graph

@@ -185,6 +185,17 @@ def test_helmholtz_singularity_extraction(ctx, which, spaces):
     _check(op, sp[spaces[:2]], sp[spaces[2:]], ctx)
 
 
+@pytest.mark.parametrize("spaces", ["p0p0", "p1p1", "p0p1", "p1p0"])
+def test_helmholtz_single_layer_double_float_near(ctx, spaces):
+    """the Helmholtz single layer's Sauter-Schwab pairs in double-float arithmetic (the
+    mixed-accurate and mixed paths, real wavenumber), with the extraction pairs of the
+    perturbed ellipsoid beside them in FP64: every entry against the oracle"""
+    m = bg.ellipsoid(2, (1.0, 0.7, 1.3), perturb=0.3, rng=3)
+    sp = {"p1": bg.lagrangec0d1(m), "p0": bg.lagrangecxd0(m)}
+    op = bg.Helmholtz3D.singlelayer(wavenumber=2.0)
+    _check(op, sp[spaces[:2]], sp[spaces[2:]], ctx, tol=1e-8, precision=bg.MIXED_ACCURATE)
+
+
 @pytest.mark.parametrize("which", ["singlelayer", "doublelayer"])
 def test_maxwell_singularity_extraction(ctx, which):
     """the Maxwell strategy's Wilton pairs: seven on the perturbed ellipsoid at k = 0.3"""
