@@ -2483,7 +2483,7 @@ DEV void dfv3(const V3<double>& a, dfl::df* o) {
 // double-float arithmetic on the FP32 pipes (GB300's FP64 pipe is a small fraction of its FP32
 // rate): one warp per pair, lanes over the nodes, x - y from the maps' own factors (D = X - Y)
 // on double-float edge vectors, 1/R by the pair reciprocal square root, exp(-ikR) from the
-// shared-memory sine table; per-lane moments as sloppy pair sums, the warp's totals as exact
+// shared-memory sine table; per-lane moments as running pair sums, the warp's totals as exact
 // pair sums, the 3 x 3 block from them in FP64 (nine lanes).  Real wavenumbers (the caller
 // keeps complex ones on k_near).
 // shared vertices of a touching pair first, in the same order (SauterSchwabQuadrature.reorder):
@@ -2587,8 +2587,8 @@ DEV void hh_sl_ss_df(const OpParams& op, const Geo& t, const Geo& s, int cls, co
       for (int b = 0; b < NB; ++b) {
         dfl::df f = TP1 ? lt[a] : one;
         if (BP1) f = BP1 && TP1 ? dfl::mul(f, ls[b]) : ls[b];
-        m[a * NB + b][0] = dfl::adds(m[a * NB + b][0], TP1 || BP1 ? dfl::mul(f, cr) : cr);
-        m[a * NB + b][1] = dfl::adds(m[a * NB + b][1], TP1 || BP1 ? dfl::mul(f, ci) : ci);
+        dfl::acc(m[a * NB + b][0], TP1 || BP1 ? dfl::mul(f, cr) : cr);
+        dfl::acc(m[a * NB + b][1], TP1 || BP1 ? dfl::mul(f, ci) : ci);
       }
   }
   const C2<double> al{op.ar, op.ai};
@@ -2597,7 +2597,7 @@ DEV void hh_sl_ss_df(const OpParams& op, const Geo& t, const Geo& s, int cls, co
   for (int a = 0; a < NT; ++a)
 #pragma unroll
     for (int b = 0; b < NB; ++b) {
-      const C2<double> M{warp_total_df(m[a * NB + b][0]), warp_total_df(m[a * NB + b][1])};
+      const C2<double> M{warp_total_df(dfl::norm(m[a * NB + b][0])), warp_total_df(dfl::norm(m[a * NB + b][1]))};
       const int i = TP1 ? pt[a] : 0, j = BP1 ? ps[b] : 0;
       z[i * NB + j] = cscale(jac, cmul(al, M));
     }
@@ -2716,8 +2716,8 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
         a[c] = xi[c];
         b[c] = eta[c];
       }
-      m[0] = dfl::adds(m[0], cr);
-      m[1] = dfl::adds(m[1], ci);
+      dfl::acc(m[0], cr);
+      dfl::acc(m[1], ci);
     } else {
       // grad G = c r, c = -(i k + 1/R) G / R
       const dfl::df pr = dfl::neg(dfl::mul(iR, iR)), pi = dfl::neg(dfl::mul(kk, iR));
@@ -2738,25 +2738,25 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
       }
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        m[16 + 2 * c] = dfl::adds(m[16 + 2 * c], dfl::mul(r[c], cr));
-        m[17 + 2 * c] = dfl::adds(m[17 + 2 * c], dfl::mul(r[c], ci));
+        dfl::acc(m[16 + 2 * c], dfl::mul(r[c], cr));
+        dfl::acc(m[17 + 2 * c], dfl::mul(r[c], ci));
       }
     }
-    m[2] = dfl::adds(m[2], dfl::mul(s0, cr));
-    m[3] = dfl::adds(m[3], dfl::mul(s0, ci));
+    dfl::acc(m[2], dfl::mul(s0, cr));
+    dfl::acc(m[3], dfl::mul(s0, ci));
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      m[4 + 2 * c] = dfl::adds(m[4 + 2 * c], dfl::mul(a[c], cr));
-      m[5 + 2 * c] = dfl::adds(m[5 + 2 * c], dfl::mul(a[c], ci));
-      m[10 + 2 * c] = dfl::adds(m[10 + 2 * c], dfl::mul(b[c], cr));
-      m[11 + 2 * c] = dfl::adds(m[11 + 2 * c], dfl::mul(b[c], ci));
+      dfl::acc(m[4 + 2 * c], dfl::mul(a[c], cr));
+      dfl::acc(m[5 + 2 * c], dfl::mul(a[c], ci));
+      dfl::acc(m[10 + 2 * c], dfl::mul(b[c], cr));
+      dfl::acc(m[11 + 2 * c], dfl::mul(b[c], ci));
     }
   }
   // the warp's totals (exact pair sums), then FP64
   double md[22];
 #pragma unroll
   for (int q = 0; q < 22; ++q) {
-    dfl::df x = m[q];
+    dfl::df x = dfl::norm(m[q]);
     if (q < 2 && !SL) x = dfl::make(0.f);
     if (q >= NM && SL) x = dfl::make(0.f);
 #pragma unroll

@@ -150,23 +150,39 @@ DF_HD void sincos(df th, df* s, df* c) {
 }
 
 // sincos with the table of m pi/32 passed in (shared memory in a kernel: lanes read different
-// entries) and pair sums that do not cancel taken as sloppy sums; the argument reduction keeps
-// the exact sums.  Same range and error class as sincos.
+// entries), on fewer FP32 additions than sincos: th.hi - n C0 is exact (Sterbenz: th.hi and
+// n C0 lie within a factor 2 of each other, or n = 0), the small rest (th.lo, the low parts
+// of n pi/32) is summed in FP32, and the sums with one dominant term (t + its cubic term,
+// 1 - t^2/2) are fast two-sums.  Absolute error below 1e-11 for |th| < 2^10.
 DF_HD void sincos_tab(df th, const float (*tab)[4], df* s, df* c) {
   const float n = rintf(mul_rn(th.hi, DF_32_OVER_PI));
-  df t = add(th, neg(two_prod(n, DF_PI32_0)));
-  t = add(t, neg(two_prod(n, DF_PI32_1)));
-  t = add(t, -mul_rn(n, DF_PI32_2));
+  const df p0 = two_prod(n, DF_PI32_0);
+  const float s0 = sub_rn(th.hi, p0.hi);
+  float e = sub_rn(th.lo, p0.lo);
+  e = fmaf(-n, DF_PI32_1, e);
+  e = fmaf(-n, DF_PI32_2, e);
+  const df t = two_sum(s0, e);
   const int m = ((int)n) & 63;
   const float t2 = mul_rn(t.hi, t.hi);
   const float q = fmaf(t2, fmaf(t2, -1.f / 5040.f, 1.f / 120.f), -1.f / 6.f);
-  const df st = add(t, mul_rn(mul_rn(t.hi, t2), q));
+  const df st = fast_two_sum(t.hi, add_rn(t.lo, mul_rn(mul_rn(t.hi, t2), q)));
   const float r4 = mul_rn(mul_rn(t2, t2), fmaf(t2, -1.f / 720.f, 1.f / 24.f));
-  const df ct = add(add(make(1.f), neg(scale(mul(t, t), 0.5f))), r4);
+  const df h = scale(mul(t, t), 0.5f);  // t^2 / 2 < 1.2e-3
+  const df c1 = fast_two_sum(1.f, -h.hi);
+  const df ct = fast_two_sum(c1.hi, add_rn(c1.lo, sub_rn(r4, h.lo)));
   const df sm = {tab[m][0], tab[m][1]}, cm = {tab[m][2], tab[m][3]};
   *s = adds(mul(sm, ct), mul(cm, st));
   *c = subs(mul(cm, ct), mul(sm, st));
 }
+
+// a += x for a running sum whose low part is normalised only at the end (norm): one TwoSum
+// of the high parts and two plain additions instead of the sloppy sum's three more
+DF_HD void acc(df& a, df x) {
+  const df s = two_sum(a.hi, x.hi);
+  a.hi = s.hi;
+  a.lo = add_rn(a.lo, add_rn(s.lo, x.lo));
+}
+DF_HD df norm(df a) { return fast_two_sum(a.hi, a.lo); }
 
 // Helmholtz / Maxwell Green's function exp(-i k R) / (4 pi R) for a real wavenumber k
 DF_HD void green(df R, df k, df* re, df* im) {

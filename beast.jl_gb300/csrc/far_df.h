@@ -81,14 +81,21 @@ DF_HD void efie_far_pair(const df* d, const df (*tau)[3], const df (*sig)[3], in
 //   * R^2 = (A_a + Q_b) - 2 P_ab with A_a = |d + xi_a|^2 (per test point), Q_b = |eta_b|^2 -
 //     2 d.eta_b (per trial point) and P_ab = xi_a.eta_b, which the M1 moment needs anyway;
 //   * 1 / R from a pair reciprocal square root, R = R^2 / R, the weight folded into 1/(4 pi R);
-//   * sums whose terms do not cancel far below their size (moments, dot products of small
-//     vectors, the angle sum of the sine / cosine) as sloppy pair sums;
+//   * sums whose terms do not cancel far below their size (dot products of small vectors, the
+//     angle sum of the sine / cosine) as sloppy pair sums, the moments as running sums
+//     normalised once;
 //   * the table of sin / cos(m pi/32) read from `tab` (shared memory in the kernel);
 //   * the 3 x 3 block from per-row and per-column parts: z_ij = C - S_j - T_i + (tau_i.sig_j) D
 //     with C = a4 M1 + beta M0, S_j = a4 sig_j.V1, T_i = a4 tau_i.V2, D = a4 M0, a4 = alpha/4.
 // eta2[b] = |eta_b|^2 (staged with the trial cell).  Matches efie_far_pair to the pair
 // arithmetic's accuracy.
 DF_HD cdf cadds(cdf a, cdf b) { return {adds(a.re, b.re), adds(a.im, b.im)}; }
+// running complex sums, normalised once at the end (acc / norm of dfloat.h)
+DF_HD void cacc(cdf& a, cdf x) {
+  acc(a.re, x.re);
+  acc(a.im, x.im);
+}
+DF_HD cdf cnorm(cdf a) { return {norm(a.re), norm(a.im)}; }
 DF_HD cdf csubs(cdf a, cdf b) { return {subs(a.re, b.re), subs(a.im, b.im)}; }
 DF_HD cdf cmuls(cdf a, cdf b) {
   return {subs(mul(a.re, b.re), mul(a.im, b.im)), adds(mul(a.re, b.im), mul(a.im, b.re))};
@@ -139,23 +146,28 @@ DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3
       sincos_tab(mul(k, R), tab, &sn, &cs);
       const df amp = mul(iR, wq);  // w_b / (4 pi R)
       const cdf K{mul(amp, cs), neg(mul(amp, sn))};
-      U0[a] = cadds(U0[a], K);
+      cacc(U0[a], K);
       const cdf wK = cscale(K, wo[a]);
-      T = cadds(T, wK);
-      M1 = cadds(M1, cscale(wK, P));
+      cacc(T, wK);
+      cacc(M1, cscale(wK, P));
     }
-    M0 = cadds(M0, T);
-    for (int c = 0; c < 3; ++c) V2[c] = cadds(V2[c], cscale(T, eta[b][c]));
+    T = cnorm(T);
+    cacc(M0, T);
+    for (int c = 0; c < 3; ++c) cacc(V2[c], cscale(T, eta[b][c]));
   }
+  M0 = cnorm(M0);
+  M1 = cnorm(M1);
+  for (int c = 0; c < 3; ++c) V2[c] = cnorm(V2[c]);
   cdf V1[3];
   for (int c = 0; c < 3; ++c) V1[c] = cdf{z0, z0};
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
   for (int a = 0; a < NO; ++a) {
-    const cdf s = cscale(U0[a], wo[a]);
-    for (int c = 0; c < 3; ++c) V1[c] = cadds(V1[c], cscale(s, xi[a][c]));
+    const cdf s = cscale(cnorm(U0[a]), wo[a]);
+    for (int c = 0; c < 3; ++c) cacc(V1[c], cscale(s, xi[a][c]));
   }
+  for (int c = 0; c < 3; ++c) V1[c] = cnorm(V1[c]);
   const cdf a4{scale(alpha.re, 0.25f), scale(alpha.im, 0.25f)};
   const cdf C = cadds(cmuls(a4, M1), cmuls(beta, M0));
   const cdf D = cmuls(a4, M0);

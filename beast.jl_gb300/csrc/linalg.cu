@@ -1679,19 +1679,28 @@ __global__ void k_gemv_partial_c128_df(int64_t n, const double2* A, int64_t lda,
   const int64_t c0 = n * s / MV_SLABS, c1 = n * (s + 1) / MV_SLABS;
   if (i >= n) return;
   float2 h = make_float2(0.f, 0.f), l = h;
-#pragma unroll 4
-  for (int64_t j = c0; j < c1; ++j) {
-    const float4 xv = xs[j];
+  auto term = [&](const double2 a, const float4 xv) {
     const float2 X1 = make_float2(xv.x, xv.y), X2 = make_float2(-xv.y, xv.x);
     const float2 L1 = make_float2(xv.z, xv.w), L2 = make_float2(-xv.w, xv.z);
-    const double2 a = A[i + j * lda];
     float2 ar, ai;
     fsplit::split_f64(a.x, &ar.x, &ar.y);
     fsplit::split_f64(a.y, &ai.x, &ai.y);
     cdf_acc2(make_float2(ar.x, ar.x), make_float2(ai.x, ai.x), X1, X2, L1, L2, h, l);
     l = __ffma2_rn(make_float2(ar.y, ar.y), X1, l);
     l = __ffma2_rn(make_float2(ai.y, ai.y), X2, l);
+  };
+  // eight streaming loads in flight per thread before their arithmetic (the matrix is read
+  // once per matvec; its latency, not the FP32 work, set the pace with four)
+  const double2* Ai = A + i;
+  int64_t j = c0;
+  for (; j + 8 <= c1; j += 8) {
+    double2 a[8];
+#pragma unroll
+    for (int u = 0; u < 8; ++u) a[u] = __ldcs(Ai + (j + u) * lda);
+#pragma unroll
+    for (int u = 0; u < 8; ++u) term(a[u], xs[j + u]);
   }
+  for (; j < c1; ++j) term(__ldcs(Ai + j * lda), xs[j]);
   part[2 * (s * n + i)] = (double)h.x + (double)l.x;
   part[2 * (s * n + i) + 1] = (double)h.y + (double)l.y;
 }

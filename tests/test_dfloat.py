@@ -36,6 +36,9 @@ void t_ops(const double* a, const double* b, int64_t n, double* out) {  // add, 
 void t_sincos(const double* th, int64_t n, double* s, double* c) {
   for (int64_t i = 0; i < n; ++i) { df a, b; dfl::sincos(from(th[i]), &a, &b); s[i] = to(a); c[i] = to(b); }
 }
+void t_sincos_tab(const double* th, int64_t n, double* s, double* c) {
+  for (int64_t i = 0; i < n; ++i) { df a, b; sincos_tab(from(th[i]), sincos_tab_host, &a, &b); s[i] = to(a); c[i] = to(b); }
+}
 void t_green(const double* R, const double* k, int64_t n, double* out) {
   for (int64_t i = 0; i < n; ++i) { df re, im; green(from(R[i]), from(k[i]), &re, &im); out[2 * i] = to(re); out[2 * i + 1] = to(im); }
 }
@@ -92,7 +95,7 @@ def lib(tmp_path_factory):
     subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I", CSRC, str(src), "-o", str(so)],
                    check=True)
     L = C.CDLL(str(so))
-    for f in ("t_two", "t_ops", "t_sincos", "t_green", "t_efie_pair"):
+    for f in ("t_two", "t_ops", "t_sincos", "t_sincos_tab", "t_green", "t_efie_pair"):
         getattr(L, f).restype = None
     return L
 
@@ -130,6 +133,20 @@ def test_sincos(lib):
     th = np.concatenate([np.linspace(-7, 7, 20001), rng.uniform(-1e3, 1e3, 50000)])
     s, c = np.zeros_like(th), np.zeros_like(th)
     lib.t_sincos(_p(th), C.c_int64(th.size), _p(s), _p(c))
+    x = _pair(th)
+    assert np.abs(s - np.sin(x)).max() < 1e-11
+    assert np.abs(c - np.cos(x)).max() < 1e-11
+
+
+def test_sincos_with_the_table(lib):
+    """the kernels' sine / cosine (table passed in, fewer FP32 additions): same error class as
+    sincos over the range of k R on the assembly path, and at the reduction's edges"""
+    rng = np.random.default_rng(5)
+    edges = (np.arange(-64, 65) * np.pi / 32)[:, None] + np.array([-1e-9, -1e-12, 0.0, 1e-12, 1e-9])[None, :]
+    th = np.concatenate([np.linspace(-7, 7, 20001), rng.uniform(-1e3, 1e3, 50000), edges.ravel(),
+                         rng.uniform(0, 1e-6, 1000)])
+    s, c = np.zeros_like(th), np.zeros_like(th)
+    lib.t_sincos_tab(_p(th), C.c_int64(th.size), _p(s), _p(c))
     x = _pair(th)
     assert np.abs(s - np.sin(x)).max() < 1e-11
     assert np.abs(c - np.cos(x)).max() < 1e-11
