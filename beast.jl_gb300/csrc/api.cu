@@ -427,6 +427,8 @@ int beast_space_upload(beast_ctx* ctx, const beast_mesh* mesh, int kind, int64_t
   up((void**)&s->fn_cell, s->h_fn_cell.data(), sizeof(int) * s->h_fn_cell.size());
   up((void**)&s->fn_shape, s->h_fn_shape.data(), sizeof(int) * s->h_fn_shape.size());
   up((void**)&s->fn_coeff, s->h_fn_coeff.data(), sizeof(double) * s->h_fn_coeff.size());
+  s->unit_coef = true;
+  for (double c : s->h_fn_coeff) s->unit_coef = s->unit_coef && (c == 1.0 || c == -1.0);
   // Zcell row order on the test side: active cells by their first (lowest) function, so that
   // consecutive functions read nearby Zcell rows in the gather
   {

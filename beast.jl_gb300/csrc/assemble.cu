@@ -1706,7 +1706,9 @@ __global__ void __launch_bounds__(256) k_gather_df(GatherArgs G, const int64_t* 
 // read once, in full sectors.  Sums in FP32 for c64 -> c64, in pairs of floats (sloppy sums,
 // as k_gather_df) for double-float blocks, else in FP64.
 constexpr int GATHER_E_MAX = 4;  // entries per function handled from registers
-template <int ZC, int OC64>
+// UC (double-float blocks only): every coefficient is +1 or -1, so a term is the block value
+// with a sign and the sums need no pair products.
+template <int ZC, int OC64, int UC = 0>
 __global__ void __launch_bounds__(256) k_gather_e(GatherArgs G, const int64_t* tptr, const double* tcoef,
                                                   const int64_t* bptr, const double* bcoef, int64_t nrows) {
   typedef typename std::conditional<ZC == ZCELL_C64 && OC64, float, double>::type A;
@@ -1772,11 +1774,26 @@ __global__ void __launch_bounds__(256) k_gather_e(GatherArgs G, const int64_t* t
       const float4* zc = reinterpret_cast<const float4*>(G.zcell);
       dfl::df re = dfl::make(0.f), im = dfl::make(0.f);
       for (int f = 0; f < nc; ++f) {
-        const dfl::df b = f < GATHER_E_MAX ? s_bd[nn][f] : df_coef(bcoef[bptr[n] + f]);
-        for (int e = 0; e < ne; ++e)
-          df_acc(re, im, zc[c0 + (int64_t)f * G.ldc + e],
-                 dfl::mul(e < GATHER_E_MAX ? tcd[e] : df_coef(tcoef[e0 + e]), b));
+        if (UC) {
+          const float sb = f < GATHER_E_MAX ? s_bd[nn][f].hi : fsplit::to_float_rn(bcoef[bptr[n] + f]);
+          for (int e = 0; e < ne; ++e) {
+            const float sg = sb * (e < GATHER_E_MAX ? tcd[e].hi : fsplit::to_float_rn(tcoef[e0 + e]));
+            const float4 z = zc[c0 + (int64_t)f * G.ldc + e];
+            dfl::acc(re, dfl::df{sg * z.x, sg * z.y});
+            dfl::acc(im, dfl::df{sg * z.z, sg * z.w});
+          }
+        } else {
+          const dfl::df b = f < GATHER_E_MAX ? s_bd[nn][f] : df_coef(bcoef[bptr[n] + f]);
+          for (int e = 0; e < ne; ++e) {
+            const float4 z = zc[c0 + (int64_t)f * G.ldc + e];
+            const dfl::df c = dfl::mul(e < GATHER_E_MAX ? tcd[e] : df_coef(tcoef[e0 + e]), b);
+            dfl::acc(re, dfl::mul(dfl::df{z.x, z.y}, c));
+            dfl::acc(im, dfl::mul(dfl::df{z.z, z.w}, c));
+          }
+        }
       }
+      re = dfl::norm(re);
+      im = dfl::norm(im);
       if (OC64) {
         out(n, (double)dfl::add_rn(re.hi, re.lo), (double)dfl::add_rn(im.hi, im.lo));
       } else {
@@ -2873,14 +2890,19 @@ cudaError_t launch_gather(const GatherArgs& g, cudaStream_t st) {
                                         bs->fn_ptr, bs->fn_cell, bs->fn_shape, bs->fn_coeff, nst, \
                                         nsb, nrows)
   if (g.entry_layout) {
-#define GATHER_E(ZC, OC) \
-  k_gather_e<ZC, OC><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_coeff, bs->fn_ptr, bs->fn_coeff, nrows)
+#define GATHER_E(ZC, OC, UC) \
+  k_gather_e<ZC, OC, UC><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_coeff, bs->fn_ptr, bs->fn_coeff, nrows)
+    const bool uc = ts->unit_coef && bs->unit_coef;
     if (g.zcell_fmt == ZCELL_DF) {
-      if (g.z_c64) GATHER_E(ZCELL_DF, 1); else GATHER_E(ZCELL_DF, 0);
+      if (uc) {
+        if (g.z_c64) GATHER_E(ZCELL_DF, 1, 1); else GATHER_E(ZCELL_DF, 0, 1);
+      } else {
+        if (g.z_c64) GATHER_E(ZCELL_DF, 1, 0); else GATHER_E(ZCELL_DF, 0, 0);
+      }
     } else if (g.zcell_fmt == ZCELL_C64) {
-      if (g.z_c64) GATHER_E(ZCELL_C64, 1); else GATHER_E(ZCELL_C64, 0);
+      if (g.z_c64) GATHER_E(ZCELL_C64, 1, 0); else GATHER_E(ZCELL_C64, 0, 0);
     } else {
-      if (g.z_c64) GATHER_E(ZCELL_C128, 1); else GATHER_E(ZCELL_C128, 0);
+      if (g.z_c64) GATHER_E(ZCELL_C128, 1, 0); else GATHER_E(ZCELL_C128, 0, 0);
     }
 #undef GATHER_E
   } else if (g.zcell_fmt == ZCELL_DF) {

@@ -108,6 +108,7 @@ struct beast_space {
   // when no (cell, shape) belongs to two entries (RT on a closed or open surface, P0, P1): the
   // cell-pair blocks can then be laid out by entries (ZLAYOUT_ENTRY)
   bool injective = false;
+  bool unit_coef = false;  // every function coefficient is +1 or -1 (RT, P0, P1 spaces)
   std::vector<int> h_cs2e;
   int* zrow_entry = nullptr;   // [ncells][nshapes] by Zcell position: the entry, or -1
   std::vector<int> h_ad_dof;   // host copy of the assembly data
