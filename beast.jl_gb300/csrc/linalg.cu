@@ -20,7 +20,6 @@
 #include <cmath>
 #include <mutex>
 #include <string>
-#include <type_traits>
 #include <vector>
 
 #include "fsplit.h"
@@ -639,147 +638,6 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
   for (int e = tid; e < TRI * TRI; e += 256) {
     const int r = e & (TRI - 1), c = e >> 6;
     inv[e] = Ls[r * LD + c];
-  }
-}
-
-// ---- the symmetric diagonal block, blocked by 16 -----------------------------------------
-// The same outputs as k_lu_inv64<float2, true> (the factored block in A: L strictly below,
-// U = D L^T on and above the diagonal; L^{-1} and U^{-1} = L^{-T} D^{-1} in inv) from a blocked
-// LDL^T of the lower triangle, with 15 block barriers instead of 64:
-//   for K = 0..3 (b = 16 K):
-//     1. warp 0: LDL^T of the 16 x 16 diagonal block by 16 pivot steps with warp
-//        synchronisation only, the same row operations applied to the identity giving
-//        L_KK^{-1};
-//     2. T = S_IK L_KK^{-T} for the rows below (= L_IK D_K), L_IK = T D_K^{-1};
-//     3. the rank-16 update S_IJ -= L_IK T_JK^T of the lower triangle below;
-//   then the off-diagonal blocks of L^{-1} by distance from the diagonal:
-//     L^{-1}_IJ = -L^{-1}_II sum_{M=J}^{I-1} L_IM L^{-1}_MJ.
-// A zero pivot sets *info (1-based column) and the kernel stops.
-constexpr int LDL_B = 16;
-constexpr int LDL_LD = TRI + 1;  // row stride (complex) of the staged matrices
-constexpr int LDL_TLD = LDL_B + 1;
-size_t ldl64_smem() { return (size_t)(2 * TRI * LDL_LD + TRI * LDL_TLD) * sizeof(float2); }
-
-__global__ void __launch_bounds__(256) k_ldl64(float2* A, int64_t lda, int64_t j0, int kb, int* info,
-                                               float2* inv) {
-  extern __shared__ __align__(16) unsigned char smraw[];
-  float2* S = reinterpret_cast<float2*>(smraw);  // the block's lower triangle, then L (below) and D
-  float2* Li = S + TRI * LDL_LD;                 // L^{-1} (lower triangle, unit diagonal)
-  float2* Tm = Li + TRI * LDL_LD;                // T of the current step (rows below), then P
-  __shared__ float2 s_dinv[TRI];
-  __shared__ int s_bad;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const float2 zero = make_float2(0.f, 0.f), one = make_float2(1.f, 0.f);
-  for (int e = tid; e < TRI * TRI; e += 256) {
-    const int r = e & (TRI - 1), c = e >> 6;
-    float2 v = zero;
-    if (c <= r) v = (r < kb && c < kb) ? A[(j0 + r) + (j0 + c) * lda] : (r == c ? one : zero);
-    S[r * LDL_LD + c] = v;
-    Li[r * LDL_LD + c] = (r == c) ? one : zero;
-  }
-  if (tid == 0) s_bad = 0;
-  __syncthreads();
-  for (int K = 0; K < TRI / LDL_B; ++K) {
-    const int b = K * LDL_B;
-    if (warp == 0) {
-      // lane: column cc of the trailing update, rows rh, rh + 2, ..; the row operations on
-      // L^{-1}: row lr = 1 + (lane >> 2) .. (lanes in fours), columns (lane & 3) + 4 j
-      const int cc = lane & 15, rh = lane >> 4;
-      for (int p = 0; p < LDL_B; ++p) {
-        const float2 d = S[(b + p) * LDL_LD + b + p];
-        float2 di;
-        if (!crecip(d, di)) {  // d is the same on every lane: a uniform exit
-          if (lane == 0) s_bad = (int)(j0 + b + p + 1);
-          break;
-        }
-        if (cc > p) {
-          const float2 scp = cmulx(S[(b + cc) * LDL_LD + b + p], di);  // S[c][p] / d
-#pragma unroll
-          for (int j = 0; j < LDL_B / 2; ++j) {
-            const int r = rh + 2 * j;
-            if (r >= cc) cfms(S[(b + r) * LDL_LD + b + cc], S[(b + r) * LDL_LD + b + p], scp);
-          }
-        }
-        // L^{-1} rows r > p: row_r -= l_r row_p on columns c <= p (l_r = S[r][p] / d, unscaled
-        // column read here, scaled below)
-        for (int e = lane; e < (LDL_B - 1 - p) * (p + 1); e += 32) {
-          const int r = p + 1 + e / (p + 1), c = e % (p + 1);
-          const float2 l = cmulx(S[(b + r) * LDL_LD + b + p], di);
-          cfms(Li[(b + r) * LDL_LD + b + c], l, Li[(b + p) * LDL_LD + b + c]);
-        }
-        __syncwarp();
-        if (lane > p && lane < LDL_B) S[(b + lane) * LDL_LD + b + p] = cmulx(S[(b + lane) * LDL_LD + b + p], di);
-        if (lane == 0) s_dinv[b + p] = di;
-        __syncwarp();
-      }
-    }
-    __syncthreads();
-    if (s_bad) {  // uniform
-      if (tid == 0) atomicCAS(info, 0, s_bad);
-      return;
-    }
-    const int r0 = b + LDL_B, nr = TRI - r0;
-    if (nr > 0) {
-      // T[r][c] = sum_{m <= c} S[r][b + m] L^{-1}[b + c][b + m]; L[r][b + c] = T[r][c] / d
-      for (int e = tid; e < nr * LDL_B; e += 256) {
-        const int r = r0 + (e >> 4), c = e & 15;
-        float2 acc = S[r * LDL_LD + b + c];
-        for (int m = 0; m < c; ++m) cfma(acc, S[r * LDL_LD + b + m], Li[(b + c) * LDL_LD + b + m]);
-        Tm[(r - r0) * LDL_TLD + c] = acc;
-      }
-      __syncthreads();
-      for (int e = tid; e < nr * LDL_B; e += 256) {
-        const int r = r0 + (e >> 4), c = e & 15;
-        S[r * LDL_LD + b + c] = cmulx(Tm[(r - r0) * LDL_TLD + c], s_dinv[b + c]);
-      }
-      // rank-16 update of the lower triangle below: S[r][c] -= sum_m L[r][b + m] T[c][m]
-      // (L written above by other threads: read T for row r too, L = T D^{-1})
-      for (int e = tid; e < nr * nr; e += 256) {
-        const int r = r0 + e % nr, c = r0 + e / nr;
-        if (r < c) continue;
-        float2 acc = S[r * LDL_LD + c];
-#pragma unroll 4
-        for (int m = 0; m < LDL_B; ++m)
-          cfms(acc, cmulx(Tm[(r - r0) * LDL_TLD + m], s_dinv[b + m]), Tm[(c - r0) * LDL_TLD + m]);
-        S[r * LDL_LD + c] = acc;
-      }
-      __syncthreads();
-    }
-  }
-  // off-diagonal blocks of L^{-1}, by distance dl from the diagonal
-  for (int dl = 1; dl < TRI / LDL_B; ++dl) {
-    const int npair = TRI / LDL_B - dl;
-    for (int e = tid; e < npair * LDL_B * LDL_B; e += 256) {  // P = sum_{M=J}^{I-1} L_IM Li_MJ
-      const int q = e >> 8, I = dl + q, J = I - dl, r = (e >> 4) & 15, c = e & 15;
-      float2 acc = zero;
-      for (int M = J; M < I; ++M)
-        for (int m = (M == J ? c : 0); m < LDL_B; ++m)
-          cfma(acc, S[(LDL_B * I + r) * LDL_LD + LDL_B * M + m], Li[(LDL_B * M + m) * LDL_LD + LDL_B * J + c]);
-      Tm[q * LDL_B * LDL_B + r * LDL_B + c] = acc;
-    }
-    __syncthreads();
-    for (int e = tid; e < npair * LDL_B * LDL_B; e += 256) {  // L^{-1}_IJ = -L^{-1}_II P
-      const int q = e >> 8, I = dl + q, J = I - dl, r = (e >> 4) & 15, c = e & 15;
-      float2 acc = Tm[q * LDL_B * LDL_B + r * LDL_B + c];  // the unit diagonal of L^{-1}_II
-      for (int m = 0; m < r; ++m)
-        cfma(acc, Li[(LDL_B * I + r) * LDL_LD + LDL_B * I + m], Tm[q * LDL_B * LDL_B + m * LDL_B + c]);
-      Li[(LDL_B * I + r) * LDL_LD + LDL_B * J + c] = make_float2(-acc.x, -acc.y);
-    }
-    __syncthreads();
-  }
-  // outputs: A (kb x kb) = L below, D on, U = D L^T above the diagonal; L^{-1} column-major in
-  // inv, and inv[4096 + r * 64 + c] = L^{-1}[r][c] / d_r (c < r), 1 / d_r (c = r): U^{-1} by rows
-  for (int e = tid; e < kb * kb; e += 256) {
-    const int r = e % kb, c = e / kb;
-    const float2 v = c < r ? S[r * LDL_LD + c]
-                           : (c == r ? S[r * LDL_LD + r] : cmulx(S[r * LDL_LD + r], S[c * LDL_LD + r]));
-    A[(j0 + r) + (j0 + c) * lda] = v;
-  }
-  for (int e = tid; e < TRI * TRI; e += 256) {
-    const int r = e & (TRI - 1), c = e >> 6;  // inv[c * 64 + r]: column-major L^{-1}
-    inv[e] = c <= r ? Li[r * LDL_LD + c] : zero;
-    const int rr = e >> 6, cq = e & (TRI - 1);  // inv[4096 + rr * 64 + cq]
-    inv[TRI * TRI + e] = cq < rr ? cmulx(Li[rr * LDL_LD + cq], s_dinv[rr]) : (cq == rr ? s_dinv[rr] : zero);
   }
 }
 
@@ -2094,12 +1952,6 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_getrf64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
-  // the symmetric diagonal block: blocked by 16 (k_ldl64) unless BEAST_LU_DIAG=elim asks for
-  // the 64-step elimination (k_lu_inv64<float2, true>); both give the same outputs
-  const char* diag_env = getenv("BEAST_LU_DIAG");
-  const bool ldl_blocked = std::is_same<T, float2>::value && !(diag_env && diag_env[0] == 'e');
-  if (ldl_blocked)
-    BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_ldl64, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)ldl64_smem()));
   if (apply_path)
     BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)panel_apply_smem()));
@@ -2144,12 +1996,6 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
                                              (int)sym_diag_update_smem()));
   bool ahead = false;
   int lu_par = 0;
-  auto sym_diag = [&](int64_t jd, int kd, float2* out_inv, cudaStream_t s_) {
-    if (ldl_blocked)
-      k_ldl64<<<1, 256, ldl64_smem(), s_>>>(reinterpret_cast<float2*>(A), lda, jd, kd, dinfo, out_inv);
-    else
-      k_lu_inv64<T, true><<<1, 256, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, reinterpret_cast<T*>(out_inv));
-  };
 
   int rc = BEAST_OK;
   // unpivoted, the outer block is factored in mid blocks of NB2 columns: the panels update
@@ -2194,7 +2040,7 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
         if (ahead)
           BEAST_CUDA_TRY(ctx, cudaStreamWaitEvent(st, ctx->la_ev[lu_par], 0));
         else if (apply_path && sym)
-          sym_diag(j0, kb, reinterpret_cast<float2*>(dblk), st);
+          k_lu_inv64<T, true><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk);
         else if (apply_path)
           k_lu_inv64<T, false><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk);
         else
@@ -2229,7 +2075,7 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
                                                               isa, static_cast<__half2*>(Bpv), isb, nBp, 0);
             BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[2], ax));
             k_sym_diag_update<<<1, 256, sym_diag_update_smem(), ax>>>(Af, lda, j0 + TRI, TRI);
-            sym_diag(j0 + TRI, TRI, reinterpret_cast<float2*>(dblk + 2 * TRI * TRI), ax);
+            k_lu_inv64<T, true><<<1, 256, getrf_sm, ax>>>(A, lda, j0 + TRI, TRI, dinfo, dblk + 2 * TRI * TRI);
             lu_par ^= 1;
             BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[lu_par], ax));
             ctx->launches += 3;

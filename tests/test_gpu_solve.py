@@ -199,32 +199,6 @@ def test_mixed_symmetric_path(n):
     assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-12
 
 
-@pytest.mark.parametrize("n", [700, 1101, 2600])
-def test_symmetric_diagonal_block_kernels_agree(n, monkeypatch):
-    """the symmetric diagonal block blocked by 16 (default) and the 64-step elimination
-    (BEAST_LU_DIAG=elim) give the same factorisation to rounding: the same factorisation mode,
-    the same number of refinement steps and the same FP64 solution"""
-    import torch
-    ctx = bg.get_context(0)
-    rng = np.random.default_rng(29)
-    R = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
-    A = (R + R.T) / 2 + 4 * n ** 0.5 * np.eye(n)
-    A = A + 1e-6 * (rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n)))
-    A = A.astype(np.complex64)
-    b = rng.normal(size=n) + 1j * rng.normal(size=n)
-    At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda().T
-    out = {}
-    for diag in ("elim", "blocked"):
-        monkeypatch.setenv("BEAST_LU_DIAG", diag)
-        x, it, res = bg.solve(At, b, precision=bg.MIXED, tol=1e-12, ctx=ctx)
-        assert ctx.last_factor_mode() == 2
-        assert it <= 5 and res < 1e-12
-        out[diag] = (x, it)
-    assert abs(out["elim"][1] - out["blocked"][1]) <= 1
-    x0, x1 = out["elim"][0], out["blocked"][0]
-    assert np.linalg.norm(x1 - x0) / np.linalg.norm(x0) < 1e-10
-
-
 @pytest.mark.parametrize("n", [1101, 2600])
 def test_mixed_symmetric_lookahead(n, monkeypatch):
     """the symmetric factorisation with lookahead (BEAST_LU_LOOKAHEAD=1: the next panel's block
