@@ -1578,11 +1578,18 @@ __device__ __forceinline__ dfl::df df_coef(double c) {
   fsplit::split_f64(c, &h, &l);
   return dfl::fast_two_sum(h, l);
 }
-__device__ __forceinline__ void df_acc(dfl::df& re, dfl::df& im, float4 z, dfl::df c) {
-  re = dfl::adds(re, dfl::mul(dfl::df{z.x, z.y}, c));
-  im = dfl::adds(im, dfl::mul(dfl::df{z.z, z.w}, c));
+// one term c z of a double-float gather sum (running sums, as k_gather_e): UC, c = +-1
+template <int UC>
+__device__ __forceinline__ void df_term(dfl::df& re, dfl::df& im, float4 z, dfl::df c) {
+  if (UC) {
+    dfl::acc(re, dfl::df{c.hi * z.x, c.hi * z.y});
+    dfl::acc(im, dfl::df{c.hi * z.z, c.hi * z.w});
+  } else {
+    dfl::acc(re, dfl::mul(dfl::df{z.x, z.y}, c));
+    dfl::acc(im, dfl::mul(dfl::df{z.z, z.w}, c));
+  }
 }
-template <int OC64>
+template <int OC64, int UC>
 __global__ void __launch_bounds__(256) k_gather_df(GatherArgs G, const int64_t* tptr, const int* tcell,
                                                    const int* tshape, const double* tcoef, const int64_t* bptr,
                                                    const int* bcell, const int* bshape, const double* bcoef, int nst,
@@ -1679,8 +1686,8 @@ __global__ void __launch_bounds__(256) k_gather_df(GatherArgs G, const int64_t* 
           for (int k = 0; k < 2; ++k)
 #pragma unroll
             for (int j = 0; j < 2; ++j)
-              if (k < s_cnt[nn] && j < ne) df_acc(re, im, z[u][k][j], dfl::mul(tc[j], s_b[nn][k]));
-          finish(nb0 + nn, re, im);
+              if (k < s_cnt[nn] && j < ne) df_term<UC>(re, im, z[u][k][j], dfl::mul(tc[j], s_b[nn][k]));
+          finish(nb0 + nn, dfl::norm(re), dfl::norm(im));
         }
       }
       nstart = nb1;
@@ -1692,9 +1699,9 @@ __global__ void __launch_bounds__(256) k_gather_df(GatherArgs G, const int64_t* 
       const int64_t col = ((int64_t)nsb * G.qlocal[bcell[f]] + bshape[f]) * G.ldc;
       const dfl::df b = df_coef(bcoef[f]);
       for (int64_t e = e0; e < e0 + ne; ++e)
-        df_acc(re, im, zc[col + (int64_t)nst * G.tpos[tcell[e]] + tshape[e]], dfl::mul(df_coef(tcoef[e]), b));
+        df_term<UC>(re, im, zc[col + (int64_t)nst * G.tpos[tcell[e]] + tshape[e]], dfl::mul(df_coef(tcoef[e]), b));
     }
-    finish(n, re, im);
+    finish(n, dfl::norm(re), dfl::norm(im));
   }
 }
 
@@ -1778,17 +1785,13 @@ __global__ void __launch_bounds__(256) k_gather_e(GatherArgs G, const int64_t* t
           const float sb = f < GATHER_E_MAX ? s_bd[nn][f].hi : fsplit::to_float_rn(bcoef[bptr[n] + f]);
           for (int e = 0; e < ne; ++e) {
             const float sg = sb * (e < GATHER_E_MAX ? tcd[e].hi : fsplit::to_float_rn(tcoef[e0 + e]));
-            const float4 z = zc[c0 + (int64_t)f * G.ldc + e];
-            dfl::acc(re, dfl::df{sg * z.x, sg * z.y});
-            dfl::acc(im, dfl::df{sg * z.z, sg * z.w});
+            df_term<1>(re, im, zc[c0 + (int64_t)f * G.ldc + e], dfl::make(sg));
           }
         } else {
           const dfl::df b = f < GATHER_E_MAX ? s_bd[nn][f] : df_coef(bcoef[bptr[n] + f]);
           for (int e = 0; e < ne; ++e) {
-            const float4 z = zc[c0 + (int64_t)f * G.ldc + e];
-            const dfl::df c = dfl::mul(e < GATHER_E_MAX ? tcd[e] : df_coef(tcoef[e0 + e]), b);
-            dfl::acc(re, dfl::mul(dfl::df{z.x, z.y}, c));
-            dfl::acc(im, dfl::mul(dfl::df{z.z, z.w}, c));
+            df_term<0>(re, im, zc[c0 + (int64_t)f * G.ldc + e],
+                       dfl::mul(e < GATHER_E_MAX ? tcd[e] : df_coef(tcoef[e0 + e]), b));
           }
         }
       }
@@ -2906,12 +2909,16 @@ cudaError_t launch_gather(const GatherArgs& g, cudaStream_t st) {
     }
 #undef GATHER_E
   } else if (g.zcell_fmt == ZCELL_DF) {
-    if (g.z_c64)
-      k_gather_df<1><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_cell, ts->fn_shape, ts->fn_coeff, bs->fn_ptr,
-                                          bs->fn_cell, bs->fn_shape, bs->fn_coeff, nst, nsb, nrows);
-    else
-      k_gather_df<0><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_cell, ts->fn_shape, ts->fn_coeff, bs->fn_ptr,
-                                          bs->fn_cell, bs->fn_shape, bs->fn_coeff, nst, nsb, nrows);
+#define GATHER_DF(OC, UC)                                                                              \
+  k_gather_df<OC, UC><<<grid, th, 0, st>>>(g, ts->fn_ptr, ts->fn_cell, ts->fn_shape, ts->fn_coeff, bs->fn_ptr, \
+                                           bs->fn_cell, bs->fn_shape, bs->fn_coeff, nst, nsb, nrows)
+    const bool uc = ts->unit_coef && bs->unit_coef;
+    if (uc) {
+      if (g.z_c64) GATHER_DF(1, 1); else GATHER_DF(0, 1);
+    } else {
+      if (g.z_c64) GATHER_DF(1, 0); else GATHER_DF(0, 0);
+    }
+#undef GATHER_DF
   } else if (g.zcell_fmt == ZCELL_C64) {
     if (g.z_c64) GATHER(1, 1); else GATHER(1, 0);
   } else {
