@@ -819,7 +819,8 @@ __device__ __forceinline__ void cmac2(float2& acc, float4 a, float4 b) {
 // is not stored; its FP16 B' columns for the first nB systems (the rest of the mid block)
 // are written from L21 and the pivots D = diag(U11) instead.
 // rb0: index of the first CTA's block (the grid covers blocks rb0 .. of the 2 nR, or nR)
-__global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, int64_t j0, int64_t n,
+template <int NS>
+__global__ void __launch_bounds__(256, NS == 64 ? 2 : 3) k_panel_apply(float2* A, int64_t lda, int64_t j0, int64_t n,
                                                         const float2* __restrict__ inv, int nR, __half2* Ap,
                                                         float* inv_sa, __half2* Bp, float* inv_sb, int nB,
                                                         int rb0) {
@@ -831,14 +832,17 @@ __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, 
   const int bi = (int)blockIdx.x + rb0;
   const bool right = bi < nR;
   const int64_t s0 = j0 + TRI;
-  const int64_t b0 = s0 + (int64_t)(right ? bi : bi - nR) * 64;  // first system
+  const int64_t b0 = s0 + (int64_t)(right ? bi : bi - nR) * NS;  // first system
+  constexpr int NU = NS / 16;         // systems per thread
+  constexpr int QN = 256 / NS;        // threads per system in the maxima passes
+  constexpr int QV = TRI / QN;        // free indices per such thread
   const float2 zero = make_float2(0.f, 0.f);
   const int sl = lane & 15, h = lane >> 4;
   const int vlo = 4 * warp + 2 * h, vhi = 60 - 4 * warp + 2 * h;  // free indices vlo, vlo+1, vhi, vhi+1
   const int k1 = 4 * warp + 4, k2 = 64 - 4 * warp;
-  float2 acc[4][4];  // [system u][free index: vlo, vlo+1, vhi, vhi+1]
+  float2 acc[NU][4];  // [system u][free index: vlo, vlo+1, vhi, vhi+1]
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < NU; ++u)
 #pragma unroll
     for (int j = 0; j < 4; ++j) acc[u][j] = zero;
 
@@ -849,32 +853,41 @@ __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, 
       // 8 + 8 elements per thread, e = tid + 256 t; coalesced along the contiguous index:
       //   right W: s = e & 63, k = e >> 6 (A21 column k)   N: k = e & 31, v = e >> 5 (Uinv column v)
       //   left  W: k = e & 31, s = e >> 5 (A12 column s)   N: v = e & 63, k = e >> 6 (Linv column k)
-      float2 w[8], v[8];
+      constexpr int TW = NS * PA_KH / 256;  // W elements per thread (N: 8)
+      float2 w[TW], v[8];
 #pragma unroll
-      for (int t = 0; t < 8; ++t) {
+      for (int t = 0; t < TW; ++t) {
         const int e = tid + 256 * t;
         if (right) {
-          const int s = e & 63, k = e >> 6;
+          const int s = e % NS, k = e / NS;
           w[t] = b0 + s < n ? A[(b0 + s) + (j0 + kb0 + k) * lda] : zero;
-          v[t] = inv[4096 + (e >> 5) * 64 + kb0 + (e & 31)];
         } else {
           const int k = e & 31, s = e >> 5;
           w[t] = b0 + s < n ? A[(j0 + kb0 + k) + (b0 + s) * lda] : zero;
-          v[t] = inv[(kb0 + (e >> 6)) * 64 + (e & 63)];
         }
       }
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
         const int e = tid + 256 * t;
+        v[t] = right ? inv[4096 + (e >> 5) * 64 + kb0 + (e & 31)] : inv[(kb0 + (e >> 6)) * 64 + (e & 63)];
+      }
+#pragma unroll
+      for (int t = 0; t < TW; ++t) {
+        const int e = tid + 256 * t;
         const float4 wv = make_float4(w[t].x, w[t].x, -w[t].y, w[t].y);
-        const float4 nv = make_float4(v[t].x, v[t].y, v[t].y, v[t].x);
-        if (right) {
-          Ws[(e >> 6) * PA_LD4 + (e & 63)] = wv;
-          Ns[(e & 31) * PA_LD4 + (e >> 5)] = nv;
-        } else {
+        if (right)
+          Ws[(e / NS) * PA_LD4 + (e % NS)] = wv;
+        else
           Ws[(e & 31) * PA_LD4 + (e >> 5)] = wv;
+      }
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int e = tid + 256 * t;
+        const float4 nv = make_float4(v[t].x, v[t].y, v[t].y, v[t].x);
+        if (right)
+          Ns[(e & 31) * PA_LD4 + (e >> 5)] = nv;
+        else
           Ns[(e >> 6) * PA_LD4 + (e & 63)] = nv;
-        }
       }
     }
     __syncthreads();
@@ -886,7 +899,7 @@ __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, 
       const float4* nr = Ns + (k - kb0) * PA_LD4;
       const float4 n0 = nr[vlo], n1 = nr[vlo + 1], n2 = nr[vhi], n3 = nr[vhi + 1];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < NU; ++u) {
         const float4 a = wr[16 * u];
         cmac2(acc[u][0], a, n0);
         cmac2(acc[u][1], a, n1);
@@ -900,7 +913,7 @@ __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, 
       const float4* nr = Ns + (k - kb0) * PA_LD4;
       const float4 n2 = nr[vhi], n3 = nr[vhi + 1];
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
+      for (int u = 0; u < NU; ++u) {
         const float4 a = wr[16 * u];
         cmac2(acc[u][2], a, n2);
         cmac2(acc[u][3], a, n3);
@@ -913,17 +926,17 @@ __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, 
   __shared__ float s_scale[64];
   const int vv[4] = {vlo, vlo + 1, vhi, vhi + 1};
 #pragma unroll
-  for (int u = 0; u < 4; ++u)
+  for (int u = 0; u < NU; ++u)
 #pragma unroll
     for (int j = 0; j < 4; ++j) Cs[(sl + 16 * u) * PA_CLD + vv[j]] = acc[u][j];
   __syncthreads();
   // the solved systems, coalesced: right -- A[b0 + s, j0 + v] (along s); left -- A[j0 + v,
   // b0 + s] (along v)
 #pragma unroll 4
-  for (int t = 0; t < 16; ++t) {
+  for (int t = 0; t < NS / 4; ++t) {
     const int e = tid + 256 * t;
     if (right) {
-      const int sy = e & 63, v = e >> 6;
+      const int sy = e % NS, v = e / NS;
       if (b0 + sy < n) A[(b0 + sy) + (j0 + v) * lda] = Cs[sy * PA_CLD + v];
     } else {
       const int v = e & 63, sy = e >> 6;
@@ -936,17 +949,17 @@ __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, 
   __half2* const dst = right ? Ap : Bp;
   if (dst == nullptr) return;  // uniform over the CTA
   {
-    const int sy = tid & 63, q = tid >> 6;
+    const int sy = tid % NS, q = tid / NS;
     float mx = 0.f;
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const float2 a = Cs[sy * PA_CLD + 16 * q + i];
+    for (int i = 0; i < QV; ++i) {
+      const float2 a = Cs[sy * PA_CLD + QV * q + i];
       mx = fmaxf(mx, fmaxf(fabsf(a.x), fabsf(a.y)));
     }
-    red[q * 64 + sy] = mx;
+    red[q * NS + sy] = mx;
     __syncthreads();
     if (q == 0) {
-      mx = fmaxf(fmaxf(red[sy], red[64 + sy]), fmaxf(red[128 + sy], red[192 + sy]));
+      for (int qq = 1; qq < QN; ++qq) mx = fmaxf(mx, red[qq * NS + sy]);
       const int sh = tc_scale_shift(mx);
       s_scale[sy] = ldexpf(1.f, sh);
       if (b0 + sy < n) (right ? inv_sa : inv_sb)[b0 + sy - s0] = ldexpf(1.f, -sh);
@@ -959,24 +972,24 @@ __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, 
     __shared__ float s_tsc[64];
     if (tid < 64) s_d[tid] = A[(j0 + tid) + (j0 + tid) * lda];
     __syncthreads();
-    const int sy = tid & 63, q = tid >> 6;
+    const int sy = tid % NS, q = tid / NS;
     float mx = 0.f;
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-      const float2 a = cmulx(Cs[sy * PA_CLD + 16 * q + i], s_d[16 * q + i]);
+    for (int i = 0; i < QV; ++i) {
+      const float2 a = cmulx(Cs[sy * PA_CLD + QV * q + i], s_d[QV * q + i]);
       mx = fmaxf(mx, fmaxf(fabsf(a.x), fabsf(a.y)));
     }
-    red[q * 64 + sy] = mx;
+    red[q * NS + sy] = mx;
     __syncthreads();
     if (q == 0) {
-      mx = fmaxf(fmaxf(red[sy], red[64 + sy]), fmaxf(red[128 + sy], red[192 + sy]));
+      for (int qq = 1; qq < QN; ++qq) mx = fmaxf(mx, red[qq * NS + sy]);
       const int sh = tc_scale_shift(mx);
       s_tsc[sy] = ldexpf(1.f, sh);
       if (b0 + sy - s0 < nB) inv_sb[b0 + sy - s0] = ldexpf(1.f, -sh);
     }
     __syncthreads();
     const int v0 = 4 * (lane & 15);
-    for (int sp = 2 * warp; sp < 64; sp += 16) {
+    for (int sp = 2 * warp; sp < NS; sp += 16) {
       const int s2 = sp + (lane >> 4);
       if (b0 + s2 - s0 < nB) {
         const float sc = s_tsc[s2];
@@ -996,7 +1009,7 @@ __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, 
   // systems per pass (256 bytes each)
   const int v0 = 4 * (lane & 15);
   if (right) {
-    for (int sy = warp; sy < 64; sy += 8) {
+    for (int sy = warp; sy < NS; sy += 8) {
       if (b0 + sy >= n) break;
       const float sc = s_scale[sy];
       const float2* cr = Cs + sy * PA_CLD + v0;
@@ -1010,7 +1023,7 @@ __global__ void __launch_bounds__(256, 2) k_panel_apply(float2* A, int64_t lda, 
       *reinterpret_cast<uint4*>(Ap + (2 * m + (lane >> 4)) * TRI + v0) = *reinterpret_cast<const uint4*>(hv);
     }
   } else {
-    for (int sp = 2 * warp; sp < 64; sp += 16) {
+    for (int sp = 2 * warp; sp < NS; sp += 16) {
       const int sy = sp + (lane >> 4);
       if (b0 + sy < n) {
         const float sc = s_scale[sy];
@@ -1953,7 +1966,9 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
   if (apply_path)
-    BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel_apply, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel_apply<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)panel_apply_smem()));
+    BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel_apply<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)panel_apply_smem()));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_trsm_tile<T, R, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)trsm_tile_smem<T>()));
@@ -2071,7 +2086,7 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
               BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[4], st));
               BEAST_CUDA_TRY(ctx, cudaStreamWaitEvent(ax, ctx->la_ev[4], 0));
             }
-            k_panel_apply<<<1, 256, panel_apply_smem(), ax>>>(Af, lda, j0, n, inv, nR, static_cast<__half2*>(Apv),
+            k_panel_apply<64><<<1, 256, panel_apply_smem(), ax>>>(Af, lda, j0, n, inv, nR, static_cast<__half2*>(Apv),
                                                               isa, static_cast<__half2*>(Bpv), isb, nBp, 0);
             BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[2], ax));
             k_sym_diag_update<<<1, 256, sym_diag_update_smem(), ax>>>(Af, lda, j0 + TRI, TRI);
@@ -2081,14 +2096,17 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
             ctx->launches += 3;
             // here: the other block rows, then (after the second stream's operands) the update
             if (nR > 1) {
-              k_panel_apply<<<(unsigned)(nR - 1), 256, panel_apply_smem(), st>>>(
+              k_panel_apply<64><<<(unsigned)(nR - 1), 256, panel_apply_smem(), st>>>(
                   Af, lda, j0, n, inv, nR, static_cast<__half2*>(Apv), isa, static_cast<__half2*>(Bpv), isb, nBp, 1);
               ctx->launches += 1;
             }
             BEAST_CUDA_TRY(ctx, cudaStreamWaitEvent(st, ctx->la_ev[2], 0));
           } else {
-            k_panel_apply<<<(unsigned)(sym ? nR : 2 * nR), 256, panel_apply_smem(), st>>>(
-                Af, lda, j0, n, inv, nR, static_cast<__half2*>(Apv), isa, static_cast<__half2*>(Bpv), isb, nBp, 0);
+            // 32 systems per CTA: twice the CTAs of half the work, so that more warps hide the
+            // shared-memory latency of the triangular products
+            const int nR32 = (int)((rb + 31) / 32);
+            k_panel_apply<32><<<(unsigned)(sym ? nR32 : 2 * nR32), 256, panel_apply_smem(), st>>>(
+                Af, lda, j0, n, inv, nR32, static_cast<__half2*>(Apv), isa, static_cast<__half2*>(Bpv), isb, nBp, 0);
             ctx->launches += 1;
           }
           applied = true;
