@@ -938,9 +938,12 @@ static int factor_copy(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, in
     if (a_dtype == BEAST_C64 && sym) {  // the symmetric factorisation reads the block-lower part only
       ProfScope ps(ctx, PK_CONVERT, (double)n * n * 8);
       BEAST_CUDA_TRY(ctx, copy_lower_c64(n, A, lda, F, n, st));
-    } else if (a_dtype == BEAST_C64)
+    } else if (a_dtype == BEAST_C64) {
       BEAST_CUDA_TRY(ctx, cudaMemcpy2DAsync(F, n * 8, A, lda * 8, n * 8, n, cudaMemcpyDeviceToDevice, st));
-    else {
+    } else if (sym) {
+      ProfScope ps(ctx, PK_CONVERT, (double)n * n * 12);
+      BEAST_CUDA_TRY(ctx, convert_lower_c128_to_c64(n, A, lda, F, n, st));
+    } else {
       ProfScope ps(ctx, PK_CONVERT, (double)n * n * 24);
       BEAST_CUDA_TRY(ctx, convert_c128_to_c64(n, n, (const double*)A, lda, (float*)F, n, st));
     }

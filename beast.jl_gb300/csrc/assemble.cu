@@ -2288,7 +2288,9 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
   for (int qi = 0; qi < nqt; ++qi) {
     const FarDfRecord& r = rec[qi];
     const int ql = q0 + qi;
-    const dfl::df d[3] = {dfl::sub(cp[0], r.c[0]), dfl::sub(cp[1], r.c[1]), dfl::sub(cp[2], r.c[2])};
+    // far pairs: |c_p - c_q| is at least a cell size, so the sloppy difference (error 2^-44 of the
+    // coordinates) keeps the pair's distance to about 1e-11 relative
+    const dfl::df d[3] = {dfl::subs(cp[0], r.c[0]), dfl::subs(cp[1], r.c[1]), dfl::subs(cp[2], r.c[2])};
     if (P.qs_kind != BEAST_QS_DOUBLENUM) {
       const float lim = radp + r.lim;
       const float dd = d[0].hi * d[0].hi + d[1].hi * d[1].hi + d[2].hi * d[2].hi;

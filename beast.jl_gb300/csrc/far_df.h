@@ -121,7 +121,7 @@ DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3
 #endif
   for (int a = 0; a < NO; ++a) {
     df dx[3];
-    for (int c = 0; c < 3; ++c) dx[c] = add(d[c], xi[a][c]);
+    for (int c = 0; c < 3; ++c) dx[c] = adds(d[c], xi[a][c]);  // |d| >> |xi|: no cancellation
     A[a] = dot3s(dx, dx);
     U0[a] = cdf{z0, z0};
   }

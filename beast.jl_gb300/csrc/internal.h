@@ -291,6 +291,8 @@ cudaError_t gemv_dev(int64_t n, const void* A, int64_t lda, int a_c64, const dou
 // the block-lower part of a c64 matrix (column j from row 64 floor(j / 64)), for the
 // symmetric factorisation's copy
 cudaError_t copy_lower_c64(int64_t n, const void* A, int64_t lda, void* F, int64_t ldf, cudaStream_t st);
+// the same from a c128 matrix into a c64 copy (round to nearest)
+cudaError_t convert_lower_c128_to_c64(int64_t n, const void* A, int64_t lda, void* F, int64_t ldf, cudaStream_t st);
 cudaError_t convert_c128_to_c64(int64_t rows, int64_t cols, const double* src, int64_t lds,
                                 float* dst, int64_t ldd, cudaStream_t st);
 cudaError_t convert_c64_to_c128(int64_t rows, int64_t cols, const float* src, int64_t lds,

@@ -1168,6 +1168,16 @@ __global__ void k_copy_lower_c64(int64_t n, const float2* A, int64_t lda, float2
   }
 }
 
+// the same block-lower part from a c128 matrix, rounded to c64 by integer operations
+__global__ void k_convert_lower_c128(int64_t n, const double2* A, int64_t lda, float2* F, int64_t ldf) {
+  for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
+    const int64_t i = (j / 64) * 64 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (i >= n) continue;
+    const double2 a = __ldcs(A + i + j * lda);
+    F[i + j * ldf] = make_float2(fsplit::to_float_rn(a.x), fsplit::to_float_rn(a.y));
+  }
+}
+
 // ---- C -= A B  (complex; C m x n, A m x k, B k x n; all column-major with ld) -------------
 constexpr int GT = 64, GK = 8;
 template <typename T, typename R>
@@ -2349,6 +2359,11 @@ cudaError_t copy_lower_c64(int64_t n, const void* A, int64_t lda, void* F, int64
   return cudaGetLastError();
 }
 
+cudaError_t convert_lower_c128_to_c64(int64_t n, const void* A, int64_t lda, void* F, int64_t ldf, cudaStream_t st) {
+  dim3 g((unsigned)((n + 255) / 256), (unsigned)std::min<int64_t>(n, 65535));
+  k_convert_lower_c128<<<g, 256, 0, st>>>(n, (const double2*)A, lda, (float2*)F, ldf);
+  return cudaGetLastError();
+}
 cudaError_t convert_c128_to_c64(int64_t rows, int64_t cols, const double* src, int64_t lds, float* dst,
                                 int64_t ldd, cudaStream_t st) {
   dim3 g((unsigned)((rows + 255) / 256), (unsigned)std::min<int64_t>(cols, 65535));
