@@ -492,19 +492,7 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
   constexpr int LD = TRI + 1, PL = TRI + TRI / 4;
   extern __shared__ unsigned char smraw[];
   T* Ls = reinterpret_cast<T*>(smraw);  // 64 x LD: staging, then the L factor, then Linv
-  // float2: the published rows as float4 (x, y, y, x), so that a complex multiply-add is two
-  // packed FMAs on operands that need no shuffling (the same roundings as four scalar FMAs)
-  constexpr bool PK = std::is_same<T, float2>::value;
   __shared__ T p1[2][PL], p2[2][PL], lc[2][TRI];
-  __shared__ float4 p1v[2][PK ? PL : 1], p2v[2][PK ? PL : 1];
-  auto put1 = [&](int bb, int c, T v) {
-    if constexpr (PK) p1v[bb][pidx<T>(c)] = make_float4(v.x, v.y, v.y, v.x);
-    else p1[bb][pidx<T>(c)] = v;
-  };
-  auto put2 = [&](int bb, int c, T v) {
-    if constexpr (PK) p2v[bb][pidx<T>(c)] = make_float4(v.x, v.y, v.y, v.x);
-    else p2[bb][pidx<T>(c)] = v;
-  };
   __shared__ T dv[2];
   __shared__ int s_zero[2];  // 1-based column of a zero pivot, by step parity
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -531,8 +519,8 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
   if (rb == 0)
 #pragma unroll
     for (int j = 0; j < 4; ++j) {
-      put1(0, c0 + j, (c0 + j == 0) ? zero : s1[0][j]);
-      if (!SYM) put2(0, c0 + j, s2[0][j]);
+      p1[0][pidx<T>(c0 + j)] = (c0 + j == 0) ? zero : s1[0][j];
+      if (!SYM) p2[0][pidx<T>(c0 + j)] = s2[0][j];
     }
   if (cb == 0)
 #pragma unroll
@@ -552,49 +540,7 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
         return;
       }
       const T d = dv[b];
-      if (r0 + 3 > k && PK) {  // some row of the tile is below the pivot (packed FMAs)
-        if constexpr (PK) {
-          T l1[4], l2[4];
-          float4 q1[4], q2[4];
-#pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            l1[i] = cmulx(lc[b][r0 + i], d);
-            if (!SYM) {
-              const float4 pv = p1v[b][pidx<T>(r0 + i)];
-              l2[i] = cmulx(make_float2(pv.x, pv.y), d);
-            }
-          }
-#pragma unroll
-          for (int j = 0; j < 4; ++j) {
-            q1[j] = p1v[b][pidx<T>(c0 + j)];
-            if (!SYM) q2[j] = p2v[b][pidx<T>(c0 + j)];
-          }
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-            if (r0 + i > k) {
-              // acc -= l q: (acc.x, acc.y) += (-l.x, -l.x) (q.x, q.y) + (l.y, -l.y) (q.y, q.x)
-              const float2 a1 = make_float2(-l1[i].x, -l1[i].x), b1 = make_float2(l1[i].y, -l1[i].y);
-#pragma unroll
-              for (int j = 0; j < 4; ++j) {
-                s1[i][j] = __ffma2_rn(a1, make_float2(q1[j].x, q1[j].y), s1[i][j]);
-                s1[i][j] = __ffma2_rn(b1, make_float2(q1[j].z, q1[j].w), s1[i][j]);
-              }
-              if (!SYM) {
-                const float2 a2 = make_float2(-l2[i].x, -l2[i].x), b2 = make_float2(l2[i].y, -l2[i].y);
-#pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                  s2[i][j] = __ffma2_rn(a2, make_float2(q2[j].x, q2[j].y), s2[i][j]);
-                  s2[i][j] = __ffma2_rn(b2, make_float2(q2[j].z, q2[j].w), s2[i][j]);
-                }
-              }
-              if (cb == kq) {  // column k: L^{-1}[r][k] = -l, and the L factor
-                s1[i][kk].x = -l1[i].x;
-                s1[i][kk].y = -l1[i].y;
-                Ls[(r0 + i) * LD + k] = l1[i];
-              }
-            }
-        }
-      } else if (r0 + 3 > k) {  // some row of the tile is below the pivot
+      if (r0 + 3 > k) {  // some row of the tile is below the pivot
         T l1[4], l2[4], q1[4], q2[4];
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
@@ -630,8 +576,8 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
         if (rb == qn)
 #pragma unroll
           for (int j = 0; j < 4; ++j) {
-            put1(bn, c0 + j, (c0 + j == kn) ? zero : s1[in][j]);
-            if (!SYM) put2(bn, c0 + j, s2[in][j]);
+            p1[bn][pidx<T>(c0 + j)] = (c0 + j == kn) ? zero : s1[in][j];
+            if (!SYM) p2[bn][pidx<T>(c0 + j)] = s2[in][j];
           }
         if (cb == qn)
 #pragma unroll
