@@ -486,9 +486,13 @@ __device__ __forceinline__ int pidx(int c) {  // conflict-free index of the publ
 // SYM: only the lower triangle of the block is current (symmetric updates); the upper one
 // is taken from it by symmetry, the elimination on U^T is skipped and, U = D L^T,
 // U^{-1} = (L^{-1})^T D^{-1} is formed from L^{-1} and the pivots at the end.
-template <typename T, bool SYM>
-__global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0, int kb, int* info, T* inv) {
+// TS: the tile edge owned by a thread: 4 (256 threads) or 2 (1024 threads: a quarter of the
+// serial instructions per warp and step, which is what bounds this latency-bound chain)
+template <typename T, bool SYM, int TS = 4>
+__global__ void __launch_bounds__(TRI * TRI / (TS * TS)) k_lu_inv64(T* A, int64_t lda, int64_t j0, int kb, int* info,
+                                                                   T* inv) {
   constexpr bool sym = SYM;
+  constexpr int NT = TRI * TRI / (TS * TS);  // threads
   constexpr int LD = TRI + 1, PL = TRI + TRI / 4;
   extern __shared__ unsigned char smraw[];
   T* Ls = reinterpret_cast<T*>(smraw);  // 64 x LD: staging, then the L factor, then Linv
@@ -496,67 +500,67 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
   __shared__ T dv[2];
   __shared__ int s_zero[2];  // 1-based column of a zero pivot, by step parity
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int cb = lane & 15, rb = 2 * warp + (lane >> 4);
-  const int r0 = 4 * rb, c0 = 4 * cb;
+  const int cb = TS == 4 ? (lane & 15) : lane, rb = TS == 4 ? 2 * warp + (lane >> 4) : warp;
+  const int r0 = TS * rb, c0 = TS * cb;
   const T zero = cmk<T>(0.0, 0.0), one = cmk<T>(1.0, 0.0);
   // coalesced load through shared memory (identity padding beyond kb)
-  for (int e = tid; e < TRI * TRI; e += 256) {
+  for (int e = tid; e < TRI * TRI; e += NT) {
     const int r = e & (TRI - 1), c = e >> 6;
     const int rr = (sym && c > r) ? c : r, cc = (sym && c > r) ? r : c;
     Ls[r * LD + c] = (r < kb && c < kb) ? A[(j0 + rr) + (j0 + cc) * lda] : (r == c ? one : zero);
   }
   if (tid < 2) s_zero[tid] = 0;
   __syncthreads();
-  T s1[4][4], s2[4][4];
+  T s1[TS][TS], s2[TS][TS];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < TS; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < TS; ++j) {
       s1[i][j] = Ls[(r0 + i) * LD + c0 + j];
       s2[i][j] = (r0 + i == c0 + j) ? one : zero;
     }
   // publish row 0, column 0 and the first pivot's reciprocal
   if (rb == 0)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < TS; ++j) {
       p1[0][pidx<T>(c0 + j)] = (c0 + j == 0) ? zero : s1[0][j];
       if (!SYM) p2[0][pidx<T>(c0 + j)] = s2[0][j];
     }
   if (cb == 0)
 #pragma unroll
-    for (int i = 0; i < 4; ++i) lc[0][r0 + i] = s1[i][0];
+    for (int i = 0; i < TS; ++i) lc[0][r0 + i] = s1[i][0];
   if (rb == 0 && cb == 0) {
     T d;
     if (!crecip(s1[0][0], d)) s_zero[0] = 1;
     dv[0] = d;
   }
   __syncthreads();  // the staging buffer is free from here on (L factor)
-  for (int kq = 0; kq < TRI / 4; ++kq) {
+  for (int kq = 0; kq < TRI / TS; ++kq) {
 #pragma unroll
-    for (int kk = 0; kk < 4; ++kk) {
-      const int k = 4 * kq + kk, b = kk & 1;
+    for (int kk = 0; kk < TS; ++kk) {
+      const int k = TS * kq + kk, b = kk & 1;
       if (s_zero[b]) {  // uniform
         if (tid == 0) atomicCAS(info, 0, (int)(j0 + s_zero[b]));
         return;
       }
       const T d = dv[b];
-      if (r0 + 3 > k) {  // some row of the tile is below the pivot
-        T l1[4], l2[4], q1[4], q2[4];
+      if (r0 + TS - 1 > k) {  // some row of the tile is below the pivot
+        T l1[TS], l2[TS], q1[TS], q2[TS];
 #pragma unroll
-        for (int i = 0; i < 4; ++i) {
+        for (int i = 0; i < TS; ++i) {
           l1[i] = cmulx(lc[b][r0 + i], d);
           l2[i] = cmulx(p1[b][pidx<T>(r0 + i)], d);
         }
 #pragma unroll
-        for (int j = 0; j < 4; ++j) {
+        for (int j = 0; j < TS; ++j) {
           q1[j] = p1[b][pidx<T>(c0 + j)];
           q2[j] = p2[b][pidx<T>(c0 + j)];
         }
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+        for (int i = 0; i < TS; ++i)
           if (r0 + i > k) {
 #pragma unroll
-            for (int j = 0; j < 4; ++j) {
+            for (int j = 0; j < TS; ++j) {
               cfms(s1[i][j], l1[i], q1[j]);
               if (!SYM) cfms(s2[i][j], l2[i], q2[j]);
             }
@@ -569,19 +573,19 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
       }
       if (!SYM && rb == kq)  // row k of X is final
 #pragma unroll
-        for (int j = 0; j < 4; ++j) s2[kk][j] = cmulx(s2[kk][j], d);
+        for (int j = 0; j < TS; ++j) s2[kk][j] = cmulx(s2[kk][j], d);
       // publish step k + 1
       if (k + 1 < TRI) {
-        const int kn = k + 1, bn = b ^ 1, qn = kn >> 2, in = kn & 3;
+        const int kn = k + 1, bn = b ^ 1, qn = kn / TS, in = kn % TS;
         if (rb == qn)
 #pragma unroll
-          for (int j = 0; j < 4; ++j) {
+          for (int j = 0; j < TS; ++j) {
             p1[bn][pidx<T>(c0 + j)] = (c0 + j == kn) ? zero : s1[in][j];
             if (!SYM) p2[bn][pidx<T>(c0 + j)] = s2[in][j];
           }
         if (cb == qn)
 #pragma unroll
-          for (int i = 0; i < 4; ++i) lc[bn][r0 + i] = s1[i][in];
+          for (int i = 0; i < TS; ++i) lc[bn][r0 + i] = s1[i][in];
         if (rb == qn && cb == qn) {
           T dn;
           if (!crecip(s1[in][in], dn)) s_zero[bn] = kn + 1;
@@ -593,12 +597,12 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
   }
   // U (upper part of S1) joins the L factor in Ls; the factored block goes back to A
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < TS; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j)
+    for (int j = 0; j < TS; ++j)
       if (c0 + j >= r0 + i) Ls[(r0 + i) * LD + c0 + j] = s1[i][j];
   __syncthreads();
-  for (int e = tid; e < kb * kb; e += 256) {
+  for (int e = tid; e < kb * kb; e += NT) {
     const int r = e % kb, c = e / kb;
     A[(j0 + r) + (j0 + c) * lda] = Ls[r * LD + c];
   }
@@ -610,32 +614,32 @@ __global__ void __launch_bounds__(256) k_lu_inv64(T* A, int64_t lda, int64_t j0,
     __shared__ T s_dinv[TRI];
     if (rb == cb)
 #pragma unroll
-      for (int i = 0; i < 4; ++i) {
+      for (int i = 0; i < TS; ++i) {
         T di;
         crecip(s1[i][i], di);  // nonzero: the elimination checked every pivot
         s_dinv[r0 + i] = di;
       }
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < 4; ++i) {
+    for (int i = 0; i < TS; ++i) {
       const T di = s_dinv[r0 + i];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) {
+      for (int j = 0; j < TS; ++j) {
         const int r = r0 + i, c = c0 + j;
         s2[i][j] = c < r ? cmulx(s1[i][j], di) : (c == r ? di : zero);
       }
     }
   }
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < TS; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
+    for (int j = 0; j < TS; ++j) {
       const int r = r0 + i, c = c0 + j;
       Ls[r * LD + c] = c < r ? s1[i][j] : (c == r ? one : zero);
       inv[TRI * TRI + r * TRI + c] = s2[i][j];
     }
   __syncthreads();
-  for (int e = tid; e < TRI * TRI; e += 256) {
+  for (int e = tid; e < TRI * TRI; e += NT) {
     const int r = e & (TRI - 1), c = e >> 6;
     inv[e] = Ls[r * LD + c];
   }
@@ -1975,6 +1979,12 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_getrf64<T>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
+  // the diagonal-block elimination with 2 x 2 tiles on 1024 threads (default) or 4 x 4 tiles on
+  // 256 (BEAST_LU_DIAG_TILE=4): the same arithmetic per element, different thread counts
+  const char* dt_env = getenv("BEAST_LU_DIAG_TILE");
+  const bool diag2 = !(dt_env && dt_env[0] == '4');
   if (apply_path)
     BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel_apply<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)panel_apply_smem()));
@@ -1999,6 +2009,16 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   T* rowj = crow + 2 * (size_t)G0 * nb;
   unsigned int* bar = reinterpret_cast<unsigned int*>(rowj + 2 * nb);
   int* dinfo = reinterpret_cast<int*>(bar + 4);
+  auto diag = [&](bool sy, int64_t jd, int kd, T* out_inv, cudaStream_t s_) {
+    if (sy && diag2)
+      k_lu_inv64<T, true, 2><<<1, TRI * TRI / 4, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, out_inv);
+    else if (sy)
+      k_lu_inv64<T, true><<<1, 256, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, out_inv);
+    else if (diag2)
+      k_lu_inv64<T, false, 2><<<1, TRI * TRI / 4, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, out_inv);
+    else
+      k_lu_inv64<T, false><<<1, 256, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, out_inv);
+  };
   BEAST_CUDA_TRY(ctx, cudaMemsetAsync(bar, 0, 4 * sizeof(unsigned int) + sizeof(int), st));
   BEAST_CUDA_TRY(ctx, cudaMemsetAsync(ctx->d_flag, 0, sizeof(int), st));
   GridSync gs{bar, bar + 1, reinterpret_cast<int*>(bar + 2)};
@@ -2064,10 +2084,8 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
         ctx->launches += ahead ? 0 : 1;
         if (ahead)
           BEAST_CUDA_TRY(ctx, cudaStreamWaitEvent(st, ctx->la_ev[lu_par], 0));
-        else if (apply_path && sym)
-          k_lu_inv64<T, true><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk);
         else if (apply_path)
-          k_lu_inv64<T, false><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo, dblk);
+          diag(sym, j0, kb, dblk, st);
         else
           k_getrf64<T><<<1, 256, getrf_sm, st>>>(A, lda, j0, kb, dinfo);
         if (apply_path && kb == TRI && rb > 0) {
@@ -2100,7 +2118,7 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
                                                               isa, static_cast<__half2*>(Bpv), isb, nBp, 0);
             BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[2], ax));
             k_sym_diag_update<<<1, 256, sym_diag_update_smem(), ax>>>(Af, lda, j0 + TRI, TRI);
-            k_lu_inv64<T, true><<<1, 256, getrf_sm, ax>>>(A, lda, j0 + TRI, TRI, dinfo, dblk + 2 * TRI * TRI);
+            diag(true, j0 + TRI, TRI, dblk + 2 * TRI * TRI, ax);
             lu_par ^= 1;
             BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[lu_par], ax));
             ctx->launches += 3;

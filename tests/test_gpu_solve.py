@@ -199,6 +199,30 @@ def test_mixed_symmetric_path(n):
     assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-12
 
 
+@pytest.mark.parametrize("symmetric", [True, False])
+def test_diagonal_block_tile_sizes_agree(symmetric, monkeypatch):
+    """the diagonal-block elimination on 1024 threads with 2 x 2 tiles (default) and on 256
+    threads with 4 x 4 tiles (BEAST_LU_DIAG_TILE=4) does the same arithmetic on every element:
+    identical solutions, symmetric and unpivoted factorisations (odd last block, n = 1101)"""
+    import torch
+    ctx = bg.get_context(0)
+    n = 1101
+    rng = np.random.default_rng(31)
+    R = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    A = ((R + R.T) / 2 if symmetric else R) + 4 * n ** 0.5 * np.eye(n)
+    A = A.astype(np.complex64)
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda().T
+    out = {}
+    for tile in ("4", "2"):
+        monkeypatch.setenv("BEAST_LU_DIAG_TILE", tile)
+        x, it, res = bg.solve(At, b, precision=bg.MIXED, tol=1e-12, ctx=ctx)
+        assert ctx.last_factor_mode() == (2 if symmetric else 1)
+        out[tile] = (x, it, res)
+    assert out["2"][1] == out["4"][1] and out["2"][2] == out["4"][2]
+    assert np.array_equal(out["2"][0], out["4"][0])
+
+
 @pytest.mark.parametrize("n", [1101, 2600])
 def test_mixed_symmetric_lookahead(n, monkeypatch):
     """the symmetric factorisation with lookahead (BEAST_LU_LOOKAHEAD=1: the next panel's block
