@@ -535,17 +535,13 @@ __global__ void __launch_bounds__(TRI * TRI / (TS * TS)) k_lu_inv64(T* A, int64_
     dv[0] = d;
   }
   __syncthreads();  // the staging buffer is free from here on (L factor)
-  // TS = 2: a warp whose rows all lie above the pivot (2 warp + 1 < k) has nothing left to do in
-  // the loop; it leaves it and waits at the closing barrier, and the warps still in the loop
-  // synchronise on named barrier 1 with their own count, 32 (32 - k / 2) threads at step k
-  bool stop = false;
-  for (int kq = 0; kq < TRI / TS && !stop; ++kq) {
+  for (int kq = 0; kq < TRI / TS; ++kq) {
 #pragma unroll
     for (int kk = 0; kk < TS; ++kk) {
       const int k = TS * kq + kk, b = kk & 1;
-      if ((TS == 2 && r0 + TS - 1 < k) || s_zero[b]) {  // warp-uniform; a zero pivot: every warp left
-        stop = true;
-        break;
+      if (s_zero[b]) {  // uniform
+        if (tid == 0) atomicCAS(info, 0, (int)(j0 + s_zero[b]));
+        return;
       }
       const T d = dv[b];
       if (r0 + TS - 1 > k) {  // some row of the tile is below the pivot
@@ -596,18 +592,7 @@ __global__ void __launch_bounds__(TRI * TRI / (TS * TS)) k_lu_inv64(T* A, int64_
           dv[bn] = dn;
         }
       }
-      if (TS == 2)
-        asm volatile("bar.sync 1, %0;" ::"r"(32 * (32 - (k >> 1))) : "memory");
-      else
-        __syncthreads();
-    }
-  }
-  __syncthreads();  // every warp: those that left the loop early and those that finished it
-  {
-    const int z = max(s_zero[0], s_zero[1]);  // set only for a zero pivot (the elimination stops there)
-    if (z) {
-      if (tid == 0) atomicCAS(info, 0, (int)(j0 + z));
-      return;
+      __syncthreads();
     }
   }
   // U (upper part of S1) joins the L factor in Ls; the factored block goes back to A
