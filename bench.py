@@ -656,12 +656,17 @@ PRECISIONS = {"mixed": 1, "mixed-accurate": 2, "fp64": 0}
 
 
 def run_c4(args):
-    """C4: mixed-precision EFIE (c64 matrix, mixed factorisation, FP64 refinement) on icosphere
-    level --level (default 6: 81920 triangles, 122880 RT unknowns, a 121 GB matrix) at k = --k
-    (default 20), with its error calibrated at level 5 (30720 unknowns, where the FP64 matrix
-    fits) against FP64 GMRES on the FP64 matrix, the reference's iterative solver
-    (src/solvers/itsolver.jl:5-176): the mixed solve of the level-5 system is compared with
-    the GMRES solution (surface current and far field)."""
+    """C4: large EFIE with a c64 matrix (122880 RT unknowns at the default level 6, k = 20: a
+    121 GB matrix and its 121 GB factor copy on one GPU), mixed factorisation and FP64
+    refinement, in two assembly modes:
+      mixed             FP32 far pairs, FP32-moment Sauter-Schwab pairs;
+      mixed-accurate    double-float far and Sauter-Schwab pairs (the pairs' values to about
+                        1e-12), rounded once into the c64 matrix;
+    each calibrated at level 5 (30720 unknowns, where the FP64 matrix fits) against FP64 GMRES
+    on the FP64 matrix, the reference's iterative solver (src/solvers/itsolver.jl:5-176): the
+    level-5 solve of each mode is compared with the GMRES solution (surface current, far
+    field).  value: solves/s of the mode whose calibrated surface current meets 1e-6 (the
+    faster one if both do)."""
     import torch
     import beastgpu as bg
     from beastgpu import lib as L
@@ -674,8 +679,9 @@ def run_c4(args):
     dirs = np.stack([np.sin(th), np.zeros_like(th), np.cos(th)], axis=1)
     op = bg.Maxwell3D.singlelayer(wavenumber=k)
     stream = torch.cuda.current_stream()
+    modes = {"mixed": L.MIXED, "mixed-accurate": L.MIXED_ACCURATE}  # assembly precision, c64 storage
 
-    # ---- calibration at level 5: FP64 GMRES on the FP64 matrix vs the mixed solve
+    # ---- calibration at level 5: FP64 GMRES on the FP64 matrix vs each mode's solve
     ctx = bg.Context(dev)
     ctx.check(ctx.lib.beast_ctx_set_stream(ctx.handle, C.c_void_p(stream.cuda_stream)))
     X5 = bg.raviartthomas(bg.icosphere(5))
@@ -693,19 +699,20 @@ def run_c4(args):
     xg = x64.cpu().numpy()
     del Z64
     torch.cuda.empty_cache()
-    Zm, dtm, bm, xm = p5.buffers(L.MIXED)
-    p5.step(L.MIXED, Zm, dtm, bm, xm, wave, args.tol)
-    torch.cuda.synchronize()
-    calib = _accuracy(bg, X5, xm.cpu().numpy(), xg, dirs, g, ctx=ctx)
-    calib.update({"unknowns": int(n5), "reference": "FP64 GMRES on the FP64 (c128) matrix, x0 = 0",
-                  "gmres": {"iterations": gm_iters, "rel_residual": gm_res, "reltol": gm_tol,
-                            "restart": gm_restart, "ms": ms_gm, "converged": bool(gm_res <= gm_tol)},
-                  "mixed_refinement": {"iters": int(p5.it.value), "rel_residual": float(p5.res.value)}})
+    calib = {"unknowns": int(n5), "reference": "FP64 GMRES on the FP64 (c128) matrix, x0 = 0",
+             "gmres": {"iterations": gm_iters, "rel_residual": gm_res, "reltol": gm_tol, "restart": gm_restart,
+                       "ms": ms_gm, "converged": bool(gm_res <= gm_tol)}}
+    Zm, dtm, bm, xm = p5.buffers(L.MIXED)  # c64
+    for name, prec in modes.items():
+        p5.step(prec, Zm, dtm, bm, xm, wave, args.tol)
+        torch.cuda.synchronize()
+        calib[name] = _accuracy(bg, X5, xm.cpu().numpy(), xg, dirs, g, ctx=ctx)
+        calib[name]["refinement"] = {"iters": int(p5.it.value), "rel_residual": float(p5.res.value)}
     del Zm, bm, xm, b64, x64
     ctx.close()
     torch.cuda.empty_cache()
 
-    # ---- the timed large solve
+    # ---- the timed large solves
     ctx = bg.Context(dev)
     ctx.check(ctx.lib.beast_ctx_set_stream(ctx.handle, C.c_void_p(stream.cuda_stream)))
     m = bg.icosphere(args.level)
@@ -713,33 +720,41 @@ def run_c4(args):
     n = X.numfunctions()
     prob = Problem(ctx, X, op, L.EXC_TANGTRACE_E)
     Z, dt, b, x = prob.buffers(L.MIXED)
-    for _ in range(args.warmup):
-        prob.step(L.MIXED, Z, dt, b, x, wave, args.tol)
-    torch.cuda.synchronize()
-    clk = Clocks(dev)
-    evs = [_events() for _ in range(args.steps)]
-    for i in range(args.steps):
-        evs[i][0].record(stream)
-        prob.step(L.MIXED, Z, dt, b, x, wave, args.tol)
-        evs[i][1].record(stream)
-    torch.cuda.synchronize()
+    timed = {}
+    clk = None
+    for name, prec in modes.items():
+        for _ in range(args.warmup):
+            prob.step(prec, Z, dt, b, x, wave, args.tol)
+        torch.cuda.synchronize()
+        if clk is None:
+            clk = Clocks(dev)
+        evs = [_events() for _ in range(args.steps)]
+        for i in range(args.steps):
+            evs[i][0].record(stream)
+            prob.step(prec, Z, dt, b, x, wave, args.tol)
+            evs[i][1].record(stream)
+        torch.cuda.synchronize()
+        ms = [a.elapsed_time(b_) for a, b_ in evs]
+        mode = C.c_int(-1)
+        ctx.lib.beast_last_factor_mode(ctx.handle, C.byref(mode))
+        t = float(np.sum(ms)) / 1000.0
+        timed[name] = {"solves_per_s": args.steps / t, "ms_per_step": 1000.0 * t / args.steps, "step_ms": ms,
+                       "refinement": {"iters": int(prob.it.value), "rel_residual": float(prob.res.value),
+                                      "factorisation": FACTOR_MODES[max(0, mode.value)]},
+                       "calibrated_surface_current": calib[name]["surface_current"]}
     clocks = clk.stop()
-    ms = [a.elapsed_time(b_) for a, b_ in evs]
-    mode = C.c_int(-1)
-    ctx.lib.beast_last_factor_mode(ctx.handle, C.byref(mode))
-    t = float(np.sum(ms)) / 1000.0
-    out = {"metric": "solves/s", "value": args.steps / t, "unit": "solves/s", "n_gpus": 1, "steps": args.steps,
-           "warmup": args.warmup, "ms_per_step": 1000.0 * t / args.steps, "step_ms": ms,
+    ok = [nm for nm in modes if calib[nm]["surface_current"] <= 1e-6]
+    head = max(ok, key=lambda nm: timed[nm]["solves_per_s"]) if ok else "mixed"
+    out = {"metric": "solves/s", "value": timed[head]["solves_per_s"], "unit": "solves/s", "n_gpus": 1,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": timed[head]["ms_per_step"],
            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64+f64",
            "data": "synthetic (icosphere, plane wave)",
-           "config": {"workload": f"C4: mixed-precision EFIE k={k:g} on icosphere level {args.level} "
-                                  f"({m.numcells()} triangles, {n} RT unknowns)",
-                      "matrix_gb": n * n * 8 / 1e9, "precision": "mixed", "refinement_tol": args.tol,
-                      "step": "assembly (c64) + excitation + mixed factorisation + FP64 refinement",
+           "config": {"workload": f"C4: EFIE k={k:g} on icosphere level {args.level} "
+                                  f"({m.numcells()} triangles, {n} RT unknowns), c64 matrix",
+                      "matrix_gb": n * n * 8 / 1e9, "mode": head, "refinement_tol": args.tol,
+                      "step": "assembly into c64 + excitation + mixed factorisation + FP64 refinement",
                       "l2": "inputs larger than L2", "parallelism": "one GPU"},
-           "refinement": {"iters": int(prob.it.value), "rel_residual": float(prob.res.value),
-                          "factorisation": FACTOR_MODES[max(0, mode.value)]},
-           "calibration": calib, "clocks": clocks}
+           "modes": timed, "calibration": calib, "clocks": clocks}
     ctx.close()
     print(json.dumps(out))
 

@@ -135,6 +135,17 @@ def test_mixed_accurate_assembly(ctx):
     assert rel_entry(Z, Zo) < 1e-8, err_profile(Z, Zo)
 
 
+def test_mixed_accurate_assembly_into_c64(ctx):
+    """double-float assembly rounded once into a c64 matrix (the large-problem mode): every
+    entry is the correctly rounded float of the c128 mixed-accurate entry"""
+    X = bg.raviartthomas(bg.icosphere(2))
+    op = bg.Maxwell3D.singlelayer(wavenumber=3.0)
+    Z64 = bg.assemble(op, X, X, precision=bg.MIXED_ACCURATE, dtype=bg.C64, ctx=ctx)
+    Z128 = bg.assemble(op, X, X, precision=bg.MIXED_ACCURATE, ctx=ctx)
+    assert Z64.dtype == np.complex64 and Z128.dtype == np.complex128
+    assert np.array_equal(Z64, Z128.astype(np.complex64))
+
+
 @pytest.mark.parametrize("which", ["singlelayer", "doublelayer"])
 def test_mixed_accurate_near_pairs(ctx, which):
     """the double-float Sauter-Schwab pairs (face, edge and vertex classes) of the RT Maxwell
