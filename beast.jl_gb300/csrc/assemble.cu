@@ -2633,20 +2633,20 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_hh_df(NearParams P) {
   for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp; e < P.nnear; e += (int64_t)gridDim.x * NEAR_WARPS) {
-    const NearPair np_ = P.near[e];
-    if (!near_is_ssdf(P, np_.cls)) continue;
-    const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
-    const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
-    constexpr int NT = TP1 ? 3 : 1, NB = BP1 ? 3 : 1;
-    C2<double> z[NT * NB];
-    hh_sl_ss_df<TP1, BP1>(P.op, t, s, np_.cls, P.ssdf_tab[np_.cls], P.ssdf_items[np_.cls], s_tab, lane, z);
-    if (lane == 0)
-      for (int i = 0; i < NT; ++i)
-        for (int j = 0; j < NB; ++j)
-          store_c<double>(P.zcell, zidx(zrow_of(P.zrow, np_.p, NT, i), zcol_of(P.zcol, np_.q, NB, j), P.ldc),
-                          z[i * NB + j], P.zfmt);
-  }
+  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
+  if (e >= P.nnear) return;
+  const NearPair np_ = P.near[e];
+  if (!near_is_ssdf(P, np_.cls)) return;
+  const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
+  const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
+  constexpr int NT = TP1 ? 3 : 1, NB = BP1 ? 3 : 1;
+  C2<double> z[NT * NB];
+  hh_sl_ss_df<TP1, BP1>(P.op, t, s, np_.cls, P.ssdf_tab[np_.cls], P.ssdf_items[np_.cls], s_tab, lane, z);
+  if (lane == 0)
+    for (int i = 0; i < NT; ++i)
+      for (int j = 0; j < NB; ++j)
+        store_c<double>(P.zcell, zidx(zrow_of(P.zrow, np_.p, NT, i), zcol_of(P.zcol, np_.q, NB, j), P.ldc),
+                        z[i * NB + j], P.zfmt);
 }
 
 // the batch's P0 single-layer Sauter-Schwab pairs in double-float (the pairs k_near_batch
@@ -2671,25 +2671,15 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_batch_df(BatchLaunch L
 }
 
 template <bool SL>
-DEV void ss_df_pair(const NearParams& P, const NearPair np_, const float (*s_tab)[4], int lane);
-
-// a persistent grid: each warp takes the pairs warp, warp + W, .. of the list (W = the grid's
-// warps), so that the mix of face / edge / vertex pairs, and their 3750 / 1536 / 162 nodes,
-// evens out over a warp's pairs instead of leaving a CTA's warps idle behind its longest pair
-template <bool SL>
 __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
   __shared__ float s_tab[64][4];  // sin / cos(m pi/32)
   for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  for (int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp; e < P.nnear; e += (int64_t)gridDim.x * NEAR_WARPS) {
-    const NearPair np_ = P.near[e];
-    if (near_is_ssdf(P, np_.cls)) ss_df_pair<SL>(P, np_, s_tab, lane);
-  }
-}
-
-template <bool SL>
-DEV void ss_df_pair(const NearParams& P, const NearPair np_, const float (*s_tab)[4], int lane) {
+  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
+  if (e >= P.nnear) return;
+  const NearPair np_ = P.near[e];
+  if (!near_is_ssdf(P, np_.cls)) return;
   const Geo t = load_geo(P.tgeo + (int64_t)P.tperm[np_.p] * GEO_STRIDE);
   const Geo s = load_geo(P.bgeo + (int64_t)P.qcells[np_.q] * GEO_STRIDE);
   int pt[3], ps[3];
@@ -2871,34 +2861,18 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   unsigned blocks = (unsigned)((nnear + NEAR_WARPS - 1) / NEAR_WARPS);
   if (P.ss32) k_near_ss32<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   if (P.ssdf) {
-    // persistent grid: as many CTAs of 4 warps as fit on the device at once (a CTA that had to
-    // wait for a slot would run its share of the list after the others), each warp striding
-    // through the pair list
-    int dev = 0, nsm = 1;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    auto launch = [&](const void* fn, void (*k)(NearParams)) -> cudaError_t {
-      int occ = 0;
-      cudaError_t oe = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, 32 * NEAR_WARPS, 0);
-      if (oe != cudaSuccess) return oe;
-      const unsigned pg = std::min<unsigned>(blocks, (unsigned)(nsm * std::max(occ, 1)));
-      k<<<pg, 32 * NEAR_WARPS, 0, st>>>(P);
-      return cudaGetLastError();
-    };
-    cudaError_t le;
     if (rt_mw && a.op.kind == BEAST_MW_SL)
-      le = launch((const void*)k_near_ss_df<true>, k_near_ss_df<true>);
+      k_near_ss_df<true><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
     else if (rt_mw)
-      le = launch((const void*)k_near_ss_df<false>, k_near_ss_df<false>);
+      k_near_ss_df<false><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
     else if (P.tk == BEAST_P1 && P.bk == BEAST_P1)
-      le = launch((const void*)k_near_hh_df<1, 1>, k_near_hh_df<1, 1>);
+      k_near_hh_df<1, 1><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
     else if (P.tk == BEAST_P1)
-      le = launch((const void*)k_near_hh_df<1, 0>, k_near_hh_df<1, 0>);
+      k_near_hh_df<1, 0><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
     else if (P.bk == BEAST_P1)
-      le = launch((const void*)k_near_hh_df<0, 1>, k_near_hh_df<0, 1>);
+      k_near_hh_df<0, 1><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
     else
-      le = launch((const void*)k_near_hh_df<0, 0>, k_near_hh_df<0, 0>);
-    if (le != cudaSuccess) return le;
+      k_near_hh_df<0, 0><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   }
   k_near<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   if (P.qs.kind == BEAST_QS_TEST_REFINES_TRIAL || P.qs.kind == BEAST_QS_TRIAL_REFINES_TEST)
