@@ -2628,12 +2628,12 @@ DEV void hh_sl_ss_df(const OpParams& op, const Geo& t, const Geo& s, int cls, co
 // the Helmholtz single layer's Sauter-Schwab pairs (P0 / P1) of one assembly in double-float
 // (near_is_ssdf), one warp per pair
 template <int TP1, int BP1>
-__global__ void __launch_bounds__(32) k_near_hh_df(NearParams P) {  // one warp per CTA, as k_near_ss_df
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_hh_df(NearParams P) {
   __shared__ float s_tab[64][4];
   for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
-  __syncwarp();
-  const int lane = threadIdx.x & 31;
-  const int64_t e = blockIdx.x;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
   if (e >= P.nnear) return;
   const NearPair np_ = P.near[e];
   if (!near_is_ssdf(P, np_.cls)) return;
@@ -2670,16 +2670,13 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_batch_df(BatchLaunch L
   }
 }
 
-// One warp per CTA: pairs take 162 (vertex) to 3750 (face) nodes, and a CTA of several warps
-// would hold its SM slot until its longest pair is done; single-warp CTAs are handed out as
-// others finish.
 template <bool SL>
-__global__ void __launch_bounds__(32) k_near_ss_df(NearParams P) {
+__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
   __shared__ float s_tab[64][4];  // sin / cos(m pi/32)
   for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
-  __syncwarp();
-  const int lane = threadIdx.x & 31;
-  const int64_t e = blockIdx.x;
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t e = blockIdx.x * (int64_t)NEAR_WARPS + warp;
   if (e >= P.nnear) return;
   const NearPair np_ = P.near[e];
   if (!near_is_ssdf(P, np_.cls)) return;
@@ -2864,19 +2861,18 @@ cudaError_t launch_near(const AsmArgs& a, int nnear, const TriRuleDev& ro, const
   unsigned blocks = (unsigned)((nnear + NEAR_WARPS - 1) / NEAR_WARPS);
   if (P.ss32) k_near_ss32<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   if (P.ssdf) {
-    const unsigned pb = (unsigned)nnear;  // one warp (CTA) per pair
     if (rt_mw && a.op.kind == BEAST_MW_SL)
-      k_near_ss_df<true><<<pb, 32, 0, st>>>(P);
+      k_near_ss_df<true><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
     else if (rt_mw)
-      k_near_ss_df<false><<<pb, 32, 0, st>>>(P);
+      k_near_ss_df<false><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
     else if (P.tk == BEAST_P1 && P.bk == BEAST_P1)
-      k_near_hh_df<1, 1><<<pb, 32, 0, st>>>(P);
+      k_near_hh_df<1, 1><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
     else if (P.tk == BEAST_P1)
-      k_near_hh_df<1, 0><<<pb, 32, 0, st>>>(P);
+      k_near_hh_df<1, 0><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
     else if (P.bk == BEAST_P1)
-      k_near_hh_df<0, 1><<<pb, 32, 0, st>>>(P);
+      k_near_hh_df<0, 1><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
     else
-      k_near_hh_df<0, 0><<<pb, 32, 0, st>>>(P);
+      k_near_hh_df<0, 0><<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   }
   k_near<<<blocks, 32 * NEAR_WARPS, 0, st>>>(P);
   if (P.qs.kind == BEAST_QS_TEST_REFINES_TRIAL || P.qs.kind == BEAST_QS_TRIAL_REFINES_TEST)
