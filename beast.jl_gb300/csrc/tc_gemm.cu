@@ -320,13 +320,16 @@ __global__ void __launch_bounds__(192, 1)
       const int row = q * 32 + lane;
       // -1 / s of this thread's row (rows beyond the block are clipped by the TMA reduce)
       const float rs = m0 + row < m_rows ? -inv_sa[(m0 + row) >> 1] : 0.f;
-      for (int c = 0; c < nch; ++c) {
+      // chunks that hold a column of the rectangle (narrow updates leave the rest of the
+      // accumulator unread: its reduce-adds would lie wholly outside the tensor map)
+      const int nchv = max(1, min(nch, (n_cols - n0 + CCH - 1) / CCH));
+      for (int c = 0; c < nchv; ++c) {
         const int b = c & 1;
         float v[CCH];
         tmem_ld16(tbase + (uint32_t)(c * CCH), v);
         tmem_ld16(tbase + (uint32_t)(c * CCH + 16), v + 16);
-        if (c == nch - 1) {
-          // accumulator fully read: hand it back to the MMA warp
+        if (c == nchv - 1) {
+          // accumulator read: hand it back to the MMA warp
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
           __syncwarp();
           if (lane == 0)

@@ -223,6 +223,31 @@ def test_diagonal_block_tile_sizes_agree(symmetric, monkeypatch):
     assert np.array_equal(out["2"][0], out["4"][0])
 
 
+@pytest.mark.parametrize("zero_at", [0, 63])
+def test_symmetric_zero_pivot_hands_over(zero_at):
+    """an exactly zero pivot in the first diagonal block of a complex-symmetric matrix (the
+    first or the last step of the block's elimination): the symmetric factorisation reports
+    it, the unpivoted LU meets the same zero, and the solve ends on partial pivoting at the
+    FP64 residual"""
+    import torch
+    ctx = bg.get_context(0)
+    n = 300
+    rng = np.random.default_rng(41)
+    R = rng.normal(size=(n, n)) + 1j * rng.normal(size=(n, n))
+    A = (R + R.T) / 2 + 4 * n ** 0.5 * np.eye(n)
+    # row / column zero_at meets nothing inside the block before it, and its own diagonal is 0
+    A[zero_at, :zero_at] = 0.0
+    A[:zero_at, zero_at] = 0.0
+    A[zero_at, zero_at] = 0.0
+    A = A.astype(np.complex64)
+    b = rng.normal(size=n) + 1j * rng.normal(size=n)
+    At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda().T
+    x, it, res = bg.solve(At, b, precision=bg.MIXED, tol=1e-12, ctx=ctx)
+    assert ctx.last_factor_mode() == 0
+    r = A.astype(np.complex128) @ x - b
+    assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-11
+
+
 @pytest.mark.parametrize("n", [1101, 2600])
 def test_mixed_symmetric_lookahead(n, monkeypatch):
     """the symmetric factorisation with lookahead (BEAST_LU_LOOKAHEAD=1: the next panel's block
