@@ -2224,7 +2224,17 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
   __shared__ FarDfRecord rec[FAR_QT];
   __shared__ float s_tab[64][4];  // sin / cos(m pi/32): lanes read different entries
   __shared__ int s_zc[FAR_QT][3];
+  constexpr int NOW = NO > 0 ? NO : 1, NIW = NI > 0 ? NI : 1;
+  __shared__ dfl::df s_wab[NOW][NIW];  // w_a w_b / (4 pi) of the fast core
   for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
+  if constexpr (NO > 0) {
+    if (threadIdx.x == 0) {
+      dfl::df w1[NOW], w2[NIW];
+      for (int a = 0; a < NO; ++a) w1[a] = df_of(P.ro.w[a]);
+      for (int b = 0; b < NI; ++b) w2[b] = df_of(P.ri.w[b]);
+      dfl::efie_far_weights<NOW, NIW>(w1, w2, s_wab);
+    }
+  }
   const int ni = P.ri.n, no = P.ro.n;
   const int q0 = blockIdx.y * FAR_QT;
   const int nqt = min(FAR_QT, P.nq - q0);
@@ -2315,7 +2325,7 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
     }
     dfl::cdf z[9];
     if constexpr (NO > 0)
-      dfl::efie_far_pair_fast<NO, NI>(d, tau, r.sig, xi, wo, r.eta, r.w, r.eta2, kk, alpha, beta, s_tab, z);
+      dfl::efie_far_pair_fast<NO, NI>(d, tau, r.sig, xi, s_wab, r.eta, r.eta2, kk, alpha, beta, s_tab, z);
     else
       dfl::efie_far_pair(d, tau, r.sig, no, xi, wo, ni, r.eta, r.w, kk, alpha, beta, z);
     for (int i = 0; i < 3; ++i)

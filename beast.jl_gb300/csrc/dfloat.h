@@ -91,6 +91,17 @@ DF_HD df mul(df a, float b) {
   const df p = two_prod(a.hi, b);
   return fast_two_sum(p.hi, fmaf(a.lo, b, p.lo));
 }
+// the pair product left unnormalised (|lo| up to about 1.5 ulp(hi) instead of 0.5): for a
+// product whose consumer is a pair sum, a running sum or another product -- they add the low
+// parts in anyway -- the final fast two-sum of mul is three additions spent for nothing
+DF_HD df mulu(df a, df b) {
+  const float p = mul_rn(a.hi, b.hi);
+  return {p, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, fmaf(a.hi, b.hi, -p)))};
+}
+DF_HD df mulu(df a, float b) {
+  const float p = mul_rn(a.hi, b);
+  return {p, fmaf(a.lo, b, fmaf(a.hi, b, -p))};
+}
 // exact scaling by a power of two
 DF_HD df scale(df a, float p2) { return {mul_rn(a.hi, p2), mul_rn(a.lo, p2)}; }
 
@@ -112,7 +123,7 @@ DF_HD df rsqrt(df a) {
   const float y0 = 1.f / sqrtf(a.hi);
 #endif
   const df y2 = two_prod(y0, y0);
-  const df ay2 = mul(a, y2);
+  const df ay2 = mulu(a, y2);
   const float e = add_rn(sub_rn(1.f, ay2.hi), -ay2.lo);  // 1 - a y0^2, about 2^-22
   return fast_two_sum(y0, mul_rn(mul_rn(y0, e), 0.5f));
 }
@@ -167,12 +178,12 @@ DF_HD void sincos_tab(df th, const float (*tab)[4], df* s, df* c) {
   const float q = fmaf(t2, fmaf(t2, -1.f / 5040.f, 1.f / 120.f), -1.f / 6.f);
   const df st = fast_two_sum(t.hi, add_rn(t.lo, mul_rn(mul_rn(t.hi, t2), q)));
   const float r4 = mul_rn(mul_rn(t2, t2), fmaf(t2, -1.f / 720.f, 1.f / 24.f));
-  const df h = scale(mul(t, t), 0.5f);  // t^2 / 2 < 1.2e-3
+  const df h = scale(mulu(t, t), 0.5f);  // t^2 / 2 < 1.2e-3
   const df c1 = fast_two_sum(1.f, -h.hi);
   const df ct = fast_two_sum(c1.hi, add_rn(c1.lo, sub_rn(r4, h.lo)));
   const df sm = {tab[m][0], tab[m][1]}, cm = {tab[m][2], tab[m][3]};
-  *s = adds(mul(sm, ct), mul(cm, st));
-  *c = subs(mul(cm, ct), mul(sm, st));
+  *s = adds(mulu(sm, ct), mulu(cm, st));
+  *c = subs(mulu(cm, ct), mulu(sm, st));
 }
 
 // a += x for a running sum whose low part is normalised only at the end (norm): one TwoSum

@@ -80,10 +80,11 @@ DF_HD void efie_far_pair(const df* d, const df (*tau)[3], const df (*sig)[3], in
 // NI = 4 trial points), with the work per point pair cut down:
 //   * R^2 = (A_a + Q_b) - 2 P_ab with A_a = |d + xi_a|^2 (per test point), Q_b = |eta_b|^2 -
 //     2 d.eta_b (per trial point) and P_ab = xi_a.eta_b, which the M1 moment needs anyway;
-//   * 1 / R from a pair reciprocal square root, R = R^2 / R, the weight folded into 1/(4 pi R);
+//   * 1 / R from a pair reciprocal square root, R = R^2 / R, and both weights in one table,
+//     wab[a][b] = w_a w_b / (4 pi) (rule constants), so that a term is wab / R exp(-i k R);
 //   * sums whose terms do not cancel far below their size (dot products of small vectors, the
 //     angle sum of the sine / cosine) as sloppy pair sums, the moments as running sums
-//     normalised once;
+//     normalised once, and products that feed a sum or another product left unnormalised;
 //   * the table of sin / cos(m pi/32) read from `tab` (shared memory in the kernel);
 //   * the 3 x 3 block from per-row and per-column parts: z_ij = C - S_j - T_i + (tau_i.sig_j) D
 //     with C = a4 M1 + beta M0, S_j = a4 sig_j.V1, T_i = a4 tau_i.V2, D = a4 M0, a4 = alpha/4.
@@ -97,32 +98,41 @@ DF_HD void cacc(cdf& a, cdf x) {
 }
 DF_HD cdf cnorm(cdf a) { return {norm(a.re), norm(a.im)}; }
 DF_HD cdf csubs(cdf a, cdf b) { return {subs(a.re, b.re), subs(a.im, b.im)}; }
-DF_HD cdf cmuls(cdf a, cdf b) {
-  return {subs(mul(a.re, b.re), mul(a.im, b.im)), adds(mul(a.re, b.im), mul(a.im, b.re))};
+// unnormalised products (mulu) for operands of sums and products
+DF_HD cdf cscaleu(cdf a, df s) { return {mulu(a.re, s), mulu(a.im, s)}; }
+DF_HD cdf cmulu(cdf a, cdf b) {
+  return {subs(mulu(a.re, b.re), mulu(a.im, b.im)), adds(mulu(a.re, b.im), mulu(a.im, b.re))};
 }
 DF_HD df dot3s(const df* a, const df* b) { return adds(adds(mul(a[0], b[0]), mul(a[1], b[1])), mul(a[2], b[2])); }
-DF_HD cdf cdot3s(const cdf* v, const df* b) {
-  return cadds(cadds(cscale(v[0], b[0]), cscale(v[1], b[1])), cscale(v[2], b[2]));
+DF_HD df dot3u(const df* a, const df* b) { return adds(adds(mulu(a[0], b[0]), mulu(a[1], b[1])), mulu(a[2], b[2])); }
+DF_HD cdf cdot3u(const cdf* v, const df* b) {
+  return cadds(cadds(cscaleu(v[0], b[0]), cscaleu(v[1], b[1])), cscaleu(v[2], b[2]));
+}
+// wab[a][b] = w_a w_b / (4 pi) for the fast core (the same products on host and device)
+template <int NO, int NI>
+DF_HD void efie_far_weights(const df* wo, const df* wi, df (*wab)[NI]) {
+  const df i4pi{DF_I4PI_HI, DF_I4PI_LO};
+  for (int a = 0; a < NO; ++a)
+    for (int b = 0; b < NI; ++b) wab[a][b] = mul(mul(wo[a], wi[b]), i4pi);
 }
 
 template <int NO, int NI>
 DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3], const df (*xi)[3],
-                              const df* wo, const df (*eta)[3], const df* wi, const df* eta2, df k, cdf alpha,
-                              cdf beta, const float (*tab)[4], cdf* out) {
+                              const df (*wab)[NI], const df (*eta)[3], const df* eta2, df k, cdf alpha, cdf beta,
+                              const float (*tab)[4], cdf* out) {
   // The loops stay rolled: unrolled (even over the three test points alone), the kernel comes
   // to thousands of instructions and its warps stall on instruction fetch (measured: 12.2 ms
   // fully unrolled, 9.2 ms with the test points unrolled, 7.5 ms rolled, at 5120 cells).
   const df z0 = make(0.f);
-  const df i4pi{DF_I4PI_HI, DF_I4PI_LO};
   df A[NO];
-  cdf U0[NO];
+  cdf U0[NO];  // sum over b of the terms of test point a (its weight included)
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
   for (int a = 0; a < NO; ++a) {
     df dx[3];
     for (int c = 0; c < 3; ++c) dx[c] = adds(d[c], xi[a][c]);  // |d| >> |xi|: no cancellation
-    A[a] = dot3s(dx, dx);
+    A[a] = dot3u(dx, dx);
     U0[a] = cdf{z0, z0};
   }
   cdf M0{z0, z0}, M1{z0, z0}, V2[3];
@@ -131,29 +141,27 @@ DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3
 #pragma unroll 1
 #endif
   for (int b = 0; b < NI; ++b) {
-    const df Q = subs(eta2[b], scale(dot3s(d, eta[b]), 2.f));
-    const df wq = mul(wi[b], i4pi);
+    const df Q = subs(eta2[b], scale(dot3u(d, eta[b]), 2.f));
     cdf T{z0, z0};
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
     for (int a = 0; a < NO; ++a) {
-      const df P = dot3s(xi[a], eta[b]);
+      const df P = dot3u(xi[a], eta[b]);
       const df R2 = subs(adds(A[a], Q), scale(P, 2.f));
       const df iR = rsqrt(R2);
-      const df R = mul(R2, iR);
+      const df R = mulu(R2, iR);
       df sn, cs;
-      sincos_tab(mul(k, R), tab, &sn, &cs);
-      const df amp = mul(iR, wq);  // w_b / (4 pi R)
-      const cdf K{mul(amp, cs), neg(mul(amp, sn))};
+      sincos_tab(mulu(k, R), tab, &sn, &cs);
+      const df amp = mulu(iR, wab[a][b]);  // w_a w_b / (4 pi R)
+      const cdf K{mulu(amp, cs), neg(mulu(amp, sn))};
       cacc(U0[a], K);
-      const cdf wK = cscale(K, wo[a]);
-      cacc(T, wK);
-      cacc(M1, cscale(wK, P));
+      cacc(T, K);
+      cacc(M1, cscaleu(K, P));
     }
     T = cnorm(T);
     cacc(M0, T);
-    for (int c = 0; c < 3; ++c) cacc(V2[c], cscale(T, eta[b][c]));
+    for (int c = 0; c < 3; ++c) cacc(V2[c], cscaleu(T, eta[b][c]));
   }
   M0 = cnorm(M0);
   M1 = cnorm(M1);
@@ -164,28 +172,28 @@ DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3
 #pragma unroll 1
 #endif
   for (int a = 0; a < NO; ++a) {
-    const cdf s = cscale(cnorm(U0[a]), wo[a]);
-    for (int c = 0; c < 3; ++c) cacc(V1[c], cscale(s, xi[a][c]));
+    const cdf s = cnorm(U0[a]);
+    for (int c = 0; c < 3; ++c) cacc(V1[c], cscaleu(s, xi[a][c]));
   }
   for (int c = 0; c < 3; ++c) V1[c] = cnorm(V1[c]);
   const cdf a4{scale(alpha.re, 0.25f), scale(alpha.im, 0.25f)};
-  const cdf C = cadds(cmuls(a4, M1), cmuls(beta, M0));
-  const cdf D = cmuls(a4, M0);
+  const cdf C = cadds(cmulu(a4, M1), cmulu(beta, M0));
+  const cdf D = cmulu(a4, M0);
   cdf S[3];
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
-  for (int j = 0; j < 3; ++j) S[j] = cmuls(a4, cdot3s(V1, sig[j]));
+  for (int j = 0; j < 3; ++j) S[j] = cmulu(a4, cdot3u(V1, sig[j]));
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
   for (int i = 0; i < 3; ++i) {
-    const cdf Ti = cmuls(a4, cdot3s(V2, tau[i]));
+    const cdf Ti = cmulu(a4, cdot3u(V2, tau[i]));
     const cdf Ci = csubs(C, Ti);
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
-    for (int j = 0; j < 3; ++j) out[3 * i + j] = cadds(csubs(Ci, S[j]), cscale(D, dot3s(tau[i], sig[j])));
+    for (int j = 0; j < 3; ++j) out[3 * i + j] = cadds(csubs(Ci, S[j]), cscaleu(D, dot3u(tau[i], sig[j])));
   }
 }
 

@@ -32,6 +32,9 @@ struct ProfRec {
 struct beast_ctx {
   int device = 0;
   int num_sms = 0;
+  // SMs a tensor-core update leaves free (its persistent grid has num_sms - tc_sm_reserve
+  // CTAs): set while kernels of the lookahead stream are meant to run beside the update
+  int tc_sm_reserve = 0;
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   size_t ws_limit = 0;   // assembly workspace byte limit

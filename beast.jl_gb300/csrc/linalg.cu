@@ -2150,8 +2150,13 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
       // the block's rows of the columns beyond the block are updated here too (what the
       // pivoted path does per panel after the block).
       if (sym) {
-        if ((rc = S.symgemm(j0 + kb + skip, u_m0 - skip, j0 + kb, u_n0, j0, kb, false, tcwork, prepped, skip)))
-          break;
+        // with the next panel's elimination running on the second stream, the update's
+        // persistent grid leaves two SMs to it (a CTA of the update needs a whole SM: one held
+        // by the elimination would hold back the update's tiles until it ends)
+        ctx->tc_sm_reserve = next ? 2 : 0;
+        rc = S.symgemm(j0 + kb + skip, u_m0 - skip, j0 + kb, u_n0, j0, kb, false, tcwork, prepped, skip);
+        ctx->tc_sm_reserve = 0;
+        if (rc) break;
         if (next) BEAST_CUDA_TRY(ctx, cudaEventRecord(ctx->la_ev[3], st));
         ahead = next;
         continue;

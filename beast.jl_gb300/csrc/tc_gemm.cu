@@ -698,7 +698,7 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
   // algorithmic work: 8 K per complex element of the region (the lower triangle: half the square)
   ProfScope ps(ctx, PK_TCGEMM,
                8.0 * K * (u.lower ? 0.5 * (double)M0 * N0 : (double)M0 * N0 + (double)M1 * N1));
-  const int grid = std::min(Rg.ntiles, std::max(1, ctx->num_sms));
+  const int grid = std::min(Rg.ntiles, std::max(1, ctx->num_sms - ctx->tc_sm_reserve));
   k_tc_gemm<<<grid, 192, SMEM_BYTES, st>>>(tmA, tmB, tmC0, tmC1, Rg, inv_sa, inv_sb, nk, ctx->d_flag);
   BEAST_CUDA_TRY(ctx, cudaGetLastError());
   return BEAST_OK;

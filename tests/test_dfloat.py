@@ -65,9 +65,10 @@ void t_efie_pair(const double* tv, const double* bv, int no, const double* uvo, 
   }
   cdf z[9];
   if (fast && no == 3 && ni == 4) {
-    df e2[4];
+    df e2[4], wab[3][4];
     for (int b = 0; b < 4; ++b) e2[b] = dot3s(eta[b], eta[b]);
-    efie_far_pair_fast<3, 4>(d, tau, sig, xi, w1, eta, w2, e2, from(k), cdf{from(al[0]), from(al[1])},
+    efie_far_weights<3, 4>(w1, w2, wab);
+    efie_far_pair_fast<3, 4>(d, tau, sig, xi, wab, eta, e2, from(k), cdf{from(al[0]), from(al[1])},
                              cdf{from(be[0]), from(be[1])}, sincos_tab_host, z);
   } else {
     efie_far_pair(d, tau, sig, no, xi, w1, ni, eta, w2, from(k), cdf{from(al[0]), from(al[1])},
