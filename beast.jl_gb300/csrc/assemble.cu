@@ -2567,6 +2567,8 @@ DEV double warp_total_df(dfl::df x) {
 // nodes, per shape pair (a, b) of the reordered vertices the moment sum_k w_k G_k lt_a ls_b
 // (P0: one moment, shape value 1), the warp's totals in FP64 on every lane.  z[i * nb + j]:
 // the block in the cells' own vertex order (alpha and the Jacobian 4 A_t A_s included).
+// (Here and in k_near_ss_df every product inside the node loop feeds a pair sum, a running
+// sum or another product, so all of them are the unnormalised dfl::mulu.)
 template <int TP1, int BP1>
 DEV void hh_sl_ss_df(const OpParams& op, const Geo& t, const Geo& s, int cls, const float2* tab, int items,
                      const float (*s_tab)[4], int lane, C2<double>* z) {
@@ -2596,20 +2598,20 @@ DEV void hh_sl_ss_df(const OpParams& op, const Geo& t, const Geo& s, int cls, co
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
       if (cls == 3)
-        r[c] = dfl::adds(dfl::mul(D0, et1[c]), dfl::mul(D1, et2[c]));
+        r[c] = dfl::adds(dfl::mulu(D0, et1[c]), dfl::mulu(D1, et2[c]));
       else if (cls == 2)
-        r[c] = dfl::adds(dfl::mul(D0, et1[c]), dfl::subs(dfl::mul(X1, et2[c]), dfl::mul(Y1, es2[c])));
+        r[c] = dfl::adds(dfl::mulu(D0, et1[c]), dfl::subs(dfl::mulu(X1, et2[c]), dfl::mulu(Y1, es2[c])));
       else
-        r[c] = dfl::subs(dfl::adds(dfl::mul(X0, et1[c]), dfl::mul(X1, et2[c])),
-                         dfl::adds(dfl::mul(Y0, es1[c]), dfl::mul(Y1, es2[c])));
+        r[c] = dfl::subs(dfl::adds(dfl::mulu(X0, et1[c]), dfl::mulu(X1, et2[c])),
+                         dfl::adds(dfl::mulu(Y0, es1[c]), dfl::mulu(Y1, es2[c])));
     }
-    const dfl::df R2 = dfl::dot3s(r, r);
+    const dfl::df R2 = dfl::dot3u(r, r);
     const dfl::df iR = dfl::rsqrt(R2);
-    const dfl::df R = dfl::mul(R2, iR);
+    const dfl::df R = dfl::mulu(R2, iR);
     dfl::df sn, cs;
-    dfl::sincos_tab(dfl::mul(kk, R), s_tab, &sn, &cs);
-    const dfl::df amp = dfl::mul(dfl::mul(iR, w), i4pi);  // w / (4 pi R)
-    const dfl::df cr = dfl::mul(amp, cs), ci = dfl::neg(dfl::mul(amp, sn));
+    dfl::sincos_tab(dfl::mulu(kk, R), s_tab, &sn, &cs);
+    const dfl::df amp = dfl::mulu(dfl::mulu(iR, w), i4pi);  // w / (4 pi R)
+    const dfl::df cr = dfl::mulu(amp, cs), ci = dfl::neg(dfl::mulu(amp, sn));
     // shape values at the node in the reordered vertex order: lt = (1 - X0, X0 - X1, X1)
     const dfl::df lt[3] = {dfl::sub(one, X0), dfl::sub(X0, X1), X1};
     const dfl::df ls[3] = {dfl::sub(one, Y0), dfl::sub(Y0, Y1), Y1};
@@ -2618,9 +2620,9 @@ DEV void hh_sl_ss_df(const OpParams& op, const Geo& t, const Geo& s, int cls, co
 #pragma unroll
       for (int b = 0; b < NB; ++b) {
         dfl::df f = TP1 ? lt[a] : one;
-        if (BP1) f = BP1 && TP1 ? dfl::mul(f, ls[b]) : ls[b];
-        dfl::acc(m[a * NB + b][0], TP1 || BP1 ? dfl::mul(f, cr) : cr);
-        dfl::acc(m[a * NB + b][1], TP1 || BP1 ? dfl::mul(f, ci) : ci);
+        if (BP1) f = BP1 && TP1 ? dfl::mulu(f, ls[b]) : ls[b];
+        dfl::acc(m[a * NB + b][0], TP1 || BP1 ? dfl::mulu(f, cr) : cr);
+        dfl::acc(m[a * NB + b][1], TP1 || BP1 ? dfl::mulu(f, ci) : ci);
       }
   }
   const C2<double> al{op.ar, op.ai};
@@ -2723,26 +2725,26 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
     dfl::df xi[3], eta[3], r[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      xi[c] = dfl::adds(a0[c], dfl::adds(dfl::mul(X0, et1[c]), dfl::mul(X1, et2[c])));
-      eta[c] = dfl::adds(b0[c], dfl::adds(dfl::mul(Y0, es1[c]), dfl::mul(Y1, es2[c])));
+      xi[c] = dfl::adds(a0[c], dfl::adds(dfl::mulu(X0, et1[c]), dfl::mulu(X1, et2[c])));
+      eta[c] = dfl::adds(b0[c], dfl::adds(dfl::mulu(Y0, es1[c]), dfl::mulu(Y1, es2[c])));
       if (cls == 3)
-        r[c] = dfl::adds(dfl::mul(D0, et1[c]), dfl::mul(D1, et2[c]));
+        r[c] = dfl::adds(dfl::mulu(D0, et1[c]), dfl::mulu(D1, et2[c]));
       else if (cls == 2)
-        r[c] = dfl::adds(dfl::mul(D0, et1[c]), dfl::subs(dfl::mul(X1, et2[c]), dfl::mul(Y1, es2[c])));
+        r[c] = dfl::adds(dfl::mulu(D0, et1[c]), dfl::subs(dfl::mulu(X1, et2[c]), dfl::mulu(Y1, es2[c])));
       else
-        r[c] = dfl::subs(dfl::adds(dfl::mul(X0, et1[c]), dfl::mul(X1, et2[c])),
-                         dfl::adds(dfl::mul(Y0, es1[c]), dfl::mul(Y1, es2[c])));
+        r[c] = dfl::subs(dfl::adds(dfl::mulu(X0, et1[c]), dfl::mulu(X1, et2[c])),
+                         dfl::adds(dfl::mulu(Y0, es1[c]), dfl::mulu(Y1, es2[c])));
     }
-    const dfl::df R2 = dfl::dot3s(r, r);
+    const dfl::df R2 = dfl::dot3u(r, r);
     const dfl::df iR = dfl::rsqrt(R2);
-    const dfl::df R = dfl::mul(R2, iR);
+    const dfl::df R = dfl::mulu(R2, iR);
     dfl::df sn, cs;
-    dfl::sincos_tab(dfl::mul(kk, R), s_tab, &sn, &cs);
-    const dfl::df amp = dfl::mul(dfl::mul(iR, w), i4pi);  // w / (4 pi R)
-    dfl::df cr = dfl::mul(amp, cs), ci = dfl::neg(dfl::mul(amp, sn));
+    dfl::sincos_tab(dfl::mulu(kk, R), s_tab, &sn, &cs);
+    const dfl::df amp = dfl::mulu(dfl::mulu(iR, w), i4pi);  // w / (4 pi R)
+    dfl::df cr = dfl::mulu(amp, cs), ci = dfl::neg(dfl::mulu(amp, sn));
     dfl::df s0, a[3], b[3];
     if (SL) {
-      s0 = dfl::dot3s(xi, eta);
+      s0 = dfl::dot3u(xi, eta);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         a[c] = xi[c];
@@ -2752,36 +2754,36 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
       dfl::acc(m[1], ci);
     } else {
       // grad G = c r, c = -(i k + 1/R) G / R
-      const dfl::df pr = dfl::neg(dfl::mul(iR, iR)), pi = dfl::neg(dfl::mul(kk, iR));
-      const dfl::df nr = dfl::subs(dfl::mul(pr, cr), dfl::mul(pi, ci));
-      const dfl::df ni = dfl::adds(dfl::mul(pr, ci), dfl::mul(pi, cr));
+      const dfl::df pr = dfl::neg(dfl::mulu(iR, iR)), pi = dfl::neg(dfl::mulu(kk, iR));
+      const dfl::df nr = dfl::subs(dfl::mulu(pr, cr), dfl::mulu(pi, ci));
+      const dfl::df ni = dfl::adds(dfl::mulu(pr, ci), dfl::mulu(pi, cr));
       cr = nr;
       ci = ni;
       // xi.(r x eta) = xi.(d x eta); a = xi x r, b = r x eta
-      const dfl::df de[3] = {dfl::subs(dfl::mul(dd[1], eta[2]), dfl::mul(dd[2], eta[1])),
-                             dfl::subs(dfl::mul(dd[2], eta[0]), dfl::mul(dd[0], eta[2])),
-                             dfl::subs(dfl::mul(dd[0], eta[1]), dfl::mul(dd[1], eta[0]))};
-      s0 = dfl::dot3s(xi, de);
+      const dfl::df de[3] = {dfl::subs(dfl::mulu(dd[1], eta[2]), dfl::mulu(dd[2], eta[1])),
+                             dfl::subs(dfl::mulu(dd[2], eta[0]), dfl::mulu(dd[0], eta[2])),
+                             dfl::subs(dfl::mulu(dd[0], eta[1]), dfl::mulu(dd[1], eta[0]))};
+      s0 = dfl::dot3u(xi, de);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const int c1 = (c + 1) % 3, c2 = (c + 2) % 3;
-        a[c] = dfl::subs(dfl::mul(xi[c1], r[c2]), dfl::mul(xi[c2], r[c1]));
-        b[c] = dfl::subs(dfl::mul(r[c1], eta[c2]), dfl::mul(r[c2], eta[c1]));
+        a[c] = dfl::subs(dfl::mulu(xi[c1], r[c2]), dfl::mulu(xi[c2], r[c1]));
+        b[c] = dfl::subs(dfl::mulu(r[c1], eta[c2]), dfl::mulu(r[c2], eta[c1]));
       }
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        dfl::acc(m[16 + 2 * c], dfl::mul(r[c], cr));
-        dfl::acc(m[17 + 2 * c], dfl::mul(r[c], ci));
+        dfl::acc(m[16 + 2 * c], dfl::mulu(r[c], cr));
+        dfl::acc(m[17 + 2 * c], dfl::mulu(r[c], ci));
       }
     }
-    dfl::acc(m[2], dfl::mul(s0, cr));
-    dfl::acc(m[3], dfl::mul(s0, ci));
+    dfl::acc(m[2], dfl::mulu(s0, cr));
+    dfl::acc(m[3], dfl::mulu(s0, ci));
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-      dfl::acc(m[4 + 2 * c], dfl::mul(a[c], cr));
-      dfl::acc(m[5 + 2 * c], dfl::mul(a[c], ci));
-      dfl::acc(m[10 + 2 * c], dfl::mul(b[c], cr));
-      dfl::acc(m[11 + 2 * c], dfl::mul(b[c], ci));
+      dfl::acc(m[4 + 2 * c], dfl::mulu(a[c], cr));
+      dfl::acc(m[5 + 2 * c], dfl::mulu(a[c], ci));
+      dfl::acc(m[10 + 2 * c], dfl::mulu(b[c], cr));
+      dfl::acc(m[11 + 2 * c], dfl::mulu(b[c], ci));
     }
   }
   // the warp's totals (exact pair sums), then FP64
