@@ -299,6 +299,9 @@ __global__ void __launch_bounds__(192, 1)
     const int q = warp & 3;
     const bool leader = (warp == 2 && lane == 0);
     const int nch = TN / CCH;
+    // the chunk buffers alternate over this CTA's whole chunk sequence (tiles may end on an odd
+    // chunk), so that the buffer being refilled is always the one of two reduces back
+    int gc = 0;
     int t = 0;
     for (int tile = unit0; tile < ntiles; tile += nunits, ++t) {
       const int a = t & 1;
@@ -323,8 +326,8 @@ __global__ void __launch_bounds__(192, 1)
       // chunks that hold a column of the rectangle (narrow updates leave the rest of the
       // accumulator unread: its reduce-adds would lie wholly outside the tensor map)
       const int nchv = max(1, min(nch, (n_cols - n0 + CCH - 1) / CCH));
-      for (int c = 0; c < nchv; ++c) {
-        const int b = c & 1;
+      for (int c = 0; c < nchv; ++c, ++gc) {
+        const int b = gc & 1;
         float v[CCH];
         tmem_ld16(tbase + (uint32_t)(c * CCH), v);
         tmem_ld16(tbase + (uint32_t)(c * CCH + 16), v + 16);
@@ -338,7 +341,7 @@ __global__ void __launch_bounds__(192, 1)
         // 1 / t of the chunk's columns, one per lane, broadcast by shuffles
         const int gcol = n0 + c * CCH + lane;
         const float cs = gcol < n_cols ? inv_sb[Rg.b_col[rr] + gcol] : 0.f;
-        if (leader) bulk_wait_read1();  // the reduce of chunk c-2 has read buffer b
+        if (leader) bulk_wait_read1();  // the reduce two chunks back has read buffer b
         asm volatile("bar.sync 1, 128;" ::: "memory");
         float* cb = cbuf_g + b * (TM * CCH);
 #pragma unroll

@@ -168,14 +168,15 @@ def test_mixed_unpivoted_path_converges_without_fallback(n):
     assert np.linalg.norm(r) / np.linalg.norm(b) < 1e-12
 
 
-@pytest.mark.parametrize("n", [700, 1101, 2600])
+@pytest.mark.parametrize("n", [700, 1101, 2600, 3664])
 def test_mixed_symmetric_path(n):
     """a complex-symmetric matrix up to a 1e-6 perturbation: the mixed solve uses the symmetric
     factorisation (diagonal-block LU from the lower triangle, L21 products only, updates of
     the lower triangle with lower-triangle tiles in the trailing update -- two outer blocks
     for n = 2600, odd last panel for all sizes; n = 700 has no trailing update and takes the
-    CUDA-core updates with B = D L^T formed explicitly) and refines to an FP64 residual
-    without handing over to an LU"""
+    CUDA-core updates with B = D L^T formed explicitly; n = 3664: a trailing update of 2640
+    columns, more tiles than SMs, whose last column tiles end on an odd number of 32-column
+    epilogue chunks) and refines to an FP64 residual without handing over to an LU"""
     import torch
     ctx = bg.get_context(0)
     rng = np.random.default_rng(21)
