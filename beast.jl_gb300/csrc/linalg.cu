@@ -499,6 +499,9 @@ __global__ void __launch_bounds__(TRI * TRI / (TS * TS)) k_lu_inv64(T* A, int64_
   __shared__ T p1[2][PL], p2[2][PL], lc[2][TRI];
   __shared__ T dv[2];
   __shared__ int s_zero[2];  // 1-based column of a zero pivot, by step parity
+  // the panel products launched after this kernel may start their loads now (they wait for
+  // its results before reading them)
+  asm volatile("griddepcontrol.launch_dependents;");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int cb = TS == 4 ? (lane & 15) : lane, rb = TS == 4 ? 2 * warp + (lane >> 4) : warp;
   const int r0 = TS * rb, c0 = TS * cb;
@@ -825,7 +828,7 @@ __device__ __forceinline__ void cmac2(float2& acc, float4 a, float4 b) {
 // rb0: index of the first CTA's block (the grid covers blocks rb0 .. of the 2 nR, or nR)
 template <int NS>
 __global__ void __launch_bounds__(256, NS == 64 ? 2 : 3) k_panel_apply(float2* A, int64_t lda, int64_t j0, int64_t n,
-                                                        const float2* __restrict__ inv, int nR, __half2* Ap,
+                                                        const float2* inv, int nR, __half2* Ap,
                                                         float* inv_sa, __half2* Bp, float* inv_sb, int nB,
                                                         int rb0) {
   extern __shared__ __align__(16) unsigned char smraw[];
@@ -870,10 +873,15 @@ __global__ void __launch_bounds__(256, NS == 64 ? 2 : 3) k_panel_apply(float2* A
           w[t] = b0 + s < n ? A[(j0 + kb0 + k) + (b0 + s) * lda] : zero;
         }
       }
+      // launched as a programmatic dependent of the diagonal block's elimination: the rows of
+      // A21 / A12 above are final already, the inverses (and the pivots below) only after this
+      // wait (a no-op for an ordinary launch); `inv` is not declared __restrict__ and is read
+      // through L2, so that no load of it is scheduled or served from before the wait
+      if (kh == 0) asm volatile("griddepcontrol.wait;" ::: "memory");
 #pragma unroll
       for (int t = 0; t < 8; ++t) {
         const int e = tid + 256 * t;
-        v[t] = right ? inv[4096 + (e >> 5) * 64 + kb0 + (e & 31)] : inv[(kb0 + (e >> 6)) * 64 + (e & 63)];
+        v[t] = __ldcg(right ? inv + 4096 + (e >> 5) * 64 + kb0 + (e & 31) : inv + (kb0 + (e >> 6)) * 64 + (e & 63));
       }
 #pragma unroll
       for (int t = 0; t < TW; ++t) {
@@ -974,7 +982,9 @@ __global__ void __launch_bounds__(256, NS == 64 ? 2 : 3) k_panel_apply(float2* A
     // symmetric: B' column of system s (< nB) = D (row s of L21), its own scale
     __shared__ float2 s_d[64];
     __shared__ float s_tsc[64];
-    if (tid < 64) s_d[tid] = A[(j0 + tid) + (j0 + tid) * lda];
+    // the pivots are the elimination's output: through L2 (the rows of A21 read before the
+    // wait may have brought a line of the diagonal block into L1 before it was written)
+    if (tid < 64) s_d[tid] = __ldcg(A + (j0 + tid) + (j0 + tid) * lda);
     __syncthreads();
     const int sy = tid % NS, q = tid / NS;
     float mx = 0.f;
@@ -1059,10 +1069,14 @@ __global__ void k_dlt(const T* L, const T* dg, int64_t lda, int K, int N, T* B) 
 // U = D L^T above the 64 x 64 diagonal blocks: block (I, J), I < J, from the transposed block
 // (J, I) of L and the pivots of rows 64 I..: U[i][j] = d_i L[j][i] (the diagonal blocks
 // already hold U11 from k_lu_inv64)
+// One CTA per block pair I < J (linear index J (J - 1) / 2 + I: no CTA on or below the diagonal).
 template <typename T>
 __global__ void __launch_bounds__(256) k_sym_upper(T* A, int64_t lda, int64_t n) {
-  const int J = blockIdx.x, I = blockIdx.y;
-  if (I >= J) return;
+  const int64_t L = blockIdx.x;
+  int J = (int)((1.0f + sqrtf(1.0f + 8.0f * (float)L)) * 0.5f);
+  while ((int64_t)J * (J - 1) / 2 > L) --J;
+  while ((int64_t)(J + 1) * J / 2 <= L) ++J;
+  const int I = (int)(L - (int64_t)J * (J - 1) / 2);
   __shared__ T t[64][65];
   __shared__ T d[64];
   const int64_t r0 = 64 * (int64_t)I, c0 = 64 * (int64_t)J;
@@ -1158,27 +1172,41 @@ __global__ void k_asym_sample(const T* A, int64_t lda, int64_t n, int64_t s, dou
 // copy of the block-lower part of a c64 matrix: column j from row 64 floor(j / 64) down (what
 // the symmetric factorisation reads; the rest of the copy is written at its end).  Two rows
 // per thread (16-byte accesses when lda and ldf are even and the bases 16-byte aligned).
-__global__ void k_copy_lower_c64(int64_t n, const float2* A, int64_t lda, float2* F, int64_t ldf, int vec) {
-  for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
-    const int64_t r0 = (j / 64) * 64;
-    const int64_t i = r0 + 2 * (blockIdx.x * (int64_t)blockDim.x + threadIdx.x);
-    if (i >= n) continue;
-    if (vec && i + 1 < n)
-      *reinterpret_cast<float4*>(F + i + j * ldf) = *reinterpret_cast<const float4*>(A + i + j * lda);
-    else {
-      F[i + j * ldf] = A[i + j * lda];
-      if (i + 1 < n) F[i + 1 + j * ldf] = A[i + 1 + j * lda];
+__global__ void __launch_bounds__(256) k_copy_lower_c64(int64_t n, const float2* A, int64_t lda, float2* F,
+                                                       int64_t ldf, int vec) {
+  // a CTA per column, two elements per thread and step (one 16-byte access when aligned)
+  for (int64_t j = blockIdx.x; j < n; j += gridDim.x) {
+    const float2* a = A + j * lda;
+    float2* f = F + j * ldf;
+    for (int64_t i = (j / 64) * 64 + 2 * threadIdx.x; i < n; i += 2 * 256) {
+      if (vec && i + 1 < n) {
+        *reinterpret_cast<float4*>(f + i) = __ldcs(reinterpret_cast<const float4*>(a + i));
+      } else {
+        f[i] = a[i];
+        if (i + 1 < n) f[i + 1] = a[i + 1];
+      }
     }
   }
 }
 
-// the same block-lower part from a c128 matrix, rounded to c64 by integer operations
-__global__ void k_convert_lower_c128(int64_t n, const double2* A, int64_t lda, float2* F, int64_t ldf) {
-  for (int64_t j = blockIdx.y; j < n; j += gridDim.y) {
-    const int64_t i = (j / 64) * 64 + blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (i >= n) continue;
-    const double2 a = __ldcs(A + i + j * lda);
-    F[i + j * ldf] = make_float2(fsplit::to_float_rn(a.x), fsplit::to_float_rn(a.y));
+// the same block-lower part from a c128 matrix, rounded to c64 by integer operations: a CTA
+// per column (its rows from the first row of the column's diagonal block on), four streaming
+// loads in flight per thread -- no CTA of the grid falls wholly above the diagonal
+__global__ void __launch_bounds__(256) k_convert_lower_c128(int64_t n, const double2* A, int64_t lda, float2* F,
+                                                           int64_t ldf) {
+  auto cvt = [](double2 a) { return make_float2(fsplit::to_float_rn(a.x), fsplit::to_float_rn(a.y)); };
+  for (int64_t j = blockIdx.x; j < n; j += gridDim.x) {
+    const double2* a = A + j * lda;
+    float2* f = F + j * ldf;
+    int64_t i = (j / 64) * 64 + threadIdx.x;
+    for (; i + 3 * 256 < n; i += 4 * 256) {
+      double2 v[4];
+#pragma unroll
+      for (int u = 0; u < 4; ++u) v[u] = __ldcs(a + i + u * 256);
+#pragma unroll
+      for (int u = 0; u < 4; ++u) f[i + u * 256] = cvt(v[u]);
+    }
+    for (; i < n; i += 256) f[i] = cvt(__ldcs(a + i));
   }
 }
 
@@ -2133,8 +2161,21 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
             // 32 systems per CTA: twice the CTAs of half the work, so that more warps hide the
             // shared-memory latency of the triangular products
             const int nR32 = (int)((rb + 31) / 32);
-            k_panel_apply<32><<<(unsigned)(sym ? nR32 : 2 * nR32), 256, panel_apply_smem(), st>>>(
-                Af, lda, j0, n, inv, nR32, static_cast<__half2*>(Apv), isa, static_cast<__half2*>(Bpv), isb, nBp, 0);
+            // a programmatic dependent launch: its CTAs take the SMs the one-CTA elimination
+            // leaves idle and load their rows while it runs
+            cudaLaunchConfig_t cfg = {};
+            cfg.gridDim = dim3((unsigned)(sym ? nR32 : 2 * nR32));
+            cfg.blockDim = dim3(256);
+            cfg.dynamicSmemBytes = panel_apply_smem();
+            cfg.stream = st;
+            cudaLaunchAttribute pdl[1];
+            pdl[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+            pdl[0].val.programmaticStreamSerializationAllowed = 1;
+            cfg.attrs = pdl;
+            cfg.numAttrs = 1;
+            BEAST_CUDA_TRY(ctx, cudaLaunchKernelEx(&cfg, k_panel_apply<32>, Af, lda, j0, n, inv, nR32,
+                                                   static_cast<__half2*>(Apv), isa, static_cast<__half2*>(Bpv), isb,
+                                                   nBp, 0));
             ctx->launches += 1;
           }
           applied = true;
@@ -2220,9 +2261,9 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   }
   BEAST_CUDA_TRY(ctx, cudaMemcpy(ipiv + n, perm.data(), n * sizeof(int), cudaMemcpyHostToDevice));
   if (sym) {  // U = D L^T above the diagonal blocks
-    const unsigned nbk = (unsigned)((n + 63) / 64);
+    const int64_t nbk = (n + 63) / 64;
     ProfScope ps(ctx, PK_CONVERT, (double)n * n * sizeof(T));
-    k_sym_upper<T><<<dim3(nbk, nbk), 256, 0, st>>>(A, lda, n);
+    if (nbk > 1) k_sym_upper<T><<<(unsigned)(nbk * (nbk - 1) / 2), 256, 0, st>>>(A, lda, n);
     BEAST_CUDA_TRY(ctx, cudaGetLastError());
   }
   // inverses of the diagonal blocks for the triangular solves (already written by k_lu_inv64
@@ -2376,15 +2417,16 @@ cudaError_t copy_lower_c64(int64_t n, const void* A, int64_t lda, void* F, int64
                    (reinterpret_cast<uintptr_t>(F) & 15) == 0)
                       ? 1
                       : 0;
-  // grid.x covers the longest column (n rows, two per thread); shorter columns exit early
-  dim3 g((unsigned)((n + 511) / 512), (unsigned)std::min<int64_t>(n, 65535));
-  k_copy_lower_c64<<<g, 256, 0, st>>>(n, (const float2*)A, lda, (float2*)F, ldf, vec);
+  if (n <= 0) return cudaSuccess;
+  k_copy_lower_c64<<<(unsigned)std::min<int64_t>(n, 65535), 256, 0, st>>>(n, (const float2*)A, lda, (float2*)F, ldf,
+                                                                          vec);
   return cudaGetLastError();
 }
 
 cudaError_t convert_lower_c128_to_c64(int64_t n, const void* A, int64_t lda, void* F, int64_t ldf, cudaStream_t st) {
-  dim3 g((unsigned)((n + 255) / 256), (unsigned)std::min<int64_t>(n, 65535));
-  k_convert_lower_c128<<<g, 256, 0, st>>>(n, (const double2*)A, lda, (float2*)F, ldf);
+  if (n <= 0) return cudaSuccess;
+  k_convert_lower_c128<<<(unsigned)std::min<int64_t>(n, 65535), 256, 0, st>>>(n, (const double2*)A, lda, (float2*)F,
+                                                                              ldf);
   return cudaGetLastError();
 }
 cudaError_t convert_c128_to_c64(int64_t rows, int64_t cols, const double* src, int64_t lds, float* dst,
