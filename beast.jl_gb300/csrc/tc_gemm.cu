@@ -164,7 +164,8 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 // lower = 1 (one square rectangle on the diagonal, symmetric updates): only the tiles that
 // hold an element on or below the diagonal, i.e. column tile n <= m / 4 for row tile m
 // (128 real rows = 64 complex rows against 256 columns); rows come in groups of four with
-// g + 1 tiles each, so tile t of group g = floor((sqrt(2t + 1) - 1) / 2) is found in closed form.
+// g + 1 tiles each, so tile t of group g = floor((sqrt(2t + 1) - 1) / 2) is found in closed form;
+// a whole group is visited column by column, a partial last group row by row.
 struct TcRegion {
   int m_rows[2], n_cols[2], b_col[2], c_col0[2];
   int c_row0;
@@ -204,8 +205,15 @@ __global__ void __launch_bounds__(192, 1)
       while (2 * g * (g + 1) > tile) --g;
       while (2 * (g + 1) * (g + 2) <= tile) ++g;
       const int t = tile - 2 * g * (g + 1);
-      m0 = (4 * g + t / (g + 1)) * TM;
-      n0 = (t % (g + 1)) * TN;
+      if (4 * (g + 1) * TM <= Rg.m_rows[0]) {
+        // a whole group: column by column, so that the CTAs at work share each B' tile four
+        // ways and the group's four A' row tiles across the wave
+        m0 = (4 * g + (t & 3)) * TM;
+        n0 = (t >> 2) * TN;
+      } else {  // the last, partial group row by row (its tiles beyond the count are the rows that do not exist)
+        m0 = (4 * g + t / (g + 1)) * TM;
+        n0 = (t % (g + 1)) * TN;
+      }
       return m0 < Rg.m_rows[0];
     }
     r = tile < Rg.ntiles0 ? 0 : 1;
