@@ -156,11 +156,12 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 // tcgen05.mma into one of two 256-column TMEM accumulators, warps 2..5 drain the other
 // accumulator (tcgen05.ld -> C' -= D) so that the epilogue of tile t overlaps the loads and
 // MMAs of tile t+1.  Barriers: full/empty per stage (TMA <-> MMA), tfull/tempty per
-// accumulator (MMA <-> epilogue).  Tiles are visited N-fastest (B' stays in L2).
+// accumulator (MMA <-> epilogue).  Tile order: see TcRegion below.
 // The update region is one or two rectangles of C' that share the operands: rectangle r
 // covers the first m_rows[r] rows of A' and the n_cols[r] columns of B' from b_col[r], and
 // writes C' through its own (clipped) tensor map at (c_row0, c_col0[r]).  Tiles of
-// rectangle 0 come first in the tile order.
+// rectangle 0 come first in the tile order; within a rectangle, groups of four row tiles,
+// each whole group column by column.
 // lower = 1 (one square rectangle on the diagonal, symmetric updates): only the tiles that
 // hold an element on or below the diagonal, i.e. column tile n <= m / 4 for row tile m
 // (128 real rows = 64 complex rows against 256 columns); rows come in groups of four with
@@ -218,8 +219,15 @@ __global__ void __launch_bounds__(192, 1)
     }
     r = tile < Rg.ntiles0 ? 0 : 1;
     const int lt = r ? tile - Rg.ntiles0 : tile;
-    m0 = (lt / Rg.ntn[r]) * TM;
-    n0 = (lt % Rg.ntn[r]) * TN;
+    // groups of four row tiles, a whole group column by column (as the lower-triangle tiles)
+    const int ntn = Rg.ntn[r], G = lt / (4 * ntn), l = lt - G * 4 * ntn;
+    if (4 * (G + 1) * TM <= Rg.m_rows[r]) {
+      m0 = (4 * G + (l & 3)) * TM;
+      n0 = (l >> 2) * TN;
+    } else {
+      m0 = (4 * G + l / ntn) * TM;
+      n0 = (l % ntn) * TN;
+    }
     return m0 < Rg.m_rows[r];
   };
 
