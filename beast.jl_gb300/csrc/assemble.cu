@@ -2682,8 +2682,10 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_batch_df(BatchLaunch L
   }
 }
 
+// five CTAs per SM (96 registers, a few spilled): measured 9.9 -> 9.6 ms per C2 solve against
+// four CTAs at 128 registers
 template <bool SL>
-__global__ void __launch_bounds__(32 * NEAR_WARPS) k_near_ss_df(NearParams P) {
+__global__ void __launch_bounds__(32 * NEAR_WARPS, 5) k_near_ss_df(NearParams P) {
   __shared__ float s_tab[64][4];  // sin / cos(m pi/32)
   for (int k = threadIdx.x; k < 256; k += blockDim.x) s_tab[k >> 2][k & 3] = dfl::sincos_tab_dev[k >> 2][k & 3];
   __syncthreads();
