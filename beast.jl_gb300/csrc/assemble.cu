@@ -2792,9 +2792,11 @@ __global__ void __launch_bounds__(32 * NEAR_WARPS, 5) k_near_ss_df(NearParams P)
   double md[22];
 #pragma unroll
   for (int q = 0; q < 22; ++q) {
+    if ((q < 2 && !SL) || (q >= NM && SL)) {  // moments this operator does not have: no butterfly
+      md[q] = 0.0;
+      continue;
+    }
     dfl::df x = dfl::norm(m[q]);
-    if (q < 2 && !SL) x = dfl::make(0.f);
-    if (q >= NM && SL) x = dfl::make(0.f);
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
       const dfl::df y{__shfl_xor_sync(0xffffffffu, x.hi, o), __shfl_xor_sync(0xffffffffu, x.lo, o)};
