@@ -486,13 +486,16 @@ __device__ __forceinline__ int pidx(int c) {  // conflict-free index of the publ
 // SYM: only the lower triangle of the block is current (symmetric updates); the upper one
 // is taken from it by symmetry, the elimination on U^T is skipped and, U = D L^T,
 // U^{-1} = (L^{-1})^T D^{-1} is formed from L^{-1} and the pivots at the end.
-// TS: the tile edge owned by a thread: 4 (256 threads) or 2 (1024 threads: a quarter of the
-// serial instructions per warp and step, which is what bounds this latency-bound chain)
-template <typename T, bool SYM, int TS = 4>
-__global__ void __launch_bounds__(TRI * TRI / (TS * TS)) k_lu_inv64(T* A, int64_t lda, int64_t j0, int kb, int* info,
+// TR x TC: the tile a thread owns (rows x columns): 4 x 4 (256 threads), 2 x 4 (512) or 2 x 2
+// (1024 threads: a quarter of the serial instructions per warp and step of 4 x 4, which is what
+// bounds this latency-bound chain).  The arithmetic per element is the same for every tile.
+template <typename T, bool SYM, int TR = 4, int TC = TR>
+__global__ void __launch_bounds__(TRI * TRI / (TR * TC)) k_lu_inv64(T* A, int64_t lda, int64_t j0, int kb, int* info,
                                                                    T* inv) {
   constexpr bool sym = SYM;
-  constexpr int NT = TRI * TRI / (TS * TS);  // threads
+  constexpr int NT = TRI * TRI / (TR * TC);  // threads
+  constexpr int NCB = TRI / TC;              // column blocks: 32 (a warp) or 16 (half a warp)
+  static_assert(TC % TR == 0 && (NCB == 32 || NCB == 16), "tile: TR divides TC, TC = 2 or 4");
   constexpr int LD = TRI + 1, PL = TRI + TRI / 4;
   extern __shared__ unsigned char smraw[];
   T* Ls = reinterpret_cast<T*>(smraw);  // 64 x LD: staging, then the L factor, then Linv
@@ -503,8 +506,8 @@ __global__ void __launch_bounds__(TRI * TRI / (TS * TS)) k_lu_inv64(T* A, int64_
   // its results before reading them)
   asm volatile("griddepcontrol.launch_dependents;");
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-  const int cb = TS == 4 ? (lane & 15) : lane, rb = TS == 4 ? 2 * warp + (lane >> 4) : warp;
-  const int r0 = TS * rb, c0 = TS * cb;
+  const int cb = NCB == 16 ? (lane & 15) : lane, rb = NCB == 16 ? 2 * warp + (lane >> 4) : warp;
+  const int r0 = TR * rb, c0 = TC * cb;
   const T zero = cmk<T>(0.0, 0.0), one = cmk<T>(1.0, 0.0);
   // coalesced load through shared memory (identity padding beyond kb)
   for (int e = tid; e < TRI * TRI; e += NT) {
@@ -514,56 +517,58 @@ __global__ void __launch_bounds__(TRI * TRI / (TS * TS)) k_lu_inv64(T* A, int64_
   }
   if (tid < 2) s_zero[tid] = 0;
   __syncthreads();
-  T s1[TS][TS], s2[TS][TS];
+  T s1[TR][TC], s2[TR][TC];
 #pragma unroll
-  for (int i = 0; i < TS; ++i)
+  for (int i = 0; i < TR; ++i)
 #pragma unroll
-    for (int j = 0; j < TS; ++j) {
+    for (int j = 0; j < TC; ++j) {
       s1[i][j] = Ls[(r0 + i) * LD + c0 + j];
       s2[i][j] = (r0 + i == c0 + j) ? one : zero;
     }
   // publish row 0, column 0 and the first pivot's reciprocal
   if (rb == 0)
 #pragma unroll
-    for (int j = 0; j < TS; ++j) {
+    for (int j = 0; j < TC; ++j) {
       p1[0][pidx<T>(c0 + j)] = (c0 + j == 0) ? zero : s1[0][j];
       if (!SYM) p2[0][pidx<T>(c0 + j)] = s2[0][j];
     }
   if (cb == 0)
 #pragma unroll
-    for (int i = 0; i < TS; ++i) lc[0][r0 + i] = s1[i][0];
+    for (int i = 0; i < TR; ++i) lc[0][r0 + i] = s1[i][0];
   if (rb == 0 && cb == 0) {
     T d;
     if (!crecip(s1[0][0], d)) s_zero[0] = 1;
     dv[0] = d;
   }
   __syncthreads();  // the staging buffer is free from here on (L factor)
-  for (int kq = 0; kq < TRI / TS; ++kq) {
+  // steps unrolled by TC: column k is slot kk of column block kq, row k slot kk % TR of row
+  // block k / TR (TR divides TC), so every register index below is known at compile time
+  for (int kq = 0; kq < TRI / TC; ++kq) {
 #pragma unroll
-    for (int kk = 0; kk < TS; ++kk) {
-      const int k = TS * kq + kk, b = kk & 1;
+    for (int kk = 0; kk < TC; ++kk) {
+      const int k = TC * kq + kk, b = kk & 1;
       if (s_zero[b]) {  // uniform
         if (tid == 0) atomicCAS(info, 0, (int)(j0 + s_zero[b]));
         return;
       }
       const T d = dv[b];
-      if (r0 + TS - 1 > k) {  // some row of the tile is below the pivot
-        T l1[TS], l2[TS], q1[TS], q2[TS];
+      if (r0 + TR - 1 > k) {  // some row of the tile is below the pivot
+        T l1[TR], l2[TR], q1[TC], q2[TC];
 #pragma unroll
-        for (int i = 0; i < TS; ++i) {
+        for (int i = 0; i < TR; ++i) {
           l1[i] = cmulx(lc[b][r0 + i], d);
           l2[i] = cmulx(p1[b][pidx<T>(r0 + i)], d);
         }
 #pragma unroll
-        for (int j = 0; j < TS; ++j) {
+        for (int j = 0; j < TC; ++j) {
           q1[j] = p1[b][pidx<T>(c0 + j)];
           q2[j] = p2[b][pidx<T>(c0 + j)];
         }
 #pragma unroll
-        for (int i = 0; i < TS; ++i)
+        for (int i = 0; i < TR; ++i)
           if (r0 + i > k) {
 #pragma unroll
-            for (int j = 0; j < TS; ++j) {
+            for (int j = 0; j < TC; ++j) {
               cfms(s1[i][j], l1[i], q1[j]);
               if (!SYM) cfms(s2[i][j], l2[i], q2[j]);
             }
@@ -574,24 +579,25 @@ __global__ void __launch_bounds__(TRI * TRI / (TS * TS)) k_lu_inv64(T* A, int64_
             }
           }
       }
-      if (!SYM && rb == kq)  // row k of X is final
+      if (!SYM && rb == k / TR)  // row k of X is final
 #pragma unroll
-        for (int j = 0; j < TS; ++j) s2[kk][j] = cmulx(s2[kk][j], d);
+        for (int j = 0; j < TC; ++j) s2[kk % TR][j] = cmulx(s2[kk % TR][j], d);
       // publish step k + 1
       if (k + 1 < TRI) {
-        const int kn = k + 1, bn = b ^ 1, qn = kn / TS, in = kn % TS;
-        if (rb == qn)
+        const int kn = k + 1, bn = b ^ 1;
+        const int qr = kn / TR, ir = (kk + 1) % TR, qc = kn / TC, ic = (kk + 1) % TC;
+        if (rb == qr)
 #pragma unroll
-          for (int j = 0; j < TS; ++j) {
-            p1[bn][pidx<T>(c0 + j)] = (c0 + j == kn) ? zero : s1[in][j];
-            if (!SYM) p2[bn][pidx<T>(c0 + j)] = s2[in][j];
+          for (int j = 0; j < TC; ++j) {
+            p1[bn][pidx<T>(c0 + j)] = (c0 + j == kn) ? zero : s1[ir][j];
+            if (!SYM) p2[bn][pidx<T>(c0 + j)] = s2[ir][j];
           }
-        if (cb == qn)
+        if (cb == qc)
 #pragma unroll
-          for (int i = 0; i < TS; ++i) lc[bn][r0 + i] = s1[i][in];
-        if (rb == qn && cb == qn) {
+          for (int i = 0; i < TR; ++i) lc[bn][r0 + i] = s1[i][ic];
+        if (rb == qr && cb == qc) {
           T dn;
-          if (!crecip(s1[in][in], dn)) s_zero[bn] = kn + 1;
+          if (!crecip(s1[ir][ic], dn)) s_zero[bn] = kn + 1;
           dv[bn] = dn;
         }
       }
@@ -600,9 +606,9 @@ __global__ void __launch_bounds__(TRI * TRI / (TS * TS)) k_lu_inv64(T* A, int64_
   }
   // U (upper part of S1) joins the L factor in Ls; the factored block goes back to A
 #pragma unroll
-  for (int i = 0; i < TS; ++i)
+  for (int i = 0; i < TR; ++i)
 #pragma unroll
-    for (int j = 0; j < TS; ++j)
+    for (int j = 0; j < TC; ++j)
       if (c0 + j >= r0 + i) Ls[(r0 + i) * LD + c0 + j] = s1[i][j];
   __syncthreads();
   for (int e = tid; e < kb * kb; e += NT) {
@@ -615,28 +621,30 @@ __global__ void __launch_bounds__(TRI * TRI / (TS * TS)) k_lu_inv64(T* A, int64_
   // symmetric: X[r][c] = Linv[r][c] / d_r
   if (SYM) {
     __shared__ T s_dinv[TRI];
-    if (rb == cb)
 #pragma unroll
-      for (int i = 0; i < TS; ++i) {
-        T di;
-        crecip(s1[i][i], di);  // nonzero: the elimination checked every pivot
-        s_dinv[r0 + i] = di;
-      }
+    for (int i = 0; i < TR; ++i)
+#pragma unroll
+      for (int j = 0; j < TC; ++j)
+        if (c0 + j == r0 + i) {  // the tile holding the pivot of row r0 + i
+          T di;
+          crecip(s1[i][j], di);  // nonzero: the elimination checked every pivot
+          s_dinv[r0 + i] = di;
+        }
     __syncthreads();
 #pragma unroll
-    for (int i = 0; i < TS; ++i) {
+    for (int i = 0; i < TR; ++i) {
       const T di = s_dinv[r0 + i];
 #pragma unroll
-      for (int j = 0; j < TS; ++j) {
+      for (int j = 0; j < TC; ++j) {
         const int r = r0 + i, c = c0 + j;
         s2[i][j] = c < r ? cmulx(s1[i][j], di) : (c == r ? di : zero);
       }
     }
   }
 #pragma unroll
-  for (int i = 0; i < TS; ++i)
+  for (int i = 0; i < TR; ++i)
 #pragma unroll
-    for (int j = 0; j < TS; ++j) {
+    for (int j = 0; j < TC; ++j) {
       const int r = r0 + i, c = c0 + j;
       Ls[r * LD + c] = c < r ? s1[i][j] : (c == r ? one : zero);
       inv[TRI * TRI + r * TRI + c] = s2[i][j];
@@ -2009,10 +2017,13 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, false, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
   BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, true, 2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
-  // the diagonal-block elimination with 2 x 2 tiles on 1024 threads (default) or 4 x 4 tiles on
-  // 256 (BEAST_LU_DIAG_TILE=4): the same arithmetic per element, different thread counts
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, false, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
+  BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_lu_inv64<T, true, 2, 4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)getrf_sm));
+  // the diagonal-block elimination with 2 x 2 tiles on 1024 threads (default), 2 x 4 tiles on 512
+  // (BEAST_LU_DIAG_TILE=24) or 4 x 4 tiles on 256 (BEAST_LU_DIAG_TILE=4): the same arithmetic
+  // per element, different thread counts
   const char* dt_env = getenv("BEAST_LU_DIAG_TILE");
-  const bool diag2 = !(dt_env && dt_env[0] == '4');
+  const int dtile = dt_env && dt_env[0] == '4' ? 44 : (dt_env && dt_env[0] == '2' && dt_env[1] == '4' ? 24 : 22);
   if (apply_path)
     BEAST_CUDA_TRY(ctx, cudaFuncSetAttribute(k_panel_apply<64>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)panel_apply_smem()));
@@ -2038,12 +2049,16 @@ int lu_factor_t(beast_ctx* ctx, int64_t n, T* A, int64_t lda, int* ipiv, int* in
   unsigned int* bar = reinterpret_cast<unsigned int*>(rowj + 2 * nb);
   int* dinfo = reinterpret_cast<int*>(bar + 4);
   auto diag = [&](bool sy, int64_t jd, int kd, T* out_inv, cudaStream_t s_) {
-    if (sy && diag2)
+    if (dtile == 22 && sy)
       k_lu_inv64<T, true, 2><<<1, TRI * TRI / 4, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, out_inv);
+    else if (dtile == 22)
+      k_lu_inv64<T, false, 2><<<1, TRI * TRI / 4, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, out_inv);
+    else if (dtile == 24 && sy)
+      k_lu_inv64<T, true, 2, 4><<<1, TRI * TRI / 8, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, out_inv);
+    else if (dtile == 24)
+      k_lu_inv64<T, false, 2, 4><<<1, TRI * TRI / 8, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, out_inv);
     else if (sy)
       k_lu_inv64<T, true><<<1, 256, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, out_inv);
-    else if (diag2)
-      k_lu_inv64<T, false, 2><<<1, TRI * TRI / 4, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, out_inv);
     else
       k_lu_inv64<T, false><<<1, 256, getrf_sm, s_>>>(A, lda, jd, kd, dinfo, out_inv);
   };

@@ -202,9 +202,10 @@ def test_mixed_symmetric_path(n):
 
 @pytest.mark.parametrize("symmetric", [True, False])
 def test_diagonal_block_tile_sizes_agree(symmetric, monkeypatch):
-    """the diagonal-block elimination on 1024 threads with 2 x 2 tiles (default) and on 256
-    threads with 4 x 4 tiles (BEAST_LU_DIAG_TILE=4) does the same arithmetic on every element:
-    identical solutions, symmetric and unpivoted factorisations (odd last block, n = 1101)"""
+    """the diagonal-block elimination on 1024 threads with 2 x 2 tiles (default), on 512 threads
+    with 2 x 4 tiles (BEAST_LU_DIAG_TILE=24) and on 256 threads with 4 x 4 tiles
+    (BEAST_LU_DIAG_TILE=4) does the same arithmetic on every element: identical solutions,
+    symmetric and unpivoted factorisations (odd last block, n = 1101)"""
     import torch
     ctx = bg.get_context(0)
     n = 1101
@@ -215,13 +216,14 @@ def test_diagonal_block_tile_sizes_agree(symmetric, monkeypatch):
     b = rng.normal(size=n) + 1j * rng.normal(size=n)
     At = torch.from_numpy(np.ascontiguousarray(A.T)).cuda().T
     out = {}
-    for tile in ("4", "2"):
+    for tile in ("4", "24", "2"):
         monkeypatch.setenv("BEAST_LU_DIAG_TILE", tile)
         x, it, res = bg.solve(At, b, precision=bg.MIXED, tol=1e-12, ctx=ctx)
         assert ctx.last_factor_mode() == (2 if symmetric else 1)
         out[tile] = (x, it, res)
-    assert out["2"][1] == out["4"][1] and out["2"][2] == out["4"][2]
-    assert np.array_equal(out["2"][0], out["4"][0])
+    for tile in ("4", "24"):
+        assert out["2"][1] == out[tile][1] and out["2"][2] == out[tile][2]
+        assert np.array_equal(out["2"][0], out[tile][0])
 
 
 @pytest.mark.parametrize("zero_at", [0, 63])
