@@ -33,13 +33,14 @@
 #include <mutex>
 
 #include "internal.h"
+#include "tc_tiles.h"
 
 namespace {
 
-constexpr int TM = 128, TN = 256, TK = 64;  // tile M (real rows), N, K per stage (halves)
+constexpr int TM = TC_TM, TN = TC_TN, TK = 64;  // tile M (real rows), N, K per stage (halves)
 constexpr int STAGES = 4;
 constexpr int A_BYTES = TM * TK * 2, B_BYTES = TN * TK * 2, STAGE_BYTES = A_BYTES + B_BYTES;
-constexpr int CCH = 32;                           // epilogue chunk: 128 rows x 32 columns of C'
+constexpr int CCH = TC_CCH;                       // epilogue chunk: 128 rows x 32 columns of C'
 constexpr int C_BYTES = TM * CCH * 4;              // 16 KB per chunk buffer
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 2 * C_BYTES + 1024 + 256;
 constexpr long long WAIT_CYCLES = 4000000000LL;  // ~2 s at 2 GHz
@@ -156,24 +157,8 @@ __device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
 // tcgen05.mma into one of two 256-column TMEM accumulators, warps 2..5 drain the other
 // accumulator (tcgen05.ld -> C' -= D) so that the epilogue of tile t overlaps the loads and
 // MMAs of tile t+1.  Barriers: full/empty per stage (TMA <-> MMA), tfull/tempty per
-// accumulator (MMA <-> epilogue).  Tile order: see TcRegion below.
-// The update region is one or two rectangles of C' that share the operands: rectangle r
-// covers the first m_rows[r] rows of A' and the n_cols[r] columns of B' from b_col[r], and
-// writes C' through its own (clipped) tensor map at (c_row0, c_col0[r]).  Tiles of
-// rectangle 0 come first in the tile order; within a rectangle, groups of four row tiles,
-// each whole group column by column.
-// lower = 1 (one square rectangle on the diagonal, symmetric updates): only the tiles that
-// hold an element on or below the diagonal, i.e. column tile n <= m / 4 for row tile m
-// (128 real rows = 64 complex rows against 256 columns); rows come in groups of four with
-// g + 1 tiles each, so tile t of group g = floor((sqrt(2t + 1) - 1) / 2) is found in closed form;
-// a whole group is visited column by column, a partial last group row by row.
-struct TcRegion {
-  int m_rows[2], n_cols[2], b_col[2], c_col0[2];
-  int c_row0;
-  int ntn[2], ntiles0, ntiles;
-  int lower;
-};
-
+// accumulator (MMA <-> epilogue).  The update region, its tiles and their order: TcRegion,
+// tc_tile_at (tc_tiles.h).
 __global__ void __launch_bounds__(192, 1)
     k_tc_gemm(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
               const __grid_constant__ CUtensorMap tmC0, const __grid_constant__ CUtensorMap tmC1,
@@ -197,39 +182,7 @@ __global__ void __launch_bounds__(192, 1)
   const int ntiles = Rg.ntiles;
   const int unit0 = (int)blockIdx.x;  // first tile of this CTA
   const int nunits = (int)gridDim.x;
-  // tile -> (rectangle, first row, first column within the rectangle); false: the tile lies
-  // beyond its rectangle
-  auto tile_at = [&](int tile, int& r, int& m0, int& n0) -> bool {
-    if (Rg.lower) {
-      r = 0;
-      int g = (int)((sqrtf(2.f * (float)tile + 1.f) - 1.f) * 0.5f);
-      while (2 * g * (g + 1) > tile) --g;
-      while (2 * (g + 1) * (g + 2) <= tile) ++g;
-      const int t = tile - 2 * g * (g + 1);
-      if (4 * (g + 1) * TM <= Rg.m_rows[0]) {
-        // a whole group: column by column, so that the CTAs at work share each B' tile four
-        // ways and the group's four A' row tiles across the wave
-        m0 = (4 * g + (t & 3)) * TM;
-        n0 = (t >> 2) * TN;
-      } else {  // the last, partial group row by row (its tiles beyond the count are the rows that do not exist)
-        m0 = (4 * g + t / (g + 1)) * TM;
-        n0 = (t % (g + 1)) * TN;
-      }
-      return m0 < Rg.m_rows[0];
-    }
-    r = tile < Rg.ntiles0 ? 0 : 1;
-    const int lt = r ? tile - Rg.ntiles0 : tile;
-    // groups of four row tiles, a whole group column by column (as the lower-triangle tiles)
-    const int ntn = Rg.ntn[r], G = lt / (4 * ntn), l = lt - G * 4 * ntn;
-    if (4 * (G + 1) * TM <= Rg.m_rows[r]) {
-      m0 = (4 * G + (l & 3)) * TM;
-      n0 = (l >> 2) * TN;
-    } else {
-      m0 = (4 * G + l / ntn) * TM;
-      n0 = (l % ntn) * TN;
-    }
-    return m0 < Rg.m_rows[r];
-  };
+  auto tile_at = [&](int tile, int& r, int& m0, int& n0) -> bool { return tc_tile_at(Rg, tile, r, m0, n0); };
 
   if (threadIdx.x == 0) {
     *s_abort = 0;
@@ -314,7 +267,6 @@ __global__ void __launch_bounds__(192, 1)
     // is rewritten once the reduce issued from it two chunks earlier has read it.
     const int q = warp & 3;
     const bool leader = (warp == 2 && lane == 0);
-    const int nch = TN / CCH;
     // the chunk buffers alternate over this CTA's whole chunk sequence (tiles may end on an odd
     // chunk), so that the buffer being refilled is always the one of two reduces back
     int gc = 0;
@@ -341,7 +293,7 @@ __global__ void __launch_bounds__(192, 1)
       const float rs = m0 + row < m_rows ? -inv_sa[(m0 + row) >> 1] : 0.f;
       // chunks that hold a column of the rectangle (narrow updates leave the rest of the
       // accumulator unread: its reduce-adds would lie wholly outside the tensor map)
-      const int nchv = max(1, min(nch, (n_cols - n0 + CCH - 1) / CCH));
+      const int nchv = tc_tile_chunks(n_cols, n0);
       for (int c = 0; c < nchv; ++c, ++gc) {
         const int b = gc & 1;
         float v[CCH];
@@ -698,20 +650,7 @@ static int tc_gemm_run(beast_ctx* ctx, float2* Mat, int64_t lda, const TcUpdate&
   Rg.n_cols[1] = (int)N1;
   Rg.b_col[1] = (int)N0;
   Rg.c_col0[1] = (int)(colB + N0);
-  int ntl[2];
-  for (int r = 0; r < 2; ++r) {
-    Rg.ntn[r] = std::max(1, (Rg.n_cols[r] + TN - 1) / TN);
-    const int ntm = (Rg.m_rows[r] + TM - 1) / TM;
-    ntl[r] = (Rg.m_rows[r] > 0 && Rg.n_cols[r] > 0) ? Rg.ntn[r] * ntm : 0;
-  }
-  Rg.ntiles0 = ntl[0];
-  Rg.ntiles = ntl[0] + ntl[1];
-  if (Rg.lower) {  // tiles n <= m / 4 of every row tile m
-    const int ntm = (Rg.m_rows[0] + TM - 1) / TM;
-    int64_t cnt = 0;
-    for (int m = 0; m < ntm; ++m) cnt += std::min(m / 4 + 1, Rg.ntn[0]);
-    Rg.ntiles0 = Rg.ntiles = (int)cnt;
-  }
+  tc_region_count(Rg);
   if (Rg.ntiles == 0) return BEAST_OK;
   const int nk = (2 * K) / TK;
   // algorithmic work: 8 K per complex element of the region (the lower triangle: half the square)
