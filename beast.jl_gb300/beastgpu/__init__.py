@@ -5,7 +5,7 @@ mirror of the reference's interface: meshes, spaces, operators, quadrature strat
 `assemble`, `solve`, `gmres` and far-field post-processing.
 """
 from . import lib
-from .lib import FP64, MIXED, MIXED_ACCURATE, C128, C64, BeastError
+from .lib import FP64, MIXED, MIXED_ACCURATE, MIXED_BALANCED, C128, C64, BeastError
 from .mesh import Mesh, readmesh, icosphere, ellipsoid, refines
 from .spaces import raviartthomas, lagrangecxd0, lagrangec0d1, P0, P1, RT
 from .operators import (Maxwell3D, Helmholtz3D, nxdoublelayer, Identity, NCross,

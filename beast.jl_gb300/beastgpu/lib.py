@@ -12,7 +12,7 @@ from . import build as _build
 _LIB = None
 
 OK, ERR_ARG, ERR_OOM, ERR_CUDA, ERR_TIMEOUT, ERR_NOCONV, ERR_SINGULAR, ERR_UNSUPPORTED = range(8)
-FP64, MIXED, MIXED_ACCURATE = 0, 1, 2
+FP64, MIXED, MIXED_ACCURATE, MIXED_BALANCED = 0, 1, 2, 3
 C128, C64 = 0, 1
 HOST, DEVICE = 0, 1
 EXC_TANGTRACE_E, EXC_CROSSTRACE_H, EXC_HH_DIRICHLET = 0, 1, 2

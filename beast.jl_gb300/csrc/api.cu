@@ -499,7 +499,9 @@ static int assemble_device(beast_ctx* ctx, const beast_op_desc* op, const beast_
     if (ev && ev[0] == 'c') entry_layout = false;
   }
   const int64_t ldc = entry_layout ? ts->h_fn_ptr[ts->nfuncs] : (int64_t)nst * ts->ncells;
-  const int zfmt = precision == BEAST_MIXED ? ZCELL_C64 : precision == BEAST_MIXED_ACCURATE ? ZCELL_DF : ZCELL_C128;
+  const int zfmt = precision == BEAST_MIXED                                                  ? ZCELL_C64
+                   : precision == BEAST_MIXED_ACCURATE || precision == BEAST_MIXED_BALANCED ? ZCELL_DF
+                                                                                              : ZCELL_C128;
   const size_t elem = zfmt == ZCELL_C64 ? 8 : 16;
   // rules
   TriRuleDev ro, ri, ron, rin;
@@ -679,7 +681,7 @@ int beast_assemble(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc*
               "TrialRefinesTestQStrat: RT spaces and the test mesh's children (beast_mesh_set_children)");
   else
     ARG_CHECK(ctx, ts->mesh == bs->mesh, "test and trial spaces must share the mesh");
-  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
+  ARG_CHECK(ctx, precision >= BEAST_FP64 && precision <= BEAST_MIXED_BALANCED,
             "unknown precision");
   ARG_CHECK(ctx, z_dtype == BEAST_C128 || z_dtype == BEAST_C64, "unknown matrix dtype");
   ARG_CHECK(ctx, row_off >= 0 && col_off >= 0 && ldz >= row_off + ts->nfuncs, "bad Z addressing");
@@ -1163,9 +1165,9 @@ int beast_solve_dense(beast_ctx* ctx, int64_t n, const void* A, int64_t lda, int
                       int precision, const double* b, double* x, int64_t nrhs, int bx_loc,
                       double tol, int maxiter, int* iters, double* resid) {
   ARG_CHECK(ctx, ctx && A && b && x && n > 0 && lda >= n && nrhs >= 1, "invalid solve arguments");
-  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
+  ARG_CHECK(ctx, precision >= BEAST_FP64 && precision <= BEAST_MIXED_BALANCED,
             "unknown precision");
-  if (precision == BEAST_MIXED_ACCURATE) precision = BEAST_MIXED;  // mixed factorisation
+  if (precision == BEAST_MIXED_ACCURATE || precision == BEAST_MIXED_BALANCED) precision = BEAST_MIXED;  // mixed factorisation
   if (set_device(ctx)) return BEAST_ERR_CUDA;
   if (maxiter <= 0) maxiter = 30;
   if (tol <= 0) tol = 1e-12;
@@ -1325,7 +1327,7 @@ extern "C" {
 int beast_system_create(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs, const beast_space* space,
                         int local_which, double local_re, double local_im, int precision, beast_system** out) {
   ARG_CHECK(ctx, ctx && op && qs && space && out, "null argument");
-  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
+  ARG_CHECK(ctx, precision >= BEAST_FP64 && precision <= BEAST_MIXED_BALANCED,
             "unknown precision");
   ARG_CHECK(ctx, local_which >= -1 && local_which <= 1, "local_which must be -1 (none), 0 (Identity) or 1 (NCross)");
   if (set_device(ctx)) return BEAST_ERR_CUDA;
@@ -1409,7 +1411,7 @@ int beast_batch_create(beast_ctx* ctx, const beast_qs_desc* qs, int64_t njobs, c
                        const beast_op_desc* ops, void* const* Z, int precision, int tile_m, int tile_q, int order,
                        beast_batch** out) {
   ARG_CHECK(ctx, ctx && qs && spaces && ops && Z && out && njobs > 0, "null argument");
-  ARG_CHECK(ctx, precision == BEAST_FP64 || precision == BEAST_MIXED || precision == BEAST_MIXED_ACCURATE,
+  ARG_CHECK(ctx, precision >= BEAST_FP64 && precision <= BEAST_MIXED_BALANCED,
             "unknown precision");
   ARG_CHECK(ctx, order >= 0 && order <= 2, "order must be 0, 1 or 2");
   if (tile_m <= 0) tile_m = 128;

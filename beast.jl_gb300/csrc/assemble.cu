@@ -2219,7 +2219,9 @@ DEV dfl::df df_of(double x) {
 // FAR_QT trial cells staged in shared memory), every operation on FP32 pairs (dfloat.h), the
 // cell-pair blocks stored as double-float pairs (ZCELL_DF).  NO x NI > 0: the rule sizes known
 // at compile time (the default 3 x 4 far rules; efie_far_pair_fast), else the general core.
-template <int NO, int NI>
+// BETA: the balanced core (efie_far_pair_beta: Green's function values and the beta term of
+// the pair in double-float, the alpha terms in FP32; BEAST_MIXED_BALANCED)
+template <int NO, int NI, bool BETA = false>
 __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
   __shared__ FarDfRecord rec[FAR_QT];
   __shared__ float s_tab[64][4];  // sin / cos(m pi/32): lanes read different entries
@@ -2324,7 +2326,9 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
       }
     }
     dfl::cdf z[9];
-    if constexpr (NO > 0)
+    if constexpr (NO > 0 && BETA)
+      dfl::efie_far_pair_beta<NO, NI>(d, tau, r.sig, xi, s_wab, r.eta, r.eta2, kk, alpha, beta, s_tab, z);
+    else if constexpr (NO > 0)
       dfl::efie_far_pair_fast<NO, NI>(d, tau, r.sig, xi, s_wab, r.eta, r.eta2, kk, alpha, beta, s_tab, z);
     else
       dfl::efie_far_pair(d, tau, r.sig, no, xi, wo, ni, r.eta, r.w, kk, alpha, beta, z);
@@ -2337,9 +2341,13 @@ __global__ void __launch_bounds__(FAR_THREADS) k_far_efie_df(FarParams P) {
   }
 }
 
-static cudaError_t far_efie_df(const FarParams& P, cudaStream_t st) {
+// balanced: the balanced core for the default rule sizes (3 x 4 points); other rule sizes run
+// the general double-float core in both modes
+static cudaError_t far_efie_df(const FarParams& P, bool balanced, cudaStream_t st) {
   dim3 grid((unsigned)((P.np + FAR_THREADS - 1) / FAR_THREADS), (unsigned)((P.nq + FAR_QT - 1) / FAR_QT));
-  if (P.ro.n == 3 && P.ri.n == 4)
+  if (P.ro.n == 3 && P.ri.n == 4 && balanced)
+    k_far_efie_df<3, 4, true><<<grid, FAR_THREADS, 0, st>>>(P);
+  else if (P.ro.n == 3 && P.ri.n == 4)
     k_far_efie_df<3, 4><<<grid, FAR_THREADS, 0, st>>>(P);
   else
     k_far_efie_df<0, 0><<<grid, FAR_THREADS, 0, st>>>(P);
@@ -2383,12 +2391,15 @@ cudaError_t launch_far(const AsmArgs& a, const TriRuleDev& ro, const TriRuleDev&
   const int kind = a.op.kind;
   if (kind == BEAST_MW_SL || kind == BEAST_MW_DL || kind == BEAST_MW_NXDL) {
     if (tk != BEAST_RT || bk != BEAST_RT) return cudaErrorInvalidValue;
-    if (kind == BEAST_MW_SL && a.precision == BEAST_MIXED_ACCURATE && a.zcell_fmt == ZCELL_DF && P.op.gr == 0.0) {
+    const bool balanced = a.precision == BEAST_MIXED_BALANCED;
+    if (kind == BEAST_MW_SL && (a.precision == BEAST_MIXED_ACCURATE || balanced) && a.zcell_fmt == ZCELL_DF &&
+        P.op.gr == 0.0) {
       // mixed-accurate EFIE assemblies (real wavenumber): far pairs in double-float arithmetic
       // on the FP32 pipes (about 1e-12 relative to the FP64 values, at a fraction of the FP64
-      // kernel's time on GB300); BEAST_FAR_DF=0 selects the FP64 kernel instead
+      // kernel's time on GB300); BEAST_FAR_DF=0 selects the FP64 kernel instead.  Balanced:
+      // the alpha terms in FP32 (about 1e-7 of a block's largest entry)
       const char* e = getenv("BEAST_FAR_DF");
-      if (!(e && e[0] == '0')) return far_efie_df(P, st);
+      if (!(e && e[0] == '0')) return far_efie_df(P, balanced, st);
     }
     if (kind == BEAST_MW_SL) return far_prec<BEAST_MW_SL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_fmt, st);
     if (kind == BEAST_MW_DL) return far_prec<BEAST_MW_DL, BEAST_RT, BEAST_RT>(P, a.precision, a.zcell_fmt, st);

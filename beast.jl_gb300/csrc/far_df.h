@@ -197,4 +197,111 @@ DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3
   }
 }
 
+// The same block for the balanced mode: the Green's-function values in double-float, the beta
+// (divergence) term beta M0 in double-float, the alpha (vector-potential) term in FP32.  An RT
+// entry sums four cell-pair blocks with signs; their beta terms cancel by about (h / R)^2 there
+// (the divergences integrate to zero) and need the double-float values, while their alpha
+// terms do not cancel, so FP32 moments and an FP32 finish (relative error ~1e-7 of the alpha
+// term) cost the entry about what rounding it to FP32 would -- at a fraction of the pair sums
+// of efie_far_pair_fast.  Same arguments and point-pair loop.
+struct cf {  // complex FP32 (host and device)
+  float x, y;
+};
+DF_HD float f32(df a) { return add_rn(a.hi, a.lo); }
+DF_HD cf cmulf(cf a, cf b) { return {fmaf(a.x, b.x, -mul_rn(a.y, b.y)), fmaf(a.x, b.y, mul_rn(a.y, b.x))}; }
+template <int NO, int NI>
+DF_HD void efie_far_pair_beta(const df* d, const df (*tau)[3], const df (*sig)[3], const df (*xi)[3],
+                              const df (*wab)[NI], const df (*eta)[3], const df* eta2, df k, cdf alpha, cdf beta,
+                              const float (*tab)[4], cdf* out) {
+  const df z0 = make(0.f);
+  df A[NO];
+  cf U0[NO];  // FP32 sums over b of the terms of test point a
+#if defined(__CUDA_ARCH__)
+#pragma unroll 1
+#endif
+  for (int a = 0; a < NO; ++a) {
+    df dx[3];
+    for (int c = 0; c < 3; ++c) dx[c] = adds(d[c], xi[a][c]);
+    A[a] = dot3u(dx, dx);
+    U0[a] = cf{0.f, 0.f};
+  }
+  cdf M0{z0, z0};  // the beta term's moment, double-float
+  cf M1 = cf{0.f, 0.f}, V2[3];
+  for (int c = 0; c < 3; ++c) V2[c] = cf{0.f, 0.f};
+#if defined(__CUDA_ARCH__)
+#pragma unroll 1
+#endif
+  for (int b = 0; b < NI; ++b) {
+    const df Q = subs(eta2[b], scale(dot3u(d, eta[b]), 2.f));
+    cdf T{z0, z0};
+    cf Tf = cf{0.f, 0.f};
+#if defined(__CUDA_ARCH__)
+#pragma unroll 1
+#endif
+    for (int a = 0; a < NO; ++a) {
+      const df P = dot3u(xi[a], eta[b]);
+      const df R2 = subs(adds(A[a], Q), scale(P, 2.f));
+      const df iR = rsqrt(R2);
+      const df R = mulu(R2, iR);
+      df sn, cs;
+      sincos_tab(mulu(k, R), tab, &sn, &cs);
+      const df amp = mulu(iR, wab[a][b]);
+      const cdf K{mulu(amp, cs), neg(mulu(amp, sn))};
+      cacc(T, K);
+      const float kr = f32(K.re), ki = f32(K.im), p = f32(P);
+      U0[a].x += kr;
+      U0[a].y += ki;
+      Tf.x += kr;
+      Tf.y += ki;
+      M1.x = fmaf(kr, p, M1.x);
+      M1.y = fmaf(ki, p, M1.y);
+    }
+    cacc(M0, cnorm(T));
+    for (int c = 0; c < 3; ++c) {
+      const float e = f32(eta[b][c]);
+      V2[c].x = fmaf(Tf.x, e, V2[c].x);
+      V2[c].y = fmaf(Tf.y, e, V2[c].y);
+    }
+  }
+  M0 = cnorm(M0);
+  cf V1[3];
+  for (int c = 0; c < 3; ++c) V1[c] = cf{0.f, 0.f};
+  for (int a = 0; a < NO; ++a)
+    for (int c = 0; c < 3; ++c) {
+      const float x = f32(xi[a][c]);
+      V1[c].x = fmaf(U0[a].x, x, V1[c].x);
+      V1[c].y = fmaf(U0[a].y, x, V1[c].y);
+    }
+  // alpha term in FP32: a4 (M1 - sig_j.V1 - tau_i.V2 + (tau_i.sig_j) M0)
+  const cf a4 = cf{0.25f * f32(alpha.re), 0.25f * f32(alpha.im)};
+  const cf C = cmulf(a4, M1), D = cmulf(a4, cf{f32(M0.re), f32(M0.im)});
+  float ts[3][3], ss[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int c = 0; c < 3; ++c) {
+      ts[i][c] = f32(tau[i][c]);
+      ss[i][c] = f32(sig[i][c]);
+    }
+  cf S[3], Tm[3];
+  for (int j = 0; j < 3; ++j) {
+    cf sv = cf{0.f, 0.f}, tv = cf{0.f, 0.f};
+    for (int c = 0; c < 3; ++c) {
+      sv.x = fmaf(ss[j][c], V1[c].x, sv.x);
+      sv.y = fmaf(ss[j][c], V1[c].y, sv.y);
+      tv.x = fmaf(ts[j][c], V2[c].x, tv.x);
+      tv.y = fmaf(ts[j][c], V2[c].y, tv.y);
+    }
+    S[j] = cmulf(a4, sv);
+    Tm[j] = cmulf(a4, tv);
+  }
+  // beta term in double-float, once per pair
+  const cdf bM0 = cmulu(beta, M0);
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      const float g = fmaf(ts[i][0], ss[j][0], fmaf(ts[i][1], ss[j][1], ts[i][2] * ss[j][2]));
+      const float zr = C.x - S[j].x - Tm[i].x + g * D.x;
+      const float zi = C.y - S[j].y - Tm[i].y + g * D.y;
+      out[3 * i + j] = cdf{add(bM0.re, zr), add(bM0.im, zi)};
+    }
+}
+
 }  // namespace dfl

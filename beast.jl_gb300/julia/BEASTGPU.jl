@@ -14,8 +14,8 @@ not ask for it:
     u = BEASTGPU.solve(mfie)                                     # `solve(eq)` of @discretise
 
 `assemble` (src/operator.jl:100-116) calls `allocatestorage(op, X, Y, storage_policy)`
-(src/operator.jl:168-183); for the policies `Val{:gpu}` (FP64), `Val{:gpu_mixed_accurate}`
-and `Val{:gpu_mixed}` this returns a `DenseStore` instead of the `store(v,m,n) = (Z[m,n] += v)`
+(src/operator.jl:168-183); for the policies `Val{:gpu}` (FP64), `Val{:gpu_mixed_accurate}`,
+`Val{:gpu_mixed_balanced}` and `Val{:gpu_mixed}` this returns a `DenseStore` instead of the `store(v,m,n) = (Z[m,n] += v)`
 closure.  `assemble!` (src/operator.jl:207-357) then dispatches on the store's type:
 
   * integral operators of the supported kinds on RT / P0 / P1 spaces with a supported
@@ -43,7 +43,7 @@ const MW_SL, MW_DL, MW_NXDL, HH_SL, HH_DL, HH_DLT = 1, 2, 3, 4, 5, 6
 const P0, P1, RT = 0, 1, 2
 const QS_WILTON_SAUTER, QS_SAUTER, QS_DOUBLENUM = 1, 2, 3
 const QS_TEST_REFINES_TRIAL, QS_TRIAL_REFINES_TEST = 4, 5
-const FP64, MIXED, MIXED_ACCURATE = 0, 1, 2
+const FP64, MIXED, MIXED_ACCURATE, MIXED_BALANCED = 0, 1, 2, 3
 const C128, C64 = 0, 1
 const HOST, DEVICE = 0, 1
 
@@ -166,9 +166,11 @@ end
 scaled(s::DenseStore, a) = DenseStore(s.Z, s.row_off, s.col_off, s.coeff * a, s.precision)
 shifted(s::DenseStore, dm, dn) = DenseStore(s.Z, s.row_off + dm, s.col_off + dn, s.coeff, s.precision)
 
-const GPUPolicy = Union{Type{Val{:gpu}}, Type{Val{:gpu_mixed_accurate}}, Type{Val{:gpu_mixed}}}
+const GPUPolicy = Union{Type{Val{:gpu}}, Type{Val{:gpu_mixed_accurate}}, Type{Val{:gpu_mixed_balanced}},
+                        Type{Val{:gpu_mixed}}}
 policy_precision(::Type{Val{:gpu}}) = FP64
 policy_precision(::Type{Val{:gpu_mixed_accurate}}) = MIXED_ACCURATE
+policy_precision(::Type{Val{:gpu_mixed_balanced}}) = MIXED_BALANCED
 policy_precision(::Type{Val{:gpu_mixed}}) = MIXED
 
 function BEAST.allocatestorage(op::BEAST.AbstractOperator, tfs, bfs, policy::GPUPolicy,
@@ -366,7 +368,7 @@ end
 
 `Z \\ b` on the device: FP64 LU (`FP64`), or a complex FP32 factorisation with tensor-core
 updates and FP64 iterative refinement to `tol` against `Z` as given (`MIXED`,
-`MIXED_ACCURATE`: for an FP64 `Z` the FP64 solution to the tolerance).
+`MIXED_ACCURATE`, `MIXED_BALANCED`: for an FP64 `Z` the FP64 solution to the tolerance).
 """
 function solve(Z::Matrix{ComplexF64}, b::Vector{ComplexF64}; precision=MIXED_ACCURATE, tol=1e-10,
                maxiter=30)
@@ -399,7 +401,8 @@ function solve(eq; precision=MIXED_ACCURATE, tol=1e-10)
     X = BEAST._spacedict_to_directproductspace(eq.test_space_dict)
     Y = BEAST._spacedict_to_directproductspace(eq.trial_space_dict)
     b = BEAST.assemble(eq.equation.rhs, X)
-    policy = precision == FP64 ? Val{:gpu} : precision == MIXED ? Val{:gpu_mixed} : Val{:gpu_mixed_accurate}
+    policy = precision == FP64 ? Val{:gpu} : precision == MIXED ? Val{:gpu_mixed} :
+             precision == MIXED_BALANCED ? Val{:gpu_mixed_balanced} : Val{:gpu_mixed_accurate}
     materialize = (a, x, y; kw...) -> BEAST.assemble(a, x, y; storage_policy=policy, kw...)
     Z = BEAST.assemble(eq.equation.lhs, X, Y; materialize)
     u = solve(Matrix{ComplexF64}(Matrix(Z)), Vector{ComplexF64}(Vector(b)); precision, tol)

@@ -79,9 +79,14 @@ enum {
                       (double-float partial sums), other near pairs FP64, c64 storage; solve:
                       FP32 panels with FP16-operand tensor-core trailing updates of a c64
                       copy, FP64 iterative refinement against the c64 matrix                 */
-  BEAST_MIXED_ACCURATE = 2 /* assembly as BEAST_FP64 (c128 matrix); solve as BEAST_MIXED, the
+  BEAST_MIXED_ACCURATE = 2, /* assembly as BEAST_FP64 (c128 matrix); solve as BEAST_MIXED, the
                       refinement residual taken against the c128 matrix, so the solution is
                       the FP64 one to the refinement tolerance                               */
+  BEAST_MIXED_BALANCED = 3 /* as BEAST_MIXED_ACCURATE, but the far pairs of the RT Maxwell
+                      single layer keep double-float arithmetic only where the gather cancels:
+                      the Green's function values and the divergence (beta) term of each cell
+                      pair; the vector-potential (alpha) terms run in FP32 (about 1e-7 of the
+                      largest entry of a block).  Other operators: as BEAST_MIXED_ACCURATE    */
 };
 
 /* ---- element type of a dense matrix / vector argument */
@@ -169,7 +174,7 @@ int beast_space_free(beast_space* space);
  * Z: ldz leading dimension, element type z_dtype (BEAST_C128/C64), location z_loc.
  * accumulate = 0 overwrites the addressed block, 1 adds (linear combinations,
  * src/operator.jl:294-304).  precision: BEAST_FP64 or BEAST_MIXED (BEAST_MIXED_ACCURATE
- * assembles as BEAST_FP64).  Singularity-extraction pairs (DoubleNumWiltonSauterQStrat) are
+ * assembles as BEAST_FP64, BEAST_MIXED_BALANCED as described at its enum).  Singularity-extraction pairs (DoubleNumWiltonSauterQStrat) are
  * available for the Maxwell operators on RT and the Helmholtz single, double and transposed
  * double layers on any P0 / P1 combination. */
 int beast_assemble(beast_ctx* ctx, const beast_op_desc* op, const beast_qs_desc* qs,
@@ -229,7 +234,7 @@ int beast_lu_free(beast_lu* lu);
 int beast_lu_solve_noalloc(beast_ctx* ctx, const beast_lu* lu, int64_t nrhs, void* B, int64_t ldb);
 
 /* x = A \ b for a device matrix A (c128 or c64).  precision BEAST_FP64: FP64 LU;
- * BEAST_MIXED (or BEAST_MIXED_ACCURATE, the same here): FP32 LU of a c64 copy + FP64
+ * BEAST_MIXED (or BEAST_MIXED_ACCURATE / BALANCED, the same here): FP32 LU of a c64 copy + FP64
  * iterative refinement to `tol` relative residual (residual matvec and update in FP64,
  * against A as stored: c128 for the FP64 solution to the tolerance).
  * b, x: complex FP64 [n x nrhs], location bx_loc.  iters/resid (may be NULL) report the
@@ -285,7 +290,7 @@ int beast_batch_free(beast_batch* batch);
  * assembly and factorisation; src/solvers/lusolver.jl:9-39 assembles and factors per call).
  * beast_system_create assembles op (+ local_coeff * Identity / NCross when local_which is 0 /
  * 1; -1: none) on space x space in `precision` and factors it (the mixed factorisation for
- * BEAST_MIXED / BEAST_MIXED_ACCURATE, FP64 LU for BEAST_FP64).  beast_system_solve builds nrhs
+ * BEAST_MIXED / BEAST_MIXED_ACCURATE / BEAST_MIXED_BALANCED, FP64 LU for BEAST_FP64).  beast_system_solve builds nrhs
  * plane-wave excitations (dirs, pols: [nrhs][3]; same gamma) and solves them against the
  * kept factors (FP64 refinement to `tol` on the mixed paths); x: complex FP64 [nrhs][nfuncs],
  * location x_loc.  beast_system_bytes: device memory the system holds (matrix, factors,

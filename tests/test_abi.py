@@ -33,11 +33,12 @@ def test_precision_constants_match_header():
     """the precision enum of the C header, the Python constants and the Julia shim agree"""
     import beastgpu as bg
     hdr = open(os.path.join(ROOT, "include", "beastgpu.h")).read()
-    enum = {m.group(1): int(m.group(2)) for m in re.finditer(r"BEAST_(FP64|MIXED|MIXED_ACCURATE)\s*=\s*(\d+)", hdr)}
-    assert enum == {"FP64": 0, "MIXED": 1, "MIXED_ACCURATE": 2}
-    assert (bg.FP64, bg.MIXED, bg.MIXED_ACCURATE) == (0, 1, 2)
+    enum = {m.group(1): int(m.group(2))
+            for m in re.finditer(r"BEAST_(FP64|MIXED|MIXED_ACCURATE|MIXED_BALANCED)\s*=\s*(\d+)", hdr)}
+    assert enum == {"FP64": 0, "MIXED": 1, "MIXED_ACCURATE": 2, "MIXED_BALANCED": 3}
+    assert (bg.FP64, bg.MIXED, bg.MIXED_ACCURATE, bg.MIXED_BALANCED) == (0, 1, 2, 3)
     jl = open(os.path.join(ROOT, "beast.jl_gb300", "julia", "BEASTGPU.jl")).read()
-    assert "const FP64, MIXED, MIXED_ACCURATE = 0, 1, 2" in jl
+    assert "const FP64, MIXED, MIXED_ACCURATE, MIXED_BALANCED = 0, 1, 2, 3" in jl
 
 
 def _split_top(s):

@@ -146,6 +146,26 @@ def test_mixed_accurate_assembly_into_c64(ctx):
     assert np.array_equal(Z64, Z128.astype(np.complex64))
 
 
+def test_mixed_balanced_assembly(ctx):
+    """the balanced EFIE assembly: the far pairs' vector-potential (alpha) terms in FP32, about
+    1e-7 of a far block's largest entry, everything else as mixed-accurate; with alpha = 0 the
+    far blocks are their double-float divergence (beta) terms alone and the matrix is the
+    mixed-accurate one to double-float accuracy"""
+    X = bg.raviartthomas(bg.icosphere(2))
+    op = bg.Maxwell3D.singlelayer(wavenumber=3.0)
+    Z = bg.assemble(op, X, X, precision=bg.MIXED_BALANCED, ctx=ctx)
+    assert Z.dtype == np.complex128
+    Zo = O.assemble(_orc_op(op), _orc_qs(bg.defaultquadstrat(op, X, X)), X, X)
+    assert rel_fro(Z, Zo) < 1e-6, rel_fro(Z, Zo)
+    Za = bg.assemble(op, X, X, precision=bg.MIXED_ACCURATE, ctx=ctx)
+    assert 1e-12 < rel_fro(Z, Za) < 1e-6  # the balanced core ran, and stays in its error class
+    g = 3.0j
+    opb = bg.Maxwell3D.singlelayer(gamma=g, alpha=0.0, beta=-1.0 / g)
+    Zb = bg.assemble(opb, X, X, precision=bg.MIXED_BALANCED, ctx=ctx)
+    Zab = bg.assemble(opb, X, X, precision=bg.MIXED_ACCURATE, ctx=ctx)
+    assert rel_fro(Zb, Zab) < 1e-11, rel_fro(Zb, Zab)
+
+
 @pytest.mark.parametrize("which", ["singlelayer", "doublelayer"])
 def test_mixed_accurate_near_pairs(ctx, which):
     """the double-float Sauter-Schwab pairs (face, edge and vertex classes) of the RT Maxwell
