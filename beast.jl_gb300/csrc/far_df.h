@@ -199,11 +199,11 @@ DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3
 
 // The same block for the balanced mode: the Green's-function values in double-float, the beta
 // (divergence) term beta M0 in double-float, the alpha (vector-potential) term in FP32.  An RT
-// entry sums four cell-pair blocks with signs; their beta terms cancel by about (h / R)^2 there
-// (the divergences integrate to zero) and need the double-float values, while their alpha
-// terms do not cancel, so FP32 moments and an FP32 finish (relative error ~1e-7 of the alpha
-// term) cost the entry about what rounding it to FP32 would -- at a fraction of the pair sums
-// of efie_far_pair_fast.  Same arguments and point-pair loop.
+// entry sums four cell-pair blocks with signs; their beta terms cancel there to a second
+// difference of the Green's function (the divergences integrate to zero) and need the
+// double-float values, while their alpha terms do not cancel, so FP32 moments and an FP32
+// finish (relative error ~1e-7 of the alpha term) cost the entry about what rounding it to
+// FP32 would -- at a fraction of the pair sums of efie_far_pair_fast.  Same arguments.
 struct cf {  // complex FP32 (host and device)
   float x, y;
 };
@@ -213,65 +213,57 @@ template <int NO, int NI>
 DF_HD void efie_far_pair_beta(const df* d, const df (*tau)[3], const df (*sig)[3], const df (*xi)[3],
                               const df (*wab)[NI], const df (*eta)[3], const df* eta2, df k, cdf alpha, cdf beta,
                               const float (*tab)[4], cdf* out) {
+  // Test points outside, trial points inside: every per-test-point value (x_a - c_q, its square,
+  // the U0 sum) lives in registers for one pass of the inner loop, and the trial points come
+  // from the caller's shared-memory record, so nothing is indexed by a rolled loop's counter in
+  // thread-local arrays.  R^2 = |d + xi_a|^2 + |eta_b|^2 - 2 (d + xi_a).eta_b.
   const df z0 = make(0.f);
-  df A[NO];
-  cf U0[NO];  // FP32 sums over b of the terms of test point a
+  cdf M0{z0, z0};  // the beta term's moment, double-float running sum over all point pairs
+  cf M1 = cf{0.f, 0.f}, V1[3], V2[3];
+  for (int c = 0; c < 3; ++c) V1[c] = V2[c] = cf{0.f, 0.f};
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
   for (int a = 0; a < NO; ++a) {
     df dx[3];
-    for (int c = 0; c < 3; ++c) dx[c] = adds(d[c], xi[a][c]);
-    A[a] = dot3u(dx, dx);
-    U0[a] = cf{0.f, 0.f};
-  }
-  cdf M0{z0, z0};  // the beta term's moment, double-float
-  cf M1 = cf{0.f, 0.f}, V2[3];
-  for (int c = 0; c < 3; ++c) V2[c] = cf{0.f, 0.f};
+    float xf[3];
+    for (int c = 0; c < 3; ++c) {
+      dx[c] = adds(d[c], xi[a][c]);
+      xf[c] = f32(xi[a][c]);
+    }
+    const df A = dot3u(dx, dx);
+    cf U0 = cf{0.f, 0.f};  // FP32 sum over b of the terms of test point a
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
-  for (int b = 0; b < NI; ++b) {
-    const df Q = subs(eta2[b], scale(dot3u(d, eta[b]), 2.f));
-    cdf T{z0, z0};
-    cf Tf = cf{0.f, 0.f};
-#if defined(__CUDA_ARCH__)
-#pragma unroll 1
-#endif
-    for (int a = 0; a < NO; ++a) {
-      const df P = dot3u(xi[a], eta[b]);
-      const df R2 = subs(adds(A[a], Q), scale(P, 2.f));
+    for (int b = 0; b < NI; ++b) {
+      const df R2 = subs(adds(A, eta2[b]), scale(dot3u(dx, eta[b]), 2.f));
       const df iR = rsqrt(R2);
       const df R = mulu(R2, iR);
       df sn, cs;
       sincos_tab(mulu(k, R), tab, &sn, &cs);
       const df amp = mulu(iR, wab[a][b]);
       const cdf K{mulu(amp, cs), neg(mulu(amp, sn))};
-      cacc(T, K);
-      const float kr = f32(K.re), ki = f32(K.im), p = f32(P);
-      U0[a].x += kr;
-      U0[a].y += ki;
-      Tf.x += kr;
-      Tf.y += ki;
+      cacc(M0, K);
+      const float kr = f32(K.re), ki = f32(K.im);
+      float ef[3];
+      for (int c = 0; c < 3; ++c) ef[c] = f32(eta[b][c]);
+      const float p = fmaf(xf[0], ef[0], fmaf(xf[1], ef[1], xf[2] * ef[2]));
+      U0.x += kr;
+      U0.y += ki;
       M1.x = fmaf(kr, p, M1.x);
       M1.y = fmaf(ki, p, M1.y);
+      for (int c = 0; c < 3; ++c) {
+        V2[c].x = fmaf(kr, ef[c], V2[c].x);
+        V2[c].y = fmaf(ki, ef[c], V2[c].y);
+      }
     }
-    cacc(M0, cnorm(T));
     for (int c = 0; c < 3; ++c) {
-      const float e = f32(eta[b][c]);
-      V2[c].x = fmaf(Tf.x, e, V2[c].x);
-      V2[c].y = fmaf(Tf.y, e, V2[c].y);
+      V1[c].x = fmaf(U0.x, xf[c], V1[c].x);
+      V1[c].y = fmaf(U0.y, xf[c], V1[c].y);
     }
   }
   M0 = cnorm(M0);
-  cf V1[3];
-  for (int c = 0; c < 3; ++c) V1[c] = cf{0.f, 0.f};
-  for (int a = 0; a < NO; ++a)
-    for (int c = 0; c < 3; ++c) {
-      const float x = f32(xi[a][c]);
-      V1[c].x = fmaf(U0[a].x, x, V1[c].x);
-      V1[c].y = fmaf(U0[a].y, x, V1[c].y);
-    }
   // alpha term in FP32: a4 (M1 - sig_j.V1 - tau_i.V2 + (tau_i.sig_j) M0)
   const cf a4 = cf{0.25f * f32(alpha.re), 0.25f * f32(alpha.im)};
   const cf C = cmulf(a4, M1), D = cmulf(a4, cf{f32(M0.re), f32(M0.im)});
