@@ -83,6 +83,14 @@ DF_HD df adds(df a, df b) {
   return fast_two_sum(s.hi, add_rn(s.lo, add_rn(a.lo, b.lo)));
 }
 DF_HD df subs(df a, df b) { return adds(a, neg(b)); }
+// the pair sum left unnormalised (the low part collects the TwoSum error and both low parts,
+// a few ulp of the larger high part at most): for a sum whose consumer is a pair product, a
+// running sum or another such sum, which add the low parts in anyway
+DF_HD df addu(df a, df b) {
+  const df s = two_sum(a.hi, b.hi);
+  return {s.hi, add_rn(s.lo, add_rn(a.lo, b.lo))};
+}
+DF_HD df subu(df a, df b) { return addu(a, neg(b)); }
 DF_HD df mul(df a, df b) {
   const df p = two_prod(a.hi, b.hi);
   return fast_two_sum(p.hi, fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, p.lo)));
@@ -165,6 +173,8 @@ DF_HD void sincos(df th, df* s, df* c) {
 // n C0 lie within a factor 2 of each other, or n = 0), the small rest (th.lo, the low parts
 // of n pi/32) is summed in FP32, and the sums with one dominant term (t + its cubic term,
 // 1 - t^2/2) are fast two-sums.  Absolute error below 1e-11 for |th| < 2^10.
+// NORM = false: the angle sum left unnormalised (addu) for consumers that take pair products
+template <bool NORM = true>
 DF_HD void sincos_tab(df th, const float (*tab)[4], df* s, df* c) {
   const float n = rintf(mul_rn(th.hi, DF_32_OVER_PI));
   const df p0 = two_prod(n, DF_PI32_0);
@@ -182,8 +192,13 @@ DF_HD void sincos_tab(df th, const float (*tab)[4], df* s, df* c) {
   const df c1 = fast_two_sum(1.f, -h.hi);
   const df ct = fast_two_sum(c1.hi, add_rn(c1.lo, sub_rn(r4, h.lo)));
   const df sm = {tab[m][0], tab[m][1]}, cm = {tab[m][2], tab[m][3]};
-  *s = adds(mulu(sm, ct), mulu(cm, st));
-  *c = subs(mulu(cm, ct), mulu(sm, st));
+  if (NORM) {
+    *s = adds(mulu(sm, ct), mulu(cm, st));
+    *c = subs(mulu(cm, ct), mulu(sm, st));
+  } else {
+    *s = addu(mulu(sm, ct), mulu(cm, st));
+    *c = subu(mulu(cm, ct), mulu(sm, st));
+  }
 }
 
 // a += x for a running sum whose low part is normalised only at the end (norm): one TwoSum

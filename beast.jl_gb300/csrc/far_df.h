@@ -237,11 +237,18 @@ DF_HD void efie_far_pair_beta(const df* d, const df (*tau)[3], const df (*sig)[3
 #pragma unroll 1
 #endif
     for (int b = 0; b < NI; ++b) {
-      const df R2 = subs(adds(A, eta2[b]), scale(dot3u(dx, eta[b]), 2.f));
+      // R^2 and the sine / cosine as unnormalised pair sums: their consumers are the
+      // reciprocal square root's pair product and the pair products of K
+      df Pd = mulu(dx[0], eta[b][0]);
+      acc(Pd, mulu(dx[1], eta[b][1]));
+      acc(Pd, mulu(dx[2], eta[b][2]));
+      df R2 = A;
+      acc(R2, eta2[b]);
+      acc(R2, scale(Pd, -2.f));
       const df iR = rsqrt(R2);
       const df R = mulu(R2, iR);
       df sn, cs;
-      sincos_tab(mulu(k, R), tab, &sn, &cs);
+      sincos_tab<false>(mulu(k, R), tab, &sn, &cs);
       const df amp = mulu(iR, wab[a][b]);
       const cdf K{mulu(amp, cs), neg(mulu(amp, sn))};
       cacc(M0, K);
