@@ -135,6 +135,19 @@ DF_HD df rsqrt(df a) {
   const float e = add_rn(sub_rn(1.f, ay2.hi), -ay2.lo);  // 1 - a y0^2, about 2^-22
   return fast_two_sum(y0, mul_rn(mul_rn(y0, e), 0.5f));
 }
+// the same left unnormalised: the correction y0 (1 - a y0^2) / 2 is at most about 2 ulp of y0,
+// for consumers that take pair products
+DF_HD df rsqrtu(df a) {
+#if defined(__CUDA_ARCH__)
+  const float y0 = rsqrtf(a.hi);
+#else
+  const float y0 = 1.f / sqrtf(a.hi);
+#endif
+  const df y2 = two_prod(y0, y0);
+  const df ay2 = mulu(a, y2);
+  const float e = add_rn(sub_rn(1.f, ay2.hi), -ay2.lo);
+  return {y0, mul_rn(mul_rn(y0, e), 0.5f)};
+}
 // 1 / a: one Newton correction of the FP32 reciprocal
 DF_HD df rcp(df a) {
   const float r = 1.f / a.hi;
@@ -190,7 +203,9 @@ DF_HD void sincos_tab(df th, const float (*tab)[4], df* s, df* c) {
   const float r4 = mul_rn(mul_rn(t2, t2), fmaf(t2, -1.f / 720.f, 1.f / 24.f));
   const df h = scale(mulu(t, t), 0.5f);  // t^2 / 2 < 1.2e-3
   const df c1 = fast_two_sum(1.f, -h.hi);
-  const df ct = fast_two_sum(c1.hi, add_rn(c1.lo, sub_rn(r4, h.lo)));
+  // unnormalised: the low part (c1's, the quartic term and h's low part) is a few ulp of 1
+  const df ct = NORM ? fast_two_sum(c1.hi, add_rn(c1.lo, sub_rn(r4, h.lo)))
+                     : df{c1.hi, add_rn(c1.lo, sub_rn(r4, h.lo))};
   const df sm = {tab[m][0], tab[m][1]}, cm = {tab[m][2], tab[m][3]};
   if (NORM) {
     *s = adds(mulu(sm, ct), mulu(cm, st));

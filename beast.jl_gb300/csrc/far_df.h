@@ -237,15 +237,15 @@ DF_HD void efie_far_pair_beta(const df* d, const df (*tau)[3], const df (*sig)[3
 #pragma unroll 1
 #endif
     for (int b = 0; b < NI; ++b) {
-      // R^2 and the sine / cosine as unnormalised pair sums: their consumers are the
-      // reciprocal square root's pair product and the pair products of K
+      // R^2, 1 / R and the sine / cosine left unnormalised: their consumers are pair
+      // products (the reciprocal square root's, R, k R, the amplitude and K)
       df Pd = mulu(dx[0], eta[b][0]);
       acc(Pd, mulu(dx[1], eta[b][1]));
       acc(Pd, mulu(dx[2], eta[b][2]));
       df R2 = A;
       acc(R2, eta2[b]);
       acc(R2, scale(Pd, -2.f));
-      const df iR = rsqrt(R2);
+      const df iR = rsqrtu(R2);
       const df R = mulu(R2, iR);
       df sn, cs;
       sincos_tab<false>(mulu(k, R), tab, &sn, &cs);
