@@ -23,3 +23,21 @@ def test_reference_arm_json_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["value"] == d["value"]
     assert d["e2e"] == {"value": d["value"], "unit": "solves/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+
+
+def test_bench_precisions_are_the_library_constants():
+    """bench.py's --precision names map to the C header's precision enum, and the default is the
+    balanced mode (the fastest mode within the 1e-6 surface-current contract at C2)"""
+    import importlib.util
+    from beastgpu import lib as L
+    spec = importlib.util.spec_from_file_location("bench_mod", os.path.join(ROOT, "bench.py"))
+    bench = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(bench)
+    assert bench.PRECISIONS == {"mixed": L.MIXED, "mixed-accurate": L.MIXED_ACCURATE,
+                                "mixed-balanced": L.MIXED_BALANCED, "fp64": L.FP64}
+    sys_argv = sys.argv
+    try:
+        sys.argv = ["bench.py"]
+        assert bench.parse().precision == "mixed-balanced"
+    finally:
+        sys.argv = sys_argv
