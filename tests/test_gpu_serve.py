@@ -30,8 +30,14 @@ def _jobs():
     return out
 
 
-def test_each_result_is_the_same_alone_and_in_the_mix():
+@pytest.mark.parametrize("precision", [None, bg.MIXED_BALANCED])
+def test_each_result_is_the_same_alone_and_in_the_mix(precision):
+    """the default (mixed) requests, and the same requests in the balanced mode (double-float
+    Green's function values and divergence terms, c128 matrices in the footprint)"""
     jobs = _jobs()
+    if precision is not None:
+        for j in jobs:
+            j["precision"] = precision
     with bg.Server(slots=1, hbm_budget=16 << 30) as s:
         alone = [s.submit(j).result(timeout=600) for j in jobs]
     with bg.Server(slots=3, hbm_budget=16 << 30) as s:
