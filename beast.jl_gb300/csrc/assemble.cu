@@ -2221,9 +2221,9 @@ DEV dfl::df df_of(double x) {
 // at compile time (the default 3 x 4 far rules; efie_far_pair_fast), else the general core.
 // BETA: the balanced core (efie_far_pair_beta: Green's function values and the beta term of
 // the pair in double-float, the alpha terms in FP32; BEAST_MIXED_BALANCED)
-// (five CTAs per SM for the balanced core: 96 registers, no spills)
+// (five CTAs per SM for the cores of the default rule sizes: 96 registers, no spills)
 template <int NO, int NI, bool BETA = false>
-__global__ void __launch_bounds__(FAR_THREADS, BETA ? 5 : 1) k_far_efie_df(FarParams P) {
+__global__ void __launch_bounds__(FAR_THREADS, NO > 0 ? 5 : 1) k_far_efie_df(FarParams P) {
   __shared__ FarDfRecord rec[FAR_QT];
   __shared__ float s_tab[64][4];  // sin / cos(m pi/32): lanes read different entries
   __shared__ int s_zc[FAR_QT][3];

@@ -141,18 +141,27 @@ DF_HD void efie_far_pair_fast(const df* d, const df (*tau)[3], const df (*sig)[3
 #pragma unroll 1
 #endif
   for (int b = 0; b < NI; ++b) {
-    const df Q = subs(eta2[b], scale(dot3u(d, eta[b]), 2.f));
+    // Q, P, R^2, 1 / R and the sine / cosine left unnormalised: their consumers are running
+    // sums and pair products (the reciprocal square root's, R, k R, the amplitude, K, K P)
+    df Q = mulu(d[0], eta[b][0]);
+    acc(Q, mulu(d[1], eta[b][1]));
+    acc(Q, mulu(d[2], eta[b][2]));
+    Q = addu(eta2[b], scale(Q, -2.f));
     cdf T{z0, z0};
 #if defined(__CUDA_ARCH__)
 #pragma unroll 1
 #endif
     for (int a = 0; a < NO; ++a) {
-      const df P = dot3u(xi[a], eta[b]);
-      const df R2 = subs(adds(A[a], Q), scale(P, 2.f));
-      const df iR = rsqrt(R2);
+      df P = mulu(xi[a][0], eta[b][0]);
+      acc(P, mulu(xi[a][1], eta[b][1]));
+      acc(P, mulu(xi[a][2], eta[b][2]));
+      df R2 = A[a];
+      acc(R2, Q);
+      acc(R2, scale(P, -2.f));
+      const df iR = rsqrtu(R2);
       const df R = mulu(R2, iR);
       df sn, cs;
-      sincos_tab(mulu(k, R), tab, &sn, &cs);
+      sincos_tab<false>(mulu(k, R), tab, &sn, &cs);
       const df amp = mulu(iR, wab[a][b]);  // w_a w_b / (4 pi R)
       const cdf K{mulu(amp, cs), neg(mulu(amp, sn))};
       cacc(U0[a], K);
