@@ -39,6 +39,16 @@ void t_sincos(const double* th, int64_t n, double* s, double* c) {
 void t_sincos_tab(const double* th, int64_t n, double* s, double* c) {
   for (int64_t i = 0; i < n; ++i) { df a, b; sincos_tab(from(th[i]), sincos_tab_host, &a, &b); s[i] = to(a); c[i] = to(b); }
 }
+// the unnormalised forms the far cores use where pair products consume the result
+void t_unnorm(const double* th, const double* a, const double* b, int64_t n, double* out) {
+  for (int64_t i = 0; i < n; ++i) {
+    df s, c;
+    sincos_tab<false>(from(th[i]), sincos_tab_host, &s, &c);
+    const double aa = a[i] < 0 ? -a[i] : a[i];
+    out[5 * i] = to(s); out[5 * i + 1] = to(c); out[5 * i + 2] = to(rsqrtu(from(aa)));
+    out[5 * i + 3] = to(addu(from(a[i]), from(b[i]))); out[5 * i + 4] = to(subu(from(a[i]), from(b[i])));
+  }
+}
 void t_green(const double* R, const double* k, int64_t n, double* out) {
   for (int64_t i = 0; i < n; ++i) { df re, im; green(from(R[i]), from(k[i]), &re, &im); out[2 * i] = to(re); out[2 * i + 1] = to(im); }
 }
@@ -100,7 +110,7 @@ def lib(tmp_path_factory):
     subprocess.run(["g++", "-O2", "-ffp-contract=off", "-fPIC", "-shared", "-I", CSRC, str(src), "-o", str(so)],
                    check=True)
     L = C.CDLL(str(so))
-    for f in ("t_two", "t_ops", "t_sincos", "t_sincos_tab", "t_green", "t_efie_pair"):
+    for f in ("t_two", "t_ops", "t_sincos", "t_sincos_tab", "t_unnorm", "t_green", "t_efie_pair"):
         getattr(L, f).restype = None
     return L
 
@@ -155,6 +165,28 @@ def test_sincos_with_the_table(lib):
     x = _pair(th)
     assert np.abs(s - np.sin(x)).max() < 1e-11
     assert np.abs(c - np.cos(x)).max() < 1e-11
+
+
+def test_unnormalised_forms(lib):
+    """the unnormalised sine / cosine, reciprocal square root and pair sums of the far cores
+    (their low parts a few ulp of the high part instead of half an ulp): the values hi + lo keep
+    the pair accuracy of the normalised forms"""
+    rng = np.random.default_rng(11)
+    n = 40000
+    th = np.concatenate([np.linspace(-7, 7, n // 2), rng.uniform(-1e3, 1e3, n // 2)])
+    a = 10 ** rng.uniform(-4, 4, n) * rng.choice([-1.0, 1.0], n)
+    b = a * (1 + rng.uniform(-1e-3, 1e-3, n)) * rng.choice([-1.0, 1.0], n)  # includes near cancellation
+    out = np.zeros(5 * n)
+    lib.t_unnorm(_p(th), _p(a), _p(b), C.c_int64(n), _p(out))
+    out = out.reshape(n, 5)
+    x, pa, pb = _pair(th), _pair(np.abs(a)), _pair(a)
+    pbb = _pair(b)
+    assert np.abs(out[:, 0] - np.sin(x)).max() < 1e-11
+    assert np.abs(out[:, 1] - np.cos(x)).max() < 1e-11
+    assert np.abs(out[:, 2] * np.sqrt(pa) - 1).max() < 2e-13
+    scale = np.maximum(np.abs(pb), np.abs(pbb))
+    assert (np.abs(out[:, 3] - (pb + pbb)) / scale).max() < 1e-13
+    assert (np.abs(out[:, 4] - (pb - pbb)) / scale).max() < 1e-13
 
 
 def test_green_function(lib):
